@@ -1,0 +1,158 @@
+// Context lifetime, error reporting and host<->device marker transfers.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include "mdz_internal.cuh"
+
+mdz_status mdz_fail(mdz_ctx *ctx, mdz_status s, const char *fmt, ...) {
+    if (ctx) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        ctx->err = buf;
+    }
+    return s;
+}
+
+mdz_status mdz_cuda_check(mdz_ctx *ctx, cudaError_t e, const char *what) {
+    return mdz_fail(ctx, MDZ_ERR_CUDA, "CUDA error in %s: %s", what, cudaGetErrorString(e));
+}
+
+void *mdz_stage(mdz_ctx *ctx, int slot, size_t bytes) {
+    if (ctx->stage_bytes[slot] >= bytes && ctx->stage[slot]) return ctx->stage[slot];
+    if (ctx->stage[slot]) cudaFree(ctx->stage[slot]);
+    ctx->stage[slot] = nullptr;
+    ctx->stage_bytes[slot] = 0;
+    size_t b = bytes < 256 ? 256 : bytes;
+    if (cudaMalloc(&ctx->stage[slot], b) != cudaSuccess) return nullptr;
+    ctx->stage_bytes[slot] = b;
+    return ctx->stage[slot];
+}
+
+mdz_nodeset mdz_get_nodeset(const mdz_ctx *ctx, int centroid) {
+    const mdz_dgrid &g = ctx->g;
+    mdz_nodeset s{};
+    if (centroid == MDZ_NODES_CENTROIDS) { s.nx = g.Nx - 1; s.nz = g.Nz - 1; s.X = g.xc; s.Z = g.zc; s.tag = g.BCp; }
+    else if (centroid == MDZ_NODES_VERTICES) { s.nx = g.Nx; s.nz = g.Nz; s.X = g.xg; s.Z = g.zg; s.tag = g.BCg; }
+    else if (centroid == MDZ_NODES_VX) { s.nx = g.Nx; s.nz = g.Nz + 1; s.X = g.xg; s.Z = g.zvx; s.tag = g.BCu; }
+    else { s.nx = g.Nx + 1; s.nz = g.Nz; s.X = g.xvz; s.Z = g.zg; s.tag = g.BCv; }
+    return s;
+}
+
+template <typename T>
+static cudaError_t upload(T **dst, const T *src, size_t n) {
+    cudaError_t e = cudaMalloc((void **)dst, sizeof(T) * (n ? n : 1));
+    if (e != cudaSuccess) return e;
+    if (src && n) return cudaMemcpy(*dst, src, sizeof(T) * n, cudaMemcpyHostToDevice);
+    return cudaMemset(*dst, 0, sizeof(T) * (n ? n : 1));
+}
+
+extern "C" mdz_status mdz_create(mdz_ctx **out, const mdz_grid_desc *d, int n_phases, long long max_markers) {
+    if (!out || !d) return MDZ_ERR_ARG;
+    *out = nullptr;
+    mdz_ctx *ctx = new mdz_ctx();
+    if (d->Nx < 3 || d->Nz < 3 || n_phases < 1 || n_phases > MDZ_MAX_PHASES || max_markers < 0 ||
+        max_markers > (1LL << 31) - 1) {
+        mdz_fail(ctx, MDZ_ERR_ARG, "mdz_create: bad grid size, phase count or marker capacity");
+        delete ctx;
+        return MDZ_ERR_ARG;
+    }
+    if (!d->xg || !d->zg || !d->xc || !d->zc || !d->xvz || !d->zvx || !d->BCu_type || !d->BCv_type ||
+        !d->BCp_type || !d->BCg_type) {
+        delete ctx;
+        return MDZ_ERR_ARG;
+    }
+    if (d->isperiodic_x) {
+        delete ctx;
+        return MDZ_ERR_UNSUPPORTED;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        delete ctx;
+        return MDZ_ERR_CUDA;
+    }
+    ctx->host_desc = *d;
+    ctx->n_phases = n_phases;
+    mdz_dgrid &g = ctx->g;
+    int Nx = d->Nx, Nz = d->Nz;
+    g.Nx = Nx; g.Nz = Nz; g.ncx = Nx - 1; g.ncz = Nz - 1;
+    g.dx = d->dx; g.dz = d->dz;
+    g.xmin = d->xmin; g.xmax = d->xmax; g.zmin = d->zmin; g.zmax = d->zmax;
+    cudaError_t e = cudaSuccess;
+#define UP(dst, src, n) if (e == cudaSuccess) e = upload(&dst, src, n)
+    UP(g.xg, d->xg, Nx); UP(g.zg, d->zg, Nz); UP(g.xc, d->xc, Nx - 1); UP(g.zc, d->zc, Nz - 1);
+    UP(g.xvz, d->xvz, Nx + 1); UP(g.zvx, d->zvx, Nz + 1);
+    UP(g.BCu, d->BCu_type, (size_t)Nx * (Nz + 1)); UP(g.BCv, d->BCv_type, (size_t)(Nx + 1) * Nz);
+    UP(g.BCp, d->BCp_type, (size_t)(Nx - 1) * (Nz - 1)); UP(g.BCg, d->BCg_type, (size_t)Nx * Nz);
+    UP(g.BCu_val, d->BCu_val, (size_t)Nx * (Nz + 1)); UP(g.BCv_val, d->BCv_val, (size_t)(Nx + 1) * Nz);
+    // markers
+    long long cap = max_markers > 0 ? max_markers : 1;
+    ctx->m.cap = max_markers;
+    UP(ctx->m.x, (const double *)nullptr, cap); UP(ctx->m.z, (const double *)nullptr, cap);
+    UP(ctx->m.vx, (const double *)nullptr, cap); UP(ctx->m.vz, (const double *)nullptr, cap);
+    UP(ctx->m.phase, (const int *)nullptr, cap);
+    int ncells = (Nx - 1) * (Nz - 1);
+    ctx->bins.ncells = ncells;
+    UP(ctx->bins.cell, (const int *)nullptr, cap); UP(ctx->bins.sorted, (const int *)nullptr, cap);
+    UP(ctx->bins.count, (const int *)nullptr, ncells + 1); UP(ctx->bins.start, (const int *)nullptr, ncells + 1);
+    UP(ctx->bins.cursor, (const int *)nullptr, ncells + 1);
+    UP(ctx->bins.scan_partials, (const int *)nullptr, (ncells + 1) / 1024 + 2);
+#undef UP
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        mdz_destroy(ctx);
+        return MDZ_ERR_CUDA;
+    }
+    *out = ctx;
+    return MDZ_OK;
+}
+
+extern "C" void mdz_destroy(mdz_ctx *ctx) {
+    if (!ctx) return;
+    mdz_dgrid &g = ctx->g;
+    void *ptrs[] = {g.xg, g.zg, g.xc, g.zc, g.xvz, g.zvx, g.BCu, g.BCv, g.BCp, g.BCg, g.BCu_val, g.BCv_val,
+                    ctx->m.x, ctx->m.z, ctx->m.vx, ctx->m.vz, ctx->m.phase, ctx->bins.cell, ctx->bins.sorted,
+                    ctx->bins.count, ctx->bins.start, ctx->bins.cursor, ctx->bins.scan_partials};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    for (int i = 0; i < 8; i++)
+        if (ctx->stage[i]) cudaFree(ctx->stage[i]);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+extern "C" const char *mdz_last_error(const mdz_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+extern "C" long long mdz_kernel_launches(const mdz_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+extern "C" mdz_status mdz_set_markers(mdz_ctx *ctx, int n, const double *x, const double *z, const int *phase) {
+    if (!ctx) return MDZ_ERR_ARG;
+    if (n < 0 || (n > 0 && (!x || !z || !phase))) return mdz_fail(ctx, MDZ_ERR_ARG, "mdz_set_markers: bad arguments");
+    if (n > ctx->m.cap) return mdz_fail(ctx, MDZ_ERR_CAPACITY, "mdz_set_markers: %d markers > capacity %lld", n, ctx->m.cap);
+    cudaStream_t st = ctx->stream;
+    if (n) {
+        MDZ_CUDA(ctx, cudaMemcpyAsync(ctx->m.x, x, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+        MDZ_CUDA(ctx, cudaMemcpyAsync(ctx->m.z, z, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+        MDZ_CUDA(ctx, cudaMemcpyAsync(ctx->m.phase, phase, sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    }
+    MDZ_CUDA(ctx, cudaStreamSynchronize(st));
+    ctx->m.n = n;
+    ctx->bins.valid = false;
+    return MDZ_OK;
+}
+
+extern "C" mdz_status mdz_get_markers(mdz_ctx *ctx, int n, double *x, double *z, int *phase, double *vx, double *vz) {
+    if (!ctx) return MDZ_ERR_ARG;
+    if (n < 0 || n > ctx->m.n) return mdz_fail(ctx, MDZ_ERR_ARG, "mdz_get_markers: n=%d > resident %d", n, ctx->m.n);
+    cudaStream_t st = ctx->stream;
+    if (n) {
+        if (x) MDZ_CUDA(ctx, cudaMemcpyAsync(x, ctx->m.x, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        if (z) MDZ_CUDA(ctx, cudaMemcpyAsync(z, ctx->m.z, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        if (phase) MDZ_CUDA(ctx, cudaMemcpyAsync(phase, ctx->m.phase, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+        if (vx) MDZ_CUDA(ctx, cudaMemcpyAsync(vx, ctx->m.vx, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        if (vz) MDZ_CUDA(ctx, cudaMemcpyAsync(vz, ctx->m.vz, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+    }
+    MDZ_CUDA(ctx, cudaStreamSynchronize(st));
+    return MDZ_OK;
+}

@@ -1,0 +1,243 @@
+"""Host-side mirror of the reference's C entry points for the GB300 path.
+
+Thin ctypes layer over libmdoodz_gb300.so (include/mdoodz_gpu.h).  Function
+names follow the reference (P2Mastah, Interp_Grid2P, RogerGuntherII, ...) and
+take the same arguments; errors raise MdzError carrying the library's message
+where the reference would have printed and exit()ed.
+
+There is no CPU fallback: if the library or a CUDA device is missing, every
+entry point raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libmdoodz_gb300.so")
+
+MDZ_MAX_PHASES = 20
+MDZ_P2G_MAX_FIELDS = 8
+STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_CAPACITY", 4: "ERR_UNSUPPORTED", 5: "ERR_NOT_CONVERGED",
+          6: "ERR_NAN", 7: "ERR_STATE"}
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_sp = C.POINTER(C.c_int8)
+
+
+class MdzError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (STATUS.get(status, status), msg))
+        self.status = status
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("Nx", C.c_int), ("Nz", C.c_int), ("dx", C.c_double), ("dz", C.c_double),
+                ("xmin", C.c_double), ("xmax", C.c_double), ("zmin", C.c_double), ("zmax", C.c_double),
+                ("xg", _dp), ("zg", _dp), ("xc", _dp), ("zc", _dp), ("xvz", _dp), ("zvx", _dp),
+                ("BCu_type", _sp), ("BCv_type", _sp), ("BCp_type", _sp), ("BCg_type", _sp),
+                ("BCu_val", _dp), ("BCv_val", _dp), ("isperiodic_x", C.c_int)]
+
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Load the CUDA library (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise MdzError(2, "CUDA library not built: %s (run __graft_entry__.build())" % path)
+    L = C.CDLL(path)
+    L.mdz_last_error.restype = C.c_char_p
+    L.mdz_kernel_launches.restype = C.c_longlong
+    L.mdz_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(GridDesc), C.c_int, C.c_longlong]
+    _lib = L
+    return L
+
+
+def _dptr(a):
+    return a.ctypes.data_as(_dp) if a is not None else None
+
+
+def _iptr(a):
+    return a.ctypes.data_as(_ip) if a is not None else None
+
+
+def _sptr(a):
+    return a.ctypes.data_as(_sp) if a is not None else None
+
+
+class Grid:
+    """Staggered grid with the reference's coordinate lines and BC tags.
+
+    Coordinates accumulate exactly as SetGridCoordinates does
+    (SOURCE/GridRoutines.c:230-300), so index formulas agree bit for bit."""
+
+    def __init__(self, Nx, Nz, xmin, xmax, zmin, zmax):
+        self.Nx, self.Nz = int(Nx), int(Nz)
+        self.xmin, self.xmax, self.zmin, self.zmax = float(xmin), float(xmax), float(zmin), float(zmax)
+        self.dx = (self.xmax - self.xmin) / (Nx - 1)
+        self.dz = (self.zmax - self.zmin) / (Nz - 1)
+        self.xg = self._accum(self.xmin, self.dx, Nx)
+        self.zg = self._accum(self.zmin, self.dz, Nz)
+        self.xc = self._accum(self.xmin + self.dx / 2.0, self.dx, Nx - 1)
+        self.zc = self._accum(self.zmin + self.dz / 2.0, self.dz, Nz - 1)
+        self.xvz = self._accum(self.xmin - self.dx / 2.0, self.dx, Nx + 1)
+        self.zvx = self._accum(self.zmin - self.dz / 2.0, self.dz, Nz + 1)
+        self.BCu = np.full(Nx * (Nz + 1), -1, np.int8)
+        self.BCv = np.full((Nx + 1) * Nz, -1, np.int8)
+        self.BCp = np.full((Nx - 1) * (Nz - 1), -1, np.int8)
+        self.BCg = np.full(Nx * Nz, -1, np.int8)
+        self.BCu_val = np.zeros(Nx * (Nz + 1))
+        self.BCv_val = np.zeros((Nx + 1) * Nz)
+
+    @staticmethod
+    def _accum(x0, h, n):
+        out = np.empty(n)
+        v = x0
+        for i in range(n):
+            out[i] = v
+            v = v + h
+        return out
+
+    @property
+    def ncx(self):
+        return self.Nx - 1
+
+    @property
+    def ncz(self):
+        return self.Nz - 1
+
+    def size(self, centroid):
+        Nx, Nz = self.Nx, self.Nz
+        return {1: (Nx - 1) * (Nz - 1), 0: Nx * Nz, -1: Nx * (Nz + 1), -2: (Nx + 1) * Nz}[centroid]
+
+    def tags(self, centroid):
+        return {1: self.BCp, 0: self.BCg, -1: self.BCu, -2: self.BCv}[centroid]
+
+    def set_bc_pureshear(self, eps_bg):
+        """Free-slip pure shear: the tag and value rules of the reference's
+        shear_style = 0 setup (SOURCE/set_Shear_VEVP.c:177-265)."""
+        Nx, Nz = self.Nx, self.Nz
+        bu = self.BCu.reshape(Nz + 1, Nx)
+        vu = self.BCu_val.reshape(Nz + 1, Nx)
+        bu[:] = -1
+        vu[:] = 0.0
+        for k in (0, Nx - 1):
+            bu[:, k] = 0
+            vu[:, k] = -self.xg[k] * eps_bg
+        bu[0, :] = 13
+        bu[Nz, :] = 13
+        vu[0, :] = 0.0
+        vu[Nz, :] = 0.0
+        bv = self.BCv.reshape(Nz, Nx + 1)
+        vv = self.BCv_val.reshape(Nz, Nx + 1)
+        bv[:] = -1
+        vv[:] = 0.0
+        for l in (0, Nz - 1):
+            bv[l, :] = 0
+            vv[l, :] = self.zg[l] * eps_bg
+        bv[:, 0] = 13
+        bv[:, Nx] = 13
+        vv[:, 0] = 0.0
+        vv[:, Nx] = 0.0
+        self.BCp[:] = -1
+        self.BCg[:] = -1
+        return self
+
+    def desc(self):
+        d = GridDesc()
+        d.Nx, d.Nz, d.dx, d.dz = self.Nx, self.Nz, self.dx, self.dz
+        d.xmin, d.xmax, d.zmin, d.zmax = self.xmin, self.xmax, self.zmin, self.zmax
+        d.xg, d.zg, d.xc, d.zc = _dptr(self.xg), _dptr(self.zg), _dptr(self.xc), _dptr(self.zc)
+        d.xvz, d.zvx = _dptr(self.xvz), _dptr(self.zvx)
+        d.BCu_type, d.BCv_type = _sptr(self.BCu), _sptr(self.BCv)
+        d.BCp_type, d.BCg_type = _sptr(self.BCp), _sptr(self.BCg)
+        d.BCu_val, d.BCv_val = _dptr(self.BCu_val), _dptr(self.BCv_val)
+        d.isperiodic_x = 0
+        return d
+
+
+class Context:
+    """One device context: grid mirror + resident markers (mdz_create)."""
+
+    def __init__(self, grid, n_phases, max_markers):
+        self.L = load_library()
+        self.grid = grid
+        self.n_phases = int(n_phases)
+        self._desc = grid.desc()
+        h = C.c_void_p()
+        st = self.L.mdz_create(C.byref(h), C.byref(self._desc), C.c_int(n_phases), C.c_longlong(max_markers))
+        if st != 0:
+            raise MdzError(st, "mdz_create failed (no usable CUDA device or bad grid)")
+        self.h = h
+        self.n_markers = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.mdz_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != 0:
+            raise MdzError(st, self.L.mdz_last_error(self.h).decode())
+
+    @property
+    def kernel_launches(self):
+        return int(self.L.mdz_kernel_launches(self.h))
+
+    # markers ---------------------------------------------------------------
+    def set_markers(self, x, z, phase):
+        x = np.ascontiguousarray(x, np.float64)
+        z = np.ascontiguousarray(z, np.float64)
+        phase = np.ascontiguousarray(phase, np.int32)
+        self._check(self.L.mdz_set_markers(self.h, C.c_int(len(x)), _dptr(x), _dptr(z), _iptr(phase)))
+        self.n_markers = len(x)
+
+    def get_markers(self):
+        n = self.n_markers
+        x, z, vx, vz = np.empty(n), np.empty(n), np.empty(n), np.empty(n)
+        ph = np.empty(n, np.int32)
+        self._check(self.L.mdz_get_markers(self.h, C.c_int(n), _dptr(x), _dptr(z), _iptr(ph), _dptr(vx), _dptr(vz)))
+        return x, z, ph, vx, vz
+
+    # reference entry points -------------------------------------------------
+    def P2Mastah(self, mat_prop, node_field, node_type, flag, avg, prop, centroid, itp_stencil):
+        """P2Mastah (SOURCE/ParticleRoutines.c:3226).  Returns node_field (updated
+        copy) for prop == 0, or the phase fractions (n_phases x nnodes) for prop == 1."""
+        nn = self.grid.size(centroid)
+        nf = np.array(node_field if node_field is not None else np.zeros(nn), np.float64)
+        mp = np.ascontiguousarray(mat_prop, np.float64) if mat_prop is not None else None
+        tags = np.ascontiguousarray(node_type, np.int8) if node_type is not None else None
+        pp = np.zeros((self.n_phases, nn)) if prop == 1 else None
+        self._check(self.L.mdz_P2Mastah(self.h, _dptr(mp), _dptr(nf), _sptr(tags), C.c_int(flag), C.c_int(avg),
+                                        C.c_int(prop), C.c_int(centroid), C.c_int(itp_stencil), _dptr(pp)))
+        return pp if prop == 1 else nf
+
+    def count_markers(self):
+        g = self.grid
+        nc, nv = g.size(1), g.size(0)
+        c, v = np.zeros(nc, np.int32), np.zeros(nv, np.int32)
+        pc, pv = np.zeros((self.n_phases, nc), np.int32), np.zeros((self.n_phases, nv), np.int32)
+        self._check(self.L.mdz_count_markers(self.h, _iptr(c), _iptr(v), _iptr(pc), _iptr(pv)))
+        return c, v, pc, pv
+
+    def Interp_Grid2P(self, node_field, node_set):
+        nf = np.ascontiguousarray(node_field, np.float64)
+        out = np.zeros(self.n_markers)
+        self._check(self.L.mdz_Interp_Grid2P(self.h, _dptr(nf), C.c_int(node_set), _dptr(out)))
+        return out
+
+    def RogerGuntherII(self, u, v, dt):
+        u = np.ascontiguousarray(u, np.float64)
+        v = np.ascontiguousarray(v, np.float64)
+        self._check(self.L.mdz_RogerGuntherII(self.h, _dptr(u), _dptr(v), C.c_double(dt)))

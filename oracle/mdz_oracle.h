@@ -1,0 +1,45 @@
+/*
+ * CPU oracle: a plain-C restatement of the MDOODZ 6.0 hot-path algorithms,
+ * used ONLY as the checker in tests/, __graft_entry__.smoke() and the CPU
+ * baseline leg of bench.py.  The product library never links or calls it.
+ *
+ * Each function cites the reference function (path:line inside the MDOODZ 6.0
+ * repository) whose arithmetic it restates.  The restatement is pinned against
+ * the reference's own compiled functions through the golden fixtures in
+ * tests/golden/ (generated by tests/golden/make_golden.py from
+ * oracle/_ref/libmdoodz_ref.so).
+ *
+ * Grid and tag conventions are those of include/mdoodz_gpu.h.
+ */
+#ifndef MDZ_ORACLE_H
+#define MDZ_ORACLE_H
+#include "mdoodz_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* P2Mastah (SOURCE/ParticleRoutines.c:3226-3537), serial scatter form. */
+int orc_p2g(const mdz_grid_desc *g, int n, const double *x, const double *z, const int *phase, int n_phases,
+            const double *mat_prop, double *node_field, const signed char *node_type, int flag, int avg, int prop,
+            int centroid, int itp_stencil, double *phase_perc);
+
+/* CountPartCell_Old counting (SOURCE/ParticleRoutines.c:4530-4560 and 4898-4950). */
+int orc_count(const mdz_grid_desc *g, int n, const double *x, const double *z, const int *phase, int n_phases,
+              int *nb_part_cell, int *nb_part_vert, int *phase_count_cell, int *phase_count_vert);
+
+/* Interp_Grid2P (SOURCE/ParticleRoutines.c:2439-2608) for node_set 0/-1/-2 and
+ * Interp_Grid2P_centroids2 (SOURCE/ParticleRoutines.c:2612-2862) for node_set 1. */
+int orc_g2p(const mdz_grid_desc *g, int n, const double *x, const double *z, const int *phase,
+            const double *node_field, int node_set, double *out);
+
+/* RogerGuntherII + V2P (TarasCorr = 0) + isoutPart
+ * (SOURCE/AdvectionRoutines.c:569-628, SOURCE/ParticleRoutines.c:60-252,
+ *  SOURCE/AdvectionRoutines.c:314-335).  Updates x, z, phase, vx, vz in place. */
+int orc_rk4(const mdz_grid_desc *g, int n, double *x, double *z, int *phase, double *vx, double *vz,
+            const double *u, const double *v, double dt);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,97 @@
+"""ctypes wrapper of the CPU oracle (oracle/mdz_oracle.c, built to
+oracle/_build/libmdz_oracle.so).
+
+Test infrastructure only: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, always as the checker / reported baseline and
+never as the thing measured or shipped.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libmdz_oracle.so")
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_sp = C.POINTER(C.c_int8)
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("oracle not built: run `make -C oracle port`")
+        _lib = C.CDLL(LIB_PATH)
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp) if a is not None else None
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip) if a is not None else None
+
+
+def _s(a):
+    return a.ctypes.data_as(_sp) if a is not None else None
+
+
+class Oracle:
+    """Oracle bound to one grid (an mdz.Grid) and one marker set."""
+
+    def __init__(self, grid, n_phases):
+        self.grid = grid
+        self.n_phases = n_phases
+        self._desc = grid.desc()
+        self.L = lib()
+        self.x = self.z = self.phase = None
+
+    def set_markers(self, x, z, phase):
+        self.x = np.array(x, np.float64)
+        self.z = np.array(z, np.float64)
+        self.phase = np.array(phase, np.int32)
+
+    @property
+    def n(self):
+        return 0 if self.x is None else len(self.x)
+
+    def P2Mastah(self, mat_prop, node_field, node_type, flag, avg, prop, centroid, itp_stencil):
+        nn = self.grid.size(centroid)
+        nf = np.array(node_field if node_field is not None else np.zeros(nn), np.float64)
+        mp = np.ascontiguousarray(mat_prop, np.float64) if mat_prop is not None else None
+        tags = np.ascontiguousarray(node_type, np.int8) if node_type is not None else None
+        pp = np.zeros((self.n_phases, nn)) if prop == 1 else None
+        r = self.L.orc_p2g(C.byref(self._desc), C.c_int(self.n), _d(self.x), _d(self.z), _i(self.phase),
+                           C.c_int(self.n_phases), _d(mp), _d(nf), _s(tags), C.c_int(flag), C.c_int(avg),
+                           C.c_int(prop), C.c_int(centroid), C.c_int(itp_stencil), _d(pp))
+        assert r == 0
+        return pp if prop == 1 else nf
+
+    def count_markers(self):
+        g = self.grid
+        nc, nv = g.size(1), g.size(0)
+        c, v = np.zeros(nc, np.int32), np.zeros(nv, np.int32)
+        pc, pv = np.zeros((self.n_phases, nc), np.int32), np.zeros((self.n_phases, nv), np.int32)
+        self.L.orc_count(C.byref(self._desc), C.c_int(self.n), _d(self.x), _d(self.z), _i(self.phase),
+                         C.c_int(self.n_phases), _i(c), _i(v), _i(pc), _i(pv))
+        return c, v, pc, pv
+
+    def Interp_Grid2P(self, node_field, node_set):
+        nf = np.ascontiguousarray(node_field, np.float64)
+        out = np.zeros(self.n)
+        self.L.orc_g2p(C.byref(self._desc), C.c_int(self.n), _d(self.x), _d(self.z), _i(self.phase), _d(nf),
+                       C.c_int(node_set), _d(out))
+        return out
+
+    def RogerGuntherII(self, u, v, dt):
+        u = np.ascontiguousarray(u, np.float64)
+        v = np.ascontiguousarray(v, np.float64)
+        vx, vz = np.zeros(self.n), np.zeros(self.n)
+        self.L.orc_rk4(C.byref(self._desc), C.c_int(self.n), _d(self.x), _d(self.z), _i(self.phase), _d(vx),
+                       _d(vz), _d(u), _d(v), C.c_double(dt))
+        return vx, vz
