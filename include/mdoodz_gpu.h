@@ -138,6 +138,96 @@ mdz_status mdz_Interp_Grid2P(mdz_ctx *ctx, const double *node_field, int node_se
  * markers leaving the box get phase -1.  Updates resident x, z, Vx, Vz, phase. */
 mdz_status mdz_RogerGuntherII(mdz_ctx *ctx, const double *u, const double *v, double dt);
 
+/* ---- local rheology ------------------------------------------------------ */
+
+/* Per-phase material parameters: the subset of the reference's mat_prop
+ * (SOURCE/header_MDOODZ.h:46-63) used by the implemented creep laws.
+ * Implemented: constant viscosity (cstv), dislocation creep (pwlv), diffusion
+ * creep (linv, constant grain size), Maxwell elasticity, Drucker-Prager /
+ * von Mises plasticity with the viscoplastic regularisation eta_vp, n_vp.
+ * Not implemented (rejected with MDZ_ERR_UNSUPPORTED): Peierls (expv), GBS
+ * (gbsv), grain-size evolution (gs), reaction mixing, tension cut-off. */
+typedef struct mdz_materials {
+    int n_phases;
+    double R;                                           /* gas constant (mat_prop.R)           */
+    int cstv[MDZ_MAX_PHASES], pwlv[MDZ_MAX_PHASES], linv[MDZ_MAX_PHASES];
+    int expv[MDZ_MAX_PHASES], gbsv[MDZ_MAX_PHASES], gs[MDZ_MAX_PHASES], is_tensile[MDZ_MAX_PHASES];
+    int reac_soft[MDZ_MAX_PHASES], phase_mix[MDZ_MAX_PHASES];
+    double eta0[MDZ_MAX_PHASES], rho[MDZ_MAX_PHASES], alp[MDZ_MAX_PHASES], gs_ref[MDZ_MAX_PHASES];
+    double Slim[MDZ_MAX_PHASES], eta_vp[MDZ_MAX_PHASES], n_vp[MDZ_MAX_PHASES];
+    /* dislocation creep */
+    double npwl[MDZ_MAX_PHASES], Apwl[MDZ_MAX_PHASES], Qpwl[MDZ_MAX_PHASES], Vpwl[MDZ_MAX_PHASES];
+    double mpwl[MDZ_MAX_PHASES], rpwl[MDZ_MAX_PHASES], fpwl[MDZ_MAX_PHASES], apwl[MDZ_MAX_PHASES];
+    double Fpwl[MDZ_MAX_PHASES], pref_pwl[MDZ_MAX_PHASES];
+    /* diffusion creep */
+    double nlin[MDZ_MAX_PHASES], Alin[MDZ_MAX_PHASES], Qlin[MDZ_MAX_PHASES], Vlin[MDZ_MAX_PHASES];
+    double mlin[MDZ_MAX_PHASES], rlin[MDZ_MAX_PHASES], flin[MDZ_MAX_PHASES], alin[MDZ_MAX_PHASES];
+    double Flin[MDZ_MAX_PHASES];
+} mdz_materials;
+
+/* Model switches and scales read by the rheology (params / scale in the reference). */
+typedef struct mdz_rheo_params {
+    double dt;
+    int iselastic;          /* model.iselastic                                  */
+    int step;               /* model.step (step 0 switches elasticity off)      */
+    int eta_avg;            /* 0 arithmetic, 1 harmonic, 2 geometric phase mix   */
+    double mineta, maxeta;  /* viscosity limiter                                */
+    double scale_T, scale_E, scale_S, scale_eta, scale_L;
+} mdz_rheo_params;
+
+/* Grid fields by the reference's names (grid, SOURCE/header_MDOODZ.h:170-219).
+ * Suffix convention: no suffix or _n = centroids ((Nx-1)*(Nz-1)), _s and exz,
+ * sxz, sxz0 = vertices (Nx*Nz), u / roger_x / ru = Vx nodes, v / roger_z / rv =
+ * Vz nodes, p / p_corr / rhs_p / rp = centroids.  phase_perc_n/_s hold
+ * n_phases rows.  Host calls read the fields a function consumes and write the
+ * fields it produces; NULL pointers are skipped where a field is optional. */
+typedef struct mdz_fields {
+    double *u, *v, *p, *p_corr;
+    double *div_u, *div_u_s, *exxd, *ezzd, *exz, *exz_n, *exxd_s, *ezzd_s;
+    double *sxxd0, *szzd0, *sxz0, *sxxd0_s, *szzd0_s, *sxz0_n;
+    double *mu_n, *mu_s, *T, *T_s, *P_s, *d0_n, *d0_s, *phi0_n, *phi0_s, *X0_n, *X0_s;
+    double *strain_n, *strain_s, *dil_n, *dil_s, *fric_n, *fric_s, *C_n, *C_s, *p0_n, *p0_s;
+    double *bet_n, *bet_s, *rho_n, *rho_s;
+    double *phase_perc_n, *phase_perc_s;
+    double *eta_n, *eta_s, *eta_phys_n, *eta_phys_s, *VE_n, *VE_s, *sxxd, *szzd, *sxz, *sxz_n;
+    double *eII_el, *eII_pl, *eII_pwl, *eII_lin, *eII_cst, *d_n;
+    double *exx_el, *ezz_el, *exz_el, *exx_diss, *ezz_diss, *exz_diss;
+    double *detadexx_n, *detadezz_n, *detadgxz_n, *detadp_n;
+    double *ddivpdexx_n, *ddivpdezz_n, *ddivpdgxz_n, *ddivpdp_n;
+    double *detadexx_s, *detadezz_s, *detadgxz_s, *detadp_s;
+    double *div_u_el, *div_u_pl, *div_u_r, *Wtot, *Wel, *Wdiss, *X_n, *X_s, *OverS_n, *OverS_s;
+    double *D11_n, *D12_n, *D13_n, *D14_n, *D21_n, *D22_n, *D23_n, *D24_n;
+    double *D31_s, *D32_s, *D33_s, *D34_s;
+    double *roger_x, *roger_z, *rhs_p, *gx, *gz;
+    double *ru, *rv, *rp;
+} mdz_fields;
+
+/* Host-pointer drop-ins for the grid-side reference functions.  Each reads the
+ * fields listed and writes the fields it produces in `f` (synchronous). */
+
+/* StrainRateComponents (SOURCE/RheologyDensity.c:1902-1984): u, v ->
+ * div_u, exxd, ezzd, exz, exz_n, exxd_s, ezzd_s. */
+mdz_status mdz_StrainRateComponents(mdz_ctx *ctx, mdz_fields *f);
+
+/* NonNewtonianViscosityGrid + Viscosity (SOURCE/RheologyDensity.c:961-1415,
+ * 44-707): local VEP solve per node and phase, phase-fraction averaging, and
+ * the consistent tangent.  Reads the strain rates, old stresses, mu, T, p, d0,
+ * phi0, C, fric, dil, bet and phase_perc fields; writes eta, eta_phys, stresses,
+ * strain-rate partition, detad*, ddivpd*, p_corr, W*, OverS.  Where the
+ * reference exit()s on a failed local iteration, the count of such (node,
+ * phase) solves is returned in *n_not_converged (may be NULL). */
+mdz_status mdz_NonNewtonianViscosityGrid(mdz_ctx *ctx, const mdz_materials *mat, const mdz_rheo_params *prm,
+                                         mdz_fields *f, int *n_not_converged);
+
+/* RheologicalOperators (SOURCE/RheologyDensity.c:713-954), isotropic:
+ * Picard (jacobian = 0) or Newton (jacobian = 1) D11..D24 at centroids and
+ * D31..D34 at vertices. */
+mdz_status mdz_RheologicalOperators(mdz_ctx *ctx, const mdz_rheo_params *prm, mdz_fields *f, int jacobian);
+
+/* EvaluateRHS (SOURCE/StokesRoutines.c:922-1133), incompressible and
+ * non-polar: roger_x, roger_z (body force and elastic history), rhs_p. */
+mdz_status mdz_EvaluateRHS(mdz_ctx *ctx, const mdz_rheo_params *prm, double gx, double gz, mdz_fields *f);
+
 #ifdef __cplusplus
 }
 #endif

@@ -45,6 +45,9 @@ struct mdz_ctx {
     mdz_bins bins;
     cudaStream_t stream = nullptr;
     long long launches = 0;
+    mdz_fields d{};              // device mirrors of every grid field (allocated on first use)
+    bool fields_ready = false;
+    int *d_counters = nullptr;   // small device scratch: failure counters etc.
     std::string err;
     // host-call staging buffers (grown on demand)
     void *stage[8] = {nullptr};
@@ -85,3 +88,133 @@ mdz_nodeset mdz_get_nodeset(const mdz_ctx *ctx, int centroid);
 
 // Binning (markers.cu)
 mdz_status mdz_ensure_bins(mdz_ctx *ctx, cudaStream_t st);
+
+// Every mdz_fields member with its node set (X-macro): VX / VZ velocity nodes,
+// CEN centroids, VER vertices, PPN / PPS phase fractions (n_phases rows).
+#define MDZ_FIELD_LIST(X) \
+    X(u, VX) \
+    X(v, VZ) \
+    X(p, CEN) \
+    X(p_corr, CEN) \
+    X(div_u, CEN) \
+    X(div_u_s, VER) \
+    X(exxd, CEN) \
+    X(ezzd, CEN) \
+    X(exz, VER) \
+    X(exz_n, CEN) \
+    X(exxd_s, VER) \
+    X(ezzd_s, VER) \
+    X(sxxd0, CEN) \
+    X(szzd0, CEN) \
+    X(sxz0, VER) \
+    X(sxxd0_s, VER) \
+    X(szzd0_s, VER) \
+    X(sxz0_n, CEN) \
+    X(mu_n, CEN) \
+    X(mu_s, VER) \
+    X(T, CEN) \
+    X(T_s, VER) \
+    X(P_s, VER) \
+    X(d0_n, CEN) \
+    X(d0_s, VER) \
+    X(phi0_n, CEN) \
+    X(phi0_s, VER) \
+    X(X0_n, CEN) \
+    X(X0_s, VER) \
+    X(strain_n, CEN) \
+    X(strain_s, VER) \
+    X(dil_n, CEN) \
+    X(dil_s, VER) \
+    X(fric_n, CEN) \
+    X(fric_s, VER) \
+    X(C_n, CEN) \
+    X(C_s, VER) \
+    X(p0_n, CEN) \
+    X(p0_s, VER) \
+    X(bet_n, CEN) \
+    X(bet_s, VER) \
+    X(rho_n, CEN) \
+    X(rho_s, VER) \
+    X(phase_perc_n, PPN) \
+    X(phase_perc_s, PPS) \
+    X(eta_n, CEN) \
+    X(eta_s, VER) \
+    X(eta_phys_n, CEN) \
+    X(eta_phys_s, VER) \
+    X(VE_n, CEN) \
+    X(VE_s, VER) \
+    X(sxxd, CEN) \
+    X(szzd, CEN) \
+    X(sxz, VER) \
+    X(sxz_n, CEN) \
+    X(eII_el, CEN) \
+    X(eII_pl, CEN) \
+    X(eII_pwl, CEN) \
+    X(eII_lin, CEN) \
+    X(eII_cst, CEN) \
+    X(d_n, CEN) \
+    X(exx_el, CEN) \
+    X(ezz_el, CEN) \
+    X(exz_el, VER) \
+    X(exx_diss, CEN) \
+    X(ezz_diss, CEN) \
+    X(exz_diss, VER) \
+    X(detadexx_n, CEN) \
+    X(detadezz_n, CEN) \
+    X(detadgxz_n, CEN) \
+    X(detadp_n, CEN) \
+    X(ddivpdexx_n, CEN) \
+    X(ddivpdezz_n, CEN) \
+    X(ddivpdgxz_n, CEN) \
+    X(ddivpdp_n, CEN) \
+    X(detadexx_s, VER) \
+    X(detadezz_s, VER) \
+    X(detadgxz_s, VER) \
+    X(detadp_s, VER) \
+    X(div_u_el, CEN) \
+    X(div_u_pl, CEN) \
+    X(div_u_r, CEN) \
+    X(Wtot, CEN) \
+    X(Wel, CEN) \
+    X(Wdiss, CEN) \
+    X(X_n, CEN) \
+    X(X_s, VER) \
+    X(OverS_n, CEN) \
+    X(OverS_s, VER) \
+    X(D11_n, CEN) \
+    X(D12_n, CEN) \
+    X(D13_n, CEN) \
+    X(D14_n, CEN) \
+    X(D21_n, CEN) \
+    X(D22_n, CEN) \
+    X(D23_n, CEN) \
+    X(D24_n, CEN) \
+    X(D31_s, VER) \
+    X(D32_s, VER) \
+    X(D33_s, VER) \
+    X(D34_s, VER) \
+    X(roger_x, VX) \
+    X(roger_z, VZ) \
+    X(rhs_p, CEN) \
+    X(gx, VX) \
+    X(gz, VZ) \
+    X(ru, VX) \
+    X(rv, VZ) \
+    X(rp, CEN)
+
+enum mdz_field_kind { MDZ_K_VX, MDZ_K_VZ, MDZ_K_CEN, MDZ_K_VER, MDZ_K_PPN, MDZ_K_PPS };
+size_t mdz_field_count(const mdz_ctx *ctx, int kind);
+mdz_status mdz_ensure_fields(mdz_ctx *ctx);
+
+// device launchers (rheology.cu)
+mdz_status mdz_dev_strain_rates(mdz_ctx *ctx, const mdz_fields &f, cudaStream_t st);
+mdz_status mdz_dev_c2v(mdz_ctx *ctx, const double *cen, double *ver, cudaStream_t st);
+mdz_status mdz_dev_v2c(mdz_ctx *ctx, double *cen, const double *ver, cudaStream_t st);
+mdz_status mdz_check_materials(mdz_ctx *ctx, const mdz_materials *m);
+mdz_status mdz_dev_viscosity(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm, const mdz_fields &f,
+                             int *d_fail, cudaStream_t st);
+mdz_status mdz_dev_operators(mdz_ctx *ctx, const mdz_rheo_params *prm, const mdz_fields &f, int jacobian,
+                             cudaStream_t st);
+mdz_status mdz_dev_rhs(mdz_ctx *ctx, const mdz_rheo_params *prm, double gx, double gz, const mdz_fields &f,
+                       cudaStream_t st);
+mdz_status mdz_dev_rk4(mdz_ctx *ctx, const double *du, const double *dv, double dt, cudaStream_t st);

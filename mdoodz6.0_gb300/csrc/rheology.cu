@@ -1,0 +1,633 @@
+// Grid-side rheology kernels: strain rates, centroid<->vertex averaging, the
+// local visco-elasto-plastic solve per node and phase with its consistent
+// tangent, the rheological operators D11..D34 and the momentum RHS.
+//
+// Reference behaviour followed (paths inside the MDOODZ 6.0 repository):
+//   StrainRateComponents            SOURCE/RheologyDensity.c:1902-1984
+//   InterpCentroidsToVerticesDouble SOURCE/GridRoutines.c:106-198
+//   InterpVerticesToCentroidsDouble SOURCE/GridRoutines.c:204-228
+//   Viscosity                       SOURCE/RheologyDensity.c:44-707
+//   NonNewtonianViscosityGrid       SOURCE/RheologyDensity.c:961-1415
+//   RheologicalOperators            SOURCE/RheologyDensity.c:713-954
+//   EvaluateRHS                     SOURCE/StokesRoutines.c:922-1133
+// Isotropic, incompressible, non-reactive subset; the host rejects the rest.
+#include <cmath>
+#include "mdz_internal.cuh"
+
+
+#define ZEROC 273.15
+
+// ---------------------------------------------------------------------------
+// Strain rates.  One thread per vertex computes exz; one per centroid div, exx, ezz.
+__global__ void k_strain_centroids(mdz_dgrid g, const double *__restrict__ u, const double *__restrict__ v,
+                                   double *__restrict__ div, double *__restrict__ exx, double *__restrict__ ezz) {
+    int c0 = blockIdx.x * blockDim.x + threadIdx.x;
+    int ncx = g.ncx, Nx = g.Nx;
+    if (c0 >= ncx * g.ncz) return;
+    int k = c0 % ncx, l = c0 / ncx, c1 = k + l * Nx, c2 = k + l * (Nx + 1);
+    signed char t = g.BCp[c0];
+    if (t != 30 && t != 31) {
+        double d = (u[c1 + 1 + Nx] - u[c1 + Nx]) / g.dx + (v[c2 + Nx + 1 + 1] - v[c2 + 1]) / g.dz;
+        div[c0] = d;
+        exx[c0] = (u[c1 + 1 + Nx] - u[c1 + Nx]) / g.dx - 1.0 / 3.0 * d;
+        ezz[c0] = (v[c2 + 1 + (Nx + 1)] - v[c2 + 1]) / g.dz - 1.0 / 3.0 * d;
+    } else {
+        div[c0] = 0.0; exx[c0] = 0.0; ezz[c0] = 0.0;
+    }
+}
+
+__global__ void k_strain_vertices(mdz_dgrid g, const double *__restrict__ u, const double *__restrict__ v,
+                                  double *__restrict__ exz) {
+    int c1 = blockIdx.x * blockDim.x + threadIdx.x;
+    int Nx = g.Nx;
+    if (c1 >= Nx * g.Nz) return;
+    int k = c1 % Nx, l = c1 / Nx, c2 = k + l * (Nx + 1);
+    double e = 0.0;
+    if (g.BCg[c1] != 30) {
+        if (g.BCu[c1] != 30 && g.BCu[c1 + Nx] != 30) e += 0.5 * (u[c1 + Nx] - u[c1]) / g.dz;
+        if (g.BCv[c2] != 30 && g.BCv[c2 + 1] != 30) e += 0.5 * (v[c2 + 1] - v[c2]) / g.dx;
+    }
+    exz[c1] = e;
+}
+
+__global__ void k_exz_to_centroids(mdz_dgrid g, const double *__restrict__ exz, double *__restrict__ exz_n) {
+    int c0 = blockIdx.x * blockDim.x + threadIdx.x;
+    int ncx = g.ncx, Nx = g.Nx;
+    if (c0 >= ncx * g.ncz) return;
+    int k = c0 % ncx, l = c0 / ncx, c1 = k + l * Nx;
+    double e = 0.0, s = 0.0;
+    if (g.BCp[c0] != 30 && g.BCp[c0] != 31) {
+        if (g.BCg[c1] != 30) { e += exz[c1]; s++; }
+        if (g.BCg[c1 + 1] != 30) { e += exz[c1 + 1]; s++; }
+        if (g.BCg[c1 + Nx] != 30) { e += exz[c1 + Nx]; s++; }
+        if (g.BCg[c1 + Nx + 1] != 30) { e += exz[c1 + Nx + 1]; s++; }
+        if (s > 0) e /= s;
+    }
+    exz_n[c0] = e;
+}
+
+// Centroid -> vertex average with the zero-flux padding of the reference:
+// the padded ring repeats the nearest interior centroid (corners: diagonal).
+__global__ void k_c2v(mdz_dgrid g, const double *__restrict__ cen, double *__restrict__ ver) {
+    int c1 = blockIdx.x * blockDim.x + threadIdx.x;
+    int Nx = g.Nx, ncx = g.ncx, ncz = g.ncz;
+    if (c1 >= Nx * g.Nz) return;
+    int k = c1 % Nx, l = c1 / Nx;
+    double r = 0.0;
+    if (g.BCg[c1] != 30) {
+        // padded indices of the four centroids around vertex (k, l): columns k-1, k; rows l-1, l
+        int kw = k - 1 < 0 ? 0 : k - 1, ke = k > ncx - 1 ? ncx - 1 : k;
+        int ls = l - 1 < 0 ? 0 : l - 1, ln = l > ncz - 1 ? ncz - 1 : l;
+        r = 0.25 * (cen[kw + ls * ncx] + cen[ke + ls * ncx] + cen[kw + ln * ncx] + cen[ke + ln * ncx]);
+    }
+    ver[c1] = r;
+}
+
+__global__ void k_v2c(mdz_dgrid g, double *__restrict__ cen, const double *__restrict__ ver) {
+    int c0 = blockIdx.x * blockDim.x + threadIdx.x;
+    int ncx = g.ncx, Nx = g.Nx;
+    if (c0 >= ncx * g.ncz) return;
+    int k = c0 % ncx, l = c0 / ncx, c1 = k + l * Nx;
+    if (g.BCp[c0] != 30 && g.BCp[c0] != 31) cen[c0] = 0.25 * (ver[c1] + ver[c1 + 1] + ver[c1 + Nx] + ver[c1 + 1 + Nx]);
+}
+
+// ---------------------------------------------------------------------------
+// Local solve.  Outputs of one (node, phase) solve.
+struct visc_res {
+    double eta, txx, tzz, txz, etaVE, VEcoeff, Eii_el, Eii_pl, Eii_pwl, Eii_lin, Eii_cst;
+    double Exx_el, Ezz_el, Exz_el, Exx_diss, Ezz_diss, Exz_diss, d1;
+    double detadexx, detadezz, detadexz, detadp, X1, OverS;
+    double ddivpdexx, ddivpdezz, ddivpdexz, ddivpdp, Pcorr, div_el, div_pl;
+    int ve_fail, vp_fail, ve_its, vp_its;
+};
+
+__device__ __forceinline__ double dmin(double a, double b) { return a <= b ? a : b; }
+
+__device__ void visc_local(int p, double G, double T, double P, double d, double phi, double X0, double Exx,
+                           double Ezz, double Exz, double Gxx, double Gzz, double Gxz, double Txx0, double Tzz0,
+                           double Txz0, const mdz_materials &m, const mdz_rheo_params &prm, double dil, double fric,
+                           double C, double P0, double beta, visc_res &o) {
+    const double R = m.R, dt = prm.dt, tol = 1.0e-11;
+    const int nitmax = 20;
+    int elastic = prm.iselastic, it;
+    const bool constant = m.cstv[p] != 0, dislocation = m.pwlv[p] != 0, diffusion = m.linv[p] != 0;
+    double K = 1.0 / beta, res = 0.0;
+    const double Tii0 = sqrt(Txx0 * Txx0 + Txz0 * Txz0);
+    const double n_pwl = m.npwl[p], Va_pwl = m.Vpwl[p], n_lin = m.nlin[p], m_lin = m.mlin[p];
+    double B_lin = 0, C_pwl = 0, C_lin = 0, dCpwldP = 0, dClindP = 0;
+    double eta_pwl = 0.0, eta_lin = 0.0, eta_cst = 0.0, eta_vep = 0.0, eta_vp = 0.0;
+    const double eta_vp0 = m.eta_vp[p], n_vp = m.n_vp[p];
+    double Eii_pwl = 0, Eii_lin = 0, Eii_cst = 0;
+    o.Eii_pl = 0.0; o.OverS = 0.0; o.ve_fail = 0; o.vp_fail = 0; o.vp_its = 0;
+
+    double Eyy = -(Exx + Ezz), Gyy = -(Gxx + Gzz);
+    double Eii = sqrt(1.0 / 2.0 * (Exx * Exx + Ezz * Ezz + Eyy * Eyy) + Exz * Exz);
+    double Gii = sqrt(1.0 / 2.0 * (Gxx * Gxx + Gzz * Gzz + Gyy * Gyy) + Gxz * Gxz);
+    if (Eii * prm.scale_E < 1e-30) Eii = 1e-30 / prm.scale_E;
+    if (Gii * prm.scale_E < 1e-30) Gii = 1e-30 / prm.scale_E;
+    const double f_ani = Gii / Eii;
+    o.Pcorr = P;
+    if (prm.step == 0) elastic = 0;
+    o.d1 = m.gs_ref[p];
+    if (elastic == 0) { G = 1e1; K = 1e1; dil = 0.0; }
+    if (T < ZEROC / prm.scale_T) T = ZEROC / prm.scale_T;
+    if (dislocation) {
+        double B_pwl = m.pref_pwl[p] * m.Fpwl[p] * pow(m.Apwl[p], -1.0 / n_pwl) *
+                       exp((m.Qpwl[p] + P * Va_pwl) / R / n_pwl / T) * pow(d, m.mpwl[p] / n_pwl) *
+                       pow(m.fpwl[p], -m.rpwl[p] / n_pwl) * exp(-m.apwl[p] * phi / n_pwl);
+        C_pwl = pow(2.0 * f_ani * B_pwl, -n_pwl);
+        dCpwldP = -C_pwl * Va_pwl / R / T;
+        eta_pwl = B_pwl * pow(Eii, 1.0 / n_pwl - 1.0);
+    }
+    if (diffusion) {
+        B_lin = m.Flin[p] * pow(m.Alin[p], -1.0 / n_lin) * exp((m.Qlin[p] + P * m.Vlin[p]) / R / n_lin / T) *
+                pow(m.flin[p], -m.rlin[p] / n_lin) * exp(-m.alin[p] * phi / n_lin);
+        C_lin = pow(2.0 * f_ani * B_lin, -n_lin);
+        dClindP = -C_lin * m.Vlin[p] / R / T;
+        eta_lin = B_lin * pow(Eii, 1.0 / n_lin - 1.0) * pow(d, m_lin / n_lin);
+    }
+    double cos_fric = cos(fric), sin_fric = sin(fric), sin_dil = sin(dil);
+    double Tyield = C * cos_fric + P * sin_fric;
+    if (m.Slim[p] < Tyield) { sin_fric = 0.0; cos_fric = 1.0; sin_dil = 0.0; C = m.Slim[p]; Tyield = m.Slim[p]; }
+    o.X1 = X0;
+    const double eta_el = G * dt;
+    if (constant) eta_cst = m.eta0[p];
+    double eta_up = 1.0e100 / prm.scale_eta;
+    if (constant) eta_up = dmin(eta_up, eta_cst);
+    if (dislocation) eta_up = dmin(eta_up, eta_pwl);
+    if (elastic) eta_up = dmin(eta_up, eta_el);
+    if (diffusion) eta_up = dmin(eta_up, eta_lin);
+    // local Newton on the visco-elastic viscosity
+    double eta_ve = eta_up, Tii;
+    const double dm_lin = pow(o.d1, -m_lin);
+    for (it = 0; it < nitmax; it++) {
+        Tii = 2.0 * f_ani * eta_ve * Eii;
+        if (constant) Eii_cst = Tii / f_ani / 2.0 / eta_cst;
+        if (dislocation) Eii_pwl = C_pwl * pow(Tii, n_pwl);
+        if (diffusion) Eii_lin = C_lin * pow(Tii, n_lin) * dm_lin;
+        double r = Eii - elastic * Tii / (2.0 * eta_el) - (Eii_pwl + Eii_lin + Eii_cst);
+        res = fabs(r / Eii);
+        if (res < tol / 100) break;
+        double dfdeta = 0.0;
+        if (elastic) dfdeta += -Eii / eta_el;
+        if (diffusion) dfdeta += -Eii_lin * n_lin / eta_ve;
+        if (dislocation) dfdeta += -Eii_pwl * n_pwl / eta_ve;
+        if (constant) dfdeta += -Eii / eta_cst;
+        eta_ve -= r / dfdeta;
+    }
+    o.ve_its = it;
+    if (it == nitmax - 1 && res > tol) o.ve_fail = 1;
+    Tii = 2.0 * eta_ve * f_ani * Eii;
+    double Txx = Gxx * Tii / f_ani / Eii, Tzz = Gzz * Tii / f_ani / Eii, Txz = Gxz * Tii / f_ani / Eii;
+    double Exx_lin = 0, Ezz_lin = 0, Exz_lin = 0, Exx_cst = 0, Ezz_cst = 0, Exz_cst = 0;
+    if (diffusion) {
+        eta_lin = B_lin * pow(Eii_lin, 1.0 / n_lin - 1.0) * pow(o.d1, m_lin / n_lin);
+        Exx_lin = Txx / 2.0 / eta_lin; Ezz_lin = Tzz / 2.0 / eta_lin; Exz_lin = Txz / 2.0 / eta_lin;
+    }
+    if (constant) { Exx_cst = Txx / 2.0 / eta_cst; Ezz_cst = Tzz / 2.0 / eta_cst; Exz_cst = Txz / 2.0 / eta_cst; }
+    // visco-elastic tangent
+    double deta = 0.0;
+    if (dislocation) deta += -C_pwl * pow(Tii, n_pwl - 3.0) * (n_pwl - 1.0);
+    if (diffusion) deta += -C_lin * pow(Tii, n_lin - 3.0) * (n_lin - 1.0) * dm_lin;
+    const double e2 = pow(eta_ve, 2.0);
+    double dTxx = deta * (2.0 * Txx + Tzz) * e2, dTzz = deta * (2.0 * Tzz + Txx) * e2, dTxz = 2.0 * deta * Txz * e2;
+    double den = 1.0 - 2.0 * (dTxx * Exx + dTzz * Ezz + dTxz * Exz);
+    double dve_dExx = dTxx * 2.0 * eta_ve / den, dve_dEzz = dTzz * 2.0 * eta_ve / den;
+    double dve_dExz = dTxz * 2.0 * eta_ve / den;
+    double dummy = 0.0, Jii = Tii * Tii;
+    if (dislocation) dummy += -2.0 * pow(Jii, (1.0 / 2.0) * n_pwl - 1.0 / 2.0) * dCpwldP;
+    if (diffusion) dummy += -2.0 * pow(Jii, (1.0 / 2.0) * n_lin - 1.0 / 2.0) * pow(d, -m_lin) * dClindP;
+    double dve_dP = pow(eta_ve, 2) * dummy;
+    // plastic return mapping on gdot
+    double gdot = 0.0, dQdtxx = 0, dQdtzz = 0, dQdtxz = 0, dQdP = 0, divp = 0.0, Pc = P;
+    double dlamdExx = 0, dlamdEzz = 0, dlamdExz = 0, dlamdP = 0;
+    double dvep_dExx = 0, dvep_dEzz = 0, dvep_dExz = 0, dvep_dP = 0;
+    double F_trial = Tii - Tyield;
+    const bool is_pl = F_trial > 1e-17;
+    if (is_pl) {
+        eta_vp = eta_vp0 * pow(Eii, 1.0 / n_vp - 1);
+        gdot = F_trial / (eta_ve + eta_vp + K * dt * sin_fric * sin_dil);
+        dQdtxx = Txx / 2.0 / Tii; dQdtzz = Tzz / 2.0 / Tii; dQdtxz = Txz / 1.0 / Tii;
+        const double F_trial0 = F_trial;
+        for (it = 0; it < nitmax; it++) {
+            dQdP = -sin_dil;
+            divp = -gdot * dQdP;
+            Pc = P + K * dt * divp;
+            eta_vp = eta_vp0 * pow(fabs(gdot), 1.0 / n_vp - 1.0);
+            Tyield = C * cos_fric + Pc * sin_fric + gdot * eta_vp;
+            F_trial = Tii - eta_ve * gdot - Tyield;
+            res = fabs(F_trial);
+            if (res < tol || res / F_trial0 < tol) break;
+            double dFdgdot = -eta_ve - eta_vp / n_vp - K * dt * sin_fric * sin_dil;
+            gdot -= F_trial / dFdgdot;
+        }
+        o.vp_its = it;
+        if (it == nitmax - 1 && (res > tol || res / F_trial0 > tol)) o.vp_fail = 1;
+        Txx = 2.0 * eta_ve * (Exx - gdot * dQdtxx);
+        Tzz = 2.0 * eta_ve * (Ezz - gdot * dQdtzz);
+        double Tyy = -(Txx + Tzz);
+        Txz = 2.0 * eta_ve * (Exz - gdot * dQdtxz / 2.0);
+        Tii = sqrt(0.5 * (pow(Txx, 2.0) + pow(Tzz, 2.0) + pow(Tyy, 2.0)) + pow(Txz, 2.0));
+        eta_vep = Tii / (2.0 * Eii);
+        o.Eii_pl = gdot / 2.0;
+        Tii = 2.0 * eta_vep * Eii;
+        o.OverS = eta_vp * gdot;
+        o.Pcorr = Pc;
+        // visco-elasto-plastic tangent
+        double dFdExx = (2.0 * Exx + Ezz) * eta_ve / Eii + 2.0 * Eii * dve_dExx;
+        double dFdEzz = (2.0 * Ezz + Exx) * eta_ve / Eii + 2.0 * Eii * dve_dEzz;
+        double dFdExz = 2.0 * Exz * eta_ve / Eii + 2.0 * Eii * dve_dExz;
+        double dFdP = -sin_fric + 2.0 * Eii * dve_dP;
+        double gg = 1.0 / (eta_ve + eta_vp / n_vp + K * dt * sin_fric * sin_dil);
+        dlamdExx = gg * (dFdExx - gdot * (dve_dExx + K * dt * sin_fric * 0.0));
+        dlamdEzz = gg * (dFdEzz - gdot * (dve_dEzz + K * dt * sin_fric * 0.0));
+        dlamdExz = gg * (dFdExz - gdot * (dve_dExz + K * dt * sin_fric * 0.0));
+        dlamdP = gg * (dFdP - gdot * (dve_dP + K * dt * sin_fric * 0.0));
+        double q = 1.0 / n_vp - 1.0;
+        double dvp_dExx = eta_vp / gdot * dlamdExx * q, dvp_dEzz = eta_vp / gdot * dlamdEzz * q;
+        double dvp_dExz = eta_vp / gdot * dlamdExz * q, dvp_dP = eta_vp / gdot * dlamdP * q;
+        double a = eta_vp + K * dt * sin_fric * sin_dil, E3 = 2.0 * pow(Eii, 3.0);
+        dvep_dExx = -0.5 * (2.0 * Exx + Ezz) * Tyield / E3 + (a * dlamdExx + gdot * dvp_dExx + gdot * K * dt * sin_fric * 0.0) / (2.0 * Eii);
+        dvep_dEzz = -0.5 * (2.0 * Ezz + Exx) * Tyield / E3 + (a * dlamdEzz + gdot * dvp_dEzz + gdot * K * dt * sin_fric * 0.0) / (2.0 * Eii);
+        dvep_dExz = -Exz * Tyield / E3 + (a * dlamdExz + gdot * dvp_dExz + gdot * K * dt * sin_fric * 0.0) / (2.0 * Eii);
+        dvep_dP = (sin_fric + a * dlamdP + gdot * dvp_dP + gdot * K * dt * sin_fric * 0.0) / (2.0 * Eii);
+    }
+    double inv_eta_diss = 0.0;
+    if (dislocation) inv_eta_diss += 1.0 / eta_pwl;
+    if (diffusion) inv_eta_diss += 1.0 / eta_lin;
+    if (constant) inv_eta_diss += 1.0 / eta_cst;
+    if (!is_pl) {
+        o.detadexx = dve_dExx; o.detadezz = dve_dEzz; o.detadexz = dve_dExz; o.detadp = dve_dP;
+        o.etaVE = eta_ve;
+        o.ddivpdexx = 0.0; o.ddivpdezz = 0.0; o.ddivpdexz = 0.0; o.ddivpdp = 0.0;
+    } else {
+        o.detadexx = dvep_dExx; o.detadezz = dvep_dEzz; o.detadexz = dvep_dExz; o.detadp = dvep_dP;
+        o.etaVE = eta_vep;
+        o.ddivpdexx = -dQdP * dlamdExx + gdot * 0.0;
+        o.ddivpdezz = -dQdP * dlamdEzz + gdot * 0.0;
+        o.ddivpdexz = -dQdP * dlamdExz + gdot * 0.0;
+        o.ddivpdp = -dQdP * dlamdP + gdot * 0.0 + 0.0;
+        inv_eta_diss += 1.0 / eta_vep;
+    }
+    // eta_pwl is re-evaluated unconditionally in the reference (C_pwl = 0 when
+    // dislocation creep is off, which makes the dislocation parts vanish)
+    eta_pwl = pow(2.0 * C_pwl, -1.0) * pow(Tii, 1.0 - n_pwl);
+    o.Exx_el = (double)elastic * (Txx - Txx0) / 2.0 / eta_el;
+    o.Ezz_el = (double)elastic * (Tzz - Tzz0) / 2.0 / eta_el;
+    o.Exz_el = (double)elastic * (Txz - Txz0) / 2.0 / eta_el;
+    o.Exx_diss = gdot * dQdtxx + Exx_lin + Txx / 2.0 / eta_pwl + Exx_cst;
+    o.Ezz_diss = gdot * dQdtzz + Ezz_lin + Tzz / 2.0 / eta_pwl + Ezz_cst;
+    o.Exz_diss = gdot * dQdtxz / 2.0 + Exz_lin + Txz / 2.0 / eta_pwl + Exz_cst;
+    o.Eii_el = (double)elastic * fabs(Tii - Tii0) / 2.0 / eta_el;
+    o.Eii_pwl = Tii / 2.0 / eta_pwl;
+    o.Eii_lin = Eii_lin;
+    o.Eii_cst = Eii_cst;
+    o.div_pl = divp;
+    o.div_el = -(Pc - P0) / (K * dt);
+    double eta = 1.0 / inv_eta_diss;
+    o.VEcoeff = elastic == 0 ? 0.0 : eta_ve / eta_el;
+    if (prm.step == 0) o.etaVE = eta;
+    o.txx = Txx; o.tzz = Tzz; o.txz = Txz;
+    if (eta > prm.maxeta) eta = prm.maxeta;
+    if (eta < prm.mineta) eta = prm.mineta;
+    if (o.etaVE > prm.maxeta) o.etaVE = prm.maxeta;
+    if (o.etaVE < prm.mineta) o.etaVE = prm.mineta;
+    o.eta = eta;
+}
+
+// Effective rates entering the local solve (isotropic form of the elastic
+// stress correction, NonNewtonianViscosityGrid :1060-1094): E[0..2] Exx, Ezz,
+// Exz and E[3..5] Gxx, Gzz, Gxz, with the reference's inverse of Da evaluated
+// for ani = 0 (iDa11 = iDa22 = 1/2, iDa33 = 1, off-diagonals 0).
+__device__ __forceinline__ void eff_rates(double exx, double ezz, double exz, double sxx0, double szz0, double sxz0,
+                                          double etae, double *E) {
+    const double i11 = 0.5, i22 = 0.5, i33 = 1.0, z = 0.0;
+    double Exx = exx + (i11 * sxx0 + z * szz0 + z * sxz0) / etae;
+    double Ezz = ezz + (z * sxx0 + i22 * szz0 + z * sxz0) / etae;
+    double Exz = exz + (z * sxx0 + z * szz0 + i33 * sxz0) / 2.0 / etae;
+    double gxz = 2.0 * exz + (z * sxx0 + z * szz0 + i33 * sxz0) / etae;
+    E[0] = Exx; E[1] = Ezz; E[2] = Exz;
+    E[3] = Exx * 1.0 + Ezz * z + gxz * z;
+    E[4] = Ezz * 1.0 + Exx * z - gxz * z;
+    E[5] = Exx * z - Exx * z + gxz * 0.5;
+}
+
+__device__ __forceinline__ void put(double *p, int i, double v) {
+    if (p) p[i] = v;
+}
+
+// One thread per centroid: loop over phases with a fraction above 1e-13.
+__global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_materials m, mdz_rheo_params prm,
+                                                             mdz_fields f, int *__restrict__ fail_count) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    int nc = g.ncx * g.ncz;
+    if (c >= nc) return;
+    const int avg = prm.eta_avg, nph = m.n_phases;
+    double eta = 0, eta_phys = 0, VE = 0, sxx = 0, szz = 0, sxz = 0, eel = 0, epl = 0, epwl = 0, elin = 0, ecst = 0,
+           dn = 0, xel = 0, xdi = 0, zel = 0, zdi = 0, dexx = 0, dezz = 0, dgxz = 0, dp = 0, vxx = 0, vzz = 0,
+           vxz = 0, vp = 0, pc = 0, del = 0, dpl = 0, Wt = 0, We = 0, Wd = 0, X = 0, OS = 0;
+    int fails = 0;
+    signed char t = g.BCp[c];
+    if (t != 30 && t != 31) {
+        const double etae = prm.iselastic == 1 ? prm.dt * f.mu_n[c] : 1.0;
+        const double exx = f.exxd[c], ezz = f.ezzd[c], exz = f.exz_n[c];
+        const double sxx0 = f.sxxd0[c], szz0 = f.szzd0[c], sxz0 = f.sxz0_n[c];
+        double E[6];
+        eff_rates(exx, ezz, exz, sxx0, szz0, sxz0, etae, E);
+        const double mu = f.mu_n[c], T = f.T[c], P = f.p[c], d0 = f.d0_n[c], phi0 = f.phi0_n[c];
+        const double X0 = f.X0_n ? f.X0_n[c] : 0.0, P0 = f.p0_n ? f.p0_n[c] : 0.0;
+        const double dil = f.dil_n[c], fric = f.fric_n[c], Coh = f.C_n[c], bet = f.bet_n[c];
+        for (int p = 0; p < nph; p++) {
+            double w = f.phase_perc_n[(size_t)p * nc + c];
+            if (!(fabs(w) > 1.0e-13)) continue;
+            visc_res o;
+            visc_local(p, mu, T, P, d0, phi0, X0, E[0], E[1], E[2], E[3], E[4], E[5], sxx0, szz0, sxz0, m, prm, dil,
+                       fric, Coh, P0, bet, o);
+            fails += o.ve_fail + o.vp_fail;
+            if (avg == 0) {
+                eta += w * o.etaVE; eta_phys += w * o.eta; dexx += w * o.detadexx; dezz += w * o.detadezz;
+                dgxz += w * o.detadexz / 2.0; dp += w * o.detadp;
+            }
+            if (avg == 0 || avg == 2) { sxx += w * o.txx; szz += w * o.tzz; sxz += w * o.txz; }
+            VE += w * o.VEcoeff; eel += w * o.Eii_el; epl += w * o.Eii_pl; epwl += w * o.Eii_pwl;
+            elin += w * o.Eii_lin; ecst += w * o.Eii_cst; dn += w * 1.0 / o.d1;
+            xel += w * o.Exx_el; xdi += w * o.Exx_diss; zel += w * o.Ezz_el; zdi += w * o.Ezz_diss;
+            Wt += w * (o.txx * exx + o.tzz * ezz + (o.txx + o.tzz) * (exx + ezz) + 2.0 * o.txz * exz);
+            Wd += w * (o.txx * o.Exx_diss + o.tzz * o.Ezz_diss + (o.txx + o.tzz) * (o.Exx_diss + o.Ezz_diss) +
+                       2.0 * o.txz * o.Exz_diss);
+            We += w * (o.txx * o.Exx_el + o.tzz * o.Ezz_el + (o.txx + o.tzz) * (o.Exx_el + o.Ezz_el) +
+                       2.0 * o.txz * o.Exz_el);
+            vxx += w * o.ddivpdexx; vzz += w * o.ddivpdezz; vxz += w * o.ddivpdexz / 2.0; vp += w * o.ddivpdp;
+            pc += w * o.Pcorr; del += w * o.div_el; dpl += w * o.div_pl;
+            X += w * o.X1; OS += w * o.OverS;
+            if (avg == 1) {
+                sxx += w * 1.0 / o.txx; szz += w * 1.0 / o.tzz; sxz += w * 1.0 / o.txz;
+                eta += w * 1.0 / o.etaVE; eta_phys += w * 1.0 / o.eta;
+                double ie2 = pow(o.etaVE, 2.0);
+                dexx += w * o.detadexx / ie2; dezz += w * o.detadezz / ie2;
+                dgxz += w * o.detadexz / 2.0 / ie2; dp += w * o.detadp / ie2;
+            }
+            if (avg == 2) {
+                eta += w * log(o.etaVE); eta_phys += w * log(o.eta);
+                dexx += w * o.detadexx / o.etaVE; dezz += w * o.detadezz / o.etaVE;
+                dgxz += w * o.detadexz / 2.0 / o.etaVE; dp += w * o.detadp / o.etaVE;
+            }
+        }
+        dn = 1.0 / dn;
+        if (avg == 1) {
+            sxx = 1.0 / sxx; szz = 1.0 / szz; sxz = 1.0 / sxz; eta = 1.0 / eta; eta_phys = 1.0 / eta_phys;
+            double e2 = pow(eta, 2.0);
+            dexx *= e2; dezz *= e2; dgxz *= e2; dp *= e2;
+        }
+        if (avg == 2) {
+            eta = exp(eta); eta_phys = exp(eta_phys);
+            dexx *= eta; dezz *= eta; dgxz *= eta; dp *= eta;
+        }
+    }
+    put(f.eta_n, c, eta); put(f.eta_phys_n, c, eta_phys); put(f.VE_n, c, VE);
+    put(f.sxxd, c, sxx); put(f.szzd, c, szz); put(f.sxz_n, c, sxz);
+    put(f.eII_el, c, eel); put(f.eII_pl, c, epl); put(f.eII_pwl, c, epwl); put(f.eII_lin, c, elin);
+    put(f.eII_cst, c, ecst); put(f.d_n, c, dn);
+    put(f.exx_el, c, xel); put(f.exx_diss, c, xdi); put(f.ezz_el, c, zel); put(f.ezz_diss, c, zdi);
+    put(f.detadexx_n, c, dexx); put(f.detadezz_n, c, dezz); put(f.detadgxz_n, c, dgxz); put(f.detadp_n, c, dp);
+    put(f.ddivpdexx_n, c, vxx); put(f.ddivpdezz_n, c, vzz); put(f.ddivpdgxz_n, c, vxz); put(f.ddivpdp_n, c, vp);
+    put(f.p_corr, c, pc); put(f.div_u_el, c, del); put(f.div_u_pl, c, dpl); put(f.div_u_r, c, 0.0);
+    put(f.Wtot, c, Wt); put(f.Wel, c, We); put(f.Wdiss, c, Wd); put(f.X_n, c, X); put(f.OverS_n, c, OS);
+    if (fails && fail_count) atomicAdd(fail_count, fails);
+}
+
+__global__ void __launch_bounds__(128) k_viscosity_vertices(mdz_dgrid g, mdz_materials m, mdz_rheo_params prm,
+                                                            mdz_fields f, int *__restrict__ fail_count) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    int nv = g.Nx * g.Nz;
+    if (c >= nv) return;
+    const int avg = prm.eta_avg, nph = m.n_phases;
+    double VE = 0, sxz = 0, eta_phys = 0, eta = 0, zel = 0, zdi = 0, dexx = 0, dezz = 0, dgxz = 0, dp = 0, X = 0,
+           OS = 0;
+    int fails = 0;
+    if (g.BCg[c] != 30) {
+        const double etae = prm.iselastic == 1 ? prm.dt * f.mu_s[c] : 1.0;
+        const double sxx0 = f.sxxd0_s[c], szz0 = f.szzd0_s[c], sxz0 = f.sxz0[c];
+        double E[6];
+        eff_rates(f.exxd_s[c], f.ezzd_s[c], f.exz[c], sxx0, szz0, sxz0, etae, E);
+        const double mu = f.mu_s[c], T = f.T_s[c], P = f.P_s[c], d0 = f.d0_s[c], phi0 = f.phi0_s[c];
+        const double X0 = f.X0_s ? f.X0_s[c] : 0.0, P0 = f.p0_s ? f.p0_s[c] : 0.0;
+        const double dil = f.dil_s[c], fric = f.fric_s[c], Coh = f.C_s[c], bet = f.bet_s[c];
+        for (int p = 0; p < nph; p++) {
+            double w = f.phase_perc_s[(size_t)p * nv + c];
+            if (!(fabs(w) > 1.0e-13)) continue;
+            visc_res o;
+            visc_local(p, mu, T, P, d0, phi0, X0, E[0], E[1], E[2], E[3], E[4], E[5], sxx0, szz0, sxz0, m, prm, dil,
+                       fric, Coh, P0, bet, o);
+            fails += o.ve_fail + o.vp_fail;
+            if (avg == 0) {
+                eta += w * o.etaVE; eta_phys += w * o.eta; dexx += w * o.detadexx; dezz += w * o.detadezz;
+                dgxz += w * o.detadexz / 2.0; dp += w * o.detadp;
+            }
+            if (avg == 0 || avg == 2) sxz += w * o.txz;
+            VE += w * o.VEcoeff; zel += w * o.Exz_el; zdi += w * o.Exz_diss; OS += w * o.OverS; X += w * o.X1;
+            if (avg == 1) {
+                sxz += w * 1.0 / o.txz; eta += w * 1.0 / o.etaVE; eta_phys += w * 1.0 / o.eta;
+                double ie2 = pow(o.etaVE, 2.0);
+                dexx += w * o.detadexx / ie2; dezz += w * o.detadezz / ie2;
+                dgxz += w * o.detadexz / 2.0 / ie2; dp += w * o.detadp / ie2;
+            }
+            if (avg == 2) {
+                eta += w * log(o.etaVE); eta_phys += w * log(o.eta);
+                dexx += w * o.detadexx / o.etaVE; dezz += w * o.detadezz / o.etaVE;
+                dgxz += w * o.detadexz / 2.0 / o.etaVE; dp += w * o.detadp / o.etaVE;
+            }
+        }
+        if (avg == 1) {
+            sxz = 1.0 / sxz; eta = 1.0 / eta; eta_phys = 1.0 / eta_phys;
+            double e2 = pow(eta, 2.0);
+            dexx *= e2; dezz *= e2; dgxz *= e2; dp *= e2;
+        }
+        if (avg == 2) {
+            eta = exp(eta); eta_phys = exp(eta_phys);
+            dexx *= eta; dezz *= eta; dgxz *= eta; dp *= eta;
+        }
+    }
+    put(f.VE_s, c, VE); put(f.sxz, c, sxz); put(f.eta_phys_s, c, eta_phys); put(f.eta_s, c, eta);
+    put(f.exz_el, c, zel); put(f.exz_diss, c, zdi);
+    put(f.detadexx_s, c, dexx); put(f.detadezz_s, c, dezz); put(f.detadgxz_s, c, dgxz); put(f.detadp_s, c, dp);
+    put(f.X_s, c, X); put(f.OverS_s, c, OS);
+    if (fails && fail_count) atomicAdd(fail_count, fails);
+}
+
+// ---------------------------------------------------------------------------
+// Rheological operators (isotropic): Picard D = 2 eta I / eta; Newton adds the
+// tangent terms 2 deta/dE * G.
+__global__ void k_operators(mdz_dgrid g, mdz_rheo_params prm, mdz_fields f, int jacobian) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int nc = g.ncx * g.ncz, nv = g.Nx * g.Nz;
+    if (i < nc) {
+        int k = i;
+        double d11 = 0, d12 = 0, d13 = 0, d14 = 0, d21 = 0, d22 = 0, d23 = 0, d24 = 0;
+        if (g.BCp[k] != 30 && g.BCp[k] != 31) {
+            double eta = f.eta_n[k];
+            d11 = 2.0 * eta; d22 = 2.0 * eta;
+            if (jacobian) {
+                double etae = prm.iselastic == 1 ? prm.dt * f.mu_n[k] : 1.0, E[6];
+                eff_rates(f.exxd[k], f.ezzd[k], f.exz_n[k], f.sxxd0[k], f.szzd0[k], f.sxz0_n[k], etae, E);
+                // K = 0 (incompressible): the K*dt*ddivp terms vanish
+                d11 += 2.0 * f.detadexx_n[k] * E[3];
+                d12 = 2.0 * f.detadezz_n[k] * E[3];
+                d13 = 2.0 * f.detadgxz_n[k] * E[3];
+                d14 = 2.0 * f.detadp_n[k] * E[0];
+                d21 = 2.0 * f.detadexx_n[k] * E[4];
+                d22 += 2.0 * f.detadezz_n[k] * E[4];
+                d23 = 2.0 * f.detadgxz_n[k] * E[4];
+                d24 = 2.0 * f.detadp_n[k] * E[1];
+            }
+        }
+        f.D11_n[k] = d11; f.D12_n[k] = d12; f.D13_n[k] = d13; f.D14_n[k] = d14;
+        f.D21_n[k] = d21; f.D22_n[k] = d22; f.D23_n[k] = d23; f.D24_n[k] = d24;
+    }
+    if (i < nv) {
+        int k = i;
+        double d31 = 0, d32 = 0, d33 = 0, d34 = 0;
+        if (g.BCg[k] != 30) {
+            double eta = f.eta_s[k];
+            d33 = eta;
+            if (jacobian) {
+                double etae = prm.iselastic == 1 ? prm.dt * f.mu_s[k] : 1.0, E[6];
+                eff_rates(f.exxd_s[k], f.ezzd_s[k], f.exz[k], f.sxxd0_s[k], f.szzd0_s[k], f.sxz0[k], etae, E);
+                d31 = 2.0 * f.detadexx_s[k] * E[5];
+                d32 = 2.0 * f.detadezz_s[k] * E[5];
+                d33 += 2.0 * f.detadgxz_s[k] * E[5];
+                d34 = 2.0 * f.detadp_s[k] * E[2];
+            }
+        }
+        f.D31_s[k] = d31; f.D32_s[k] = d32; f.D33_s[k] = d33; f.D34_s[k] = d34;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Momentum RHS (body force + elastic stress history), continuity RHS = 0.
+__global__ void k_rhs(mdz_dgrid g, mdz_rheo_params prm, double gx, double gz, mdz_fields f) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int Nx = g.Nx, Nz = g.Nz, ncx = g.ncx, nu = Nx * (Nz + 1), nvz = (Nx + 1) * Nz;
+    double dx = g.dx, dz = g.dz, dt = prm.dt;
+    if (i < nu) {
+        int c = i, k = c % Nx, l = c / Nx, c2 = k + (l - 1) * ncx;
+        double r = 0.0;
+        if (f.gx) f.gx[c] = gx;
+        signed char t = g.BCu[c];
+        if (l > 0 && l < Nz && (t == -1 || t == 2 || t == -2)) {
+            int iPrW = c2 - 1, iPrE = c2, ixyN = c, ixyS = c - Nx;
+            double inW = (k > 0 && g.BCp[iPrW] == -1) ? 1.0 : 0.0, inE = (k < Nx - 1 && g.BCp[iPrE] == -1) ? 1.0 : 0.0;
+            double inS = (g.BCg[ixyS] != 30 && g.BCu[c - Nx] != 13) ? 1.0 : 0.0;
+            double inN = (g.BCg[ixyN] != 30 && g.BCu[c + Nx] != 13) ? 1.0 : 0.0;
+            r = -gx * (0.5 * (f.rho_s[ixyS] + f.rho_s[ixyN]));
+            if (prm.iselastic == 1 && k > 0 && k < Nx - 1) {
+                if (inE) r -= 1.0 / dx * (f.eta_n[iPrE] / (f.mu_n[iPrE] * dt) * f.sxxd0[iPrE]);
+                if (inW) r -= 1.0 / dx * (-f.eta_n[iPrW] / (f.mu_n[iPrW] * dt) * f.sxxd0[iPrW]);
+                if (inN) r -= 1.0 / dz * (f.eta_s[ixyN] / (f.mu_s[ixyN] * dt) * f.sxz0[ixyN]);
+                if (inS) r -= 1.0 / dz * (-f.eta_s[ixyS] / (f.mu_s[ixyS] * dt) * f.sxz0[ixyS]);
+            }
+        }
+        f.roger_x[c] = -r;
+    }
+    if (i < nvz) {
+        int c = i, NxVz = Nx + 1, k = c % NxVz, l = c / NxVz, c1 = k + l * Nx - 1, c2 = k - 1 + (l - 1) * ncx;
+        double r = 0.0;
+        if (f.gz) f.gz[c] = gz;
+        if (k > 0 && k < NxVz - 1 && g.BCv[c] == -1) {
+            int iPrS = c2, iPrN = c2 + ncx, ixyE = c1 + 1, ixyW = c1;
+            double inS = (l > 0 && g.BCp[iPrS] == -1) ? 1.0 : 0.0, inN = (l < Nz - 1 && g.BCp[iPrN] == -1) ? 1.0 : 0.0;
+            double inW = (g.BCg[ixyW] != 30 && g.BCv[c - 1] != 13) ? 1.0 : 0.0;
+            double inE = (g.BCg[ixyE] != 30 && g.BCv[c + 1] != 13) ? 1.0 : 0.0;
+            r = -gz * (0.5 * ((l > 0 ? f.rho_n[iPrS] : 0.0) + (l < Nz - 1 ? f.rho_n[iPrN] : 0.0)));
+            if (prm.iselastic == 1 && l > 0 && l < Nz - 1) {
+                if (inN) r -= 1.0 / dz * (f.eta_n[iPrN] / (f.mu_n[iPrN] * dt) * (f.szzd0[iPrN]));
+                if (inS) r -= 1.0 / dz * (-f.eta_n[iPrS] / (f.mu_n[iPrS] * dt) * (f.szzd0[iPrS]));
+                if (inE) r -= 1.0 / dx * (f.eta_s[ixyE] / (f.mu_s[ixyE] * dt) * f.sxz0[ixyE]);
+                if (inW) r -= 1.0 / dx * (-f.eta_s[ixyW] / (f.mu_s[ixyW] * dt) * f.sxz0[ixyW]);
+            }
+        }
+        f.roger_z[c] = -r;
+    }
+    if (i < ncx * g.ncz && g.BCp[i] != 30 && g.BCp[i] != 31) f.rhs_p[i] = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Device-level launchers (used by the host drop-ins and by the time step).
+mdz_status mdz_dev_strain_rates(mdz_ctx *ctx, const mdz_fields &f, cudaStream_t st) {
+    const mdz_dgrid &g = ctx->g;
+    int nc = g.ncx * g.ncz, nv = g.Nx * g.Nz;
+    k_strain_centroids<<<mdz_blocks(nc), MDZ_THREADS, 0, st>>>(g, f.u, f.v, f.div_u, f.exxd, f.ezzd);
+    MDZ_LAUNCHED(ctx);
+    k_strain_vertices<<<mdz_blocks(nv), MDZ_THREADS, 0, st>>>(g, f.u, f.v, f.exz);
+    MDZ_LAUNCHED(ctx);
+    k_exz_to_centroids<<<mdz_blocks(nc), MDZ_THREADS, 0, st>>>(g, f.exz, f.exz_n);
+    MDZ_LAUNCHED(ctx);
+    k_c2v<<<mdz_blocks(nv), MDZ_THREADS, 0, st>>>(g, f.exxd, f.exxd_s);
+    MDZ_LAUNCHED(ctx);
+    k_c2v<<<mdz_blocks(nv), MDZ_THREADS, 0, st>>>(g, f.ezzd, f.ezzd_s);
+    MDZ_LAUNCHED(ctx);
+    return MDZ_OK;
+}
+
+mdz_status mdz_dev_c2v(mdz_ctx *ctx, const double *cen, double *ver, cudaStream_t st) {
+    k_c2v<<<mdz_blocks(ctx->g.Nx * ctx->g.Nz), MDZ_THREADS, 0, st>>>(ctx->g, cen, ver);
+    MDZ_LAUNCHED(ctx);
+    return MDZ_OK;
+}
+
+mdz_status mdz_dev_v2c(mdz_ctx *ctx, double *cen, const double *ver, cudaStream_t st) {
+    k_v2c<<<mdz_blocks(ctx->g.ncx * ctx->g.ncz), MDZ_THREADS, 0, st>>>(ctx->g, cen, ver);
+    MDZ_LAUNCHED(ctx);
+    return MDZ_OK;
+}
+
+mdz_status mdz_check_materials(mdz_ctx *ctx, const mdz_materials *m) {
+    if (m->n_phases < 1 || m->n_phases > MDZ_MAX_PHASES || m->n_phases > ctx->n_phases)
+        return mdz_fail(ctx, MDZ_ERR_ARG, "materials: %d phases (context has %d)", m->n_phases, ctx->n_phases);
+    for (int p = 0; p < m->n_phases; p++) {
+        if (m->expv[p] || m->gbsv[p] || m->gs[p] || m->reac_soft[p] || m->phase_mix[p] || m->is_tensile[p])
+            return mdz_fail(ctx, MDZ_ERR_UNSUPPORTED,
+                            "phase %d: Peierls, GBS, grain-size evolution, reaction mixing and the tension cut-off "
+                            "are not implemented", p);
+        if (m->pwlv[p] && m->npwl[p] <= 0) return mdz_fail(ctx, MDZ_ERR_ARG, "phase %d: npwl must be > 0", p);
+        if (m->linv[p] && m->nlin[p] <= 0) return mdz_fail(ctx, MDZ_ERR_ARG, "phase %d: nlin must be > 0", p);
+        if (m->n_vp[p] <= 0) return mdz_fail(ctx, MDZ_ERR_ARG, "phase %d: n_vp must be > 0", p);
+    }
+    return MDZ_OK;
+}
+
+mdz_status mdz_dev_viscosity(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm, const mdz_fields &f,
+                             int *d_fail, cudaStream_t st) {
+    const mdz_dgrid &g = ctx->g;
+    int nc = g.ncx * g.ncz, nv = g.Nx * g.Nz;
+    // vertex copies of centroid fields (NonNewtonianViscosityGrid :979-983)
+    mdz_status s;
+    if ((s = mdz_dev_c2v(ctx, f.div_u, f.div_u_s, st)) != MDZ_OK) return s;
+    if ((s = mdz_dev_c2v(ctx, f.T, f.T_s, st)) != MDZ_OK) return s;
+    if ((s = mdz_dev_c2v(ctx, f.p, f.P_s, st)) != MDZ_OK) return s;
+    if ((s = mdz_dev_c2v(ctx, f.d0_n, f.d0_s, st)) != MDZ_OK) return s;
+    if ((s = mdz_dev_c2v(ctx, f.phi0_n, f.phi0_s, st)) != MDZ_OK) return s;
+    k_viscosity_centroids<<<mdz_blocks(nc, 128), 128, 0, st>>>(g, *m, *prm, f, d_fail);
+    MDZ_LAUNCHED(ctx);
+    k_viscosity_vertices<<<mdz_blocks(nv, 128), 128, 0, st>>>(g, *m, *prm, f, d_fail);
+    MDZ_LAUNCHED(ctx);
+    return MDZ_OK;
+}
+
+mdz_status mdz_dev_operators(mdz_ctx *ctx, const mdz_rheo_params *prm, const mdz_fields &f, int jacobian,
+                             cudaStream_t st) {
+    const mdz_dgrid &g = ctx->g;
+    int n = g.Nx * g.Nz;
+    k_operators<<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(g, *prm, f, jacobian);
+    MDZ_LAUNCHED(ctx);
+    return MDZ_OK;
+}
+
+mdz_status mdz_dev_rhs(mdz_ctx *ctx, const mdz_rheo_params *prm, double gx, double gz, const mdz_fields &f,
+                       cudaStream_t st) {
+    const mdz_dgrid &g = ctx->g;
+    int n = (g.Nx + 1) * (g.Nz + 1);
+    k_rhs<<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(g, *prm, gx, gz, f);
+    MDZ_LAUNCHED(ctx);
+    return MDZ_OK;
+}

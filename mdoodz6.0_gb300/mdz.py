@@ -241,3 +241,126 @@ class Context:
         u = np.ascontiguousarray(u, np.float64)
         v = np.ascontiguousarray(v, np.float64)
         self._check(self.L.mdz_RogerGuntherII(self.h, _dptr(u), _dptr(v), C.c_double(dt)))
+
+    # grid-side entry points (fields: a GridFields) --------------------------
+    def StrainRateComponents(self, fields):
+        s = fields.struct()
+        self._check(self.L.mdz_StrainRateComponents(self.h, C.byref(s)))
+
+    def NonNewtonianViscosityGrid(self, mat, prm, fields):
+        s = fields.struct()
+        nc = C.c_int(0)
+        self._check(self.L.mdz_NonNewtonianViscosityGrid(self.h, C.byref(mat), C.byref(prm), C.byref(s),
+                                                         C.byref(nc)))
+        return nc.value
+
+    def RheologicalOperators(self, prm, fields, jacobian):
+        s = fields.struct()
+        self._check(self.L.mdz_RheologicalOperators(self.h, C.byref(prm), C.byref(s), C.c_int(jacobian)))
+
+    def EvaluateRHS(self, prm, gx, gz, fields):
+        s = fields.struct()
+        self._check(self.L.mdz_EvaluateRHS(self.h, C.byref(prm), C.c_double(gx), C.c_double(gz), C.byref(s)))
+
+
+# ---- grid fields / rheology structures (mdz_fields, mdz_materials, mdz_rheo_params) ----
+FIELD_NAMES = [
+    "u", "v", "p", "p_corr",
+    "div_u", "div_u_s", "exxd", "ezzd", "exz", "exz_n", "exxd_s", "ezzd_s",
+    "sxxd0", "szzd0", "sxz0", "sxxd0_s", "szzd0_s", "sxz0_n",
+    "mu_n", "mu_s", "T", "T_s", "P_s", "d0_n", "d0_s", "phi0_n", "phi0_s", "X0_n", "X0_s",
+    "strain_n", "strain_s", "dil_n", "dil_s", "fric_n", "fric_s", "C_n", "C_s", "p0_n", "p0_s",
+    "bet_n", "bet_s", "rho_n", "rho_s",
+    "phase_perc_n", "phase_perc_s",
+    "eta_n", "eta_s", "eta_phys_n", "eta_phys_s", "VE_n", "VE_s", "sxxd", "szzd", "sxz", "sxz_n",
+    "eII_el", "eII_pl", "eII_pwl", "eII_lin", "eII_cst", "d_n",
+    "exx_el", "ezz_el", "exz_el", "exx_diss", "ezz_diss", "exz_diss",
+    "detadexx_n", "detadezz_n", "detadgxz_n", "detadp_n",
+    "ddivpdexx_n", "ddivpdezz_n", "ddivpdgxz_n", "ddivpdp_n",
+    "detadexx_s", "detadezz_s", "detadgxz_s", "detadp_s",
+    "div_u_el", "div_u_pl", "div_u_r", "Wtot", "Wel", "Wdiss", "X_n", "X_s", "OverS_n", "OverS_s",
+    "D11_n", "D12_n", "D13_n", "D14_n", "D21_n", "D22_n", "D23_n", "D24_n",
+    "D31_s", "D32_s", "D33_s", "D34_s",
+    "roger_x", "roger_z", "rhs_p", "gx", "gz",
+    "ru", "rv", "rp",
+]
+
+VERTEX_FIELDS = {"div_u_s", "exz", "exxd_s", "ezzd_s", "sxz0", "sxxd0_s", "szzd0_s", "mu_s", "T_s", "P_s", "d0_s",
+                 "phi0_s", "X0_s", "strain_s", "dil_s", "fric_s", "C_s", "p0_s", "bet_s", "rho_s", "eta_s",
+                 "eta_phys_s", "VE_s", "sxz", "exz_el", "exz_diss", "detadexx_s", "detadezz_s", "detadgxz_s",
+                 "detadp_s", "X_s", "OverS_s", "D31_s", "D32_s", "D33_s", "D34_s"}
+VX_FIELDS = {"u", "roger_x", "gx", "ru"}
+VZ_FIELDS = {"v", "roger_z", "gz", "rv"}
+
+
+def field_size(grid, name, n_phases=1):
+    if name in VX_FIELDS:
+        return grid.size(-1)
+    if name in VZ_FIELDS:
+        return grid.size(-2)
+    if name == "phase_perc_n":
+        return n_phases * grid.size(1)
+    if name == "phase_perc_s":
+        return n_phases * grid.size(0)
+    if name in VERTEX_FIELDS:
+        return grid.size(0)
+    return grid.size(1)
+
+
+class FieldsStruct(C.Structure):
+    _fields_ = [(n, _dp) for n in FIELD_NAMES]
+
+
+class GridFields:
+    """Host arrays for every mdz_fields member (zero-initialised), by name."""
+
+    def __init__(self, grid, n_phases, init=None):
+        self.grid, self.n_phases = grid, n_phases
+        self.a = {n: np.zeros(field_size(grid, n, n_phases)) for n in FIELD_NAMES}
+        for k, v in (init or {}).items():
+            self.a[k][:] = np.asarray(v, np.float64).ravel()
+
+    def __getitem__(self, k):
+        return self.a[k]
+
+    def __setitem__(self, k, v):
+        self.a[k][:] = np.asarray(v, np.float64).ravel()
+
+    def struct(self):
+        s = FieldsStruct()
+        for n in FIELD_NAMES:
+            setattr(s, n, self.a[n].ctypes.data_as(_dp))
+        return s
+
+
+MAT_INT = ["cstv", "pwlv", "linv", "expv", "gbsv", "gs", "is_tensile", "reac_soft", "phase_mix"]
+MAT_DBL = ["eta0", "rho", "alp", "gs_ref", "Slim", "eta_vp", "n_vp",
+           "npwl", "Apwl", "Qpwl", "Vpwl", "mpwl", "rpwl", "fpwl", "apwl", "Fpwl", "pref_pwl",
+           "nlin", "Alin", "Qlin", "Vlin", "mlin", "rlin", "flin", "alin", "Flin"]
+
+
+class Materials(C.Structure):
+    _fields_ = ([("n_phases", C.c_int), ("R", C.c_double)]
+                + [(n, C.c_int * MDZ_MAX_PHASES) for n in MAT_INT]
+                + [(n, C.c_double * MDZ_MAX_PHASES) for n in MAT_DBL])
+
+    @classmethod
+    def from_phases(cls, phases, R=8.314510):
+        m = cls()
+        m.n_phases = len(phases)
+        m.R = R
+        for p, props in enumerate(phases):
+            for k, v in props.items():
+                getattr(m, k)[p] = v
+        return m
+
+
+class RheoParams(C.Structure):
+    _fields_ = [("dt", C.c_double), ("iselastic", C.c_int), ("step", C.c_int), ("eta_avg", C.c_int),
+                ("mineta", C.c_double), ("maxeta", C.c_double), ("scale_T", C.c_double), ("scale_E", C.c_double),
+                ("scale_S", C.c_double), ("scale_eta", C.c_double), ("scale_L", C.c_double)]
+
+    @classmethod
+    def make(cls, dt, iselastic=1, step=1, eta_avg=0, mineta=1e-100, maxeta=1e100, scale_T=1.0, scale_E=1.0,
+             scale_S=1.0, scale_eta=1.0, scale_L=1.0):
+        return cls(dt, iselastic, step, eta_avg, mineta, maxeta, scale_T, scale_E, scale_S, scale_eta, scale_L)

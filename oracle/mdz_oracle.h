@@ -43,3 +43,26 @@ int orc_rk4(const mdz_grid_desc *g, int n, double *x, double *z, int *phase, dou
 }
 #endif
 #endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+/* StrainRateComponents (SOURCE/RheologyDensity.c:1902-1984), incl. the two
+ * InterpCentroidsToVerticesDouble calls at its end. */
+int orc_strain_rates(const mdz_grid_desc *g, mdz_fields *f);
+/* InterpCentroidsToVerticesDouble (SOURCE/GridRoutines.c:106-198), non-periodic. */
+int orc_c2v(const mdz_grid_desc *g, const double *cen, double *ver);
+/* InterpVerticesToCentroidsDouble (SOURCE/GridRoutines.c:204-228). */
+int orc_v2c(const mdz_grid_desc *g, double *cen, const double *ver);
+/* NonNewtonianViscosityGrid + Viscosity, isotropic (SOURCE/RheologyDensity.c:961-1415, 44-707).
+ * not_conv (optional, 2 ints) receives the number of local visco-elastic and
+ * visco-plastic solves that hit the 20-iteration cap. */
+int orc_viscosity_grid(const mdz_grid_desc *g, const mdz_materials *mat, const mdz_rheo_params *prm, mdz_fields *f,
+                       int *not_conv);
+/* RheologicalOperators, isotropic (SOURCE/RheologyDensity.c:713-954). */
+int orc_rheo_operators(const mdz_grid_desc *g, const mdz_rheo_params *prm, mdz_fields *f, int jacobian);
+/* EvaluateRHS, incompressible, non-polar (SOURCE/StokesRoutines.c:922-1133). */
+int orc_rhs(const mdz_grid_desc *g, const mdz_rheo_params *prm, double gx, double gz, mdz_fields *f);
+#ifdef __cplusplus
+}
+#endif

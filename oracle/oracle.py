@@ -95,3 +95,25 @@ class Oracle:
         self.L.orc_rk4(C.byref(self._desc), C.c_int(self.n), _d(self.x), _d(self.z), _i(self.phase), _d(vx),
                        _d(vz), _d(u), _d(v), C.c_double(dt))
         return vx, vz
+
+
+def strain_rates(grid, fields):
+    s = fields.struct()
+    lib().orc_strain_rates(C.byref(grid.desc()), C.byref(s))
+
+
+def viscosity_grid(grid, mat, prm, fields):
+    s = fields.struct()
+    nc = np.zeros(2, np.int32)
+    lib().orc_viscosity_grid(C.byref(grid.desc()), C.byref(mat), C.byref(prm), C.byref(s), _i(nc))
+    return nc
+
+
+def rheo_operators(grid, prm, fields, jacobian):
+    s = fields.struct()
+    lib().orc_rheo_operators(C.byref(grid.desc()), C.byref(prm), C.byref(s), C.c_int(jacobian))
+
+
+def rhs(grid, prm, gx, gz, fields):
+    s = fields.struct()
+    lib().orc_rhs(C.byref(grid.desc()), C.byref(prm), C.c_double(gx), C.c_double(gz), C.byref(s))

@@ -95,7 +95,140 @@ def make_markers_fixture():
     print("markers_ref.npz:", len(out), "arrays")
 
 
+
+
+# ---- local rheology -------------------------------------------------------------
+RHEO_PHASES = [
+    # constant viscosity + elasticity + Drucker-Prager
+    dict(cstv=1, eta0=1.0, rho=1.0, Slim=1e10, eta_vp=0.0, n_vp=1.0, gs_ref=1.0),
+    # dislocation creep + elasticity + plasticity with a viscoplastic regularisation
+    dict(pwlv=1, npwl=3.0, Apwl=2.0e-3, Qpwl=1.2e4, Vpwl=0.05, mpwl=0.0, rpwl=0.0, fpwl=1.0, apwl=0.0, Fpwl=1.0,
+         pref_pwl=1.0, rho=1.1, Slim=1e10, eta_vp=0.02, n_vp=1.0, gs_ref=1.0),
+    # diffusion + dislocation creep, von Mises cap
+    dict(linv=1, nlin=1.0, Alin=0.3, Qlin=5.0e3, Vlin=0.0, mlin=0.0, rlin=0.0, flin=1.0, alin=0.0, Flin=1.0,
+         pwlv=1, npwl=3.5, Apwl=1.0e-3, Qpwl=1.5e4, Vpwl=0.0, mpwl=0.0, rpwl=0.0, fpwl=1.0, apwl=0.0, Fpwl=1.0,
+         pref_pwl=1.0, rho=0.9, Slim=1.3, eta_vp=0.0, n_vp=1.0, gs_ref=1.0),
+]
+RHEO_MODEL = dict(dt=0.5, iselastic=1, step=1, eta_avg=0, mineta=1e-3, maxeta=1e6)
+RHEO_R = 8.314
+
+
+def rheology_inputs(g, rng):
+    """Smooth random grid fields for the rheology fixtures."""
+    Nx, Nz = g.Nx, g.Nz
+    X, Z = np.meshgrid(g.xg, g.zvx)
+    u = (-X + 0.3 * np.sin(2.3 * Z + 0.4) * np.cos(1.7 * X)).ravel()
+    X, Z = np.meshgrid(g.xvz, g.zg)
+    v = (Z + 0.25 * np.cos(1.9 * X) * np.sin(2.1 * Z + 0.2)).ravel()
+    Xc, Zc = np.meshgrid(g.xc, g.zc)
+    Xv, Zv = np.meshgrid(g.xg, g.zg)
+    f = dict(
+        u=u, v=v,
+        p=(0.6 + 0.8 * np.sin(3 * Xc) * np.cos(2 * Zc)).ravel(),
+        T=(900.0 + 400.0 * Zc + 100 * Xc).ravel(),
+        mu_n=np.full(Xc.size, 1.0), mu_s=np.full(Xv.size, 1.0),
+        C_n=(0.3 + 0.3 * rng.random(Xc.size)), C_s=(0.3 + 0.3 * rng.random(Xv.size)),
+        fric_n=np.full(Xc.size, np.pi / 6), fric_s=np.full(Xv.size, np.pi / 6),
+        dil_n=np.zeros(Xc.size), dil_s=np.zeros(Xv.size),
+        bet_n=np.full(Xc.size, 1e-2), bet_s=np.full(Xv.size, 1e-2),
+        sxxd0=0.3 * rng.standard_normal(Xc.size), szzd0=0.3 * rng.standard_normal(Xc.size),
+        sxz0=0.3 * rng.standard_normal(Xv.size),
+        d0_n=np.full(Xc.size, 1.0), phi0_n=np.zeros(Xc.size),
+        rho_n=np.full(Xc.size, 1.0), rho_s=np.full(Xv.size, 1.0),
+    )
+    return f
+
+
+def make_rheology_fixture(avg=0, tag=""):
+    g = _grid()
+    r = RefMDOODZ(NX, NZ, XMIN, XMAX, ZMIN, ZMAX, 3)
+    r.set_bc_pureshear(1.0)
+    for k, v in RHEO_MODEL.items():
+        r.set_param(k, v)
+    r.set_param("eta_avg", avg)
+    r.set_param("R", RHEO_R)
+    for p, props in enumerate(RHEO_PHASES):
+        for k, v in props.items():
+            r.set_mat(k, p, v)
+    x, z, ph = _markers(g, seed=11)
+    ph[ph == -1] = 0
+    r.set_markers(x, z, ph)
+    pp = {}
+    for centroid, key in ((1, "phase_perc_n"), (0, "phase_perc_s")):
+        r.p2g(np.zeros(3), 0, 0, 1, centroid, 1)
+        pp[key] = np.array([r.phase_perc(centroid, p).copy() for p in range(3)])
+    rng = np.random.default_rng(5)
+    f = rheology_inputs(g, rng)
+    for name, arr in f.items():
+        key = {"u": "u_in", "v": "v_in", "p": "p_in"}.get(name, name)
+        r.field(key)[:] = arr
+    for p in range(3):
+        r.phase_perc(1, p)[:] = pp["phase_perc_n"][p]
+        r.phase_perc(0, p)[:] = pp["phase_perc_s"][p]
+    # old stresses on the other node sets, as the time loop prepares them
+    # (InterpCentroidsToVerticesDouble / InterpVerticesToCentroidsDouble)
+    r.strain_rates()
+    out = dict(inputs=np.array(sorted(f)), **{"in_" + k: v for k, v in f.items()}, **{"in_" + k: v for k, v in pp.items()})
+    # sxxd0_s, szzd0_s, sxz0_n are inputs too: build them like the time loop does
+    import ctypes
+    Lr = r.lib
+    Lr.ref_field.restype = ctypes.POINTER(ctypes.c_double)
+    sxxd0_s = _c2v_np(g, f["sxxd0"])
+    szzd0_s = _c2v_np(g, f["szzd0"])
+    sxz0_n = _v2c_np(g, f["sxz0"])
+    r.field("sxxd0_s")[:] = sxxd0_s
+    r.field("szzd0_s")[:] = szzd0_s
+    r.field("sxz0_n")[:] = sxz0_n
+    out["in_sxxd0_s"], out["in_szzd0_s"], out["in_sxz0_n"] = sxxd0_s, szzd0_s, sxz0_n
+    for name in ("div_u", "exxd", "ezzd", "exz", "exz_n", "exxd_s", "ezzd_s"):
+        out["sr_" + name] = r.field(name).copy()
+    r.viscosity_grid()
+    for name in ("eta_n", "eta_s", "eta_phys_n", "eta_phys_s", "VE_n", "VE_s", "sxxd", "szzd", "sxz", "sxz_n",
+                 "eII_el", "eII_pl", "eII_pwl", "eII_lin", "eII_cst", "d_n", "exx_el", "ezz_el", "exz_el",
+                 "exx_diss", "ezz_diss", "exz_diss", "detadexx_n", "detadezz_n", "detadgxz_n", "detadp_n",
+                 "ddivpdexx_n", "ddivpdezz_n", "ddivpdgxz_n", "ddivpdp_n", "detadexx_s", "detadezz_s",
+                 "detadgxz_s", "detadp_s", "p_corr", "div_u_el", "div_u_pl", "div_u_r", "Wtot", "Wel", "Wdiss",
+                 "OverS_n", "OverS_s", "T_s", "P_s", "div_u_s"):
+        out["vg_" + name] = r.field(name).copy()
+    r.rheo_operators(0)
+    for name in ("D11_n", "D12_n", "D13_n", "D14_n", "D21_n", "D22_n", "D23_n", "D24_n", "D31_s", "D32_s", "D33_s",
+                 "D34_s"):
+        out["op0_" + name] = r.field(name).copy()
+    r.rheo_operators(1)
+    for name in ("D11_n", "D12_n", "D13_n", "D14_n", "D21_n", "D22_n", "D23_n", "D24_n", "D31_s", "D32_s", "D33_s",
+                 "D34_s"):
+        out["op1_" + name] = r.field(name).copy()
+    r.set_param("gz", -1.0)
+    r.rhs()
+    for name in ("roger_x", "roger_z", "rhs_p"):
+        out["rhs_" + name] = r.field(name).copy()
+    out["gz"] = -1.0
+    np.savez_compressed(os.path.join(HERE, "rheology_ref%s.npz" % tag), **out)
+    print("rheology_ref%s.npz: plastic centroids %d / %d" % (tag, (out["vg_eII_pl"] > 0).sum(), out["vg_eII_pl"].size))
+
+
+def _c2v_np(g, cen):
+    ncx, ncz = g.ncx, g.ncz
+    t = np.zeros((ncz + 2, ncx + 2))
+    t[1:-1, 1:-1] = cen.reshape(ncz, ncx)
+    t[0, 1:-1] = t[1, 1:-1]
+    t[-1, 1:-1] = t[-2, 1:-1]
+    t[1:-1, 0] = t[1:-1, 1]
+    t[1:-1, -1] = t[1:-1, -2]
+    t[0, 0], t[0, -1], t[-1, 0], t[-1, -1] = t[1, 1], t[1, -2], t[-2, 1], t[-2, -2]
+    return (0.25 * (t[:-1, :-1] + t[:-1, 1:] + t[1:, :-1] + t[1:, 1:])).ravel()
+
+
+def _v2c_np(g, ver):
+    V = ver.reshape(g.Nz, g.Nx)
+    return (0.25 * (V[:-1, :-1] + V[:-1, 1:] + V[1:, :-1] + V[1:, 1:])).ravel()
+
+
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["markers"]
+    what = sys.argv[1:] or ["markers", "rheology"]
     if "markers" in what:
         make_markers_fixture()
+    if "rheology" in what:
+        make_rheology_fixture(0)
+        make_rheology_fixture(1, "_harm")
+        make_rheology_fixture(2, "_geom")
