@@ -228,6 +228,25 @@ mdz_status mdz_RheologicalOperators(mdz_ctx *ctx, const mdz_rheo_params *prm, md
  * non-polar: roger_x, roger_z (body force and elastic history), rhs_p. */
 mdz_status mdz_EvaluateRHS(mdz_ctx *ctx, const mdz_rheo_params *prm, double gx, double gz, mdz_fields *f);
 
+/* ---- decoupled Stokes ----------------------------------------------------- */
+
+/* EvaluateStokesResidualDecoupled (SOURCE/StokesRoutines.c:839-920) with the
+ * residual rows of BuildStokesOperatorDecoupled(Assemble = 0)
+ * (SOURCE/StokesAssemblyDecoupled.c:1573-2150): reads u, v, p_corr, D11_n,
+ * D22_n, D33_s (Picard operators), roger_x, roger_z, rhs_p; writes ru, rv, rp
+ * (grid layout, zero off the equations) and norms3 = sqrt(sum F^2 / n) for the
+ * x-momentum, z-momentum and continuity blocks.  MDZ_ERR_NAN where the
+ * reference exit(122)s. */
+mdz_status mdz_EvaluateStokesResidualDecoupled(mdz_ctx *ctx, mdz_fields *f, double *norms3);
+
+/* Matrix-free linear operator, the product of the reference's assembled
+ * blocks with a correction vector (x zero on non-equation nodes):
+ * jacobian = 0: BuildStokesOperatorDecoupled(Assemble = 1) blocks [A B; C D];
+ * jacobian = 1: BuildJacobianOperatorDecoupled (SOURCE/StokesAssemblyDecoupled.c:3834-4376).
+ * Uses the D-tensor fields in f.  Host buffers in grid layout. */
+mdz_status mdz_StokesOperatorApply(mdz_ctx *ctx, mdz_fields *f, int jacobian, const double *xu, const double *xv,
+                                   const double *xp, double *yu, double *yv, double *yp);
+
 #ifdef __cplusplus
 }
 #endif

@@ -45,7 +45,7 @@ void mdz_free_fields(mdz_ctx *ctx) {
 
 // Upload every non-null host field (the host drop-ins are synchronous and
 // simple: they mirror the caller's whole grid state), or download a named set.
-static mdz_status upload_all(mdz_ctx *ctx, const mdz_fields *h, cudaStream_t st) {
+mdz_status mdz_upload_fields(mdz_ctx *ctx, const mdz_fields *h, cudaStream_t st) {
     mdz_fields &d = ctx->d;
 #define UP(name, kind)                                                                                         \
     if (h->name)                                                                                               \
@@ -56,7 +56,7 @@ static mdz_status upload_all(mdz_ctx *ctx, const mdz_fields *h, cudaStream_t st)
     return MDZ_OK;
 }
 
-static mdz_status download(mdz_ctx *ctx, const mdz_fields *h, const char *const *names, int n, cudaStream_t st) {
+mdz_status mdz_download_fields(mdz_ctx *ctx, const mdz_fields *h, const char *const *names, int n, cudaStream_t st) {
     const mdz_fields &d = ctx->d;
     for (int i = 0; i < n; i++) {
 #define DOWN(name, kind)                                                                                       \
@@ -77,10 +77,10 @@ extern "C" mdz_status mdz_StrainRateComponents(mdz_ctx *ctx, mdz_fields *f) {
     mdz_status s = mdz_ensure_fields(ctx);
     if (s != MDZ_OK) return s;
     cudaStream_t st = ctx->stream;
-    if ((s = upload_all(ctx, f, st)) != MDZ_OK) return s;
+    if ((s = mdz_upload_fields(ctx, f, st)) != MDZ_OK) return s;
     if ((s = mdz_dev_strain_rates(ctx, ctx->d, st)) != MDZ_OK) return s;
     NAMES("div_u", "exxd", "ezzd", "exz", "exz_n", "exxd_s", "ezzd_s");
-    return download(ctx, f, names, nnames, st);
+    return mdz_download_fields(ctx, f, names, nnames, st);
 }
 
 extern "C" mdz_status mdz_NonNewtonianViscosityGrid(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm,
@@ -90,7 +90,7 @@ extern "C" mdz_status mdz_NonNewtonianViscosityGrid(mdz_ctx *ctx, const mdz_mate
     if (s != MDZ_OK) return s;
     if ((s = mdz_ensure_fields(ctx)) != MDZ_OK) return s;
     cudaStream_t st = ctx->stream;
-    if ((s = upload_all(ctx, f, st)) != MDZ_OK) return s;
+    if ((s = mdz_upload_fields(ctx, f, st)) != MDZ_OK) return s;
     MDZ_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(int), st));
     if ((s = mdz_dev_viscosity(ctx, m, prm, ctx->d, ctx->d_counters, st)) != MDZ_OK) return s;
     int fails = 0;
@@ -101,7 +101,7 @@ extern "C" mdz_status mdz_NonNewtonianViscosityGrid(mdz_ctx *ctx, const mdz_mate
           "detadp_n", "ddivpdexx_n", "ddivpdezz_n", "ddivpdgxz_n", "ddivpdp_n", "detadexx_s", "detadezz_s",
           "detadgxz_s", "detadp_s", "p_corr", "div_u_el", "div_u_pl", "div_u_r", "Wtot", "Wel", "Wdiss", "X_n",
           "X_s", "OverS_n", "OverS_s");
-    s = download(ctx, f, names, nnames, st);
+    s = mdz_download_fields(ctx, f, names, nnames, st);
     if (n_not_converged) *n_not_converged = fails;
     return s;
 }
@@ -111,10 +111,10 @@ extern "C" mdz_status mdz_RheologicalOperators(mdz_ctx *ctx, const mdz_rheo_para
     mdz_status s = mdz_ensure_fields(ctx);
     if (s != MDZ_OK) return s;
     cudaStream_t st = ctx->stream;
-    if ((s = upload_all(ctx, f, st)) != MDZ_OK) return s;
+    if ((s = mdz_upload_fields(ctx, f, st)) != MDZ_OK) return s;
     if ((s = mdz_dev_operators(ctx, prm, ctx->d, jacobian, st)) != MDZ_OK) return s;
     NAMES("D11_n", "D12_n", "D13_n", "D14_n", "D21_n", "D22_n", "D23_n", "D24_n", "D31_s", "D32_s", "D33_s", "D34_s");
-    return download(ctx, f, names, nnames, st);
+    return mdz_download_fields(ctx, f, names, nnames, st);
 }
 
 extern "C" mdz_status mdz_EvaluateRHS(mdz_ctx *ctx, const mdz_rheo_params *prm, double gx, double gz, mdz_fields *f) {
@@ -122,8 +122,8 @@ extern "C" mdz_status mdz_EvaluateRHS(mdz_ctx *ctx, const mdz_rheo_params *prm, 
     mdz_status s = mdz_ensure_fields(ctx);
     if (s != MDZ_OK) return s;
     cudaStream_t st = ctx->stream;
-    if ((s = upload_all(ctx, f, st)) != MDZ_OK) return s;
+    if ((s = mdz_upload_fields(ctx, f, st)) != MDZ_OK) return s;
     if ((s = mdz_dev_rhs(ctx, prm, gx, gz, ctx->d, st)) != MDZ_OK) return s;
     NAMES("roger_x", "roger_z", "rhs_p", "gx", "gz");
-    return download(ctx, f, names, nnames, st);
+    return mdz_download_fields(ctx, f, names, nnames, st);
 }

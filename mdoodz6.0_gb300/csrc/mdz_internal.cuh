@@ -48,6 +48,8 @@ struct mdz_ctx {
     mdz_fields d{};              // device mirrors of every grid field (allocated on first use)
     bool fields_ready = false;
     int *d_counters = nullptr;   // small device scratch: failure counters etc.
+    bool bcs_checked = false, bcs_ok = false;
+    struct mdz_solver *solver = nullptr;   // Krylov / multigrid workspace (solver.cu)
     std::string err;
     // host-call staging buffers (grown on demand)
     void *stage[8] = {nullptr};
@@ -205,6 +207,8 @@ mdz_status mdz_ensure_bins(mdz_ctx *ctx, cudaStream_t st);
 enum mdz_field_kind { MDZ_K_VX, MDZ_K_VZ, MDZ_K_CEN, MDZ_K_VER, MDZ_K_PPN, MDZ_K_PPS };
 size_t mdz_field_count(const mdz_ctx *ctx, int kind);
 mdz_status mdz_ensure_fields(mdz_ctx *ctx);
+mdz_status mdz_upload_fields(mdz_ctx *ctx, const mdz_fields *h, cudaStream_t st);
+mdz_status mdz_download_fields(mdz_ctx *ctx, const mdz_fields *h, const char *const *names, int n, cudaStream_t st);
 
 // device launchers (rheology.cu)
 mdz_status mdz_dev_strain_rates(mdz_ctx *ctx, const mdz_fields &f, cudaStream_t st);

@@ -180,6 +180,7 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     Tii = 2.0 * eta_ve * f_ani * Eii;
     double Txx = Gxx * Tii / f_ani / Eii, Tzz = Gzz * Tii / f_ani / Eii, Txz = Gxz * Tii / f_ani / Eii;
     double Exx_lin = 0, Ezz_lin = 0, Exz_lin = 0, Exx_cst = 0, Ezz_cst = 0, Exz_cst = 0;
+    if (dislocation) eta_pwl = pow(2.0 * C_pwl, -1.0) * pow(Tii, 1.0 - n_pwl);
     if (diffusion) {
         eta_lin = B_lin * pow(Eii_lin, 1.0 / n_lin - 1.0) * pow(o.d1, m_lin / n_lin);
         Exx_lin = Txx / 2.0 / eta_lin; Ezz_lin = Tzz / 2.0 / eta_lin; Exz_lin = Txz / 2.0 / eta_lin;

@@ -262,6 +262,20 @@ class Context:
         s = fields.struct()
         self._check(self.L.mdz_EvaluateRHS(self.h, C.byref(prm), C.c_double(gx), C.c_double(gz), C.byref(s)))
 
+    def EvaluateStokesResidualDecoupled(self, fields):
+        s = fields.struct()
+        norms = np.zeros(3)
+        self._check(self.L.mdz_EvaluateStokesResidualDecoupled(self.h, C.byref(s), _dptr(norms)))
+        return norms
+
+    def StokesOperatorApply(self, fields, jacobian, xu, xv, xp):
+        s = fields.struct()
+        xu, xv, xp = (np.ascontiguousarray(a, np.float64) for a in (xu, xv, xp))
+        yu, yv, yp = np.zeros_like(xu), np.zeros_like(xv), np.zeros_like(xp)
+        self._check(self.L.mdz_StokesOperatorApply(self.h, C.byref(s), C.c_int(jacobian), _dptr(xu), _dptr(xv),
+                                                   _dptr(xp), _dptr(yu), _dptr(yv), _dptr(yp)))
+        return yu, yv, yp
+
 
 # ---- grid fields / rheology structures (mdz_fields, mdz_materials, mdz_rheo_params) ----
 FIELD_NAMES = [

@@ -66,3 +66,17 @@ int orc_rhs(const mdz_grid_desc *g, const mdz_rheo_params *prm, double gx, doubl
 #ifdef __cplusplus
 }
 #endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+/* Decoupled Stokes rows (SOURCE/StokesAssemblyDecoupled.c): y = K x (residual = 0)
+ * or y = K x - b (residual = 1), Picard (jacobian = 0) or Newton (jacobian = 1),
+ * every row times the cell volume; non-equation entries set to 0. */
+int orc_stokes_apply(const mdz_grid_desc *g, const mdz_fields *f, int jacobian, int residual, const double *u,
+                     const double *v, const double *p, double *yu, double *yv, double *yp);
+/* EvaluateStokesResidualDecoupled (SOURCE/StokesRoutines.c:839-920). */
+int orc_residual(const mdz_grid_desc *g, mdz_fields *f, double *norms3);
+#ifdef __cplusplus
+}
+#endif

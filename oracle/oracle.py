@@ -117,3 +117,19 @@ def rheo_operators(grid, prm, fields, jacobian):
 def rhs(grid, prm, gx, gz, fields):
     s = fields.struct()
     lib().orc_rhs(C.byref(grid.desc()), C.byref(prm), C.c_double(gx), C.c_double(gz), C.byref(s))
+
+
+def stokes_apply(grid, fields, jacobian, xu, xv, xp, residual=False):
+    s = fields.struct()
+    xu, xv, xp = (np.ascontiguousarray(a, np.float64) for a in (xu, xv, xp))
+    yu, yv, yp = np.zeros_like(xu), np.zeros_like(xv), np.zeros_like(xp)
+    lib().orc_stokes_apply(C.byref(grid.desc()), C.byref(s), C.c_int(jacobian), C.c_int(int(residual)), _d(xu),
+                           _d(xv), _d(xp), _d(yu), _d(yv), _d(yp))
+    return yu, yv, yp
+
+
+def residual(grid, fields):
+    s = fields.struct()
+    norms = np.zeros(3)
+    lib().orc_residual(C.byref(grid.desc()), C.byref(s), _d(norms))
+    return norms

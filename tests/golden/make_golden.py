@@ -203,6 +203,25 @@ def make_rheology_fixture(avg=0, tag=""):
     for name in ("roger_x", "roger_z", "rhs_p"):
         out["rhs_" + name] = r.field(name).copy()
     out["gz"] = -1.0
+    if avg == 0:
+        # decoupled Stokes: non-linear residual (Picard operator, p_corr) and
+        # the assembled Picard and Newton blocks in the reference's numbering
+        r.rheo_operators(0)
+        norms, Fm, Fc = r.residual()
+        out["st_norms"] = norms
+        for name in ("ru", "rv", "rp"):
+            out["st_" + name] = r.field(name).copy()
+        for w in range(3):
+            out["st_eqn%d" % w] = r.eqn(w)
+        for jac in (0, 1):
+            if jac:
+                r.rheo_operators(1)
+            blocks = r.assemble(jac)
+            for b, M in zip("ABCD", blocks):
+                out["st_J%d_%s_data" % (jac, b)] = M.data
+                out["st_J%d_%s_indices" % (jac, b)] = M.indices
+                out["st_J%d_%s_indptr" % (jac, b)] = M.indptr
+                out["st_J%d_%s_shape" % (jac, b)] = np.array(M.shape)
     np.savez_compressed(os.path.join(HERE, "rheology_ref%s.npz" % tag), **out)
     print("rheology_ref%s.npz: plastic centroids %d / %d" % (tag, (out["vg_eII_pl"] > 0).sum(), out["vg_eII_pl"].size))
 
