@@ -247,6 +247,21 @@ mdz_status mdz_EvaluateStokesResidualDecoupled(mdz_ctx *ctx, mdz_fields *f, doub
 mdz_status mdz_StokesOperatorApply(mdz_ctx *ctx, mdz_fields *f, int jacobian, const double *xu, const double *xv,
                                    const double *xp, double *yu, double *yv, double *yp);
 
+/* Linear defect solve K dx = F, the job of SolveStokesDefectDecoupled ->
+ * KillerSolver (SOURCE/StokesRoutines.c:700-764, SOURCE/Solvers.c:2226-2755),
+ * done matrix-free: GCR preconditioned by a block-triangular operator whose
+ * velocity block is one geometric-multigrid V-cycle on the Picard operator
+ * (eta_n, eta_s) and whose pressure block is eta_n / cell volume.
+ * K = Picard (jacobian = 0) or Newton Jacobian (jacobian = 1) from the
+ * D-tensor in f.  precision 64: plain FP64; 32: FP32 stencils and V-cycles
+ * inside FP64 iterative refinement.  Stops at ||F - K dx|| <= rtol ||F||;
+ * MDZ_ERR_NOT_CONVERGED if maxit Krylov iterations do not reach it.  The
+ * caller applies the update as the reference does: u <- u + alpha dx with
+ * alpha = -1 without line search.  Host buffers in grid layout. */
+mdz_status mdz_SolveStokesDefect(mdz_ctx *ctx, mdz_fields *f, int jacobian, int precision, double rtol, int maxit,
+                                 const double *Fu, const double *Fv, const double *Fp, double *dxu, double *dxv,
+                                 double *dxp, int *iterations, double *rel_residual);
+
 #ifdef __cplusplus
 }
 #endif

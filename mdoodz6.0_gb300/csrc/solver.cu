@@ -1,0 +1,916 @@
+// Linear solver for the decoupled Stokes correction  K dx = F  (K = Picard
+// operator or Newton Jacobian, applied matrix-free): right-preconditioned,
+// restarted GCR with classical Gram-Schmidt applied twice, FP64 dot products
+// (warp-shuffle block reductions), and an upper block-triangular
+// preconditioner [[A, B], [0, S]]:
+//   S^-1 = eta_n / cell volume            (viscosity-scaled pressure mass)
+//   A^-1 = one geometric-multigrid V-cycle on the Picard velocity block
+//          (damped Jacobi smoothing, cell-doubling coarsening, bilinear
+//          prolongation with R = P^T, re-discretised coarse operators, and a
+//          single-CTA Jacobi-PCG solve on the coarsest level).
+// The same code runs in FP64 (plain form) and with FP32 storage and FP32
+// stencil / V-cycle arithmetic (T = float) inside an FP64 defect-correction
+// loop (iterative refinement); all inner products accumulate in FP64.
+//
+// This replaces the reference's CHOLMOD-preconditioned GCR with
+// Powell-Hestenes iterations (KillerSolver, SOURCE/Solvers.c:2226-2755 and
+// kspgcr, SOURCE/Solvers.c:100-228): same defect-correction equation, solved to
+// a relative tolerance, without assembling a matrix.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#include "stokes.cuh"
+#include "solver.cuh"
+
+#define MG_MAX_LEVELS 16
+#define GCR_MAX_M 48
+
+// ---------------------------------------------------------------------------
+template <typename T>
+struct mg_level {
+    int Nx = 0, Nz = 0, ncx = 0, ncz = 0;
+    double dx = 0, dz = 0;
+    signed char *BCu = nullptr, *BCv = nullptr, *BCp = nullptr, *BCg = nullptr;
+    bool own_tags = false;
+    T *D11 = nullptr, *D33 = nullptr;           // Picard: D11 = D22 = 2 eta_n; D33 = eta_s
+    T *xu = nullptr, *xv = nullptr, *yu = nullptr, *yv = nullptr;
+    T *fu = nullptr, *fv = nullptr, *ru = nullptr, *rv = nullptr;
+    T *idu = nullptr, *idv = nullptr;
+    T *cg[8] = {nullptr};                       // coarsest-level CG workspace
+    size_t nu() const { return (size_t)Nx * (Nz + 1); }
+    size_t nv() const { return (size_t)(Nx + 1) * Nz; }
+    stokes_geom geom() const { return stokes_geom{Nx, Nz, ncx, ncz, dx, dz, BCu, BCv, BCp, BCg}; }
+    stokes_coefs<T> coefs() const {
+        return stokes_coefs<T>{D11, nullptr, nullptr, nullptr, nullptr, D11, nullptr, nullptr,
+                               nullptr, nullptr, D33, nullptr};
+    }
+};
+
+template <typename T>
+struct gcr_space {
+    size_t nu = 0, nv = 0, np = 0, n = 0;
+    int m = 0;
+    T *Z = nullptr, *W = nullptr;       // m basis vectors each (u, v, p contiguous)
+    T *x = nullptr, *r = nullptr, *z = nullptr, *w = nullptr, *t = nullptr;
+    const T **dA0 = nullptr, **dA1 = nullptr, **dA2 = nullptr;   // multidot pointer tables
+    double *dots = nullptr;             // device scalars
+    // FP32 copies of the operator (only used for T = float)
+    T *Dc[12] = {nullptr};
+};
+
+template <typename T>
+struct mg_hier {
+    int nlev = 0;
+    mg_level<T> L[MG_MAX_LEVELS];
+};
+
+struct mdz_solver {
+    mg_hier<double> mg64;
+    mg_hier<float> mg32;
+    gcr_space<double> g64;
+    gcr_space<float> g32;
+    double *sc = nullptr;        // host-pinned scalars
+    bool ready = false;
+    int nu1 = 2, nu2 = 2;
+    double omega = 0.7;
+};
+
+// ---------------------------------------------------------------------------
+// Tag rule of the free-slip pure-shear box on any level (the fine level must
+// follow it too): Vx Dirichlet on the W/E lines, free-slip ghosts on the S/N
+// rows; Vz Dirichlet on the S/N lines, ghosts on W/E; everything else inner.
+__global__ void k_level_tags(int Nx, int Nz, signed char *BCu, signed char *BCv, signed char *BCp, signed char *BCg) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int nu = Nx * (Nz + 1), nv = (Nx + 1) * Nz, np = (Nx - 1) * (Nz - 1), ng = Nx * Nz;
+    if (i < nu) {
+        int k = i % Nx, l = i / Nx;
+        signed char t = -1;
+        if (k == 0 || k == Nx - 1) t = 0;
+        if (l == 0 || l == Nz) t = 13;
+        BCu[i] = t;
+    }
+    if (i < nv) {
+        int k = i % (Nx + 1), l = i / (Nx + 1);
+        signed char t = -1;
+        if (l == 0 || l == Nz - 1) t = 0;
+        if (k == 0 || k == Nx) t = 13;
+        BCv[i] = t;
+    }
+    if (i < np) BCp[i] = -1;
+    if (i < ng) BCg[i] = -1;
+}
+
+static bool fine_tags_follow_rule(const mdz_grid_desc &d) {
+    int Nx = d.Nx, Nz = d.Nz;
+    for (int l = 0; l <= Nz; l++)
+        for (int k = 0; k < Nx; k++) {
+            signed char t = -1;
+            if (k == 0 || k == Nx - 1) t = 0;
+            if (l == 0 || l == Nz) t = 13;
+            if (d.BCu_type[k + l * Nx] != t) return false;
+        }
+    for (int l = 0; l < Nz; l++)
+        for (int k = 0; k <= Nx; k++) {
+            signed char t = -1;
+            if (l == 0 || l == Nz - 1) t = 0;
+            if (k == 0 || k == Nx) t = 13;
+            if (d.BCv_type[k + l * (Nx + 1)] != t) return false;
+        }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Multigrid kernels (velocity block, Picard, homogeneous boundaries).
+template <typename T>
+__global__ void k_mg_diag(stokes_geom G, const T *__restrict__ D11, const T *__restrict__ D33, T *__restrict__ idu,
+                          T *__restrict__ idv) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int Nx = G.Nx, Nz = G.Nz, ncx = G.ncx, nu = Nx * (Nz + 1), nv = (Nx + 1) * Nz;
+    const double celvol = G.dx * G.dz, dx2 = G.dx * G.dx, dz2 = G.dz * G.dz;
+    if (i < nu) {
+        int k = i % Nx, l = i / Nx;
+        T d = 0;
+        if (G.BCu[i] == -1) {
+            int c2 = k - 1 + (l - 1) * ncx;
+            double inS = G.BCu[i - Nx] != 13 ? 1.0 : 0.0, inN = G.BCu[i + Nx] != 13 ? 1.0 : 0.0;
+            double a = (inN * (double)D33[i] + inS * (double)D33[i - Nx]) / dz2 +
+                       (2.0 / 3.0) * ((double)D11[c2 + 1] + (double)D11[c2]) / dx2;
+            d = (T)(1.0 / (a * celvol));
+        }
+        idu[i] = d;
+    }
+    if (i < nv) {
+        int k = i % (Nx + 1), l = i / (Nx + 1);
+        T d = 0;
+        if (G.BCv[i] == -1) {
+            int c1 = k + l * Nx, c2 = k - 1 + (l - 1) * ncx;
+            double inW = G.BCv[i - 1] != 13 ? 1.0 : 0.0, inE = G.BCv[i + 1] != 13 ? 1.0 : 0.0;
+            double a = (2.0 / 3.0) * ((double)D11[c2 + ncx] + (double)D11[c2]) / dz2 +
+                       (inE * (double)D33[c1] + inW * (double)D33[c1 - 1]) / dx2;
+            d = (T)(1.0 / (a * celvol));
+        }
+        idv[i] = d;
+    }
+}
+
+// out = x + omega * D^-1 (f - A x)  (x == nullptr: x = 0)
+template <typename T>
+__global__ void __launch_bounds__(256) k_mg_smooth(stokes_geom G, stokes_coefs<T> D, const T *__restrict__ xu,
+                                                   const T *__restrict__ xv, const T *__restrict__ fu,
+                                                   const T *__restrict__ fv, const T *__restrict__ idu,
+                                                   const T *__restrict__ idv, T omega, T *__restrict__ ou,
+                                                   T *__restrict__ ov) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int Nx = G.Nx, Nz = G.Nz;
+    const T celvol = (T)(G.dx * G.dz);
+    stokes_cvec<T> x{xu, xv, nullptr};
+    if (i < Nx && j <= Nz) {
+        int c = i + j * Nx;
+        T r = 0;
+        if (G.BCu[c] == -1) {
+            T ax = xu ? xrow<T, false>(G, D, x, i, j) * celvol : T(0);
+            r = (xu ? xu[c] : T(0)) + omega * idu[c] * (fu[c] - ax);
+        }
+        ou[c] = r;
+    }
+    if (i <= Nx && j < Nz) {
+        int c = i + j * (Nx + 1);
+        T r = 0;
+        if (G.BCv[c] == -1) {
+            T ax = xv ? zrow<T, false>(G, D, x, i, j) * celvol : T(0);
+            r = (xv ? xv[c] : T(0)) + omega * idv[c] * (fv[c] - ax);
+        }
+        ov[c] = r;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_mg_residual(stokes_geom G, stokes_coefs<T> D, const T *__restrict__ xu,
+                                                     const T *__restrict__ xv, const T *__restrict__ fu,
+                                                     const T *__restrict__ fv, T *__restrict__ ru,
+                                                     T *__restrict__ rv) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int Nx = G.Nx, Nz = G.Nz;
+    const T celvol = (T)(G.dx * G.dz);
+    stokes_cvec<T> x{xu, xv, nullptr};
+    if (i < Nx && j <= Nz) {
+        int c = i + j * Nx;
+        ru[c] = G.BCu[c] == -1 ? fu[c] - xrow<T, false>(G, D, x, i, j) * celvol : T(0);
+    }
+    if (i <= Nx && j < Nz) {
+        int c = i + j * (Nx + 1);
+        rv[c] = G.BCv[c] == -1 ? fv[c] - zrow<T, false>(G, D, x, i, j) * celvol : T(0);
+    }
+}
+
+// Prolongation weights along the "cell-centred" direction of a staggered
+// component: fine line j (1..ncf) -> main coarse line and neighbour, with the
+// ghost neighbour mirrored onto the main line (free slip).
+__device__ __forceinline__ void cc_weights(int j, int ncc, int &J0, float &w0, int &J1, float &w1) {
+    int r = j - 1, R = r >> 1;
+    J0 = R + 1;
+    J1 = (r & 1) ? J0 + 1 : J0 - 1;
+    w0 = 0.75f; w1 = 0.25f;
+    if (J1 < 1 || J1 > ncc) { w0 = 1.0f; w1 = 0.0f; J1 = J0; }
+}
+
+// Weight of coarse vertex line I for fine vertex line i (node-centred direction).
+__device__ __forceinline__ float nc_weight(int i, int I) {
+    if ((i & 1) == 0) return i == 2 * I ? 1.0f : 0.0f;
+    return (i == 2 * I - 1 || i == 2 * I + 1) ? 0.5f : 0.0f;
+}
+
+// fine x += P xc   (both components)
+template <typename T>
+__global__ void k_mg_prolong_add(stokes_geom F, stokes_geom Cg, const T *__restrict__ cu, const T *__restrict__ cv,
+                                 T *__restrict__ fu, T *__restrict__ fv) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int Nx = F.Nx, Nz = F.Nz, Nxc = Cg.Nx;
+    if (i < Nx && j <= Nz) {   // Vx: x node-centred, z cell-centred
+        int c = i + j * Nx;
+        if (F.BCu[c] == -1) {
+            int J0, J1;
+            float w0, w1;
+            cc_weights(j, Cg.ncz, J0, w0, J1, w1);
+            int Ia = i >> 1, Ib = (i + 1) >> 1;
+            float wa = (i & 1) ? 0.5f : 1.0f, wb = (i & 1) ? 0.5f : 0.0f;
+            T s = (T)(wa * w0) * cu[Ia + J0 * Nxc] + (T)(wa * w1) * cu[Ia + J1 * Nxc];
+            if (wb != 0.0f) s += (T)(wb * w0) * cu[Ib + J0 * Nxc] + (T)(wb * w1) * cu[Ib + J1 * Nxc];
+            fu[c] += s;
+        }
+    }
+    if (i <= Nx && j < Nz) {   // Vz: x cell-centred, z node-centred
+        int c = i + j * (Nx + 1);
+        if (F.BCv[c] == -1) {
+            int I0, I1;
+            float w0, w1;
+            cc_weights(i, Cg.ncx, I0, w0, I1, w1);
+            int Ja = j >> 1, Jb = (j + 1) >> 1;
+            float wa = (j & 1) ? 0.5f : 1.0f, wb = (j & 1) ? 0.5f : 0.0f;
+            const int W = Nxc + 1;
+            T s = (T)(wa * w0) * cv[I0 + Ja * W] + (T)(wa * w1) * cv[I1 + Ja * W];
+            if (wb != 0.0f) s += (T)(wb * w0) * cv[I0 + Jb * W] + (T)(wb * w1) * cv[I1 + Jb * W];
+            fv[c] += s;
+        }
+    }
+}
+
+// coarse f = P^T fine r
+template <typename T>
+__global__ void k_mg_restrict(stokes_geom F, stokes_geom Cg, const T *__restrict__ ru, const T *__restrict__ rv,
+                              T *__restrict__ cu, T *__restrict__ cv) {
+    int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y * blockDim.y + threadIdx.y;
+    const int Nxf = F.Nx, Nzf = F.Nz, Nx = Cg.Nx, Nz = Cg.Nz;
+    if (I < Nx && J <= Nz) {
+        int c = I + J * Nx;
+        T s = 0;
+        if (Cg.BCu[c] == -1) {
+            for (int j = 2 * J - 2; j <= 2 * J + 1; j++) {
+                if (j < 1 || j > F.ncz) continue;
+                int J0, J1;
+                float w0, w1;
+                cc_weights(j, Cg.ncz, J0, w0, J1, w1);
+                float wz = (J0 == J ? w0 : 0.0f) + (J1 == J && J1 != J0 ? w1 : 0.0f);
+                if (wz == 0.0f) continue;
+                for (int i = 2 * I - 1; i <= 2 * I + 1; i++) {
+                    if (i < 0 || i >= Nxf) continue;
+                    float wx = nc_weight(i, I);
+                    if (wx == 0.0f) continue;
+                    int fcidx = i + j * Nxf;
+                    if (F.BCu[fcidx] == -1) s += (T)(wx * wz) * ru[fcidx];
+                }
+            }
+        }
+        cu[c] = s;
+    }
+    if (I <= Nx && J < Nz) {
+        int c = I + J * (Nx + 1);
+        T s = 0;
+        if (Cg.BCv[c] == -1) {
+            for (int i = 2 * I - 2; i <= 2 * I + 1; i++) {
+                if (i < 1 || i > F.ncx) continue;
+                int I0, I1;
+                float w0, w1;
+                cc_weights(i, Cg.ncx, I0, w0, I1, w1);
+                float wx = (I0 == I ? w0 : 0.0f) + (I1 == I && I1 != I0 ? w1 : 0.0f);
+                if (wx == 0.0f) continue;
+                for (int j = 2 * J - 1; j <= 2 * J + 1; j++) {
+                    if (j < 0 || j >= Nzf) continue;
+                    float wz = nc_weight(j, J);
+                    if (wz == 0.0f) continue;
+                    int fcidx = i + j * (Nxf + 1);
+                    if (F.BCv[fcidx] == -1) s += (T)(wx * wz) * rv[fcidx];
+                }
+            }
+        }
+        cv[c] = s;
+    }
+}
+
+// coarse coefficients: centroid average of the 4 children, vertex injection
+template <typename T>
+__global__ void k_mg_coarsen(int ncxf, int Nxf, int ncxc, int nczc, int Nxc, int Nzc, const T *__restrict__ D11f,
+                             const T *__restrict__ D33f, T *__restrict__ D11c, T *__restrict__ D33c) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < ncxc * nczc) {
+        int I = i % ncxc, J = i / ncxc, a = 2 * I + 2 * J * ncxf;
+        D11c[i] = (T)0.25 * (D11f[a] + D11f[a + 1] + D11f[a + ncxf] + D11f[a + ncxf + 1]);
+    }
+    if (i < Nxc * Nzc) {
+        int I = i % Nxc, J = i / Nxc;
+        D33c[i] = D33f[2 * I + 2 * J * Nxf];
+    }
+}
+
+template <typename T>
+__global__ void k_fill_D11_D33(int nc, int nv, const double *__restrict__ eta_n, const double *__restrict__ eta_s,
+                               T *__restrict__ D11, T *__restrict__ D33) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nc) D11[i] = (T)(2.0 * eta_n[i]);
+    if (i < nv) D33[i] = (T)eta_s[i];
+}
+
+// ---------------------------------------------------------------------------
+// Coarsest level: one CTA runs Jacobi-preconditioned CG on the whole level.
+template <typename T>
+__device__ double cta_dot(const T *a, const T *b, int n0, int n1, const T *a1, const T *b1, double *sh) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n0; i += blockDim.x) s += (double)a[i] * (double)b[i];
+    for (int i = threadIdx.x; i < n1; i += blockDim.x) s += (double)a1[i] * (double)b1[i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = s;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) sh[32] = t;
+    }
+    __syncthreads();
+    return sh[32];
+}
+
+template <typename T>
+__device__ void cta_apply(const stokes_geom &G, const stokes_coefs<T> &D, const T *xu, const T *xv, T *yu, T *yv) {
+    const int Nx = G.Nx, Nz = G.Nz;
+    const T celvol = (T)(G.dx * G.dz);
+    stokes_cvec<T> x{xu, xv, nullptr};
+    for (int c = threadIdx.x; c < Nx * (Nz + 1); c += blockDim.x)
+        yu[c] = G.BCu[c] == -1 ? xrow<T, false>(G, D, x, c % Nx, c / Nx) * celvol : T(0);
+    for (int c = threadIdx.x; c < (Nx + 1) * Nz; c += blockDim.x)
+        yv[c] = G.BCv[c] == -1 ? zrow<T, false>(G, D, x, c % (Nx + 1), c / (Nx + 1)) * celvol : T(0);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) k_mg_coarse_cg(stokes_geom G, stokes_coefs<T> D, const T *__restrict__ fu,
+                                                       const T *__restrict__ fv, const T *__restrict__ idu,
+                                                       const T *__restrict__ idv, T *xu, T *xv, T *ru, T *rv, T *zu,
+                                                       T *zv, T *pu, T *pv, T *qu, T *qv, int maxit, double rtol) {
+    __shared__ double sh[34];
+    const int nu = G.Nx * (G.Nz + 1), nv = (G.Nx + 1) * G.Nz;
+    for (int i = threadIdx.x; i < nu; i += blockDim.x) { xu[i] = 0; ru[i] = fu[i]; zu[i] = idu[i] * fu[i]; pu[i] = zu[i]; }
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) { xv[i] = 0; rv[i] = fv[i]; zv[i] = idv[i] * fv[i]; pv[i] = zv[i]; }
+    __syncthreads();
+    double rz = cta_dot<T>(ru, zu, nu, nv, rv, zv, sh);
+    double r0 = cta_dot<T>(ru, ru, nu, nv, rv, rv, sh);
+    if (r0 == 0.0) return;
+    for (int it = 0; it < maxit; it++) {
+        cta_apply<T>(G, D, pu, pv, qu, qv);
+        __syncthreads();
+        double pq = cta_dot<T>(pu, qu, nu, nv, pv, qv, sh);
+        if (pq <= 0.0) break;
+        T a = (T)(rz / pq);
+        for (int i = threadIdx.x; i < nu; i += blockDim.x) { xu[i] += a * pu[i]; ru[i] -= a * qu[i]; zu[i] = idu[i] * ru[i]; }
+        for (int i = threadIdx.x; i < nv; i += blockDim.x) { xv[i] += a * pv[i]; rv[i] -= a * qv[i]; zv[i] = idv[i] * rv[i]; }
+        __syncthreads();
+        double rz1 = cta_dot<T>(ru, zu, nu, nv, rv, zv, sh);
+        double rr = cta_dot<T>(ru, ru, nu, nv, rv, rv, sh);
+        if (rr <= rtol * rtol * r0) break;
+        T b = (T)(rz1 / rz);
+        rz = rz1;
+        for (int i = threadIdx.x; i < nu; i += blockDim.x) pu[i] = zu[i] + b * pu[i];
+        for (int i = threadIdx.x; i < nv; i += blockDim.x) pv[i] = zv[i] + b * pv[i];
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+template <typename T>
+static cudaError_t alloc0(T **p, size_t n) {
+    cudaError_t e = cudaMalloc((void **)p, sizeof(T) * (n ? n : 1));
+    if (e == cudaSuccess) e = cudaMemset(*p, 0, sizeof(T) * (n ? n : 1));
+    return e;
+}
+
+template <typename T>
+static mdz_status build_hierarchy(mdz_ctx *ctx, mg_hier<T> &H) {
+    const mdz_dgrid &g = ctx->g;
+    int Nx = g.Nx, Nz = g.Nz;
+    double dx = g.dx, dz = g.dz;
+    cudaError_t e = cudaSuccess;
+    int lev = 0;
+    while (lev < MG_MAX_LEVELS) {
+        mg_level<T> &L = H.L[lev];
+        L.Nx = Nx; L.Nz = Nz; L.ncx = Nx - 1; L.ncz = Nz - 1; L.dx = dx; L.dz = dz;
+        if (lev == 0) {
+            L.BCu = g.BCu; L.BCv = g.BCv; L.BCp = g.BCp; L.BCg = g.BCg; L.own_tags = false;
+        } else {
+            L.own_tags = true;
+            if (e == cudaSuccess) e = alloc0(&L.BCu, L.nu());
+            if (e == cudaSuccess) e = alloc0(&L.BCv, L.nv());
+            if (e == cudaSuccess) e = alloc0(&L.BCp, (size_t)L.ncx * L.ncz);
+            if (e == cudaSuccess) e = alloc0(&L.BCg, (size_t)Nx * Nz);
+            if (e == cudaSuccess) {
+                k_level_tags<<<mdz_blocks((size_t)(Nx + 1) * (Nz + 1)), MDZ_THREADS>>>(Nx, Nz, L.BCu, L.BCv, L.BCp, L.BCg);
+                e = cudaGetLastError();
+            }
+        }
+        if (e == cudaSuccess) e = alloc0(&L.D11, (size_t)L.ncx * L.ncz);
+        if (e == cudaSuccess) e = alloc0(&L.D33, (size_t)Nx * Nz);
+        T **bufs[] = {&L.xu, &L.yu, &L.fu, &L.ru, &L.idu};
+        for (T **b : bufs) if (e == cudaSuccess) e = alloc0(b, L.nu());
+        T **bufv[] = {&L.xv, &L.yv, &L.fv, &L.rv, &L.idv};
+        for (T **b : bufv) if (e == cudaSuccess) e = alloc0(b, L.nv());
+        lev++;
+        bool can = (L.ncx % 2 == 0) && (L.ncz % 2 == 0) && L.ncx >= 8 && L.ncz >= 8 &&
+                   (size_t)L.ncx * L.ncz > 64;
+        if (!can) break;
+        Nx = L.ncx / 2 + 1; Nz = L.ncz / 2 + 1; dx *= 2; dz *= 2;
+    }
+    H.nlev = lev;
+    mg_level<T> &C = H.L[lev - 1];
+    for (int q = 0; q < 4; q++) {
+        if (e == cudaSuccess) e = alloc0(&C.cg[2 * q], C.nu());
+        if (e == cudaSuccess) e = alloc0(&C.cg[2 * q + 1], C.nv());
+    }
+    if (e != cudaSuccess) return mdz_cuda_check(ctx, e, "multigrid allocation");
+    return MDZ_OK;
+}
+
+template <typename T>
+static void free_hierarchy(mg_hier<T> &H) {
+    for (int l = 0; l < H.nlev; l++) {
+        mg_level<T> &L = H.L[l];
+        if (L.own_tags) { cudaFree(L.BCu); cudaFree(L.BCv); cudaFree(L.BCp); cudaFree(L.BCg); }
+        void *p[] = {L.D11, L.D33, L.xu, L.xv, L.yu, L.yv, L.fu, L.fv, L.ru, L.rv, L.idu, L.idv,
+                     L.cg[0], L.cg[1], L.cg[2], L.cg[3], L.cg[4], L.cg[5], L.cg[6], L.cg[7]};
+        for (void *q : p) if (q) cudaFree(q);
+    }
+    H.nlev = 0;
+}
+
+template <typename T>
+static mdz_status alloc_gcr(mdz_ctx *ctx, gcr_space<T> &S, int m) {
+    const mdz_dgrid &g = ctx->g;
+    S.nu = (size_t)g.Nx * (g.Nz + 1); S.nv = (size_t)(g.Nx + 1) * g.Nz; S.np = (size_t)g.ncx * g.ncz;
+    S.n = S.nu + S.nv + S.np;
+    S.m = m;
+    cudaError_t e = alloc0(&S.Z, S.n * m);
+    if (e == cudaSuccess) e = alloc0(&S.W, S.n * m);
+    T **v[] = {&S.x, &S.r, &S.z, &S.w, &S.t};
+    for (T **b : v) if (e == cudaSuccess) e = alloc0(b, S.n);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&S.dA0, sizeof(T *) * (GCR_MAX_M + 4));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&S.dA1, sizeof(T *) * (GCR_MAX_M + 4));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&S.dA2, sizeof(T *) * (GCR_MAX_M + 4));
+    if (e == cudaSuccess) e = alloc0(&S.dots, 4 * (GCR_MAX_M + 8));
+    if (e != cudaSuccess) return mdz_cuda_check(ctx, e, "GCR allocation");
+    // pointer tables: rows 0..m-1 = W_i, row m = w, row m+1 = r
+    std::vector<const T *> a0(m + 2), a1(m + 2), a2(m + 2);
+    for (int i = 0; i < m + 2; i++) {
+        const T *base = i < m ? S.W + S.n * i : (i == m ? S.w : S.r);
+        a0[i] = base; a1[i] = base + S.nu; a2[i] = base + S.nu + S.nv;
+    }
+    cudaMemcpy(S.dA0, a0.data(), sizeof(T *) * (m + 2), cudaMemcpyHostToDevice);
+    cudaMemcpy(S.dA1, a1.data(), sizeof(T *) * (m + 2), cudaMemcpyHostToDevice);
+    cudaMemcpy(S.dA2, a2.data(), sizeof(T *) * (m + 2), cudaMemcpyHostToDevice);
+    if (sizeof(T) == 4) {
+        for (int q = 0; q < 12; q++) {
+            size_t n = (q < 8) ? S.np : (size_t)g.Nx * g.Nz;
+            if (alloc0(&S.Dc[q], n) != cudaSuccess) return mdz_cuda_check(ctx, cudaGetLastError(), "GCR allocation");
+        }
+    }
+    return MDZ_OK;
+}
+
+template <typename T>
+static void free_gcr(gcr_space<T> &S) {
+    void *p[] = {S.Z, S.W, S.x, S.r, S.z, S.w, S.t, S.dA0, S.dA1, S.dA2, S.dots};
+    for (void *q : p) if (q) cudaFree(q);
+    for (int q = 0; q < 12; q++) if (S.Dc[q]) cudaFree(S.Dc[q]);
+}
+
+mdz_status mdz_solver_ensure(mdz_ctx *ctx) {
+    if (ctx->solver && ctx->solver->ready) return MDZ_OK;
+    mdz_status s = mdz_check_stokes_bcs(ctx);
+    if (s != MDZ_OK) return s;
+    if (!fine_tags_follow_rule(ctx->host_desc))
+        return mdz_fail(ctx, MDZ_ERR_UNSUPPORTED, "solver: boundary tags must be the free-slip box pattern");
+    if (!ctx->solver) ctx->solver = new mdz_solver();
+    mdz_solver *S = ctx->solver;
+    if ((s = build_hierarchy<double>(ctx, S->mg64)) != MDZ_OK) return s;
+    if ((s = build_hierarchy<float>(ctx, S->mg32)) != MDZ_OK) return s;
+    if ((s = alloc_gcr<double>(ctx, S->g64, 30)) != MDZ_OK) return s;
+    if ((s = alloc_gcr<float>(ctx, S->g32, 30)) != MDZ_OK) return s;
+    MDZ_CUDA(ctx, cudaMallocHost((void **)&S->sc, 64 * sizeof(double)));
+    MDZ_CUDA(ctx, cudaDeviceSynchronize());
+    S->ready = true;
+    return MDZ_OK;
+}
+
+void mdz_solver_free(mdz_ctx *ctx) {
+    if (!ctx->solver) return;
+    mdz_solver *S = ctx->solver;
+    free_hierarchy(S->mg64);
+    free_hierarchy(S->mg32);
+    free_gcr(S->g64);
+    free_gcr(S->g32);
+    if (S->sc) cudaFreeHost(S->sc);
+    delete S;
+    ctx->solver = nullptr;
+}
+
+int mdz_solver_levels(const mdz_ctx *ctx) { return ctx->solver ? ctx->solver->mg64.nlev : 0; }
+
+// ---------------------------------------------------------------------------
+// Multigrid setup (coefficients) and V-cycle.
+template <typename T>
+static mdz_status mg_setup(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n, const double *eta_s, cudaStream_t st) {
+    mg_level<T> &F = H.L[0];
+    int nc = F.ncx * F.ncz, nv = F.Nx * F.Nz;
+    k_fill_D11_D33<T><<<mdz_blocks(nv > nc ? nv : nc), MDZ_THREADS, 0, st>>>(nc, nv, eta_n, eta_s, F.D11, F.D33);
+    MDZ_LAUNCHED(ctx);
+    for (int l = 0; l < H.nlev; l++) {
+        mg_level<T> &L = H.L[l];
+        if (l > 0) {
+            mg_level<T> &P = H.L[l - 1];
+            int n = L.Nx * L.Nz;
+            k_mg_coarsen<T><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(P.ncx, P.Nx, L.ncx, L.ncz, L.Nx, L.Nz, P.D11, P.D33,
+                                                                     L.D11, L.D33);
+            MDZ_LAUNCHED(ctx);
+        }
+        size_t n = L.nu() > L.nv() ? L.nu() : L.nv();
+        k_mg_diag<T><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(L.geom(), L.D11, L.D33, L.idu, L.idv);
+        MDZ_LAUNCHED(ctx);
+    }
+    return MDZ_OK;
+}
+
+static inline dim3 box_grid(int Nx, int Nz) { return dim3((Nx + 1 + 31) / 32, (Nz + 1 + 7) / 8); }
+
+// One V-cycle: H.L[l].x <- approx A^-1 H.L[l].f
+template <typename T>
+static mdz_status vcycle(mdz_ctx *ctx, mg_hier<T> &H, int l, int nu1, int nu2, T omega, cudaStream_t st) {
+    mg_level<T> &L = H.L[l];
+    stokes_geom G = L.geom();
+    stokes_coefs<T> D = L.coefs();
+    dim3 bl(32, 8), gr = box_grid(L.Nx, L.Nz);
+    if (l == H.nlev - 1) {
+        int maxit = 4 * (L.ncx > L.ncz ? L.ncx : L.ncz) + 50;
+        k_mg_coarse_cg<T><<<1, 1024, 0, st>>>(G, D, L.fu, L.fv, L.idu, L.idv, L.xu, L.xv, L.ru, L.rv, L.cg[0],
+                                              L.cg[1], L.cg[2], L.cg[3], L.cg[4], L.cg[5], maxit, 1e-6);
+        MDZ_LAUNCHED(ctx);
+        return MDZ_OK;
+    }
+    // pre-smoothing from x = 0
+    k_mg_smooth<T><<<gr, bl, 0, st>>>(G, D, nullptr, nullptr, L.fu, L.fv, L.idu, L.idv, omega, L.xu, L.xv);
+    MDZ_LAUNCHED(ctx);
+    for (int s = 1; s < nu1; s++) {
+        k_mg_smooth<T><<<gr, bl, 0, st>>>(G, D, L.xu, L.xv, L.fu, L.fv, L.idu, L.idv, omega, L.yu, L.yv);
+        MDZ_LAUNCHED(ctx);
+        std::swap(L.xu, L.yu); std::swap(L.xv, L.yv);
+    }
+    k_mg_residual<T><<<gr, bl, 0, st>>>(G, D, L.xu, L.xv, L.fu, L.fv, L.ru, L.rv);
+    MDZ_LAUNCHED(ctx);
+    mg_level<T> &C = H.L[l + 1];
+    k_mg_restrict<T><<<box_grid(C.Nx, C.Nz), bl, 0, st>>>(G, C.geom(), L.ru, L.rv, C.fu, C.fv);
+    MDZ_LAUNCHED(ctx);
+    mdz_status s = vcycle<T>(ctx, H, l + 1, nu1, nu2, omega, st);
+    if (s != MDZ_OK) return s;
+    k_mg_prolong_add<T><<<gr, bl, 0, st>>>(G, C.geom(), C.xu, C.xv, L.xu, L.xv);
+    MDZ_LAUNCHED(ctx);
+    for (int q = 0; q < nu2; q++) {
+        k_mg_smooth<T><<<gr, bl, 0, st>>>(G, D, L.xu, L.xv, L.fu, L.fv, L.idu, L.idv, omega, L.yu, L.yv);
+        MDZ_LAUNCHED(ctx);
+        std::swap(L.xu, L.yu); std::swap(L.xv, L.yv);
+    }
+    return MDZ_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Block preconditioner: zp = (eta_n / celvol) rp ; zu = V-cycle(ru - B zp).
+template <typename T>
+__global__ void k_precond_p(stokes_geom G, const double *__restrict__ eta_n, const T *__restrict__ rp,
+                            T *__restrict__ zp) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= G.ncx * G.ncz) return;
+    zp[i] = G.BCp[i] == -1 ? (T)(eta_n[i] / (G.dx * G.dz)) * rp[i] : T(0);
+}
+
+// f = r_vel - B zp  on the fine MG level (B: celvol-scaled pressure gradient)
+template <typename T>
+__global__ void k_precond_rhs(stokes_geom G, const T *__restrict__ ru, const T *__restrict__ rv,
+                              const T *__restrict__ zp, T *__restrict__ fu, T *__restrict__ fv) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int Nx = G.Nx, Nz = G.Nz, ncx = G.ncx;
+    if (i < Nx && j <= Nz) {
+        int c = i + j * Nx;
+        T r = 0;
+        if (G.BCu[c] == -1) {
+            int c2 = i - 1 + (j - 1) * ncx;
+            r = ru[c] - (T)G.dz * (zp[c2 + 1] - zp[c2]);
+        }
+        fu[c] = r;
+    }
+    if (i <= Nx && j < Nz) {
+        int c = i + j * (Nx + 1);
+        T r = 0;
+        if (G.BCv[c] == -1) {
+            int c2 = i - 1 + (j - 1) * ncx;
+            r = rv[c] - (T)G.dx * (zp[c2 + ncx] - zp[c2]);
+        }
+        fv[c] = r;
+    }
+}
+
+template <typename T>
+__global__ void k_copy_vel(size_t nu, size_t nv, const T *__restrict__ xu, const T *__restrict__ xv,
+                           T *__restrict__ zu, T *__restrict__ zv) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nu) zu[i] = xu[i];
+    if (i < nv) zv[i] = xv[i];
+}
+
+template <typename T>
+static mdz_status precondition(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n, const T *r, T *z, size_t nu,
+                               size_t nv, cudaStream_t st) {
+    mg_level<T> &F = H.L[0];
+    stokes_geom G = F.geom();
+    k_precond_p<T><<<mdz_blocks(F.ncx * F.ncz), MDZ_THREADS, 0, st>>>(G, eta_n, r + nu + nv, z + nu + nv);
+    MDZ_LAUNCHED(ctx);
+    k_precond_rhs<T><<<box_grid(F.Nx, F.Nz), dim3(32, 8), 0, st>>>(G, r, r + nu, z + nu + nv, F.fu, F.fv);
+    MDZ_LAUNCHED(ctx);
+    mdz_solver *S = ctx->solver;
+    mdz_status s = vcycle<T>(ctx, H, 0, S->nu1, S->nu2, (T)S->omega, st);
+    if (s != MDZ_OK) return s;
+    size_t n = nu > nv ? nu : nv;
+    k_copy_vel<T><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(nu, nv, F.xu, F.xv, z, z + nu);
+    MDZ_LAUNCHED(ctx);
+    return MDZ_OK;
+}
+
+// ---------------------------------------------------------------------------
+// GCR kernels (vectors are u|v|p contiguous of length n).
+template <typename T>
+__global__ void k_gcr_orth(size_t n, int k, const T *__restrict__ Z, const T *__restrict__ W,
+                           const double *__restrict__ beta, T *__restrict__ z, T *__restrict__ w) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double zs = z[i], ws = w[i];
+    for (int q = 0; q < k; q++) {
+        double b = beta[q];
+        zs -= b * (double)Z[q * n + i];
+        ws -= b * (double)W[q * n + i];
+    }
+    z[i] = (T)zs;
+    w[i] = (T)ws;
+}
+
+// second Gram-Schmidt pass, normalisation, store into slot k, update x and r.
+// dots[0..k-1] = (w, W_q), dots[k] = (w, w), dots[k+1] = (w, r)
+__global__ void k_gcr_scalars(int k, double *dots, double *out3) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double nrm2 = dots[k], wr = dots[k + 1];
+    for (int q = 0; q < k; q++) nrm2 -= dots[q] * dots[q];
+    double nrm = sqrt(nrm2 > 0 ? nrm2 : 0.0);
+    out3[0] = nrm > 0 ? 1.0 / nrm : 0.0;
+    out3[1] = nrm > 0 ? wr / nrm : 0.0;      // alpha = (r, w_hat); r is orthogonal to W_q, q < k
+    out3[2] = nrm2;
+}
+
+template <typename T>
+__global__ void k_gcr_finish(size_t n, int k, T *__restrict__ Z, T *__restrict__ W, const double *__restrict__ beta,
+                             const double *__restrict__ sc, const T *__restrict__ z, const T *__restrict__ w,
+                             T *__restrict__ x, T *__restrict__ r) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double zs = z[i], ws = w[i];
+    for (int q = 0; q < k; q++) {
+        double b = beta[q];
+        zs -= b * (double)Z[q * n + i];
+        ws -= b * (double)W[q * n + i];
+    }
+    double inv = sc[0], alpha = sc[1];
+    zs *= inv;
+    ws *= inv;
+    Z[(size_t)k * n + i] = (T)zs;
+    W[(size_t)k * n + i] = (T)ws;
+    x[i] = (T)((double)x[i] + alpha * zs);
+    r[i] = (T)((double)r[i] - alpha * ws);
+}
+
+template <typename T>
+__global__ void k_axpby(size_t n, double a, const T *__restrict__ x, double b, T *__restrict__ y) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = (T)(a * (double)x[i] + b * (double)y[i]);
+}
+
+template <typename Tin, typename Tout>
+__global__ void k_convert(size_t n, const Tin *__restrict__ a, Tout *__restrict__ b) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (Tout)a[i];
+}
+
+// dx(FP64) += e(FP32)
+__global__ void k_add_f32(size_t n, const float *__restrict__ e, double *__restrict__ x) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] += (double)e[i];
+}
+
+template <typename T>
+static mdz_status dots_launch(mdz_ctx *ctx, gcr_space<T> &S, int q0, int nq, const T *b, double *out,
+                              cudaStream_t st) {
+    if (nq <= 0) return MDZ_OK;
+    MDZ_CUDA(ctx, cudaMemsetAsync(out, 0, sizeof(double) * nq, st));
+    multidot_launch<T>(nq, (int)S.nu, (int)S.nv, (int)S.np, S.dA0 + q0, S.dA1 + q0, S.dA2 + q0, b, b + S.nu,
+                       b + S.nu + S.nv, out, st);
+    MDZ_LAUNCHED(ctx);
+    return MDZ_OK;
+}
+
+// ---------------------------------------------------------------------------
+// GCR on K x = b (x0 = 0), right-preconditioned; T-precision operator.
+template <typename T>
+static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, mg_hier<T> &H, const stokes_coefs<T> &K, bool newton,
+                            const double *eta_n, double rtol, int maxit, int *its_out, double *rel_out,
+                            cudaStream_t st) {
+    mdz_solver *SV = ctx->solver;
+    stokes_geom G = mdz_stokes_geom(ctx);
+    const size_t n = S.n, nu = S.nu, nv = S.nv;
+    int nb = mdz_blocks(n);
+    MDZ_CUDA(ctx, cudaMemsetAsync(S.x, 0, sizeof(T) * n, st));
+    // ||r0||
+    double *dots = S.dots, *sc = S.dots + (GCR_MAX_M + 4);
+    mdz_status s;
+    // (r, r) via the pointer-table slot m+1 against r itself
+    if ((s = dots_launch<T>(ctx, S, S.m + 1, 1, S.r, dots, st)) != MDZ_OK) return s;
+    MDZ_CUDA(ctx, cudaMemcpyAsync(SV->sc, dots, sizeof(double), cudaMemcpyDeviceToHost, st));
+    MDZ_CUDA(ctx, cudaStreamSynchronize(st));
+    double rn2 = SV->sc[0], rn02 = rn2;
+    int it = 0;
+    if (rn02 == 0.0) { if (its_out) *its_out = 0; if (rel_out) *rel_out = 0.0; return MDZ_OK; }
+    int k = 0;
+    for (it = 0; it < maxit; it++) {
+        if (k == S.m) k = 0;   // restart: keep x and r, drop the basis
+        if ((s = precondition<T>(ctx, H, eta_n, S.r, S.z, nu, nv, st)) != MDZ_OK) return s;
+        stokes_apply_launch<T>(G, K, stokes_cvec<T>{S.z, S.z + nu, S.z + nu + nv},
+                               stokes_vec<T>{S.w, S.w + nu, S.w + nu + nv}, nullptr, newton, st);
+        MDZ_LAUNCHED(ctx);
+        if (k > 0) {   // first Gram-Schmidt pass
+            if ((s = dots_launch<T>(ctx, S, 0, k, S.w, dots, st)) != MDZ_OK) return s;
+            k_gcr_orth<T><<<nb, MDZ_THREADS, 0, st>>>(n, k, S.Z, S.W, dots, S.z, S.w);
+            MDZ_LAUNCHED(ctx);
+        }
+        // second pass dots: (w, W_q) q<k, (w, w), (w, r)
+        if ((s = dots_launch<T>(ctx, S, 0, k, S.w, dots, st)) != MDZ_OK) return s;
+        if ((s = dots_launch<T>(ctx, S, S.m, 2, S.w, dots + k, st)) != MDZ_OK) return s;
+        k_gcr_scalars<<<1, 32, 0, st>>>(k, dots, sc);
+        MDZ_LAUNCHED(ctx);
+        k_gcr_finish<T><<<nb, MDZ_THREADS, 0, st>>>(n, k, S.Z, S.W, dots, sc, S.z, S.w, S.x, S.r);
+        MDZ_LAUNCHED(ctx);
+        MDZ_CUDA(ctx, cudaMemcpyAsync(SV->sc, sc, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        MDZ_CUDA(ctx, cudaStreamSynchronize(st));
+        double alpha = SV->sc[1];
+        rn2 -= alpha * alpha;
+        k++;
+        if (!std::isfinite(alpha)) return mdz_fail(ctx, MDZ_ERR_NAN, "GCR: NaN in the Krylov iteration");
+        if (rn2 <= rtol * rtol * rn02 || (k == S.m)) {
+            // recompute the true norm of r at convergence and at each restart
+            if ((s = dots_launch<T>(ctx, S, S.m + 1, 1, S.r, dots, st)) != MDZ_OK) return s;
+            MDZ_CUDA(ctx, cudaMemcpyAsync(SV->sc, dots, sizeof(double), cudaMemcpyDeviceToHost, st));
+            MDZ_CUDA(ctx, cudaStreamSynchronize(st));
+            rn2 = SV->sc[0];
+            if (rn2 <= rtol * rtol * rn02) { it++; break; }
+        }
+    }
+    if (its_out) *its_out = it;
+    if (rel_out) *rel_out = sqrt(rn2 > 0 ? rn2 : 0.0) / sqrt(rn02);
+    return MDZ_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Public device-level solve: K dx = F.  F and dx in grid layout (u | v | p
+// contiguous, length n), FP64.  precision 64: plain FP64 GCR + FP64 V-cycle;
+// precision 32: FP64 defect correction around FP32 GCR + FP32 V-cycle.
+mdz_status mdz_dev_solve(mdz_ctx *ctx, const mdz_fields &f, bool newton, int precision, double rtol, int maxit,
+                         const double *F, double *dx, mdz_solve_stats *stats, cudaStream_t st) {
+    mdz_status s = mdz_solver_ensure(ctx);
+    if (s != MDZ_OK) return s;
+    mdz_solver *SV = ctx->solver;
+    gcr_space<double> &S64 = SV->g64;
+    const size_t n = S64.n, nu = S64.nu, nv = S64.nv;
+    stokes_geom G = mdz_stokes_geom(ctx);
+    stokes_coefs<double> K64 = mdz_coefs64(f);
+    int its = 0, total = 0, cycles = 0;
+    double rel = 1.0;
+    if (precision == 64) {
+        if ((s = mg_setup<double>(ctx, SV->mg64, f.eta_n, f.eta_s, st)) != MDZ_OK) return s;
+        MDZ_CUDA(ctx, cudaMemcpyAsync(S64.r, F, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+        if ((s = gcr_solve<double>(ctx, S64, SV->mg64, K64, newton, f.eta_n, rtol, maxit, &its, &rel, st)) != MDZ_OK)
+            return s;
+        MDZ_CUDA(ctx, cudaMemcpyAsync(dx, S64.x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+        total = its;
+        cycles = 1;
+    } else {
+        gcr_space<float> &S32 = SV->g32;
+        if ((s = mg_setup<float>(ctx, SV->mg32, f.eta_n, f.eta_s, st)) != MDZ_OK) return s;
+        // FP32 copy of the operator
+        const double *Dsrc[12] = {f.D11_n, f.D12_n, f.D13_n, f.D14_n, f.D21_n, f.D22_n, f.D23_n, f.D24_n,
+                                  f.D31_s, f.D32_s, f.D33_s, f.D34_s};
+        for (int q = 0; q < 12; q++) {
+            size_t m = q < 8 ? S32.np : (size_t)ctx->g.Nx * ctx->g.Nz;
+            if (!newton && q != 0 && q != 5 && q != 10) continue;
+            k_convert<double, float><<<mdz_blocks(m), MDZ_THREADS, 0, st>>>(m, Dsrc[q], S32.Dc[q]);
+            MDZ_LAUNCHED(ctx);
+        }
+        stokes_coefs<float> K32{S32.Dc[0], S32.Dc[1], S32.Dc[2], S32.Dc[3], S32.Dc[4], S32.Dc[5], S32.Dc[6],
+                                S32.Dc[7], S32.Dc[8], S32.Dc[9], S32.Dc[10], S32.Dc[11]};
+        // defect correction: r64 = F - K64 dx64 ; solve K32 e = r64 ; dx64 += e
+        MDZ_CUDA(ctx, cudaMemsetAsync(dx, 0, sizeof(double) * n, st));
+        MDZ_CUDA(ctx, cudaMemcpyAsync(S64.r, F, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+        double *dn = (double *)(ctx->d_counters + 8);
+        double r0 = -1.0;
+        for (cycles = 0; cycles < 12; cycles++) {
+            // norm of the FP64 defect
+            if ((s = dots_launch<double>(ctx, S64, S64.m + 1, 1, S64.r, dn, st)) != MDZ_OK) return s;
+            MDZ_CUDA(ctx, cudaMemcpyAsync(SV->sc + 8, dn, sizeof(double), cudaMemcpyDeviceToHost, st));
+            MDZ_CUDA(ctx, cudaStreamSynchronize(st));
+            double rn = sqrt(SV->sc[8]);
+            if (r0 < 0) r0 = rn;
+            rel = r0 > 0 ? rn / r0 : 0.0;
+            if (rel <= rtol || r0 == 0.0) break;
+            k_convert<double, float><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, S64.r, S32.r);
+            MDZ_LAUNCHED(ctx);
+            double inner_rtol = rtol / rel;
+            if (inner_rtol < 1e-4) inner_rtol = 1e-4;
+            if (inner_rtol > 0.1) inner_rtol = 0.1;
+            if ((s = gcr_solve<float>(ctx, S32, SV->mg32, K32, newton, f.eta_n, inner_rtol, maxit, &its, nullptr,
+                                      st)) != MDZ_OK)
+                return s;
+            total += its;
+            k_add_f32<<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, S32.x, dx);
+            MDZ_LAUNCHED(ctx);
+            // r64 = F - K64 dx
+            stokes_apply_launch<double>(G, K64, stokes_cvec<double>{dx, dx + nu, dx + nu + nv},
+                                        stokes_vec<double>{S64.t, S64.t + nu, S64.t + nu + nv}, nullptr, newton, st);
+            MDZ_LAUNCHED(ctx);
+            MDZ_CUDA(ctx, cudaMemcpyAsync(S64.r, F, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+            k_axpby<double><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, -1.0, S64.t, 1.0, S64.r);
+            MDZ_LAUNCHED(ctx);
+        }
+    }
+    if (stats) {
+        stats->iterations = total;
+        stats->refinements = cycles;
+        stats->rel_residual = rel;
+        stats->mg_levels = SV->mg64.nlev;
+    }
+    return MDZ_OK;
+}
+
+// ---------------------------------------------------------------------------
+extern "C" mdz_status mdz_SolveStokesDefect(mdz_ctx *ctx, mdz_fields *f, int jacobian, int precision, double rtol,
+                                            int maxit, const double *Fu, const double *Fv, const double *Fp,
+                                            double *dxu, double *dxv, double *dxp, int *iterations,
+                                            double *rel_residual) {
+    if (!ctx || !f || !Fu || !Fv || !Fp || !dxu || !dxv || !dxp)
+        return ctx ? mdz_fail(ctx, MDZ_ERR_ARG, "SolveStokesDefect: null argument") : MDZ_ERR_ARG;
+    if (precision != 64 && precision != 32) return mdz_fail(ctx, MDZ_ERR_ARG, "SolveStokesDefect: precision 64 or 32");
+    mdz_status s = mdz_ensure_fields(ctx);
+    if (s != MDZ_OK) return s;
+    if ((s = mdz_solver_ensure(ctx)) != MDZ_OK) return s;
+    cudaStream_t st = ctx->stream;
+    if ((s = mdz_upload_fields(ctx, f, st)) != MDZ_OK) return s;
+    const mdz_dgrid &g = ctx->g;
+    size_t nu = (size_t)g.Nx * (g.Nz + 1), nv = (size_t)(g.Nx + 1) * g.Nz, np = (size_t)g.ncx * g.ncz;
+    double *buf = (double *)mdz_stage(ctx, 7, sizeof(double) * 2 * (nu + nv + np));
+    if (!buf) return mdz_fail(ctx, MDZ_ERR_CUDA, "SolveStokesDefect: staging allocation failed");
+    double *F = buf, *dx = buf + nu + nv + np;
+    MDZ_CUDA(ctx, cudaMemcpyAsync(F, Fu, nu * 8, cudaMemcpyHostToDevice, st));
+    MDZ_CUDA(ctx, cudaMemcpyAsync(F + nu, Fv, nv * 8, cudaMemcpyHostToDevice, st));
+    MDZ_CUDA(ctx, cudaMemcpyAsync(F + nu + nv, Fp, np * 8, cudaMemcpyHostToDevice, st));
+    mdz_solve_stats stt{};
+    if ((s = mdz_dev_solve(ctx, ctx->d, jacobian != 0, precision, rtol, maxit, F, dx, &stt, st)) != MDZ_OK) return s;
+    MDZ_CUDA(ctx, cudaMemcpyAsync(dxu, dx, nu * 8, cudaMemcpyDeviceToHost, st));
+    MDZ_CUDA(ctx, cudaMemcpyAsync(dxv, dx + nu, nv * 8, cudaMemcpyDeviceToHost, st));
+    MDZ_CUDA(ctx, cudaMemcpyAsync(dxp, dx + nu + nv, np * 8, cudaMemcpyDeviceToHost, st));
+    MDZ_CUDA(ctx, cudaStreamSynchronize(st));
+    if (iterations) *iterations = stt.iterations;
+    if (rel_residual) *rel_residual = stt.rel_residual;
+    if (!(stt.rel_residual <= rtol))
+        return mdz_fail(ctx, MDZ_ERR_NOT_CONVERGED, "SolveStokesDefect: relative residual %.3e > %.3e after %d its",
+                        stt.rel_residual, rtol, stt.iterations);
+    return MDZ_OK;
+}

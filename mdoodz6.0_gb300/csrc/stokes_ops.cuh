@@ -127,7 +127,7 @@ __device__ __forceinline__ T xrow(const stokes_geom &G, const stokes_coefs<T> &D
         TxzS = D.D31[ixyS] * exxS + D.D32[ixyS] * ezzS + D.D33[ixyS] * gS + D.D34[ixyS] * pS_;
         TxzN = D.D31[ixyN] * exxN + D.D32[ixyN] * ezzN + D.D33[ixyN] * gN + D.D34[ixyN] * pN_;
     }
-    T grad = (G.BCp[iPrE] != 30 && G.BCp[iPrW] != 30) ? (p[iPrE] - p[iPrW]) / dx : T(0);
+    T grad = (p && G.BCp[iPrE] != 30 && G.BCp[iPrW] != 30) ? (p[iPrE] - p[iPrW]) / dx : T(0);
     if (NEWTON) grad = (inE * p[iPrE] - inW * p[iPrW]) / dx;
     return -(inE * TxxE - inW * TxxW) / dx - (inN * TxzN - inS * TxzS) / dz + grad;
 }
@@ -217,7 +217,7 @@ __device__ __forceinline__ T zrow(const stokes_geom &G, const stokes_coefs<T> &D
         TxzW = D.D31[ixyW] * exxW + D.D32[ixyW] * ezzW + D.D33[ixyW] * gW + D.D34[ixyW] * pW_;
         TxzE = D.D31[ixyE] * exxE + D.D32[ixyE] * ezzE + D.D33[ixyE] * gE + D.D34[ixyE] * pE_;
     }
-    T grad = (G.BCp[iPrS] != 30 && G.BCp[iPrN] != 30) ? (p[iPrN] - p[iPrS]) / dz : T(0);
+    T grad = (p && G.BCp[iPrS] != 30 && G.BCp[iPrN] != 30) ? (p[iPrN] - p[iPrS]) / dz : T(0);
     return -(inN * TzzN - inS * TzzS) / dz - (inE * TxzE - inW * TxzW) / dx + grad;
 }
 

@@ -268,6 +268,17 @@ class Context:
         self._check(self.L.mdz_EvaluateStokesResidualDecoupled(self.h, C.byref(s), _dptr(norms)))
         return norms
 
+    def SolveStokesDefect(self, fields, jacobian, precision, rtol, maxit, Fu, Fv, Fp):
+        """Solve K dx = F; returns (dxu, dxv, dxp, iterations, relative residual)."""
+        s = fields.struct()
+        Fu, Fv, Fp = (np.ascontiguousarray(a, np.float64) for a in (Fu, Fv, Fp))
+        du, dv, dp = np.zeros_like(Fu), np.zeros_like(Fv), np.zeros_like(Fp)
+        its, rel = C.c_int(0), C.c_double(0)
+        self._check(self.L.mdz_SolveStokesDefect(self.h, C.byref(s), C.c_int(jacobian), C.c_int(precision),
+                                                 C.c_double(rtol), C.c_int(maxit), _dptr(Fu), _dptr(Fv), _dptr(Fp),
+                                                 _dptr(du), _dptr(dv), _dptr(dp), C.byref(its), C.byref(rel)))
+        return du, dv, dp, its.value, rel.value
+
     def StokesOperatorApply(self, fields, jacobian, xu, xv, xp):
         s = fields.struct()
         xu, xv, xp = (np.ascontiguousarray(a, np.float64) for a in (xu, xv, xp))

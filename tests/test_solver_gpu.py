@@ -1,0 +1,90 @@
+"""GPU linear defect solve (matrix-free GCR + multigrid): the solution of
+K dx = F against a direct solve of the reference's assembled blocks (golden),
+and on larger seeded problems through the oracle's independent operator."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+import mdz
+import oracle
+from stokes_case import assembled, eqn_maps, reference_state, to_eqn, to_grid
+
+pytestmark = pytest.mark.gpu
+
+
+def bordered_solve(K, F, n_p):
+    """Direct solve with the pressure null space fixed by a zero-mean constraint."""
+    n = K.shape[0]
+    e = np.zeros(n)
+    e[n - n_p:] = 1.0
+    Kb = sp.bmat([[K, sp.csr_matrix(e).T], [sp.csr_matrix(e), None]]).tocsc()
+    x = spla.spsolve(Kb, np.concatenate([F, [0.0]]))
+    return x[:n]
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("jacobian", [0, 1])
+@pytest.mark.parametrize("precision", [64, 32])
+def test_solve_vs_direct_on_reference_blocks(golden, jacobian, precision):
+    ref = golden("rheology_ref.npz")
+    g, f = reference_state(ref, jacobian)
+    f["eta_n"], f["eta_s"] = ref["vg_eta_n"], ref["vg_eta_s"]
+    K = assembled(ref, jacobian)
+    maps = eqn_maps(ref)
+    n_p = int((maps[2] >= 0).sum())
+    F = to_eqn(ref["st_ru"], ref["st_rv"], ref["st_rp"], maps, K.shape[0])
+    want = bordered_solve(K, F, n_p)
+    ctx = mdz.Context(g, 3, 1)
+    du, dv, dp, its, rel = ctx.SolveStokesDefect(f, jacobian, precision, 1e-11, 400, *to_grid(F, maps, g))
+    ctx.close()
+    got = to_eqn(du, dv, dp - dp[maps[2] >= 0].mean() * (maps[2] >= 0), maps, K.shape[0])
+    assert rel <= 1e-11
+    nm = K.shape[0] - n_p
+    assert _rel(got[:nm], want[:nm]) < 1e-8
+    assert _rel(got[nm:], want[nm:]) < 1e-8
+
+
+def inclusion_problem(N, contrast, seed=0):
+    g = mdz.Grid(N, N, -0.5, 0.5, -0.5, 0.5).set_bc_pureshear(1.0)
+    Xc, Zc = np.meshgrid(g.xc, g.zc)
+    Xv, Zv = np.meshgrid(g.xg, g.zg)
+    eta_n = np.where(np.hypot(Xc, Zc) < 0.1, contrast, 1.0).ravel()
+    eta_s = np.where(np.hypot(Xv, Zv) < 0.1, contrast, 1.0).ravel()
+    f = mdz.GridFields(g, 1)
+    f["eta_n"], f["eta_s"] = eta_n, eta_s
+    f["D11_n"], f["D22_n"], f["D33_s"] = 2 * eta_n, 2 * eta_n, eta_s
+    rng = np.random.default_rng(seed)
+    Fu = rng.normal(size=g.size(-1)) * (g.BCu == -1)
+    Fv = rng.normal(size=g.size(-2)) * (g.BCv == -1)
+    Fp = rng.normal(size=g.size(1))
+    Fp -= Fp.mean()                    # compatible continuity right-hand side
+    return g, f, Fu, Fv, Fp
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_solve_inclusion_residual_via_oracle(precision):
+    g, f, Fu, Fv, Fp = inclusion_problem(129, 1e3)
+    ctx = mdz.Context(g, 1, 1)
+    du, dv, dp, its, rel = ctx.SolveStokesDefect(f, 0, precision, 1e-9, 500, Fu, Fv, Fp)
+    ctx.close()
+    ru, rv, rp = oracle.stokes_apply(g, f, 0, du, dv, dp)
+    res = np.sqrt(np.sum((ru - Fu) ** 2) + np.sum((rv - Fv) ** 2) + np.sum((rp - Fp) ** 2))
+    nrm = np.sqrt(np.sum(Fu ** 2) + np.sum(Fv ** 2) + np.sum(Fp ** 2))
+    assert res / nrm < 1e-8, (res / nrm, its)
+    assert its < 200
+
+
+def test_fp32_refined_matches_fp64():
+    g, f, Fu, Fv, Fp = inclusion_problem(257, 1e3, seed=2)
+    ctx = mdz.Context(g, 1, 1)
+    a = ctx.SolveStokesDefect(f, 0, 64, 1e-10, 600, Fu, Fv, Fp)
+    b = ctx.SolveStokesDefect(f, 0, 32, 1e-10, 600, Fu, Fv, Fp)
+    ctx.close()
+    for x, y in zip(a[:2], b[:2]):
+        assert _rel(y, x) < 1e-8
+    pa, pb = a[2] - a[2].mean(), b[2] - b[2].mean()
+    assert _rel(pb, pa) < 1e-8
