@@ -163,6 +163,12 @@ typedef struct mdz_materials {
     double nlin[MDZ_MAX_PHASES], Alin[MDZ_MAX_PHASES], Qlin[MDZ_MAX_PHASES], Vlin[MDZ_MAX_PHASES];
     double mlin[MDZ_MAX_PHASES], rlin[MDZ_MAX_PHASES], flin[MDZ_MAX_PHASES], alin[MDZ_MAX_PHASES];
     double Flin[MDZ_MAX_PHASES];
+    /* grid-property inputs of the time step (ShearModCompExpGrid,
+     * CohesionFrictionDilationGrid: SOURCE/RheologyDensity.c:1422-1791) */
+    double mu[MDZ_MAX_PHASES], bet[MDZ_MAX_PHASES], C[MDZ_MAX_PHASES], phi[MDZ_MAX_PHASES], psi[MDZ_MAX_PHASES];
+    double C_end[MDZ_MAX_PHASES], phi_end[MDZ_MAX_PHASES], psi_end[MDZ_MAX_PHASES];
+    double pls_start[MDZ_MAX_PHASES], pls_end[MDZ_MAX_PHASES];
+    int coh_soft[MDZ_MAX_PHASES], phi_soft[MDZ_MAX_PHASES], psi_soft[MDZ_MAX_PHASES];
 } mdz_materials;
 
 /* Model switches and scales read by the rheology (params / scale in the reference). */
@@ -261,6 +267,56 @@ mdz_status mdz_StokesOperatorApply(mdz_ctx *ctx, mdz_fields *f, int jacobian, co
 mdz_status mdz_SolveStokesDefect(mdz_ctx *ctx, mdz_fields *f, int jacobian, int precision, double rtol, int maxit,
                                  const double *Fu, const double *Fv, const double *Fp, double *dxu, double *dxv,
                                  double *dxp, int *iterations, double *rel_residual);
+
+/* ---- resident state and the whole time step ------------------------------- */
+
+/* Per-marker attributes kept on the device next to x, z, phase (the marker
+ * arrays of the reference, SOURCE/header_MDOODZ.h:66-78).  MDZ_M_CMUL is a
+ * per-marker cohesion multiplier (harness extension: seeded cohesion noise;
+ * 1 reproduces the reference). */
+enum {
+    MDZ_M_SXXD = 0, MDZ_M_SZZD = 1, MDZ_M_SXZ = 2, MDZ_M_STRAIN_PL = 3, MDZ_M_STRAIN = 4, MDZ_M_T = 5,
+    MDZ_M_CMUL = 6, MDZ_M_NATTR = 7
+};
+mdz_status mdz_set_marker_attr(mdz_ctx *ctx, int attr, int n, const double *values);
+mdz_status mdz_get_marker_attr(mdz_ctx *ctx, int attr, int n, double *values);
+
+/* Copy grid fields between the caller's host arrays and the context's device
+ * mirrors: to_device = 1 uploads every non-NULL member, 0 downloads them. */
+mdz_status mdz_sync_fields(mdz_ctx *ctx, mdz_fields *f, int to_device);
+
+/* Switches of one time step (the reference's params / Nparams keys). */
+typedef struct mdz_model {
+    mdz_rheo_params rheo;   /* dt, elasticity, averaging, viscosity limits, scales        */
+    double gx, gz;          /* gravity                                                      */
+    int newton;             /* 1: Newton linearisation (Jacobian), 0: Picard                */
+    int nit_max;            /* non-linear iterations allowed (Nparams.nit_max)              */
+    double rel_tol, abs_tol;/* non-linear tolerances on resx/resz/resp (rel_tol_u etc.)     */
+    double lin_rtol;        /* relative tolerance of each linear defect solve               */
+    int lin_maxit;
+    int line_search;        /* 1: LineSearchDecoupled (6 trial steps)                      */
+    double line_search_min;
+    int precision;          /* 64: plain FP64; 32: FP32 stencils + V-cycles in FP64 refinement */
+    int learned_guess;      /* 1: MLP initial guess for the local rheology (mdz_mlp_*)       */
+    int itp_stencil;        /* 1 or 9                                                        */
+    int softening;          /* 0: smooth erfc law (reference); 1: linear law                 */
+    int advect;             /* 1: update marker stress/strain and advect (RK4)               */
+} mdz_model;
+
+typedef struct mdz_step_report {
+    int nonlinear_its, linear_its, converged, stagnated;
+    double res0[3], res[3];           /* first and final resx, resz, resp                    */
+    long long local_solves, local_fallbacks, local_failures;
+    double ms_projection, ms_rheology, ms_residual, ms_solve, ms_line_search, ms_markers, ms_total;
+} mdz_step_report;
+
+/* One time step of Main_DOODZ.c's loop (SOURCE/Main_DOODZ.c:459-1320) on the
+ * resident state: marker->grid projections, grid properties, the Newton (or
+ * Picard) loop with matrix-free defect solves and optional line search, the
+ * final rheology update, marker stress/strain updates and RK4 advection.
+ * Velocities and pressure (mdz_fields u, v, p on the device) are the initial
+ * guess and receive the solution. */
+mdz_status mdz_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_model *model, mdz_step_report *rep);
 
 #ifdef __cplusplus
 }

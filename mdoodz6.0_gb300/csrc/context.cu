@@ -93,6 +93,7 @@ extern "C" mdz_status mdz_create(mdz_ctx **out, const mdz_grid_desc *d, int n_ph
     UP(ctx->m.x, (const double *)nullptr, cap); UP(ctx->m.z, (const double *)nullptr, cap);
     UP(ctx->m.vx, (const double *)nullptr, cap); UP(ctx->m.vz, (const double *)nullptr, cap);
     UP(ctx->m.phase, (const int *)nullptr, cap);
+    for (int a = 0; a < MDZ_M_NATTR; a++) UP(ctx->m.attr[a], (const double *)nullptr, cap);
     int ncells = (Nx - 1) * (Nz - 1);
     ctx->bins.ncells = ncells;
     UP(ctx->bins.cell, (const int *)nullptr, cap); UP(ctx->bins.sorted, (const int *)nullptr, cap);
@@ -122,6 +123,8 @@ extern "C" void mdz_destroy(mdz_ctx *ctx) {
                     ctx->bins.count, ctx->bins.start, ctx->bins.cursor, ctx->bins.scan_partials};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    for (int a = 0; a < MDZ_M_NATTR; a++)
+        if (ctx->m.attr[a]) cudaFree(ctx->m.attr[a]);
     for (int i = 0; i < 8; i++)
         if (ctx->stage[i]) cudaFree(ctx->stage[i]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -159,5 +162,26 @@ extern "C" mdz_status mdz_get_markers(mdz_ctx *ctx, int n, double *x, double *z,
         if (vz) MDZ_CUDA(ctx, cudaMemcpyAsync(vz, ctx->m.vz, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
     }
     MDZ_CUDA(ctx, cudaStreamSynchronize(st));
+    return MDZ_OK;
+}
+
+extern "C" mdz_status mdz_set_marker_attr(mdz_ctx *ctx, int attr, int n, const double *values) {
+    if (!ctx) return MDZ_ERR_ARG;
+    if (attr < 0 || attr >= MDZ_M_NATTR || n < 0 || n > ctx->m.n || (n > 0 && !values))
+        return mdz_fail(ctx, MDZ_ERR_ARG, "mdz_set_marker_attr: bad attribute %d or size %d (resident %d)", attr, n,
+                        ctx->m.n);
+    if (n) MDZ_CUDA(ctx, cudaMemcpyAsync(ctx->m.attr[attr], values, sizeof(double) * n, cudaMemcpyHostToDevice,
+                                         ctx->stream));
+    MDZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return MDZ_OK;
+}
+
+extern "C" mdz_status mdz_get_marker_attr(mdz_ctx *ctx, int attr, int n, double *values) {
+    if (!ctx) return MDZ_ERR_ARG;
+    if (attr < 0 || attr >= MDZ_M_NATTR || n < 0 || n > ctx->m.n || (n > 0 && !values))
+        return mdz_fail(ctx, MDZ_ERR_ARG, "mdz_get_marker_attr: bad attribute %d or size %d", attr, n);
+    if (n) MDZ_CUDA(ctx, cudaMemcpyAsync(values, ctx->m.attr[attr], sizeof(double) * n, cudaMemcpyDeviceToHost,
+                                         ctx->stream));
+    MDZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return MDZ_OK;
 }

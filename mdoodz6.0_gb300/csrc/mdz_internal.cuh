@@ -23,6 +23,7 @@ struct mdz_markers {
     long long cap = 0;
     double *x = nullptr, *z = nullptr, *vx = nullptr, *vz = nullptr;
     int *phase = nullptr;
+    double *attr[MDZ_M_NATTR] = {nullptr};
 };
 
 // Cell binning of the resident markers: markers sorted by cell (stable).

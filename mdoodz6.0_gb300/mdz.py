@@ -268,6 +268,29 @@ class Context:
         self._check(self.L.mdz_EvaluateStokesResidualDecoupled(self.h, C.byref(s), _dptr(norms)))
         return norms
 
+    # resident state and the time step -----------------------------------------
+    def set_marker_attr(self, attr, values):
+        v = np.ascontiguousarray(values, np.float64)
+        self._check(self.L.mdz_set_marker_attr(self.h, C.c_int(attr), C.c_int(len(v)), _dptr(v)))
+
+    def get_marker_attr(self, attr):
+        v = np.zeros(self.n_markers)
+        self._check(self.L.mdz_get_marker_attr(self.h, C.c_int(attr), C.c_int(len(v)), _dptr(v)))
+        return v
+
+    def upload_fields(self, fields):
+        s = fields.struct()
+        self._check(self.L.mdz_sync_fields(self.h, C.byref(s), C.c_int(1)))
+
+    def download_fields(self, fields):
+        s = fields.struct()
+        self._check(self.L.mdz_sync_fields(self.h, C.byref(s), C.c_int(0)))
+
+    def time_step(self, mat, model):
+        rep = StepReport()
+        self._check(self.L.mdz_time_step(self.h, C.byref(mat), C.byref(model), C.byref(rep)))
+        return rep
+
     def SolveStokesDefect(self, fields, jacobian, precision, rtol, maxit, Fu, Fv, Fp):
         """Solve K dx = F; returns (dxu, dxv, dxp, iterations, relative residual)."""
         s = fields.struct()
@@ -362,12 +385,16 @@ MAT_INT = ["cstv", "pwlv", "linv", "expv", "gbsv", "gs", "is_tensile", "reac_sof
 MAT_DBL = ["eta0", "rho", "alp", "gs_ref", "Slim", "eta_vp", "n_vp",
            "npwl", "Apwl", "Qpwl", "Vpwl", "mpwl", "rpwl", "fpwl", "apwl", "Fpwl", "pref_pwl",
            "nlin", "Alin", "Qlin", "Vlin", "mlin", "rlin", "flin", "alin", "Flin"]
+MAT_DBL2 = ["mu", "bet", "C", "phi", "psi", "C_end", "phi_end", "psi_end", "pls_start", "pls_end"]
+MAT_INT2 = ["coh_soft", "phi_soft", "psi_soft"]
 
 
 class Materials(C.Structure):
     _fields_ = ([("n_phases", C.c_int), ("R", C.c_double)]
                 + [(n, C.c_int * MDZ_MAX_PHASES) for n in MAT_INT]
-                + [(n, C.c_double * MDZ_MAX_PHASES) for n in MAT_DBL])
+                + [(n, C.c_double * MDZ_MAX_PHASES) for n in MAT_DBL]
+                + [(n, C.c_double * MDZ_MAX_PHASES) for n in MAT_DBL2]
+                + [(n, C.c_int * MDZ_MAX_PHASES) for n in MAT_INT2])
 
     @classmethod
     def from_phases(cls, phases, R=8.314510):
@@ -389,3 +416,39 @@ class RheoParams(C.Structure):
     def make(cls, dt, iselastic=1, step=1, eta_avg=0, mineta=1e-100, maxeta=1e100, scale_T=1.0, scale_E=1.0,
              scale_S=1.0, scale_eta=1.0, scale_L=1.0):
         return cls(dt, iselastic, step, eta_avg, mineta, maxeta, scale_T, scale_E, scale_S, scale_eta, scale_L)
+
+
+# marker attributes (enum in include/mdoodz_gpu.h)
+M_SXXD, M_SZZD, M_SXZ, M_STRAIN_PL, M_STRAIN, M_T, M_CMUL = range(7)
+
+
+class Model(C.Structure):
+    """mdz_model: switches of one time step."""
+    _fields_ = [("rheo", RheoParams), ("gx", C.c_double), ("gz", C.c_double), ("newton", C.c_int),
+                ("nit_max", C.c_int), ("rel_tol", C.c_double), ("abs_tol", C.c_double), ("lin_rtol", C.c_double),
+                ("lin_maxit", C.c_int), ("line_search", C.c_int), ("line_search_min", C.c_double),
+                ("precision", C.c_int), ("learned_guess", C.c_int), ("itp_stencil", C.c_int),
+                ("softening", C.c_int), ("advect", C.c_int)]
+
+    @classmethod
+    def make(cls, rheo, gx=0.0, gz=0.0, newton=1, nit_max=10, rel_tol=1e-8, abs_tol=1e-300, lin_rtol=1e-5,
+             lin_maxit=500, line_search=0, line_search_min=0.0, precision=64, learned_guess=0, itp_stencil=1,
+             softening=0, advect=1):
+        return cls(rheo, gx, gz, newton, nit_max, rel_tol, abs_tol, lin_rtol, lin_maxit, line_search,
+                   line_search_min, precision, learned_guess, itp_stencil, softening, advect)
+
+
+class StepReport(C.Structure):
+    _fields_ = [("nonlinear_its", C.c_int), ("linear_its", C.c_int), ("converged", C.c_int), ("stagnated", C.c_int),
+                ("res0", C.c_double * 3), ("res", C.c_double * 3), ("local_solves", C.c_longlong),
+                ("local_fallbacks", C.c_longlong), ("local_failures", C.c_longlong),
+                ("ms_projection", C.c_double), ("ms_rheology", C.c_double), ("ms_residual", C.c_double),
+                ("ms_solve", C.c_double), ("ms_line_search", C.c_double), ("ms_markers", C.c_double),
+                ("ms_total", C.c_double)]
+
+    def as_dict(self):
+        d = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            d[name] = list(v) if hasattr(v, "__len__") else v
+        return d

@@ -1,0 +1,78 @@
+"""One full time step on the GPU (projection -> Newton loop with matrix-free
+GCR/multigrid and line search -> marker update -> RK4) against the CPU oracle
+time step (restated reference functions + direct linear solves)."""
+import numpy as np
+import pytest
+
+import mdz
+import mdz_setups
+import oracle_step
+
+pytestmark = pytest.mark.gpu
+
+VEP_PHASES = [
+    dict(cstv=1, eta0=1e3, mu=1.0, bet=1e-2, C=1.0, phi=np.pi / 6, psi=0.0, rho=1.0, Slim=1e10, eta_vp=0.05, n_vp=1.0,
+         gs_ref=1.0, pls_start=0.0, pls_end=1.0),
+    dict(cstv=1, eta0=1e3, mu=1.0, bet=1e-2, C=0.5, phi=np.pi / 6, psi=0.0, rho=1.0, Slim=1e10, eta_vp=0.05, n_vp=1.0,
+         gs_ref=1.0, pls_start=0.0, pls_end=1.0),
+]
+
+
+def vep_case(N=33, nm=4, seed=5):
+    g = mdz.Grid(N, N, -0.5, 0.5, -0.5, 0.5).set_bc_pureshear(1.0)
+    x, z = mdz_setups.seed_markers(g, nm, nm, 0.5, seed)
+    ph = mdz_setups.inclusion_phase(x, z, 0.0, 0.0, 0.08)
+    rng = np.random.default_rng(seed)
+    m = dict(x=x, z=z, phase=ph, sxxd=np.full(len(x), -0.7), szzd=np.full(len(x), 0.7),
+             sxz=0.05 * rng.standard_normal(len(x)), strain_pl=np.zeros(len(x)), strain=np.zeros(len(x)),
+             T=np.zeros(len(x)), cmul=1.0 + 0.01 * rng.standard_normal(len(x)))
+    u = (-g.xg[None, :] + 0 * g.zvx[:, None]).ravel()
+    v = (g.zg[:, None] + 0 * g.xvz[None, :]).ravel()
+    p = np.zeros(g.size(1))
+    mat = mdz.Materials.from_phases(VEP_PHASES)
+    return g, m, u, v, p, mat
+
+
+def run_gpu(g, m, u, v, p, mat, model):
+    ctx = mdz.Context(g, mat.n_phases, len(m["x"]))
+    ctx.set_markers(m["x"], m["z"], m["phase"])
+    for attr, key in ((mdz.M_SXXD, "sxxd"), (mdz.M_SZZD, "szzd"), (mdz.M_SXZ, "sxz"), (mdz.M_STRAIN_PL, "strain_pl"),
+                      (mdz.M_STRAIN, "strain"), (mdz.M_T, "T"), (mdz.M_CMUL, "cmul")):
+        ctx.set_marker_attr(attr, m[key])
+    f = mdz.GridFields(g, mat.n_phases)
+    f["u"], f["v"], f["p"] = u, v, p
+    s = f.struct()
+    for name in mdz.FIELD_NAMES:
+        if name not in ("u", "v", "p"):
+            setattr(s, name, None)
+    ctx._check(ctx.L.mdz_sync_fields(ctx.h, mdz.C.byref(s), 1))
+    rep = ctx.time_step(mat, model)
+    out = mdz.GridFields(g, mat.n_phases)
+    ctx.download_fields(out)
+    x, z, ph, _, _ = ctx.get_markers()
+    mk = dict(x=x, z=z, phase=ph, sxxd=ctx.get_marker_attr(mdz.M_SXXD), szzd=ctx.get_marker_attr(mdz.M_SZZD),
+              sxz=ctx.get_marker_attr(mdz.M_SXZ), strain_pl=ctx.get_marker_attr(mdz.M_STRAIN_PL))
+    ctx.close()
+    return out, mk, rep
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_vep_newton_step_vs_oracle(precision):
+    g, m, u, v, p, mat = vep_case()
+    prm = mdz.RheoParams.make(dt=0.5, iselastic=1, step=1)
+    model = mdz.Model.make(prm, newton=1, nit_max=12, rel_tol=1e-11, lin_rtol=1e-9, line_search=1,
+                           precision=precision)
+    out, mk, rep = run_gpu(g, dict((k, np.array(v_)) for k, v_ in m.items()), u, v, p, mat, model)
+    mo = dict((k, np.array(v_)) for k, v_ in m.items())
+    uo, vo, po, ro = oracle_step.time_step(g, mat, model, mo, u, v, p)
+    assert rep.converged == 1 and ro["converged"] == 1, (rep.as_dict(), ro)
+    assert (out["eII_pl"] > 0).any()                       # plasticity active
+    assert _rel(out["u"], uo) < 1e-8 and _rel(out["v"], vo) < 1e-8
+    assert _rel(out["p"] - out["p"].mean(), po - po.mean()) < 1e-8
+    for k in ("sxxd", "szzd", "sxz", "strain_pl", "x", "z"):
+        assert _rel(mk[k], mo[k]) < 1e-8, k
+    assert np.array_equal(mk["phase"], mo["phase"])
