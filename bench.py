@@ -1,0 +1,263 @@
+"""Benchmark: wall time of one full Newton time step of the lithosphere model
+(1025 x 513 grid over 1000 x 400 km, 4 phases, 16 markers per cell ~ 8.4 M
+markers) on one GB300, in the plain FP64 form and in the FP32-refined
+(+ learned local-rheology guess, when an MLP is loaded) form.
+
+A step is one pass of the hot path: marker->grid projection, the Newton loop
+to a 1e-8 relative Stokes residual (local VEP rheology + tangent, matrix-free
+residual / Jacobian, GCR + multigrid, line search), marker stress/strain
+update and RK4 advection.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  For N > 1 (torchrun) every rank runs an
+independent replica of the model (the build does not shard the path).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [os.path.join(ROOT, "mdoodz6.0_gb300"), os.path.join(ROOT, "oracle")]
+
+METRIC = "Newton-step time @1025x513: learned+FP32-IR vs plain FP64 GPU, 1e-8 resid"
+UNIT = "ms/step"
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([s.strip() for s in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        import statistics
+        mhz = [float(s[1]) for s in self.samples if len(s) > 2 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) > 2 and s[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            for nm, v in zip(names, s[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(mhz) if mhz else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return d["hbm_gbs"], d.get("bf16_tflops"), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+def run_form(cfg_builder, precision, learned, steps, warmup, size):
+    import mdz
+    import mdz_setups
+    cfg = cfg_builder(precision, learned, size)
+    ctx = mdz_setups.load_context(cfg)
+    model, mat = cfg["model"], cfg["mat"]
+    reps = []
+    for _ in range(warmup):
+        ctx.time_step(mat, model)
+    ctx.L.mdz_sync(ctx.h)
+    ctx.set_profiling(True)
+    l0 = ctx.kernel_launches
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        reps.append(ctx.time_step(mat, model).as_dict())
+    ctx.L.mdz_sync(ctx.h)
+    wall = (time.perf_counter() - t0) * 1e3 / steps
+    launches = ctx.kernel_launches - l0
+    gpu_ms = sum(r["ms_total"] for r in reps) / steps
+    kern = ctx.kernel_timing()
+    ctx.close()
+    return dict(ms_wall=wall, ms_gpu=gpu_ms, reports=reps, launches=launches, kernel=kern, cfg=cfg)
+
+
+def e2e_form(cfg_builder, precision, learned, steps, size):
+    """Same step through the public API with host buffers: markers, attributes
+    and initial fields uploaded from host memory every step, the solution and
+    the marker state read back."""
+    import numpy as np
+    import mdz
+    import mdz_setups
+    cfg = cfg_builder(precision, learned, size)
+    m = cfg["markers"]
+    ctx = mdz_setups.load_context(cfg)
+    model, mat = cfg["model"], cfg["mat"]
+    ctx.time_step(mat, model)
+    g = cfg["grid"]
+    out = mdz.GridFields(g, mat.n_phases)
+    times, h2d, d2h = [], 0, 0
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        ctx.set_markers(m["x"], m["z"], m["phase"])
+        for attr, key in ((mdz.M_SXXD, "sxxd"), (mdz.M_SZZD, "szzd"), (mdz.M_SXZ, "sxz"),
+                          (mdz.M_STRAIN_PL, "strain_pl"), (mdz.M_STRAIN, "strain"), (mdz.M_T, "T"),
+                          (mdz.M_CMUL, "cmul")):
+            ctx.set_marker_attr(attr, m[key])
+        ctx.time_step(mat, model)
+        x, z, ph, vx, vz = ctx.get_markers()
+        sxx = ctx.get_marker_attr(mdz.M_SXXD)
+        u = np.empty(g.size(-1))
+        ctx.L.mdz_get_velocity(ctx.h, mdz._dptr(u), None, None)
+        times.append((time.perf_counter() - t0) * 1e3)
+    n = len(m["x"])
+    h2d = n * (8 * 2 + 4) + n * 8 * 7
+    d2h = n * (8 * 4 + 4) + n * 8 + g.size(-1) * 8
+    ctx.close()
+    return sum(times) / len(times), h2d, d2h
+
+
+def builder(size):
+    import mdz_setups
+
+    def b(precision, learned, sz=size):
+        if sz:
+            nx, nz = sz
+            return mdz_setups.config_lithosphere(Nx=nx, Nz=nz, precision=precision, learned=learned)
+        return mdz_setups.config_lithosphere(precision=precision, learned=learned)
+    return b
+
+
+def cpu_reference(size, budget_s=20.0):
+    """The oracle's CPU time step (restated reference functions + SuperLU) on a
+    bounded strip of the same model: full width, a few cells deep, timed and
+    scaled to the full grid by the cell count."""
+    import numpy as np
+    import mdz_setups
+    import oracle_step
+    nx, nz = size if size else (1025, 513)
+    strip_nz = 17
+    cfg = mdz_setups.config_lithosphere(Nx=nx, Nz=strip_nz, precision=64)
+    m = cfg["markers"]
+    t0 = time.perf_counter()
+    oracle_step.time_step(cfg["grid"], cfg["mat"], cfg["model"], m, cfg["u"], cfg["v"], cfg["p"])
+    dt = time.perf_counter() - t0
+    scale = ((nx - 1) * (nz - 1)) / ((nx - 1) * (strip_nz - 1))
+    return dict(value=dt * 1e3 * scale, unit=UNIT, cores=1, kind="port",
+                sample="one oracle time step on a %dx%d strip of the model (%.1f s), scaled by cells x%.1f"
+                       % (nx, strip_nz, dt, scale))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", default=None, help="NXxNZ override (tests only)")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = _dist()
+    size = tuple(int(s) for s in args.size.split("x")) if args.size else None
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        times = []
+        for _ in range(args.warmup + args.steps):
+            times.append(cpu_reference(size))
+        ref = times[-1]
+        val = sum(t["value"] for t in times[args.warmup:]) / args.steps
+        line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": val, "higher_is_better": False,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "lithosphere 1025x513, 4 phases, 16 markers/cell, one Newton time step"},
+                "cpu_baseline": dict(ref, value=val),
+                "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import mdz
+    mdz.load_library()
+    b = builder(size)
+    if world > 1:
+        torch.distributed.barrier()
+    hbm, bf16, peak_kind = peaks()
+    with ClockSampler(local) as clk:
+        plain = run_form(b, 64, 0, args.steps, args.warmup, size)
+        fast = run_form(b, 32, 0, args.steps, args.warmup, size)
+    ms = fast["ms_wall"]
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    e2e_ms, h2d, d2h = e2e_form(b, 32, 0, max(1, args.steps - 1), size)
+    k = fast["kernel"]
+    achieved = k["bytes"] / (k["ms"] * 1e-3) / 1e9 if k["ms"] > 0 else None
+    line = {
+        "metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+        "data": "synthetic",
+        "config": {"workload": "lithosphere %s, 4 phases, 16 markers/cell, one Newton time step"
+                               % ("x".join(map(str, size)) if size else "1025x513"),
+                   "markers": len(fast["cfg"]["markers"]["x"]),
+                   "l2": "inputs larger than L2 (markers %.0f MB)" % (len(fast["cfg"]["markers"]["x"]) * 84 / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "forms": {"plain_fp64_ms": plain["ms_wall"], "fp32_ir_ms": fast["ms_wall"],
+                  "speedup_fp32_ir_vs_fp64": plain["ms_wall"] / fast["ms_wall"],
+                  "plain_report": plain["reports"][-1], "fp32_ir_report": fast["reports"][-1]},
+        "e2e": {"value": e2e_ms, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": fast["launches"] // args.steps,
+        "roofline": {"bound": "hbm", "kernel": k["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                     "peak_kind": peak_kind},
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_reference(size)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -305,6 +305,7 @@ typedef struct mdz_model {
 
 typedef struct mdz_step_report {
     int nonlinear_its, linear_its, converged, stagnated;
+    int picard_fallbacks;             /* Newton iterations solved with the Picard operator instead */
     double res0[3], res[3];           /* first and final resx, resz, resp                    */
     long long local_solves, local_fallbacks, local_failures;
     double ms_projection, ms_rheology, ms_residual, ms_solve, ms_line_search, ms_markers, ms_total;
@@ -317,6 +318,20 @@ typedef struct mdz_step_report {
  * Velocities and pressure (mdz_fields u, v, p on the device) are the initial
  * guess and receive the solution. */
 mdz_status mdz_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_model *model, mdz_step_report *rep);
+
+/* Read back the resident velocity / pressure solution (any pointer may be NULL). */
+mdz_status mdz_get_velocity(mdz_ctx *ctx, double *u, double *v, double *p);
+
+/* Wait for all work queued on the context's stream. */
+mdz_status mdz_sync(mdz_ctx *ctx);
+
+/* Launch timing of the main kernel classes with CUDA events on the context's
+ * stream (off by default; turning it on or off resets the totals).  Classes:
+ * 0 local rheology, 1 Stokes operator apply inside the Krylov solver,
+ * 2 multigrid smoothing, 3 projection.  Returns the summed time (ms), the
+ * summed algorithmic bytes and the number of launches of one class. */
+mdz_status mdz_set_profiling(mdz_ctx *ctx, int on);
+mdz_status mdz_kernel_timing(mdz_ctx *ctx, int kernel_class, double *ms, double *bytes, long long *launches);
 
 #ifdef __cplusplus
 }

@@ -185,3 +185,57 @@ extern "C" mdz_status mdz_get_marker_attr(mdz_ctx *ctx, int attr, int n, double 
     MDZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return MDZ_OK;
 }
+
+// ---- optional launch timing of the main kernel classes -------------------------
+void mdz_prof_begin(mdz_ctx *ctx, int cls, cudaStream_t st, cudaEvent_t *ev) {
+    (void)cls;
+    *ev = nullptr;
+    if (!ctx->profiling) return;
+    cudaEventCreate(ev);
+    cudaEventRecord(*ev, st);
+}
+
+void mdz_prof_end(mdz_ctx *ctx, int cls, double bytes, cudaStream_t st, cudaEvent_t a) {
+    if (!ctx->profiling || !a) return;
+    cudaEvent_t b;
+    cudaEventCreate(&b);
+    cudaEventRecord(b, st);
+    ctx->prof.push_back(mdz_ctx::prof_rec{cls, a, b, bytes});
+}
+
+static void prof_resolve(mdz_ctx *ctx) {
+    for (auto &r : ctx->prof) {
+        cudaEventSynchronize(r.b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, r.a, r.b);
+        ctx->prof_ms[r.cls] += ms;
+        ctx->prof_bytes[r.cls] += r.bytes;
+        ctx->prof_n[r.cls] += 1;
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    ctx->prof.clear();
+}
+
+extern "C" mdz_status mdz_set_profiling(mdz_ctx *ctx, int on) {
+    if (!ctx) return MDZ_ERR_ARG;
+    prof_resolve(ctx);
+    for (int i = 0; i < 8; i++) { ctx->prof_ms[i] = 0; ctx->prof_bytes[i] = 0; ctx->prof_n[i] = 0; }
+    ctx->profiling = on != 0;
+    return MDZ_OK;
+}
+
+extern "C" mdz_status mdz_kernel_timing(mdz_ctx *ctx, int cls, double *ms, double *bytes, long long *launches) {
+    if (!ctx || cls < 0 || cls >= MDZ_PROF_NCLS) return MDZ_ERR_ARG;
+    prof_resolve(ctx);
+    if (ms) *ms = ctx->prof_ms[cls];
+    if (bytes) *bytes = ctx->prof_bytes[cls];
+    if (launches) *launches = ctx->prof_n[cls];
+    return MDZ_OK;
+}
+
+extern "C" mdz_status mdz_sync(mdz_ctx *ctx) {
+    if (!ctx) return MDZ_ERR_ARG;
+    MDZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return MDZ_OK;
+}

@@ -3,7 +3,14 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string>
+#include <vector>
 #include "mdoodz_gpu.h"
+
+// kernel classes timed when profiling is on
+enum { MDZ_PROF_VISCOSITY = 0, MDZ_PROF_STOKES_APPLY = 1, MDZ_PROF_MG_SMOOTH = 2, MDZ_PROF_P2G = 3, MDZ_PROF_NCLS = 4 };
+struct mdz_ctx;
+void mdz_prof_begin(mdz_ctx *ctx, int cls, cudaStream_t st, cudaEvent_t *ev);
+void mdz_prof_end(mdz_ctx *ctx, int cls, double bytes, cudaStream_t st, cudaEvent_t a);
 
 #define MDZ_THREADS 256
 
@@ -50,6 +57,12 @@ struct mdz_ctx {
     bool fields_ready = false;
     int *d_counters = nullptr;   // small device scratch: failure counters etc.
     bool bcs_checked = false, bcs_ok = false;
+    // optional per-launch event timing of the main kernel classes (bench roofline)
+    bool profiling = false;
+    struct prof_rec { int cls; cudaEvent_t a, b; double bytes; };
+    std::vector<prof_rec> prof;
+    double prof_ms[8] = {0}, prof_bytes[8] = {0};
+    long long prof_n[8] = {0};
     struct mdz_solver *solver = nullptr;   // Krylov / multigrid workspace (solver.cu)
     std::string err;
     // host-call staging buffers (grown on demand)

@@ -608,10 +608,16 @@ mdz_status mdz_dev_viscosity(mdz_ctx *ctx, const mdz_materials *m, const mdz_rhe
     if ((s = mdz_dev_c2v(ctx, f.p, f.P_s, st)) != MDZ_OK) return s;
     if ((s = mdz_dev_c2v(ctx, f.d0_n, f.d0_s, st)) != MDZ_OK) return s;
     if ((s = mdz_dev_c2v(ctx, f.phi0_n, f.phi0_s, st)) != MDZ_OK) return s;
+    cudaEvent_t ev;
+    mdz_prof_begin(ctx, MDZ_PROF_VISCOSITY, st, &ev);
     k_viscosity_centroids<<<mdz_blocks(nc, 128), 128, 0, st>>>(g, *m, *prm, f, d_fail);
     MDZ_LAUNCHED(ctx);
     k_viscosity_vertices<<<mdz_blocks(nv, 128), 128, 0, st>>>(g, *m, *prm, f, d_fail);
     MDZ_LAUNCHED(ctx);
+    // algorithmic bytes: per centroid 17 + n_phases FP64 inputs and 35 outputs,
+    // per vertex 17 + n_phases inputs and 12 outputs, plus the tags
+    double bytes = (double)nc * (8.0 * (17 + m->n_phases + 35) + 1) + (double)nv * (8.0 * (17 + m->n_phases + 12) + 1);
+    mdz_prof_end(ctx, MDZ_PROF_VISCOSITY, bytes, st, ev);
     return MDZ_OK;
 }
 

@@ -765,9 +765,17 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, mg_hier<T> &H, const 
     for (it = 0; it < maxit; it++) {
         if (k == S.m) k = 0;   // restart: keep x and r, drop the basis
         if ((s = precondition<T>(ctx, H, eta_n, S.r, S.z, nu, nv, st)) != MDZ_OK) return s;
+        cudaEvent_t ev;
+        mdz_prof_begin(ctx, MDZ_PROF_STOKES_APPLY, st, &ev);
         stokes_apply_launch<T>(G, K, stokes_cvec<T>{S.z, S.z + nu, S.z + nu + nv},
                                stokes_vec<T>{S.w, S.w + nu, S.w + nu + nv}, nullptr, newton, st);
         MDZ_LAUNCHED(ctx);
+        {   // algorithmic bytes: input and output vectors, the D-tensor read once, tags
+            size_t nc = S.np, ng = (size_t)G.Nx * G.Nz;
+            double coef = newton ? (8.0 * nc + 4.0 * ng) : (2.0 * nc + ng);
+            double bytes = sizeof(T) * (2.0 * n + coef) + (double)(nu + nv + nc + ng);
+            mdz_prof_end(ctx, MDZ_PROF_STOKES_APPLY, bytes, st, ev);
+        }
         if (k > 0) {   // first Gram-Schmidt pass
             if ((s = dots_launch<T>(ctx, S, 0, k, S.w, dots, st)) != MDZ_OK) return s;
             k_gcr_orth<T><<<nb, MDZ_THREADS, 0, st>>>(n, k, S.Z, S.W, dots, S.z, S.w);

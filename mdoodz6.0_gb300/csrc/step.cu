@@ -392,8 +392,18 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
             step_timer T(st, &R.ms_solve);
             s = mdz_dev_solve(ctx, f, M->newton != 0, M->precision, M->lin_rtol, M->lin_maxit, B.F, B.dx, &ss, st);
             if (s != MDZ_OK) return s;
+            R.linear_its += ss.iterations;
+            // A Newton system whose pressure Schur complement the Picard-based
+            // preconditioner cannot follow (strong non-associated plasticity)
+            // stalls the Krylov solve: take a Picard step for this iteration.
+            if (M->newton && !(ss.rel_residual <= 1e-2)) {
+                if ((s = mdz_dev_operators(ctx, &M->rheo, f, 0, st)) != MDZ_OK) return s;
+                s = mdz_dev_solve(ctx, f, false, M->precision, M->lin_rtol, M->lin_maxit, B.F, B.dx, &ss, st);
+                if (s != MDZ_OK) return s;
+                R.linear_its += ss.iterations;
+                R.picard_fallbacks++;
+            }
         }
-        R.linear_its += ss.iterations;
         // line search / update
         k_copy3<<<mdz_blocks(nmax), MDZ_THREADS, 0, st>>>(nu, nv, np, f.u, f.v, f.p, B.u0, B.v0, B.p0);
         MDZ_LAUNCHED(ctx);
@@ -523,4 +533,17 @@ extern "C" mdz_status mdz_sync_fields(mdz_ctx *ctx, mdz_fields *f, int to_device
 #undef NAME
     };
     return mdz_download_fields(ctx, f, all, (int)(sizeof(all) / sizeof(all[0])), ctx->stream);
+}
+
+extern "C" mdz_status mdz_get_velocity(mdz_ctx *ctx, double *u, double *v, double *p) {
+    if (!ctx) return MDZ_ERR_ARG;
+    mdz_status s = mdz_ensure_fields(ctx);
+    if (s != MDZ_OK) return s;
+    const mdz_dgrid &g = ctx->g;
+    cudaStream_t st = ctx->stream;
+    if (u) MDZ_CUDA(ctx, cudaMemcpyAsync(u, ctx->d.u, sizeof(double) * g.Nx * (g.Nz + 1), cudaMemcpyDeviceToHost, st));
+    if (v) MDZ_CUDA(ctx, cudaMemcpyAsync(v, ctx->d.v, sizeof(double) * (g.Nx + 1) * g.Nz, cudaMemcpyDeviceToHost, st));
+    if (p) MDZ_CUDA(ctx, cudaMemcpyAsync(p, ctx->d.p, sizeof(double) * g.ncx * g.ncz, cudaMemcpyDeviceToHost, st));
+    MDZ_CUDA(ctx, cudaStreamSynchronize(st));
+    return MDZ_OK;
 }

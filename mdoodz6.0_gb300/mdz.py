@@ -286,6 +286,25 @@ class Context:
         s = fields.struct()
         self._check(self.L.mdz_sync_fields(self.h, C.byref(s), C.c_int(0)))
 
+    def set_profiling(self, on):
+        self._check(self.L.mdz_set_profiling(self.h, C.c_int(int(on))))
+
+    KERNEL_CLASSES = ["local_rheology", "stokes_apply", "mg_smooth", "projection"]
+
+    def kernel_timing(self):
+        """Summed event time, algorithmic bytes and launch count per kernel class,
+        plus the dominant class (largest time)."""
+        out = {}
+        for i, name in enumerate(self.KERNEL_CLASSES):
+            ms, by, n = C.c_double(0), C.c_double(0), C.c_longlong(0)
+            self._check(self.L.mdz_kernel_timing(self.h, C.c_int(i), C.byref(ms), C.byref(by), C.byref(n)))
+            out[name] = dict(ms=ms.value, bytes=by.value, launches=n.value)
+        dom = max(out, key=lambda k: out[k]["ms"])
+        d = dict(out[dom])
+        d["name"] = dom
+        d["classes"] = out
+        return d
+
     def time_step(self, mat, model):
         rep = StepReport()
         self._check(self.L.mdz_time_step(self.h, C.byref(mat), C.byref(model), C.byref(rep)))
@@ -440,7 +459,7 @@ class Model(C.Structure):
 
 class StepReport(C.Structure):
     _fields_ = [("nonlinear_its", C.c_int), ("linear_its", C.c_int), ("converged", C.c_int), ("stagnated", C.c_int),
-                ("res0", C.c_double * 3), ("res", C.c_double * 3), ("local_solves", C.c_longlong),
+                ("picard_fallbacks", C.c_int), ("res0", C.c_double * 3), ("res", C.c_double * 3), ("local_solves", C.c_longlong),
                 ("local_fallbacks", C.c_longlong), ("local_failures", C.c_longlong),
                 ("ms_projection", C.c_double), ("ms_rheology", C.c_double), ("ms_residual", C.c_double),
                 ("ms_solve", C.c_double), ("ms_line_search", C.c_double), ("ms_markers", C.c_double),

@@ -33,3 +33,161 @@ def seed_markers(grid, nmx, nmz, jitter=0.5, seed=12345):
 
 def inclusion_phase(x, z, xc, zc, r):
     return (np.hypot(x - xc, z - zc) < r).astype(np.int32)
+
+
+# ---------------------------------------------------------------------------
+# Benchmark configurations.  Each builder returns a dict with the grid, the
+# markers (positions, phases and attributes), the materials, the step model
+# and the initial velocity / pressure.  `N` overrides the grid size so the same
+# physics runs small in tests.
+
+class Scales:
+    """Characteristic scales of the lithosphere setup (the reference
+    non-dimensionalises every input with such a set, ScaleMe in
+    SOURCE/InputOutput.c): viscosity, length, velocity; time, stress and
+    strain rate follow.  Temperature stays in kelvin."""
+
+    def __init__(self, eta=1e22, L=1e3, V=1e-10):
+        self.eta, self.L, self.V = eta, L, V
+        self.t = L / V
+        self.E = 1.0 / self.t
+        self.S = eta * self.E
+
+
+def _markers_dict(x, z, ph, **attrs):
+    n = len(x)
+    m = dict(x=x, z=z, phase=ph.astype(np.int32))
+    for k in ("sxxd", "szzd", "sxz", "strain_pl", "strain", "T"):
+        m[k] = np.zeros(n)
+    m["cmul"] = np.ones(n)
+    m.update(attrs)
+    return m
+
+
+def pure_shear_velocity(grid, eps):
+    u = (-grid.xg[None, :] * eps + 0.0 * grid.zvx[:, None]).ravel()
+    v = (grid.zg[:, None] * eps + 0.0 * grid.xvz[None, :]).ravel()
+    return u, v
+
+
+def config_inclusion(N=101, nm=4, seed=12345):
+    """Linear-viscous pure shear, unit square, circular inclusion r = 0.1 with
+    viscosity 1e3 in a matrix of viscosity 1; free-slip walls, eps_BG = 1."""
+    import mdz
+    g = mdz.Grid(N, N, -0.5, 0.5, -0.5, 0.5).set_bc_pureshear(1.0)
+    x, z = seed_markers(g, nm, nm, 0.5, seed)
+    ph = inclusion_phase(x, z, 0.0, 0.0, 0.1)
+    phases = [dict(cstv=1, eta0=1.0, mu=1.0, bet=1.0, C=1e90, phi=0.0, rho=1.0, Slim=1e90, n_vp=1.0, gs_ref=1.0),
+              dict(cstv=1, eta0=1e3, mu=1.0, bet=1.0, C=1e90, phi=0.0, rho=1.0, Slim=1e90, n_vp=1.0, gs_ref=1.0)]
+    mat = mdz.Materials.from_phases(phases)
+    prm = mdz.RheoParams.make(dt=1e-3, iselastic=0, step=1, eta_avg=0)
+    model = mdz.Model.make(prm, newton=0, nit_max=4, rel_tol=1e-8, lin_rtol=1e-9, line_search=0)
+    u, v = pure_shear_velocity(g, 1.0)
+    return dict(name="inclusion", grid=g, markers=_markers_dict(x, z, ph), mat=mat, model=model, u=u, v=v,
+                p=np.zeros(g.size(1)))
+
+
+def config_vep(N=401, nm=4, seed=12345, noise=0.01):
+    """Visco-elasto-plastic Drucker-Prager pure shear: G = 1, eta = 1e3, C = 1
+    with 1 % seeded per-marker noise, phi = 30 deg, psi = 0, dt = 1e-2,
+    eps_BG = 1; viscoplastic regularisation eta_vp = 0.05."""
+    import mdz
+    g = mdz.Grid(N, N, -0.5, 0.5, -0.5, 0.5).set_bc_pureshear(1.0)
+    x, z = seed_markers(g, nm, nm, 0.5, seed)
+    ph = np.zeros(len(x), np.int32)
+    rng = np.random.default_rng(seed + 1)
+    phases = [dict(cstv=1, eta0=1e3, mu=1.0, bet=1e-2, C=1.0, phi=np.pi / 6, psi=0.0, rho=1.0, Slim=1e10,
+                   eta_vp=0.05, n_vp=1.0, gs_ref=1.0, pls_start=0.0, pls_end=1.0)]
+    mat = mdz.Materials.from_phases(phases)
+    prm = mdz.RheoParams.make(dt=1e-2, iselastic=1, step=1, eta_avg=0)
+    model = mdz.Model.make(prm, newton=1, nit_max=10, rel_tol=1e-8, lin_rtol=1e-6, line_search=1)
+    u, v = pure_shear_velocity(g, 1.0)
+    m = _markers_dict(x, z, ph, cmul=1.0 + noise * rng.standard_normal(len(x)))
+    return dict(name="vep", grid=g, markers=m, mat=mat, model=model, u=u, v=v, p=np.zeros(g.size(1)))
+
+
+def config_lithosphere(Nx=1025, Nz=513, nm=4, seed=12345, precision=64, learned=0):
+    """Layered lithosphere over 1000 x 400 km: upper crust 0-20 km, lower crust
+    20-35 km, mantle lithosphere 35-120 km, asthenosphere; each phase with
+    dislocation creep (n in [3.0, 3.5], A and Q log-uniform from the seed),
+    diffusion creep and Drucker-Prager plasticity; linear geotherm
+    0 -> 1330 C at 120 km then adiabatic (0.3 K/km); 1 cm/yr extension
+    (pure-shear walls); gravity.  Non-dimensionalised with Scales()."""
+    import mdz
+    sc = Scales()
+    L = sc.L
+    g = mdz.Grid(Nx, Nz, -500e3 / L, 500e3 / L, -400e3 / L, 0.0).set_bc_pureshear(0.0)
+    Vext = 0.01 / (365.25 * 24 * 3600)               # 1 cm/yr in m/s
+    eps = -2 * 0.5 * Vext / 1000e3                   # extension: u = -x eps > 0 on the east wall
+    g.set_bc_pureshear(eps / sc.E)
+    x, z = seed_markers(g, nm, nm, 0.5, seed)
+    depth = -z * L                                   # m
+    ph = np.where(depth < 20e3, 0, np.where(depth < 35e3, 1, np.where(depth < 120e3, 2, 3))).astype(np.int32)
+    T = np.where(depth < 120e3, 273.15 + 1330.0 * depth / 120e3, 273.15 + 1330.0 + 0.3e-3 * (depth - 120e3))
+    rng = np.random.default_rng(seed)
+    R = 8.314510
+
+    def logu(a, b):
+        return float(np.exp(rng.uniform(np.log(a), np.log(b))))
+    # (A range Pa^-n s^-1, Q range J/mol, diffusion A, Q), per phase
+    specs = [((1e-28, 1e-25), (135e3, 225e3), 1e-19, 200e3, 2700.0),
+             ((1e-26, 1e-23), (200e3, 300e3), 1e-20, 250e3, 2900.0),
+             ((1e-17, 1e-15), (480e3, 540e3), 1e-15, 375e3, 3300.0),
+             ((1e-16, 1e-14), (430e3, 480e3), 1e-14, 335e3, 3300.0)]
+    phases = []
+    S, t = sc.S, sc.t
+    for (Ar, Qr, Ad, Qd, rho) in specs:
+        n = float(rng.uniform(3.0, 3.5))
+        A = logu(*Ar)
+        Q = logu(*Qr)
+        phases.append(dict(
+            pwlv=1, npwl=n, Apwl=A * S ** n * t, Qpwl=Q, Vpwl=0.0, mpwl=0.0, rpwl=0.0, fpwl=1.0, apwl=0.0, Fpwl=1.0,
+            pref_pwl=1.0, linv=1, nlin=1.0, Alin=Ad * S * t, Qlin=Qd, Vlin=0.0, mlin=0.0, rlin=0.0, flin=1.0,
+            alin=0.0, Flin=1.0, mu=3e10 / S, bet=1e-11 * S, C=1e7 / S, phi=np.pi / 6, psi=0.0, rho=rho, Slim=1e90,
+            eta_vp=1e21 / sc.eta, n_vp=1.0, gs_ref=1.0, pls_start=0.0, pls_end=1.0))
+    mat = mdz.Materials.from_phases(phases, R=R)
+    prm = mdz.RheoParams.make(dt=1e4 * 365.25 * 24 * 3600 / t, iselastic=0, step=1, eta_avg=0,
+                              mineta=1e19 / sc.eta, maxeta=1e24 / sc.eta, scale_T=1.0, scale_E=sc.E,
+                              scale_S=sc.S, scale_eta=sc.eta, scale_L=sc.L)
+    model = mdz.Model.make(prm, gz=-9.81 * L / S, newton=1, nit_max=15, rel_tol=1e-8, lin_rtol=1e-5,
+                           line_search=1, precision=precision, learned_guess=learned)
+    u, v = pure_shear_velocity(g, eps / sc.E)
+    m = _markers_dict(x, z, ph, T=T)
+    return dict(name="lithosphere", grid=g, markers=m, mat=mat, model=model, u=u, v=v, p=np.zeros(g.size(1)),
+                scales=sc)
+
+
+def config_shear_band(N=2049, nm=4, seed=12345, noise=0.01, precision=64, learned=0):
+    """Shear-band localisation: VEP pure shear with cohesion softening linearly
+    from 1 to 0.5 over accumulated plastic strain 0-1, 1 % seeded cohesion
+    noise, 16 markers per cell."""
+    cfg = config_vep(N=N, nm=nm, seed=seed, noise=noise)
+    import mdz
+    phases = [dict(cstv=1, eta0=1e3, mu=1.0, bet=1e-2, C=1.0, C_end=0.5, coh_soft=1, phi=np.pi / 6, psi=0.0,
+                   rho=1.0, Slim=1e10, eta_vp=0.05, n_vp=1.0, gs_ref=1.0, pls_start=0.0, pls_end=1.0)]
+    cfg["mat"] = mdz.Materials.from_phases(phases)
+    cfg["model"].softening = 1
+    cfg["model"].nit_max = 15
+    cfg["model"].precision = precision
+    cfg["model"].learned_guess = learned
+    cfg["name"] = "shear_band"
+    return cfg
+
+
+def load_context(cfg, max_markers=None):
+    """Context with the configuration's markers, attributes and initial fields resident."""
+    import mdz
+    g, m = cfg["grid"], cfg["markers"]
+    ctx = mdz.Context(g, cfg["mat"].n_phases, max_markers or len(m["x"]))
+    ctx.set_markers(m["x"], m["z"], m["phase"])
+    for attr, key in ((mdz.M_SXXD, "sxxd"), (mdz.M_SZZD, "szzd"), (mdz.M_SXZ, "sxz"), (mdz.M_STRAIN_PL, "strain_pl"),
+                      (mdz.M_STRAIN, "strain"), (mdz.M_T, "T"), (mdz.M_CMUL, "cmul")):
+        ctx.set_marker_attr(attr, m[key])
+    f = mdz.GridFields(g, cfg["mat"].n_phases)
+    f["u"], f["v"], f["p"] = cfg["u"], cfg["v"], cfg["p"]
+    s = f.struct()
+    for name in mdz.FIELD_NAMES:
+        if name not in ("u", "v", "p"):
+            setattr(s, name, None)
+    ctx._check(ctx.L.mdz_sync_fields(ctx.h, mdz.C.byref(s), 1))
+    return ctx
