@@ -72,7 +72,7 @@ struct mdz_solver {
     gcr_space<float> g32;
     double *sc = nullptr;        // host-pinned scalars
     bool ready = false;
-    int nu1 = 2, nu2 = 2;
+    int nu1 = 3, nu2 = 3;
     double omega = 0.7;
 };
 
@@ -308,10 +308,14 @@ __global__ void k_mg_restrict(stokes_geom F, stokes_geom Cg, const T *__restrict
     }
 }
 
-// coarse coefficients: centroid average of the 4 children, vertex injection
+// coarse coefficients: centroid average of the 4 children; vertex full-weighting
+// (1/4, 1/8, 1/16 over the 3 x 3 fine vertices, edge-clamped).  Injection of the
+// vertex viscosity makes the V-cycle diverge at 1e3 contrasts; full weighting
+// keeps it convergent as a preconditioner up to 1e5.
 template <typename T>
-__global__ void k_mg_coarsen(int ncxf, int Nxf, int ncxc, int nczc, int Nxc, int Nzc, const T *__restrict__ D11f,
-                             const T *__restrict__ D33f, T *__restrict__ D11c, T *__restrict__ D33c) {
+__global__ void k_mg_coarsen(int ncxf, int Nxf, int Nzf, int ncxc, int nczc, int Nxc, int Nzc,
+                             const T *__restrict__ D11f, const T *__restrict__ D33f, T *__restrict__ D11c,
+                             T *__restrict__ D33c) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < ncxc * nczc) {
         int I = i % ncxc, J = i / ncxc, a = 2 * I + 2 * J * ncxf;
@@ -319,7 +323,16 @@ __global__ void k_mg_coarsen(int ncxf, int Nxf, int ncxc, int nczc, int Nxc, int
     }
     if (i < Nxc * Nzc) {
         int I = i % Nxc, J = i / Nxc;
-        D33c[i] = D33f[2 * I + 2 * J * Nxf];
+        double s = 0.0;
+        for (int b = -1; b <= 1; b++)
+            for (int a = -1; a <= 1; a++) {
+                int x = 2 * I + a, z = 2 * J + b;
+                x = x < 0 ? 0 : (x > Nxf - 1 ? Nxf - 1 : x);
+                z = z < 0 ? 0 : (z > Nzf - 1 ? Nzf - 1 : z);
+                double w = (a == 0 ? 0.5 : 0.25) * (b == 0 ? 0.5 : 0.25);
+                s += w * (double)D33f[x + z * Nxf];
+            }
+        D33c[i] = (T)s;
     }
 }
 
@@ -547,8 +560,8 @@ static mdz_status mg_setup(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n, con
         if (l > 0) {
             mg_level<T> &P = H.L[l - 1];
             int n = L.Nx * L.Nz;
-            k_mg_coarsen<T><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(P.ncx, P.Nx, L.ncx, L.ncz, L.Nx, L.Nz, P.D11, P.D33,
-                                                                     L.D11, L.D33);
+            k_mg_coarsen<T><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(P.ncx, P.Nx, P.Nz, L.ncx, L.ncz, L.Nx, L.Nz,
+                                                                     P.D11, P.D33, L.D11, L.D33);
             MDZ_LAUNCHED(ctx);
         }
         size_t n = L.nu() > L.nv() ? L.nu() : L.nv();
@@ -849,7 +862,7 @@ mdz_status mdz_dev_solve(mdz_ctx *ctx, const mdz_fields &f, bool newton, int pre
         MDZ_CUDA(ctx, cudaMemsetAsync(dx, 0, sizeof(double) * n, st));
         MDZ_CUDA(ctx, cudaMemcpyAsync(S64.r, F, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
         double *dn = (double *)(ctx->d_counters + 8);
-        double r0 = -1.0;
+        double r0 = -1.0, prev = 1e300;
         for (cycles = 0; cycles < 12; cycles++) {
             // norm of the FP64 defect
             if ((s = dots_launch<double>(ctx, S64, S64.m + 1, 1, S64.r, dn, st)) != MDZ_OK) return s;
@@ -859,13 +872,15 @@ mdz_status mdz_dev_solve(mdz_ctx *ctx, const mdz_fields &f, bool newton, int pre
             if (r0 < 0) r0 = rn;
             rel = r0 > 0 ? rn / r0 : 0.0;
             if (rel <= rtol || r0 == 0.0) break;
+            if (rel > 0.5 * prev || total >= maxit) break;   // refinement stalled or budget spent
+            prev = rel;
             k_convert<double, float><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, S64.r, S32.r);
             MDZ_LAUNCHED(ctx);
             double inner_rtol = rtol / rel;
             if (inner_rtol < 1e-4) inner_rtol = 1e-4;
             if (inner_rtol > 0.1) inner_rtol = 0.1;
-            if ((s = gcr_solve<float>(ctx, S32, SV->mg32, K32, newton, f.eta_n, inner_rtol, maxit, &its, nullptr,
-                                      st)) != MDZ_OK)
+            if ((s = gcr_solve<float>(ctx, S32, SV->mg32, K32, newton, f.eta_n, inner_rtol, maxit - total, &its,
+                                      nullptr, st)) != MDZ_OK)
                 return s;
             total += its;
             k_add_f32<<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, S32.x, dx);
