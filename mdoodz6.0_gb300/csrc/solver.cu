@@ -736,6 +736,38 @@ __global__ void k_convert(size_t n, const Tin *__restrict__ a, Tout *__restrict_
     if (i < n) b[i] = (Tout)a[i];
 }
 
+// Pressure gauge: the decoupled operator annihilates a constant pressure, but
+// the rheology does not (pressure-dependent yield), so every correction is
+// returned with zero mean over the pressure equations.
+__global__ void k_psum(int np, const signed char *__restrict__ tp, const double *__restrict__ p, double *out) {
+    double acc[2] = {0.0, 0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x)
+        if (tp[i] == -1) { acc[0] += p[i]; acc[1] += 1.0; }
+    for (int q = 0; q < 2; q++)
+        for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+    if ((threadIdx.x & 31) == 0) { atomicAdd(&out[0], acc[0]); atomicAdd(&out[1], acc[1]); }
+}
+
+__global__ void k_psub(int np, const signed char *__restrict__ tp, const double *__restrict__ sum,
+                       double *__restrict__ p) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < np && tp[i] == -1 && sum[1] > 0) p[i] -= sum[0] / sum[1];
+}
+
+static mdz_status remove_pressure_mean(mdz_ctx *ctx, double *p, cudaStream_t st) {
+    const mdz_dgrid &g = ctx->g;
+    int np = g.ncx * g.ncz;
+    double *d = (double *)(ctx->d_counters + 24);
+    MDZ_CUDA(ctx, cudaMemsetAsync(d, 0, 2 * sizeof(double), st));
+    int blocks = mdz_blocks(np, 256);
+    if (blocks > 152 * 4) blocks = 152 * 4;
+    k_psum<<<blocks, 256, 0, st>>>(np, g.BCp, p, d);
+    MDZ_LAUNCHED(ctx);
+    k_psub<<<mdz_blocks(np), MDZ_THREADS, 0, st>>>(np, g.BCp, d, p);
+    MDZ_LAUNCHED(ctx);
+    return MDZ_OK;
+}
+
 // dx(FP64) += e(FP32)
 __global__ void k_add_f32(size_t n, const float *__restrict__ e, double *__restrict__ x) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -894,6 +926,7 @@ mdz_status mdz_dev_solve(mdz_ctx *ctx, const mdz_fields &f, bool newton, int pre
             MDZ_LAUNCHED(ctx);
         }
     }
+    if ((s = remove_pressure_mean(ctx, dx + nu + nv, st)) != MDZ_OK) return s;
     if (stats) {
         stats->iterations = total;
         stats->refinements = cycles;

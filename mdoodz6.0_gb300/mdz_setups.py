@@ -153,8 +153,15 @@ def config_lithosphere(Nx=1025, Nz=513, nm=4, seed=12345, precision=64, learned=
                            line_search=1, precision=precision, learned_guess=learned)
     u, v = pure_shear_velocity(g, eps / sc.E)
     m = _markers_dict(x, z, ph, T=T)
-    return dict(name="lithosphere", grid=g, markers=m, mat=mat, model=model, u=u, v=v, p=np.zeros(g.size(1)),
-                scales=sc)
+    # initial pressure: lithostatic column of the layered densities (the
+    # reference starts from ComputeLithostaticPressure as well)
+    zc = g.zc
+    dz = g.dz
+    rho_of = lambda d: np.where(d < 20e3, specs[0][4], np.where(d < 35e3, specs[1][4], specs[2][4]))
+    rho_c = rho_of(-zc * L)
+    col = np.cumsum((rho_c * (-model.gz) * dz)[::-1])[::-1] - 0.5 * rho_c * (-model.gz) * dz
+    p0 = np.repeat(col[:, None], g.ncx, axis=1).ravel()
+    return dict(name="lithosphere", grid=g, markers=m, mat=mat, model=model, u=u, v=v, p=p0, scales=sc)
 
 
 def config_shear_band(N=2049, nm=4, seed=12345, noise=0.01, precision=64, learned=0):
