@@ -179,6 +179,10 @@ typedef struct mdz_rheo_params {
     int eta_avg;            /* 0 arithmetic, 1 harmonic, 2 geometric phase mix   */
     double mineta, maxeta;  /* viscosity limiter                                */
     double scale_T, scale_E, scale_S, scale_eta, scale_L;
+    int clamp_tangent;      /* 0: the reference's tangent, which differentiates the
+                               unlimited viscosity also where the limiter is active;
+                               1: zero tangent where mineta / maxeta clip (the
+                               derivative of the limited law)                       */
 } mdz_rheo_params;
 
 /* Grid fields by the reference's names (grid, SOURCE/header_MDOODZ.h:170-219).
@@ -268,6 +272,30 @@ mdz_status mdz_SolveStokesDefect(mdz_ctx *ctx, mdz_fields *f, int jacobian, int 
                                  const double *Fu, const double *Fv, const double *Fp, double *dxu, double *dxv,
                                  double *dxp, int *iterations, double *rel_residual);
 
+/* Knobs of the defect solve (no counterpart in the reference, whose direct
+ * factorisation has none): V-cycle pre/post Jacobi sweeps nu1 (1..16) and nu2
+ * (0..16), Jacobi damping omega in (0, 2), GCR restart length (2..48), the
+ * number of Krylov iterations between host-side convergence checks (1..64), and
+ * mg_jacobian = 1 to build the multigrid hierarchy of a Newton solve from the
+ * Jacobian's velocity block instead of the Picard block.
+ * Defaults 3, 3, 0.7, 30, 4, 0. */
+mdz_status mdz_set_solver_options(mdz_ctx *ctx, int nu1, int nu2, double omega, int restart, int check,
+                                  int mg_jacobian);
+
+/* Multigrid stencils of one level after a solve (diagnostics and tests; no
+ * counterpart in the reference).  31 coefficient planes per velocity row,
+ * structure of arrays: su[31][Nx*(Nz+1)] for Vx rows, sv[31][(Nx+1)*Nz] for Vz
+ * rows.  Vx row (k, l): planes 0..14 couple Vx (k+dk, l+dl), dk in -1..1,
+ * dl in -2..2, plane (dk+1) + 3 (dl+2); planes 15..30 couple Vz (k+di, l+dj),
+ * di in -1..2, dj in -2..1, plane 15 + (di+1) + 4 (dj+2).  Vz row (i, j):
+ * planes 0..14 couple Vz (i+di, j+dj), di in -2..2, dj in -1..1, plane
+ * (di+2) + 5 (dj+1); planes 15..30 couple Vx (i+dk, j+dl), dk in -2..1,
+ * dl in -1..2, plane 15 + (dk+2) + 4 (dl+1).  Level 0 is the fine operator
+ * (times the cell volume), level l > 0 the Galerkin product R A P.  su / sv may
+ * be NULL to query the sizes and the number of levels. */
+mdz_status mdz_mg_stencils(mdz_ctx *ctx, int precision, int level, int *levels, int *Nx, int *Nz, double *su,
+                           double *sv);
+
 /* ---- resident state and the whole time step ------------------------------- */
 
 /* Per-marker attributes kept on the device next to x, z, phase (the marker
@@ -301,6 +329,15 @@ typedef struct mdz_model {
     int itp_stencil;        /* 1 or 9                                                        */
     int softening;          /* 0: smooth erfc law (reference); 1: linear law                 */
     int advect;             /* 1: update marker stress/strain and advect (RK4)               */
+    /* Picard -> Newton switch of Main_DOODZ.c:728-743: with picard2newton = 1 the
+     * step starts with Picard iterations and switches to the Jacobian once resx
+     * or resz fell below pic2newt_cond times its first value, or after
+     * nit_pic_max iterations (Nparams.Picard2Newton, Pic2NewtCond, nit_Pic_max). */
+    int picard2newton;
+    double pic2newt_cond;
+    int nit_pic_max;
+    int newton_maxit;       /* Krylov cap of a Jacobian solve before the Picard operator takes
+                               that iteration over (0: lin_maxit)                              */
 } mdz_model;
 
 typedef struct mdz_step_report {
@@ -309,6 +346,7 @@ typedef struct mdz_step_report {
     double res0[3], res[3];           /* first and final resx, resz, resp                    */
     long long local_solves, local_fallbacks, local_failures;
     double ms_projection, ms_rheology, ms_residual, ms_solve, ms_line_search, ms_markers, ms_total;
+    int newton_its;                   /* iterations solved with the Jacobian                  */
 } mdz_step_report;
 
 /* One time step of Main_DOODZ.c's loop (SOURCE/Main_DOODZ.c:459-1320) on the
@@ -328,8 +366,9 @@ mdz_status mdz_sync(mdz_ctx *ctx);
 /* Launch timing of the main kernel classes with CUDA events on the context's
  * stream (off by default; turning it on or off resets the totals).  Classes:
  * 0 local rheology, 1 Stokes operator apply inside the Krylov solver,
- * 2 multigrid smoothing, 3 projection.  Returns the summed time (ms), the
- * summed algorithmic bytes and the number of launches of one class. */
+ * 2 multigrid V-cycle (the whole preconditioner application), 3 projection,
+ * 4 learned-guess inference.  Returns the summed time (ms), the summed
+ * algorithmic bytes and the number of launches of one class. */
 mdz_status mdz_set_profiling(mdz_ctx *ctx, int on);
 mdz_status mdz_kernel_timing(mdz_ctx *ctx, int kernel_class, double *ms, double *bytes, long long *launches);
 

@@ -112,10 +112,12 @@ extern "C" mdz_status mdz_create(mdz_ctx **out, const mdz_grid_desc *d, int n_ph
 
 void mdz_free_fields(mdz_ctx *ctx);
 void mdz_solver_free(mdz_ctx *ctx);
+void mdz_mlp_free(mdz_ctx *ctx);
 
 extern "C" void mdz_destroy(mdz_ctx *ctx) {
     if (!ctx) return;
     mdz_solver_free(ctx);
+    mdz_mlp_free(ctx);
     mdz_free_fields(ctx);
     mdz_dgrid &g = ctx->g;
     void *ptrs[] = {g.xg, g.zg, g.xc, g.zc, g.xvz, g.zvx, g.BCu, g.BCv, g.BCp, g.BCg, g.BCu_val, g.BCv_val,

@@ -7,7 +7,8 @@
 #include "mdoodz_gpu.h"
 
 // kernel classes timed when profiling is on
-enum { MDZ_PROF_VISCOSITY = 0, MDZ_PROF_STOKES_APPLY = 1, MDZ_PROF_MG_SMOOTH = 2, MDZ_PROF_P2G = 3, MDZ_PROF_NCLS = 4 };
+enum { MDZ_PROF_VISCOSITY = 0, MDZ_PROF_STOKES_APPLY = 1, MDZ_PROF_MG_SMOOTH = 2, MDZ_PROF_P2G = 3, MDZ_PROF_MLP = 4,
+       MDZ_PROF_NCLS = 5 };
 struct mdz_ctx;
 void mdz_prof_begin(mdz_ctx *ctx, int cls, cudaStream_t st, cudaEvent_t *ev);
 void mdz_prof_end(mdz_ctx *ctx, int cls, double bytes, cudaStream_t st, cudaEvent_t a);
@@ -64,6 +65,7 @@ struct mdz_ctx {
     double prof_ms[8] = {0}, prof_bytes[8] = {0};
     long long prof_n[8] = {0};
     struct mdz_solver *solver = nullptr;   // Krylov / multigrid workspace (solver.cu)
+    struct mdz_mlp *mlp = nullptr;         // learned local-rheology guess (mlp.cu)
     std::string err;
     // host-call staging buffers (grown on demand)
     void *stage[8] = {nullptr};
@@ -229,8 +231,12 @@ mdz_status mdz_dev_strain_rates(mdz_ctx *ctx, const mdz_fields &f, cudaStream_t 
 mdz_status mdz_dev_c2v(mdz_ctx *ctx, const double *cen, double *ver, cudaStream_t st);
 mdz_status mdz_dev_v2c(mdz_ctx *ctx, double *cen, const double *ver, cudaStream_t st);
 mdz_status mdz_check_materials(mdz_ctx *ctx, const mdz_materials *m);
+// Local rheology on centroids and vertices.  d_counters: [0] local solves not
+// converged, [1] learned starts that fell back to the plain solve, [2] learned
+// starts.  learned: every local solve starts from the MLP's guess (weights
+// loaded in the context) and the plain solve reruns where the polish fails.
 mdz_status mdz_dev_viscosity(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm, const mdz_fields &f,
-                             int *d_fail, cudaStream_t st);
+                             int *d_counters, cudaStream_t st, bool learned = false);
 mdz_status mdz_dev_operators(mdz_ctx *ctx, const mdz_rheo_params *prm, const mdz_fields &f, int jacobian,
                              cudaStream_t st);
 mdz_status mdz_dev_rhs(mdz_ctx *ctx, const mdz_rheo_params *prm, double gx, double gz, const mdz_fields &f,

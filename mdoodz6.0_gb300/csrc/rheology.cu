@@ -13,6 +13,7 @@
 // Isotropic, incompressible, non-reactive subset; the host rejects the rest.
 #include <cmath>
 #include "mdz_internal.cuh"
+#include "mlp.cuh"
 
 
 #define ZEROC 273.15
@@ -98,15 +99,21 @@ struct visc_res {
     double Exx_el, Ezz_el, Exz_el, Exx_diss, Ezz_diss, Exz_diss, d1;
     double detadexx, detadezz, detadexz, detadp, X1, OverS;
     double ddivpdexx, ddivpdezz, ddivpdexz, ddivpdp, Pcorr, div_el, div_pl;
+    double eta_ve, gdot;    // converged local unknowns (training labels of the learned guess)
     int ve_fail, vp_fail, ve_its, vp_its;
+    int learned, fallback;  // started from a learned guess; polish failed and the plain solve reran
 };
+
+// Polish budget of a learned start: Newton-type updates allowed before the
+// plain solve takes over.
+#define MDZ_POLISH_STEPS 2
 
 __device__ __forceinline__ double dmin(double a, double b) { return a <= b ? a : b; }
 
 __device__ void visc_local(int p, double G, double T, double P, double d, double phi, double X0, double Exx,
                            double Ezz, double Exz, double Gxx, double Gzz, double Gxz, double Txx0, double Tzz0,
                            double Txz0, const mdz_materials &m, const mdz_rheo_params &prm, double dil, double fric,
-                           double C, double P0, double beta, visc_res &o) {
+                           double C, double P0, double beta, visc_res &o, const float *guess = nullptr) {
     const double R = m.R, dt = prm.dt, tol = 1.0e-11;
     const int nitmax = 20;
     int elastic = prm.iselastic, it;
@@ -160,7 +167,42 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     // local Newton on the visco-elastic viscosity
     double eta_ve = eta_up, Tii;
     const double dm_lin = pow(o.d1, -m_lin);
-    for (it = 0; it < nitmax; it++) {
+    bool ve_done = false;
+    o.learned = guess != nullptr;
+    o.fallback = 0;
+    if (guess) {
+        // Learned start s = log(eta_ve), polished by Halley steps on
+        // g(s) = log(sum of the strain rates) - log(Eii): every mechanism's
+        // rate is c_k exp(n_k s), so g' and g'' are rate-weighted means of n_k
+        // and n_k^2.  Converged means the reference's own test below holds.
+        double s = (double)guess[0];
+        for (it = 0; it <= MDZ_POLISH_STEPS; it++) {
+            eta_ve = exp(s);
+            Tii = 2.0 * f_ani * eta_ve * Eii;
+            const double Eel = elastic ? Tii / (2.0 * eta_el) : 0.0;
+            if (constant) Eii_cst = Tii / f_ani / 2.0 / eta_cst;
+            if (dislocation) Eii_pwl = C_pwl * pow(Tii, n_pwl);
+            if (diffusion) Eii_lin = C_lin * pow(Tii, n_lin) * dm_lin;
+            double r = Eii - elastic * Tii / (2.0 * eta_el) - (Eii_pwl + Eii_lin + Eii_cst);
+            res = fabs(r / Eii);
+            if (res < tol / 100) { ve_done = true; break; }
+            if (it == MDZ_POLISH_STEPS) break;
+            const double S0 = Eel + Eii_pwl + Eii_lin + Eii_cst;
+            const double S1 = Eel + n_pwl * Eii_pwl + n_lin * Eii_lin + Eii_cst;
+            const double S2 = Eel + n_pwl * n_pwl * Eii_pwl + n_lin * n_lin * Eii_lin + Eii_cst;
+            if (!(S0 > 0.0)) break;
+            const double g = log(S0 / Eii), g1 = S1 / S0, g2 = S2 / S0 - g1 * g1;
+            const double den = 2.0 * g1 * g1 - g * g2;
+            s -= den > 0.0 ? 2.0 * g * g1 / den : g / g1;
+        }
+        o.ve_its = it;
+        if (!ve_done) {
+            o.fallback = 1;
+            eta_ve = eta_up;
+            Eii_pwl = 0; Eii_lin = 0; Eii_cst = 0;
+        }
+    }
+    for (it = 0; !ve_done && it < nitmax; it++) {
         Tii = 2.0 * f_ani * eta_ve * Eii;
         if (constant) Eii_cst = Tii / f_ani / 2.0 / eta_cst;
         if (dislocation) Eii_pwl = C_pwl * pow(Tii, n_pwl);
@@ -175,8 +217,11 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
         if (constant) dfdeta += -Eii / eta_cst;
         eta_ve -= r / dfdeta;
     }
-    o.ve_its = it;
-    if (it == nitmax - 1 && res > tol) o.ve_fail = 1;
+    if (!ve_done) {
+        o.ve_its = it;
+        if (it == nitmax - 1 && res > tol) o.ve_fail = 1;
+    }
+    o.eta_ve = eta_ve;
     Tii = 2.0 * eta_ve * f_ani * Eii;
     double Txx = Gxx * Tii / f_ani / Eii, Tzz = Gzz * Tii / f_ani / Eii, Txz = Gxz * Tii / f_ani / Eii;
     double Exx_lin = 0, Ezz_lin = 0, Exz_lin = 0, Exx_cst = 0, Ezz_cst = 0, Exz_cst = 0;
@@ -210,7 +255,34 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
         gdot = F_trial / (eta_ve + eta_vp + K * dt * sin_fric * sin_dil);
         dQdtxx = Txx / 2.0 / Tii; dQdtzz = Tzz / 2.0 / Tii; dQdtxz = Txz / 1.0 / Tii;
         const double F_trial0 = F_trial;
-        for (it = 0; it < nitmax; it++) {
+        bool vp_done = false;
+        if (guess) {
+            // learned start: gdot = fraction * 2 Eii, at most MDZ_POLISH_STEPS
+            // Newton updates, the reference's own convergence test
+            double frac = (double)guess[1];
+            frac = frac > 1e-6 ? (frac < 1.0 ? frac : 1.0) : 1e-6;
+            const double gdot_plain = gdot;
+            gdot = frac * 2.0 * Eii;
+            for (it = 0; it <= MDZ_POLISH_STEPS; it++) {
+                dQdP = -sin_dil;
+                divp = -gdot * dQdP;
+                Pc = P + K * dt * divp;
+                eta_vp = eta_vp0 * pow(fabs(gdot), 1.0 / n_vp - 1.0);
+                Tyield = C * cos_fric + Pc * sin_fric + gdot * eta_vp;
+                F_trial = Tii - eta_ve * gdot - Tyield;
+                res = fabs(F_trial);
+                if (res < tol || res / F_trial0 < tol) { vp_done = true; break; }
+                if (it == MDZ_POLISH_STEPS) break;
+                double dFdgdot = -eta_ve - eta_vp / n_vp - K * dt * sin_fric * sin_dil;
+                gdot -= F_trial / dFdgdot;
+            }
+            o.vp_its = it;
+            if (!vp_done) {
+                o.fallback = 1;
+                gdot = gdot_plain;
+            }
+        }
+        for (it = 0; !vp_done && it < nitmax; it++) {
             dQdP = -sin_dil;
             divp = -gdot * dQdP;
             Pc = P + K * dt * divp;
@@ -222,8 +294,10 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
             double dFdgdot = -eta_ve - eta_vp / n_vp - K * dt * sin_fric * sin_dil;
             gdot -= F_trial / dFdgdot;
         }
-        o.vp_its = it;
-        if (it == nitmax - 1 && (res > tol || res / F_trial0 > tol)) o.vp_fail = 1;
+        if (!vp_done) {
+            o.vp_its = it;
+            if (it == nitmax - 1 && (res > tol || res / F_trial0 > tol)) o.vp_fail = 1;
+        }
         Txx = 2.0 * eta_ve * (Exx - gdot * dQdtxx);
         Tzz = 2.0 * eta_ve * (Ezz - gdot * dQdtzz);
         double Tyy = -(Txx + Tzz);
@@ -253,6 +327,7 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
         dvep_dExz = -Exz * Tyield / E3 + (a * dlamdExz + gdot * dvp_dExz + gdot * K * dt * sin_fric * 0.0) / (2.0 * Eii);
         dvep_dP = (sin_fric + a * dlamdP + gdot * dvp_dP + gdot * K * dt * sin_fric * 0.0) / (2.0 * Eii);
     }
+    o.gdot = gdot;
     double inv_eta_diss = 0.0;
     if (dislocation) inv_eta_diss += 1.0 / eta_pwl;
     if (diffusion) inv_eta_diss += 1.0 / eta_lin;
@@ -291,8 +366,12 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     o.txx = Txx; o.tzz = Tzz; o.txz = Txz;
     if (eta > prm.maxeta) eta = prm.maxeta;
     if (eta < prm.mineta) eta = prm.mineta;
+    const bool clamped = o.etaVE > prm.maxeta || o.etaVE < prm.mineta;
     if (o.etaVE > prm.maxeta) o.etaVE = prm.maxeta;
     if (o.etaVE < prm.mineta) o.etaVE = prm.mineta;
+    if (clamped && prm.clamp_tangent) {   // the limiter is flat: its tangent is zero
+        o.detadexx = 0.0; o.detadezz = 0.0; o.detadexz = 0.0; o.detadp = 0.0;
+    }
     o.eta = eta;
 }
 
@@ -317,9 +396,25 @@ __device__ __forceinline__ void put(double *p, int i, double v) {
     if (p) p[i] = v;
 }
 
+// Counters of the local solves: [0] not converged, [1] learned starts whose
+// polish failed (plain solve rerun), [2] learned starts; warp-aggregated.
+__device__ __forceinline__ void count_local(int *counters, int fails, int fallbacks, int learned) {
+    if (!counters) return;
+    const unsigned mask = __activemask();
+    const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
+    const int a = __reduce_add_sync(mask, fails), b = __reduce_add_sync(mask, fallbacks),
+              c = __reduce_add_sync(mask, learned);
+    if (lane == leader) {
+        if (a) atomicAdd(&counters[0], a);
+        if (b) atomicAdd(&counters[1], b);
+        if (c) atomicAdd(&counters[2], c);
+    }
+}
+
 // One thread per centroid: loop over phases with a fraction above 1e-13.
 __global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_materials m, mdz_rheo_params prm,
-                                                             mdz_fields f, int *__restrict__ fail_count) {
+                                                             mdz_fields f, int *__restrict__ counters,
+                                                             const float2 *__restrict__ guess) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     int nc = g.ncx * g.ncz;
     if (c >= nc) return;
@@ -327,7 +422,7 @@ __global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_ma
     double eta = 0, eta_phys = 0, VE = 0, sxx = 0, szz = 0, sxz = 0, eel = 0, epl = 0, epwl = 0, elin = 0, ecst = 0,
            dn = 0, xel = 0, xdi = 0, zel = 0, zdi = 0, dexx = 0, dezz = 0, dgxz = 0, dp = 0, vxx = 0, vzz = 0,
            vxz = 0, vp = 0, pc = 0, del = 0, dpl = 0, Wt = 0, We = 0, Wd = 0, X = 0, OS = 0;
-    int fails = 0;
+    int fails = 0, fallbacks = 0, learned = 0;
     signed char t = g.BCp[c];
     if (t != 30 && t != 31) {
         const double etae = prm.iselastic == 1 ? prm.dt * f.mu_n[c] : 1.0;
@@ -342,9 +437,16 @@ __global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_ma
             double w = f.phase_perc_n[(size_t)p * nc + c];
             if (!(fabs(w) > 1.0e-13)) continue;
             visc_res o;
+            float gs[2];
+            if (guess) {
+                const float2 q = guess[(size_t)p * nc + c];
+                gs[0] = q.x; gs[1] = q.y;
+            }
             visc_local(p, mu, T, P, d0, phi0, X0, E[0], E[1], E[2], E[3], E[4], E[5], sxx0, szz0, sxz0, m, prm, dil,
-                       fric, Coh, P0, bet, o);
+                       fric, Coh, P0, bet, o, guess ? gs : nullptr);
             fails += o.ve_fail + o.vp_fail;
+            fallbacks += o.fallback;
+            learned += o.learned;
             if (avg == 0) {
                 eta += w * o.etaVE; eta_phys += w * o.eta; dexx += w * o.detadexx; dezz += w * o.detadezz;
                 dgxz += w * o.detadexz / 2.0; dp += w * o.detadp;
@@ -394,18 +496,19 @@ __global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_ma
     put(f.ddivpdexx_n, c, vxx); put(f.ddivpdezz_n, c, vzz); put(f.ddivpdgxz_n, c, vxz); put(f.ddivpdp_n, c, vp);
     put(f.p_corr, c, pc); put(f.div_u_el, c, del); put(f.div_u_pl, c, dpl); put(f.div_u_r, c, 0.0);
     put(f.Wtot, c, Wt); put(f.Wel, c, We); put(f.Wdiss, c, Wd); put(f.X_n, c, X); put(f.OverS_n, c, OS);
-    if (fails && fail_count) atomicAdd(fail_count, fails);
+    count_local(counters, fails, fallbacks, learned);
 }
 
 __global__ void __launch_bounds__(128) k_viscosity_vertices(mdz_dgrid g, mdz_materials m, mdz_rheo_params prm,
-                                                            mdz_fields f, int *__restrict__ fail_count) {
+                                                            mdz_fields f, int *__restrict__ counters,
+                                                            const float2 *__restrict__ guess) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     int nv = g.Nx * g.Nz;
     if (c >= nv) return;
     const int avg = prm.eta_avg, nph = m.n_phases;
     double VE = 0, sxz = 0, eta_phys = 0, eta = 0, zel = 0, zdi = 0, dexx = 0, dezz = 0, dgxz = 0, dp = 0, X = 0,
            OS = 0;
-    int fails = 0;
+    int fails = 0, fallbacks = 0, learned = 0;
     if (g.BCg[c] != 30) {
         const double etae = prm.iselastic == 1 ? prm.dt * f.mu_s[c] : 1.0;
         const double sxx0 = f.sxxd0_s[c], szz0 = f.szzd0_s[c], sxz0 = f.sxz0[c];
@@ -418,9 +521,16 @@ __global__ void __launch_bounds__(128) k_viscosity_vertices(mdz_dgrid g, mdz_mat
             double w = f.phase_perc_s[(size_t)p * nv + c];
             if (!(fabs(w) > 1.0e-13)) continue;
             visc_res o;
+            float gs[2];
+            if (guess) {
+                const float2 q = guess[(size_t)p * nv + c];
+                gs[0] = q.x; gs[1] = q.y;
+            }
             visc_local(p, mu, T, P, d0, phi0, X0, E[0], E[1], E[2], E[3], E[4], E[5], sxx0, szz0, sxz0, m, prm, dil,
-                       fric, Coh, P0, bet, o);
+                       fric, Coh, P0, bet, o, guess ? gs : nullptr);
             fails += o.ve_fail + o.vp_fail;
+            fallbacks += o.fallback;
+            learned += o.learned;
             if (avg == 0) {
                 eta += w * o.etaVE; eta_phys += w * o.eta; dexx += w * o.detadexx; dezz += w * o.detadezz;
                 dgxz += w * o.detadexz / 2.0; dp += w * o.detadp;
@@ -453,7 +563,7 @@ __global__ void __launch_bounds__(128) k_viscosity_vertices(mdz_dgrid g, mdz_mat
     put(f.exz_el, c, zel); put(f.exz_diss, c, zdi);
     put(f.detadexx_s, c, dexx); put(f.detadezz_s, c, dezz); put(f.detadgxz_s, c, dgxz); put(f.detadp_s, c, dp);
     put(f.X_s, c, X); put(f.OverS_s, c, OS);
-    if (fails && fail_count) atomicAdd(fail_count, fails);
+    count_local(counters, fails, fallbacks, learned);
 }
 
 // ---------------------------------------------------------------------------
@@ -597,8 +707,138 @@ mdz_status mdz_check_materials(mdz_ctx *ctx, const mdz_materials *m) {
     return MDZ_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Learned guess: per (node, phase) MLP inference, one warp per 32 nodes and a
+// warp-synchronous tensor-core pass per phase present in the warp.
+__device__ __forceinline__ double eii_of(const double *E, const mdz_rheo_params &prm) {
+    const double Eyy = -(E[0] + E[1]);
+    double Eii = sqrt(0.5 * (E[0] * E[0] + E[1] * E[1] + Eyy * Eyy) + E[2] * E[2]);
+    if (Eii * prm.scale_E < 1e-30) Eii = 1e-30 / prm.scale_E;
+    return Eii;
+}
+
+template <bool CENT>
+__global__ void __launch_bounds__(256) k_mlp_guess(mdz_dgrid g, int nph, mdz_rheo_params prm, mdz_fields f,
+                                                   mdz_mlp_norm nm, const unsigned char *__restrict__ packed,
+                                                   float2 *__restrict__ guess) {
+    extern __shared__ __align__(16) unsigned char sm[];
+    __nv_bfloat16 *XS = reinterpret_cast<__nv_bfloat16 *>(sm + MLP_PACK_BYTES);
+    float *YS = reinterpret_cast<float *>(XS + 8 * 32 * MLP_S1);
+    mlp_load_weights(sm, packed);
+    for (int i = threadIdx.x; i < 8 * 32 * MLP_S1; i += blockDim.x) XS[i] = __float2bfloat16_rn(0.f);
+    __syncthreads();
+    const mlp_w W = mlp_views(sm);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __nv_bfloat16 *xs = XS + warp * 32 * MLP_S1;
+    float *ys = YS + warp * 64;
+    const int nn = CENT ? g.ncx * g.ncz : g.Nx * g.Nz;
+    for (int base = (blockIdx.x * 8 + warp) * 32; base < nn; base += gridDim.x * 8 * 32) {
+        const int c = base + lane;
+        bool act = c < nn;
+        if (act) act = CENT ? (g.BCp[c] != 30 && g.BCp[c] != 31) : (g.BCg[c] != 30);
+        double Eii = 1.0 / prm.scale_E, T = ZEROC / prm.scale_T, P = 0.0;
+        if (act) {
+            double E[6];
+            if (CENT) {
+                const double etae = prm.iselastic == 1 ? prm.dt * f.mu_n[c] : 1.0;
+                eff_rates(f.exxd[c], f.ezzd[c], f.exz_n[c], f.sxxd0[c], f.szzd0[c], f.sxz0_n[c], etae, E);
+                T = f.T[c];
+                P = f.p[c];
+            } else {
+                const double etae = prm.iselastic == 1 ? prm.dt * f.mu_s[c] : 1.0;
+                eff_rates(f.exxd_s[c], f.ezzd_s[c], f.exz[c], f.sxxd0_s[c], f.szzd0_s[c], f.sxz0[c], etae, E);
+                T = f.T_s[c];
+                P = f.P_s[c];
+            }
+            Eii = eii_of(E, prm);
+            if (T < ZEROC / prm.scale_T) T = ZEROC / prm.scale_T;
+        }
+        for (int p = 0; p < nph; p++) {
+            const double w = act ? (CENT ? f.phase_perc_n[(size_t)p * nn + c] : f.phase_perc_s[(size_t)p * nn + c]) : 0.0;
+            const bool need = act && fabs(w) > 1.0e-13;
+            if (!__any_sync(0xffffffffu, need)) continue;
+            float x[8];
+            mlp_inputs(nm, prm, Eii, T, P, prm.dt, p, x);
+            *reinterpret_cast<uint4 *>(xs + lane * MLP_S1) =
+                make_uint4(mlp_pack2(x[0], x[1]), mlp_pack2(x[2], x[3]), mlp_pack2(x[4], x[5]), mlp_pack2(x[6], x[7]));
+            __syncwarp();
+            mlp_warp_infer(W, xs, ys);
+            __syncwarp();
+            if (need) guess[(size_t)p * nn + c] = mlp_to_guess(ys[2 * lane], ys[2 * lane + 1], prm);
+            __syncwarp();
+        }
+    }
+}
+
+mdz_status mdz_dev_mlp_guess(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm, const mdz_fields &f,
+                             float2 *guess_n, float2 *guess_s, cudaStream_t st) {
+    const mdz_dgrid &g = ctx->g;
+    const int nc = g.ncx * g.ncz, nv = g.Nx * g.Nz;
+    const size_t smem = MLP_PACK_BYTES + 8 * 32 * MLP_S1 * 2 + 8 * 64 * 4;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    auto grid = [&](int n) { int b = (n + 255) / 256; return b < 4 * sms ? (b < 1 ? 1 : b) : 4 * sms; };
+    cudaEvent_t ev;
+    mdz_prof_begin(ctx, MDZ_PROF_MLP, st, &ev);
+    k_mlp_guess<true><<<grid(nc), 256, smem, st>>>(g, m->n_phases, *prm, f, ctx->mlp->norm, ctx->mlp->packed, guess_n);
+    MDZ_LAUNCHED(ctx);
+    k_mlp_guess<false><<<grid(nv), 256, smem, st>>>(g, m->n_phases, *prm, f, ctx->mlp->norm, ctx->mlp->packed, guess_s);
+    MDZ_LAUNCHED(ctx);
+    // per node: 6 FP64 rate/stress inputs, mu, T, P, the phase fractions, the tag; one float2 per phase out
+    const double bytes = (double)(nc + nv) * (8.0 * (9 + m->n_phases) + 1 + 8.0 * m->n_phases);
+    mdz_prof_end(ctx, MDZ_PROF_MLP, bytes, st, ev);
+    return MDZ_OK;
+}
+
+// Training tuples: (strain rate, T, P, dt, phase) drawn from the ranges with a
+// counter-based generator, labelled by the plain local solve.
+__device__ __forceinline__ double mlp_u01(unsigned long long seed, long long i, int k) {
+    unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (unsigned long long)(5 * i + k + 1);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+}
+
+__global__ void __launch_bounds__(128) k_mlp_samples(long long n, unsigned long long seed, mdz_materials m,
+                                                     mdz_rheo_params prm, double lo0, double hi0, double lo1,
+                                                     double hi1, double lo2, double hi2, double lo3, double hi3,
+                                                     mdz_mlp_norm nm, uint4 *__restrict__ X, float2 *__restrict__ Y) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double Eii = pow(10.0, lo0 + (hi0 - lo0) * mlp_u01(seed, i, 0)) / prm.scale_E;
+    double T = (lo1 + (hi1 - lo1) * mlp_u01(seed, i, 1)) / prm.scale_T;
+    const double P = (lo2 + (hi2 - lo2) * mlp_u01(seed, i, 2)) / prm.scale_S;
+    const double dt = pow(10.0, lo3 + (hi3 - lo3) * mlp_u01(seed, i, 3)) * prm.scale_E;
+    int ph = (int)(mlp_u01(seed, i, 4) * m.n_phases);
+    if (ph > m.n_phases - 1) ph = m.n_phases - 1;
+    mdz_rheo_params q = prm;
+    q.dt = dt;
+    if (T < ZEROC / q.scale_T) T = ZEROC / q.scale_T;
+    visc_res o;
+    visc_local(ph, m.mu[ph], T, P, m.gs_ref[ph], 0.0, 0.0, Eii, -Eii, 0.0, Eii, -Eii, 0.0, 0.0, 0.0, 0.0, m, q,
+               m.psi[ph], m.phi[ph], m.C[ph], P, m.bet[ph], o);
+    float2 lab = mlp_labels(o.eta_ve, o.gdot, Eii, q);
+    lab.x = fminf(fmaxf(lab.x, -4.f), 8.f);
+    lab.y = fminf(fmaxf(lab.y, 0.f), 1.f);
+    float x[8];
+    mlp_inputs(nm, q, Eii, T, P, dt, ph, x);
+    X[i] = make_uint4(mlp_pack2(x[0], x[1]), mlp_pack2(x[2], x[3]), mlp_pack2(x[4], x[5]), mlp_pack2(x[6], x[7]));
+    Y[i] = lab;
+}
+
+mdz_status mdz_dev_mlp_samples(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm, long long n,
+                               unsigned long long seed, const double lo[4], const double hi[4],
+                               const mdz_mlp_norm &norm, uint4 *X, float2 *Y, cudaStream_t st) {
+    k_mlp_samples<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, seed, *m, *prm, lo[0], hi[0], lo[1], hi[1], lo[2],
+                                                                hi[2], lo[3], hi[3], norm, X, Y);
+    MDZ_LAUNCHED(ctx);
+    return MDZ_OK;
+}
+
 mdz_status mdz_dev_viscosity(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm, const mdz_fields &f,
-                             int *d_fail, cudaStream_t st) {
+                             int *d_counters, cudaStream_t st, bool learned) {
     const mdz_dgrid &g = ctx->g;
     int nc = g.ncx * g.ncz, nv = g.Nx * g.Nz;
     // vertex copies of centroid fields (NonNewtonianViscosityGrid :979-983)
@@ -608,11 +848,19 @@ mdz_status mdz_dev_viscosity(mdz_ctx *ctx, const mdz_materials *m, const mdz_rhe
     if ((s = mdz_dev_c2v(ctx, f.p, f.P_s, st)) != MDZ_OK) return s;
     if ((s = mdz_dev_c2v(ctx, f.d0_n, f.d0_s, st)) != MDZ_OK) return s;
     if ((s = mdz_dev_c2v(ctx, f.phi0_n, f.phi0_s, st)) != MDZ_OK) return s;
+    const float2 *guess_n = nullptr, *guess_s = nullptr;
+    if (learned) {
+        float2 *buf = mdz_mlp_guess_buffer(ctx, (size_t)m->n_phases * (nc + nv));
+        if (!buf) return mdz_fail(ctx, MDZ_ERR_CUDA, "learned guess: buffer allocation failed");
+        if ((s = mdz_dev_mlp_guess(ctx, m, prm, f, buf, buf + (size_t)m->n_phases * nc, st)) != MDZ_OK) return s;
+        guess_n = buf;
+        guess_s = buf + (size_t)m->n_phases * nc;
+    }
     cudaEvent_t ev;
     mdz_prof_begin(ctx, MDZ_PROF_VISCOSITY, st, &ev);
-    k_viscosity_centroids<<<mdz_blocks(nc, 128), 128, 0, st>>>(g, *m, *prm, f, d_fail);
+    k_viscosity_centroids<<<mdz_blocks(nc, 128), 128, 0, st>>>(g, *m, *prm, f, d_counters, guess_n);
     MDZ_LAUNCHED(ctx);
-    k_viscosity_vertices<<<mdz_blocks(nv, 128), 128, 0, st>>>(g, *m, *prm, f, d_fail);
+    k_viscosity_vertices<<<mdz_blocks(nv, 128), 128, 0, st>>>(g, *m, *prm, f, d_counters, guess_s);
     MDZ_LAUNCHED(ctx);
     // algorithmic bytes: per centroid 17 + n_phases FP64 inputs and 35 outputs,
     // per vertex 17 + n_phases inputs and 12 outputs, plus the tags

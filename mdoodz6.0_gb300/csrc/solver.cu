@@ -24,6 +24,9 @@
 #include "solver.cuh"
 
 #define MG_MAX_LEVELS 16
+#define MG_DENSE_MAX 256
+#define MG_NST 31        // stencil coefficients per velocity row (15 same-component + 16 cross)
+#define MG_CENTER 7      // plane of the diagonal entry in both layouts
 #define GCR_MAX_M 48
 
 // ---------------------------------------------------------------------------
@@ -33,14 +36,24 @@ struct mg_level {
     double dx = 0, dz = 0;
     signed char *BCu = nullptr, *BCv = nullptr, *BCp = nullptr, *BCg = nullptr;
     bool own_tags = false;
-    T *D11 = nullptr, *D33 = nullptr;           // Picard: D11 = D22 = 2 eta_n; D33 = eta_s
+    T *D11 = nullptr, *D33 = nullptr;           // level 0 (Picard): D11 = D22 = 2 eta_n; D33 = eta_s
+    // 31-point stencils of the velocity block (MG_NST coefficient planes per
+    // component, structure of arrays): level 0 probed from the re-discretised
+    // operator, coarser levels the Galerkin product R A P of the level above.
+    T *su = nullptr, *sv = nullptr;
+    T *pz = nullptr;                            // level 0: zero pressure vector for Newton probes
     T *xu = nullptr, *xv = nullptr, *yu = nullptr, *yv = nullptr;
     T *fu = nullptr, *fv = nullptr, *ru = nullptr, *rv = nullptr;
     T *idu = nullptr, *idv = nullptr;
     T *cg[8] = {nullptr};                       // coarsest-level CG workspace
+    // coarsest level with at most MG_DENSE_MAX unknowns: explicit inverse
+    int ndense = 0;
+    int *dmap = nullptr;                        // dense index -> u index, or nu + v index
+    double *Awork = nullptr;                    // 2 ndense^2 FP64: [A | I] for Gauss-Jordan
+    T *AinvT = nullptr;                         // inverse, column-major
     size_t nu() const { return (size_t)Nx * (Nz + 1); }
     size_t nv() const { return (size_t)(Nx + 1) * Nz; }
-    stokes_geom geom() const { return stokes_geom{Nx, Nz, ncx, ncz, dx, dz, BCu, BCv, BCp, BCg}; }
+    stokes_geom geom() const { return make_geom(Nx, Nz, dx, dz, BCu, BCv, BCp, BCg); }
     stokes_coefs<T> coefs() const {
         return stokes_coefs<T>{D11, nullptr, nullptr, nullptr, nullptr, D11, nullptr, nullptr,
                                nullptr, nullptr, D33, nullptr};
@@ -62,6 +75,8 @@ struct gcr_space {
 template <typename T>
 struct mg_hier {
     int nlev = 0;
+    bool newton = false;          // level 0 is the probed Newton block (smoothed by its stencil)
+    double *pmean = nullptr;      // preconditioner scratch: pressure sum and count
     mg_level<T> L[MG_MAX_LEVELS];
 };
 
@@ -74,6 +89,16 @@ struct mdz_solver {
     bool ready = false;
     int nu1 = 3, nu2 = 3;
     double omega = 0.7;
+    int check = 4;               // GCR iterations between host convergence checks
+    int restart = 30;            // GCR basis size
+    int mg_jacobian = 0;         // 1: multigrid on the Newton Jacobian's velocity block (else Picard)
+    // preconditioner application captured as a CUDA graph, per precision
+    // ([0] FP64, [1] FP32): one graph launch per Krylov iteration
+    // [precision (0 FP64, 1 FP32) * 2 + newton]
+    cudaGraphExec_t pre[4] = {nullptr, nullptr, nullptr, nullptr};
+    long long pre_launches[4] = {0, 0, 0, 0};
+    const double *pre_eta[4] = {nullptr, nullptr, nullptr, nullptr};
+    double pre_bytes[4] = {0, 0, 0, 0};   // algorithmic bytes of one application
 };
 
 // ---------------------------------------------------------------------------
@@ -308,31 +333,350 @@ __global__ void k_mg_restrict(stokes_geom F, stokes_geom Cg, const T *__restrict
     }
 }
 
-// coarse coefficients: centroid average of the 4 children; vertex full-weighting
-// (1/4, 1/8, 1/16 over the 3 x 3 fine vertices, edge-clamped).  Injection of the
-// vertex viscosity makes the V-cycle diverge at 1e3 contrasts; full weighting
-// keeps it convergent as a preconditioner up to 1e5.
+// ---------------------------------------------------------------------------
+// Galerkin coarse operators.  Re-discretised coarse levels (averaged
+// viscosities) lose the coupling across layers of 1e5 viscosity contrast and
+// the V-cycle stops converging; R A P keeps it.  With this P (bilinear in the
+// staggered sense) and R = P^T the coarse stencils close on a fixed footprint:
+//   u-row (K, L):  uu  dK in [-1, 1], dL in [-2, 2]   planes  0..14: (dK+1) + 3 (dL+2)
+//                  uv  I-K in [-1, 2], J-L in [-2, 1]  planes 15..30: 15 + (dI+1) + 4 (dJ+2)
+//   v-row (I, J):  vv  dI in [-2, 2], dJ in [-1, 1]   planes  0..14: (dI+2) + 5 (dJ+1)
+//                  vu  K-I in [-2, 1], L-J in [-1, 2]  planes 15..30: 15 + (dK+2) + 4 (dL+1)
+// (u index (k, l) of the Nx x (Nz+1) box, v index (i, j) of the (Nx+1) x Nz box).
+// The level-0 stencil is a subset of this footprint.
+
+// parents of fine u node (i, j) on the coarse level: 4 (index, weight) pairs
+__device__ __forceinline__ void u_parents(int i, int j, int Nxc, int nczc, int *idx, float *w) {
+    int J0, J1;
+    float w0, w1;
+    cc_weights(j, nczc, J0, w0, J1, w1);
+    int Ia = i >> 1, Ib = (i + 1) >> 1;
+    float wa = (i & 1) ? 0.5f : 1.0f, wb = (i & 1) ? 0.5f : 0.0f;
+    idx[0] = Ia + J0 * Nxc; w[0] = wa * w0;
+    idx[1] = Ia + J1 * Nxc; w[1] = wa * w1;
+    idx[2] = Ib + J0 * Nxc; w[2] = wb * w0;
+    idx[3] = Ib + J1 * Nxc; w[3] = wb * w1;
+}
+
+__device__ __forceinline__ void v_parents(int i, int j, int Nxc, int ncxc, int *idx, float *w) {
+    int I0, I1;
+    float w0, w1;
+    cc_weights(i, ncxc, I0, w0, I1, w1);
+    int Ja = j >> 1, Jb = (j + 1) >> 1;
+    float wa = (j & 1) ? 0.5f : 1.0f, wb = (j & 1) ? 0.5f : 0.0f;
+    const int W = Nxc + 1;
+    idx[0] = I0 + Ja * W; w[0] = wa * w0;
+    idx[1] = I1 + Ja * W; w[1] = wa * w1;
+    idx[2] = I0 + Jb * W; w[2] = wb * w0;
+    idx[3] = I1 + Jb * W; w[3] = wb * w1;
+}
+
+// y = A x for a stencil level, one u-row / v-row
 template <typename T>
-__global__ void k_mg_coarsen(int ncxf, int Nxf, int Nzf, int ncxc, int nczc, int Nxc, int Nzc,
-                             const T *__restrict__ D11f, const T *__restrict__ D33f, T *__restrict__ D11c,
-                             T *__restrict__ D33c) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < ncxc * nczc) {
-        int I = i % ncxc, J = i / ncxc, a = 2 * I + 2 * J * ncxf;
-        D11c[i] = (T)0.25 * (D11f[a] + D11f[a + 1] + D11f[a + ncxf] + D11f[a + ncxf + 1]);
+__device__ __forceinline__ T st_urow(int Nx, int Nz, const T *__restrict__ su, size_t nu, const T *__restrict__ xu,
+                                     const T *__restrict__ xv, int k, int l) {
+    const size_t c = (size_t)k + (size_t)l * Nx;
+    T s = 0;
+#pragma unroll
+    for (int dl = -2; dl <= 2; dl++) {
+        const int ll = l + dl;
+        if (ll < 0 || ll > Nz) continue;
+#pragma unroll
+        for (int dk = -1; dk <= 1; dk++) {
+            const int kk = k + dk;
+            if (kk < 0 || kk >= Nx) continue;
+            s += su[(size_t)((dk + 1) + 3 * (dl + 2)) * nu + c] * xu[kk + ll * Nx];
+        }
     }
-    if (i < Nxc * Nzc) {
-        int I = i % Nxc, J = i / Nxc;
-        double s = 0.0;
-        for (int b = -1; b <= 1; b++)
-            for (int a = -1; a <= 1; a++) {
-                int x = 2 * I + a, z = 2 * J + b;
-                x = x < 0 ? 0 : (x > Nxf - 1 ? Nxf - 1 : x);
-                z = z < 0 ? 0 : (z > Nzf - 1 ? Nzf - 1 : z);
-                double w = (a == 0 ? 0.5 : 0.25) * (b == 0 ? 0.5 : 0.25);
-                s += w * (double)D33f[x + z * Nxf];
+#pragma unroll
+    for (int dJ = -2; dJ <= 1; dJ++) {
+        const int j = l + dJ;
+        if (j < 0 || j >= Nz) continue;
+#pragma unroll
+        for (int dI = -1; dI <= 2; dI++) {
+            const int i = k + dI;
+            if (i < 0 || i > Nx) continue;
+            s += su[(size_t)(15 + (dI + 1) + 4 * (dJ + 2)) * nu + c] * xv[i + j * (Nx + 1)];
+        }
+    }
+    return s;
+}
+
+template <typename T>
+__device__ __forceinline__ T st_vrow(int Nx, int Nz, const T *__restrict__ sv, size_t nv, const T *__restrict__ xu,
+                                     const T *__restrict__ xv, int i, int j) {
+    const size_t c = (size_t)i + (size_t)j * (Nx + 1);
+    T s = 0;
+#pragma unroll
+    for (int dJ = -1; dJ <= 1; dJ++) {
+        const int jj = j + dJ;
+        if (jj < 0 || jj >= Nz) continue;
+#pragma unroll
+        for (int dI = -2; dI <= 2; dI++) {
+            const int ii = i + dI;
+            if (ii < 0 || ii > Nx) continue;
+            s += sv[(size_t)((dI + 2) + 5 * (dJ + 1)) * nv + c] * xv[ii + jj * (Nx + 1)];
+        }
+    }
+#pragma unroll
+    for (int dL = -1; dL <= 2; dL++) {
+        const int l = j + dL;
+        if (l < 0 || l > Nz) continue;
+#pragma unroll
+        for (int dK = -2; dK <= 1; dK++) {
+            const int k = i + dK;
+            if (k < 0 || k >= Nx) continue;
+            s += sv[(size_t)(15 + (dK + 2) + 4 * (dL + 1)) * nv + c] * xu[k + l * Nx];
+        }
+    }
+    return s;
+}
+
+// out = x + omega D^-1 (f - A x) on a stencil level (x == nullptr: x = 0)
+template <typename T>
+__global__ void __launch_bounds__(256) k_st_smooth(stokes_geom G, const T *__restrict__ su, const T *__restrict__ sv,
+                                                   const T *__restrict__ xu, const T *__restrict__ xv,
+                                                   const T *__restrict__ fu, const T *__restrict__ fv,
+                                                   const T *__restrict__ idu, const T *__restrict__ idv, T omega,
+                                                   T *__restrict__ ou, T *__restrict__ ov) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int Nx = G.Nx, Nz = G.Nz;
+    const size_t nu = (size_t)Nx * (Nz + 1), nv = (size_t)(Nx + 1) * Nz;
+    if (i < Nx && j <= Nz) {
+        int c = i + j * Nx;
+        T r = 0;
+        if (G.BCu[c] == -1) {
+            if (xu) r = xu[c] + omega * idu[c] * (fu[c] - st_urow<T>(Nx, Nz, su, nu, xu, xv, i, j));
+            else r = omega * idu[c] * fu[c];
+        }
+        ou[c] = r;
+    }
+    if (i <= Nx && j < Nz) {
+        int c = i + j * (Nx + 1);
+        T r = 0;
+        if (G.BCv[c] == -1) {
+            if (xv) r = xv[c] + omega * idv[c] * (fv[c] - st_vrow<T>(Nx, Nz, sv, nv, xu, xv, i, j));
+            else r = omega * idv[c] * fv[c];
+        }
+        ov[c] = r;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_st_residual(stokes_geom G, const T *__restrict__ su,
+                                                     const T *__restrict__ sv, const T *__restrict__ xu,
+                                                     const T *__restrict__ xv, const T *__restrict__ fu,
+                                                     const T *__restrict__ fv, T *__restrict__ ru,
+                                                     T *__restrict__ rv) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int Nx = G.Nx, Nz = G.Nz;
+    const size_t nu = (size_t)Nx * (Nz + 1), nv = (size_t)(Nx + 1) * Nz;
+    if (i < Nx && j <= Nz) {
+        int c = i + j * Nx;
+        ru[c] = G.BCu[c] == -1 ? fu[c] - st_urow<T>(Nx, Nz, su, nu, xu, xv, i, j) : T(0);
+    }
+    if (i <= Nx && j < Nz) {
+        int c = i + j * (Nx + 1);
+        rv[c] = G.BCv[c] == -1 ? fv[c] - st_vrow<T>(Nx, Nz, sv, nv, xu, xv, i, j) : T(0);
+    }
+}
+
+template <typename T>
+__global__ void k_st_diag(stokes_geom G, const T *__restrict__ su, const T *__restrict__ sv, T *__restrict__ idu,
+                          T *__restrict__ idv) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t nu = (size_t)G.Nx * (G.Nz + 1), nv = (size_t)(G.Nx + 1) * G.Nz;
+    if (i < (long long)nu) idu[i] = G.BCu[i] == -1 ? T(1) / su[(size_t)MG_CENTER * nu + i] : T(0);
+    if (i < (long long)nv) idv[i] = G.BCv[i] == -1 ? T(1) / sv[(size_t)MG_CENTER * nv + i] : T(0);
+}
+
+// Level-0 probing: x = indicator of the unknowns of component comp with
+// (k mod 4, l mod 4) = (cx, cz); y = A x.  The level-0 operator (Picard or
+// Newton) couples a row to same-component nodes within [-1, 1]^2 and to
+// other-component nodes within a 4 x 4 window, so each colour class holds at
+// most one node of a row's footprint and y at the row is one coefficient.
+#define MG_PROBE 4
+template <typename T>
+__global__ void k_probe_vec(stokes_geom G, int comp, int cx, int cz, T *__restrict__ xu, T *__restrict__ xv) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int Nx = G.Nx, Nz = G.Nz;
+    if (i < Nx && j <= Nz) {
+        int c = i + j * Nx;
+        xu[c] = (comp == 0 && G.BCu[c] == -1 && i % MG_PROBE == cx && j % MG_PROBE == cz) ? T(1) : T(0);
+    }
+    if (i <= Nx && j < Nz) {
+        int c = i + j * (Nx + 1);
+        xv[c] = (comp == 1 && G.BCv[c] == -1 && i % MG_PROBE == cx && j % MG_PROBE == cz) ? T(1) : T(0);
+    }
+}
+
+// velocity rows of the Picard (NEWTON = false, p0 unused) or Newton operator
+// (p0 = a zero pressure vector) applied to (xu, xv, 0)
+template <typename T, bool NEWTON>
+__global__ void __launch_bounds__(256) k_mg_apply(stokes_geom G, stokes_coefs<T> D, const T *__restrict__ xu,
+                                                  const T *__restrict__ xv, const T *__restrict__ p0,
+                                                  T *__restrict__ yu, T *__restrict__ yv) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int Nx = G.Nx, Nz = G.Nz;
+    const T celvol = (T)(G.dx * G.dz);
+    stokes_cvec<T> x{xu, xv, NEWTON ? p0 : nullptr};
+    if (i < Nx && j <= Nz) {
+        int c = i + j * Nx;
+        yu[c] = G.BCu[c] == -1 ? xrow<T, NEWTON>(G, D, x, i, j) * celvol : T(0);
+    }
+    if (i <= Nx && j < Nz) {
+        int c = i + j * (Nx + 1);
+        yv[c] = G.BCv[c] == -1 ? zrow<T, NEWTON>(G, D, x, i, j) * celvol : T(0);
+    }
+}
+
+// offset of the colour-cx node from position p along one direction inside the
+// window [lo, hi] (at most MG_PROBE wide): returns 1 and the offset, or 0
+__device__ __forceinline__ int colour_offset(int p, int cx, int lo, int hi, int *d) {
+    for (int o = lo; o <= hi; o++)
+        if ((((p + o) % MG_PROBE) + MG_PROBE) % MG_PROBE == cx) { *d = o; return 1; }
+    return 0;
+}
+
+template <typename T>
+__global__ void k_probe_collect(stokes_geom G, int comp, int cx, int cz, const T *__restrict__ yu,
+                                const T *__restrict__ yv, T *__restrict__ su, T *__restrict__ sv) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int Nx = G.Nx, Nz = G.Nz;
+    const size_t nu = (size_t)Nx * (Nz + 1), nv = (size_t)(Nx + 1) * Nz;
+    int a, b;
+    if (i < Nx && j <= Nz) {
+        int c = i + j * Nx;
+        if (G.BCu[c] == -1) {
+            if (comp == 0) {   // uu within [-1, 1]^2
+                if (colour_offset(i, cx, -1, 1, &a) && colour_offset(j, cz, -1, 1, &b))
+                    su[(size_t)((a + 1) + 3 * (b + 2)) * nu + c] = yu[c];
+            } else {           // uv: I - k in [-1, 2], J - l in [-2, 1]
+                if (colour_offset(i, cx, -1, 2, &a) && colour_offset(j, cz, -2, 1, &b))
+                    su[(size_t)(15 + (a + 1) + 4 * (b + 2)) * nu + c] = yu[c];
             }
-        D33c[i] = (T)s;
+        }
+    }
+    if (i <= Nx && j < Nz) {
+        int c = i + j * (Nx + 1);
+        if (G.BCv[c] == -1) {
+            if (comp == 1) {   // vv within [-1, 1]^2
+                if (colour_offset(i, cx, -1, 1, &a) && colour_offset(j, cz, -1, 1, &b))
+                    sv[(size_t)((a + 2) + 5 * (b + 1)) * nv + c] = yv[c];
+            } else {           // vu: K - i in [-2, 1], L - j in [-1, 2]
+                if (colour_offset(i, cx, -2, 1, &a) && colour_offset(j, cz, -1, 2, &b))
+                    sv[(size_t)(15 + (a + 2) + 4 * (b + 1)) * nv + c] = yv[c];
+            }
+        }
+    }
+}
+
+// Coarse stencils = R A P, one thread per coarse row; FP64 accumulation.
+// An entry landing outside the footprint (impossible with this P) sets *bad.
+template <typename T>
+__global__ void __launch_bounds__(128) k_galerkin(stokes_geom F, const T *__restrict__ suF,
+                                                  const T *__restrict__ svF, stokes_geom Cg, T *__restrict__ suC,
+                                                  T *__restrict__ svC, int *bad) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int Nxf = F.Nx, Nzf = F.Nz, Nxc = Cg.Nx, Nzc = Cg.Nz;
+    const size_t nuf = (size_t)Nxf * (Nzf + 1), nvf = (size_t)(Nxf + 1) * Nzf;
+    const size_t nuc = (size_t)Nxc * (Nzc + 1), nvc = (size_t)(Nxc + 1) * Nzc;
+    double acc[MG_NST];
+    int pi[4];
+    float pw[4];
+    if (t < (long long)nuc) {   // coarse u-row (K, L)
+        const int K = t % Nxc, L = t / Nxc;
+        for (int q = 0; q < MG_NST; q++) acc[q] = 0.0;
+        if (Cg.BCu[t] == -1) {
+            for (int lf = 2 * L - 2; lf <= 2 * L + 1; lf++) {
+                if (lf < 1 || lf > F.ncz) continue;
+                int J0, J1;
+                float w0, w1;
+                cc_weights(lf, Cg.ncz, J0, w0, J1, w1);
+                const float wz = (J0 == L ? w0 : 0.0f) + (J1 == L && J1 != J0 ? w1 : 0.0f);
+                if (wz == 0.0f) continue;
+                for (int k = 2 * K - 1; k <= 2 * K + 1; k++) {
+                    if (k < 0 || k >= Nxf) continue;
+                    const float wx = nc_weight(k, K);
+                    if (wx == 0.0f) continue;
+                    const int f = k + lf * Nxf;
+                    if (F.BCu[f] != -1) continue;
+                    const double R = (double)wx * wz;
+                    for (int q = 0; q < 15; q++) {          // uu entries of the fine row
+                        const double a = (double)suF[(size_t)q * nuf + f];
+                        if (a == 0.0) continue;
+                        const int tk = k + q % 3 - 1, tl = lf + q / 3 - 2;
+                        u_parents(tk, tl, Nxc, Cg.ncz, pi, pw);
+                        for (int s = 0; s < 4; s++) {
+                            if (pw[s] == 0.0f || Cg.BCu[pi[s]] != -1) continue;
+                            const int dK = pi[s] % Nxc - K, dL = pi[s] / Nxc - L;
+                            if (dK < -1 || dK > 1 || dL < -2 || dL > 2) { *bad = 1; continue; }
+                            acc[(dK + 1) + 3 * (dL + 2)] += R * a * pw[s];
+                        }
+                    }
+                    for (int q = 0; q < 16; q++) {          // uv entries of the fine row
+                        const double a = (double)suF[(size_t)(15 + q) * nuf + f];
+                        if (a == 0.0) continue;
+                        const int ti = k + q % 4 - 1, tj = lf + q / 4 - 2;
+                        v_parents(ti, tj, Nxc, Cg.ncx, pi, pw);
+                        for (int s = 0; s < 4; s++) {
+                            if (pw[s] == 0.0f || Cg.BCv[pi[s]] != -1) continue;
+                            const int dI = pi[s] % (Nxc + 1) - K, dJ = pi[s] / (Nxc + 1) - L;
+                            if (dI < -1 || dI > 2 || dJ < -2 || dJ > 1) { *bad = 1; continue; }
+                            acc[15 + (dI + 1) + 4 * (dJ + 2)] += R * a * pw[s];
+                        }
+                    }
+                }
+            }
+        }
+        for (int q = 0; q < MG_NST; q++) suC[(size_t)q * nuc + t] = (T)acc[q];
+    }
+    if (t < (long long)nvc) {   // coarse v-row (I, J)
+        const int I = t % (Nxc + 1), J = t / (Nxc + 1);
+        for (int q = 0; q < MG_NST; q++) acc[q] = 0.0;
+        if (Cg.BCv[t] == -1) {
+            for (int i = 2 * I - 2; i <= 2 * I + 1; i++) {
+                if (i < 1 || i > F.ncx) continue;
+                int I0, I1;
+                float w0, w1;
+                cc_weights(i, Cg.ncx, I0, w0, I1, w1);
+                const float wx = (I0 == I ? w0 : 0.0f) + (I1 == I && I1 != I0 ? w1 : 0.0f);
+                if (wx == 0.0f) continue;
+                for (int j = 2 * J - 1; j <= 2 * J + 1; j++) {
+                    if (j < 0 || j >= Nzf) continue;
+                    const float wz = nc_weight(j, J);
+                    if (wz == 0.0f) continue;
+                    const int f = i + j * (Nxf + 1);
+                    if (F.BCv[f] != -1) continue;
+                    const double R = (double)wx * wz;
+                    for (int q = 0; q < 15; q++) {          // vv entries
+                        const double a = (double)svF[(size_t)q * nvf + f];
+                        if (a == 0.0) continue;
+                        const int ti = i + q % 5 - 2, tj = j + q / 5 - 1;
+                        v_parents(ti, tj, Nxc, Cg.ncx, pi, pw);
+                        for (int s = 0; s < 4; s++) {
+                            if (pw[s] == 0.0f || Cg.BCv[pi[s]] != -1) continue;
+                            const int dI = pi[s] % (Nxc + 1) - I, dJ = pi[s] / (Nxc + 1) - J;
+                            if (dI < -2 || dI > 2 || dJ < -1 || dJ > 1) { *bad = 1; continue; }
+                            acc[(dI + 2) + 5 * (dJ + 1)] += R * a * pw[s];
+                        }
+                    }
+                    for (int q = 0; q < 16; q++) {          // vu entries
+                        const double a = (double)svF[(size_t)(15 + q) * nvf + f];
+                        if (a == 0.0) continue;
+                        const int tk = i + q % 4 - 2, tl = j + q / 4 - 1;
+                        u_parents(tk, tl, Nxc, Cg.ncz, pi, pw);
+                        for (int s = 0; s < 4; s++) {
+                            if (pw[s] == 0.0f || Cg.BCu[pi[s]] != -1) continue;
+                            const int dK = pi[s] % Nxc - I, dL = pi[s] / Nxc - J;
+                            if (dK < -2 || dK > 1 || dL < -1 || dL > 2) { *bad = 1; continue; }
+                            acc[15 + (dK + 2) + 4 * (dL + 1)] += R * a * pw[s];
+                        }
+                    }
+                }
+            }
+        }
+        for (int q = 0; q < MG_NST; q++) svC[(size_t)q * nvc + t] = (T)acc[q];
     }
 }
 
@@ -367,18 +711,17 @@ __device__ double cta_dot(const T *a, const T *b, int n0, int n1, const T *a1, c
 }
 
 template <typename T>
-__device__ void cta_apply(const stokes_geom &G, const stokes_coefs<T> &D, const T *xu, const T *xv, T *yu, T *yv) {
+__device__ void cta_apply(const stokes_geom &G, const T *su, const T *sv, const T *xu, const T *xv, T *yu, T *yv) {
     const int Nx = G.Nx, Nz = G.Nz;
-    const T celvol = (T)(G.dx * G.dz);
-    stokes_cvec<T> x{xu, xv, nullptr};
-    for (int c = threadIdx.x; c < Nx * (Nz + 1); c += blockDim.x)
-        yu[c] = G.BCu[c] == -1 ? xrow<T, false>(G, D, x, c % Nx, c / Nx) * celvol : T(0);
-    for (int c = threadIdx.x; c < (Nx + 1) * Nz; c += blockDim.x)
-        yv[c] = G.BCv[c] == -1 ? zrow<T, false>(G, D, x, c % (Nx + 1), c / (Nx + 1)) * celvol : T(0);
+    const size_t nu = (size_t)Nx * (Nz + 1), nv = (size_t)(Nx + 1) * Nz;
+    for (int c = threadIdx.x; c < (int)nu; c += blockDim.x)
+        yu[c] = G.BCu[c] == -1 ? st_urow<T>(Nx, Nz, su, nu, xu, xv, c % Nx, c / Nx) : T(0);
+    for (int c = threadIdx.x; c < (int)nv; c += blockDim.x)
+        yv[c] = G.BCv[c] == -1 ? st_vrow<T>(Nx, Nz, sv, nv, xu, xv, c % (Nx + 1), c / (Nx + 1)) : T(0);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(1024) k_mg_coarse_cg(stokes_geom G, stokes_coefs<T> D, const T *__restrict__ fu,
+__global__ void __launch_bounds__(1024) k_mg_coarse_cg(stokes_geom G, const T *su, const T *sv, const T *__restrict__ fu,
                                                        const T *__restrict__ fv, const T *__restrict__ idu,
                                                        const T *__restrict__ idv, T *xu, T *xv, T *ru, T *rv, T *zu,
                                                        T *zv, T *pu, T *pv, T *qu, T *qv, int maxit, double rtol) {
@@ -391,7 +734,7 @@ __global__ void __launch_bounds__(1024) k_mg_coarse_cg(stokes_geom G, stokes_coe
     double r0 = cta_dot<T>(ru, ru, nu, nv, rv, rv, sh);
     if (r0 == 0.0) return;
     for (int it = 0; it < maxit; it++) {
-        cta_apply<T>(G, D, pu, pv, qu, qv);
+        cta_apply<T>(G, su, sv, pu, pv, qu, qv);
         __syncthreads();
         double pq = cta_dot<T>(pu, qu, nu, nv, pv, qv, sh);
         if (pq <= 0.0) break;
@@ -407,6 +750,142 @@ __global__ void __launch_bounds__(1024) k_mg_coarse_cg(stokes_geom G, stokes_coe
         for (int i = threadIdx.x; i < nu; i += blockDim.x) pu[i] = zu[i] + b * pu[i];
         for (int i = threadIdx.x; i < nv; i += blockDim.x) pv[i] = zv[i] + b * pv[i];
         __syncthreads();
+    }
+}
+
+// Small coarsest level: the velocity block is gathered from the level's
+// stencils into a dense matrix (one CTA) and inverted by Gauss-Jordan
+// elimination with partial pivoting in FP64 (a zero pivot column sets
+// *status).  AinvT is stored column-major so that the solve's threads read it
+// coalesced.  Dense numbering: u unknowns (k, l), k in 1..Nx-2, l in 1..Nz-1,
+// row by row, then v unknowns (i, j), i in 1..Nx-1, j in 1..Nz-2.
+__device__ __forceinline__ int dense_u(int Nx, int Nz, int k, int l) {
+    return (k >= 1 && k <= Nx - 2 && l >= 1 && l <= Nz - 1) ? (k - 1) + (l - 1) * (Nx - 2) : -1;
+}
+__device__ __forceinline__ int dense_v(int Nx, int Nz, int i, int j) {
+    return (i >= 1 && i <= Nx - 1 && j >= 1 && j <= Nz - 2) ? (Nx - 2) * (Nz - 1) + (i - 1) + (j - 1) * (Nx - 1) : -1;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(512) k_coarse_dense_setup(stokes_geom G, const T *__restrict__ su,
+                                                            const T *__restrict__ sv, int n,
+                                                            const int *__restrict__ map, double *A,
+                                                            T *__restrict__ AinvT, int *status) {
+    __shared__ double col[MG_DENSE_MAX];
+    __shared__ int bad;
+    const int Nx = G.Nx, Nz = G.Nz;
+    const size_t nu = (size_t)Nx * (Nz + 1), nv = (size_t)(Nx + 1) * Nz;
+    if (threadIdx.x == 0) bad = 0;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) A[e] = 0.0;
+    __syncthreads();
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        const int m = map[r];
+        if (m < (int)nu) {
+            const int k = m % Nx, l = m / Nx;
+            for (int q = 0; q < 15; q++) {
+                int c = dense_u(Nx, Nz, k + q % 3 - 1, l + q / 3 - 2);
+                if (c >= 0) A[(size_t)r * n + c] += (double)su[(size_t)q * nu + m];
+            }
+            for (int q = 0; q < 16; q++) {
+                int c = dense_v(Nx, Nz, k + q % 4 - 1, l + q / 4 - 2);
+                if (c >= 0) A[(size_t)r * n + c] += (double)su[(size_t)(15 + q) * nu + m];
+            }
+        } else {
+            const int mv = m - (int)nu, i = mv % (Nx + 1), j = mv / (Nx + 1);
+            for (int q = 0; q < 15; q++) {
+                int c = dense_v(Nx, Nz, i + q % 5 - 2, j + q / 5 - 1);
+                if (c >= 0) A[(size_t)r * n + c] += (double)sv[(size_t)q * nv + mv];
+            }
+            for (int q = 0; q < 16; q++) {
+                int c = dense_u(Nx, Nz, i + q % 4 - 2, j + q / 4 - 1);
+                if (c >= 0) A[(size_t)r * n + c] += (double)sv[(size_t)(15 + q) * nv + mv];
+            }
+        }
+    }
+    __syncthreads();
+    // Gauss-Jordan on [A | I] with partial pivoting (the Newton block is
+    // neither symmetric nor definite); B ends as A^-1
+    double *B = A + (size_t)n * n;
+    __shared__ double red_v[32];
+    __shared__ int red_i[32];
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) B[e] = (e / n == e % n) ? 1.0 : 0.0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    for (int k = 0; k < n; k++) {
+        double bv = -1.0;
+        int bi = k;
+        for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
+            const double v = fabs(A[(size_t)i * n + k]);
+            if (v > bv) { bv = v; bi = i; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+        }
+        if (lane == 0) { red_v[wid] = bv; red_i[wid] = bi; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < nw; w++)
+                if (red_v[w] > red_v[0] || (red_v[w] == red_v[0] && red_i[w] < red_i[0])) {
+                    red_v[0] = red_v[w];
+                    red_i[0] = red_i[w];
+                }
+        }
+        __syncthreads();
+        const double pmax = red_v[0];
+        const int pr = red_i[0];
+        if (!(pmax > 0.0) || !isfinite(pmax)) { if (threadIdx.x == 0) bad = 1; break; }   // uniform
+        if (pr != k)
+            for (int j = threadIdx.x; j < n; j += blockDim.x) {
+                double t = A[(size_t)k * n + j]; A[(size_t)k * n + j] = A[(size_t)pr * n + j]; A[(size_t)pr * n + j] = t;
+                t = B[(size_t)k * n + j]; B[(size_t)k * n + j] = B[(size_t)pr * n + j]; B[(size_t)pr * n + j] = t;
+            }
+        __syncthreads();
+        const double inv = 1.0 / A[(size_t)k * n + k];
+        __syncthreads();
+        for (int j = threadIdx.x; j < n; j += blockDim.x) {
+            A[(size_t)k * n + j] *= inv;
+            B[(size_t)k * n + j] *= inv;
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += blockDim.x) col[i] = A[(size_t)i * n + k];
+        __syncthreads();
+        for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+            const int i = e / n, j = e % n;
+            if (i == k) continue;
+            A[(size_t)i * n + j] -= col[i] * A[(size_t)k * n + j];
+            B[(size_t)i * n + j] -= col[i] * B[(size_t)k * n + j];
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+    if (bad) { if (threadIdx.x == 0) *status = 1; return; }
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+        int i = e / n, j = e % n;
+        AinvT[(size_t)j * n + i] = (T)B[(size_t)i * n + j];
+    }
+}
+
+// x = A^-1 f on the small coarsest level (zero outside the unknowns)
+template <typename T>
+__global__ void __launch_bounds__(256) k_coarse_dense_solve(int n, int nu, int nv, const int *__restrict__ map,
+                                                            const T *__restrict__ AinvT, const T *__restrict__ fu,
+                                                            const T *__restrict__ fv, T *__restrict__ xu,
+                                                            T *__restrict__ xv) {
+    __shared__ T fs[MG_DENSE_MAX];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        int m = map[i];
+        fs[i] = m < nu ? fu[m] : fv[m - nu];
+    }
+    for (int i = threadIdx.x; i < nu; i += blockDim.x) xu[i] = T(0);
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) xv[i] = T(0);
+    __syncthreads();
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        T s = 0;
+        for (int j = 0; j < n; j++) s += AinvT[(size_t)j * n + r] * fs[j];
+        int m = map[r];
+        if (m < nu) xu[m] = s; else xv[m - nu] = s;
     }
 }
 
@@ -441,23 +920,44 @@ static mdz_status build_hierarchy(mdz_ctx *ctx, mg_hier<T> &H) {
                 e = cudaGetLastError();
             }
         }
-        if (e == cudaSuccess) e = alloc0(&L.D11, (size_t)L.ncx * L.ncz);
-        if (e == cudaSuccess) e = alloc0(&L.D33, (size_t)Nx * Nz);
+        if (lev == 0) {
+            if (e == cudaSuccess) e = alloc0(&L.D11, (size_t)L.ncx * L.ncz);
+            if (e == cudaSuccess) e = alloc0(&L.D33, (size_t)Nx * Nz);
+            if (e == cudaSuccess) e = alloc0(&L.pz, (size_t)L.ncx * L.ncz);
+            if (e == cudaSuccess) e = alloc0(&H.pmean, 2);
+        }
+        if (e == cudaSuccess) e = alloc0(&L.su, (size_t)MG_NST * L.nu());
+        if (e == cudaSuccess) e = alloc0(&L.sv, (size_t)MG_NST * L.nv());
         T **bufs[] = {&L.xu, &L.yu, &L.fu, &L.ru, &L.idu};
         for (T **b : bufs) if (e == cudaSuccess) e = alloc0(b, L.nu());
         T **bufv[] = {&L.xv, &L.yv, &L.fv, &L.rv, &L.idv};
         for (T **b : bufv) if (e == cudaSuccess) e = alloc0(b, L.nv());
         lev++;
-        bool can = (L.ncx % 2 == 0) && (L.ncz % 2 == 0) && L.ncx >= 8 && L.ncz >= 8 &&
-                   (size_t)L.ncx * L.ncz > 64;
+        // halve while both cell counts are even and the coarse level keeps >= 4 cells a side
+        bool can = (L.ncx % 2 == 0) && (L.ncz % 2 == 0) && L.ncx / 2 >= 4 && L.ncz / 2 >= 4;
         if (!can) break;
         Nx = L.ncx / 2 + 1; Nz = L.ncz / 2 + 1; dx *= 2; dz *= 2;
     }
     H.nlev = lev;
     mg_level<T> &C = H.L[lev - 1];
-    for (int q = 0; q < 4; q++) {
-        if (e == cudaSuccess) e = alloc0(&C.cg[2 * q], C.nu());
-        if (e == cudaSuccess) e = alloc0(&C.cg[2 * q + 1], C.nv());
+    // unknowns of the coarsest level (tag rule of the free-slip box)
+    std::vector<int> map;
+    for (int l = 1; l <= C.Nz - 1; l++)
+        for (int k = 1; k <= C.Nx - 2; k++) map.push_back(k + l * C.Nx);
+    for (int l = 1; l <= C.Nz - 2; l++)
+        for (int k = 1; k <= C.Nx - 1; k++) map.push_back((int)C.nu() + k + l * (C.Nx + 1));
+    if ((int)map.size() <= MG_DENSE_MAX) {
+        C.ndense = (int)map.size();
+        size_t n2 = (size_t)C.ndense * C.ndense;
+        if (e == cudaSuccess) e = alloc0(&C.dmap, map.size());
+        if (e == cudaSuccess) e = cudaMemcpy(C.dmap, map.data(), sizeof(int) * map.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = alloc0(&C.Awork, 2 * n2);
+        if (e == cudaSuccess) e = alloc0(&C.AinvT, n2);
+    } else {
+        for (int q = 0; q < 4; q++) {
+            if (e == cudaSuccess) e = alloc0(&C.cg[2 * q], C.nu());
+            if (e == cudaSuccess) e = alloc0(&C.cg[2 * q + 1], C.nv());
+        }
     }
     if (e != cudaSuccess) return mdz_cuda_check(ctx, e, "multigrid allocation");
     return MDZ_OK;
@@ -469,9 +969,12 @@ static void free_hierarchy(mg_hier<T> &H) {
         mg_level<T> &L = H.L[l];
         if (L.own_tags) { cudaFree(L.BCu); cudaFree(L.BCv); cudaFree(L.BCp); cudaFree(L.BCg); }
         void *p[] = {L.D11, L.D33, L.xu, L.xv, L.yu, L.yv, L.fu, L.fv, L.ru, L.rv, L.idu, L.idv,
-                     L.cg[0], L.cg[1], L.cg[2], L.cg[3], L.cg[4], L.cg[5], L.cg[6], L.cg[7]};
+                     L.cg[0], L.cg[1], L.cg[2], L.cg[3], L.cg[4], L.cg[5], L.cg[6], L.cg[7],
+                     L.dmap, L.Awork, L.AinvT, L.su, L.sv, L.pz};
         for (void *q : p) if (q) cudaFree(q);
     }
+    if (H.pmean) cudaFree(H.pmean);
+    H.pmean = nullptr;
     H.nlev = 0;
 }
 
@@ -525,17 +1028,83 @@ mdz_status mdz_solver_ensure(mdz_ctx *ctx) {
     mdz_solver *S = ctx->solver;
     if ((s = build_hierarchy<double>(ctx, S->mg64)) != MDZ_OK) return s;
     if ((s = build_hierarchy<float>(ctx, S->mg32)) != MDZ_OK) return s;
-    if ((s = alloc_gcr<double>(ctx, S->g64, 30)) != MDZ_OK) return s;
-    if ((s = alloc_gcr<float>(ctx, S->g32, 30)) != MDZ_OK) return s;
+    if ((s = alloc_gcr<double>(ctx, S->g64, S->restart)) != MDZ_OK) return s;
+    if ((s = alloc_gcr<float>(ctx, S->g32, S->restart)) != MDZ_OK) return s;
     MDZ_CUDA(ctx, cudaMallocHost((void **)&S->sc, 64 * sizeof(double)));
+    memset(S->sc, 0, 64 * sizeof(double));
     MDZ_CUDA(ctx, cudaDeviceSynchronize());
     S->ready = true;
+    return MDZ_OK;
+}
+
+template <typename T>
+static mdz_status copy_stencils(mdz_ctx *ctx, const mg_hier<T> &H, int level, int *Nx, int *Nz, double *su,
+                                double *sv) {
+    if (level < 0 || level >= H.nlev) return mdz_fail(ctx, MDZ_ERR_ARG, "mg_stencils: level %d of %d", level, H.nlev);
+    const mg_level<T> &L = H.L[level];
+    *Nx = L.Nx;
+    *Nz = L.Nz;
+    MDZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const T *src[2] = {L.su, L.sv};
+    double *dst[2] = {su, sv};
+    size_t cnt[2] = {MG_NST * L.nu(), MG_NST * L.nv()};
+    for (int q = 0; q < 2; q++) {
+        if (!dst[q]) continue;
+        std::vector<T> h(cnt[q]);
+        MDZ_CUDA(ctx, cudaMemcpy(h.data(), src[q], sizeof(T) * cnt[q], cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < cnt[q]; i++) dst[q][i] = (double)h[i];
+    }
+    return MDZ_OK;
+}
+
+extern "C" mdz_status mdz_mg_stencils(mdz_ctx *ctx, int precision, int level, int *levels, int *Nx, int *Nz,
+                                      double *su, double *sv) {
+    if (!ctx || !Nx || !Nz || !levels) return ctx ? mdz_fail(ctx, MDZ_ERR_ARG, "mg_stencils: null argument") : MDZ_ERR_ARG;
+    if (!ctx->solver || !ctx->solver->ready)
+        return mdz_fail(ctx, MDZ_ERR_STATE, "mg_stencils: no multigrid hierarchy (run a solve first)");
+    if (precision == 64) {
+        *levels = ctx->solver->mg64.nlev;
+        return copy_stencils<double>(ctx, ctx->solver->mg64, level, Nx, Nz, su, sv);
+    }
+    if (precision == 32) {
+        *levels = ctx->solver->mg32.nlev;
+        return copy_stencils<float>(ctx, ctx->solver->mg32, level, Nx, Nz, su, sv);
+    }
+    return mdz_fail(ctx, MDZ_ERR_ARG, "mg_stencils: precision 64 or 32");
+}
+
+extern "C" mdz_status mdz_set_solver_options(mdz_ctx *ctx, int nu1, int nu2, double omega, int restart, int check,
+                                             int mg_jacobian) {
+    if (!ctx) return MDZ_ERR_ARG;
+    if (nu1 < 1 || nu1 > 16 || nu2 < 0 || nu2 > 16 || !(omega > 0.0 && omega < 2.0) || restart < 2 ||
+        restart > GCR_MAX_M || check < 1 || check > 64 || (mg_jacobian != 0 && mg_jacobian != 1))
+        return mdz_fail(ctx, MDZ_ERR_ARG, "solver options: nu1 1..16, nu2 0..16, omega in (0, 2), restart 2..%d, "
+                                          "check 1..64, mg_jacobian 0/1", GCR_MAX_M);
+    if (!ctx->solver) ctx->solver = new mdz_solver();
+    mdz_solver *S = ctx->solver;
+    MDZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int q = 0; q < 4; q++)
+        if (S->pre[q]) { cudaGraphExecDestroy(S->pre[q]); S->pre[q] = nullptr; }
+    S->nu1 = nu1; S->nu2 = nu2; S->omega = omega; S->check = check; S->mg_jacobian = mg_jacobian;
+    if (S->ready && restart != S->restart) {
+        free_gcr(S->g64);
+        free_gcr(S->g32);
+        S->g64 = gcr_space<double>();
+        S->g32 = gcr_space<float>();
+        S->restart = restart;
+        mdz_status s;
+        if ((s = alloc_gcr<double>(ctx, S->g64, restart)) != MDZ_OK) return s;
+        if ((s = alloc_gcr<float>(ctx, S->g32, restart)) != MDZ_OK) return s;
+    }
+    S->restart = restart;
     return MDZ_OK;
 }
 
 void mdz_solver_free(mdz_ctx *ctx) {
     if (!ctx->solver) return;
     mdz_solver *S = ctx->solver;
+    for (int q = 0; q < 4; q++)
+        if (S->pre[q]) cudaGraphExecDestroy(S->pre[q]);
     free_hierarchy(S->mg64);
     free_hierarchy(S->mg32);
     free_gcr(S->g64);
@@ -550,52 +1119,93 @@ int mdz_solver_levels(const mdz_ctx *ctx) { return ctx->solver ? ctx->solver->mg
 // ---------------------------------------------------------------------------
 // Multigrid setup (coefficients) and V-cycle.
 template <typename T>
-static mdz_status mg_setup(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n, const double *eta_s, cudaStream_t st) {
+static mdz_status mg_setup(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n, const double *eta_s,
+                           const stokes_coefs<T> &K, bool newton, cudaStream_t st) {
     mg_level<T> &F = H.L[0];
     int nc = F.ncx * F.ncz, nv = F.Nx * F.Nz;
+    H.newton = newton;
     k_fill_D11_D33<T><<<mdz_blocks(nv > nc ? nv : nc), MDZ_THREADS, 0, st>>>(nc, nv, eta_n, eta_s, F.D11, F.D33);
     MDZ_LAUNCHED(ctx);
-    for (int l = 0; l < H.nlev; l++) {
-        mg_level<T> &L = H.L[l];
-        if (l > 0) {
-            mg_level<T> &P = H.L[l - 1];
-            int n = L.Nx * L.Nz;
-            k_mg_coarsen<T><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(P.ncx, P.Nx, P.Nz, L.ncx, L.ncz, L.Nx, L.Nz,
-                                                                     P.D11, P.D33, L.D11, L.D33);
-            MDZ_LAUNCHED(ctx);
-        }
-        size_t n = L.nu() > L.nv() ? L.nu() : L.nv();
-        k_mg_diag<T><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(L.geom(), L.D11, L.D33, L.idu, L.idv);
+    // level-0 stencils by probing the fine velocity block (the Picard block from
+    // eta, or the Newton Jacobian's) with 2 x 16 colour classes
+    const dim3 bl(32, 8), gr0((F.Nx + 1 + 31) / 32, (F.Nz + 1 + 7) / 8);
+    MDZ_CUDA(ctx, cudaMemsetAsync(F.su, 0, sizeof(T) * MG_NST * F.nu(), st));
+    MDZ_CUDA(ctx, cudaMemsetAsync(F.sv, 0, sizeof(T) * MG_NST * F.nv(), st));
+    for (int comp = 0; comp < 2; comp++)
+        for (int cz = 0; cz < MG_PROBE; cz++)
+            for (int cx = 0; cx < MG_PROBE; cx++) {
+                k_probe_vec<T><<<gr0, bl, 0, st>>>(F.geom(), comp, cx, cz, F.xu, F.xv);
+                MDZ_LAUNCHED(ctx);
+                if (newton) k_mg_apply<T, true><<<gr0, bl, 0, st>>>(F.geom(), K, F.xu, F.xv, F.pz, F.ru, F.rv);
+                else k_mg_apply<T, false><<<gr0, bl, 0, st>>>(F.geom(), F.coefs(), F.xu, F.xv, nullptr, F.ru, F.rv);
+                MDZ_LAUNCHED(ctx);
+                k_probe_collect<T><<<gr0, bl, 0, st>>>(F.geom(), comp, cx, cz, F.ru, F.rv, F.su, F.sv);
+                MDZ_LAUNCHED(ctx);
+            }
+    {   // Jacobi diagonal of level 0: the viscosity formula (Picard) or the probed stencil (Newton)
+        size_t n = F.nu() > F.nv() ? F.nu() : F.nv();
+        if (newton) k_st_diag<T><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(F.geom(), F.su, F.sv, F.idu, F.idv);
+        else k_mg_diag<T><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(F.geom(), F.D11, F.D33, F.idu, F.idv);
         MDZ_LAUNCHED(ctx);
     }
+    int *status = ctx->d_counters + 40;   // [0] coarse inverse, [1] Galerkin footprint
+    MDZ_CUDA(ctx, cudaMemsetAsync(status, 0, 2 * sizeof(int), st));
+    for (int l = 1; l < H.nlev; l++) {
+        mg_level<T> &P = H.L[l - 1], &L = H.L[l];
+        size_t n = L.nu() > L.nv() ? L.nu() : L.nv();
+        k_galerkin<T><<<mdz_blocks(n, 128), 128, 0, st>>>(P.geom(), P.su, P.sv, L.geom(), L.su, L.sv, status + 1);
+        MDZ_LAUNCHED(ctx);
+        k_st_diag<T><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(L.geom(), L.su, L.sv, L.idu, L.idv);
+        MDZ_LAUNCHED(ctx);
+    }
+    mg_level<T> &C = H.L[H.nlev - 1];
+    if (C.ndense) {
+        k_coarse_dense_setup<T><<<1, 512, 0, st>>>(C.geom(), C.su, C.sv, C.ndense, C.dmap, C.Awork, C.AinvT, status);
+        MDZ_LAUNCHED(ctx);
+    }
+    MDZ_CUDA(ctx, cudaMemcpyAsync((int *)(ctx->solver->sc + 20), status, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
     return MDZ_OK;
 }
 
 static inline dim3 box_grid(int Nx, int Nz) { return dim3((Nx + 1 + 31) / 32, (Nz + 1 + 7) / 8); }
 
-// One V-cycle: H.L[l].x <- approx A^-1 H.L[l].f
+// One V-cycle: H.L[l].x <- approx A^-1 H.L[l].f.  Level 0 smooths with the
+// re-discretised stencil (viscosities read directly), coarser levels with the
+// Galerkin stencils.
 template <typename T>
 static mdz_status vcycle(mdz_ctx *ctx, mg_hier<T> &H, int l, int nu1, int nu2, T omega, cudaStream_t st) {
     mg_level<T> &L = H.L[l];
     stokes_geom G = L.geom();
     stokes_coefs<T> D = L.coefs();
     dim3 bl(32, 8), gr = box_grid(L.Nx, L.Nz);
-    if (l == H.nlev - 1) {
-        int maxit = 4 * (L.ncx > L.ncz ? L.ncx : L.ncz) + 50;
-        k_mg_coarse_cg<T><<<1, 1024, 0, st>>>(G, D, L.fu, L.fv, L.idu, L.idv, L.xu, L.xv, L.ru, L.rv, L.cg[0],
-                                              L.cg[1], L.cg[2], L.cg[3], L.cg[4], L.cg[5], maxit, 1e-6);
+    if (l == H.nlev - 1 && L.ndense) {
+        k_coarse_dense_solve<T><<<1, 256, 0, st>>>(L.ndense, (int)L.nu(), (int)L.nv(), L.dmap, L.AinvT, L.fu, L.fv,
+                                                   L.xu, L.xv);
         MDZ_LAUNCHED(ctx);
         return MDZ_OK;
     }
+    if (l == H.nlev - 1) {
+        int maxit = 4 * (L.ncx > L.ncz ? L.ncx : L.ncz) + 50;
+        k_mg_coarse_cg<T><<<1, 1024, 0, st>>>(G, L.su, L.sv, L.fu, L.fv, L.idu, L.idv, L.xu, L.xv, L.ru, L.rv,
+                                              L.cg[0], L.cg[1], L.cg[2], L.cg[3], L.cg[4], L.cg[5], maxit, 1e-6);
+        MDZ_LAUNCHED(ctx);
+        return MDZ_OK;
+    }
+    const bool viscous = l == 0 && !H.newton;   // level 0 of a Picard hierarchy: stencil from eta directly
+    auto smooth = [&](const T *xu, const T *xv, T *ou, T *ov) {
+        if (viscous) k_mg_smooth<T><<<gr, bl, 0, st>>>(G, D, xu, xv, L.fu, L.fv, L.idu, L.idv, omega, ou, ov);
+        else k_st_smooth<T><<<gr, bl, 0, st>>>(G, L.su, L.sv, xu, xv, L.fu, L.fv, L.idu, L.idv, omega, ou, ov);
+    };
     // pre-smoothing from x = 0
-    k_mg_smooth<T><<<gr, bl, 0, st>>>(G, D, nullptr, nullptr, L.fu, L.fv, L.idu, L.idv, omega, L.xu, L.xv);
+    smooth(nullptr, nullptr, L.xu, L.xv);
     MDZ_LAUNCHED(ctx);
     for (int s = 1; s < nu1; s++) {
-        k_mg_smooth<T><<<gr, bl, 0, st>>>(G, D, L.xu, L.xv, L.fu, L.fv, L.idu, L.idv, omega, L.yu, L.yv);
+        smooth(L.xu, L.xv, L.yu, L.yv);
         MDZ_LAUNCHED(ctx);
         std::swap(L.xu, L.yu); std::swap(L.xv, L.yv);
     }
-    k_mg_residual<T><<<gr, bl, 0, st>>>(G, D, L.xu, L.xv, L.fu, L.fv, L.ru, L.rv);
+    if (viscous) k_mg_residual<T><<<gr, bl, 0, st>>>(G, D, L.xu, L.xv, L.fu, L.fv, L.ru, L.rv);
+    else k_st_residual<T><<<gr, bl, 0, st>>>(G, L.su, L.sv, L.xu, L.xv, L.fu, L.fv, L.ru, L.rv);
     MDZ_LAUNCHED(ctx);
     mg_level<T> &C = H.L[l + 1];
     k_mg_restrict<T><<<box_grid(C.Nx, C.Nz), bl, 0, st>>>(G, C.geom(), L.ru, L.rv, C.fu, C.fv);
@@ -605,11 +1215,29 @@ static mdz_status vcycle(mdz_ctx *ctx, mg_hier<T> &H, int l, int nu1, int nu2, T
     k_mg_prolong_add<T><<<gr, bl, 0, st>>>(G, C.geom(), C.xu, C.xv, L.xu, L.xv);
     MDZ_LAUNCHED(ctx);
     for (int q = 0; q < nu2; q++) {
-        k_mg_smooth<T><<<gr, bl, 0, st>>>(G, D, L.xu, L.xv, L.fu, L.fv, L.idu, L.idv, omega, L.yu, L.yv);
+        smooth(L.xu, L.xv, L.yu, L.yv);
         MDZ_LAUNCHED(ctx);
         std::swap(L.xu, L.yu); std::swap(L.xv, L.yv);
     }
     return MDZ_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Pressure mean over the pressure equations (sum, count) and its removal.
+template <typename T>
+__global__ void k_psum(int np, const signed char *__restrict__ tp, const T *__restrict__ p, double *out) {
+    double acc[2] = {0.0, 0.0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x)
+        if (tp[i] == -1) { acc[0] += (double)p[i]; acc[1] += 1.0; }
+    for (int q = 0; q < 2; q++)
+        for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+    if ((threadIdx.x & 31) == 0) { atomicAdd(&out[0], acc[0]); atomicAdd(&out[1], acc[1]); }
+}
+
+template <typename T>
+__global__ void k_psub(int np, const signed char *__restrict__ tp, const double *__restrict__ sum, T *__restrict__ p) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < np && tp[i] == -1 && sum[1] > 0) p[i] = (T)((double)p[i] - sum[0] / sum[1]);
 }
 
 // ---------------------------------------------------------------------------
@@ -619,7 +1247,7 @@ __global__ void k_precond_p(stokes_geom G, const double *__restrict__ eta_n, con
                             T *__restrict__ zp) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= G.ncx * G.ncz) return;
-    zp[i] = G.BCp[i] == -1 ? (T)(eta_n[i] / (G.dx * G.dz)) * rp[i] : T(0);
+    zp[i] = G.BCp[i] == -1 ? (T)(eta_n[i] * (G.idx * G.idz)) * rp[i] : T(0);
 }
 
 // f = r_vel - B zp  on the fine MG level (B: celvol-scaled pressure gradient)
@@ -661,8 +1289,20 @@ static mdz_status precondition(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n,
                                size_t nv, cudaStream_t st) {
     mg_level<T> &F = H.L[0];
     stokes_geom G = F.geom();
-    k_precond_p<T><<<mdz_blocks(F.ncx * F.ncz), MDZ_THREADS, 0, st>>>(G, eta_n, r + nu + nv, z + nu + nv);
+    const int np = F.ncx * F.ncz;
+    k_precond_p<T><<<mdz_blocks(np), MDZ_THREADS, 0, st>>>(G, eta_n, r + nu + nv, z + nu + nv);
     MDZ_LAUNCHED(ctx);
+    // zero-mean pressure block: constants are the operator's null space; left
+    // in, they grow in the iterates and cost the FP32 gradients their accuracy
+    MDZ_CUDA(ctx, cudaMemsetAsync(H.pmean, 0, 2 * sizeof(double), st));
+    {
+        int blocks = mdz_blocks(np, 256);
+        if (blocks > 152 * 4) blocks = 152 * 4;
+        k_psum<T><<<blocks, 256, 0, st>>>(np, G.BCp, z + nu + nv, H.pmean);
+        MDZ_LAUNCHED(ctx);
+        k_psub<T><<<mdz_blocks(np), MDZ_THREADS, 0, st>>>(np, G.BCp, H.pmean, z + nu + nv);
+        MDZ_LAUNCHED(ctx);
+    }
     k_precond_rhs<T><<<box_grid(F.Nx, F.Nz), dim3(32, 8), 0, st>>>(G, r, r + nu, z + nu + nv, F.fu, F.fv);
     MDZ_LAUNCHED(ctx);
     mdz_solver *S = ctx->solver;
@@ -692,15 +1332,23 @@ __global__ void k_gcr_orth(size_t n, int k, const T *__restrict__ Z, const T *__
 }
 
 // second Gram-Schmidt pass, normalisation, store into slot k, update x and r.
-// dots[0..k-1] = (w, W_q), dots[k] = (w, w), dots[k+1] = (w, r)
-__global__ void k_gcr_scalars(int k, double *dots, double *out3) {
+// dots[0..k-1] = (w, W_q), dots[k] = (w, w), dots[k+1] = (w, r).
+// sc[0] = 1/||w||, sc[1] = alpha, sc[2] = ||w||^2, sc[3] = running ||r||^2
+// (updated here so the host reads it only every few iterations).
+__global__ void k_gcr_scalars(int k, double *dots, double *sc) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     double nrm2 = dots[k], wr = dots[k + 1];
     for (int q = 0; q < k; q++) nrm2 -= dots[q] * dots[q];
     double nrm = sqrt(nrm2 > 0 ? nrm2 : 0.0);
-    out3[0] = nrm > 0 ? 1.0 / nrm : 0.0;
-    out3[1] = nrm > 0 ? wr / nrm : 0.0;      // alpha = (r, w_hat); r is orthogonal to W_q, q < k
-    out3[2] = nrm2;
+    double alpha = nrm > 0 ? wr / nrm : 0.0;   // alpha = (r, w_hat); r is orthogonal to W_q, q < k
+    sc[0] = nrm > 0 ? 1.0 / nrm : 0.0;
+    sc[1] = alpha;
+    sc[2] = nrm2;
+    sc[3] -= alpha * alpha;
+}
+
+__global__ void k_set_scalar(double *dst, const double *src) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *dst = *src;
 }
 
 template <typename T>
@@ -739,20 +1387,6 @@ __global__ void k_convert(size_t n, const Tin *__restrict__ a, Tout *__restrict_
 // Pressure gauge: the decoupled operator annihilates a constant pressure, but
 // the rheology does not (pressure-dependent yield), so every correction is
 // returned with zero mean over the pressure equations.
-__global__ void k_psum(int np, const signed char *__restrict__ tp, const double *__restrict__ p, double *out) {
-    double acc[2] = {0.0, 0.0};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x)
-        if (tp[i] == -1) { acc[0] += p[i]; acc[1] += 1.0; }
-    for (int q = 0; q < 2; q++)
-        for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
-    if ((threadIdx.x & 31) == 0) { atomicAdd(&out[0], acc[0]); atomicAdd(&out[1], acc[1]); }
-}
-
-__global__ void k_psub(int np, const signed char *__restrict__ tp, const double *__restrict__ sum,
-                       double *__restrict__ p) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < np && tp[i] == -1 && sum[1] > 0) p[i] -= sum[0] / sum[1];
-}
 
 static mdz_status remove_pressure_mean(mdz_ctx *ctx, double *p, cudaStream_t st) {
     const mdz_dgrid &g = ctx->g;
@@ -761,17 +1395,17 @@ static mdz_status remove_pressure_mean(mdz_ctx *ctx, double *p, cudaStream_t st)
     MDZ_CUDA(ctx, cudaMemsetAsync(d, 0, 2 * sizeof(double), st));
     int blocks = mdz_blocks(np, 256);
     if (blocks > 152 * 4) blocks = 152 * 4;
-    k_psum<<<blocks, 256, 0, st>>>(np, g.BCp, p, d);
+    k_psum<double><<<blocks, 256, 0, st>>>(np, g.BCp, p, d);
     MDZ_LAUNCHED(ctx);
-    k_psub<<<mdz_blocks(np), MDZ_THREADS, 0, st>>>(np, g.BCp, d, p);
+    k_psub<double><<<mdz_blocks(np), MDZ_THREADS, 0, st>>>(np, g.BCp, d, p);
     MDZ_LAUNCHED(ctx);
     return MDZ_OK;
 }
 
-// dx(FP64) += e(FP32)
-__global__ void k_add_f32(size_t n, const float *__restrict__ e, double *__restrict__ x) {
+// dx(FP64) += sign * e(FP32)
+__global__ void k_add_f32(size_t n, const float *__restrict__ e, double *__restrict__ x, double sign) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) x[i] += (double)e[i];
+    if (i < n) x[i] += sign * (double)e[i];
 }
 
 template <typename T>
@@ -782,6 +1416,52 @@ static mdz_status dots_launch(mdz_ctx *ctx, gcr_space<T> &S, int q0, int nq, con
     multidot_launch<T>(nq, (int)S.nu, (int)S.nv, (int)S.np, S.dA0 + q0, S.dA1 + q0, S.dA2 + q0, b, b + S.nu,
                        b + S.nu + S.nv, out, st);
     MDZ_LAUNCHED(ctx);
+    return MDZ_OK;
+}
+
+// The preconditioner's ~10 launches per level, captured once per precision
+// (its buffers, coefficients and the Krylov vectors r, z never move; the
+// coefficients' values are refreshed by mg_setup outside the graph).
+template <typename T>
+static mdz_status precond_graph(mdz_ctx *ctx, gcr_space<T> &S, mg_hier<T> &H, const double *eta_n, cudaStream_t st,
+                                cudaGraphExec_t *out, long long *launches) {
+    mdz_solver *SV = ctx->solver;
+    const int slot = (sizeof(T) == 8 ? 0 : 2) + (H.newton ? 1 : 0);
+    if (SV->pre[slot] && SV->pre_eta[slot] == eta_n) {
+        *out = SV->pre[slot];
+        *launches = SV->pre_launches[slot];
+        return MDZ_OK;
+    }
+    if (SV->pre[slot]) { cudaGraphExecDestroy(SV->pre[slot]); SV->pre[slot] = nullptr; }
+    const long long l0 = ctx->launches;
+    MDZ_CUDA(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    mdz_status s = precondition<T>(ctx, H, eta_n, S.r, S.z, S.nu, S.nv, st);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (s != MDZ_OK) { if (g) cudaGraphDestroy(g); return s; }
+    if (e != cudaSuccess) return mdz_cuda_check(ctx, e, "preconditioner capture");
+    e = cudaGraphInstantiate(&SV->pre[slot], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { SV->pre[slot] = nullptr; return mdz_cuda_check(ctx, e, "preconditioner graph"); }
+    SV->pre_launches[slot] = ctx->launches - l0;
+    SV->pre_eta[slot] = eta_n;
+    {   // per level: nu1 + nu2 sweeps and one residual, each reading x, f, the
+        // inverse diagonal and both viscosities and writing one vector, plus
+        // the tags; restriction and prolongation one read + one write each;
+        // the fine-level pressure block and right-hand side 3 vectors
+        double b = 0.0;
+        for (int l = 0; l < H.nlev; l++) {
+            const mg_level<T> &L = H.L[l];
+            double nuv = (double)(L.nu() + L.nv()), nc = (double)L.ncx * L.ncz, ng = (double)L.Nx * L.Nz;
+            b += (SV->nu1 + SV->nu2 + 1) * (sizeof(T) * (4.0 * nuv + nc + ng) + (nuv + nc + ng));
+            b += 4.0 * sizeof(T) * nuv;
+        }
+        b += 3.0 * sizeof(T) * (double)S.n;
+        SV->pre_bytes[slot] = b;
+    }
+    ctx->launches = l0;
+    *out = SV->pre[slot];
+    *launches = SV->pre_launches[slot];
     return MDZ_OK;
 }
 
@@ -799,18 +1479,32 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, mg_hier<T> &H, const 
     // ||r0||
     double *dots = S.dots, *sc = S.dots + (GCR_MAX_M + 4);
     mdz_status s;
+    cudaGraphExec_t pre = nullptr;
+    long long pre_launches = 0;
+    if ((s = precond_graph<T>(ctx, S, H, eta_n, st, &pre, &pre_launches)) != MDZ_OK) return s;
     // (r, r) via the pointer-table slot m+1 against r itself
     if ((s = dots_launch<T>(ctx, S, S.m + 1, 1, S.r, dots, st)) != MDZ_OK) return s;
+    k_set_scalar<<<1, 32, 0, st>>>(sc + 3, dots);
+    MDZ_LAUNCHED(ctx);
     MDZ_CUDA(ctx, cudaMemcpyAsync(SV->sc, dots, sizeof(double), cudaMemcpyDeviceToHost, st));
     MDZ_CUDA(ctx, cudaStreamSynchronize(st));
+    {
+        const volatile int *flags = (const volatile int *)(SV->sc + 20);
+        if (flags[0]) return mdz_fail(ctx, MDZ_ERR_NOT_CONVERGED, "multigrid: coarsest-level block singular");
+        if (flags[1]) return mdz_fail(ctx, MDZ_ERR_STATE, "multigrid: Galerkin entry outside the stencil footprint");
+    }
     double rn2 = SV->sc[0], rn02 = rn2;
     int it = 0;
     if (rn02 == 0.0) { if (its_out) *its_out = 0; if (rel_out) *rel_out = 0.0; return MDZ_OK; }
     int k = 0;
+    const int check = SV->check > 0 ? SV->check : 1;
     for (it = 0; it < maxit; it++) {
         if (k == S.m) k = 0;   // restart: keep x and r, drop the basis
-        if ((s = precondition<T>(ctx, H, eta_n, S.r, S.z, nu, nv, st)) != MDZ_OK) return s;
         cudaEvent_t ev;
+        mdz_prof_begin(ctx, MDZ_PROF_MG_SMOOTH, st, &ev);
+        MDZ_CUDA(ctx, cudaGraphLaunch(pre, st));
+        ctx->launches += pre_launches;
+        mdz_prof_end(ctx, MDZ_PROF_MG_SMOOTH, SV->pre_bytes[(sizeof(T) == 8 ? 0 : 2) + (H.newton ? 1 : 0)], st, ev);
         mdz_prof_begin(ctx, MDZ_PROF_STOKES_APPLY, st, &ev);
         stokes_apply_launch<T>(G, K, stokes_cvec<T>{S.z, S.z + nu, S.z + nu + nv},
                                stokes_vec<T>{S.w, S.w + nu, S.w + nu + nv}, nullptr, newton, st);
@@ -833,15 +1527,19 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, mg_hier<T> &H, const 
         MDZ_LAUNCHED(ctx);
         k_gcr_finish<T><<<nb, MDZ_THREADS, 0, st>>>(n, k, S.Z, S.W, dots, sc, S.z, S.w, S.x, S.r);
         MDZ_LAUNCHED(ctx);
-        MDZ_CUDA(ctx, cudaMemcpyAsync(SV->sc, sc, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
-        MDZ_CUDA(ctx, cudaStreamSynchronize(st));
-        double alpha = SV->sc[1];
-        rn2 -= alpha * alpha;
         k++;
-        if (!std::isfinite(alpha)) return mdz_fail(ctx, MDZ_ERR_NAN, "GCR: NaN in the Krylov iteration");
+        // the running norm lives on the device; the host looks every `check`
+        // iterations, at each restart and at the iteration limit
+        if ((it + 1) % check != 0 && k != S.m && it + 1 < maxit) continue;
+        MDZ_CUDA(ctx, cudaMemcpyAsync(SV->sc, sc, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        MDZ_CUDA(ctx, cudaStreamSynchronize(st));
+        rn2 = SV->sc[3];
+        if (!std::isfinite(rn2)) return mdz_fail(ctx, MDZ_ERR_NAN, "GCR: NaN in the Krylov iteration");
         if (rn2 <= rtol * rtol * rn02 || (k == S.m)) {
             // recompute the true norm of r at convergence and at each restart
             if ((s = dots_launch<T>(ctx, S, S.m + 1, 1, S.r, dots, st)) != MDZ_OK) return s;
+            k_set_scalar<<<1, 32, 0, st>>>(sc + 3, dots);
+            MDZ_LAUNCHED(ctx);
             MDZ_CUDA(ctx, cudaMemcpyAsync(SV->sc, dots, sizeof(double), cudaMemcpyDeviceToHost, st));
             MDZ_CUDA(ctx, cudaStreamSynchronize(st));
             rn2 = SV->sc[0];
@@ -869,7 +1567,8 @@ mdz_status mdz_dev_solve(mdz_ctx *ctx, const mdz_fields &f, bool newton, int pre
     int its = 0, total = 0, cycles = 0;
     double rel = 1.0;
     if (precision == 64) {
-        if ((s = mg_setup<double>(ctx, SV->mg64, f.eta_n, f.eta_s, st)) != MDZ_OK) return s;
+        if ((s = mg_setup<double>(ctx, SV->mg64, f.eta_n, f.eta_s, K64, newton && SV->mg_jacobian, st)) != MDZ_OK)
+            return s;
         MDZ_CUDA(ctx, cudaMemcpyAsync(S64.r, F, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
         if ((s = gcr_solve<double>(ctx, S64, SV->mg64, K64, newton, f.eta_n, rtol, maxit, &its, &rel, st)) != MDZ_OK)
             return s;
@@ -878,7 +1577,6 @@ mdz_status mdz_dev_solve(mdz_ctx *ctx, const mdz_fields &f, bool newton, int pre
         cycles = 1;
     } else {
         gcr_space<float> &S32 = SV->g32;
-        if ((s = mg_setup<float>(ctx, SV->mg32, f.eta_n, f.eta_s, st)) != MDZ_OK) return s;
         // FP32 copy of the operator
         const double *Dsrc[12] = {f.D11_n, f.D12_n, f.D13_n, f.D14_n, f.D21_n, f.D22_n, f.D23_n, f.D24_n,
                                   f.D31_s, f.D32_s, f.D33_s, f.D34_s};
@@ -890,12 +1588,28 @@ mdz_status mdz_dev_solve(mdz_ctx *ctx, const mdz_fields &f, bool newton, int pre
         }
         stokes_coefs<float> K32{S32.Dc[0], S32.Dc[1], S32.Dc[2], S32.Dc[3], S32.Dc[4], S32.Dc[5], S32.Dc[6],
                                 S32.Dc[7], S32.Dc[8], S32.Dc[9], S32.Dc[10], S32.Dc[11]};
+        if ((s = mg_setup<float>(ctx, SV->mg32, f.eta_n, f.eta_s, K32, newton && SV->mg_jacobian, st)) != MDZ_OK)
+            return s;
         // defect correction: r64 = F - K64 dx64 ; solve K32 e = r64 ; dx64 += e
         MDZ_CUDA(ctx, cudaMemsetAsync(dx, 0, sizeof(double) * n, st));
         MDZ_CUDA(ctx, cudaMemcpyAsync(S64.r, F, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
         double *dn = (double *)(ctx->d_counters + 8);
         double r0 = -1.0, prev = 1e300;
-        for (cycles = 0; cycles < 12; cycles++) {
+        auto defect = [&]() -> mdz_status {   // r64 = F - K64 dx
+            stokes_apply_launch<double>(G, K64, stokes_cvec<double>{dx, dx + nu, dx + nu + nv},
+                                        stokes_vec<double>{S64.t, S64.t + nu, S64.t + nu + nv}, nullptr, newton, st);
+            MDZ_LAUNCHED(ctx);
+            MDZ_CUDA(ctx, cudaMemcpyAsync(S64.r, F, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+            k_axpby<double><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, -1.0, S64.t, 1.0, S64.r);
+            MDZ_LAUNCHED(ctx);
+            return MDZ_OK;
+        };
+        // Each cycle solves for the current FP64 defect in FP32.  An FP32 solve
+        // cannot resolve corrections whose K-image is below FP32 rounding of the
+        // stresses, so the contraction per cycle degrades on stiff problems: the
+        // loop runs while the defect still shrinks by 10 % and takes back a
+        // cycle that made it grow.
+        for (cycles = 0; cycles < 40; cycles++) {
             // norm of the FP64 defect
             if ((s = dots_launch<double>(ctx, S64, S64.m + 1, 1, S64.r, dn, st)) != MDZ_OK) return s;
             MDZ_CUDA(ctx, cudaMemcpyAsync(SV->sc + 8, dn, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -904,7 +1618,14 @@ mdz_status mdz_dev_solve(mdz_ctx *ctx, const mdz_fields &f, bool newton, int pre
             if (r0 < 0) r0 = rn;
             rel = r0 > 0 ? rn / r0 : 0.0;
             if (rel <= rtol || r0 == 0.0) break;
-            if (rel > 0.5 * prev || total >= maxit) break;   // refinement stalled or budget spent
+            if (cycles > 0 && rel > prev) {   // the last correction made it worse: undo it
+                k_add_f32<<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, S32.x, dx, -1.0);
+                MDZ_LAUNCHED(ctx);
+                if ((s = defect()) != MDZ_OK) return s;
+                rel = prev;
+                break;
+            }
+            if (rel > 0.9 * prev || total >= maxit) break;   // refinement stalled or budget spent
             prev = rel;
             k_convert<double, float><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, S64.r, S32.r);
             MDZ_LAUNCHED(ctx);
@@ -915,15 +1636,9 @@ mdz_status mdz_dev_solve(mdz_ctx *ctx, const mdz_fields &f, bool newton, int pre
                                       nullptr, st)) != MDZ_OK)
                 return s;
             total += its;
-            k_add_f32<<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, S32.x, dx);
+            k_add_f32<<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, S32.x, dx, 1.0);
             MDZ_LAUNCHED(ctx);
-            // r64 = F - K64 dx
-            stokes_apply_launch<double>(G, K64, stokes_cvec<double>{dx, dx + nu, dx + nu + nv},
-                                        stokes_vec<double>{S64.t, S64.t + nu, S64.t + nu + nv}, nullptr, newton, st);
-            MDZ_LAUNCHED(ctx);
-            MDZ_CUDA(ctx, cudaMemcpyAsync(S64.r, F, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-            k_axpby<double><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, -1.0, S64.t, 1.0, S64.r);
-            MDZ_LAUNCHED(ctx);
+            if ((s = defect()) != MDZ_OK) return s;
         }
     }
     if ((s = remove_pressure_mean(ctx, dx + nu + nv, st)) != MDZ_OK) return s;

@@ -281,10 +281,13 @@ static mdz_status residual_norms(mdz_ctx *ctx, double *norms3, cudaStream_t st) 
 // Main_DOODZ.c:830: each block converged in absolute or relative terms; a
 // block whose first residual is exactly zero (e.g. continuity of a
 // divergence-free initial guess) is measured against the largest first residual.
+// Each block converges on its absolute or relative tolerance; a block whose
+// first residual is negligible next to the largest one (an initially
+// divergence-free velocity makes resp0 round-off) is measured against that one.
 static bool converged(const mdz_model *M, const double *r, const double *r0) {
     double rmax = fmax(r0[0], fmax(r0[1], r0[2]));
     for (int q = 0; q < 3; q++) {
-        double ref = r0[q] > 0 ? r0[q] : rmax;
+        double ref = r0[q] > 1e-6 * rmax ? r0[q] : rmax;
         bool ok = r[q] < M->abs_tol || (ref > 0 && r[q] / ref < M->rel_tol);
         if (!ok) return false;
     }
@@ -365,6 +368,7 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
     // ---- 2. non-linear iterations -----------------------------------------------
     double r0[3] = {0, 0, 0}, r[3] = {0, 0, 0};
     int nit = 0;
+    bool use_newton = M->newton && !M->picard2newton;
     MDZ_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(int) * 4, st));
     for (nit = 0; nit <= M->nit_max; nit++) {
         {
@@ -381,27 +385,36 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
             break;
         }
         if (nit == M->nit_max) break;
+        // Picard -> Newton switch (Main_DOODZ.c:735-743)
+        if (M->newton && !use_newton && nit > 0 &&
+            (r[0] < M->pic2newt_cond * r0[0] || r[1] < M->pic2newt_cond * r0[1] || nit >= M->nit_pic_max))
+            use_newton = true;
         // defect F (grid layout) and the linear operator
         k_copy3<<<mdz_blocks(nmax), MDZ_THREADS, 0, st>>>(nu, nv, np, f.ru, f.rv, f.rp, B.F, B.F + nu, B.F + nu + nv);
         MDZ_LAUNCHED(ctx);
-        if (M->newton) {
+        if (use_newton) {
             if ((s = mdz_dev_operators(ctx, &M->rheo, f, 1, st)) != MDZ_OK) return s;
         }
         mdz_solve_stats ss{};
+        bool newton_step = use_newton;
         {
             step_timer T(st, &R.ms_solve);
-            s = mdz_dev_solve(ctx, f, M->newton != 0, M->precision, M->lin_rtol, M->lin_maxit, B.F, B.dx, &ss, st);
+            const int maxit = use_newton && M->newton_maxit > 0 ? M->newton_maxit : M->lin_maxit;
+            s = mdz_dev_solve(ctx, f, use_newton, M->precision, M->lin_rtol, maxit, B.F, B.dx, &ss, st);
             if (s != MDZ_OK) return s;
             R.linear_its += ss.iterations;
+            R.newton_its += use_newton ? 1 : 0;
             // A Newton system whose pressure Schur complement the Picard-based
-            // preconditioner cannot follow (strong non-associated plasticity)
+            // preconditioner cannot follow (strong pressure-dependent plasticity)
             // stalls the Krylov solve: take a Picard step for this iteration.
-            if (M->newton && !(ss.rel_residual <= 1e-2)) {
+            if (use_newton && !(ss.rel_residual <= 1e-2)) {
                 if ((s = mdz_dev_operators(ctx, &M->rheo, f, 0, st)) != MDZ_OK) return s;
                 s = mdz_dev_solve(ctx, f, false, M->precision, M->lin_rtol, M->lin_maxit, B.F, B.dx, &ss, st);
                 if (s != MDZ_OK) return s;
                 R.linear_its += ss.iterations;
                 R.picard_fallbacks++;
+                R.newton_its--;
+                newton_step = false;
             }
         }
         // line search / update
@@ -411,7 +424,7 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
         if (M->line_search) {
             step_timer T(st, &R.ms_line_search);
             const int ntry = 6;
-            double amin = M->newton ? -1.0 : -2.5, amax = M->newton ? -M->line_search_min : -0.0;
+            double amin = newton_step ? -1.0 : -2.5, amax = newton_step ? -M->line_search_min : -0.0;
             double da = fabs(amax - amin) / (ntry - 1), a = amax;
             double best = 1e300, rx[6], rz[6], rp[6], av[6];
             int ibest = 0;

@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(256) k_stokes_apply(stokes_geom G, stokes_coef
 
 stokes_geom mdz_stokes_geom(const mdz_ctx *ctx) {
     const mdz_dgrid &g = ctx->g;
-    return stokes_geom{g.Nx, g.Nz, g.ncx, g.ncz, g.dx, g.dz, g.BCu, g.BCv, g.BCp, g.BCg};
+    return make_geom(g.Nx, g.Nz, g.dx, g.dz, g.BCu, g.BCv, g.BCp, g.BCg);
 }
 
 template <typename T>

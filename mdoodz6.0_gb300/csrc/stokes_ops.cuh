@@ -44,7 +44,21 @@ struct stokes_geom {
     int Nx, Nz, ncx, ncz;
     double dx, dz;
     const signed char *BCu, *BCv, *BCp, *BCg;
+    double idx, idz;   // 1/dx, 1/dz: the stencils multiply (a division costs a
+                       // long FP64 instruction sequence on this part)
 };
+
+inline stokes_geom make_geom(int Nx, int Nz, double dx, double dz, const signed char *BCu, const signed char *BCv,
+                             const signed char *BCp, const signed char *BCg) {
+    return stokes_geom{Nx, Nz, Nx - 1, Nz - 1, dx, dz, BCu, BCv, BCp, BCg, 1.0 / dx, 1.0 / dz};
+}
+
+// 1/w for the averaging weights w in {2, 3, 4}; w in {0, 1} stays (exact
+// constants, identical to the division)
+template <typename T>
+__device__ __forceinline__ T wrecip(T w) {
+    return w > T(3.5) ? T(0.25) : (w > T(2.5) ? T(1.0 / 3.0) : (w > T(1.5) ? T(0.5) : w));
+}
 
 // x-momentum row at Vx node (k, l), k in 1..Nx-2, l in 1..Nz-1.
 template <typename T, bool NEWTON>
@@ -52,7 +66,7 @@ __device__ __forceinline__ T xrow(const stokes_geom &G, const stokes_coefs<T> &D
                                   int l) {
     const int nx = G.Nx, ncx = G.ncx, nxvz = nx + 1;
     const int c1 = k + l * nx, c2 = k - 1 + (l - 1) * ncx, c3 = k + l * nxvz;
-    const T dx = (T)G.dx, dz = (T)G.dz;
+    const T idx = (T)G.idx, idz = (T)G.idz;
     const int iPrW = c2, iPrE = c2 + 1, ixyN = c1, ixyS = c1 - nx;
     const T inW = G.BCp[iPrW] == -1 ? T(1) : T(0), inE = G.BCp[iPrE] == -1 ? T(1) : T(0);
     const T inS = (G.BCg[ixyS] != 30 && G.BCu[c1 - nx] != 13) ? T(1) : T(0);
@@ -61,13 +75,13 @@ __device__ __forceinline__ T xrow(const stokes_geom &G, const stokes_coefs<T> &D
     const T *u = x.u, *v = x.v, *p = x.p;
     auto exx_c = [&](int kc, int lc) {   // deviatoric normal rates at centroid (kc, lc)
         int cu = kc + (lc + 1) * nx, cv = kc + 1 + lc * nxvz;
-        T dudx = (u[cu + 1] - u[cu]) / dx, dvdz = (v[cv + nxvz] - v[cv]) / dz;
+        T dudx = (u[cu + 1] - u[cu]) * idx, dvdz = (v[cv + nxvz] - v[cv]) * idz;
         T div = dudx + dvdz;
-        return pair2<T>{dudx - div / T(3), dvdz - div / T(3)};
+        return pair2<T>{dudx - div * T(1.0 / 3.0), dvdz - div * T(1.0 / 3.0)};
     };
     auto gxz_v = [&](int kv, int lv) {   // engineering shear rate at vertex (kv, lv)
         int cu = kv + lv * nx, cv = kv + lv * nxvz;
-        return (u[cu + nx] - u[cu]) / dz + (v[cv + 1] - v[cv]) / dx;
+        return (u[cu + nx] - u[cu]) * idz + (v[cv + 1] - v[cv]) * idx;
     };
     pair2<T> eW = exx_c(k - 1, l - 1), eE = exx_c(k, l - 1);
     T gN = gxz_v(k, l), gS = gxz_v(k, l - 1);
@@ -100,10 +114,10 @@ __device__ __forceinline__ T xrow(const stokes_geom &G, const stokes_coefs<T> &D
         }
         T wE = inN + inS + inNEv + inSEv, wW = inN + inS + inNWv + inSWv;
         T wS = inW + inE + inSWc + inSEc, wN = inW + inE + inNWc + inNEc;
-        if (wW > T(1)) wW = T(1) / wW;
-        if (wE > T(1)) wE = T(1) / wE;
-        if (wS > T(1)) wS = T(1) / wS;
-        if (wN > T(1)) wN = T(1) / wN;
+        wW = wrecip(wW);
+        wE = wrecip(wE);
+        wS = wrecip(wS);
+        wN = wrecip(wN);
         // shear rate averaged onto the two centroids, with this row's weights
         T gNW = inNWv != T(0) ? gxz_v(k - 1, l) : T(0), gSW = inSWv != T(0) ? gxz_v(k - 1, l - 1) : T(0);
         T gNE = inNEv != T(0) ? gxz_v(k + 1, l) : T(0), gSE = inSEv != T(0) ? gxz_v(k + 1, l - 1) : T(0);
@@ -127,9 +141,9 @@ __device__ __forceinline__ T xrow(const stokes_geom &G, const stokes_coefs<T> &D
         TxzS = D.D31[ixyS] * exxS + D.D32[ixyS] * ezzS + D.D33[ixyS] * gS + D.D34[ixyS] * pS_;
         TxzN = D.D31[ixyN] * exxN + D.D32[ixyN] * ezzN + D.D33[ixyN] * gN + D.D34[ixyN] * pN_;
     }
-    T grad = (p && G.BCp[iPrE] != 30 && G.BCp[iPrW] != 30) ? (p[iPrE] - p[iPrW]) / dx : T(0);
-    if (NEWTON) grad = (inE * p[iPrE] - inW * p[iPrW]) / dx;
-    return -(inE * TxxE - inW * TxxW) / dx - (inN * TxzN - inS * TxzS) / dz + grad;
+    T grad = (p && G.BCp[iPrE] != 30 && G.BCp[iPrW] != 30) ? (p[iPrE] - p[iPrW]) * idx : T(0);
+    if (NEWTON) grad = (inE * p[iPrE] - inW * p[iPrW]) * idx;
+    return -(inE * TxxE - inW * TxxW) * idx - (inN * TxzN - inS * TxzS) * idz + grad;
 }
 
 // z-momentum row at Vz node (k, l), k in 1..Nx-1, l in 1..Nz-2.
@@ -138,7 +152,7 @@ __device__ __forceinline__ T zrow(const stokes_geom &G, const stokes_coefs<T> &D
                                   int l) {
     const int nx = G.Nx, ncx = G.ncx, nxvz = nx + 1;
     const int c3 = k + l * nxvz, c1 = k + l * nx, c2 = k - 1 + (l - 1) * ncx;
-    const T dx = (T)G.dx, dz = (T)G.dz;
+    const T idx = (T)G.idx, idz = (T)G.idz;
     const int iPrS = c2, iPrN = c2 + ncx, ixyW = c1 - 1, ixyE = c1;
     T inS = 0, inN = 0;
     if (G.BCv[c3 - nxvz] != 30 && G.BCv[c3 + nxvz] != 30) { inS = 1; inN = 1; }
@@ -151,13 +165,13 @@ __device__ __forceinline__ T zrow(const stokes_geom &G, const stokes_coefs<T> &D
     const T *u = x.u, *v = x.v, *p = x.p;
     auto exx_c = [&](int kc, int lc) {
         int cu = kc + (lc + 1) * nx, cv = kc + 1 + lc * nxvz;
-        T dudx = (u[cu + 1] - u[cu]) / dx, dvdz = (v[cv + nxvz] - v[cv]) / dz;
+        T dudx = (u[cu + 1] - u[cu]) * idx, dvdz = (v[cv + nxvz] - v[cv]) * idz;
         T div = dudx + dvdz;
-        return pair2<T>{dudx - div / T(3), dvdz - div / T(3)};
+        return pair2<T>{dudx - div * T(1.0 / 3.0), dvdz - div * T(1.0 / 3.0)};
     };
     auto gxz_v = [&](int kv, int lv) {
         int cu = kv + lv * nx, cv = kv + lv * nxvz;
-        return (u[cu + nx] - u[cu]) / dz + (v[cv + 1] - v[cv]) / dx;
+        return (u[cu + nx] - u[cu]) * idz + (v[cv + 1] - v[cv]) * idx;
     };
     pair2<T> eS = exx_c(k - 1, l - 1), eN = exx_c(k - 1, l);
     T gW = gxz_v(k - 1, l), gE = gxz_v(k, l);
@@ -190,10 +204,10 @@ __device__ __forceinline__ T zrow(const stokes_geom &G, const stokes_coefs<T> &D
         }
         T wE = inN + inS + inNEc + inSEc, wW = inN + inS + inNWc + inSWc;
         T wS = inW + inE + inSWv + inSEv, wN = inW + inE + inNWv + inNEv;
-        if (wW > T(1)) wW = T(1) / wW;
-        if (wE > T(1)) wE = T(1) / wE;
-        if (wS > T(1)) wS = T(1) / wS;
-        if (wN > T(1)) wN = T(1) / wN;
+        wW = wrecip(wW);
+        wE = wrecip(wE);
+        wS = wrecip(wS);
+        wN = wrecip(wN);
         // shear rate averaged onto centroids S and N
         T gSW = inSWv != T(0) ? gxz_v(k - 1, l - 1) : T(0), gSE = inSEv != T(0) ? gxz_v(k, l - 1) : T(0);
         T gNW = inNWv != T(0) ? gxz_v(k - 1, l + 1) : T(0), gNE = inNEv != T(0) ? gxz_v(k, l + 1) : T(0);
@@ -217,8 +231,8 @@ __device__ __forceinline__ T zrow(const stokes_geom &G, const stokes_coefs<T> &D
         TxzW = D.D31[ixyW] * exxW + D.D32[ixyW] * ezzW + D.D33[ixyW] * gW + D.D34[ixyW] * pW_;
         TxzE = D.D31[ixyE] * exxE + D.D32[ixyE] * ezzE + D.D33[ixyE] * gE + D.D34[ixyE] * pE_;
     }
-    T grad = (p && G.BCp[iPrS] != 30 && G.BCp[iPrN] != 30) ? (p[iPrN] - p[iPrS]) / dz : T(0);
-    return -(inN * TzzN - inS * TzzS) / dz - (inE * TxzE - inW * TxzW) / dx + grad;
+    T grad = (p && G.BCp[iPrS] != 30 && G.BCp[iPrN] != 30) ? (p[iPrN] - p[iPrS]) * idz : T(0);
+    return -(inN * TzzN - inS * TzzS) * idz - (inE * TxzE - inW * TxzW) * idx + grad;
 }
 
 // continuity row at centroid (k, l)
@@ -226,11 +240,11 @@ template <typename T>
 __device__ __forceinline__ T crow(const stokes_geom &G, const stokes_cvec<T> &x, int k, int l) {
     const int nx = G.Nx, nxvz = nx + 1;
     const int c1 = k + (l + 1) * nx, c3 = k + l * nxvz + 1;
-    const T dx = (T)G.dx, dz = (T)G.dz;
+    const T idx = (T)G.idx, idz = (T)G.idz;
     T r = 0;
-    if (G.BCu[c1] != 13) r += -x.u[c1] / dx;
-    if (G.BCu[c1 + 1] != 13) r += x.u[c1 + 1] / dx;
-    if (G.BCv[c3] != 13) r += -x.v[c3] / dz;
-    if (G.BCv[c3 + nxvz] != 13) r += x.v[c3 + nxvz] / dz;
+    if (G.BCu[c1] != 13) r += -x.u[c1] * idx;
+    if (G.BCu[c1 + 1] != 13) r += x.u[c1 + 1] * idx;
+    if (G.BCv[c3] != 13) r += -x.v[c3] * idz;
+    if (G.BCv[c3 + nxvz] != 13) r += x.v[c3 + nxvz] * idz;
     return r;
 }

@@ -289,7 +289,7 @@ class Context:
     def set_profiling(self, on):
         self._check(self.L.mdz_set_profiling(self.h, C.c_int(int(on))))
 
-    KERNEL_CLASSES = ["local_rheology", "stokes_apply", "mg_smooth", "projection"]
+    KERNEL_CLASSES = ["local_rheology", "stokes_apply", "mg_vcycle", "projection", "mlp_guess"]
 
     def kernel_timing(self):
         """Summed event time, algorithmic bytes and launch count per kernel class,
@@ -320,6 +320,21 @@ class Context:
                                                  C.c_double(rtol), C.c_int(maxit), _dptr(Fu), _dptr(Fv), _dptr(Fp),
                                                  _dptr(du), _dptr(dv), _dptr(dp), C.byref(its), C.byref(rel)))
         return du, dv, dp, its.value, rel.value
+
+    def set_solver_options(self, nu1=3, nu2=3, omega=0.7, restart=30, check=4, mg_jacobian=0):
+        self._check(self.L.mdz_set_solver_options(self.h, C.c_int(nu1), C.c_int(nu2), C.c_double(omega),
+                                                  C.c_int(restart), C.c_int(check), C.c_int(mg_jacobian)))
+
+    def mg_stencils(self, precision, level):
+        """(levels, Nx, Nz, su[31, Nx*(Nz+1)], sv[31, (Nx+1)*Nz]) of one multigrid level."""
+        nl, nx, nz = C.c_int(0), C.c_int(0), C.c_int(0)
+        self._check(self.L.mdz_mg_stencils(self.h, C.c_int(precision), C.c_int(level), C.byref(nl), C.byref(nx),
+                                           C.byref(nz), None, None))
+        su = np.zeros((31, nx.value * (nz.value + 1)))
+        sv = np.zeros((31, (nx.value + 1) * nz.value))
+        self._check(self.L.mdz_mg_stencils(self.h, C.c_int(precision), C.c_int(level), C.byref(nl), C.byref(nx),
+                                           C.byref(nz), _dptr(su), _dptr(sv)))
+        return nl.value, nx.value, nz.value, su, sv
 
     def StokesOperatorApply(self, fields, jacobian, xu, xv, xp):
         s = fields.struct()
@@ -429,12 +444,14 @@ class Materials(C.Structure):
 class RheoParams(C.Structure):
     _fields_ = [("dt", C.c_double), ("iselastic", C.c_int), ("step", C.c_int), ("eta_avg", C.c_int),
                 ("mineta", C.c_double), ("maxeta", C.c_double), ("scale_T", C.c_double), ("scale_E", C.c_double),
-                ("scale_S", C.c_double), ("scale_eta", C.c_double), ("scale_L", C.c_double)]
+                ("scale_S", C.c_double), ("scale_eta", C.c_double), ("scale_L", C.c_double),
+                ("clamp_tangent", C.c_int)]
 
     @classmethod
     def make(cls, dt, iselastic=1, step=1, eta_avg=0, mineta=1e-100, maxeta=1e100, scale_T=1.0, scale_E=1.0,
-             scale_S=1.0, scale_eta=1.0, scale_L=1.0):
-        return cls(dt, iselastic, step, eta_avg, mineta, maxeta, scale_T, scale_E, scale_S, scale_eta, scale_L)
+             scale_S=1.0, scale_eta=1.0, scale_L=1.0, clamp_tangent=0):
+        return cls(dt, iselastic, step, eta_avg, mineta, maxeta, scale_T, scale_E, scale_S, scale_eta, scale_L,
+                   clamp_tangent)
 
 
 # marker attributes (enum in include/mdoodz_gpu.h)
@@ -447,14 +464,16 @@ class Model(C.Structure):
                 ("nit_max", C.c_int), ("rel_tol", C.c_double), ("abs_tol", C.c_double), ("lin_rtol", C.c_double),
                 ("lin_maxit", C.c_int), ("line_search", C.c_int), ("line_search_min", C.c_double),
                 ("precision", C.c_int), ("learned_guess", C.c_int), ("itp_stencil", C.c_int),
-                ("softening", C.c_int), ("advect", C.c_int)]
+                ("softening", C.c_int), ("advect", C.c_int), ("picard2newton", C.c_int),
+                ("pic2newt_cond", C.c_double), ("nit_pic_max", C.c_int), ("newton_maxit", C.c_int)]
 
     @classmethod
     def make(cls, rheo, gx=0.0, gz=0.0, newton=1, nit_max=10, rel_tol=1e-8, abs_tol=1e-300, lin_rtol=1e-5,
              lin_maxit=500, line_search=0, line_search_min=0.0, precision=64, learned_guess=0, itp_stencil=1,
-             softening=0, advect=1):
+             softening=0, advect=1, picard2newton=0, pic2newt_cond=1e-1, nit_pic_max=10, newton_maxit=0):
         return cls(rheo, gx, gz, newton, nit_max, rel_tol, abs_tol, lin_rtol, lin_maxit, line_search,
-                   line_search_min, precision, learned_guess, itp_stencil, softening, advect)
+                   line_search_min, precision, learned_guess, itp_stencil, softening, advect, picard2newton,
+                   pic2newt_cond, nit_pic_max, newton_maxit)
 
 
 class StepReport(C.Structure):
@@ -463,7 +482,7 @@ class StepReport(C.Structure):
                 ("local_fallbacks", C.c_longlong), ("local_failures", C.c_longlong),
                 ("ms_projection", C.c_double), ("ms_rheology", C.c_double), ("ms_residual", C.c_double),
                 ("ms_solve", C.c_double), ("ms_line_search", C.c_double), ("ms_markers", C.c_double),
-                ("ms_total", C.c_double)]
+                ("ms_total", C.c_double), ("newton_its", C.c_int)]
 
     def as_dict(self):
         d = {}

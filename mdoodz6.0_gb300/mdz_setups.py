@@ -110,9 +110,9 @@ def config_lithosphere(Nx=1025, Nz=513, nm=4, seed=12345, precision=64, learned=
     """Layered lithosphere over 1000 x 400 km: upper crust 0-20 km, lower crust
     20-35 km, mantle lithosphere 35-120 km, asthenosphere; each phase with
     dislocation creep (n in [3.0, 3.5], A and Q log-uniform from the seed),
-    diffusion creep and Drucker-Prager plasticity; linear geotherm
-    0 -> 1330 C at 120 km then adiabatic (0.3 K/km); 1 cm/yr extension
-    (pure-shear walls); gravity.  Non-dimensionalised with Scales()."""
+    diffusion creep, Maxwell elasticity and Drucker-Prager plasticity; linear
+    geotherm 0 -> 1330 C at 120 km then adiabatic (0.3 K/km); 1 cm/yr
+    extension (pure-shear walls); gravity.  Non-dimensionalised with Scales()."""
     import mdz
     sc = Scales()
     L = sc.L
@@ -146,11 +146,16 @@ def config_lithosphere(Nx=1025, Nz=513, nm=4, seed=12345, precision=64, learned=
             alin=0.0, Flin=1.0, mu=3e10 / S, bet=1e-11 * S, C=1e7 / S, phi=np.pi / 6, psi=0.0, rho=rho, Slim=1e90,
             eta_vp=1e21 / sc.eta, n_vp=1.0, gs_ref=1.0, pls_start=0.0, pls_end=1.0))
     mat = mdz.Materials.from_phases(phases, R=R)
-    prm = mdz.RheoParams.make(dt=1e4 * 365.25 * 24 * 3600 / t, iselastic=0, step=1, eta_avg=0,
+    # visco-elasto-plastic (Maxwell elasticity, G = 30 GPa, dt = 10 kyr); the
+    # viscosity limiter's tangent is the derivative of the limited law
+    prm = mdz.RheoParams.make(dt=1e4 * 365.25 * 24 * 3600 / t, iselastic=1, step=1, eta_avg=0,
                               mineta=1e19 / sc.eta, maxeta=1e24 / sc.eta, scale_T=1.0, scale_E=sc.E,
-                              scale_S=sc.S, scale_eta=sc.eta, scale_L=sc.L)
-    model = mdz.Model.make(prm, gz=-9.81 * L / S, newton=1, nit_max=15, rel_tol=1e-8, lin_rtol=1e-5,
-                           line_search=1, precision=precision, learned_guess=learned)
+                              scale_S=sc.S, scale_eta=sc.eta, scale_L=sc.L, clamp_tangent=1)
+    # Picard iterations until resx or resz dropped tenfold, then Newton
+    # (Picard2Newton of the reference); 30 iterations at most
+    model = mdz.Model.make(prm, gz=-9.81 * L / S, newton=1, nit_max=30, rel_tol=1e-8, lin_rtol=1e-5,
+                           line_search=1, precision=precision, learned_guess=learned, picard2newton=1,
+                           pic2newt_cond=1e-1, nit_pic_max=10, newton_maxit=200)
     u, v = pure_shear_velocity(g, eps / sc.E)
     m = _markers_dict(x, z, ph, T=T)
     # initial pressure: lithostatic column of the layered densities (the

@@ -331,8 +331,15 @@ static void orc_visc(int p, double G, double T, double P, double d, double phi, 
     o->txx = Txx; o->tzz = Tzz; o->txz = Txz;
     if (eta > maxEta) eta = maxEta;
     if (eta < minEta) eta = minEta;
-    if (o->etaVE > maxEta) o->etaVE = maxEta;
-    if (o->etaVE < minEta) o->etaVE = minEta;
+    {
+        const int clamped = o->etaVE > maxEta || o->etaVE < minEta;
+        if (o->etaVE > maxEta) o->etaVE = maxEta;
+        if (o->etaVE < minEta) o->etaVE = minEta;
+        /* optional (not in the reference): tangent of the limited law */
+        if (clamped && prm->clamp_tangent) {
+            o->detadexx = 0.0; o->detadezz = 0.0; o->detadexz = 0.0; o->detadp = 0.0;
+        }
+    }
     o->eta = eta;
 }
 

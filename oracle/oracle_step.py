@@ -192,6 +192,7 @@ def time_step(g, mat, model, markers, u, v, p, fields_out=None):
     rep = dict(nonlinear_its=0, converged=0, stagnated=0)
     r0 = None
     nit = 0
+    use_newton = bool(model.newton) and not getattr(model, "picard2newton", 0)
     for nit in range(model.nit_max + 1):
         update_nonlinearity()
         r = res_norms()
@@ -202,15 +203,19 @@ def time_step(g, mat, model, markers, u, v, p, fields_out=None):
             break
         if nit == model.nit_max:
             break
+        # Picard -> Newton switch (Main_DOODZ.c:735-743)
+        if model.newton and not use_newton and nit > 0 and (
+                r[0] < model.pic2newt_cond * r0[0] or r[1] < model.pic2newt_cond * r0[1] or nit >= model.nit_pic_max):
+            use_newton = True
         F = np.concatenate([f["ru"], f["rv"], f["rp"]])
-        if model.newton:
+        if use_newton:
             orc.rheo_operators(g, prm, f, 1)
-        dx = solve_defect(g, f, model.newton, F)
+        dx = solve_defect(g, f, use_newton, F)
         u0, v0, p0 = u.copy(), v.copy(), p.copy()
         alpha = -1.0
         if model.line_search:
             ntry = 6
-            amin, amax = (-1.0, -model.line_search_min) if model.newton else (-2.5, -0.0)
+            amin, amax = (-1.0, -model.line_search_min) if use_newton else (-2.5, -0.0)
             da = abs(amax - amin) / (ntry - 1)
             a = amax
             trials = []
@@ -274,7 +279,7 @@ def time_step(g, mat, model, markers, u, v, p, fields_out=None):
 def _converged(model, r, r0):
     rmax = max(r0)
     for q in range(3):
-        ref = r0[q] if r0[q] > 0 else rmax
+        ref = r0[q] if r0[q] > 1e-6 * rmax else rmax
         if not (r[q] < model.abs_tol or (ref > 0 and r[q] / ref < model.rel_tol)):
             return False
     return True
