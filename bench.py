@@ -92,12 +92,30 @@ def peaks():
         return 6800.0, 1900.0, "fallback"
 
 
+# ranges of the learned guess's training tuples for the lithosphere model:
+# log10 strain rate [1/s], T [K], P [Pa], log10 dt [s]
+LO_LITHO, HI_LITHO = [-18.0, 273.0, 0.0, 9.0], [-12.0, 1800.0, 15e9, 12.0]
+# the local-rheology MLP workload: 2^24 tuples over these ranges, batch 65536
+LO_MLP, HI_MLP = [-18.0, 273.0, 0.0, 9.0], [-12.0, 1600.0, 5e9, 12.0]
+
+
+def train_guess(ctx, cfg, n=1 << 20, steps=3000, batch=65536, seed=1):
+    """Tuples labelled by the plain local solve of the model's materials, then
+    Adam on the device; returns (seconds, final loss)."""
+    t0 = time.perf_counter()
+    ctx.mlp_init(seed)
+    ctx.mlp_generate(cfg["mat"], cfg["model"].rheo, n, seed, LO_LITHO, HI_LITHO)
+    loss = ctx.mlp_train(steps, batch, 2e-3)
+    return time.perf_counter() - t0, loss
+
+
 def run_form(cfg_builder, precision, learned, steps, warmup, size):
     import mdz
     import mdz_setups
     cfg = cfg_builder(precision, learned, size)
     ctx = mdz_setups.load_context(cfg)
     model, mat = cfg["model"], cfg["mat"]
+    train = train_guess(ctx, cfg) if learned else None
     reps = []
     for _ in range(warmup):
         ctx.time_step(mat, model)
@@ -113,7 +131,30 @@ def run_form(cfg_builder, precision, learned, steps, warmup, size):
     gpu_ms = sum(r["ms_total"] for r in reps) / steps
     kern = ctx.kernel_timing()
     ctx.close()
-    return dict(ms_wall=wall, ms_gpu=gpu_ms, reports=reps, launches=launches, kernel=kern, cfg=cfg)
+    return dict(ms_wall=wall, ms_gpu=gpu_ms, reports=reps, launches=launches, kernel=kern, cfg=cfg, train=train)
+
+
+def mlp_workload():
+    """The local-rheology MLP on its own: 2^24 tuples of the lithosphere
+    phases, one epoch of training at batch 65536, inference over 2^24 cells."""
+    import mdz
+    import mdz_setups
+    cfg = mdz_setups.config_lithosphere(Nx=65, Nz=33)
+    ctx = mdz_setups.load_context(cfg)
+    n = 1 << 24
+    ctx.mlp_init(1)
+    t0 = time.perf_counter()
+    ctx.mlp_generate(cfg["mat"], cfg["model"].rheo, n, 5, LO_MLP, HI_MLP)
+    t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loss = ctx.mlp_train(n // 65536, 65536, 2e-3)
+    t_epoch = time.perf_counter() - t0
+    b = ctx.mlp_benchmark(65536, 5)
+    ctx.close()
+    flops = 2.0 * (16 * 64 + 64 * 64 + 64 * 8)   # per row, padded tensor-core shapes
+    return {"tuples": n, "batch": 65536, "generate_s": t_gen, "epoch_s": t_epoch, "loss": loss,
+            "ms_infer_2^24": b["ms_infer"], "ms_train_step": b["ms_train_step"], "rms_error": b["rms_error"],
+            "infer_tflops": flops * n / (b["ms_infer"] * 1e-3) / 1e12}
 
 
 def e2e_form(cfg_builder, precision, learned, steps, size):
@@ -127,6 +168,8 @@ def e2e_form(cfg_builder, precision, learned, steps, size):
     m = cfg["markers"]
     ctx = mdz_setups.load_context(cfg)
     model, mat = cfg["model"], cfg["mat"]
+    if learned:
+        train_guess(ctx, cfg)
     ctx.time_step(mat, model)
     g = cfg["grid"]
     out = mdz.GridFields(g, mat.n_phases)
@@ -190,6 +233,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", default=None, help="NXxNZ override (tests only)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mlp", action="store_true")
     args = ap.parse_args()
     rank, world, local = _dist()
     size = tuple(int(s) for s in args.size.split("x")) if args.size else None
@@ -222,13 +266,13 @@ def main():
     hbm, bf16, peak_kind = peaks()
     with ClockSampler(local) as clk:
         plain = run_form(b, 64, 0, args.steps, args.warmup, size)
-        fast = run_form(b, 32, 0, args.steps, args.warmup, size)
+        fast = run_form(b, 32, 1, args.steps, args.warmup, size)
     ms = fast["ms_wall"]
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
-    e2e_ms, h2d, d2h = e2e_form(b, 32, 0, max(1, args.steps - 1), size)
+    e2e_ms, h2d, d2h = e2e_form(b, 32, 1, max(1, args.steps - 1), size)
     k = fast["kernel"]
     achieved = k["bytes"] / (k["ms"] * 1e-3) / 1e9 if k["ms"] > 0 else None
     line = {
@@ -240,9 +284,10 @@ def main():
                    "markers": len(fast["cfg"]["markers"]["x"]),
                    "l2": "inputs larger than L2 (markers %.0f MB)" % (len(fast["cfg"]["markers"]["x"]) * 84 / 1e6),
                    "parallelism": "replicas" if world > 1 else "single"},
-        "forms": {"plain_fp64_ms": plain["ms_wall"], "fp32_ir_ms": fast["ms_wall"],
-                  "speedup_fp32_ir_vs_fp64": plain["ms_wall"] / fast["ms_wall"],
-                  "plain_report": plain["reports"][-1], "fp32_ir_report": fast["reports"][-1]},
+        "forms": {"plain_fp64_ms": plain["ms_wall"], "learned_fp32_ir_ms": fast["ms_wall"],
+                  "speedup_vs_plain_fp64": plain["ms_wall"] / fast["ms_wall"],
+                  "plain_report": plain["reports"][-1], "learned_fp32_ir_report": fast["reports"][-1],
+                  "guess_training_s": fast["train"][0], "guess_training_loss": fast["train"][1]},
         "e2e": {"value": e2e_ms, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": fast["launches"] // args.steps,
         "roofline": {"bound": "hbm", "kernel": k["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
@@ -250,6 +295,8 @@ def main():
                      "peak_kind": peak_kind},
         "clocks": clk.summary(),
     }
+    if rank == 0 and not args.no_mlp:
+        line["mlp"] = mlp_workload()
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_reference(size)
     if rank == 0:

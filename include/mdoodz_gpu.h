@@ -229,6 +229,52 @@ mdz_status mdz_StrainRateComponents(mdz_ctx *ctx, mdz_fields *f);
 mdz_status mdz_NonNewtonianViscosityGrid(mdz_ctx *ctx, const mdz_materials *mat, const mdz_rheo_params *prm,
                                          mdz_fields *f, int *n_not_converged);
 
+/* ---- learned start of the local solves (no counterpart in the reference) --
+ *
+ * An 8 -> 64 -> 64 -> 2 ReLU network (BF16 weights and activations, FP32
+ * accumulation, tensor-core kernels) maps (log10 strain-rate invariant [1/s],
+ * T [K], P [Pa], log10 dt [s], one-hot phase of at most 4) to the local
+ * Newton unknowns: y0 = (log10 eta_ve [Pa s] - 21) / 4 and y1 = gdot / (2 Eii).
+ * Each local solve then starts there, takes at most two polish updates
+ * (Halley steps in log eta_ve, Newton steps in gdot) and must pass the
+ * reference's own convergence test; otherwise it reruns the plain solve from
+ * the reference's start.  Parameters are MDZ_MLP_NPARAM FP32 values:
+ * W1[64][8], b1[64], W2[64][64], b2[64], W3[2][64], b3[2]. */
+#define MDZ_MLP_NPARAM 4866
+/* He-uniform weights from the seed, zero biases, Adam state cleared. */
+mdz_status mdz_mlp_init(mdz_ctx *ctx, unsigned long long seed);
+mdz_status mdz_mlp_set_weights(mdz_ctx *ctx, const float *params);
+mdz_status mdz_mlp_get_weights(mdz_ctx *ctx, float *params);
+/* Input normalisation ranges lo[4], hi[4] of (log10 Eii, T, P, log10 dt):
+ * x = 2 (v - lo) / (hi - lo) - 1, temperature as 1000 / T over
+ * [1000 / hi, 1000 / lo]. */
+mdz_status mdz_mlp_set_ranges(mdz_ctx *ctx, const double *lo, const double *hi);
+/* n training tuples on the device, drawn uniformly in the ranges (phase
+ * uniform among the materials' phases) and labelled by the plain local solve
+ * of these materials and switches (dt per tuple). */
+mdz_status mdz_mlp_generate(mdz_ctx *ctx, const mdz_materials *mat, const mdz_rheo_params *prm, long long n,
+                            unsigned long long seed, const double *lo, const double *hi);
+/* Adam on the mean squared error over consecutive batches of the tuples,
+ * learning rate decaying from lr to lr / 100 (cosine); *final_loss = mean loss
+ * of the last 8 steps. */
+mdz_status mdz_mlp_train(mdz_ctx *ctx, int steps, int batch, double lr, double *final_loss);
+/* Gradient of the mean squared error over n host rows (x: n x 8 normalised
+ * inputs, y: n x 2 labels) at the current weights, without an update:
+ * grad[MDZ_MLP_NPARAM] and *loss. */
+mdz_status mdz_mlp_gradients(mdz_ctx *ctx, int n, const float *x, const float *y, float *grad, double *loss);
+/* Network outputs for n host rows (x: n x 8 normalised inputs -> y: n x 2). */
+mdz_status mdz_mlp_infer(mdz_ctx *ctx, long long n, const float *x, float *y);
+/* Device timing over the generated tuples: one inference pass (ms), one
+ * training step of `batch` rows (ms), and the RMS error of the outputs against
+ * the labels. */
+mdz_status mdz_mlp_benchmark(mdz_ctx *ctx, int batch, int reps, double *ms_infer, double *ms_train_step,
+                             double *rms_error);
+/* NonNewtonianViscosityGrid with (learned = 1) or without the learned start;
+ * stats[4] = not converged, learned starts that fell back to the plain solve,
+ * learned starts, total local Newton updates. */
+mdz_status mdz_NonNewtonianViscosityGrid_learned(mdz_ctx *ctx, const mdz_materials *mat, const mdz_rheo_params *prm,
+                                                 mdz_fields *f, int learned, long long *stats);
+
 /* RheologicalOperators (SOURCE/RheologyDensity.c:713-954), isotropic:
  * Picard (jacobian = 0) or Newton (jacobian = 1) D11..D24 at centroids and
  * D31..D34 at vertices. */
@@ -347,6 +393,7 @@ typedef struct mdz_step_report {
     long long local_solves, local_fallbacks, local_failures;
     double ms_projection, ms_rheology, ms_residual, ms_solve, ms_line_search, ms_markers, ms_total;
     int newton_its;                   /* iterations solved with the Jacobian                  */
+    long long local_iterations;       /* local Newton updates of all local rheology solves    */
 } mdz_step_report;
 
 /* One time step of Main_DOODZ.c's loop (SOURCE/Main_DOODZ.c:459-1320) on the

@@ -3,6 +3,7 @@
 // RheologicalOperators, EvaluateRHS).
 #include <cstring>
 #include "mdz_internal.cuh"
+#include "mlp.cuh"
 
 size_t mdz_field_count(const mdz_ctx *ctx, int kind) {
     const mdz_dgrid &g = ctx->g;
@@ -83,18 +84,33 @@ extern "C" mdz_status mdz_StrainRateComponents(mdz_ctx *ctx, mdz_fields *f) {
     return mdz_download_fields(ctx, f, names, nnames, st);
 }
 
-extern "C" mdz_status mdz_NonNewtonianViscosityGrid(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm,
-                                                    mdz_fields *f, int *n_not_converged) {
+static mdz_status viscosity_grid(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm, mdz_fields *f,
+                                 int learned, long long *stats) {
     if (!ctx || !m || !prm || !f) return ctx ? mdz_fail(ctx, MDZ_ERR_ARG, "NonNewtonianViscosityGrid: null argument") : MDZ_ERR_ARG;
     mdz_status s = mdz_check_materials(ctx, m);
     if (s != MDZ_OK) return s;
     if ((s = mdz_ensure_fields(ctx)) != MDZ_OK) return s;
     cudaStream_t st = ctx->stream;
     if ((s = mdz_upload_fields(ctx, f, st)) != MDZ_OK) return s;
-    MDZ_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(int), st));
-    if ((s = mdz_dev_viscosity(ctx, m, prm, ctx->d, ctx->d_counters, st)) != MDZ_OK) return s;
-    int fails = 0;
-    MDZ_CUDA(ctx, cudaMemcpyAsync(&fails, ctx->d_counters, sizeof(int), cudaMemcpyDeviceToHost, st));
+    MDZ_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(int) * 4, st));
+    MDZ_CUDA(ctx, cudaMemsetAsync(ctx->d_counters + 48, 0, sizeof(unsigned long long), st));
+    if (learned) {
+        if ((s = mdz_dev_viscosity_learned(ctx, m, prm, ctx->d, ctx->d_counters, st)) != MDZ_OK) return s;
+    } else {
+        if ((s = mdz_dev_viscosity(ctx, m, prm, ctx->d, ctx->d_counters, st)) != MDZ_OK) return s;
+    }
+    int cnt[4] = {0, 0, 0, 0};
+    unsigned long long its = 0;
+    MDZ_CUDA(ctx, cudaMemcpyAsync(cnt, ctx->d_counters, sizeof cnt, cudaMemcpyDeviceToHost, st));
+    MDZ_CUDA(ctx, cudaMemcpyAsync(&its, ctx->d_counters + 48, sizeof its, cudaMemcpyDeviceToHost, st));
+    MDZ_CUDA(ctx, cudaStreamSynchronize(st));
+    if (stats) {
+        stats[0] = cnt[0];
+        stats[1] = cnt[1];
+        stats[2] = cnt[2];
+        stats[3] = (long long)its;
+    }
+    const int fails = cnt[0];
     NAMES("div_u_s", "T_s", "P_s", "d0_s", "phi0_s", "eta_n", "eta_s", "eta_phys_n", "eta_phys_s", "VE_n", "VE_s",
           "sxxd", "szzd", "sxz", "sxz_n", "eII_el", "eII_pl", "eII_pwl", "eII_lin", "eII_cst", "d_n", "exx_el",
           "ezz_el", "exz_el", "exx_diss", "ezz_diss", "exz_diss", "detadexx_n", "detadezz_n", "detadgxz_n",
@@ -102,8 +118,22 @@ extern "C" mdz_status mdz_NonNewtonianViscosityGrid(mdz_ctx *ctx, const mdz_mate
           "detadgxz_s", "detadp_s", "p_corr", "div_u_el", "div_u_pl", "div_u_r", "Wtot", "Wel", "Wdiss", "X_n",
           "X_s", "OverS_n", "OverS_s");
     s = mdz_download_fields(ctx, f, names, nnames, st);
-    if (n_not_converged) *n_not_converged = fails;
+    (void)fails;
     return s;
+}
+
+extern "C" mdz_status mdz_NonNewtonianViscosityGrid(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm,
+                                                    mdz_fields *f, int *n_not_converged) {
+    long long st4[4] = {0, 0, 0, 0};
+    mdz_status s = viscosity_grid(ctx, m, prm, f, 0, st4);
+    if (n_not_converged) *n_not_converged = (int)st4[0];
+    return s;
+}
+
+extern "C" mdz_status mdz_NonNewtonianViscosityGrid_learned(mdz_ctx *ctx, const mdz_materials *m,
+                                                            const mdz_rheo_params *prm, mdz_fields *f, int learned,
+                                                            long long *stats) {
+    return viscosity_grid(ctx, m, prm, f, learned, stats);
 }
 
 extern "C" mdz_status mdz_RheologicalOperators(mdz_ctx *ctx, const mdz_rheo_params *prm, mdz_fields *f, int jacobian) {

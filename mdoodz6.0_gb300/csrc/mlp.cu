@@ -415,12 +415,15 @@ extern "C" mdz_status mdz_mlp_set_ranges(mdz_ctx *ctx, const double *lo, const d
     mdz_status s = mlp_ensure(ctx);
     if (s != MDZ_OK) return s;
     mdz_mlp *M = ctx->mlp;
+    if (!(lo[1] > 0)) return mdz_fail(ctx, MDZ_ERR_ARG, "mlp_set_ranges: temperatures must be > 0 K");
     for (int k = 0; k < 4; k++) {
         if (!(hi[k] > lo[k])) return mdz_fail(ctx, MDZ_ERR_ARG, "mlp_set_ranges: range %d is empty", k);
         M->lo[k] = lo[k];
         M->hi[k] = hi[k];
-        M->norm.lo[k] = (float)lo[k];
-        M->norm.inv[k] = (float)(1.0 / (hi[k] - lo[k]));
+        // temperature is fed as 1000 / T
+        const double a = k == 1 ? 1000.0 / hi[k] : lo[k], b = k == 1 ? 1000.0 / lo[k] : hi[k];
+        M->norm.lo[k] = (float)a;
+        M->norm.inv[k] = (float)(1.0 / (b - a));
     }
     return MDZ_OK;
 }

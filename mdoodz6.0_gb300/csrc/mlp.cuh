@@ -2,8 +2,8 @@
 // in BF16 with FP32 accumulation on the tensor cores (mma.sync m16n8k16).
 //
 // Inputs (normalised to [-1, 1] by the training ranges): log10 of the strain
-// rate invariant [1/s], T [K], P [Pa], log10 dt [s], and a one-hot phase index
-// (4 phases).  Outputs: y0 = (log10 eta_ve [Pa s] - 21) / 4, the visco-elastic
+// rate invariant [1/s], T [K] (as 1000 / T), P [Pa], log10 dt [s], and a
+// one-hot phase index (4 phases).  Outputs: y0 = (log10 eta_ve [Pa s] - 21) / 4, the visco-elastic
 // viscosity the local Newton iteration solves for, and y1 = gdot / (2 Eii), the
 // plastic multiplier as a fraction of the strain rate.  The plain local Newton
 // polishes every guess and stays the judge (rheology.cu).
@@ -38,7 +38,7 @@
 #define MLP_PACK_BYTES (MLP_NBF16 * 2 + 136 * 4)
 
 struct mdz_mlp_norm {
-    float lo[4], inv[4];                 // x_k = 2 (v_k - lo_k) inv_k - 1
+    float lo[4], inv[4];                 // x_k = 2 (v_k - lo_k) inv_k - 1 (k = 1: v = 1000 / T)
 };
 
 // Context-resident MLP state (mlp.cu owns it).
@@ -191,10 +191,13 @@ __device__ __forceinline__ void mlp_warp_infer(const mlp_w &W, const __nv_bfloat
     }
 }
 
-// Normalised inputs of one (node, phase): Eii, T, P, dt in the solver's scaled units.
+// Normalised inputs of one (node, phase): Eii, T, P, dt in the solver's scaled
+// units.  Temperature enters as 1000 / T [1/K] (the creep laws are Arrhenius
+// in 1/T), normalised over the reciprocal of its range.
 __device__ __forceinline__ void mlp_inputs(const mdz_mlp_norm &nm, const mdz_rheo_params &prm, double Eii, double T,
                                            double P, double dt, int phase, float *x) {
-    const double v[4] = {log10(Eii * prm.scale_E), T * prm.scale_T, P * prm.scale_S, log10(dt / prm.scale_E)};
+    const double v[4] = {log10(Eii * prm.scale_E), 1000.0 / (T * prm.scale_T), P * prm.scale_S,
+                         log10(dt / prm.scale_E)};
 #pragma unroll
     for (int k = 0; k < 4; k++) x[k] = 2.0f * ((float)v[k] - nm.lo[k]) * nm.inv[k] - 1.0f;
 #pragma unroll

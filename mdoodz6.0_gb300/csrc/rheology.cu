@@ -217,8 +217,8 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
         if (constant) dfdeta += -Eii / eta_cst;
         eta_ve -= r / dfdeta;
     }
-    if (!ve_done) {
-        o.ve_its = it;
+    if (!ve_done) {   // iterations of a failed polish count too
+        o.ve_its = it + (guess ? MDZ_POLISH_STEPS : 0);
         if (it == nitmax - 1 && res > tol) o.ve_fail = 1;
     }
     o.eta_ve = eta_ve;
@@ -295,7 +295,7 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
             gdot -= F_trial / dFdgdot;
         }
         if (!vp_done) {
-            o.vp_its = it;
+            o.vp_its = it + (guess ? MDZ_POLISH_STEPS : 0);
             if (it == nitmax - 1 && (res > tol || res / F_trial0 > tol)) o.vp_fail = 1;
         }
         Txx = 2.0 * eta_ve * (Exx - gdot * dQdtxx);
@@ -397,17 +397,20 @@ __device__ __forceinline__ void put(double *p, int i, double v) {
 }
 
 // Counters of the local solves: [0] not converged, [1] learned starts whose
-// polish failed (plain solve rerun), [2] learned starts; warp-aggregated.
-__device__ __forceinline__ void count_local(int *counters, int fails, int fallbacks, int learned) {
+// polish failed (plain solve rerun), [2] learned starts (int32), and at int
+// offset 48 the 64-bit total of local Newton iterations (visco-elastic plus
+// plastic); warp-aggregated atomics.
+__device__ __forceinline__ void count_local(int *counters, int fails, int fallbacks, int learned, int iters) {
     if (!counters) return;
     const unsigned mask = __activemask();
     const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
     const int a = __reduce_add_sync(mask, fails), b = __reduce_add_sync(mask, fallbacks),
-              c = __reduce_add_sync(mask, learned);
+              c = __reduce_add_sync(mask, learned), d = __reduce_add_sync(mask, iters);
     if (lane == leader) {
         if (a) atomicAdd(&counters[0], a);
         if (b) atomicAdd(&counters[1], b);
         if (c) atomicAdd(&counters[2], c);
+        if (d) atomicAdd(reinterpret_cast<unsigned long long *>(counters + 48), (unsigned long long)d);
     }
 }
 
@@ -422,7 +425,7 @@ __global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_ma
     double eta = 0, eta_phys = 0, VE = 0, sxx = 0, szz = 0, sxz = 0, eel = 0, epl = 0, epwl = 0, elin = 0, ecst = 0,
            dn = 0, xel = 0, xdi = 0, zel = 0, zdi = 0, dexx = 0, dezz = 0, dgxz = 0, dp = 0, vxx = 0, vzz = 0,
            vxz = 0, vp = 0, pc = 0, del = 0, dpl = 0, Wt = 0, We = 0, Wd = 0, X = 0, OS = 0;
-    int fails = 0, fallbacks = 0, learned = 0;
+    int fails = 0, fallbacks = 0, learned = 0, iters = 0;
     signed char t = g.BCp[c];
     if (t != 30 && t != 31) {
         const double etae = prm.iselastic == 1 ? prm.dt * f.mu_n[c] : 1.0;
@@ -446,6 +449,7 @@ __global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_ma
                        fric, Coh, P0, bet, o, guess ? gs : nullptr);
             fails += o.ve_fail + o.vp_fail;
             fallbacks += o.fallback;
+            iters += o.ve_its + o.vp_its;
             learned += o.learned;
             if (avg == 0) {
                 eta += w * o.etaVE; eta_phys += w * o.eta; dexx += w * o.detadexx; dezz += w * o.detadezz;
@@ -496,7 +500,7 @@ __global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_ma
     put(f.ddivpdexx_n, c, vxx); put(f.ddivpdezz_n, c, vzz); put(f.ddivpdgxz_n, c, vxz); put(f.ddivpdp_n, c, vp);
     put(f.p_corr, c, pc); put(f.div_u_el, c, del); put(f.div_u_pl, c, dpl); put(f.div_u_r, c, 0.0);
     put(f.Wtot, c, Wt); put(f.Wel, c, We); put(f.Wdiss, c, Wd); put(f.X_n, c, X); put(f.OverS_n, c, OS);
-    count_local(counters, fails, fallbacks, learned);
+    count_local(counters, fails, fallbacks, learned, iters);
 }
 
 __global__ void __launch_bounds__(128) k_viscosity_vertices(mdz_dgrid g, mdz_materials m, mdz_rheo_params prm,
@@ -508,7 +512,7 @@ __global__ void __launch_bounds__(128) k_viscosity_vertices(mdz_dgrid g, mdz_mat
     const int avg = prm.eta_avg, nph = m.n_phases;
     double VE = 0, sxz = 0, eta_phys = 0, eta = 0, zel = 0, zdi = 0, dexx = 0, dezz = 0, dgxz = 0, dp = 0, X = 0,
            OS = 0;
-    int fails = 0, fallbacks = 0, learned = 0;
+    int fails = 0, fallbacks = 0, learned = 0, iters = 0;
     if (g.BCg[c] != 30) {
         const double etae = prm.iselastic == 1 ? prm.dt * f.mu_s[c] : 1.0;
         const double sxx0 = f.sxxd0_s[c], szz0 = f.szzd0_s[c], sxz0 = f.sxz0[c];
@@ -530,6 +534,7 @@ __global__ void __launch_bounds__(128) k_viscosity_vertices(mdz_dgrid g, mdz_mat
                        fric, Coh, P0, bet, o, guess ? gs : nullptr);
             fails += o.ve_fail + o.vp_fail;
             fallbacks += o.fallback;
+            iters += o.ve_its + o.vp_its;
             learned += o.learned;
             if (avg == 0) {
                 eta += w * o.etaVE; eta_phys += w * o.eta; dexx += w * o.detadexx; dezz += w * o.detadezz;
@@ -563,7 +568,7 @@ __global__ void __launch_bounds__(128) k_viscosity_vertices(mdz_dgrid g, mdz_mat
     put(f.exz_el, c, zel); put(f.exz_diss, c, zdi);
     put(f.detadexx_s, c, dexx); put(f.detadezz_s, c, dezz); put(f.detadgxz_s, c, dgxz); put(f.detadp_s, c, dp);
     put(f.X_s, c, X); put(f.OverS_s, c, OS);
-    count_local(counters, fails, fallbacks, learned);
+    count_local(counters, fails, fallbacks, learned, iters);
 }
 
 // ---------------------------------------------------------------------------

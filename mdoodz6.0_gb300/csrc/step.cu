@@ -370,6 +370,7 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
     int nit = 0;
     bool use_newton = M->newton && !M->picard2newton;
     MDZ_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(int) * 4, st));
+    MDZ_CUDA(ctx, cudaMemsetAsync(ctx->d_counters + 48, 0, sizeof(unsigned long long), st));
     for (nit = 0; nit <= M->nit_max; nit++) {
         {
             step_timer T(st, &R.ms_rheology);
@@ -507,6 +508,9 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
     R.local_failures = cnt[0];
     R.local_fallbacks = cnt[1];
     R.local_solves = cnt[2];
+    unsigned long long li = 0;
+    MDZ_CUDA(ctx, cudaMemcpy(&li, ctx->d_counters + 48, sizeof li, cudaMemcpyDeviceToHost));
+    R.local_iterations = (long long)li;
     if (rep) *rep = R;
     return MDZ_OK;
 }

@@ -254,6 +254,65 @@ class Context:
                                                          C.byref(nc)))
         return nc.value
 
+    def NonNewtonianViscosityGrid_learned(self, mat, prm, fields, learned):
+        """Local rheology with or without the learned start; returns the
+        statistics (not converged, fall-backs, learned starts, local updates)."""
+        s = fields.struct()
+        st = (C.c_longlong * 4)()
+        self._check(self.L.mdz_NonNewtonianViscosityGrid_learned(self.h, C.byref(mat), C.byref(prm), C.byref(s),
+                                                                 C.c_int(learned), st))
+        return dict(failures=st[0], fallbacks=st[1], learned=st[2], iterations=st[3])
+
+    # learned guess --------------------------------------------------------------
+    MLP_NPARAM = 4866
+
+    def mlp_init(self, seed):
+        self._check(self.L.mdz_mlp_init(self.h, C.c_ulonglong(seed)))
+
+    def mlp_set_weights(self, w):
+        w = np.ascontiguousarray(w, np.float32)
+        assert w.size == self.MLP_NPARAM
+        self._check(self.L.mdz_mlp_set_weights(self.h, w.ctypes.data_as(C.POINTER(C.c_float))))
+
+    def mlp_get_weights(self):
+        w = np.zeros(self.MLP_NPARAM, np.float32)
+        self._check(self.L.mdz_mlp_get_weights(self.h, w.ctypes.data_as(C.POINTER(C.c_float))))
+        return w
+
+    def mlp_generate(self, mat, prm, n, seed, lo, hi):
+        lo = np.ascontiguousarray(lo, np.float64)
+        hi = np.ascontiguousarray(hi, np.float64)
+        self._check(self.L.mdz_mlp_generate(self.h, C.byref(mat), C.byref(prm), C.c_longlong(n), C.c_ulonglong(seed),
+                                            _dptr(lo), _dptr(hi)))
+
+    def mlp_train(self, steps, batch, lr):
+        loss = C.c_double(0)
+        self._check(self.L.mdz_mlp_train(self.h, C.c_int(steps), C.c_int(batch), C.c_double(lr), C.byref(loss)))
+        return loss.value
+
+    def mlp_gradients(self, x, y):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.ascontiguousarray(y, np.float32)
+        g = np.zeros(self.MLP_NPARAM, np.float32)
+        loss = C.c_double(0)
+        fp = C.POINTER(C.c_float)
+        self._check(self.L.mdz_mlp_gradients(self.h, C.c_int(len(x)), x.ctypes.data_as(fp), y.ctypes.data_as(fp),
+                                             g.ctypes.data_as(fp), C.byref(loss)))
+        return g, loss.value
+
+    def mlp_infer(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.zeros((len(x), 2), np.float32)
+        fp = C.POINTER(C.c_float)
+        self._check(self.L.mdz_mlp_infer(self.h, C.c_longlong(len(x)), x.ctypes.data_as(fp), y.ctypes.data_as(fp)))
+        return y
+
+    def mlp_benchmark(self, batch, reps):
+        a, b, c = C.c_double(0), C.c_double(0), C.c_double(0)
+        self._check(self.L.mdz_mlp_benchmark(self.h, C.c_int(batch), C.c_int(reps), C.byref(a), C.byref(b),
+                                             C.byref(c)))
+        return dict(ms_infer=a.value, ms_train_step=b.value, rms_error=c.value)
+
     def RheologicalOperators(self, prm, fields, jacobian):
         s = fields.struct()
         self._check(self.L.mdz_RheologicalOperators(self.h, C.byref(prm), C.byref(s), C.c_int(jacobian)))
@@ -482,7 +541,7 @@ class StepReport(C.Structure):
                 ("local_fallbacks", C.c_longlong), ("local_failures", C.c_longlong),
                 ("ms_projection", C.c_double), ("ms_rheology", C.c_double), ("ms_residual", C.c_double),
                 ("ms_solve", C.c_double), ("ms_line_search", C.c_double), ("ms_markers", C.c_double),
-                ("ms_total", C.c_double), ("newton_its", C.c_int)]
+                ("ms_total", C.c_double), ("newton_its", C.c_int), ("local_iterations", C.c_longlong)]
 
     def as_dict(self):
         d = {}

@@ -1,0 +1,106 @@
+"""Learned local-rheology guess on the device: the tensor-core forward and
+backward passes against the CPU restatement, training on tuples labelled by
+the plain local solve, and what the learned start gains over the plain one on
+a lithosphere state (same fields to 1e-9, fewer local Newton updates)."""
+import numpy as np
+import pytest
+
+import mdz
+import mdz_setups
+import mlp_oracle as mo
+
+pytestmark = pytest.mark.gpu
+
+LO_C3 = [-18.0, 273.0, 0.0, 9.0]
+HI_C3 = [-12.0, 1800.0, 15e9, 12.0]
+
+
+def _ctx():
+    g = mdz.Grid(9, 9, 0.0, 1.0, 0.0, 1.0).set_bc_pureshear(1.0)
+    return mdz.Context(g, 4, 1)
+
+
+def _rows(n, seed):
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-1, 1, (n, 8)).astype(np.float32)
+    x[:, 4:] = np.eye(4)[rng.integers(0, 4, n)]
+    y = rng.normal(0.0, 1.0, (n, 2)).astype(np.float32)
+    return x, y
+
+
+def _rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("n", [128, 1000, 70000])     # one tile, a ragged tail, many CTAs
+def test_gradients_match_cpu_oracle(n):
+    ctx = _ctx()
+    ctx.mlp_init(11)
+    p = ctx.mlp_get_weights().astype(np.float64)
+    rng = np.random.default_rng(5)
+    p[mo.SLICES["b1"][0]:mo.SLICES["b1"][0] + 64] = rng.normal(0, 0.1, 64)   # non-zero biases
+    p[mo.SLICES["b2"][0]:mo.SLICES["b2"][0] + 64] = rng.normal(0, 0.1, 64)
+    ctx.mlp_set_weights(p)
+    x, y = _rows(n, n)
+    g, loss = ctx.mlp_gradients(x, y)
+    ref_loss, ref = mo.loss_and_gradients(p, x.astype(np.float64), y.astype(np.float64), bf=True)
+    assert abs(loss - ref_loss) <= 1e-4 * ref_loss
+    for name, (o, shape) in mo.SLICES.items():
+        k = int(np.prod(shape))
+        assert _rel(g[o:o + k], ref[o:o + k]) < 1e-2, name
+    ctx.close()
+
+
+def test_inference_matches_cpu_oracle():
+    ctx = _ctx()
+    ctx.mlp_init(2)
+    p = ctx.mlp_get_weights().astype(np.float64)
+    x, _ = _rows(5000, 9)
+    y = ctx.mlp_infer(x)
+    ref = mo.forward(p, x.astype(np.float64), bf=True)[3]
+    assert np.max(np.abs(y - ref)) <= 1e-3 * (1.0 + np.max(np.abs(ref)))
+    ctx.close()
+
+
+def _c3_materials():
+    cfg = mdz_setups.config_lithosphere(Nx=65, Nz=33)
+    return cfg
+
+
+def test_training_on_local_solves():
+    cfg = _c3_materials()
+    ctx = mdz_setups.load_context(cfg)
+    ctx.mlp_init(1)
+    ctx.mlp_generate(cfg["mat"], cfg["model"].rheo, 1 << 17, 7, LO_C3, HI_C3)
+    first = ctx.mlp_benchmark(4096, 1)["rms_error"]
+    loss = ctx.mlp_train(1500, 8192, 2e-3)
+    after = ctx.mlp_benchmark(4096, 1)["rms_error"]
+    assert np.isfinite(loss) and after < 0.1 * first, (first, after, loss)
+    ctx.close()
+
+
+def test_learned_start_ablation():
+    """Same lithosphere state, local rheology with and without the learned
+    start: identical fields within the local solver's tolerance, fewer local
+    Newton updates, few fall-backs."""
+    cfg = mdz_setups.config_lithosphere(Nx=129, Nz=65)
+    ctx = mdz_setups.load_context(cfg)
+    ctx.time_step(cfg["mat"], cfg["model"])
+    g = cfg["grid"]
+    f = mdz.GridFields(g, cfg["mat"].n_phases)
+    ctx.download_fields(f)
+    ctx.mlp_init(1)
+    ctx.mlp_generate(cfg["mat"], cfg["model"].rheo, 1 << 18, 3, LO_C3, HI_C3)
+    ctx.mlp_train(3000, 16384, 2e-3)
+    prm = cfg["model"].rheo
+    plain = ctx.NonNewtonianViscosityGrid_learned(cfg["mat"], prm, f, 0)
+    out0 = {k: f[k].copy() for k in ("eta_n", "eta_s", "sxxd", "sxz", "detadexx_n", "detadgxz_s", "p_corr")}
+    learned = ctx.NonNewtonianViscosityGrid_learned(cfg["mat"], prm, f, 1)
+    for k, v in out0.items():
+        d = np.linalg.norm(f[k] - v) / max(np.linalg.norm(v), 1e-300)
+        assert d < 1e-9, (k, d)
+    assert plain["failures"] == 0 and learned["failures"] == 0
+    assert learned["learned"] > 0
+    assert learned["fallbacks"] <= 0.1 * learned["learned"], learned
+    assert learned["iterations"] < 0.7 * plain["iterations"], (plain, learned)
+    ctx.close()
