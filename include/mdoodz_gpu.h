@@ -234,7 +234,9 @@ mdz_status mdz_NonNewtonianViscosityGrid(mdz_ctx *ctx, const mdz_materials *mat,
  * An 8 -> 64 -> 64 -> 2 ReLU network (BF16 weights and activations, FP32
  * accumulation, tensor-core kernels) maps (log10 strain-rate invariant [1/s],
  * T [K], P [Pa], log10 dt [s], one-hot phase of at most 4) to the local
- * Newton unknowns: y0 = (log10 eta_ve [Pa s] - 21) / 4 and y1 = gdot / (2 Eii).
+ * Newton unknowns: y0 = ln(eta_ve / eta_up), the visco-elastic viscosity
+ * relative to the plain iteration's start eta_up (smallest viscosity of the
+ * active mechanisms), and y1 = gdot / (2 Eii).
  * Each local solve then starts there, takes at most two polish updates
  * (Halley steps in log eta_ve, Newton steps in gdot) and must pass the
  * reference's own convergence test; otherwise it reruns the plain solve from
@@ -294,6 +296,7 @@ mdz_status mdz_EvaluateRHS(mdz_ctx *ctx, const mdz_rheo_params *prm, double gx, 
  * x-momentum, z-momentum and continuity blocks.  MDZ_ERR_NAN where the
  * reference exit(122)s. */
 mdz_status mdz_EvaluateStokesResidualDecoupled(mdz_ctx *ctx, mdz_fields *f, double *norms3);
+
 
 /* Matrix-free linear operator, the product of the reference's assembled
  * blocks with a correction vector (x zero on non-equation nodes):

@@ -3,10 +3,14 @@
 //
 // Inputs (normalised to [-1, 1] by the training ranges): log10 of the strain
 // rate invariant [1/s], T [K] (as 1000 / T), P [Pa], log10 dt [s], and a
-// one-hot phase index (4 phases).  Outputs: y0 = (log10 eta_ve [Pa s] - 21) / 4, the visco-elastic
-// viscosity the local Newton iteration solves for, and y1 = gdot / (2 Eii), the
-// plastic multiplier as a fraction of the strain rate.  The plain local Newton
-// polishes every guess and stays the judge (rheology.cu).
+// one-hot phase index (4 phases).  Outputs: y0 = ln(eta_ve / eta_up), the
+// visco-elastic viscosity the local Newton iteration solves for, relative to
+// that iteration's plain start eta_up (the smallest viscosity of the active
+// mechanisms, which the local solve computes anyway), and y1 = gdot / (2 Eii),
+// the plastic multiplier as a fraction of the strain rate.  Predicting the
+// correction to the plain start keeps the target within a few units, where the
+// BF16 network is accurate to a per cent.  The plain local Newton polishes
+// every guess and stays the judge (rheology.cu).
 //
 // Layouts shared by every kernel: weights live in shared memory as BF16 rows
 // with padded strides (24 or 72 elements: conflict-free fragment loads), in
@@ -204,13 +208,8 @@ __device__ __forceinline__ void mlp_inputs(const mdz_mlp_norm &nm, const mdz_rhe
     for (int q = 0; q < 4; q++) x[4 + q] = q == phase ? 1.0f : 0.0f;
 }
 
-// Network outputs -> local-solve start: (natural log of eta_ve in scaled units, plastic fraction)
-__device__ __forceinline__ float2 mlp_to_guess(float y0, float y1, const mdz_rheo_params &prm) {
-    const double l10 = 2.302585092994045684;
-    return make_float2((float)(l10 * (21.0 + 4.0 * (double)y0) - log(prm.scale_eta)), y1);
-}
-
-// Training labels from a converged local solve.
-__device__ __forceinline__ float2 mlp_labels(double eta_ve, double gdot, double Eii, const mdz_rheo_params &prm) {
-    return make_float2((float)((log10(eta_ve * prm.scale_eta) - 21.0) * 0.25), (float)(gdot / (2.0 * Eii)));
+// Training labels from a converged local solve: the visco-elastic viscosity
+// relative to the iteration's plain start, and the plastic fraction.
+__device__ __forceinline__ float2 mlp_labels(double eta_ve, double eta_up, double gdot, double Eii) {
+    return make_float2((float)log(eta_ve / eta_up), (float)(gdot / (2.0 * Eii)));
 }

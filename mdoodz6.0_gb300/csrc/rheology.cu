@@ -100,6 +100,7 @@ struct visc_res {
     double detadexx, detadezz, detadexz, detadp, X1, OverS;
     double ddivpdexx, ddivpdezz, ddivpdexz, ddivpdp, Pcorr, div_el, div_pl;
     double eta_ve, gdot;    // converged local unknowns (training labels of the learned guess)
+    double eta_up;          // the reference's start of the visco-elastic iteration
     int ve_fail, vp_fail, ve_its, vp_its;
     int learned, fallback;  // started from a learned guess; polish failed and the plain solve reran
 };
@@ -168,6 +169,7 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     double eta_ve = eta_up, Tii;
     const double dm_lin = pow(o.d1, -m_lin);
     bool ve_done = false;
+    o.eta_up = eta_up;
     o.learned = guess != nullptr;
     o.fallback = 0;
     if (guess) {
@@ -175,7 +177,9 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
         // g(s) = log(sum of the strain rates) - log(Eii): every mechanism's
         // rate is c_k exp(n_k s), so g' and g'' are rate-weighted means of n_k
         // and n_k^2.  Converged means the reference's own test below holds.
-        double s = (double)guess[0];
+        // The network predicts ln(eta_ve / eta_up), eta_up being the
+        // reference's start (the smallest viscosity of the active mechanisms).
+        double s = log(eta_up) + (double)guess[0];
         for (it = 0; it <= MDZ_POLISH_STEPS; it++) {
             eta_ve = exp(s);
             Tii = 2.0 * f_ani * eta_ve * Eii;
@@ -769,7 +773,7 @@ __global__ void __launch_bounds__(256) k_mlp_guess(mdz_dgrid g, int nph, mdz_rhe
             __syncwarp();
             mlp_warp_infer(W, xs, ys);
             __syncwarp();
-            if (need) guess[(size_t)p * nn + c] = mlp_to_guess(ys[2 * lane], ys[2 * lane + 1], prm);
+            if (need) guess[(size_t)p * nn + c] = make_float2(ys[2 * lane], ys[2 * lane + 1]);
             __syncwarp();
         }
     }
@@ -824,8 +828,8 @@ __global__ void __launch_bounds__(128) k_mlp_samples(long long n, unsigned long 
     visc_res o;
     visc_local(ph, m.mu[ph], T, P, m.gs_ref[ph], 0.0, 0.0, Eii, -Eii, 0.0, Eii, -Eii, 0.0, 0.0, 0.0, 0.0, m, q,
                m.psi[ph], m.phi[ph], m.C[ph], P, m.bet[ph], o);
-    float2 lab = mlp_labels(o.eta_ve, o.gdot, Eii, q);
-    lab.x = fminf(fmaxf(lab.x, -4.f), 8.f);
+    float2 lab = mlp_labels(o.eta_ve, o.eta_up, o.gdot, Eii);
+    lab.x = fminf(fmaxf(lab.x, -8.f), 1.f);
     lab.y = fminf(fmaxf(lab.y, 0.f), 1.f);
     float x[8];
     mlp_inputs(nm, q, Eii, T, P, dt, ph, x);
