@@ -99,13 +99,16 @@ LO_LITHO, HI_LITHO = [-18.0, 273.0, 0.0, 9.0], [-12.0, 1800.0, 15e9, 12.0]
 LO_MLP, HI_MLP = [-18.0, 273.0, 0.0, 9.0], [-12.0, 1600.0, 5e9, 12.0]
 
 
-def train_guess(ctx, cfg, n=1 << 20, steps=3000, batch=65536, seed=1):
+GUESS_STEPS = [3000]
+
+
+def train_guess(ctx, cfg, n=1 << 20, batch=65536, seed=1):
     """Tuples labelled by the plain local solve of the model's materials, then
     Adam on the device; returns (seconds, final loss)."""
     t0 = time.perf_counter()
     ctx.mlp_init(seed)
     ctx.mlp_generate(cfg["mat"], cfg["model"].rheo, n, seed, LO_LITHO, HI_LITHO)
-    loss = ctx.mlp_train(steps, batch, 2e-3)
+    loss = ctx.mlp_train(GUESS_STEPS[0], batch, 2e-3)
     return time.perf_counter() - t0, loss
 
 
@@ -234,6 +237,9 @@ def main():
     ap.add_argument("--size", default=None, help="NXxNZ override (tests only)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mlp", action="store_true")
+    ap.add_argument("--forms", default="both", choices=["both", "fast"],
+                    help="fast: run only the learned FP32-refined form and print nothing (profiling)")
+    ap.add_argument("--guess-steps", type=int, default=3000, help="Adam steps of the learned guess")
     args = ap.parse_args()
     rank, world, local = _dist()
     size = tuple(int(s) for s in args.size.split("x")) if args.size else None
@@ -264,6 +270,11 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     hbm, bf16, peak_kind = peaks()
+    if args.forms == "fast":   # profiling runs: the learned FP32-refined form alone, short guess training
+        GUESS_STEPS[0] = args.guess_steps
+        run_form(b, 32, 1, args.steps, args.warmup, size)
+        return 0
+    GUESS_STEPS[0] = args.guess_steps
     with ClockSampler(local) as clk:
         plain = run_form(b, 64, 0, args.steps, args.warmup, size)
         fast = run_form(b, 32, 1, args.steps, args.warmup, size)

@@ -111,6 +111,17 @@ struct visc_res {
 
 __device__ __forceinline__ double dmin(double a, double b) { return a <= b ? a : b; }
 
+// pow with the exponents the creep laws make trivial (0, 1, 2, -1: grain-size
+// and melt exponents switched off, linear diffusion creep, squares) taken
+// exactly; each costs a full FP64 log/exp pair otherwise.
+__device__ __forceinline__ double fpow(double x, double y) {
+    if (y == 0.0) return 1.0;
+    if (y == 1.0) return x;
+    if (y == 2.0) return x * x;
+    if (y == -1.0) return 1.0 / x;
+    return pow(x, y);
+}
+
 __device__ void visc_local(int p, double G, double T, double P, double d, double phi, double X0, double Exx,
                            double Ezz, double Exz, double Gxx, double Gzz, double Gxz, double Txx0, double Tzz0,
                            double Txz0, const mdz_materials &m, const mdz_rheo_params &prm, double dil, double fric,
@@ -140,19 +151,19 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     if (elastic == 0) { G = 1e1; K = 1e1; dil = 0.0; }
     if (T < ZEROC / prm.scale_T) T = ZEROC / prm.scale_T;
     if (dislocation) {
-        double B_pwl = m.pref_pwl[p] * m.Fpwl[p] * pow(m.Apwl[p], -1.0 / n_pwl) *
-                       exp((m.Qpwl[p] + P * Va_pwl) / R / n_pwl / T) * pow(d, m.mpwl[p] / n_pwl) *
-                       pow(m.fpwl[p], -m.rpwl[p] / n_pwl) * exp(-m.apwl[p] * phi / n_pwl);
-        C_pwl = pow(2.0 * f_ani * B_pwl, -n_pwl);
+        double B_pwl = m.pref_pwl[p] * m.Fpwl[p] * fpow(m.Apwl[p], -1.0 / n_pwl) *
+                       exp((m.Qpwl[p] + P * Va_pwl) / R / n_pwl / T) * fpow(d, m.mpwl[p] / n_pwl) *
+                       fpow(m.fpwl[p], -m.rpwl[p] / n_pwl) * exp(-m.apwl[p] * phi / n_pwl);
+        C_pwl = fpow(2.0 * f_ani * B_pwl, -n_pwl);
         dCpwldP = -C_pwl * Va_pwl / R / T;
-        eta_pwl = B_pwl * pow(Eii, 1.0 / n_pwl - 1.0);
+        eta_pwl = B_pwl * fpow(Eii, 1.0 / n_pwl - 1.0);
     }
     if (diffusion) {
-        B_lin = m.Flin[p] * pow(m.Alin[p], -1.0 / n_lin) * exp((m.Qlin[p] + P * m.Vlin[p]) / R / n_lin / T) *
-                pow(m.flin[p], -m.rlin[p] / n_lin) * exp(-m.alin[p] * phi / n_lin);
-        C_lin = pow(2.0 * f_ani * B_lin, -n_lin);
+        B_lin = m.Flin[p] * fpow(m.Alin[p], -1.0 / n_lin) * exp((m.Qlin[p] + P * m.Vlin[p]) / R / n_lin / T) *
+                fpow(m.flin[p], -m.rlin[p] / n_lin) * exp(-m.alin[p] * phi / n_lin);
+        C_lin = fpow(2.0 * f_ani * B_lin, -n_lin);
         dClindP = -C_lin * m.Vlin[p] / R / T;
-        eta_lin = B_lin * pow(Eii, 1.0 / n_lin - 1.0) * pow(d, m_lin / n_lin);
+        eta_lin = B_lin * fpow(Eii, 1.0 / n_lin - 1.0) * fpow(d, m_lin / n_lin);
     }
     double cos_fric = cos(fric), sin_fric = sin(fric), sin_dil = sin(dil);
     double Tyield = C * cos_fric + P * sin_fric;
@@ -167,7 +178,7 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     if (diffusion) eta_up = dmin(eta_up, eta_lin);
     // local Newton on the visco-elastic viscosity
     double eta_ve = eta_up, Tii;
-    const double dm_lin = pow(o.d1, -m_lin);
+    const double dm_lin = fpow(o.d1, -m_lin);
     bool ve_done = false;
     o.eta_up = eta_up;
     o.learned = guess != nullptr;
@@ -185,8 +196,8 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
             Tii = 2.0 * f_ani * eta_ve * Eii;
             const double Eel = elastic ? Tii / (2.0 * eta_el) : 0.0;
             if (constant) Eii_cst = Tii / f_ani / 2.0 / eta_cst;
-            if (dislocation) Eii_pwl = C_pwl * pow(Tii, n_pwl);
-            if (diffusion) Eii_lin = C_lin * pow(Tii, n_lin) * dm_lin;
+            if (dislocation) Eii_pwl = C_pwl * fpow(Tii, n_pwl);
+            if (diffusion) Eii_lin = C_lin * fpow(Tii, n_lin) * dm_lin;
             double r = Eii - elastic * Tii / (2.0 * eta_el) - (Eii_pwl + Eii_lin + Eii_cst);
             res = fabs(r / Eii);
             if (res < tol / 100) { ve_done = true; break; }
@@ -209,8 +220,8 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     for (it = 0; !ve_done && it < nitmax; it++) {
         Tii = 2.0 * f_ani * eta_ve * Eii;
         if (constant) Eii_cst = Tii / f_ani / 2.0 / eta_cst;
-        if (dislocation) Eii_pwl = C_pwl * pow(Tii, n_pwl);
-        if (diffusion) Eii_lin = C_lin * pow(Tii, n_lin) * dm_lin;
+        if (dislocation) Eii_pwl = C_pwl * fpow(Tii, n_pwl);
+        if (diffusion) Eii_lin = C_lin * fpow(Tii, n_lin) * dm_lin;
         double r = Eii - elastic * Tii / (2.0 * eta_el) - (Eii_pwl + Eii_lin + Eii_cst);
         res = fabs(r / Eii);
         if (res < tol / 100) break;
@@ -229,25 +240,25 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     Tii = 2.0 * eta_ve * f_ani * Eii;
     double Txx = Gxx * Tii / f_ani / Eii, Tzz = Gzz * Tii / f_ani / Eii, Txz = Gxz * Tii / f_ani / Eii;
     double Exx_lin = 0, Ezz_lin = 0, Exz_lin = 0, Exx_cst = 0, Ezz_cst = 0, Exz_cst = 0;
-    if (dislocation) eta_pwl = pow(2.0 * C_pwl, -1.0) * pow(Tii, 1.0 - n_pwl);
+    if (dislocation) eta_pwl = fpow(2.0 * C_pwl, -1.0) * fpow(Tii, 1.0 - n_pwl);
     if (diffusion) {
-        eta_lin = B_lin * pow(Eii_lin, 1.0 / n_lin - 1.0) * pow(o.d1, m_lin / n_lin);
+        eta_lin = B_lin * fpow(Eii_lin, 1.0 / n_lin - 1.0) * fpow(o.d1, m_lin / n_lin);
         Exx_lin = Txx / 2.0 / eta_lin; Ezz_lin = Tzz / 2.0 / eta_lin; Exz_lin = Txz / 2.0 / eta_lin;
     }
     if (constant) { Exx_cst = Txx / 2.0 / eta_cst; Ezz_cst = Tzz / 2.0 / eta_cst; Exz_cst = Txz / 2.0 / eta_cst; }
     // visco-elastic tangent
     double deta = 0.0;
-    if (dislocation) deta += -C_pwl * pow(Tii, n_pwl - 3.0) * (n_pwl - 1.0);
-    if (diffusion) deta += -C_lin * pow(Tii, n_lin - 3.0) * (n_lin - 1.0) * dm_lin;
-    const double e2 = pow(eta_ve, 2.0);
+    if (dislocation) deta += -C_pwl * fpow(Tii, n_pwl - 3.0) * (n_pwl - 1.0);
+    if (diffusion) deta += -C_lin * fpow(Tii, n_lin - 3.0) * (n_lin - 1.0) * dm_lin;
+    const double e2 = fpow(eta_ve, 2.0);
     double dTxx = deta * (2.0 * Txx + Tzz) * e2, dTzz = deta * (2.0 * Tzz + Txx) * e2, dTxz = 2.0 * deta * Txz * e2;
     double den = 1.0 - 2.0 * (dTxx * Exx + dTzz * Ezz + dTxz * Exz);
     double dve_dExx = dTxx * 2.0 * eta_ve / den, dve_dEzz = dTzz * 2.0 * eta_ve / den;
     double dve_dExz = dTxz * 2.0 * eta_ve / den;
     double dummy = 0.0, Jii = Tii * Tii;
-    if (dislocation) dummy += -2.0 * pow(Jii, (1.0 / 2.0) * n_pwl - 1.0 / 2.0) * dCpwldP;
-    if (diffusion) dummy += -2.0 * pow(Jii, (1.0 / 2.0) * n_lin - 1.0 / 2.0) * pow(d, -m_lin) * dClindP;
-    double dve_dP = pow(eta_ve, 2) * dummy;
+    if (dislocation) dummy += -2.0 * fpow(Jii, (1.0 / 2.0) * n_pwl - 1.0 / 2.0) * dCpwldP;
+    if (diffusion) dummy += -2.0 * fpow(Jii, (1.0 / 2.0) * n_lin - 1.0 / 2.0) * fpow(d, -m_lin) * dClindP;
+    double dve_dP = fpow(eta_ve, 2) * dummy;
     // plastic return mapping on gdot
     double gdot = 0.0, dQdtxx = 0, dQdtzz = 0, dQdtxz = 0, dQdP = 0, divp = 0.0, Pc = P;
     double dlamdExx = 0, dlamdEzz = 0, dlamdExz = 0, dlamdP = 0;
@@ -255,7 +266,7 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     double F_trial = Tii - Tyield;
     const bool is_pl = F_trial > 1e-17;
     if (is_pl) {
-        eta_vp = eta_vp0 * pow(Eii, 1.0 / n_vp - 1);
+        eta_vp = eta_vp0 * fpow(Eii, 1.0 / n_vp - 1);
         gdot = F_trial / (eta_ve + eta_vp + K * dt * sin_fric * sin_dil);
         dQdtxx = Txx / 2.0 / Tii; dQdtzz = Tzz / 2.0 / Tii; dQdtxz = Txz / 1.0 / Tii;
         const double F_trial0 = F_trial;
@@ -271,7 +282,7 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
                 dQdP = -sin_dil;
                 divp = -gdot * dQdP;
                 Pc = P + K * dt * divp;
-                eta_vp = eta_vp0 * pow(fabs(gdot), 1.0 / n_vp - 1.0);
+                eta_vp = eta_vp0 * fpow(fabs(gdot), 1.0 / n_vp - 1.0);
                 Tyield = C * cos_fric + Pc * sin_fric + gdot * eta_vp;
                 F_trial = Tii - eta_ve * gdot - Tyield;
                 res = fabs(F_trial);
@@ -290,7 +301,7 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
             dQdP = -sin_dil;
             divp = -gdot * dQdP;
             Pc = P + K * dt * divp;
-            eta_vp = eta_vp0 * pow(fabs(gdot), 1.0 / n_vp - 1.0);
+            eta_vp = eta_vp0 * fpow(fabs(gdot), 1.0 / n_vp - 1.0);
             Tyield = C * cos_fric + Pc * sin_fric + gdot * eta_vp;
             F_trial = Tii - eta_ve * gdot - Tyield;
             res = fabs(F_trial);
@@ -306,7 +317,7 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
         Tzz = 2.0 * eta_ve * (Ezz - gdot * dQdtzz);
         double Tyy = -(Txx + Tzz);
         Txz = 2.0 * eta_ve * (Exz - gdot * dQdtxz / 2.0);
-        Tii = sqrt(0.5 * (pow(Txx, 2.0) + pow(Tzz, 2.0) + pow(Tyy, 2.0)) + pow(Txz, 2.0));
+        Tii = sqrt(0.5 * (fpow(Txx, 2.0) + fpow(Tzz, 2.0) + fpow(Tyy, 2.0)) + fpow(Txz, 2.0));
         eta_vep = Tii / (2.0 * Eii);
         o.Eii_pl = gdot / 2.0;
         Tii = 2.0 * eta_vep * Eii;
@@ -325,7 +336,7 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
         double q = 1.0 / n_vp - 1.0;
         double dvp_dExx = eta_vp / gdot * dlamdExx * q, dvp_dEzz = eta_vp / gdot * dlamdEzz * q;
         double dvp_dExz = eta_vp / gdot * dlamdExz * q, dvp_dP = eta_vp / gdot * dlamdP * q;
-        double a = eta_vp + K * dt * sin_fric * sin_dil, E3 = 2.0 * pow(Eii, 3.0);
+        double a = eta_vp + K * dt * sin_fric * sin_dil, E3 = 2.0 * fpow(Eii, 3.0);
         dvep_dExx = -0.5 * (2.0 * Exx + Ezz) * Tyield / E3 + (a * dlamdExx + gdot * dvp_dExx + gdot * K * dt * sin_fric * 0.0) / (2.0 * Eii);
         dvep_dEzz = -0.5 * (2.0 * Ezz + Exx) * Tyield / E3 + (a * dlamdEzz + gdot * dvp_dEzz + gdot * K * dt * sin_fric * 0.0) / (2.0 * Eii);
         dvep_dExz = -Exz * Tyield / E3 + (a * dlamdExz + gdot * dvp_dExz + gdot * K * dt * sin_fric * 0.0) / (2.0 * Eii);
@@ -351,7 +362,7 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     }
     // eta_pwl is re-evaluated unconditionally in the reference (C_pwl = 0 when
     // dislocation creep is off, which makes the dislocation parts vanish)
-    eta_pwl = pow(2.0 * C_pwl, -1.0) * pow(Tii, 1.0 - n_pwl);
+    eta_pwl = fpow(2.0 * C_pwl, -1.0) * fpow(Tii, 1.0 - n_pwl);
     o.Exx_el = (double)elastic * (Txx - Txx0) / 2.0 / eta_el;
     o.Ezz_el = (double)elastic * (Tzz - Tzz0) / 2.0 / eta_el;
     o.Exz_el = (double)elastic * (Txz - Txz0) / 2.0 / eta_el;

@@ -1402,12 +1402,6 @@ static mdz_status remove_pressure_mean(mdz_ctx *ctx, double *p, cudaStream_t st)
     return MDZ_OK;
 }
 
-// dx(FP64) += sign * e(FP32)
-__global__ void k_add_f32(size_t n, const float *__restrict__ e, double *__restrict__ x, double sign) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) x[i] += sign * (double)e[i];
-}
-
 template <typename T>
 static mdz_status dots_launch(mdz_ctx *ctx, gcr_space<T> &S, int q0, int nq, const T *b, double *out,
                               cudaStream_t st) {
@@ -1465,12 +1459,26 @@ static mdz_status precond_graph(mdz_ctx *ctx, gcr_space<T> &S, mg_hier<T> &H, co
     return MDZ_OK;
 }
 
+// z, w (precision T) <- z, w (precision P)
+template <typename P, typename T>
+__global__ void k_widen2(size_t n, const P *__restrict__ a, const P *__restrict__ b, T *__restrict__ A,
+                         T *__restrict__ B) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) { A[i] = (T)a[i]; B[i] = (T)b[i]; }
+}
+
 // ---------------------------------------------------------------------------
-// GCR on K x = b (x0 = 0), right-preconditioned; T-precision operator.
-template <typename T>
-static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, mg_hier<T> &H, const stokes_coefs<T> &K, bool newton,
-                            const double *eta_n, double rtol, int maxit, int *its_out, double *rel_out,
-                            cudaStream_t st) {
+// GCR on K x = b (x0 = 0), right-preconditioned.  Krylov vectors,
+// orthogonalisation and updates in precision T; the preconditioner (V-cycle)
+// and the operator apply in precision P.  P = T: one precision throughout
+// (SP is S).  T = double, P = float: FP64 Krylov space with FP32 stencils and
+// V-cycles (r narrowed to FP32 before the preconditioner, z and K z widened to
+// FP64 after the apply), so the cancellations of the Krylov sums happen in FP64.
+template <typename T, typename P>
+static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_hier<P> &H,
+                            const stokes_coefs<P> &K, bool newton, const double *eta_n, double rtol, int maxit,
+                            int *its_out, double *rel_out, cudaStream_t st) {
+    constexpr bool mixed = sizeof(T) != sizeof(P);
     mdz_solver *SV = ctx->solver;
     stokes_geom G = mdz_stokes_geom(ctx);
     const size_t n = S.n, nu = S.nu, nv = S.nv;
@@ -1481,7 +1489,7 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, mg_hier<T> &H, const 
     mdz_status s;
     cudaGraphExec_t pre = nullptr;
     long long pre_launches = 0;
-    if ((s = precond_graph<T>(ctx, S, H, eta_n, st, &pre, &pre_launches)) != MDZ_OK) return s;
+    if ((s = precond_graph<P>(ctx, SP, H, eta_n, st, &pre, &pre_launches)) != MDZ_OK) return s;
     // (r, r) via the pointer-table slot m+1 against r itself
     if ((s = dots_launch<T>(ctx, S, S.m + 1, 1, S.r, dots, st)) != MDZ_OK) return s;
     k_set_scalar<<<1, 32, 0, st>>>(sc + 3, dots);
@@ -1501,19 +1509,27 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, mg_hier<T> &H, const 
     for (it = 0; it < maxit; it++) {
         if (k == S.m) k = 0;   // restart: keep x and r, drop the basis
         cudaEvent_t ev;
+        if (mixed) {   // r (T) -> r (P) for the preconditioner
+            k_convert<T, P><<<nb, MDZ_THREADS, 0, st>>>(n, S.r, SP.r);
+            MDZ_LAUNCHED(ctx);
+        }
         mdz_prof_begin(ctx, MDZ_PROF_MG_SMOOTH, st, &ev);
         MDZ_CUDA(ctx, cudaGraphLaunch(pre, st));
         ctx->launches += pre_launches;
-        mdz_prof_end(ctx, MDZ_PROF_MG_SMOOTH, SV->pre_bytes[(sizeof(T) == 8 ? 0 : 2) + (H.newton ? 1 : 0)], st, ev);
+        mdz_prof_end(ctx, MDZ_PROF_MG_SMOOTH, SV->pre_bytes[(sizeof(P) == 8 ? 0 : 2) + (H.newton ? 1 : 0)], st, ev);
         mdz_prof_begin(ctx, MDZ_PROF_STOKES_APPLY, st, &ev);
-        stokes_apply_launch<T>(G, K, stokes_cvec<T>{S.z, S.z + nu, S.z + nu + nv},
-                               stokes_vec<T>{S.w, S.w + nu, S.w + nu + nv}, nullptr, newton, st);
+        stokes_apply_launch<P>(G, K, stokes_cvec<P>{SP.z, SP.z + nu, SP.z + nu + nv},
+                               stokes_vec<P>{SP.w, SP.w + nu, SP.w + nu + nv}, nullptr, newton, st);
         MDZ_LAUNCHED(ctx);
         {   // algorithmic bytes: input and output vectors, the D-tensor read once, tags
             size_t nc = S.np, ng = (size_t)G.Nx * G.Nz;
             double coef = newton ? (8.0 * nc + 4.0 * ng) : (2.0 * nc + ng);
-            double bytes = sizeof(T) * (2.0 * n + coef) + (double)(nu + nv + nc + ng);
+            double bytes = sizeof(P) * (2.0 * n + coef) + (double)(nu + nv + nc + ng);
             mdz_prof_end(ctx, MDZ_PROF_STOKES_APPLY, bytes, st, ev);
+        }
+        if (mixed) {   // z, K z (P) -> (T)
+            k_widen2<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, SP.z, SP.w, S.z, S.w);
+            MDZ_LAUNCHED(ctx);
         }
         if (k > 0) {   // first Gram-Schmidt pass
             if ((s = dots_launch<T>(ctx, S, 0, k, S.w, dots, st)) != MDZ_OK) return s;
@@ -1570,7 +1586,8 @@ mdz_status mdz_dev_solve(mdz_ctx *ctx, const mdz_fields &f, bool newton, int pre
         if ((s = mg_setup<double>(ctx, SV->mg64, f.eta_n, f.eta_s, K64, newton && SV->mg_jacobian, st)) != MDZ_OK)
             return s;
         MDZ_CUDA(ctx, cudaMemcpyAsync(S64.r, F, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-        if ((s = gcr_solve<double>(ctx, S64, SV->mg64, K64, newton, f.eta_n, rtol, maxit, &its, &rel, st)) != MDZ_OK)
+        if ((s = gcr_solve<double, double>(ctx, S64, S64, SV->mg64, K64, newton, f.eta_n, rtol, maxit, &its, &rel,
+                                           st)) != MDZ_OK)
             return s;
         MDZ_CUDA(ctx, cudaMemcpyAsync(dx, S64.x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
         total = its;
@@ -1609,7 +1626,7 @@ mdz_status mdz_dev_solve(mdz_ctx *ctx, const mdz_fields &f, bool newton, int pre
         // stresses, so the contraction per cycle degrades on stiff problems: the
         // loop runs while the defect still shrinks by 10 % and takes back a
         // cycle that made it grow.
-        for (cycles = 0; cycles < 40; cycles++) {
+        for (cycles = 0; cycles < 60; cycles++) {
             // norm of the FP64 defect
             if ((s = dots_launch<double>(ctx, S64, S64.m + 1, 1, S64.r, dn, st)) != MDZ_OK) return s;
             MDZ_CUDA(ctx, cudaMemcpyAsync(SV->sc + 8, dn, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1619,7 +1636,7 @@ mdz_status mdz_dev_solve(mdz_ctx *ctx, const mdz_fields &f, bool newton, int pre
             rel = r0 > 0 ? rn / r0 : 0.0;
             if (rel <= rtol || r0 == 0.0) break;
             if (cycles > 0 && rel > prev) {   // the last correction made it worse: undo it
-                k_add_f32<<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, S32.x, dx, -1.0);
+                k_axpby<double><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, -1.0, S64.x, 1.0, dx);
                 MDZ_LAUNCHED(ctx);
                 if ((s = defect()) != MDZ_OK) return s;
                 rel = prev;
@@ -1627,16 +1644,20 @@ mdz_status mdz_dev_solve(mdz_ctx *ctx, const mdz_fields &f, bool newton, int pre
             }
             if (rel > 0.9 * prev || total >= maxit) break;   // refinement stalled or budget spent
             prev = rel;
-            k_convert<double, float><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, S64.r, S32.r);
-            MDZ_LAUNCHED(ctx);
+            // Inner solve on the FP64 defect: FP64 Krylov space, FP32 stencils
+            // and V-cycles.  The recursive residual differs from b - K64 x by
+            // the FP32 rounding of the applies times the cancellation in the
+            // Krylov sums, so each inner solve asks for at most three digits
+            // and one basis length; the FP64 cycles carry the accuracy.
             double inner_rtol = rtol / rel;
-            if (inner_rtol < 1e-4) inner_rtol = 1e-4;
+            if (inner_rtol < 1e-3) inner_rtol = 1e-3;
             if (inner_rtol > 0.1) inner_rtol = 0.1;
-            if ((s = gcr_solve<float>(ctx, S32, SV->mg32, K32, newton, f.eta_n, inner_rtol, maxit - total, &its,
-                                      nullptr, st)) != MDZ_OK)
+            const int inner_max = maxit - total < S64.m ? maxit - total : S64.m;
+            if ((s = gcr_solve<double, float>(ctx, S64, S32, SV->mg32, K32, newton, f.eta_n, inner_rtol, inner_max,
+                                              &its, nullptr, st)) != MDZ_OK)
                 return s;
             total += its;
-            k_add_f32<<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, S32.x, dx, 1.0);
+            k_axpby<double><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, 1.0, S64.x, 1.0, dx);
             MDZ_LAUNCHED(ctx);
             if ((s = defect()) != MDZ_OK) return s;
         }
