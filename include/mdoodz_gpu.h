@@ -297,6 +297,25 @@ mdz_status mdz_EvaluateRHS(mdz_ctx *ctx, const mdz_rheo_params *prm, double gx, 
  * reference exit(122)s. */
 mdz_status mdz_EvaluateStokesResidualDecoupled(mdz_ctx *ctx, mdz_fields *f, double *norms3);
 
+/* The norms3 of EvaluateStokesResidualDecoupled from residual rows the caller
+ * already holds on the device, without allocating anything and without a
+ * context (no counterpart in the reference, which reduces on the host).
+ * Device pointers in grid layout: ru (Nx*(Nz+1)), rv ((Nx+1)*Nz),
+ * rp ((Nx-1)*(Nz-1)) and their tag arrays; norms3 is a device array of 3
+ * doubles written on `stream` (a cudaStream_t; NULL = legacy default stream).
+ * Scratch: a static device array of 8192 * 6 doubles (384 KiB), one slot per
+ * index-box row; grids with Nz + 1 > 8192 rows are rejected with
+ * MDZ_ERR_CAPACITY.  No scratch value has to start at zero (every slot a call
+ * reads is written by that call first) and the result is bitwise
+ * reproducible.  The first call on a device looks the scratch address up
+ * (cudaGetSymbolAddress, with that device current): make it once before any
+ * stream capture.  The scratch is shared, so calls that overlap in time
+ * (several streams or host threads on one device) race and must be
+ * serialised.  Status only (no context for a message): MDZ_ERR_ARG for a
+ * null pointer or Nx, Nz < 3, MDZ_ERR_CUDA for a launch error. */
+mdz_status mdz_dev_residual_norms_noalloc(int Nx, int Nz, const double *ru, const double *rv, const double *rp,
+                                          const signed char *BCu, const signed char *BCv, const signed char *BCp,
+                                          double *norms3, void *stream);
 
 /* Matrix-free linear operator, the product of the reference's assembled
  * blocks with a correction vector (x zero on non-equation nodes):
