@@ -94,6 +94,15 @@ mdz_status mdz_set_markers(mdz_ctx *ctx, int n, const double *x, const double *z
 /* Download resident marker positions / phases (any pointer may be NULL). */
 mdz_status mdz_get_markers(mdz_ctx *ctx, int n, double *x, double *z, int *phase, double *vx, double *vz);
 
+/* Page-lock (register) an existing host array, e.g. the reference's marker
+ * arrays from PartAlloc (SOURCE/MemoryAllocFree.c:333), so that the marker
+ * and field transfers above run as DMA copies instead of staged pageable
+ * copies; mdz_host_unregister undoes it before the caller frees the array.
+ * No counterpart in the reference (it keeps everything in host memory).
+ * MDZ_ERR_ARG for a null pointer or zero size, MDZ_ERR_CUDA if CUDA refuses. */
+mdz_status mdz_host_register(void *p, size_t bytes);
+mdz_status mdz_host_unregister(void *p);
+
 /* ---- marker -> grid projection ----------------------------------------- */
 
 /* Drop-in for P2Mastah (SOURCE/ParticleRoutines.c:3226-3537) on the markers
@@ -436,7 +445,9 @@ mdz_status mdz_sync(mdz_ctx *ctx);
  * stream (off by default; turning it on or off resets the totals).  Classes:
  * 0 local rheology, 1 Stokes operator apply inside the Krylov solver,
  * 2 multigrid V-cycle (the whole preconditioner application), 3 projection,
- * 4 learned-guess inference.  Returns the summed time (ms), the summed
+ * 4 learned-guess inference, 5 Krylov vector work of the GCR iterations
+ * (orthogonalisation, dot products, updates), 6 multigrid set-up (level-0
+ * stencils, Galerkin products, coarsest inverse).  Returns the summed time (ms), the summed
  * algorithmic bytes and the number of launches of one class. */
 mdz_status mdz_set_profiling(mdz_ctx *ctx, int on);
 mdz_status mdz_kernel_timing(mdz_ctx *ctx, int kernel_class, double *ms, double *bytes, long long *launches);

@@ -167,6 +167,16 @@ extern "C" mdz_status mdz_get_markers(mdz_ctx *ctx, int n, double *x, double *z,
     return MDZ_OK;
 }
 
+extern "C" mdz_status mdz_host_register(void *p, size_t bytes) {
+    if (!p || bytes == 0) return MDZ_ERR_ARG;
+    return cudaHostRegister(p, bytes, cudaHostRegisterDefault) == cudaSuccess ? MDZ_OK : MDZ_ERR_CUDA;
+}
+
+extern "C" mdz_status mdz_host_unregister(void *p) {
+    if (!p) return MDZ_ERR_ARG;
+    return cudaHostUnregister(p) == cudaSuccess ? MDZ_OK : MDZ_ERR_CUDA;
+}
+
 extern "C" mdz_status mdz_set_marker_attr(mdz_ctx *ctx, int attr, int n, const double *values) {
     if (!ctx) return MDZ_ERR_ARG;
     if (attr < 0 || attr >= MDZ_M_NATTR || n < 0 || n > ctx->m.n || (n > 0 && !values))

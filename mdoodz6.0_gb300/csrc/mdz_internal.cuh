@@ -8,7 +8,7 @@
 
 // kernel classes timed when profiling is on
 enum { MDZ_PROF_VISCOSITY = 0, MDZ_PROF_STOKES_APPLY = 1, MDZ_PROF_MG_SMOOTH = 2, MDZ_PROF_P2G = 3, MDZ_PROF_MLP = 4,
-       MDZ_PROF_NCLS = 5 };
+       MDZ_PROF_KRYLOV = 5, MDZ_PROF_MG_SETUP = 6, MDZ_PROF_NCLS = 7 };
 struct mdz_ctx;
 void mdz_prof_begin(mdz_ctx *ctx, int cls, cudaStream_t st, cudaEvent_t *ev);
 void mdz_prof_end(mdz_ctx *ctx, int cls, double bytes, cudaStream_t st, cudaEvent_t a);

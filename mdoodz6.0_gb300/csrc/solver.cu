@@ -4,10 +4,12 @@
 // (warp-shuffle block reductions), and an upper block-triangular
 // preconditioner [[A, B], [0, S]]:
 //   S^-1 = eta_n / cell volume            (viscosity-scaled pressure mass)
-//   A^-1 = one geometric-multigrid V-cycle on the Picard velocity block
-//          (damped Jacobi smoothing, cell-doubling coarsening, bilinear
-//          prolongation with R = P^T, re-discretised coarse operators, and a
-//          single-CTA Jacobi-PCG solve on the coarsest level).
+//   A^-1 = one geometric-multigrid V-cycle on the velocity block (Picard,
+//          or optionally the Newton Jacobian's): damped Jacobi smoothing,
+//          cell-doubling coarsening, bilinear prolongation with R = P^T,
+//          Galerkin coarse operators R A P as 31-point stencils, and an
+//          explicit inverse (or a single-CTA Jacobi-PCG solve) on the
+//          coarsest level.
 // The same code runs in FP64 (plain form) and with FP32 storage and FP32
 // stencil / V-cycle arithmetic (T = float) inside an FP64 defect-correction
 // loop (iterative refinement); all inner products accumulate in FP64.
@@ -345,60 +347,36 @@ __global__ void k_mg_restrict(stokes_geom F, stokes_geom Cg, const T *__restrict
 // (u index (k, l) of the Nx x (Nz+1) box, v index (i, j) of the (Nx+1) x Nz box).
 // The level-0 stencil is a subset of this footprint.
 
-// parents of fine u node (i, j) on the coarse level: 4 (index, weight) pairs
-__device__ __forceinline__ void u_parents(int i, int j, int Nxc, int nczc, int *idx, float *w) {
-    int J0, J1;
-    float w0, w1;
-    cc_weights(j, nczc, J0, w0, J1, w1);
-    int Ia = i >> 1, Ib = (i + 1) >> 1;
-    float wa = (i & 1) ? 0.5f : 1.0f, wb = (i & 1) ? 0.5f : 0.0f;
-    idx[0] = Ia + J0 * Nxc; w[0] = wa * w0;
-    idx[1] = Ia + J1 * Nxc; w[1] = wa * w1;
-    idx[2] = Ib + J0 * Nxc; w[2] = wb * w0;
-    idx[3] = Ib + J1 * Nxc; w[3] = wb * w1;
-}
-
-__device__ __forceinline__ void v_parents(int i, int j, int Nxc, int ncxc, int *idx, float *w) {
-    int I0, I1;
-    float w0, w1;
-    cc_weights(i, ncxc, I0, w0, I1, w1);
-    int Ja = j >> 1, Jb = (j + 1) >> 1;
-    float wa = (j & 1) ? 0.5f : 1.0f, wb = (j & 1) ? 0.5f : 0.0f;
-    const int W = Nxc + 1;
-    idx[0] = I0 + Ja * W; w[0] = wa * w0;
-    idx[1] = I1 + Ja * W; w[1] = wa * w1;
-    idx[2] = I0 + Jb * W; w[2] = wb * w0;
-    idx[3] = I1 + Jb * W; w[3] = wb * w1;
-}
-
-// y = A x for a stencil level, one u-row / v-row
+// y = A x for a stencil level, one u-row / v-row.  All 31 coefficients and
+// neighbour values are loaded before the first multiply (neighbour indices
+// clamped into the box, out-of-box terms masked to zero) so that the loads
+// overlap instead of waiting on each other behind the bounds tests.
 template <typename T>
 __device__ __forceinline__ T st_urow(int Nx, int Nz, const T *__restrict__ su, size_t nu, const T *__restrict__ xu,
                                      const T *__restrict__ xv, int k, int l) {
     const size_t c = (size_t)k + (size_t)l * Nx;
+    T cf[MG_NST], xn[MG_NST];
+#pragma unroll
+    for (int q = 0; q < 15; q++) {   // uu: (dk, dl) = (q % 3 - 1, q / 3 - 2)
+        const int kk = k + q % 3 - 1, ll = l + q / 3 - 2;
+        const bool in = kk >= 0 && kk < Nx && ll >= 0 && ll <= Nz;
+        const int kc = min(max(kk, 0), Nx - 1), lc = min(max(ll, 0), Nz);
+        cf[q] = su[(size_t)q * nu + c];
+        xn[q] = xu[kc + lc * Nx];
+        if (!in) cf[q] = T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < 16; q++) {   // uv: (dI, dJ) = (q % 4 - 1, q / 4 - 2)
+        const int i = k + q % 4 - 1, j = l + q / 4 - 2;
+        const bool in = i >= 0 && i <= Nx && j >= 0 && j < Nz;
+        const int ic = min(max(i, 0), Nx), jc = min(max(j, 0), Nz - 1);
+        cf[15 + q] = su[(size_t)(15 + q) * nu + c];
+        xn[15 + q] = xv[ic + jc * (Nx + 1)];
+        if (!in) cf[15 + q] = T(0);
+    }
     T s = 0;
 #pragma unroll
-    for (int dl = -2; dl <= 2; dl++) {
-        const int ll = l + dl;
-        if (ll < 0 || ll > Nz) continue;
-#pragma unroll
-        for (int dk = -1; dk <= 1; dk++) {
-            const int kk = k + dk;
-            if (kk < 0 || kk >= Nx) continue;
-            s += su[(size_t)((dk + 1) + 3 * (dl + 2)) * nu + c] * xu[kk + ll * Nx];
-        }
-    }
-#pragma unroll
-    for (int dJ = -2; dJ <= 1; dJ++) {
-        const int j = l + dJ;
-        if (j < 0 || j >= Nz) continue;
-#pragma unroll
-        for (int dI = -1; dI <= 2; dI++) {
-            const int i = k + dI;
-            if (i < 0 || i > Nx) continue;
-            s += su[(size_t)(15 + (dI + 1) + 4 * (dJ + 2)) * nu + c] * xv[i + j * (Nx + 1)];
-        }
-    }
+    for (int q = 0; q < MG_NST; q++) s += cf[q] * xn[q];
     return s;
 }
 
@@ -406,29 +384,28 @@ template <typename T>
 __device__ __forceinline__ T st_vrow(int Nx, int Nz, const T *__restrict__ sv, size_t nv, const T *__restrict__ xu,
                                      const T *__restrict__ xv, int i, int j) {
     const size_t c = (size_t)i + (size_t)j * (Nx + 1);
+    T cf[MG_NST], xn[MG_NST];
+#pragma unroll
+    for (int q = 0; q < 15; q++) {   // vv: (dI, dJ) = (q % 5 - 2, q / 5 - 1)
+        const int ii = i + q % 5 - 2, jj = j + q / 5 - 1;
+        const bool in = ii >= 0 && ii <= Nx && jj >= 0 && jj < Nz;
+        const int ic = min(max(ii, 0), Nx), jc = min(max(jj, 0), Nz - 1);
+        cf[q] = sv[(size_t)q * nv + c];
+        xn[q] = xv[ic + jc * (Nx + 1)];
+        if (!in) cf[q] = T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < 16; q++) {   // vu: (dK, dL) = (q % 4 - 2, q / 4 - 1)
+        const int k = i + q % 4 - 2, l = j + q / 4 - 1;
+        const bool in = k >= 0 && k < Nx && l >= 0 && l <= Nz;
+        const int kc = min(max(k, 0), Nx - 1), lc = min(max(l, 0), Nz);
+        cf[15 + q] = sv[(size_t)(15 + q) * nv + c];
+        xn[15 + q] = xu[kc + lc * Nx];
+        if (!in) cf[15 + q] = T(0);
+    }
     T s = 0;
 #pragma unroll
-    for (int dJ = -1; dJ <= 1; dJ++) {
-        const int jj = j + dJ;
-        if (jj < 0 || jj >= Nz) continue;
-#pragma unroll
-        for (int dI = -2; dI <= 2; dI++) {
-            const int ii = i + dI;
-            if (ii < 0 || ii > Nx) continue;
-            s += sv[(size_t)((dI + 2) + 5 * (dJ + 1)) * nv + c] * xv[ii + jj * (Nx + 1)];
-        }
-    }
-#pragma unroll
-    for (int dL = -1; dL <= 2; dL++) {
-        const int l = j + dL;
-        if (l < 0 || l > Nz) continue;
-#pragma unroll
-        for (int dK = -2; dK <= 1; dK++) {
-            const int k = i + dK;
-            if (k < 0 || k >= Nx) continue;
-            s += sv[(size_t)(15 + (dK + 2) + 4 * (dL + 1)) * nv + c] * xu[k + l * Nx];
-        }
-    }
+    for (int q = 0; q < MG_NST; q++) s += cf[q] * xn[q];
     return s;
 }
 
@@ -571,23 +548,150 @@ __global__ void k_probe_collect(stokes_geom G, int comp, int cx, int cz, const T
     }
 }
 
-// Coarse stencils = R A P, one thread per coarse row; FP64 accumulation.
-// An entry landing outside the footprint (impossible with this P) sets *bad.
+// Level-0 stencils of the Picard velocity block written out directly from
+// the viscosities (the composition strain rate -> D11 / D33 stress ->
+// divergence of xrow / zrow with the same row flags, times the cell volume),
+// one thread per (i, j); every plane of every row is written, zeros outside
+// the unknowns.  Equal to probing the Picard operator, in one pass.
+//   u-row (k, l), aE = inE D11[E], aW = inW D11[W], bN = inN D33[N], bS = inS D33[S]:
+//     u(k+-1, l): -2/3 aE|aW / dx^2   u(k, l+-1): -bN|bS / dz^2   u(k, l): the sum of their negatives
+//     v(k+1, l): aE/3 - bN   v(k+1, l-1): bS - aE/3   v(k, l): bN - aW/3   v(k, l-1): aW/3 - bS   (/ dx dz)
+//   v-row (i, j), cN = inN D22[N], cS = inS D22[S], dE = inE D33[E], dW = inW D33[W]:
+//     v(i, j+-1): -2/3 cN|cS / dz^2   v(i+-1, j): -dE|dW / dx^2   v(i, j): the sum of their negatives
+//     u(i, j+1): cN/3 - dE   u(i-1, j+1): dW - cN/3   u(i, j): dE - cS/3   u(i-1, j): cS/3 - dW   (/ dx dz)
 template <typename T>
-__global__ void __launch_bounds__(128) k_galerkin(stokes_geom F, const T *__restrict__ suF,
-                                                  const T *__restrict__ svF, stokes_geom Cg, T *__restrict__ suC,
-                                                  T *__restrict__ svC, int *bad) {
+__global__ void __launch_bounds__(256) k_picard_stencil(stokes_geom G, const T *__restrict__ D11,
+                                                        const T *__restrict__ D33, T *__restrict__ su,
+                                                        T *__restrict__ sv) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int Nx = G.Nx, Nz = G.Nz, nx = Nx, ncx = G.ncx, nxvz = Nx + 1;
+    const size_t nu = (size_t)Nx * (Nz + 1), nv = (size_t)(Nx + 1) * Nz;
+    const double celvol = G.dx * G.dz, ixx = G.idx * G.idx, izz = G.idz * G.idz, ixz = G.idx * G.idz;
+    if (i < Nx && j <= Nz) {   // u-row (k, l) = (i, j)
+        const int k = i, l = j, c1 = k + l * nx;
+        double a[MG_NST];
+#pragma unroll
+        for (int q = 0; q < MG_NST; q++) a[q] = 0.0;
+        if (G.BCu[c1] == -1) {
+            const int c2 = k - 1 + (l - 1) * ncx, iPrW = c2, iPrE = c2 + 1, ixyN = c1, ixyS = c1 - nx;
+            const double inW = G.BCp[iPrW] == -1 ? 1.0 : 0.0, inE = G.BCp[iPrE] == -1 ? 1.0 : 0.0;
+            const double inS = (G.BCg[ixyS] != 30 && G.BCu[c1 - nx] != 13) ? 1.0 : 0.0;
+            const double inN = (G.BCg[ixyN] != 30 && G.BCu[c1 + nx] != 13) ? 1.0 : 0.0;
+            const double aE = inE * (double)D11[iPrE], aW = inW * (double)D11[iPrW];
+            const double bN = inN * (double)D33[ixyN], bS = inS * (double)D33[ixyS];
+            const double uE = -(2.0 / 3.0) * aE * ixx, uW = -(2.0 / 3.0) * aW * ixx;
+            const double uN = -bN * izz, uS = -bS * izz;
+            auto isu = [&](int kk, int ll) { return G.BCu[kk + ll * nx] == -1 ? 1.0 : 0.0; };
+            auto isv = [&](int ii, int jj) { return G.BCv[ii + jj * nxvz] == -1 ? 1.0 : 0.0; };
+            a[(0 + 1) + 3 * (0 + 2)] = -(uE + uW + uN + uS);
+            a[(1 + 1) + 3 * (0 + 2)] = uE * isu(k + 1, l);
+            a[(-1 + 1) + 3 * (0 + 2)] = uW * isu(k - 1, l);
+            a[(0 + 1) + 3 * (1 + 2)] = uN * isu(k, l + 1);
+            a[(0 + 1) + 3 * (-1 + 2)] = uS * isu(k, l - 1);
+            a[15 + (1 + 1) + 4 * (0 + 2)] = (aE / 3.0 - bN) * ixz * isv(k + 1, l);
+            a[15 + (1 + 1) + 4 * (-1 + 2)] = (bS - aE / 3.0) * ixz * isv(k + 1, l - 1);
+            a[15 + (0 + 1) + 4 * (0 + 2)] = (bN - aW / 3.0) * ixz * isv(k, l);
+            a[15 + (0 + 1) + 4 * (-1 + 2)] = (aW / 3.0 - bS) * ixz * isv(k, l - 1);
+        }
+#pragma unroll
+        for (int q = 0; q < MG_NST; q++) su[(size_t)q * nu + c1] = (T)(a[q] * celvol);
+    }
+    if (i <= Nx && j < Nz) {   // v-row (k, l) = (i, j)
+        const int k = i, l = j, c3 = k + l * nxvz;
+        double a[MG_NST];
+#pragma unroll
+        for (int q = 0; q < MG_NST; q++) a[q] = 0.0;
+        if (G.BCv[c3] == -1) {
+            const int c1 = k + l * nx, c2 = k - 1 + (l - 1) * ncx;
+            const int iPrS = c2, iPrN = c2 + ncx, ixyW = c1 - 1, ixyE = c1;
+            double inS = 0.0, inN = 0.0;
+            const bool s30 = G.BCv[c3 - nxvz] == 30, n30 = G.BCv[c3 + nxvz] == 30;
+            if (!s30 && !n30) { inS = 1.0; inN = 1.0; }
+            if (s30 && !n30) inN = 1.0;
+            if (!s30 && n30) inS = 1.0;
+            if (G.BCp[iPrS] == -1) inS = 1.0;
+            if (G.BCp[iPrN] == -1) inN = 1.0;
+            const double inW = (G.BCg[ixyW] != 30 && G.BCv[c3 - 1] != 13) ? 1.0 : 0.0;
+            const double inE = (G.BCg[ixyE] != 30 && G.BCv[c3 + 1] != 13) ? 1.0 : 0.0;
+            const double cN = inN * (double)D11[iPrN], cS = inS * (double)D11[iPrS];
+            const double dE = inE * (double)D33[ixyE], dW = inW * (double)D33[ixyW];
+            const double vN = -(2.0 / 3.0) * cN * izz, vS = -(2.0 / 3.0) * cS * izz;
+            const double vE = -dE * ixx, vW = -dW * ixx;
+            auto isu = [&](int kk, int ll) { return G.BCu[kk + ll * nx] == -1 ? 1.0 : 0.0; };
+            auto isv = [&](int ii, int jj) { return G.BCv[ii + jj * nxvz] == -1 ? 1.0 : 0.0; };
+            a[(0 + 2) + 5 * (0 + 1)] = -(vN + vS + vE + vW);
+            a[(0 + 2) + 5 * (1 + 1)] = vN * isv(k, l + 1);
+            a[(0 + 2) + 5 * (-1 + 1)] = vS * isv(k, l - 1);
+            a[(1 + 2) + 5 * (0 + 1)] = vE * isv(k + 1, l);
+            a[(-1 + 2) + 5 * (0 + 1)] = vW * isv(k - 1, l);
+            a[15 + (0 + 2) + 4 * (1 + 1)] = (cN / 3.0 - dE) * ixz * isu(k, l + 1);
+            a[15 + (-1 + 2) + 4 * (1 + 1)] = (dW - cN / 3.0) * ixz * isu(k - 1, l + 1);
+            a[15 + (0 + 2) + 4 * (0 + 1)] = (dE - cS / 3.0) * ixz * isu(k, l);
+            a[15 + (-1 + 2) + 4 * (0 + 1)] = (cS / 3.0 - dW) * ixz * isu(k - 1, l);
+        }
+#pragma unroll
+        for (int q = 0; q < MG_NST; q++) sv[(size_t)q * nv + c3] = (T)(a[q] * celvol);
+    }
+}
+
+// Coarse stencils = R A P, one thread per coarse row, FP64 accumulation in
+// shared memory (plane-major, one column per thread).  Every level of the
+// hierarchy follows the tag rule of k_level_tags (the fine level is checked
+// before the hierarchy is built), so "is an unknown" is index arithmetic and
+// the kernel reads no tags.  Each fine row's 31 coefficients are loaded in
+// one batch before use: loaded one at a time behind the zero test they
+// serialise on memory latency.  An entry landing outside the footprint
+// (impossible with this P) sets *bad.
+__device__ __forceinline__ bool u_unknown(int k, int l, int Nx, int Nz) {
+    return k >= 1 && k <= Nx - 2 && l >= 1 && l <= Nz - 1;
+}
+__device__ __forceinline__ bool v_unknown(int i, int j, int Nx, int Nz) {
+    return i >= 1 && i <= Nx - 1 && j >= 1 && j <= Nz - 2;
+}
+
+// parents of fine u node (i, j) / v node (i, j) as coarse (I, J) pairs
+__device__ __forceinline__ void u_parents_ij(int i, int j, int nczc, int *I, int *J, float *w) {
+    int J0, J1;
+    float w0, w1;
+    cc_weights(j, nczc, J0, w0, J1, w1);
+    const int Ia = i >> 1, Ib = (i + 1) >> 1;
+    const float wa = (i & 1) ? 0.5f : 1.0f, wb = (i & 1) ? 0.5f : 0.0f;
+    I[0] = Ia; J[0] = J0; w[0] = wa * w0;
+    I[1] = Ia; J[1] = J1; w[1] = wa * w1;
+    I[2] = Ib; J[2] = J0; w[2] = wb * w0;
+    I[3] = Ib; J[3] = J1; w[3] = wb * w1;
+}
+__device__ __forceinline__ void v_parents_ij(int i, int j, int ncxc, int *I, int *J, float *w) {
+    int I0, I1;
+    float w0, w1;
+    cc_weights(i, ncxc, I0, w0, I1, w1);
+    const int Ja = j >> 1, Jb = (j + 1) >> 1;
+    const float wa = (j & 1) ? 0.5f : 1.0f, wb = (j & 1) ? 0.5f : 0.0f;
+    I[0] = I0; J[0] = Ja; w[0] = wa * w0;
+    I[1] = I1; J[1] = Ja; w[1] = wa * w1;
+    I[2] = I0; J[2] = Jb; w[2] = wb * w0;
+    I[3] = I1; J[3] = Jb; w[3] = wb * w1;
+}
+
+#define GAL_THREADS 128
+template <typename T>
+__global__ void __launch_bounds__(GAL_THREADS) k_galerkin(stokes_geom F, const T *__restrict__ suF,
+                                                          const T *__restrict__ svF, stokes_geom Cg,
+                                                          T *__restrict__ suC, T *__restrict__ svC, int *bad) {
+    __shared__ double acc_sh[MG_NST * GAL_THREADS];
+    double *acc = acc_sh + threadIdx.x;
+#define ACC(q) acc[(q) * GAL_THREADS]
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int Nxf = F.Nx, Nzf = F.Nz, Nxc = Cg.Nx, Nzc = Cg.Nz;
     const size_t nuf = (size_t)Nxf * (Nzf + 1), nvf = (size_t)(Nxf + 1) * Nzf;
-    const size_t nuc = (size_t)Nxc * (Nzc + 1), nvc = (size_t)(Nxc + 1) * Nzc;
-    double acc[MG_NST];
-    int pi[4];
+    const int nuc = Nxc * (Nzc + 1), nvc = (Nxc + 1) * Nzc;
+    int PI[4], PJ[4];
     float pw[4];
-    if (t < (long long)nuc) {   // coarse u-row (K, L)
+    T a[MG_NST];
+    if (t < nuc) {   // coarse u-row (K, L)
         const int K = t % Nxc, L = t / Nxc;
-        for (int q = 0; q < MG_NST; q++) acc[q] = 0.0;
-        if (Cg.BCu[t] == -1) {
+        for (int q = 0; q < MG_NST; q++) ACC(q) = 0.0;
+        if (u_unknown(K, L, Nxc, Nzc)) {
             for (int lf = 2 * L - 2; lf <= 2 * L + 1; lf++) {
                 if (lf < 1 || lf > F.ncz) continue;
                 int J0, J1;
@@ -596,45 +700,46 @@ __global__ void __launch_bounds__(128) k_galerkin(stokes_geom F, const T *__rest
                 const float wz = (J0 == L ? w0 : 0.0f) + (J1 == L && J1 != J0 ? w1 : 0.0f);
                 if (wz == 0.0f) continue;
                 for (int k = 2 * K - 1; k <= 2 * K + 1; k++) {
-                    if (k < 0 || k >= Nxf) continue;
-                    const float wx = nc_weight(k, K);
-                    if (wx == 0.0f) continue;
-                    const int f = k + lf * Nxf;
-                    if (F.BCu[f] != -1) continue;
-                    const double R = (double)wx * wz;
-                    for (int q = 0; q < 15; q++) {          // uu entries of the fine row
-                        const double a = (double)suF[(size_t)q * nuf + f];
-                        if (a == 0.0) continue;
-                        const int tk = k + q % 3 - 1, tl = lf + q / 3 - 2;
-                        u_parents(tk, tl, Nxc, Cg.ncz, pi, pw);
+                    if (!u_unknown(k, lf, Nxf, Nzf)) continue;
+                    const size_t f = (size_t)k + (size_t)lf * Nxf;
+                    const double R = (double)(nc_weight(k, K) * wz);
+#pragma unroll
+                    for (int q = 0; q < MG_NST; q++) a[q] = __ldg(suF + (size_t)q * nuf + f);
+#pragma unroll
+                    for (int q = 0; q < 15; q++) {   // uu entries of the fine row
+                        if (a[q] == T(0)) continue;
+                        u_parents_ij(k + q % 3 - 1, lf + q / 3 - 2, Cg.ncz, PI, PJ, pw);
+                        const double ra = R * (double)a[q];
+#pragma unroll
                         for (int s = 0; s < 4; s++) {
-                            if (pw[s] == 0.0f || Cg.BCu[pi[s]] != -1) continue;
-                            const int dK = pi[s] % Nxc - K, dL = pi[s] / Nxc - L;
+                            if (pw[s] == 0.0f || !u_unknown(PI[s], PJ[s], Nxc, Nzc)) continue;
+                            const int dK = PI[s] - K, dL = PJ[s] - L;
                             if (dK < -1 || dK > 1 || dL < -2 || dL > 2) { *bad = 1; continue; }
-                            acc[(dK + 1) + 3 * (dL + 2)] += R * a * pw[s];
+                            ACC((dK + 1) + 3 * (dL + 2)) += ra * pw[s];
                         }
                     }
-                    for (int q = 0; q < 16; q++) {          // uv entries of the fine row
-                        const double a = (double)suF[(size_t)(15 + q) * nuf + f];
-                        if (a == 0.0) continue;
-                        const int ti = k + q % 4 - 1, tj = lf + q / 4 - 2;
-                        v_parents(ti, tj, Nxc, Cg.ncx, pi, pw);
+#pragma unroll
+                    for (int q = 0; q < 16; q++) {   // uv entries of the fine row
+                        if (a[15 + q] == T(0)) continue;
+                        v_parents_ij(k + q % 4 - 1, lf + q / 4 - 2, Cg.ncx, PI, PJ, pw);
+                        const double ra = R * (double)a[15 + q];
+#pragma unroll
                         for (int s = 0; s < 4; s++) {
-                            if (pw[s] == 0.0f || Cg.BCv[pi[s]] != -1) continue;
-                            const int dI = pi[s] % (Nxc + 1) - K, dJ = pi[s] / (Nxc + 1) - L;
+                            if (pw[s] == 0.0f || !v_unknown(PI[s], PJ[s], Nxc, Nzc)) continue;
+                            const int dI = PI[s] - K, dJ = PJ[s] - L;
                             if (dI < -1 || dI > 2 || dJ < -2 || dJ > 1) { *bad = 1; continue; }
-                            acc[15 + (dI + 1) + 4 * (dJ + 2)] += R * a * pw[s];
+                            ACC(15 + (dI + 1) + 4 * (dJ + 2)) += ra * pw[s];
                         }
                     }
                 }
             }
         }
-        for (int q = 0; q < MG_NST; q++) suC[(size_t)q * nuc + t] = (T)acc[q];
+        for (int q = 0; q < MG_NST; q++) suC[(size_t)q * nuc + t] = (T)ACC(q);
     }
-    if (t < (long long)nvc) {   // coarse v-row (I, J)
+    if (t < nvc) {   // coarse v-row (I, J)
         const int I = t % (Nxc + 1), J = t / (Nxc + 1);
-        for (int q = 0; q < MG_NST; q++) acc[q] = 0.0;
-        if (Cg.BCv[t] == -1) {
+        for (int q = 0; q < MG_NST; q++) ACC(q) = 0.0;
+        if (v_unknown(I, J, Nxc, Nzc)) {
             for (int i = 2 * I - 2; i <= 2 * I + 1; i++) {
                 if (i < 1 || i > F.ncx) continue;
                 int I0, I1;
@@ -643,41 +748,43 @@ __global__ void __launch_bounds__(128) k_galerkin(stokes_geom F, const T *__rest
                 const float wx = (I0 == I ? w0 : 0.0f) + (I1 == I && I1 != I0 ? w1 : 0.0f);
                 if (wx == 0.0f) continue;
                 for (int j = 2 * J - 1; j <= 2 * J + 1; j++) {
-                    if (j < 0 || j >= Nzf) continue;
-                    const float wz = nc_weight(j, J);
-                    if (wz == 0.0f) continue;
-                    const int f = i + j * (Nxf + 1);
-                    if (F.BCv[f] != -1) continue;
-                    const double R = (double)wx * wz;
-                    for (int q = 0; q < 15; q++) {          // vv entries
-                        const double a = (double)svF[(size_t)q * nvf + f];
-                        if (a == 0.0) continue;
-                        const int ti = i + q % 5 - 2, tj = j + q / 5 - 1;
-                        v_parents(ti, tj, Nxc, Cg.ncx, pi, pw);
+                    if (!v_unknown(i, j, Nxf, Nzf)) continue;
+                    const size_t f = (size_t)i + (size_t)j * (Nxf + 1);
+                    const double R = (double)(wx * nc_weight(j, J));
+#pragma unroll
+                    for (int q = 0; q < MG_NST; q++) a[q] = __ldg(svF + (size_t)q * nvf + f);
+#pragma unroll
+                    for (int q = 0; q < 15; q++) {   // vv entries
+                        if (a[q] == T(0)) continue;
+                        v_parents_ij(i + q % 5 - 2, j + q / 5 - 1, Cg.ncx, PI, PJ, pw);
+                        const double ra = R * (double)a[q];
+#pragma unroll
                         for (int s = 0; s < 4; s++) {
-                            if (pw[s] == 0.0f || Cg.BCv[pi[s]] != -1) continue;
-                            const int dI = pi[s] % (Nxc + 1) - I, dJ = pi[s] / (Nxc + 1) - J;
+                            if (pw[s] == 0.0f || !v_unknown(PI[s], PJ[s], Nxc, Nzc)) continue;
+                            const int dI = PI[s] - I, dJ = PJ[s] - J;
                             if (dI < -2 || dI > 2 || dJ < -1 || dJ > 1) { *bad = 1; continue; }
-                            acc[(dI + 2) + 5 * (dJ + 1)] += R * a * pw[s];
+                            ACC((dI + 2) + 5 * (dJ + 1)) += ra * pw[s];
                         }
                     }
-                    for (int q = 0; q < 16; q++) {          // vu entries
-                        const double a = (double)svF[(size_t)(15 + q) * nvf + f];
-                        if (a == 0.0) continue;
-                        const int tk = i + q % 4 - 2, tl = j + q / 4 - 1;
-                        u_parents(tk, tl, Nxc, Cg.ncz, pi, pw);
+#pragma unroll
+                    for (int q = 0; q < 16; q++) {   // vu entries
+                        if (a[15 + q] == T(0)) continue;
+                        u_parents_ij(i + q % 4 - 2, j + q / 4 - 1, Cg.ncz, PI, PJ, pw);
+                        const double ra = R * (double)a[15 + q];
+#pragma unroll
                         for (int s = 0; s < 4; s++) {
-                            if (pw[s] == 0.0f || Cg.BCu[pi[s]] != -1) continue;
-                            const int dK = pi[s] % Nxc - I, dL = pi[s] / Nxc - J;
+                            if (pw[s] == 0.0f || !u_unknown(PI[s], PJ[s], Nxc, Nzc)) continue;
+                            const int dK = PI[s] - I, dL = PJ[s] - J;
                             if (dK < -2 || dK > 1 || dL < -1 || dL > 2) { *bad = 1; continue; }
-                            acc[15 + (dK + 2) + 4 * (dL + 1)] += R * a * pw[s];
+                            ACC(15 + (dK + 2) + 4 * (dL + 1)) += ra * pw[s];
                         }
                     }
                 }
             }
         }
-        for (int q = 0; q < MG_NST; q++) svC[(size_t)q * nvc + t] = (T)acc[q];
+        for (int q = 0; q < MG_NST; q++) svC[(size_t)q * nvc + t] = (T)ACC(q);
     }
+#undef ACC
 }
 
 template <typename T>
@@ -1124,11 +1231,17 @@ static mdz_status mg_setup(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n, con
     mg_level<T> &F = H.L[0];
     int nc = F.ncx * F.ncz, nv = F.Nx * F.Nz;
     H.newton = newton;
+    cudaEvent_t ev;
+    mdz_prof_begin(ctx, MDZ_PROF_MG_SETUP, st, &ev);
     k_fill_D11_D33<T><<<mdz_blocks(nv > nc ? nv : nc), MDZ_THREADS, 0, st>>>(nc, nv, eta_n, eta_s, F.D11, F.D33);
     MDZ_LAUNCHED(ctx);
-    // level-0 stencils by probing the fine velocity block (the Picard block from
-    // eta, or the Newton Jacobian's) with 2 x 16 colour classes
+    // level-0 stencils: the Picard block written out from eta, or the Newton
+    // Jacobian's velocity block probed with 2 x 16 colour classes
     const dim3 bl(32, 8), gr0((F.Nx + 1 + 31) / 32, (F.Nz + 1 + 7) / 8);
+    if (!newton) {
+        k_picard_stencil<T><<<gr0, bl, 0, st>>>(F.geom(), F.D11, F.D33, F.su, F.sv);
+        MDZ_LAUNCHED(ctx);
+    } else {
     MDZ_CUDA(ctx, cudaMemsetAsync(F.su, 0, sizeof(T) * MG_NST * F.nu(), st));
     MDZ_CUDA(ctx, cudaMemsetAsync(F.sv, 0, sizeof(T) * MG_NST * F.nv(), st));
     for (int comp = 0; comp < 2; comp++)
@@ -1142,6 +1255,7 @@ static mdz_status mg_setup(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n, con
                 k_probe_collect<T><<<gr0, bl, 0, st>>>(F.geom(), comp, cx, cz, F.ru, F.rv, F.su, F.sv);
                 MDZ_LAUNCHED(ctx);
             }
+    }
     {   // Jacobi diagonal of level 0: the viscosity formula (Picard) or the probed stencil (Newton)
         size_t n = F.nu() > F.nv() ? F.nu() : F.nv();
         if (newton) k_st_diag<T><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(F.geom(), F.su, F.sv, F.idu, F.idv);
@@ -1153,7 +1267,7 @@ static mdz_status mg_setup(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n, con
     for (int l = 1; l < H.nlev; l++) {
         mg_level<T> &P = H.L[l - 1], &L = H.L[l];
         size_t n = L.nu() > L.nv() ? L.nu() : L.nv();
-        k_galerkin<T><<<mdz_blocks(n, 128), 128, 0, st>>>(P.geom(), P.su, P.sv, L.geom(), L.su, L.sv, status + 1);
+        k_galerkin<T><<<mdz_blocks(n, GAL_THREADS), GAL_THREADS, 0, st>>>(P.geom(), P.su, P.sv, L.geom(), L.su, L.sv, status + 1);
         MDZ_LAUNCHED(ctx);
         k_st_diag<T><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(L.geom(), L.su, L.sv, L.idu, L.idv);
         MDZ_LAUNCHED(ctx);
@@ -1162,6 +1276,15 @@ static mdz_status mg_setup(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n, con
     if (C.ndense) {
         k_coarse_dense_setup<T><<<1, 512, 0, st>>>(C.geom(), C.su, C.sv, C.ndense, C.dmap, C.Awork, C.AinvT, status);
         MDZ_LAUNCHED(ctx);
+    }
+    {   // algorithmic bytes: viscosities in, D11 / D33 out; level-0 stencils
+        // written once; each Galerkin level reads the finer stencils once and
+        // writes its own plus the inverse diagonal
+        double b = 8.0 * (nc + nv) + sizeof(T) * (nc + nv) + sizeof(T) * MG_NST * (double)(F.nu() + F.nv());
+        for (int l = 1; l < H.nlev; l++)
+            b += sizeof(T) * (MG_NST * (double)(H.L[l - 1].nu() + H.L[l - 1].nv()) +
+                              (MG_NST + 1.0) * (double)(H.L[l].nu() + H.L[l].nv()));
+        mdz_prof_end(ctx, MDZ_PROF_MG_SETUP, b, st, ev);
     }
     MDZ_CUDA(ctx, cudaMemcpyAsync((int *)(ctx->solver->sc + 20), status, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
     return MDZ_OK;
@@ -1527,6 +1650,7 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
             double bytes = sizeof(P) * (2.0 * n + coef) + (double)(nu + nv + nc + ng);
             mdz_prof_end(ctx, MDZ_PROF_STOKES_APPLY, bytes, st, ev);
         }
+        mdz_prof_begin(ctx, MDZ_PROF_KRYLOV, st, &ev);
         if (mixed) {   // z, K z (P) -> (T)
             k_widen2<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, SP.z, SP.w, S.z, S.w);
             MDZ_LAUNCHED(ctx);
@@ -1543,6 +1667,14 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
         MDZ_LAUNCHED(ctx);
         k_gcr_finish<T><<<nb, MDZ_THREADS, 0, st>>>(n, k, S.Z, S.W, dots, sc, S.z, S.w, S.x, S.r);
         MDZ_LAUNCHED(ctx);
+        {   // algorithmic bytes: widening (2 P reads, 2 T writes); the two
+            // Gram-Schmidt passes read W_q and w (k + 1 each) plus (w, w),
+            // (w, r); the orthogonalisation reads Z_q, W_q, z, w and writes
+            // z, w; the finish reads Z_q, W_q, z, w, x, r, writes Z_k, W_k, x, r
+            double vecs = (k > 0 ? (k + 1.0) + (2.0 * k + 4.0) : 0.0) + (k + 3.0) + (2.0 * k + 8.0);
+            double bytes = sizeof(T) * (double)n * vecs + (mixed ? (2.0 * sizeof(P) + 2.0 * sizeof(T)) * n : 0.0);
+            mdz_prof_end(ctx, MDZ_PROF_KRYLOV, bytes, st, ev);
+        }
         k++;
         // the running norm lives on the device; the host looks every `check`
         // iterations, at each restart and at the iteration limit

@@ -54,8 +54,24 @@ def load_library(path=LIB_PATH):
     L.mdz_last_error.restype = C.c_char_p
     L.mdz_kernel_launches.restype = C.c_longlong
     L.mdz_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(GridDesc), C.c_int, C.c_longlong]
+    L.mdz_host_register.argtypes = [C.c_void_p, C.c_size_t]
+    L.mdz_host_unregister.argtypes = [C.c_void_p]
     _lib = L
     return L
+
+
+def host_register(a):
+    """Page-lock the memory of a contiguous numpy array (mdz_host_register) so
+    that uploads from it and downloads into it run as DMA copies."""
+    st = load_library().mdz_host_register(C.c_void_p(a.ctypes.data), C.c_size_t(a.nbytes))
+    if st:
+        raise MdzError(st, "mdz_host_register: %d bytes refused" % a.nbytes)
+
+
+def host_unregister(a):
+    st = load_library().mdz_host_unregister(C.c_void_p(a.ctypes.data))
+    if st:
+        raise MdzError(st, "mdz_host_unregister refused")
 
 
 def _dptr(a):
@@ -203,10 +219,18 @@ class Context:
         self._check(self.L.mdz_set_markers(self.h, C.c_int(len(x)), _dptr(x), _dptr(z), _iptr(phase)))
         self.n_markers = len(x)
 
-    def get_markers(self):
+    def get_markers(self, out=None):
+        """(x, z, phase, vx, vz) of the resident markers; `out` may hold five
+        preallocated arrays (e.g. registered with host_register) to fill."""
         n = self.n_markers
-        x, z, vx, vz = np.empty(n), np.empty(n), np.empty(n), np.empty(n)
-        ph = np.empty(n, np.int32)
+        if out is not None:
+            x, z, ph, vx, vz = out
+            for a, dt in ((x, np.float64), (z, np.float64), (ph, np.int32), (vx, np.float64), (vz, np.float64)):
+                if a.dtype != dt or a.size < n or not a.flags.c_contiguous:
+                    raise MdzError(1, "get_markers: out arrays must be contiguous x, z, vx, vz float64 and phase int32")
+        else:
+            x, z, vx, vz = np.empty(n), np.empty(n), np.empty(n), np.empty(n)
+            ph = np.empty(n, np.int32)
         self._check(self.L.mdz_get_markers(self.h, C.c_int(n), _dptr(x), _dptr(z), _iptr(ph), _dptr(vx), _dptr(vz)))
         return x, z, ph, vx, vz
 
@@ -332,8 +356,10 @@ class Context:
         v = np.ascontiguousarray(values, np.float64)
         self._check(self.L.mdz_set_marker_attr(self.h, C.c_int(attr), C.c_int(len(v)), _dptr(v)))
 
-    def get_marker_attr(self, attr):
-        v = np.zeros(self.n_markers)
+    def get_marker_attr(self, attr, out=None):
+        v = np.zeros(self.n_markers) if out is None else out
+        if v.dtype != np.float64 or v.size < self.n_markers or not v.flags.c_contiguous:
+            raise MdzError(1, "get_marker_attr: out must be a contiguous float64 array of the marker count")
         self._check(self.L.mdz_get_marker_attr(self.h, C.c_int(attr), C.c_int(len(v)), _dptr(v)))
         return v
 
@@ -348,7 +374,7 @@ class Context:
     def set_profiling(self, on):
         self._check(self.L.mdz_set_profiling(self.h, C.c_int(int(on))))
 
-    KERNEL_CLASSES = ["local_rheology", "stokes_apply", "mg_vcycle", "projection", "mlp_guess"]
+    KERNEL_CLASSES = ["local_rheology", "stokes_apply", "mg_vcycle", "projection", "mlp_guess", "krylov", "mg_setup"]
 
     def kernel_timing(self):
         """Summed event time, algorithmic bytes and launch count per kernel class,

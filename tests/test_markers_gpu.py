@@ -166,3 +166,32 @@ def test_g2p_rk4_vs_oracle_large():
     np.testing.assert_allclose(gx, o.x, rtol=1e-14, atol=1e-15)
     np.testing.assert_allclose(gz, o.z, rtol=1e-14, atol=1e-15)
     ctx.close()
+
+
+def test_registered_host_round_trip(ref, gctx):
+    """Markers uploaded from page-locked (registered) host arrays and read back
+    into registered arrays come back bit for bit; attributes likewise."""
+    g, ctx = gctx
+    n = len(ref["x"])
+    x = np.ascontiguousarray(ref["x"], np.float64).copy()
+    z = np.ascontiguousarray(ref["z"], np.float64).copy()
+    ph = np.ascontiguousarray(ref["phase"], np.int32).copy()
+    out = [np.zeros(n), np.zeros(n), np.zeros(n, np.int32), np.zeros(n), np.zeros(n)]
+    attr_in = np.linspace(-1.0, 1.0, n)
+    attr_out = np.zeros(n)
+    arrays = [x, z, ph, attr_in, attr_out] + out
+    for a in arrays:
+        mdz.host_register(a)
+    try:
+        ctx.set_markers(x, z, ph)
+        ctx.set_marker_attr(mdz.M_SXXD, attr_in)
+        ctx.get_markers(out=out)
+        ctx.get_marker_attr(mdz.M_SXXD, out=attr_out)
+    finally:
+        for a in arrays:
+            mdz.host_unregister(a)
+        ctx.set_markers(ref["x"], ref["z"], ref["phase"])
+    np.testing.assert_array_equal(out[0], x)
+    np.testing.assert_array_equal(out[1], z)
+    np.testing.assert_array_equal(out[2], ph)
+    np.testing.assert_array_equal(attr_out, attr_in)
