@@ -248,91 +248,108 @@ __device__ __forceinline__ float nc_weight(int i, int I) {
     return (i == 2 * I - 1 || i == 2 * I + 1) ? 0.5f : 0.0f;
 }
 
-// fine x += P xc   (both components)
+// Unknowns under the tag rule of k_level_tags (every level of a hierarchy
+// follows it; the fine level is checked before the hierarchy is built).
+__device__ __forceinline__ bool u_unknown(int k, int l, int Nx, int Nz) {
+    return k >= 1 && k <= Nx - 2 && l >= 1 && l <= Nz - 1;
+}
+__device__ __forceinline__ bool v_unknown(int i, int j, int Nx, int Nz) {
+    return i >= 1 && i <= Nx - 1 && j >= 1 && j <= Nz - 2;
+}
+
+// fine x += P xc at fine point (i, j) of the (Nx+1) x (Nz+1) box (both components)
 template <typename T>
-__global__ void k_mg_prolong_add(stokes_geom F, stokes_geom Cg, const T *__restrict__ cu, const T *__restrict__ cv,
-                                 T *__restrict__ fu, T *__restrict__ fv) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void mg_prolong_pt(const stokes_geom &F, const stokes_geom &Cg, const T *__restrict__ cu,
+                                              const T *__restrict__ cv, T *__restrict__ fu, T *__restrict__ fv,
+                                              int i, int j) {
     const int Nx = F.Nx, Nz = F.Nz, Nxc = Cg.Nx;
-    if (i < Nx && j <= Nz) {   // Vx: x node-centred, z cell-centred
-        int c = i + j * Nx;
-        if (F.BCu[c] == -1) {
-            int J0, J1;
-            float w0, w1;
-            cc_weights(j, Cg.ncz, J0, w0, J1, w1);
-            int Ia = i >> 1, Ib = (i + 1) >> 1;
-            float wa = (i & 1) ? 0.5f : 1.0f, wb = (i & 1) ? 0.5f : 0.0f;
-            T s = (T)(wa * w0) * cu[Ia + J0 * Nxc] + (T)(wa * w1) * cu[Ia + J1 * Nxc];
-            if (wb != 0.0f) s += (T)(wb * w0) * cu[Ib + J0 * Nxc] + (T)(wb * w1) * cu[Ib + J1 * Nxc];
-            fu[c] += s;
-        }
+    if (i < Nx && j <= Nz && u_unknown(i, j, Nx, Nz)) {   // Vx: x node-centred, z cell-centred
+        const int c = i + j * Nx;
+        int J0, J1;
+        float w0, w1;
+        cc_weights(j, Cg.ncz, J0, w0, J1, w1);
+        const int Ia = i >> 1, Ib = (i + 1) >> 1;
+        const float wa = (i & 1) ? 0.5f : 1.0f, wb = (i & 1) ? 0.5f : 0.0f;
+        const T a0 = cu[Ia + J0 * Nxc], a1 = cu[Ia + J1 * Nxc], b0 = cu[Ib + J0 * Nxc], b1 = cu[Ib + J1 * Nxc];
+        fu[c] += (T)(wa * w0) * a0 + (T)(wa * w1) * a1 + (T)(wb * w0) * b0 + (T)(wb * w1) * b1;
     }
-    if (i <= Nx && j < Nz) {   // Vz: x cell-centred, z node-centred
-        int c = i + j * (Nx + 1);
-        if (F.BCv[c] == -1) {
-            int I0, I1;
-            float w0, w1;
-            cc_weights(i, Cg.ncx, I0, w0, I1, w1);
-            int Ja = j >> 1, Jb = (j + 1) >> 1;
-            float wa = (j & 1) ? 0.5f : 1.0f, wb = (j & 1) ? 0.5f : 0.0f;
-            const int W = Nxc + 1;
-            T s = (T)(wa * w0) * cv[I0 + Ja * W] + (T)(wa * w1) * cv[I1 + Ja * W];
-            if (wb != 0.0f) s += (T)(wb * w0) * cv[I0 + Jb * W] + (T)(wb * w1) * cv[I1 + Jb * W];
-            fv[c] += s;
-        }
+    if (i <= Nx && j < Nz && v_unknown(i, j, Nx, Nz)) {   // Vz: x cell-centred, z node-centred
+        const int c = i + j * (Nx + 1);
+        int I0, I1;
+        float w0, w1;
+        cc_weights(i, Cg.ncx, I0, w0, I1, w1);
+        const int Ja = j >> 1, Jb = (j + 1) >> 1;
+        const float wa = (j & 1) ? 0.5f : 1.0f, wb = (j & 1) ? 0.5f : 0.0f;
+        const int W = Nxc + 1;
+        const T a0 = cv[I0 + Ja * W], a1 = cv[I1 + Ja * W], b0 = cv[I0 + Jb * W], b1 = cv[I1 + Jb * W];
+        fv[c] += (T)(wa * w0) * a0 + (T)(wa * w1) * a1 + (T)(wb * w0) * b0 + (T)(wb * w1) * b1;
     }
 }
 
-// coarse f = P^T fine r
 template <typename T>
-__global__ void k_mg_restrict(stokes_geom F, stokes_geom Cg, const T *__restrict__ ru, const T *__restrict__ rv,
-                              T *__restrict__ cu, T *__restrict__ cv) {
-    int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y * blockDim.y + threadIdx.y;
+__global__ void k_mg_prolong_add(stokes_geom F, stokes_geom Cg, const T *__restrict__ cu, const T *__restrict__ cv,
+                                 T *__restrict__ fu, T *__restrict__ fv) {
+    mg_prolong_pt<T>(F, Cg, cu, cv, fu, fv, blockIdx.x * blockDim.x + threadIdx.x,
+                     blockIdx.y * blockDim.y + threadIdx.y);
+}
+
+// coarse f = P^T fine r at coarse point (I, J): the 12 fine values of each
+// component are loaded together (indices clamped into the box, weights of
+// points outside the unknowns zero)
+template <typename T>
+__device__ __forceinline__ void mg_restrict_pt(const stokes_geom &F, const stokes_geom &Cg, const T *__restrict__ ru,
+                                               const T *__restrict__ rv, T *__restrict__ cu, T *__restrict__ cv,
+                                               int I, int J) {
     const int Nxf = F.Nx, Nzf = F.Nz, Nx = Cg.Nx, Nz = Cg.Nz;
     if (I < Nx && J <= Nz) {
-        int c = I + J * Nx;
         T s = 0;
-        if (Cg.BCu[c] == -1) {
-            for (int j = 2 * J - 2; j <= 2 * J + 1; j++) {
-                if (j < 1 || j > F.ncz) continue;
+        if (u_unknown(I, J, Nx, Nz)) {
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                const int j = 2 * J - 2 + a;
                 int J0, J1;
                 float w0, w1;
                 cc_weights(j, Cg.ncz, J0, w0, J1, w1);
-                float wz = (J0 == J ? w0 : 0.0f) + (J1 == J && J1 != J0 ? w1 : 0.0f);
-                if (wz == 0.0f) continue;
-                for (int i = 2 * I - 1; i <= 2 * I + 1; i++) {
-                    if (i < 0 || i >= Nxf) continue;
-                    float wx = nc_weight(i, I);
-                    if (wx == 0.0f) continue;
-                    int fcidx = i + j * Nxf;
-                    if (F.BCu[fcidx] == -1) s += (T)(wx * wz) * ru[fcidx];
+                const float wz = (J0 == J ? w0 : 0.0f) + (J1 == J && J1 != J0 ? w1 : 0.0f);
+                const int jc = min(max(j, 0), Nzf);
+#pragma unroll
+                for (int b = 0; b < 3; b++) {
+                    const int i = 2 * I - 1 + b;
+                    const float w = (j >= 1 && j <= F.ncz && u_unknown(i, j, Nxf, Nzf)) ? nc_weight(i, I) * wz : 0.0f;
+                    s += (T)w * ru[min(max(i, 0), Nxf - 1) + jc * Nxf];
                 }
             }
         }
-        cu[c] = s;
+        cu[I + J * Nx] = s;
     }
     if (I <= Nx && J < Nz) {
-        int c = I + J * (Nx + 1);
         T s = 0;
-        if (Cg.BCv[c] == -1) {
-            for (int i = 2 * I - 2; i <= 2 * I + 1; i++) {
-                if (i < 1 || i > F.ncx) continue;
+        if (v_unknown(I, J, Nx, Nz)) {
+#pragma unroll
+            for (int a = 0; a < 4; a++) {
+                const int i = 2 * I - 2 + a;
                 int I0, I1;
                 float w0, w1;
                 cc_weights(i, Cg.ncx, I0, w0, I1, w1);
-                float wx = (I0 == I ? w0 : 0.0f) + (I1 == I && I1 != I0 ? w1 : 0.0f);
-                if (wx == 0.0f) continue;
-                for (int j = 2 * J - 1; j <= 2 * J + 1; j++) {
-                    if (j < 0 || j >= Nzf) continue;
-                    float wz = nc_weight(j, J);
-                    if (wz == 0.0f) continue;
-                    int fcidx = i + j * (Nxf + 1);
-                    if (F.BCv[fcidx] == -1) s += (T)(wx * wz) * rv[fcidx];
+                const float wx = (I0 == I ? w0 : 0.0f) + (I1 == I && I1 != I0 ? w1 : 0.0f);
+                const int ic = min(max(i, 0), Nxf);
+#pragma unroll
+                for (int b = 0; b < 3; b++) {
+                    const int j = 2 * J - 1 + b;
+                    const float w = (i >= 1 && i <= F.ncx && v_unknown(i, j, Nxf, Nzf)) ? wx * nc_weight(j, J) : 0.0f;
+                    s += (T)w * rv[ic + min(max(j, 0), Nzf - 1) * (Nxf + 1)];
                 }
             }
         }
-        cv[c] = s;
+        cv[I + J * (Nx + 1)] = s;
     }
+}
+
+template <typename T>
+__global__ void k_mg_restrict(stokes_geom F, stokes_geom Cg, const T *__restrict__ ru, const T *__restrict__ rv,
+                              T *__restrict__ cu, T *__restrict__ cv) {
+    mg_restrict_pt<T>(F, Cg, ru, rv, cu, cv, blockIdx.x * blockDim.x + threadIdx.x,
+                      blockIdx.y * blockDim.y + threadIdx.y);
 }
 
 // ---------------------------------------------------------------------------
@@ -409,20 +426,20 @@ __device__ __forceinline__ T st_vrow(int Nx, int Nz, const T *__restrict__ sv, s
     return s;
 }
 
-// out = x + omega D^-1 (f - A x) on a stencil level (x == nullptr: x = 0)
+// out = x + omega D^-1 (f - A x) on a stencil level at point (i, j)
+// (x == nullptr: x = 0)
 template <typename T>
-__global__ void __launch_bounds__(256) k_st_smooth(stokes_geom G, const T *__restrict__ su, const T *__restrict__ sv,
-                                                   const T *__restrict__ xu, const T *__restrict__ xv,
-                                                   const T *__restrict__ fu, const T *__restrict__ fv,
-                                                   const T *__restrict__ idu, const T *__restrict__ idv, T omega,
-                                                   T *__restrict__ ou, T *__restrict__ ov) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void st_smooth_pt(const stokes_geom &G, const T *__restrict__ su, const T *__restrict__ sv,
+                                             const T *__restrict__ xu, const T *__restrict__ xv,
+                                             const T *__restrict__ fu, const T *__restrict__ fv,
+                                             const T *__restrict__ idu, const T *__restrict__ idv, T omega,
+                                             T *__restrict__ ou, T *__restrict__ ov, int i, int j) {
     const int Nx = G.Nx, Nz = G.Nz;
     const size_t nu = (size_t)Nx * (Nz + 1), nv = (size_t)(Nx + 1) * Nz;
     if (i < Nx && j <= Nz) {
         int c = i + j * Nx;
         T r = 0;
-        if (G.BCu[c] == -1) {
+        if (u_unknown(i, j, Nx, Nz)) {
             if (xu) r = xu[c] + omega * idu[c] * (fu[c] - st_urow<T>(Nx, Nz, su, nu, xu, xv, i, j));
             else r = omega * idu[c] * fu[c];
         }
@@ -431,11 +448,39 @@ __global__ void __launch_bounds__(256) k_st_smooth(stokes_geom G, const T *__res
     if (i <= Nx && j < Nz) {
         int c = i + j * (Nx + 1);
         T r = 0;
-        if (G.BCv[c] == -1) {
+        if (v_unknown(i, j, Nx, Nz)) {
             if (xv) r = xv[c] + omega * idv[c] * (fv[c] - st_vrow<T>(Nx, Nz, sv, nv, xu, xv, i, j));
             else r = omega * idv[c] * fv[c];
         }
         ov[c] = r;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_st_smooth(stokes_geom G, const T *__restrict__ su, const T *__restrict__ sv,
+                                                   const T *__restrict__ xu, const T *__restrict__ xv,
+                                                   const T *__restrict__ fu, const T *__restrict__ fv,
+                                                   const T *__restrict__ idu, const T *__restrict__ idv, T omega,
+                                                   T *__restrict__ ou, T *__restrict__ ov) {
+    st_smooth_pt<T>(G, su, sv, xu, xv, fu, fv, idu, idv, omega, ou, ov, blockIdx.x * blockDim.x + threadIdx.x,
+                    blockIdx.y * blockDim.y + threadIdx.y);
+}
+
+template <typename T>
+__device__ __forceinline__ void st_residual_pt(const stokes_geom &G, const T *__restrict__ su,
+                                               const T *__restrict__ sv, const T *__restrict__ xu,
+                                               const T *__restrict__ xv, const T *__restrict__ fu,
+                                               const T *__restrict__ fv, T *__restrict__ ru, T *__restrict__ rv,
+                                               int i, int j) {
+    const int Nx = G.Nx, Nz = G.Nz;
+    const size_t nu = (size_t)Nx * (Nz + 1), nv = (size_t)(Nx + 1) * Nz;
+    if (i < Nx && j <= Nz) {
+        int c = i + j * Nx;
+        ru[c] = u_unknown(i, j, Nx, Nz) ? fu[c] - st_urow<T>(Nx, Nz, su, nu, xu, xv, i, j) : T(0);
+    }
+    if (i <= Nx && j < Nz) {
+        int c = i + j * (Nx + 1);
+        rv[c] = v_unknown(i, j, Nx, Nz) ? fv[c] - st_vrow<T>(Nx, Nz, sv, nv, xu, xv, i, j) : T(0);
     }
 }
 
@@ -445,17 +490,8 @@ __global__ void __launch_bounds__(256) k_st_residual(stokes_geom G, const T *__r
                                                      const T *__restrict__ xv, const T *__restrict__ fu,
                                                      const T *__restrict__ fv, T *__restrict__ ru,
                                                      T *__restrict__ rv) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int Nx = G.Nx, Nz = G.Nz;
-    const size_t nu = (size_t)Nx * (Nz + 1), nv = (size_t)(Nx + 1) * Nz;
-    if (i < Nx && j <= Nz) {
-        int c = i + j * Nx;
-        ru[c] = G.BCu[c] == -1 ? fu[c] - st_urow<T>(Nx, Nz, su, nu, xu, xv, i, j) : T(0);
-    }
-    if (i <= Nx && j < Nz) {
-        int c = i + j * (Nx + 1);
-        rv[c] = G.BCv[c] == -1 ? fv[c] - st_vrow<T>(Nx, Nz, sv, nv, xu, xv, i, j) : T(0);
-    }
+    st_residual_pt<T>(G, su, sv, xu, xv, fu, fv, ru, rv, blockIdx.x * blockDim.x + threadIdx.x,
+                      blockIdx.y * blockDim.y + threadIdx.y);
 }
 
 template <typename T>
@@ -636,19 +672,11 @@ __global__ void __launch_bounds__(256) k_picard_stencil(stokes_geom G, const T *
 
 // Coarse stencils = R A P, one thread per coarse row, FP64 accumulation in
 // shared memory (plane-major, one column per thread).  Every level of the
-// hierarchy follows the tag rule of k_level_tags (the fine level is checked
-// before the hierarchy is built), so "is an unknown" is index arithmetic and
-// the kernel reads no tags.  Each fine row's 31 coefficients are loaded in
+// hierarchy follows the tag rule (u_unknown / v_unknown), so the kernel
+// reads no tags.  Each fine row's 31 coefficients are loaded in
 // one batch before use: loaded one at a time behind the zero test they
 // serialise on memory latency.  An entry landing outside the footprint
 // (impossible with this P) sets *bad.
-__device__ __forceinline__ bool u_unknown(int k, int l, int Nx, int Nz) {
-    return k >= 1 && k <= Nx - 2 && l >= 1 && l <= Nz - 1;
-}
-__device__ __forceinline__ bool v_unknown(int i, int j, int Nx, int Nz) {
-    return i >= 1 && i <= Nx - 1 && j >= 1 && j <= Nz - 2;
-}
-
 // parents of fine u node (i, j) / v node (i, j) as coarse (I, J) pairs
 __device__ __forceinline__ void u_parents_ij(int i, int j, int nczc, int *I, int *J, float *w) {
     int J0, J1;
@@ -996,6 +1024,110 @@ __global__ void __launch_bounds__(256) k_coarse_dense_solve(int n, int nu, int n
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// Bottom of the V-cycle in one CTA.  The small levels (a few thousand points
+// each) cost one launch per sweep, residual and transfer when run as grid
+// kernels, and each such launch is a few microseconds of latency for a few
+// hundred rows of work; here the whole descent from level `first` to the
+// dense coarsest level and the ascent back run in one 1024-thread block with
+// a barrier between phases.  Same arithmetic as the grid kernels (the same
+// point functions), so the result is identical.  The level's result ends in
+// its xu / xv buffers like the grid path's.
+#define MG_BOTTOM_MAX 6
+#define MG_BOTTOM_POINTS 4096
+#define MG_BOTTOM_THREADS 1024
+template <typename T>
+struct mg_bottom_level {
+    stokes_geom G;
+    const T *su, *sv, *idu, *idv;
+    T *xu, *xv, *yu, *yv, *fu, *fv, *ru, *rv;
+};
+
+template <typename T>
+struct mg_bottom_args {
+    int nlev, nu1, nu2, ndense;   // nlev levels, the last one the dense coarsest
+    T omega;
+    const int *dmap;
+    const T *AinvT;
+    mg_bottom_level<T> L[MG_BOTTOM_MAX];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(MG_BOTTOM_THREADS) k_mg_bottom(const __grid_constant__ mg_bottom_args<T> A) {
+    __shared__ T fs[MG_DENSE_MAX];
+    T *xu[MG_BOTTOM_MAX], *xv[MG_BOTTOM_MAX], *yu[MG_BOTTOM_MAX], *yv[MG_BOTTOM_MAX];
+    for (int l = 0; l < A.nlev; l++) { xu[l] = A.L[l].xu; xv[l] = A.L[l].xv; yu[l] = A.L[l].yu; yv[l] = A.L[l].yv; }
+    const int tid = threadIdx.x;
+    auto swap_xy = [&](int l) {
+        T *t = xu[l]; xu[l] = yu[l]; yu[l] = t;
+        t = xv[l]; xv[l] = yv[l]; yv[l] = t;
+    };
+    for (int l = 0; l < A.nlev - 1; l++) {   // descent
+        const mg_bottom_level<T> &L = A.L[l];
+        const int W = L.G.Nx + 1, npt = W * (L.G.Nz + 1);
+        for (int p = tid; p < npt; p += blockDim.x)
+            st_smooth_pt<T>(L.G, L.su, L.sv, nullptr, nullptr, L.fu, L.fv, L.idu, L.idv, A.omega, xu[l], xv[l],
+                            p % W, p / W);
+        __syncthreads();
+        for (int s = 1; s < A.nu1; s++) {
+            for (int p = tid; p < npt; p += blockDim.x)
+                st_smooth_pt<T>(L.G, L.su, L.sv, xu[l], xv[l], L.fu, L.fv, L.idu, L.idv, A.omega, yu[l], yv[l],
+                                p % W, p / W);
+            __syncthreads();
+            swap_xy(l);
+        }
+        for (int p = tid; p < npt; p += blockDim.x)
+            st_residual_pt<T>(L.G, L.su, L.sv, xu[l], xv[l], L.fu, L.fv, L.ru, L.rv, p % W, p / W);
+        __syncthreads();
+        const mg_bottom_level<T> &C = A.L[l + 1];
+        const int Wc = C.G.Nx + 1, nptc = Wc * (C.G.Nz + 1);
+        for (int p = tid; p < nptc; p += blockDim.x)
+            mg_restrict_pt<T>(L.G, C.G, L.ru, L.rv, C.fu, C.fv, p % Wc, p / Wc);
+        __syncthreads();
+    }
+    {   // dense coarsest: x = A^-1 f (zero outside the unknowns)
+        const int lc = A.nlev - 1, n = A.ndense;
+        const mg_bottom_level<T> &C = A.L[lc];
+        const int nu = C.G.Nx * (C.G.Nz + 1), nv = (C.G.Nx + 1) * C.G.Nz;
+        for (int i = tid; i < n; i += blockDim.x) {
+            const int m = A.dmap[i];
+            fs[i] = m < nu ? C.fu[m] : C.fv[m - nu];
+        }
+        for (int i = tid; i < nu; i += blockDim.x) xu[lc][i] = T(0);
+        for (int i = tid; i < nv; i += blockDim.x) xv[lc][i] = T(0);
+        __syncthreads();
+        for (int r = tid; r < n; r += blockDim.x) {
+            T s = 0;
+            for (int j = 0; j < n; j++) s += A.AinvT[(size_t)j * n + r] * fs[j];
+            const int m = A.dmap[r];
+            if (m < nu) xu[lc][m] = s; else xv[lc][m - nu] = s;
+        }
+        __syncthreads();
+    }
+    for (int l = A.nlev - 2; l >= 0; l--) {   // ascent
+        const mg_bottom_level<T> &L = A.L[l];
+        const mg_bottom_level<T> &C = A.L[l + 1];
+        const int W = L.G.Nx + 1, npt = W * (L.G.Nz + 1);
+        for (int p = tid; p < npt; p += blockDim.x)
+            mg_prolong_pt<T>(L.G, C.G, xu[l + 1], xv[l + 1], xu[l], xv[l], p % W, p / W);
+        __syncthreads();
+        for (int s = 0; s < A.nu2; s++) {
+            for (int p = tid; p < npt; p += blockDim.x)
+                st_smooth_pt<T>(L.G, L.su, L.sv, xu[l], xv[l], L.fu, L.fv, L.idu, L.idv, A.omega, yu[l], yv[l],
+                                p % W, p / W);
+            __syncthreads();
+            swap_xy(l);
+        }
+    }
+    if (xu[0] != A.L[0].xu) {   // odd number of swaps on the first level: copy back
+        const mg_bottom_level<T> &L = A.L[0];
+        const int nu = L.G.Nx * (L.G.Nz + 1), nv = (L.G.Nx + 1) * L.G.Nz;
+        for (int i = tid; i < nu; i += blockDim.x) L.xu[i] = xu[0][i];
+        for (int i = tid; i < nv; i += blockDim.x) L.xv[i] = xv[0][i];
+    }
+}
+
 // ---------------------------------------------------------------------------
 template <typename T>
 static cudaError_t alloc0(T **p, size_t n) {
@@ -1315,6 +1447,21 @@ static mdz_status vcycle(mdz_ctx *ctx, mg_hier<T> &H, int l, int nu1, int nu2, T
         return MDZ_OK;
     }
     const bool viscous = l == 0 && !H.newton;   // level 0 of a Picard hierarchy: stencil from eta directly
+    const mg_level<T> &Cd = H.L[H.nlev - 1];
+    if (!viscous && Cd.ndense && H.nlev - l <= MG_BOTTOM_MAX &&
+        (long long)(L.Nx + 1) * (L.Nz + 1) <= MG_BOTTOM_POINTS) {   // this level and all below in one CTA
+        mg_bottom_args<T> A;
+        A.nlev = H.nlev - l; A.nu1 = nu1; A.nu2 = nu2; A.ndense = Cd.ndense; A.omega = omega;
+        A.dmap = Cd.dmap; A.AinvT = Cd.AinvT;
+        for (int q = 0; q < A.nlev; q++) {
+            const mg_level<T> &B = H.L[l + q];
+            A.L[q] = mg_bottom_level<T>{B.geom(), B.su, B.sv, B.idu, B.idv, B.xu, B.xv, B.yu, B.yv,
+                                        B.fu, B.fv, B.ru, B.rv};
+        }
+        k_mg_bottom<T><<<1, MG_BOTTOM_THREADS, 0, st>>>(A);
+        MDZ_LAUNCHED(ctx);
+        return MDZ_OK;
+    }
     auto smooth = [&](const T *xu, const T *xv, T *ou, T *ov) {
         if (viscous) k_mg_smooth<T><<<gr, bl, 0, st>>>(G, D, xu, xv, L.fu, L.fv, L.idu, L.idv, omega, ou, ov);
         else k_st_smooth<T><<<gr, bl, 0, st>>>(G, L.su, L.sv, xu, xv, L.fu, L.fv, L.idu, L.idv, omega, ou, ov);
