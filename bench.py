@@ -190,23 +190,29 @@ def e2e_form(cfg_builder, precision, learned, steps, size):
     pinned = list(hin.values()) + hout + [hsxx, hu]
     for a in pinned:
         mdz.host_register(a)
-    times = []
+    times, parts = [], [0.0, 0.0, 0.0, 0.0]
     for _ in range(steps):
         t0 = time.perf_counter()
         ctx.set_markers(hin["x"], hin["z"], hin["phase"])
         for attr, key in attrs:
             ctx.set_marker_attr(attr, hin[key])
-        ctx.time_step(mat, model)
+        t1 = time.perf_counter()
+        rep = ctx.time_step(mat, model)
+        t2 = time.perf_counter()
         ctx.get_markers(out=hout)
         ctx.get_marker_attr(mdz.M_SXXD, out=hsxx)
         ctx.L.mdz_get_velocity(ctx.h, mdz._dptr(hu), None, None)
-        times.append((time.perf_counter() - t0) * 1e3)
+        t3 = time.perf_counter()
+        times.append((t3 - t0) * 1e3)
+        for q, v in enumerate(((t1 - t0) * 1e3, (t2 - t1) * 1e3, (t3 - t2) * 1e3, rep.ms_total)):
+            parts[q] += v / steps
     for a in pinned:
         mdz.host_unregister(a)
     h2d = n * (8 * 2 + 4) + n * 8 * len(attrs)
     d2h = n * (8 * 4 + 4) + n * 8 + g.size(-1) * 8
     ctx.close()
-    return sum(times) / len(times), h2d, d2h
+    split = dict(zip(("upload_ms", "step_ms", "download_ms", "step_device_ms"), parts))
+    return sum(times) / len(times), h2d, d2h, split
 
 
 def builder(size):
@@ -295,7 +301,7 @@ def main():
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
-    e2e_ms, h2d, d2h = e2e_form(b, 32, 1, max(1, args.steps - 1), size)
+    e2e_ms, h2d, d2h, e2e_split = e2e_form(b, 32, 1, max(1, args.steps - 1), size)
     k = fast["kernel"]
     achieved = k["bytes"] / (k["ms"] * 1e-3) / 1e9 if k["ms"] > 0 else None
     line = {
@@ -310,8 +316,10 @@ def main():
         "forms": {"plain_fp64_ms": plain["ms_wall"], "learned_fp32_ir_ms": fast["ms_wall"],
                   "speedup_vs_plain_fp64": plain["ms_wall"] / fast["ms_wall"],
                   "plain_report": plain["reports"][-1], "learned_fp32_ir_report": fast["reports"][-1],
-                  "guess_training_s": fast["train"][0], "guess_training_loss": fast["train"][1]},
-        "e2e": {"value": e2e_ms, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                  "guess_training_s": fast["train"][0], "guess_training_loss": fast["train"][1],
+                  "plain_fp64_classes": plain["kernel"]["classes"], "learned_fp32_ir_classes": fast["kernel"]["classes"]},
+        "e2e": {"value": e2e_ms, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "split": e2e_split},
         "gpu_launches": fast["launches"] // args.steps,
         "roofline": {"bound": "hbm", "kernel": k["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None, "traffic": None,

@@ -154,16 +154,17 @@ __global__ void k_mg_diag(stokes_geom G, const T *__restrict__ D11, const T *__r
                           T *__restrict__ idv) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int Nx = G.Nx, Nz = G.Nz, ncx = G.ncx, nu = Nx * (Nz + 1), nv = (Nx + 1) * Nz;
-    const double celvol = G.dx * G.dz, dx2 = G.dx * G.dx, dz2 = G.dz * G.dz;
+    // in the level's precision, with 1/dx^2, 1/dz^2 precomputed (FP64
+    // divisions are long instruction sequences on this part)
+    const T celvol = (T)(G.dx * G.dz), idx2 = (T)(G.idx * G.idx), idz2 = (T)(G.idz * G.idz);
     if (i < nu) {
         int k = i % Nx, l = i / Nx;
         T d = 0;
         if (G.BCu[i] == -1) {
             int c2 = k - 1 + (l - 1) * ncx;
-            double inS = G.BCu[i - Nx] != 13 ? 1.0 : 0.0, inN = G.BCu[i + Nx] != 13 ? 1.0 : 0.0;
-            double a = (inN * (double)D33[i] + inS * (double)D33[i - Nx]) / dz2 +
-                       (2.0 / 3.0) * ((double)D11[c2 + 1] + (double)D11[c2]) / dx2;
-            d = (T)(1.0 / (a * celvol));
+            T inS = G.BCu[i - Nx] != 13 ? T(1) : T(0), inN = G.BCu[i + Nx] != 13 ? T(1) : T(0);
+            T a = (inN * D33[i] + inS * D33[i - Nx]) * idz2 + T(2.0 / 3.0) * (D11[c2 + 1] + D11[c2]) * idx2;
+            d = T(1) / (a * celvol);
         }
         idu[i] = d;
     }
@@ -172,10 +173,9 @@ __global__ void k_mg_diag(stokes_geom G, const T *__restrict__ D11, const T *__r
         T d = 0;
         if (G.BCv[i] == -1) {
             int c1 = k + l * Nx, c2 = k - 1 + (l - 1) * ncx;
-            double inW = G.BCv[i - 1] != 13 ? 1.0 : 0.0, inE = G.BCv[i + 1] != 13 ? 1.0 : 0.0;
-            double a = (2.0 / 3.0) * ((double)D11[c2 + ncx] + (double)D11[c2]) / dz2 +
-                       (inE * (double)D33[c1] + inW * (double)D33[c1 - 1]) / dx2;
-            d = (T)(1.0 / (a * celvol));
+            T inW = G.BCv[i - 1] != 13 ? T(1) : T(0), inE = G.BCv[i + 1] != 13 ? T(1) : T(0);
+            T a = T(2.0 / 3.0) * (D11[c2 + ncx] + D11[c2]) * idz2 + (inE * D33[c1] + inW * D33[c1 - 1]) * idx2;
+            d = T(1) / (a * celvol);
         }
         idv[i] = d;
     }
@@ -587,8 +587,9 @@ __global__ void k_probe_collect(stokes_geom G, int comp, int cx, int cz, const T
 // Level-0 stencils of the Picard velocity block written out directly from
 // the viscosities (the composition strain rate -> D11 / D33 stress ->
 // divergence of xrow / zrow with the same row flags, times the cell volume),
-// one thread per (i, j); every plane of every row is written, zeros outside
-// the unknowns.  Equal to probing the Picard operator, in one pass.
+// one thread per (i, j), in the level's precision; every plane of every row
+// is written, zeros outside the unknowns.  Equal to probing the Picard
+// operator, in one pass.
 //   u-row (k, l), aE = inE D11[E], aW = inW D11[W], bN = inN D33[N], bS = inS D33[S]:
 //     u(k+-1, l): -2/3 aE|aW / dx^2   u(k, l+-1): -bN|bS / dz^2   u(k, l): the sum of their negatives
 //     v(k+1, l): aE/3 - bN   v(k+1, l-1): bS - aE/3   v(k, l): bN - aW/3   v(k, l-1): aW/3 - bS   (/ dx dz)
@@ -602,76 +603,78 @@ __global__ void __launch_bounds__(256) k_picard_stencil(stokes_geom G, const T *
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     const int Nx = G.Nx, Nz = G.Nz, nx = Nx, ncx = G.ncx, nxvz = Nx + 1;
     const size_t nu = (size_t)Nx * (Nz + 1), nv = (size_t)(Nx + 1) * Nz;
-    const double celvol = G.dx * G.dz, ixx = G.idx * G.idx, izz = G.idz * G.idz, ixz = G.idx * G.idz;
+    const T celvol = (T)(G.dx * G.dz), ixx = (T)(G.idx * G.idx), izz = (T)(G.idz * G.idz),
+            ixz = (T)(G.idx * G.idz);
     if (i < Nx && j <= Nz) {   // u-row (k, l) = (i, j)
         const int k = i, l = j, c1 = k + l * nx;
-        double a[MG_NST];
+        T a[MG_NST];
 #pragma unroll
-        for (int q = 0; q < MG_NST; q++) a[q] = 0.0;
+        for (int q = 0; q < MG_NST; q++) a[q] = T(0);
         if (G.BCu[c1] == -1) {
             const int c2 = k - 1 + (l - 1) * ncx, iPrW = c2, iPrE = c2 + 1, ixyN = c1, ixyS = c1 - nx;
-            const double inW = G.BCp[iPrW] == -1 ? 1.0 : 0.0, inE = G.BCp[iPrE] == -1 ? 1.0 : 0.0;
-            const double inS = (G.BCg[ixyS] != 30 && G.BCu[c1 - nx] != 13) ? 1.0 : 0.0;
-            const double inN = (G.BCg[ixyN] != 30 && G.BCu[c1 + nx] != 13) ? 1.0 : 0.0;
-            const double aE = inE * (double)D11[iPrE], aW = inW * (double)D11[iPrW];
-            const double bN = inN * (double)D33[ixyN], bS = inS * (double)D33[ixyS];
-            const double uE = -(2.0 / 3.0) * aE * ixx, uW = -(2.0 / 3.0) * aW * ixx;
-            const double uN = -bN * izz, uS = -bS * izz;
-            auto isu = [&](int kk, int ll) { return G.BCu[kk + ll * nx] == -1 ? 1.0 : 0.0; };
-            auto isv = [&](int ii, int jj) { return G.BCv[ii + jj * nxvz] == -1 ? 1.0 : 0.0; };
+            const T inW = G.BCp[iPrW] == -1 ? T(1) : T(0), inE = G.BCp[iPrE] == -1 ? T(1) : T(0);
+            const T inS = (G.BCg[ixyS] != 30 && G.BCu[c1 - nx] != 13) ? T(1) : T(0);
+            const T inN = (G.BCg[ixyN] != 30 && G.BCu[c1 + nx] != 13) ? T(1) : T(0);
+            const T aE = inE * D11[iPrE], aW = inW * D11[iPrW];
+            const T bN = inN * D33[ixyN], bS = inS * D33[ixyS];
+            const T uE = -T(2.0 * T(1.0 / 3.0)) * aE * ixx, uW = -T(2.0 * T(1.0 / 3.0)) * aW * ixx;
+            const T uN = -bN * izz, uS = -bS * izz;
+            auto isu = [&](int kk, int ll) { return G.BCu[kk + ll * nx] == -1 ? T(1) : T(0); };
+            auto isv = [&](int ii, int jj) { return G.BCv[ii + jj * nxvz] == -1 ? T(1) : T(0); };
             a[(0 + 1) + 3 * (0 + 2)] = -(uE + uW + uN + uS);
             a[(1 + 1) + 3 * (0 + 2)] = uE * isu(k + 1, l);
             a[(-1 + 1) + 3 * (0 + 2)] = uW * isu(k - 1, l);
             a[(0 + 1) + 3 * (1 + 2)] = uN * isu(k, l + 1);
             a[(0 + 1) + 3 * (-1 + 2)] = uS * isu(k, l - 1);
-            a[15 + (1 + 1) + 4 * (0 + 2)] = (aE / 3.0 - bN) * ixz * isv(k + 1, l);
-            a[15 + (1 + 1) + 4 * (-1 + 2)] = (bS - aE / 3.0) * ixz * isv(k + 1, l - 1);
-            a[15 + (0 + 1) + 4 * (0 + 2)] = (bN - aW / 3.0) * ixz * isv(k, l);
-            a[15 + (0 + 1) + 4 * (-1 + 2)] = (aW / 3.0 - bS) * ixz * isv(k, l - 1);
+            a[15 + (1 + 1) + 4 * (0 + 2)] = (aE * T(1.0 / 3.0) - bN) * ixz * isv(k + 1, l);
+            a[15 + (1 + 1) + 4 * (-1 + 2)] = (bS - aE * T(1.0 / 3.0)) * ixz * isv(k + 1, l - 1);
+            a[15 + (0 + 1) + 4 * (0 + 2)] = (bN - aW * T(1.0 / 3.0)) * ixz * isv(k, l);
+            a[15 + (0 + 1) + 4 * (-1 + 2)] = (aW * T(1.0 / 3.0) - bS) * ixz * isv(k, l - 1);
         }
 #pragma unroll
-        for (int q = 0; q < MG_NST; q++) su[(size_t)q * nu + c1] = (T)(a[q] * celvol);
+        for (int q = 0; q < MG_NST; q++) su[(size_t)q * nu + c1] = a[q] * celvol;
     }
     if (i <= Nx && j < Nz) {   // v-row (k, l) = (i, j)
         const int k = i, l = j, c3 = k + l * nxvz;
-        double a[MG_NST];
+        T a[MG_NST];
 #pragma unroll
-        for (int q = 0; q < MG_NST; q++) a[q] = 0.0;
+        for (int q = 0; q < MG_NST; q++) a[q] = T(0);
         if (G.BCv[c3] == -1) {
             const int c1 = k + l * nx, c2 = k - 1 + (l - 1) * ncx;
             const int iPrS = c2, iPrN = c2 + ncx, ixyW = c1 - 1, ixyE = c1;
-            double inS = 0.0, inN = 0.0;
+            T inS = 0, inN = 0;
             const bool s30 = G.BCv[c3 - nxvz] == 30, n30 = G.BCv[c3 + nxvz] == 30;
-            if (!s30 && !n30) { inS = 1.0; inN = 1.0; }
-            if (s30 && !n30) inN = 1.0;
-            if (!s30 && n30) inS = 1.0;
-            if (G.BCp[iPrS] == -1) inS = 1.0;
-            if (G.BCp[iPrN] == -1) inN = 1.0;
-            const double inW = (G.BCg[ixyW] != 30 && G.BCv[c3 - 1] != 13) ? 1.0 : 0.0;
-            const double inE = (G.BCg[ixyE] != 30 && G.BCv[c3 + 1] != 13) ? 1.0 : 0.0;
-            const double cN = inN * (double)D11[iPrN], cS = inS * (double)D11[iPrS];
-            const double dE = inE * (double)D33[ixyE], dW = inW * (double)D33[ixyW];
-            const double vN = -(2.0 / 3.0) * cN * izz, vS = -(2.0 / 3.0) * cS * izz;
-            const double vE = -dE * ixx, vW = -dW * ixx;
-            auto isu = [&](int kk, int ll) { return G.BCu[kk + ll * nx] == -1 ? 1.0 : 0.0; };
-            auto isv = [&](int ii, int jj) { return G.BCv[ii + jj * nxvz] == -1 ? 1.0 : 0.0; };
+            if (!s30 && !n30) { inS = 1; inN = 1; }
+            if (s30 && !n30) inN = 1;
+            if (!s30 && n30) inS = 1;
+            if (G.BCp[iPrS] == -1) inS = 1;
+            if (G.BCp[iPrN] == -1) inN = 1;
+            const T inW = (G.BCg[ixyW] != 30 && G.BCv[c3 - 1] != 13) ? T(1) : T(0);
+            const T inE = (G.BCg[ixyE] != 30 && G.BCv[c3 + 1] != 13) ? T(1) : T(0);
+            const T cN = inN * D11[iPrN], cS = inS * D11[iPrS];
+            const T dE = inE * D33[ixyE], dW = inW * D33[ixyW];
+            const T vN = -T(2.0 * T(1.0 / 3.0)) * cN * izz, vS = -T(2.0 * T(1.0 / 3.0)) * cS * izz;
+            const T vE = -dE * ixx, vW = -dW * ixx;
+            auto isu = [&](int kk, int ll) { return G.BCu[kk + ll * nx] == -1 ? T(1) : T(0); };
+            auto isv = [&](int ii, int jj) { return G.BCv[ii + jj * nxvz] == -1 ? T(1) : T(0); };
             a[(0 + 2) + 5 * (0 + 1)] = -(vN + vS + vE + vW);
             a[(0 + 2) + 5 * (1 + 1)] = vN * isv(k, l + 1);
             a[(0 + 2) + 5 * (-1 + 1)] = vS * isv(k, l - 1);
             a[(1 + 2) + 5 * (0 + 1)] = vE * isv(k + 1, l);
             a[(-1 + 2) + 5 * (0 + 1)] = vW * isv(k - 1, l);
-            a[15 + (0 + 2) + 4 * (1 + 1)] = (cN / 3.0 - dE) * ixz * isu(k, l + 1);
-            a[15 + (-1 + 2) + 4 * (1 + 1)] = (dW - cN / 3.0) * ixz * isu(k - 1, l + 1);
-            a[15 + (0 + 2) + 4 * (0 + 1)] = (dE - cS / 3.0) * ixz * isu(k, l);
-            a[15 + (-1 + 2) + 4 * (0 + 1)] = (cS / 3.0 - dW) * ixz * isu(k - 1, l);
+            a[15 + (0 + 2) + 4 * (1 + 1)] = (cN * T(1.0 / 3.0) - dE) * ixz * isu(k, l + 1);
+            a[15 + (-1 + 2) + 4 * (1 + 1)] = (dW - cN * T(1.0 / 3.0)) * ixz * isu(k - 1, l + 1);
+            a[15 + (0 + 2) + 4 * (0 + 1)] = (dE - cS * T(1.0 / 3.0)) * ixz * isu(k, l);
+            a[15 + (-1 + 2) + 4 * (0 + 1)] = (cS * T(1.0 / 3.0) - dW) * ixz * isu(k - 1, l);
         }
 #pragma unroll
-        for (int q = 0; q < MG_NST; q++) sv[(size_t)q * nv + c3] = (T)(a[q] * celvol);
+        for (int q = 0; q < MG_NST; q++) sv[(size_t)q * nv + c3] = a[q] * celvol;
     }
 }
 
-// Coarse stencils = R A P, one thread per coarse row, FP64 accumulation in
-// shared memory (plane-major, one column per thread).  Every level of the
+// Coarse stencils = R A P, one thread per coarse row, accumulated in the
+// level's precision (FP64 throughput is a small fraction of FP32 on this
+// part) in shared memory (plane-major, one column per thread).  Every level of the
 // hierarchy follows the tag rule (u_unknown / v_unknown), so the kernel
 // reads no tags.  Each fine row's 31 coefficients are loaded in
 // one batch before use: loaded one at a time behind the zero test they
@@ -706,8 +709,8 @@ template <typename T>
 __global__ void __launch_bounds__(GAL_THREADS) k_galerkin(stokes_geom F, const T *__restrict__ suF,
                                                           const T *__restrict__ svF, stokes_geom Cg,
                                                           T *__restrict__ suC, T *__restrict__ svC, int *bad) {
-    __shared__ double acc_sh[MG_NST * GAL_THREADS];
-    double *acc = acc_sh + threadIdx.x;
+    __shared__ T acc_sh[MG_NST * GAL_THREADS];
+    T *acc = acc_sh + threadIdx.x;
 #define ACC(q) acc[(q) * GAL_THREADS]
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int Nxf = F.Nx, Nzf = F.Nz, Nxc = Cg.Nx, Nzc = Cg.Nz;
@@ -718,7 +721,7 @@ __global__ void __launch_bounds__(GAL_THREADS) k_galerkin(stokes_geom F, const T
     T a[MG_NST];
     if (t < nuc) {   // coarse u-row (K, L)
         const int K = t % Nxc, L = t / Nxc;
-        for (int q = 0; q < MG_NST; q++) ACC(q) = 0.0;
+        for (int q = 0; q < MG_NST; q++) ACC(q) = T(0);
         if (u_unknown(K, L, Nxc, Nzc)) {
             for (int lf = 2 * L - 2; lf <= 2 * L + 1; lf++) {
                 if (lf < 1 || lf > F.ncz) continue;
@@ -730,43 +733,43 @@ __global__ void __launch_bounds__(GAL_THREADS) k_galerkin(stokes_geom F, const T
                 for (int k = 2 * K - 1; k <= 2 * K + 1; k++) {
                     if (!u_unknown(k, lf, Nxf, Nzf)) continue;
                     const size_t f = (size_t)k + (size_t)lf * Nxf;
-                    const double R = (double)(nc_weight(k, K) * wz);
+                    const T R = (T)(nc_weight(k, K) * wz);
 #pragma unroll
                     for (int q = 0; q < MG_NST; q++) a[q] = __ldg(suF + (size_t)q * nuf + f);
 #pragma unroll
                     for (int q = 0; q < 15; q++) {   // uu entries of the fine row
                         if (a[q] == T(0)) continue;
                         u_parents_ij(k + q % 3 - 1, lf + q / 3 - 2, Cg.ncz, PI, PJ, pw);
-                        const double ra = R * (double)a[q];
+                        const T ra = R * a[q];
 #pragma unroll
                         for (int s = 0; s < 4; s++) {
                             if (pw[s] == 0.0f || !u_unknown(PI[s], PJ[s], Nxc, Nzc)) continue;
                             const int dK = PI[s] - K, dL = PJ[s] - L;
                             if (dK < -1 || dK > 1 || dL < -2 || dL > 2) { *bad = 1; continue; }
-                            ACC((dK + 1) + 3 * (dL + 2)) += ra * pw[s];
+                            ACC((dK + 1) + 3 * (dL + 2)) += ra * (T)pw[s];
                         }
                     }
 #pragma unroll
                     for (int q = 0; q < 16; q++) {   // uv entries of the fine row
                         if (a[15 + q] == T(0)) continue;
                         v_parents_ij(k + q % 4 - 1, lf + q / 4 - 2, Cg.ncx, PI, PJ, pw);
-                        const double ra = R * (double)a[15 + q];
+                        const T ra = R * a[15 + q];
 #pragma unroll
                         for (int s = 0; s < 4; s++) {
                             if (pw[s] == 0.0f || !v_unknown(PI[s], PJ[s], Nxc, Nzc)) continue;
                             const int dI = PI[s] - K, dJ = PJ[s] - L;
                             if (dI < -1 || dI > 2 || dJ < -2 || dJ > 1) { *bad = 1; continue; }
-                            ACC(15 + (dI + 1) + 4 * (dJ + 2)) += ra * pw[s];
+                            ACC(15 + (dI + 1) + 4 * (dJ + 2)) += ra * (T)pw[s];
                         }
                     }
                 }
             }
         }
-        for (int q = 0; q < MG_NST; q++) suC[(size_t)q * nuc + t] = (T)ACC(q);
+        for (int q = 0; q < MG_NST; q++) suC[(size_t)q * nuc + t] = ACC(q);
     }
     if (t < nvc) {   // coarse v-row (I, J)
         const int I = t % (Nxc + 1), J = t / (Nxc + 1);
-        for (int q = 0; q < MG_NST; q++) ACC(q) = 0.0;
+        for (int q = 0; q < MG_NST; q++) ACC(q) = T(0);
         if (v_unknown(I, J, Nxc, Nzc)) {
             for (int i = 2 * I - 2; i <= 2 * I + 1; i++) {
                 if (i < 1 || i > F.ncx) continue;
@@ -778,39 +781,39 @@ __global__ void __launch_bounds__(GAL_THREADS) k_galerkin(stokes_geom F, const T
                 for (int j = 2 * J - 1; j <= 2 * J + 1; j++) {
                     if (!v_unknown(i, j, Nxf, Nzf)) continue;
                     const size_t f = (size_t)i + (size_t)j * (Nxf + 1);
-                    const double R = (double)(wx * nc_weight(j, J));
+                    const T R = (T)(wx * nc_weight(j, J));
 #pragma unroll
                     for (int q = 0; q < MG_NST; q++) a[q] = __ldg(svF + (size_t)q * nvf + f);
 #pragma unroll
                     for (int q = 0; q < 15; q++) {   // vv entries
                         if (a[q] == T(0)) continue;
                         v_parents_ij(i + q % 5 - 2, j + q / 5 - 1, Cg.ncx, PI, PJ, pw);
-                        const double ra = R * (double)a[q];
+                        const T ra = R * a[q];
 #pragma unroll
                         for (int s = 0; s < 4; s++) {
                             if (pw[s] == 0.0f || !v_unknown(PI[s], PJ[s], Nxc, Nzc)) continue;
                             const int dI = PI[s] - I, dJ = PJ[s] - J;
                             if (dI < -2 || dI > 2 || dJ < -1 || dJ > 1) { *bad = 1; continue; }
-                            ACC((dI + 2) + 5 * (dJ + 1)) += ra * pw[s];
+                            ACC((dI + 2) + 5 * (dJ + 1)) += ra * (T)pw[s];
                         }
                     }
 #pragma unroll
                     for (int q = 0; q < 16; q++) {   // vu entries
                         if (a[15 + q] == T(0)) continue;
                         u_parents_ij(i + q % 4 - 2, j + q / 4 - 1, Cg.ncz, PI, PJ, pw);
-                        const double ra = R * (double)a[15 + q];
+                        const T ra = R * a[15 + q];
 #pragma unroll
                         for (int s = 0; s < 4; s++) {
                             if (pw[s] == 0.0f || !u_unknown(PI[s], PJ[s], Nxc, Nzc)) continue;
                             const int dK = PI[s] - I, dL = PJ[s] - J;
                             if (dK < -2 || dK > 1 || dL < -1 || dL > 2) { *bad = 1; continue; }
-                            ACC(15 + (dK + 2) + 4 * (dL + 1)) += ra * pw[s];
+                            ACC(15 + (dK + 2) + 4 * (dL + 1)) += ra * (T)pw[s];
                         }
                     }
                 }
             }
         }
-        for (int q = 0; q < MG_NST; q++) svC[(size_t)q * nvc + t] = (T)ACC(q);
+        for (int q = 0; q < MG_NST; q++) svC[(size_t)q * nvc + t] = ACC(q);
     }
 #undef ACC
 }
