@@ -161,11 +161,13 @@ def mlp_workload():
 
 
 def e2e_form(cfg_builder, precision, learned, steps, size):
-    """Same step through the public API with host buffers: markers, attributes
-    and initial fields uploaded from host memory every step, the solution and
-    the marker state read back.  The host arrays are page-locked once with
-    host_register (as a caller would register its marker arrays), so the
-    copies inside the timed region are DMA transfers."""
+    """Same step through the public API with the marker state owned by the
+    host, as in the reference's time loop: every step uploads the markers
+    (positions, phases, the seven attributes), runs the step and downloads the
+    advected markers, their velocities, the updated attributes and the grid
+    velocity into the same host arrays, which the next step uploads again.
+    The host arrays are page-locked once with host_register (as a caller
+    would register its marker arrays), so the copies are DMA transfers."""
     import numpy as np
     import mdz
     import mdz_setups
@@ -184,10 +186,10 @@ def e2e_form(cfg_builder, precision, learned, steps, size):
            "phase": np.ascontiguousarray(m["phase"], np.int32)}
     for _, key in attrs:
         hin[key] = np.ascontiguousarray(m[key], np.float64)
-    hout = [np.empty(n), np.empty(n), np.empty(n, np.int32), np.empty(n), np.empty(n)]
-    hsxx = np.empty(n)
+    hvx, hvz = np.empty(n), np.empty(n)
+    hout = [hin["x"], hin["z"], hin["phase"], hvx, hvz]
     hu = np.empty(g.size(-1))
-    pinned = list(hin.values()) + hout + [hsxx, hu]
+    pinned = list(hin.values()) + [hvx, hvz, hu]
     for a in pinned:
         mdz.host_register(a)
     times, parts = [], [0.0, 0.0, 0.0, 0.0]
@@ -200,7 +202,8 @@ def e2e_form(cfg_builder, precision, learned, steps, size):
         rep = ctx.time_step(mat, model)
         t2 = time.perf_counter()
         ctx.get_markers(out=hout)
-        ctx.get_marker_attr(mdz.M_SXXD, out=hsxx)
+        for attr, key in attrs:
+            ctx.get_marker_attr(attr, out=hin[key])
         ctx.L.mdz_get_velocity(ctx.h, mdz._dptr(hu), None, None)
         t3 = time.perf_counter()
         times.append((t3 - t0) * 1e3)
@@ -209,7 +212,7 @@ def e2e_form(cfg_builder, precision, learned, steps, size):
     for a in pinned:
         mdz.host_unregister(a)
     h2d = n * (8 * 2 + 4) + n * 8 * len(attrs)
-    d2h = n * (8 * 4 + 4) + n * 8 + g.size(-1) * 8
+    d2h = n * (8 * 4 + 4) + n * 8 * len(attrs) + g.size(-1) * 8
     ctx.close()
     split = dict(zip(("upload_ms", "step_ms", "download_ms", "step_device_ms"), parts))
     return sum(times) / len(times), h2d, d2h, split
