@@ -22,6 +22,7 @@
 #include <cstdio>
 #include <cstring>
 #include <vector>
+#include <cooperative_groups.h>
 #include "stokes.cuh"
 #include "solver.cuh"
 
@@ -94,6 +95,7 @@ struct mdz_solver {
     int check = 4;               // GCR iterations between host convergence checks
     int restart = 30;            // GCR basis size
     int mg_jacobian = 0;         // 1: multigrid on the Newton Jacobian's velocity block (else Picard)
+    int bottom_cs[2] = {1, 1};   // cluster size of the V-cycle bottom kernel ([0] FP64, [1] FP32)
     // preconditioner application captured as a CUDA graph, per precision
     // ([0] FP64, [1] FP32): one graph launch per Krylov iteration
     // [precision (0 FP64, 1 FP32) * 2 + newton]
@@ -1029,16 +1031,17 @@ __global__ void __launch_bounds__(256) k_coarse_dense_solve(int n, int nu, int n
 
 
 // ---------------------------------------------------------------------------
-// Bottom of the V-cycle in one CTA.  The small levels (a few thousand points
-// each) cost one launch per sweep, residual and transfer when run as grid
-// kernels, and each such launch is a few microseconds of latency for a few
-// hundred rows of work; here the whole descent from level `first` to the
-// dense coarsest level and the ascent back run in one 1024-thread block with
-// a barrier between phases.  Same arithmetic as the grid kernels (the same
-// point functions), so the result is identical.  The level's result ends in
-// its xu / xv buffers like the grid path's.
+// Bottom of the V-cycle in one thread-block cluster.  The small levels (a few
+// thousand points each) cost one launch per sweep, residual and transfer when
+// run as grid kernels, and each such launch is several microseconds of
+// latency for little work; here the whole descent from level `first` to the
+// dense coarsest level and the ascent back run in one launch of one cluster
+// (up to 16 CTAs of 1024 threads on 16 SMs; a single CTA where clusters are
+// not available), with a cluster barrier between phases.  Same arithmetic
+// as the grid kernels (the same point functions), so the result is
+// identical.  The first level's result ends in its xu / xv buffers like the
+// grid path's.
 #define MG_BOTTOM_MAX 6
-#define MG_BOTTOM_POINTS 4096
 #define MG_BOTTOM_THREADS 1024
 template <typename T>
 struct mg_bottom_level {
@@ -1056,12 +1059,21 @@ struct mg_bottom_args {
     mg_bottom_level<T> L[MG_BOTTOM_MAX];
 };
 
+// points a bottom launch of `cs` CTAs takes on per level
+static inline long long mg_bottom_points(int cs) { return (long long)cs * MG_BOTTOM_THREADS * (cs == 1 ? 4 : 2); }
+
 template <typename T>
 __global__ void __launch_bounds__(MG_BOTTOM_THREADS) k_mg_bottom(const __grid_constant__ mg_bottom_args<T> A) {
     __shared__ T fs[MG_DENSE_MAX];
     T *xu[MG_BOTTOM_MAX], *xv[MG_BOTTOM_MAX], *yu[MG_BOTTOM_MAX], *yv[MG_BOTTOM_MAX];
     for (int l = 0; l < A.nlev; l++) { xu[l] = A.L[l].xu; xv[l] = A.L[l].xv; yu[l] = A.L[l].yu; yv[l] = A.L[l].yv; }
-    const int tid = threadIdx.x;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
+    // barrier over every thread of the launch: the grid is one cluster (or one CTA);
+    // release / acquire at cluster scope orders the global-memory phases
+    auto bar = [&]() {
+        if (gridDim.x > 1) cooperative_groups::this_cluster().sync();
+        else __syncthreads();
+    };
     auto swap_xy = [&](int l) {
         T *t = xu[l]; xu[l] = yu[l]; yu[l] = t;
         t = xv[l]; xv[l] = yv[l]; yv[l] = t;
@@ -1069,66 +1081,93 @@ __global__ void __launch_bounds__(MG_BOTTOM_THREADS) k_mg_bottom(const __grid_co
     for (int l = 0; l < A.nlev - 1; l++) {   // descent
         const mg_bottom_level<T> &L = A.L[l];
         const int W = L.G.Nx + 1, npt = W * (L.G.Nz + 1);
-        for (int p = tid; p < npt; p += blockDim.x)
+        for (int p = tid; p < npt; p += nthr)
             st_smooth_pt<T>(L.G, L.su, L.sv, nullptr, nullptr, L.fu, L.fv, L.idu, L.idv, A.omega, xu[l], xv[l],
                             p % W, p / W);
-        __syncthreads();
+        bar();
         for (int s = 1; s < A.nu1; s++) {
-            for (int p = tid; p < npt; p += blockDim.x)
+            for (int p = tid; p < npt; p += nthr)
                 st_smooth_pt<T>(L.G, L.su, L.sv, xu[l], xv[l], L.fu, L.fv, L.idu, L.idv, A.omega, yu[l], yv[l],
                                 p % W, p / W);
-            __syncthreads();
+            bar();
             swap_xy(l);
         }
-        for (int p = tid; p < npt; p += blockDim.x)
+        for (int p = tid; p < npt; p += nthr)
             st_residual_pt<T>(L.G, L.su, L.sv, xu[l], xv[l], L.fu, L.fv, L.ru, L.rv, p % W, p / W);
-        __syncthreads();
+        bar();
         const mg_bottom_level<T> &C = A.L[l + 1];
         const int Wc = C.G.Nx + 1, nptc = Wc * (C.G.Nz + 1);
-        for (int p = tid; p < nptc; p += blockDim.x)
+        for (int p = tid; p < nptc; p += nthr)
             mg_restrict_pt<T>(L.G, C.G, L.ru, L.rv, C.fu, C.fv, p % Wc, p / Wc);
-        __syncthreads();
+        bar();
     }
-    {   // dense coarsest: x = A^-1 f (zero outside the unknowns)
+    {   // dense coarsest: x = A^-1 f (zero outside the unknowns); every CTA
+        // gathers f into its own shared memory
         const int lc = A.nlev - 1, n = A.ndense;
         const mg_bottom_level<T> &C = A.L[lc];
         const int nu = C.G.Nx * (C.G.Nz + 1), nv = (C.G.Nx + 1) * C.G.Nz;
-        for (int i = tid; i < n; i += blockDim.x) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
             const int m = A.dmap[i];
             fs[i] = m < nu ? C.fu[m] : C.fv[m - nu];
         }
-        for (int i = tid; i < nu; i += blockDim.x) xu[lc][i] = T(0);
-        for (int i = tid; i < nv; i += blockDim.x) xv[lc][i] = T(0);
-        __syncthreads();
-        for (int r = tid; r < n; r += blockDim.x) {
+        for (int i = tid; i < nu; i += nthr) xu[lc][i] = T(0);
+        for (int i = tid; i < nv; i += nthr) xv[lc][i] = T(0);
+        bar();
+        for (int r = tid; r < n; r += nthr) {
             T s = 0;
             for (int j = 0; j < n; j++) s += A.AinvT[(size_t)j * n + r] * fs[j];
             const int m = A.dmap[r];
             if (m < nu) xu[lc][m] = s; else xv[lc][m - nu] = s;
         }
-        __syncthreads();
+        bar();
     }
     for (int l = A.nlev - 2; l >= 0; l--) {   // ascent
         const mg_bottom_level<T> &L = A.L[l];
         const mg_bottom_level<T> &C = A.L[l + 1];
         const int W = L.G.Nx + 1, npt = W * (L.G.Nz + 1);
-        for (int p = tid; p < npt; p += blockDim.x)
+        for (int p = tid; p < npt; p += nthr)
             mg_prolong_pt<T>(L.G, C.G, xu[l + 1], xv[l + 1], xu[l], xv[l], p % W, p / W);
-        __syncthreads();
+        bar();
         for (int s = 0; s < A.nu2; s++) {
-            for (int p = tid; p < npt; p += blockDim.x)
+            for (int p = tid; p < npt; p += nthr)
                 st_smooth_pt<T>(L.G, L.su, L.sv, xu[l], xv[l], L.fu, L.fv, L.idu, L.idv, A.omega, yu[l], yv[l],
                                 p % W, p / W);
-            __syncthreads();
+            bar();
             swap_xy(l);
         }
     }
     if (xu[0] != A.L[0].xu) {   // odd number of swaps on the first level: copy back
         const mg_bottom_level<T> &L = A.L[0];
         const int nu = L.G.Nx * (L.G.Nz + 1), nv = (L.G.Nx + 1) * L.G.Nz;
-        for (int i = tid; i < nu; i += blockDim.x) L.xu[i] = xu[0][i];
-        for (int i = tid; i < nv; i += blockDim.x) L.xv[i] = xv[0][i];
+        for (int i = tid; i < nu; i += nthr) L.xu[i] = xu[0][i];
+        for (int i = tid; i < nv; i += nthr) L.xv[i] = xv[0][i];
     }
+}
+
+// Largest cluster (16, 8 or 4 CTAs of 1024 threads) the device can place for
+// the bottom kernel, else 1 (a single CTA).
+template <typename T>
+static int mg_bottom_cluster_size() {
+    if (cudaFuncSetAttribute(k_mg_bottom<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+        cudaGetLastError();
+    const int sizes[3] = {16, 8, 4};
+    for (int q = 0; q < 3; q++) {
+        const int cs = sizes[q];
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(cs);
+        cfg.blockDim = dim3(MG_BOTTOM_THREADS);
+        cudaLaunchAttribute at;
+        at.id = cudaLaunchAttributeClusterDimension;
+        at.val.clusterDim.x = cs;
+        at.val.clusterDim.y = 1;
+        at.val.clusterDim.z = 1;
+        cfg.attrs = &at;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, k_mg_bottom<T>, &cfg) == cudaSuccess && n >= 1) return cs;
+        cudaGetLastError();
+    }
+    return 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -1274,6 +1313,8 @@ mdz_status mdz_solver_ensure(mdz_ctx *ctx) {
     if ((s = alloc_gcr<float>(ctx, S->g32, S->restart)) != MDZ_OK) return s;
     MDZ_CUDA(ctx, cudaMallocHost((void **)&S->sc, 64 * sizeof(double)));
     memset(S->sc, 0, 64 * sizeof(double));
+    S->bottom_cs[0] = mg_bottom_cluster_size<double>();
+    S->bottom_cs[1] = mg_bottom_cluster_size<float>();
     MDZ_CUDA(ctx, cudaDeviceSynchronize());
     S->ready = true;
     return MDZ_OK;
@@ -1451,8 +1492,9 @@ static mdz_status vcycle(mdz_ctx *ctx, mg_hier<T> &H, int l, int nu1, int nu2, T
     }
     const bool viscous = l == 0 && !H.newton;   // level 0 of a Picard hierarchy: stencil from eta directly
     const mg_level<T> &Cd = H.L[H.nlev - 1];
+    const int cs = ctx->solver->bottom_cs[sizeof(T) == 8 ? 0 : 1];
     if (!viscous && Cd.ndense && H.nlev - l <= MG_BOTTOM_MAX &&
-        (long long)(L.Nx + 1) * (L.Nz + 1) <= MG_BOTTOM_POINTS) {   // this level and all below in one CTA
+        (long long)(L.Nx + 1) * (L.Nz + 1) <= mg_bottom_points(cs)) {   // this level and all below in one launch
         mg_bottom_args<T> A;
         A.nlev = H.nlev - l; A.nu1 = nu1; A.nu2 = nu2; A.ndense = Cd.ndense; A.omega = omega;
         A.dmap = Cd.dmap; A.AinvT = Cd.AinvT;
@@ -1461,7 +1503,22 @@ static mdz_status vcycle(mdz_ctx *ctx, mg_hier<T> &H, int l, int nu1, int nu2, T
             A.L[q] = mg_bottom_level<T>{B.geom(), B.su, B.sv, B.idu, B.idv, B.xu, B.xv, B.yu, B.yv,
                                         B.fu, B.fv, B.ru, B.rv};
         }
-        k_mg_bottom<T><<<1, MG_BOTTOM_THREADS, 0, st>>>(A);
+        if (cs > 1) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(cs);
+            cfg.blockDim = dim3(MG_BOTTOM_THREADS);
+            cfg.stream = st;
+            cudaLaunchAttribute at;
+            at.id = cudaLaunchAttributeClusterDimension;
+            at.val.clusterDim.x = cs;
+            at.val.clusterDim.y = 1;
+            at.val.clusterDim.z = 1;
+            cfg.attrs = &at;
+            cfg.numAttrs = 1;
+            MDZ_CUDA(ctx, cudaLaunchKernelEx(&cfg, k_mg_bottom<T>, A));
+        } else {
+            k_mg_bottom<T><<<1, MG_BOTTOM_THREADS, 0, st>>>(A);
+        }
         MDZ_LAUNCHED(ctx);
         return MDZ_OK;
     }
