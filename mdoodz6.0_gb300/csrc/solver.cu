@@ -428,44 +428,79 @@ __device__ __forceinline__ T st_vrow(int Nx, int Nz, const T *__restrict__ sv, s
     return s;
 }
 
-// out = x + omega D^-1 (f - A x) on a stencil level at point (i, j)
-// (x == nullptr: x = 0)
+// out = x + omega D^-1 (f - A x) on a stencil level, one u-row (i, j) or
+// v-row (i, j) (x == nullptr: x = 0)
+template <typename T>
+__device__ __forceinline__ void st_smooth_u(const stokes_geom &G, const T *__restrict__ su, const T *__restrict__ sv,
+                                            const T *__restrict__ xu, const T *__restrict__ xv,
+                                            const T *__restrict__ fu, const T *__restrict__ idu, T omega,
+                                            T *__restrict__ ou, int i, int j) {
+    const int Nx = G.Nx, Nz = G.Nz;
+    const size_t nu = (size_t)Nx * (Nz + 1);
+    const int c = i + j * Nx;
+    T r = 0;
+    if (u_unknown(i, j, Nx, Nz)) {
+        if (xu) r = xu[c] + omega * idu[c] * (fu[c] - st_urow<T>(Nx, Nz, su, nu, xu, xv, i, j));
+        else r = omega * idu[c] * fu[c];
+    }
+    ou[c] = r;
+}
+
+template <typename T>
+__device__ __forceinline__ void st_smooth_v(const stokes_geom &G, const T *__restrict__ su, const T *__restrict__ sv,
+                                            const T *__restrict__ xu, const T *__restrict__ xv,
+                                            const T *__restrict__ fv, const T *__restrict__ idv, T omega,
+                                            T *__restrict__ ov, int i, int j) {
+    const int Nx = G.Nx, Nz = G.Nz;
+    const size_t nv = (size_t)(Nx + 1) * Nz;
+    const int c = i + j * (Nx + 1);
+    T r = 0;
+    if (v_unknown(i, j, Nx, Nz)) {
+        if (xv) r = xv[c] + omega * idv[c] * (fv[c] - st_vrow<T>(Nx, Nz, sv, nv, xu, xv, i, j));
+        else r = omega * idv[c] * fv[c];
+    }
+    ov[c] = r;
+}
+
+// both rows at point (i, j) of the (Nx+1) x (Nz+1) box
 template <typename T>
 __device__ __forceinline__ void st_smooth_pt(const stokes_geom &G, const T *__restrict__ su, const T *__restrict__ sv,
                                              const T *__restrict__ xu, const T *__restrict__ xv,
                                              const T *__restrict__ fu, const T *__restrict__ fv,
                                              const T *__restrict__ idu, const T *__restrict__ idv, T omega,
                                              T *__restrict__ ou, T *__restrict__ ov, int i, int j) {
-    const int Nx = G.Nx, Nz = G.Nz;
-    const size_t nu = (size_t)Nx * (Nz + 1), nv = (size_t)(Nx + 1) * Nz;
-    if (i < Nx && j <= Nz) {
-        int c = i + j * Nx;
-        T r = 0;
-        if (u_unknown(i, j, Nx, Nz)) {
-            if (xu) r = xu[c] + omega * idu[c] * (fu[c] - st_urow<T>(Nx, Nz, su, nu, xu, xv, i, j));
-            else r = omega * idu[c] * fu[c];
-        }
-        ou[c] = r;
-    }
-    if (i <= Nx && j < Nz) {
-        int c = i + j * (Nx + 1);
-        T r = 0;
-        if (v_unknown(i, j, Nx, Nz)) {
-            if (xv) r = xv[c] + omega * idv[c] * (fv[c] - st_vrow<T>(Nx, Nz, sv, nv, xu, xv, i, j));
-            else r = omega * idv[c] * fv[c];
-        }
-        ov[c] = r;
-    }
+    if (i < G.Nx && j <= G.Nz) st_smooth_u<T>(G, su, sv, xu, xv, fu, idu, omega, ou, i, j);
+    if (i <= G.Nx && j < G.Nz) st_smooth_v<T>(G, su, sv, xu, xv, fv, idv, omega, ov, i, j);
 }
 
+// one thread per row (u rows first, then v rows): twice the threads of a
+// point-per-thread launch, so that the fine stencil levels fill the machine
 template <typename T>
-__global__ void __launch_bounds__(256) k_st_smooth(stokes_geom G, const T *__restrict__ su, const T *__restrict__ sv,
+__global__ void __launch_bounds__(128) k_st_smooth(stokes_geom G, const T *__restrict__ su, const T *__restrict__ sv,
                                                    const T *__restrict__ xu, const T *__restrict__ xv,
                                                    const T *__restrict__ fu, const T *__restrict__ fv,
                                                    const T *__restrict__ idu, const T *__restrict__ idv, T omega,
                                                    T *__restrict__ ou, T *__restrict__ ov) {
-    st_smooth_pt<T>(G, su, sv, xu, xv, fu, fv, idu, idv, omega, ou, ov, blockIdx.x * blockDim.x + threadIdx.x,
-                    blockIdx.y * blockDim.y + threadIdx.y);
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int Nx = G.Nx, nu = Nx * (G.Nz + 1), nv = (Nx + 1) * G.Nz;
+    if (t < nu) st_smooth_u<T>(G, su, sv, xu, xv, fu, idu, omega, ou, t % Nx, t / Nx);
+    else if (t < nu + nv) st_smooth_v<T>(G, su, sv, xu, xv, fv, idv, omega, ov, (t - nu) % (Nx + 1), (t - nu) / (Nx + 1));
+}
+
+template <typename T>
+__device__ __forceinline__ void st_residual_u(const stokes_geom &G, const T *__restrict__ su, const T *__restrict__ xu,
+                                              const T *__restrict__ xv, const T *__restrict__ fu, T *__restrict__ ru,
+                                              int i, int j) {
+    const int Nx = G.Nx, Nz = G.Nz, c = i + j * Nx;
+    ru[c] = u_unknown(i, j, Nx, Nz) ? fu[c] - st_urow<T>(Nx, Nz, su, (size_t)Nx * (Nz + 1), xu, xv, i, j) : T(0);
+}
+
+template <typename T>
+__device__ __forceinline__ void st_residual_v(const stokes_geom &G, const T *__restrict__ sv, const T *__restrict__ xu,
+                                              const T *__restrict__ xv, const T *__restrict__ fv, T *__restrict__ rv,
+                                              int i, int j) {
+    const int Nx = G.Nx, Nz = G.Nz, c = i + j * (Nx + 1);
+    rv[c] = v_unknown(i, j, Nx, Nz) ? fv[c] - st_vrow<T>(Nx, Nz, sv, (size_t)(Nx + 1) * Nz, xu, xv, i, j) : T(0);
 }
 
 template <typename T>
@@ -474,26 +509,20 @@ __device__ __forceinline__ void st_residual_pt(const stokes_geom &G, const T *__
                                                const T *__restrict__ xv, const T *__restrict__ fu,
                                                const T *__restrict__ fv, T *__restrict__ ru, T *__restrict__ rv,
                                                int i, int j) {
-    const int Nx = G.Nx, Nz = G.Nz;
-    const size_t nu = (size_t)Nx * (Nz + 1), nv = (size_t)(Nx + 1) * Nz;
-    if (i < Nx && j <= Nz) {
-        int c = i + j * Nx;
-        ru[c] = u_unknown(i, j, Nx, Nz) ? fu[c] - st_urow<T>(Nx, Nz, su, nu, xu, xv, i, j) : T(0);
-    }
-    if (i <= Nx && j < Nz) {
-        int c = i + j * (Nx + 1);
-        rv[c] = v_unknown(i, j, Nx, Nz) ? fv[c] - st_vrow<T>(Nx, Nz, sv, nv, xu, xv, i, j) : T(0);
-    }
+    if (i < G.Nx && j <= G.Nz) st_residual_u<T>(G, su, xu, xv, fu, ru, i, j);
+    if (i <= G.Nx && j < G.Nz) st_residual_v<T>(G, sv, xu, xv, fv, rv, i, j);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_st_residual(stokes_geom G, const T *__restrict__ su,
+__global__ void __launch_bounds__(128) k_st_residual(stokes_geom G, const T *__restrict__ su,
                                                      const T *__restrict__ sv, const T *__restrict__ xu,
                                                      const T *__restrict__ xv, const T *__restrict__ fu,
                                                      const T *__restrict__ fv, T *__restrict__ ru,
                                                      T *__restrict__ rv) {
-    st_residual_pt<T>(G, su, sv, xu, xv, fu, fv, ru, rv, blockIdx.x * blockDim.x + threadIdx.x,
-                      blockIdx.y * blockDim.y + threadIdx.y);
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int Nx = G.Nx, nu = Nx * (G.Nz + 1), nv = (Nx + 1) * G.Nz;
+    if (t < nu) st_residual_u<T>(G, su, xu, xv, fu, ru, t % Nx, t / Nx);
+    else if (t < nu + nv) st_residual_v<T>(G, sv, xu, xv, fv, rv, (t - nu) % (Nx + 1), (t - nu) / (Nx + 1));
 }
 
 template <typename T>
@@ -1522,9 +1551,10 @@ static mdz_status vcycle(mdz_ctx *ctx, mg_hier<T> &H, int l, int nu1, int nu2, T
         MDZ_LAUNCHED(ctx);
         return MDZ_OK;
     }
+    const int rows_grid = mdz_blocks(L.nu() + L.nv(), 128);
     auto smooth = [&](const T *xu, const T *xv, T *ou, T *ov) {
         if (viscous) k_mg_smooth<T><<<gr, bl, 0, st>>>(G, D, xu, xv, L.fu, L.fv, L.idu, L.idv, omega, ou, ov);
-        else k_st_smooth<T><<<gr, bl, 0, st>>>(G, L.su, L.sv, xu, xv, L.fu, L.fv, L.idu, L.idv, omega, ou, ov);
+        else k_st_smooth<T><<<rows_grid, 128, 0, st>>>(G, L.su, L.sv, xu, xv, L.fu, L.fv, L.idu, L.idv, omega, ou, ov);
     };
     // pre-smoothing from x = 0
     smooth(nullptr, nullptr, L.xu, L.xv);
@@ -1535,7 +1565,7 @@ static mdz_status vcycle(mdz_ctx *ctx, mg_hier<T> &H, int l, int nu1, int nu2, T
         std::swap(L.xu, L.yu); std::swap(L.xv, L.yv);
     }
     if (viscous) k_mg_residual<T><<<gr, bl, 0, st>>>(G, D, L.xu, L.xv, L.fu, L.fv, L.ru, L.rv);
-    else k_st_residual<T><<<gr, bl, 0, st>>>(G, L.su, L.sv, L.xu, L.xv, L.fu, L.fv, L.ru, L.rv);
+    else k_st_residual<T><<<rows_grid, 128, 0, st>>>(G, L.su, L.sv, L.xu, L.xv, L.fu, L.fv, L.ru, L.rv);
     MDZ_LAUNCHED(ctx);
     mg_level<T> &C = H.L[l + 1];
     k_mg_restrict<T><<<box_grid(C.Nx, C.Nz), bl, 0, st>>>(G, C.geom(), L.ru, L.rv, C.fu, C.fv);
