@@ -192,7 +192,7 @@ def e2e_form(cfg_builder, precision, learned, steps, size):
     pinned = list(hin.values()) + [hvx, hvz, hu]
     for a in pinned:
         mdz.host_register(a)
-    times, parts = [], [0.0, 0.0, 0.0, 0.0]
+    times, parts, reps = [], [0.0, 0.0, 0.0, 0.0], []
     for _ in range(steps):
         t0 = time.perf_counter()
         ctx.set_markers(hin["x"], hin["z"], hin["phase"])
@@ -201,6 +201,8 @@ def e2e_form(cfg_builder, precision, learned, steps, size):
         t1 = time.perf_counter()
         rep = ctx.time_step(mat, model)
         t2 = time.perf_counter()
+        reps.append({k: rep.as_dict()[k] for k in ("nonlinear_its", "linear_its", "ms_solve", "ms_rheology",
+                                                    "ms_total")})
         ctx.get_markers(out=hout)
         for attr, key in attrs:
             ctx.get_marker_attr(attr, out=hin[key])
@@ -215,6 +217,7 @@ def e2e_form(cfg_builder, precision, learned, steps, size):
     d2h = n * (8 * 4 + 4) + n * 8 * len(attrs) + g.size(-1) * 8
     ctx.close()
     split = dict(zip(("upload_ms", "step_ms", "download_ms", "step_device_ms"), parts))
+    split["reports"] = reps
     return sum(times) / len(times), h2d, d2h, split
 
 
