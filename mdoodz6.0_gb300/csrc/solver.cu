@@ -1676,27 +1676,15 @@ static mdz_status precondition(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n,
 
 // ---------------------------------------------------------------------------
 // GCR kernels (vectors are u|v|p contiguous of length n).
-template <typename T>
-__global__ void k_gcr_orth(size_t n, int k, const T *__restrict__ Z, const T *__restrict__ W,
-                           const double *__restrict__ beta, T *__restrict__ z, T *__restrict__ w) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    double zs = z[i], ws = w[i];
-    for (int q = 0; q < k; q++) {
-        double b = beta[q];
-        zs -= b * (double)Z[q * n + i];
-        ws -= b * (double)W[q * n + i];
-    }
-    z[i] = (T)zs;
-    w[i] = (T)ws;
-}
-
-// second Gram-Schmidt pass, normalisation, store into slot k, update x and r.
-// dots[0..k-1] = (w, W_q), dots[k] = (w, w), dots[k+1] = (w, r).
-// sc[0] = 1/||w||, sc[1] = alpha, sc[2] = ||w||^2, sc[3] = running ||r||^2
-// (updated here so the host reads it only every few iterations).
-__global__ void k_gcr_scalars(int k, double *dots, double *sc) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// Orthogonalisation: classical Gram-Schmidt, with a second pass only where
+// the first lost more than half of w's squared norm (the DGKS criterion),
+// decided on the device: k_gcr_check sets sc[5] = 1 for a second pass, and
+// the second-pass kernels return at once when it is 0.
+// dots[0..k-1] = (w, W_q), dots[k] = (w, w), dots[k+1] = (w, r) of the pass
+// whose coefficients the finish applies; sc[0] = 1/||w||, sc[1] = alpha,
+// sc[2] = ||w||^2, sc[3] = running ||r||^2 (so the host reads it only every
+// few iterations).
+__device__ void gcr_scalars(int k, const double *dots, double *sc) {
     double nrm2 = dots[k], wr = dots[k + 1];
     for (int q = 0; q < k; q++) nrm2 -= dots[q] * dots[q];
     double nrm = sqrt(nrm2 > 0 ? nrm2 : 0.0);
@@ -1707,16 +1695,50 @@ __global__ void k_gcr_scalars(int k, double *dots, double *sc) {
     sc[3] -= alpha * alpha;
 }
 
+__global__ void k_gcr_check(int k, const double *dots, double *sc) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double nrm2 = dots[k];
+    for (int q = 0; q < k; q++) nrm2 -= dots[q] * dots[q];
+    if (k > 0 && !(nrm2 > 0.5 * dots[k])) { sc[5] = 1.0; return; }
+    sc[5] = 0.0;
+    gcr_scalars(k, dots, sc);
+}
+
+__global__ void k_gcr_scalars2(int k, const double *dots2, double *sc) {
+    if (threadIdx.x != 0 || blockIdx.x != 0 || sc[5] == 0.0) return;
+    gcr_scalars(k, dots2, sc);
+}
+
+// first-pass correction z -= sum beta_q Z_q, w -= sum beta_q W_q, only when
+// sc[5] asks for a second pass (grid-stride, so a skipped launch is short)
+template <typename T>
+__global__ void k_gcr_orth_if(size_t n, int k, const T *__restrict__ Z, const T *__restrict__ W,
+                              const double *__restrict__ beta, const double *__restrict__ sc, T *__restrict__ z,
+                              T *__restrict__ w) {
+    if (sc[5] == 0.0) return;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        double zs = z[i], ws = w[i];
+        for (int q = 0; q < k; q++) {
+            double b = beta[q];
+            zs -= b * (double)Z[q * n + i];
+            ws -= b * (double)W[q * n + i];
+        }
+        z[i] = (T)zs;
+        w[i] = (T)ws;
+    }
+}
+
 __global__ void k_set_scalar(double *dst, const double *src) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *dst = *src;
 }
 
 template <typename T>
-__global__ void k_gcr_finish(size_t n, int k, T *__restrict__ Z, T *__restrict__ W, const double *__restrict__ beta,
-                             const double *__restrict__ sc, const T *__restrict__ z, const T *__restrict__ w,
-                             T *__restrict__ x, T *__restrict__ r) {
+__global__ void k_gcr_finish(size_t n, int k, T *__restrict__ Z, T *__restrict__ W, const double *__restrict__ dots1,
+                             const double *__restrict__ dots2, const double *__restrict__ sc,
+                             const T *__restrict__ z, const T *__restrict__ w, T *__restrict__ x, T *__restrict__ r) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const double *__restrict__ beta = sc[5] != 0.0 ? dots2 : dots1;
     double zs = z[i], ws = w[i];
     for (int q = 0; q < k; q++) {
         double b = beta[q];
@@ -1764,11 +1786,11 @@ static mdz_status remove_pressure_mean(mdz_ctx *ctx, double *p, cudaStream_t st)
 
 template <typename T>
 static mdz_status dots_launch(mdz_ctx *ctx, gcr_space<T> &S, int q0, int nq, const T *b, double *out,
-                              cudaStream_t st) {
+                              cudaStream_t st, const double *flag = nullptr) {
     if (nq <= 0) return MDZ_OK;
     MDZ_CUDA(ctx, cudaMemsetAsync(out, 0, sizeof(double) * nq, st));
     multidot_launch<T>(nq, (int)S.nu, (int)S.nv, (int)S.np, S.dA0 + q0, S.dA1 + q0, S.dA2 + q0, b, b + S.nu,
-                       b + S.nu + S.nv, out, st);
+                       b + S.nu + S.nv, out, st, flag);
     MDZ_LAUNCHED(ctx);
     return MDZ_OK;
 }
@@ -1845,7 +1867,7 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
     int nb = mdz_blocks(n);
     MDZ_CUDA(ctx, cudaMemsetAsync(S.x, 0, sizeof(T) * n, st));
     // ||r0||
-    double *dots = S.dots, *sc = S.dots + (GCR_MAX_M + 4);
+    double *dots = S.dots, *sc = S.dots + (GCR_MAX_M + 4), *dots2 = S.dots + 2 * (GCR_MAX_M + 8);
     mdz_status s;
     cudaGraphExec_t pre = nullptr;
     long long pre_launches = 0;
@@ -1892,23 +1914,27 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
             k_widen2<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, SP.z, SP.w, S.z, S.w);
             MDZ_LAUNCHED(ctx);
         }
-        if (k > 0) {   // first Gram-Schmidt pass
-            if ((s = dots_launch<T>(ctx, S, 0, k, S.w, dots, st)) != MDZ_OK) return s;
-            k_gcr_orth<T><<<nb, MDZ_THREADS, 0, st>>>(n, k, S.Z, S.W, dots, S.z, S.w);
-            MDZ_LAUNCHED(ctx);
-        }
-        // second pass dots: (w, W_q) q<k, (w, w), (w, r)
+        // first pass: (w, W_q) q < k, (w, w), (w, r); the check decides on the
+        // device whether a second pass runs
         if ((s = dots_launch<T>(ctx, S, 0, k, S.w, dots, st)) != MDZ_OK) return s;
         if ((s = dots_launch<T>(ctx, S, S.m, 2, S.w, dots + k, st)) != MDZ_OK) return s;
-        k_gcr_scalars<<<1, 32, 0, st>>>(k, dots, sc);
+        k_gcr_check<<<1, 32, 0, st>>>(k, dots, sc);
         MDZ_LAUNCHED(ctx);
-        k_gcr_finish<T><<<nb, MDZ_THREADS, 0, st>>>(n, k, S.Z, S.W, dots, sc, S.z, S.w, S.x, S.r);
+        if (k > 0) {   // second pass (each launch returns at once unless sc[5] = 1)
+            const int ng = nb < 152 * 8 ? nb : 152 * 8;
+            k_gcr_orth_if<T><<<ng, MDZ_THREADS, 0, st>>>(n, k, S.Z, S.W, dots, sc, S.z, S.w);
+            MDZ_LAUNCHED(ctx);
+            if ((s = dots_launch<T>(ctx, S, 0, k, S.w, dots2, st, sc + 5)) != MDZ_OK) return s;
+            if ((s = dots_launch<T>(ctx, S, S.m, 2, S.w, dots2 + k, st, sc + 5)) != MDZ_OK) return s;
+            k_gcr_scalars2<<<1, 32, 0, st>>>(k, dots2, sc);
+            MDZ_LAUNCHED(ctx);
+        }
+        k_gcr_finish<T><<<nb, MDZ_THREADS, 0, st>>>(n, k, S.Z, S.W, dots, dots2, sc, S.z, S.w, S.x, S.r);
         MDZ_LAUNCHED(ctx);
-        {   // algorithmic bytes: widening (2 P reads, 2 T writes); the two
-            // Gram-Schmidt passes read W_q and w (k + 1 each) plus (w, w),
-            // (w, r); the orthogonalisation reads Z_q, W_q, z, w and writes
-            // z, w; the finish reads Z_q, W_q, z, w, x, r, writes Z_k, W_k, x, r
-            double vecs = (k > 0 ? (k + 1.0) + (2.0 * k + 4.0) : 0.0) + (k + 3.0) + (2.0 * k + 8.0);
+        {   // algorithmic bytes (one Gram-Schmidt pass): widening (2 P reads,
+            // 2 T writes); the dots read W_q, w (k + 1) and w, r; the finish
+            // reads Z_q, W_q, z, w, x, r and writes Z_k, W_k, x, r
+            double vecs = (k > 0 ? k + 1.0 : 0.0) + 2.0 + (2.0 * k + 8.0);
             double bytes = sizeof(T) * (double)n * vecs + (mixed ? (2.0 * sizeof(P) + 2.0 * sizeof(T)) * n : 0.0);
             mdz_prof_end(ctx, MDZ_PROF_KRYLOV, bytes, st, ev);
         }

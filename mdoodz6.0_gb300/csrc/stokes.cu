@@ -133,11 +133,14 @@ template mdz_status stokes_norms_launch<double>(mdz_ctx *, stokes_cvec<double>, 
 template mdz_status stokes_norms_launch<float>(mdz_ctx *, stokes_cvec<float>, double *, cudaStream_t);
 
 // Multi-dot: out[q] = <a_q, b> over the three components, for up to 32 a_q.
+// A non-null `flag` that holds 0 makes the launch a no-op (a device-side
+// decision inside a stream or graph).
 template <typename T>
 __global__ void k_multidot(int nq, int n0, int n1, int n2, const T *const *__restrict__ a0,
                            const T *const *__restrict__ a1, const T *const *__restrict__ a2,
                            const T *__restrict__ b0, const T *__restrict__ b1, const T *__restrict__ b2,
-                           double *out) {
+                           double *out, const double *flag) {
+    if (flag && *flag == 0.0) return;
     // one q per blockIdx.y
     int q = blockIdx.y;
     double acc[1] = {0.0};
@@ -151,20 +154,20 @@ __global__ void k_multidot(int nq, int n0, int n1, int n2, const T *const *__res
 
 template <typename T>
 void multidot_launch(int nq, int n0, int n1, int n2, const T *const *a0, const T *const *a1, const T *const *a2,
-                     const T *b0, const T *b1, const T *b2, double *out, cudaStream_t st) {
+                     const T *b0, const T *b1, const T *b2, double *out, cudaStream_t st, const double *flag) {
     int bx = mdz_blocks(n0 > n1 ? n0 : n1, 256);
     int cap = (152 * 4 + nq - 1) / nq;
     if (cap < 8) cap = 8;
     if (bx > cap) bx = cap;
     dim3 gr(bx, nq);
-    k_multidot<T><<<gr, 256, 0, st>>>(nq, n0, n1, n2, a0, a1, a2, b0, b1, b2, out);
+    k_multidot<T><<<gr, 256, 0, st>>>(nq, n0, n1, n2, a0, a1, a2, b0, b1, b2, out, flag);
 }
 template void multidot_launch<double>(int, int, int, int, const double *const *, const double *const *,
                                       const double *const *, const double *, const double *, const double *,
-                                      double *, cudaStream_t);
+                                      double *, cudaStream_t, const double *);
 template void multidot_launch<float>(int, int, int, int, const float *const *, const float *const *,
                                      const float *const *, const float *, const float *, const float *, double *,
-                                     cudaStream_t);
+                                     cudaStream_t, const double *);
 
 // ---------------------------------------------------------------------------
 // Host drop-ins.
