@@ -417,6 +417,7 @@ typedef struct mdz_model {
                                that iteration over (0: lin_maxit)                              */
 } mdz_model;
 
+#define MDZ_HISTORY 32
 typedef struct mdz_step_report {
     int nonlinear_its, linear_its, converged, stagnated;
     int picard_fallbacks;             /* Newton iterations solved with the Picard operator instead */
@@ -425,6 +426,14 @@ typedef struct mdz_step_report {
     double ms_projection, ms_rheology, ms_residual, ms_solve, ms_line_search, ms_markers, ms_total;
     int newton_its;                   /* iterations solved with the Jacobian                  */
     long long local_iterations;       /* local Newton updates of all local rheology solves    */
+    /* per non-linear iteration (the first MDZ_HISTORY; the reference prints the same
+     * lines): resx, resz, resp before the solve, Krylov iterations and relative
+     * residual of its defect solve, 1 where the Jacobian was used */
+    double res_history[MDZ_HISTORY][3];
+    int lin_its_history[MDZ_HISTORY];
+    double lin_rel_history[MDZ_HISTORY];
+    int newton_history[MDZ_HISTORY];
+    int precision_fallbacks;          /* FP32-refined solves that missed 10 x lin_rtol, redone in FP64 */
 } mdz_step_report;
 
 /* One time step of Main_DOODZ.c's loop (SOURCE/Main_DOODZ.c:459-1320) on the

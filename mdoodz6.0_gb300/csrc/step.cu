@@ -381,6 +381,7 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
             if ((s = residual_norms(ctx, r, st)) != MDZ_OK) return s;
         }
         if (nit == 0) memcpy(r0, r, sizeof r0);
+        if (nit < MDZ_HISTORY) memcpy(R.res_history[nit], r, sizeof r);
         if (converged(M, r, r0) && (nit > 0 || (r[0] < M->abs_tol && r[1] < M->abs_tol && r[2] < M->abs_tol))) {
             R.converged = 1;
             break;
@@ -405,6 +406,15 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
             if (s != MDZ_OK) return s;
             R.linear_its += ss.iterations;
             R.newton_its += use_newton ? 1 : 0;
+            // an FP32-refined solve that stopped short of the tolerance (its
+            // refinement stagnates where FP32 cannot resolve the correction) is
+            // redone in FP64, so a missed digit never reaches the Newton update
+            if (M->precision == 32 && !(ss.rel_residual <= 10.0 * M->lin_rtol)) {
+                s = mdz_dev_solve(ctx, f, use_newton, 64, M->lin_rtol, maxit, B.F, B.dx, &ss, st);
+                if (s != MDZ_OK) return s;
+                R.linear_its += ss.iterations;
+                R.precision_fallbacks++;
+            }
             // A Newton system whose pressure Schur complement the Picard-based
             // preconditioner cannot follow (strong pressure-dependent plasticity)
             // stalls the Krylov solve: take a Picard step for this iteration.
@@ -416,6 +426,11 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
                 R.picard_fallbacks++;
                 R.newton_its--;
                 newton_step = false;
+            }
+            if (nit < MDZ_HISTORY) {
+                R.lin_its_history[nit] = ss.iterations;
+                R.lin_rel_history[nit] = ss.rel_residual;
+                R.newton_history[nit] = newton_step ? 1 : 0;
             }
         }
         // line search / update

@@ -567,7 +567,10 @@ class StepReport(C.Structure):
                 ("local_fallbacks", C.c_longlong), ("local_failures", C.c_longlong),
                 ("ms_projection", C.c_double), ("ms_rheology", C.c_double), ("ms_residual", C.c_double),
                 ("ms_solve", C.c_double), ("ms_line_search", C.c_double), ("ms_markers", C.c_double),
-                ("ms_total", C.c_double), ("newton_its", C.c_int), ("local_iterations", C.c_longlong)]
+                ("ms_total", C.c_double), ("newton_its", C.c_int), ("local_iterations", C.c_longlong),
+                ("res_history", (C.c_double * 3) * 32), ("lin_its_history", C.c_int * 32),
+                ("lin_rel_history", C.c_double * 32), ("newton_history", C.c_int * 32),
+                ("precision_fallbacks", C.c_int)]
 
     def as_dict(self):
         d = {}
