@@ -111,16 +111,21 @@ struct visc_res {
 
 __device__ __forceinline__ double dmin(double a, double b) { return a <= b ? a : b; }
 
-// pow with the exponents the creep laws make trivial (0, 1, 2, -1: grain-size
-// and melt exponents switched off, linear diffusion creep, squares) taken
-// exactly; each costs a full FP64 log/exp pair otherwise.
+// pow with the exponents the creep laws make trivial (0, 1, 2, -1, -2:
+// grain-size and melt exponents switched off, linear diffusion creep and its
+// tangent, squares) taken exactly; each costs a full FP64 log/exp pair
+// otherwise, and FP64 throughput is what bounds the local solves on this part.
 __device__ __forceinline__ double fpow(double x, double y) {
     if (y == 0.0) return 1.0;
     if (y == 1.0) return x;
     if (y == 2.0) return x * x;
     if (y == -1.0) return 1.0 / x;
+    if (y == -2.0) return 1.0 / (x * x);
     return pow(x, y);
 }
+
+// exp with the zero argument of switched-off melt weakening taken exactly
+__device__ __forceinline__ double fexp(double x) { return x == 0.0 ? 1.0 : exp(x); }
 
 __device__ void visc_local(int p, double G, double T, double P, double d, double phi, double X0, double Exx,
                            double Ezz, double Exz, double Gxx, double Gzz, double Gxz, double Txx0, double Tzz0,
@@ -153,19 +158,21 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     if (dislocation) {
         double B_pwl = m.pref_pwl[p] * m.Fpwl[p] * fpow(m.Apwl[p], -1.0 / n_pwl) *
                        exp((m.Qpwl[p] + P * Va_pwl) / R / n_pwl / T) * fpow(d, m.mpwl[p] / n_pwl) *
-                       fpow(m.fpwl[p], -m.rpwl[p] / n_pwl) * exp(-m.apwl[p] * phi / n_pwl);
+                       fpow(m.fpwl[p], -m.rpwl[p] / n_pwl) * fexp(-m.apwl[p] * phi / n_pwl);
         C_pwl = fpow(2.0 * f_ani * B_pwl, -n_pwl);
         dCpwldP = -C_pwl * Va_pwl / R / T;
         eta_pwl = B_pwl * fpow(Eii, 1.0 / n_pwl - 1.0);
     }
     if (diffusion) {
         B_lin = m.Flin[p] * fpow(m.Alin[p], -1.0 / n_lin) * exp((m.Qlin[p] + P * m.Vlin[p]) / R / n_lin / T) *
-                fpow(m.flin[p], -m.rlin[p] / n_lin) * exp(-m.alin[p] * phi / n_lin);
+                fpow(m.flin[p], -m.rlin[p] / n_lin) * fexp(-m.alin[p] * phi / n_lin);
         C_lin = fpow(2.0 * f_ani * B_lin, -n_lin);
         dClindP = -C_lin * m.Vlin[p] / R / T;
         eta_lin = B_lin * fpow(Eii, 1.0 / n_lin - 1.0) * fpow(d, m_lin / n_lin);
     }
-    double cos_fric = cos(fric), sin_fric = sin(fric), sin_dil = sin(dil);
+    double cos_fric, sin_fric;
+    sincos(fric, &sin_fric, &cos_fric);
+    double sin_dil = dil == 0.0 ? 0.0 : sin(dil);
     double Tyield = C * cos_fric + P * sin_fric;
     if (m.Slim[p] < Tyield) { sin_fric = 0.0; cos_fric = 1.0; sin_dil = 0.0; C = m.Slim[p]; Tyield = m.Slim[p]; }
     o.X1 = X0;
@@ -237,10 +244,16 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
         if (it == nitmax - 1 && res > tol) o.ve_fail = 1;
     }
     o.eta_ve = eta_ve;
+    // Eii_pwl = C_pwl Tii^n_pwl was evaluated at the final eta_ve when the
+    // iteration stopped on its convergence test (not when it ran out): then
+    // Tii^n_pwl is Eii_pwl / C_pwl, and the powers of Tii below follow from it
+    // without another FP64 pow each
+    const bool pwl_fresh = dislocation && (ve_done || res < tol / 100) && C_pwl > 0.0 && Eii_pwl > 0.0;
     Tii = 2.0 * eta_ve * f_ani * Eii;
+    const double Tn = !dislocation ? 0.0 : (pwl_fresh ? Eii_pwl / C_pwl : fpow(Tii, n_pwl));   // Tii^n_pwl
     double Txx = Gxx * Tii / f_ani / Eii, Tzz = Gzz * Tii / f_ani / Eii, Txz = Gxz * Tii / f_ani / Eii;
     double Exx_lin = 0, Ezz_lin = 0, Exz_lin = 0, Exx_cst = 0, Ezz_cst = 0, Exz_cst = 0;
-    if (dislocation) eta_pwl = fpow(2.0 * C_pwl, -1.0) * fpow(Tii, 1.0 - n_pwl);
+    if (dislocation) eta_pwl = fpow(2.0 * C_pwl, -1.0) * (Tii / Tn);   // (2 C)^-1 Tii^(1-n)
     if (diffusion) {
         eta_lin = B_lin * fpow(Eii_lin, 1.0 / n_lin - 1.0) * fpow(o.d1, m_lin / n_lin);
         Exx_lin = Txx / 2.0 / eta_lin; Ezz_lin = Tzz / 2.0 / eta_lin; Exz_lin = Txz / 2.0 / eta_lin;
@@ -248,7 +261,7 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     if (constant) { Exx_cst = Txx / 2.0 / eta_cst; Ezz_cst = Tzz / 2.0 / eta_cst; Exz_cst = Txz / 2.0 / eta_cst; }
     // visco-elastic tangent
     double deta = 0.0;
-    if (dislocation) deta += -C_pwl * fpow(Tii, n_pwl - 3.0) * (n_pwl - 1.0);
+    if (dislocation) deta += -C_pwl * (Tn / (Tii * Tii * Tii)) * (n_pwl - 1.0);   // Tii^(n-3)
     if (diffusion) deta += -C_lin * fpow(Tii, n_lin - 3.0) * (n_lin - 1.0) * dm_lin;
     const double e2 = fpow(eta_ve, 2.0);
     double dTxx = deta * (2.0 * Txx + Tzz) * e2, dTzz = deta * (2.0 * Tzz + Txx) * e2, dTxz = 2.0 * deta * Txz * e2;
@@ -256,7 +269,7 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     double dve_dExx = dTxx * 2.0 * eta_ve / den, dve_dEzz = dTzz * 2.0 * eta_ve / den;
     double dve_dExz = dTxz * 2.0 * eta_ve / den;
     double dummy = 0.0, Jii = Tii * Tii;
-    if (dislocation) dummy += -2.0 * fpow(Jii, (1.0 / 2.0) * n_pwl - 1.0 / 2.0) * dCpwldP;
+    if (dislocation) dummy += -2.0 * (Tn / Tii) * dCpwldP;   // Jii^((n-1)/2) = Tii^(n-1)
     if (diffusion) dummy += -2.0 * fpow(Jii, (1.0 / 2.0) * n_lin - 1.0 / 2.0) * fpow(d, -m_lin) * dClindP;
     double dve_dP = fpow(eta_ve, 2) * dummy;
     // plastic return mapping on gdot
@@ -361,8 +374,9 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
         inv_eta_diss += 1.0 / eta_vep;
     }
     // eta_pwl is re-evaluated unconditionally in the reference (C_pwl = 0 when
-    // dislocation creep is off, which makes the dislocation parts vanish)
-    eta_pwl = fpow(2.0 * C_pwl, -1.0) * fpow(Tii, 1.0 - n_pwl);
+    // dislocation creep is off, which makes the dislocation parts vanish); Tii
+    // is still the visco-elastic one unless the plastic branch changed it
+    eta_pwl = fpow(2.0 * C_pwl, -1.0) * (dislocation && !is_pl ? Tii / Tn : fpow(Tii, 1.0 - n_pwl));
     o.Exx_el = (double)elastic * (Txx - Txx0) / 2.0 / eta_el;
     o.Ezz_el = (double)elastic * (Tzz - Tzz0) / 2.0 / eta_el;
     o.Exz_el = (double)elastic * (Txz - Txz0) / 2.0 / eta_el;

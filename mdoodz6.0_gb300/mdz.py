@@ -573,8 +573,13 @@ class StepReport(C.Structure):
                 ("precision_fallbacks", C.c_int)]
 
     def as_dict(self):
+        def plain(v):
+            return [plain(x) for x in v] if hasattr(v, "__len__") else v
         d = {}
         for name, _ in self._fields_:
-            v = getattr(self, name)
-            d[name] = list(v) if hasattr(v, "__len__") else v
+            d[name] = plain(getattr(self, name))
+        if d["nonlinear_its"] < 32:   # history rows past the last iteration are empty
+            n = d["nonlinear_its"] + 1
+            for key in ("res_history", "lin_its_history", "lin_rel_history", "newton_history"):
+                d[key] = d[key][:n]
         return d
