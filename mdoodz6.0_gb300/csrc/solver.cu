@@ -1732,10 +1732,11 @@ __global__ void k_set_scalar(double *dst, const double *src) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *dst = *src;
 }
 
-template <typename T>
-__global__ void k_gcr_finish(size_t n, int k, T *__restrict__ Z, T *__restrict__ W, const double *__restrict__ dots1,
+// basis Z, W and the new pair z, w in precision P; x, r in precision T
+template <typename P, typename T>
+__global__ void k_gcr_finish(size_t n, int k, P *__restrict__ Z, P *__restrict__ W, const double *__restrict__ dots1,
                              const double *__restrict__ dots2, const double *__restrict__ sc,
-                             const T *__restrict__ z, const T *__restrict__ w, T *__restrict__ x, T *__restrict__ r) {
+                             const P *__restrict__ z, const P *__restrict__ w, T *__restrict__ x, T *__restrict__ r) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double *__restrict__ beta = sc[5] != 0.0 ? dots2 : dots1;
@@ -1748,10 +1749,35 @@ __global__ void k_gcr_finish(size_t n, int k, T *__restrict__ Z, T *__restrict__
     double inv = sc[0], alpha = sc[1];
     zs *= inv;
     ws *= inv;
-    Z[(size_t)k * n + i] = (T)zs;
-    W[(size_t)k * n + i] = (T)ws;
+    Z[(size_t)k * n + i] = (P)zs;
+    W[(size_t)k * n + i] = (P)ws;
     x[i] = (T)((double)x[i] + alpha * zs);
     r[i] = (T)((double)r[i] - alpha * ws);
+}
+
+// out[0] += (w, w), out[1] += (w, r) (FP64 accumulation); a non-null flag
+// holding 0 makes the launch a no-op
+template <typename P, typename T>
+__global__ void __launch_bounds__(256) k_gcr_wdots(size_t n, const P *__restrict__ w, const T *__restrict__ r,
+                                                   double *out, const double *flag) {
+    if (flag && *flag == 0.0) return;
+    double a[2] = {0.0, 0.0};
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const double wi = (double)w[i];
+        a[0] += wi * wi;
+        a[1] += wi * (double)r[i];
+    }
+    __shared__ double sh[2][8];
+    for (int q = 0; q < 2; q++) {
+        for (int o = 16; o > 0; o >>= 1) a[q] += __shfl_xor_sync(0xffffffffu, a[q], o);
+        if ((threadIdx.x & 31) == 0) sh[q][threadIdx.x >> 5] = a[q];
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+        double s = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) s += sh[threadIdx.x][q];
+        atomicAdd(out + threadIdx.x, s);
+    }
 }
 
 template <typename T>
@@ -1841,21 +1867,14 @@ static mdz_status precond_graph(mdz_ctx *ctx, gcr_space<T> &S, mg_hier<T> &H, co
     return MDZ_OK;
 }
 
-// z, w (precision T) <- z, w (precision P)
-template <typename P, typename T>
-__global__ void k_widen2(size_t n, const P *__restrict__ a, const P *__restrict__ b, T *__restrict__ A,
-                         T *__restrict__ B) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) { A[i] = (T)a[i]; B[i] = (T)b[i]; }
-}
-
 // ---------------------------------------------------------------------------
-// GCR on K x = b (x0 = 0), right-preconditioned.  Krylov vectors,
-// orthogonalisation and updates in precision T; the preconditioner (V-cycle)
-// and the operator apply in precision P.  P = T: one precision throughout
-// (SP is S).  T = double, P = float: FP64 Krylov space with FP32 stencils and
-// V-cycles (r narrowed to FP32 before the preconditioner, z and K z widened to
-// FP64 after the apply), so the cancellations of the Krylov sums happen in FP64.
+// GCR on K x = b (x0 = 0), right-preconditioned.  The preconditioner
+// (V-cycle), the operator apply and the stored basis Z, W run in precision
+// P; the iterate x, the residual r and every inner product are FP64 (T).
+// P = T = double: the plain FP64 solve.  T = double, P = float: the inner
+// solve of the FP32 form (r narrowed to FP32 before the preconditioner), whose
+// recursive residual differs from b - K x only by FP32 rounding of the
+// applies and basis vectors, which the FP64 defect correction outside absorbs.
 template <typename T, typename P>
 static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_hier<P> &H,
                             const stokes_coefs<P> &K, bool newton, const double *eta_n, double rtol, int maxit,
@@ -1910,32 +1929,36 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
             mdz_prof_end(ctx, MDZ_PROF_STOKES_APPLY, bytes, st, ev);
         }
         mdz_prof_begin(ctx, MDZ_PROF_KRYLOV, st, &ev);
-        if (mixed) {   // z, K z (P) -> (T)
-            k_widen2<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, SP.z, SP.w, S.z, S.w);
-            MDZ_LAUNCHED(ctx);
-        }
-        // first pass: (w, W_q) q < k, (w, w), (w, r); the check decides on the
-        // device whether a second pass runs
-        if ((s = dots_launch<T>(ctx, S, 0, k, S.w, dots, st)) != MDZ_OK) return s;
-        if ((s = dots_launch<T>(ctx, S, S.m, 2, S.w, dots + k, st)) != MDZ_OK) return s;
+        // The basis Z, W and the new pair z, K z stay in the apply's precision
+        // P (in the FP32 form: as the FP32 V-cycle and apply produced them; the
+        // FP32 rounding of a stored basis vector is the rounding K z already
+        // carries); x, r and every sum are FP64.
+        // First pass: (w, W_q) q < k, (w, w), (w, r); the check decides on the
+        // device whether a second pass runs.
+        const int ng = nb < 152 * 8 ? nb : 152 * 8;
+        if ((s = dots_launch<P>(ctx, SP, 0, k, SP.w, dots, st)) != MDZ_OK) return s;
+        MDZ_CUDA(ctx, cudaMemsetAsync(dots + k, 0, 2 * sizeof(double), st));
+        k_gcr_wdots<P, T><<<ng, 256, 0, st>>>(n, SP.w, S.r, dots + k, nullptr);
+        MDZ_LAUNCHED(ctx);
         k_gcr_check<<<1, 32, 0, st>>>(k, dots, sc);
         MDZ_LAUNCHED(ctx);
         if (k > 0) {   // second pass (each launch returns at once unless sc[5] = 1)
-            const int ng = nb < 152 * 8 ? nb : 152 * 8;
-            k_gcr_orth_if<T><<<ng, MDZ_THREADS, 0, st>>>(n, k, S.Z, S.W, dots, sc, S.z, S.w);
+            k_gcr_orth_if<P><<<ng, MDZ_THREADS, 0, st>>>(n, k, SP.Z, SP.W, dots, sc, SP.z, SP.w);
             MDZ_LAUNCHED(ctx);
-            if ((s = dots_launch<T>(ctx, S, 0, k, S.w, dots2, st, sc + 5)) != MDZ_OK) return s;
-            if ((s = dots_launch<T>(ctx, S, S.m, 2, S.w, dots2 + k, st, sc + 5)) != MDZ_OK) return s;
+            if ((s = dots_launch<P>(ctx, SP, 0, k, SP.w, dots2, st, sc + 5)) != MDZ_OK) return s;
+            MDZ_CUDA(ctx, cudaMemsetAsync(dots2 + k, 0, 2 * sizeof(double), st));
+            k_gcr_wdots<P, T><<<ng, 256, 0, st>>>(n, SP.w, S.r, dots2 + k, sc + 5);
+            MDZ_LAUNCHED(ctx);
             k_gcr_scalars2<<<1, 32, 0, st>>>(k, dots2, sc);
             MDZ_LAUNCHED(ctx);
         }
-        k_gcr_finish<T><<<nb, MDZ_THREADS, 0, st>>>(n, k, S.Z, S.W, dots, dots2, sc, S.z, S.w, S.x, S.r);
+        k_gcr_finish<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, k, SP.Z, SP.W, dots, dots2, sc, SP.z, SP.w, S.x, S.r);
         MDZ_LAUNCHED(ctx);
-        {   // algorithmic bytes (one Gram-Schmidt pass): widening (2 P reads,
-            // 2 T writes); the dots read W_q, w (k + 1) and w, r; the finish
-            // reads Z_q, W_q, z, w, x, r and writes Z_k, W_k, x, r
-            double vecs = (k > 0 ? k + 1.0 : 0.0) + 2.0 + (2.0 * k + 8.0);
-            double bytes = sizeof(T) * (double)n * vecs + (mixed ? (2.0 * sizeof(P) + 2.0 * sizeof(T)) * n : 0.0);
+        {   // algorithmic bytes (one Gram-Schmidt pass): the dots read W_q, w
+            // (k + 1 P vectors) and w, r; the finish reads Z_q, W_q, z, w (P),
+            // x, r (T) and writes Z_k, W_k (P), x, r (T)
+            double pv = (k > 0 ? k + 1.0 : 0.0) + 1.0 + (2.0 * k + 2.0) + 2.0, tv = 1.0 + 4.0;
+            double bytes = (double)n * (sizeof(P) * pv + sizeof(T) * tv);
             mdz_prof_end(ctx, MDZ_PROF_KRYLOV, bytes, st, ev);
         }
         k++;
