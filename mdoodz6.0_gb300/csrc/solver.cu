@@ -1711,20 +1711,22 @@ __global__ void k_gcr_scalars2(int k, const double *dots2, double *sc) {
 
 // first-pass correction z -= sum beta_q Z_q, w -= sum beta_q W_q, only when
 // sc[5] asks for a second pass (grid-stride, so a skipped launch is short)
-template <typename T>
-__global__ void k_gcr_orth_if(size_t n, int k, const T *__restrict__ Z, const T *__restrict__ W,
-                              const double *__restrict__ beta, const double *__restrict__ sc, T *__restrict__ z,
-                              T *__restrict__ w) {
+template <typename P>
+__global__ void k_gcr_orth_if(size_t n, int k, const P *__restrict__ Z, const P *__restrict__ W,
+                              const double *__restrict__ beta, const double *__restrict__ sc, P *__restrict__ z,
+                              P *__restrict__ w) {
     if (sc[5] == 0.0) return;
+    __shared__ P bsh[GCR_MAX_M];
+    for (int q = threadIdx.x; q < k; q += blockDim.x) bsh[q] = (P)beta[q];
+    __syncthreads();
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        double zs = z[i], ws = w[i];
+        P zs = z[i], ws = w[i];
         for (int q = 0; q < k; q++) {
-            double b = beta[q];
-            zs -= b * (double)Z[q * n + i];
-            ws -= b * (double)W[q * n + i];
+            zs -= bsh[q] * Z[q * n + i];
+            ws -= bsh[q] * W[q * n + i];
         }
-        z[i] = (T)zs;
-        w[i] = (T)ws;
+        z[i] = zs;
+        w[i] = ws;
     }
 }
 
@@ -1732,41 +1734,53 @@ __global__ void k_set_scalar(double *dst, const double *src) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *dst = *src;
 }
 
-// basis Z, W and the new pair z, w in precision P; x, r in precision T
+// basis Z, W and the new pair z, w in precision P; x, r in precision T.
+// With P = float the basis arithmetic is FP32 (FP64 throughput is a small
+// fraction of FP32 on this part; only the x, r updates are FP64).
 template <typename P, typename T>
 __global__ void k_gcr_finish(size_t n, int k, P *__restrict__ Z, P *__restrict__ W, const double *__restrict__ dots1,
                              const double *__restrict__ dots2, const double *__restrict__ sc,
                              const P *__restrict__ z, const P *__restrict__ w, T *__restrict__ x, T *__restrict__ r) {
+    __shared__ P bsh[GCR_MAX_M];
+    const double *__restrict__ beta = sc[5] != 0.0 ? dots2 : dots1;
+    for (int q = threadIdx.x; q < k; q += blockDim.x) bsh[q] = (P)beta[q];
+    __syncthreads();
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double *__restrict__ beta = sc[5] != 0.0 ? dots2 : dots1;
-    double zs = z[i], ws = w[i];
+    P zs = z[i], ws = w[i];
     for (int q = 0; q < k; q++) {
-        double b = beta[q];
-        zs -= b * (double)Z[q * n + i];
-        ws -= b * (double)W[q * n + i];
+        const P b = bsh[q];
+        zs -= b * Z[q * n + i];
+        ws -= b * W[q * n + i];
     }
-    double inv = sc[0], alpha = sc[1];
+    const P inv = (P)sc[0];
+    const double alpha = sc[1];
     zs *= inv;
     ws *= inv;
-    Z[(size_t)k * n + i] = (P)zs;
-    W[(size_t)k * n + i] = (P)ws;
-    x[i] = (T)((double)x[i] + alpha * zs);
-    r[i] = (T)((double)r[i] - alpha * ws);
+    Z[(size_t)k * n + i] = zs;
+    W[(size_t)k * n + i] = ws;
+    x[i] = (T)((double)x[i] + alpha * (double)zs);
+    r[i] = (T)((double)r[i] - alpha * (double)ws);
 }
 
-// out[0] += (w, w), out[1] += (w, r) (FP64 accumulation); a non-null flag
-// holding 0 makes the launch a no-op
-template <typename P, typename T>
-__global__ void __launch_bounds__(256) k_gcr_wdots(size_t n, const P *__restrict__ w, const T *__restrict__ r,
+// out[0] += (w, w), out[1] += (w, r), FP64 totals (FP32 partial sums over
+// runs of 64 elements for FP32 vectors); a non-null flag holding 0 makes the
+// launch a no-op
+template <typename P>
+__global__ void __launch_bounds__(256) k_gcr_wdots(size_t n, const P *__restrict__ w, const P *__restrict__ r,
                                                    double *out, const double *flag) {
     if (flag && *flag == 0.0) return;
     double a[2] = {0.0, 0.0};
+    P p0 = 0, p1 = 0;
+    int cnt = 0;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const double wi = (double)w[i];
-        a[0] += wi * wi;
-        a[1] += wi * (double)r[i];
+        const P wi = w[i];
+        p0 += wi * wi;
+        p1 += wi * r[i];
+        if (sizeof(P) == 8 || ++cnt == 64) { a[0] += (double)p0; a[1] += (double)p1; p0 = 0; p1 = 0; cnt = 0; }
     }
+    a[0] += (double)p0;
+    a[1] += (double)p1;
     __shared__ double sh[2][8];
     for (int q = 0; q < 2; q++) {
         for (int o = 16; o > 0; o >>= 1) a[q] += __shfl_xor_sync(0xffffffffu, a[q], o);
@@ -1774,9 +1788,9 @@ __global__ void __launch_bounds__(256) k_gcr_wdots(size_t n, const P *__restrict
     }
     __syncthreads();
     if (threadIdx.x < 2) {
-        double s = 0.0;
-        for (int q = 0; q < (int)(blockDim.x >> 5); q++) s += sh[threadIdx.x][q];
-        atomicAdd(out + threadIdx.x, s);
+        double t = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += sh[threadIdx.x][q];
+        atomicAdd(out + threadIdx.x, t);
     }
 }
 
@@ -1938,7 +1952,9 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
         const int ng = nb < 152 * 8 ? nb : 152 * 8;
         if ((s = dots_launch<P>(ctx, SP, 0, k, SP.w, dots, st)) != MDZ_OK) return s;
         MDZ_CUDA(ctx, cudaMemsetAsync(dots + k, 0, 2 * sizeof(double), st));
-        k_gcr_wdots<P, T><<<ng, 256, 0, st>>>(n, SP.w, S.r, dots + k, nullptr);
+        // (w, r) against the residual as the preconditioner saw it (SP.r: the
+        // FP32 copy in the FP32 form, r itself otherwise)
+        k_gcr_wdots<P><<<ng, 256, 0, st>>>(n, SP.w, SP.r, dots + k, nullptr);
         MDZ_LAUNCHED(ctx);
         k_gcr_check<<<1, 32, 0, st>>>(k, dots, sc);
         MDZ_LAUNCHED(ctx);
@@ -1947,7 +1963,7 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
             MDZ_LAUNCHED(ctx);
             if ((s = dots_launch<P>(ctx, SP, 0, k, SP.w, dots2, st, sc + 5)) != MDZ_OK) return s;
             MDZ_CUDA(ctx, cudaMemsetAsync(dots2 + k, 0, 2 * sizeof(double), st));
-            k_gcr_wdots<P, T><<<ng, 256, 0, st>>>(n, SP.w, S.r, dots2 + k, sc + 5);
+            k_gcr_wdots<P><<<ng, 256, 0, st>>>(n, SP.w, SP.r, dots2 + k, sc + 5);
             MDZ_LAUNCHED(ctx);
             k_gcr_scalars2<<<1, 32, 0, st>>>(k, dots2, sc);
             MDZ_LAUNCHED(ctx);

@@ -146,9 +146,26 @@ __global__ void k_multidot(int nq, int n0, int n1, int n2, const T *const *__res
     double acc[1] = {0.0};
     const T *x0 = a0[q], *x1 = a1[q], *x2 = a2[q];
     int stride = gridDim.x * blockDim.x;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n0; i += stride) acc[0] += (double)x0[i] * (double)b0[i];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n1; i += stride) acc[0] += (double)x1[i] * (double)b1[i];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += stride) acc[0] += (double)x2[i] * (double)b2[i];
+    if constexpr (sizeof(T) == 4) {
+        // FP32 operands: FP32 products and partial sums over runs of 64
+        // elements, flushed into the FP64 total.  A conversion and an FP64
+        // multiply per element would bound the kernel far below the memory
+        // rate: FP64 throughput is a small fraction of FP32 on this part.
+        float part = 0.0f;
+        int cnt = 0;
+        auto add = [&](float a, float b) {
+            part = fmaf(a, b, part);
+            if (++cnt == 64) { acc[0] += (double)part; part = 0.0f; cnt = 0; }
+        };
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n0; i += stride) add(x0[i], b0[i]);
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n1; i += stride) add(x1[i], b1[i]);
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += stride) add(x2[i], b2[i]);
+        acc[0] += (double)part;
+    } else {
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n0; i += stride) acc[0] += (double)x0[i] * (double)b0[i];
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n1; i += stride) acc[0] += (double)x1[i] * (double)b1[i];
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += stride) acc[0] += (double)x2[i] * (double)b2[i];
+    }
     block_sum_atomic<1>(acc, out + q);
 }
 
