@@ -69,7 +69,7 @@ struct gcr_space {
     int m = 0;
     T *Z = nullptr, *W = nullptr;       // m basis vectors each (u, v, p contiguous)
     T *x = nullptr, *r = nullptr, *z = nullptr, *w = nullptr, *t = nullptr;
-    const T **dA0 = nullptr, **dA1 = nullptr, **dA2 = nullptr;   // multidot pointer tables
+    const T **dA0 = nullptr, **dA1 = nullptr, **dA2 = nullptr;   // dot-product pointer tables (k_dots uses dA0)
     double *dots = nullptr;             // device scalars
     // FP32 copies of the operator (only used for T = float)
     T *Dc[12] = {nullptr};
@@ -1824,13 +1824,66 @@ static mdz_status remove_pressure_mean(mdz_ctx *ctx, double *p, cudaStream_t st)
     return MDZ_OK;
 }
 
+// out[q] += (a_q, b) for the nq vectors of the pointer table (each of length
+// n, contiguous u|v|p like b).  One thread keeps MDOT_Q running sums, so b is
+// read once per MDOT_Q vectors and the loads of MDOT_Q independent chains
+// overlap.  FP32 vectors: FP32 products and partial sums over runs of 32
+// elements, flushed into FP64 (FP64 throughput is a small fraction of FP32 on
+// this part); FP64 vectors: FP64 throughout.  A non-null flag holding 0
+// makes the launch a no-op.
+#define MDOT_Q 8
+template <typename T>
+__global__ void __launch_bounds__(256) k_dots(int nq, size_t n, const T *const *__restrict__ a,
+                                              const T *__restrict__ b, double *out, const double *flag) {
+    if (flag && *flag == 0.0) return;
+    const int q0 = blockIdx.y * MDOT_Q;
+    const T *ap[MDOT_Q];
+    double acc[MDOT_Q];
+    T part[MDOT_Q];
+#pragma unroll
+    for (int j = 0; j < MDOT_Q; j++) {
+        ap[j] = q0 + j < nq ? a[q0 + j] : nullptr;
+        acc[j] = 0.0;
+        part[j] = T(0);
+    }
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    int cnt = 0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const T bi = b[i];
+#pragma unroll
+        for (int j = 0; j < MDOT_Q; j++)
+            if (ap[j]) part[j] += ap[j][i] * bi;
+        if (sizeof(T) == 8 || ++cnt == 32) {
+#pragma unroll
+            for (int j = 0; j < MDOT_Q; j++) { acc[j] += (double)part[j]; part[j] = T(0); }
+            cnt = 0;
+        }
+    }
+    __shared__ double sh[MDOT_Q][8];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < MDOT_Q; j++) {
+        double v = acc[j] + (double)part[j];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[j][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < MDOT_Q && q0 + (int)threadIdx.x < nq) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += sh[threadIdx.x][w];
+        atomicAdd(out + q0 + threadIdx.x, v);
+    }
+}
+
 template <typename T>
 static mdz_status dots_launch(mdz_ctx *ctx, gcr_space<T> &S, int q0, int nq, const T *b, double *out,
                               cudaStream_t st, const double *flag = nullptr) {
     if (nq <= 0) return MDZ_OK;
     MDZ_CUDA(ctx, cudaMemsetAsync(out, 0, sizeof(double) * nq, st));
-    multidot_launch<T>(nq, (int)S.nu, (int)S.nv, (int)S.np, S.dA0 + q0, S.dA1 + q0, S.dA2 + q0, b, b + S.nu,
-                       b + S.nu + S.nv, out, st, flag);
+    const int tiles = (nq + MDOT_Q - 1) / MDOT_Q;
+    int bx = mdz_blocks((long long)S.n, 256), cap = (152 * 8) / tiles;
+    if (bx > cap) bx = cap;
+    k_dots<T><<<dim3(bx, tiles), 256, 0, st>>>(nq, S.n, S.dA0 + q0, b, out, flag);
     MDZ_LAUNCHED(ctx);
     return MDZ_OK;
 }

@@ -132,60 +132,6 @@ mdz_status stokes_norms_launch(mdz_ctx *ctx, stokes_cvec<T> f, double *d_out6, c
 template mdz_status stokes_norms_launch<double>(mdz_ctx *, stokes_cvec<double>, double *, cudaStream_t);
 template mdz_status stokes_norms_launch<float>(mdz_ctx *, stokes_cvec<float>, double *, cudaStream_t);
 
-// Multi-dot: out[q] = <a_q, b> over the three components, for up to 32 a_q.
-// A non-null `flag` that holds 0 makes the launch a no-op (a device-side
-// decision inside a stream or graph).
-template <typename T>
-__global__ void k_multidot(int nq, int n0, int n1, int n2, const T *const *__restrict__ a0,
-                           const T *const *__restrict__ a1, const T *const *__restrict__ a2,
-                           const T *__restrict__ b0, const T *__restrict__ b1, const T *__restrict__ b2,
-                           double *out, const double *flag) {
-    if (flag && *flag == 0.0) return;
-    // one q per blockIdx.y
-    int q = blockIdx.y;
-    double acc[1] = {0.0};
-    const T *x0 = a0[q], *x1 = a1[q], *x2 = a2[q];
-    int stride = gridDim.x * blockDim.x;
-    if constexpr (sizeof(T) == 4) {
-        // FP32 operands: FP32 products and partial sums over runs of 64
-        // elements, flushed into the FP64 total.  A conversion and an FP64
-        // multiply per element would bound the kernel far below the memory
-        // rate: FP64 throughput is a small fraction of FP32 on this part.
-        float part = 0.0f;
-        int cnt = 0;
-        auto add = [&](float a, float b) {
-            part = fmaf(a, b, part);
-            if (++cnt == 64) { acc[0] += (double)part; part = 0.0f; cnt = 0; }
-        };
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n0; i += stride) add(x0[i], b0[i]);
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n1; i += stride) add(x1[i], b1[i]);
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += stride) add(x2[i], b2[i]);
-        acc[0] += (double)part;
-    } else {
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n0; i += stride) acc[0] += (double)x0[i] * (double)b0[i];
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n1; i += stride) acc[0] += (double)x1[i] * (double)b1[i];
-        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n2; i += stride) acc[0] += (double)x2[i] * (double)b2[i];
-    }
-    block_sum_atomic<1>(acc, out + q);
-}
-
-template <typename T>
-void multidot_launch(int nq, int n0, int n1, int n2, const T *const *a0, const T *const *a1, const T *const *a2,
-                     const T *b0, const T *b1, const T *b2, double *out, cudaStream_t st, const double *flag) {
-    int bx = mdz_blocks(n0 > n1 ? n0 : n1, 256);
-    int cap = (152 * 4 + nq - 1) / nq;
-    if (cap < 8) cap = 8;
-    if (bx > cap) bx = cap;
-    dim3 gr(bx, nq);
-    k_multidot<T><<<gr, 256, 0, st>>>(nq, n0, n1, n2, a0, a1, a2, b0, b1, b2, out, flag);
-}
-template void multidot_launch<double>(int, int, int, int, const double *const *, const double *const *,
-                                      const double *const *, const double *, const double *, const double *,
-                                      double *, cudaStream_t, const double *);
-template void multidot_launch<float>(int, int, int, int, const float *const *, const float *const *,
-                                     const float *const *, const float *, const float *, const float *, double *,
-                                     cudaStream_t, const double *);
-
 // ---------------------------------------------------------------------------
 // Host drop-ins.
 static bool supported_bcs(const mdz_ctx *ctx) {

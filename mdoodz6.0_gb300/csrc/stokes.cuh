@@ -12,10 +12,6 @@ void stokes_apply_launch(const stokes_geom &G, const stokes_coefs<T> &D, stokes_
                          const stokes_cvec<T> *b, bool newton, cudaStream_t st);
 template <typename T>
 mdz_status stokes_norms_launch(mdz_ctx *ctx, stokes_cvec<T> f, double *d_out6, cudaStream_t st);
-template <typename T>
-void multidot_launch(int nq, int n0, int n1, int n2, const T *const *a0, const T *const *a1, const T *const *a2,
-                     const T *b0, const T *b1, const T *b2, double *out, cudaStream_t st,
-                     const double *flag = nullptr);
 
 // Picard residual of the current state (u, v, p_corr, D from RheologicalOperators(0)),
 // written to ru, rv, rp; optional device norms (sum F^2 per block, row counts).
