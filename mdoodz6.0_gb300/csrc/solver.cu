@@ -1594,10 +1594,12 @@ __global__ void k_psum(int np, const signed char *__restrict__ tp, const T *__re
     if ((threadIdx.x & 31) == 0) { atomicAdd(&out[0], acc[0]); atomicAdd(&out[1], acc[1]); }
 }
 
+// (the mean in the vector's precision: an FP64 division per thread is a long
+// instruction sequence on this part)
 template <typename T>
 __global__ void k_psub(int np, const signed char *__restrict__ tp, const double *__restrict__ sum, T *__restrict__ p) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < np && tp[i] == -1 && sum[1] > 0) p[i] = (T)((double)p[i] - sum[0] / sum[1]);
+    if (i < np && tp[i] == -1 && sum[1] > 0) p[i] -= (T)sum[0] / (T)sum[1];
 }
 
 // ---------------------------------------------------------------------------
@@ -1763,34 +1765,29 @@ __global__ void k_gcr_finish(size_t n, int k, P *__restrict__ Z, P *__restrict__
     r[i] = (T)((double)r[i] - alpha * (double)ws);
 }
 
-// out[0] += (w, w), out[1] += (w, r), FP64 totals (FP32 partial sums over
-// runs of 64 elements for FP32 vectors); a non-null flag holding 0 makes the
-// launch a no-op
+// out[0] += (w, w), out[1] += (w, r): products, sums and the block reduction
+// in the vectors' precision, block totals added in FP64 (as k_dots); a
+// non-null flag holding 0 makes the launch a no-op
 template <typename P>
 __global__ void __launch_bounds__(256) k_gcr_wdots(size_t n, const P *__restrict__ w, const P *__restrict__ r,
                                                    double *out, const double *flag) {
     if (flag && *flag == 0.0) return;
-    double a[2] = {0.0, 0.0};
-    P p0 = 0, p1 = 0;
-    int cnt = 0;
+    P a[2] = {0, 0};
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const P wi = w[i];
-        p0 += wi * wi;
-        p1 += wi * r[i];
-        if (sizeof(P) == 8 || ++cnt == 64) { a[0] += (double)p0; a[1] += (double)p1; p0 = 0; p1 = 0; cnt = 0; }
+        a[0] += wi * wi;
+        a[1] += wi * r[i];
     }
-    a[0] += (double)p0;
-    a[1] += (double)p1;
-    __shared__ double sh[2][8];
+    __shared__ P sh[2][8];
     for (int q = 0; q < 2; q++) {
         for (int o = 16; o > 0; o >>= 1) a[q] += __shfl_xor_sync(0xffffffffu, a[q], o);
         if ((threadIdx.x & 31) == 0) sh[q][threadIdx.x >> 5] = a[q];
     }
     __syncthreads();
     if (threadIdx.x < 2) {
-        double t = 0.0;
+        P t = 0;
         for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += sh[threadIdx.x][q];
-        atomicAdd(out + threadIdx.x, t);
+        atomicAdd(out + threadIdx.x, (double)t);
     }
 }
 
@@ -1827,10 +1824,12 @@ static mdz_status remove_pressure_mean(mdz_ctx *ctx, double *p, cudaStream_t st)
 // out[q] += (a_q, b) for the nq vectors of the pointer table (each of length
 // n, contiguous u|v|p like b).  One thread keeps MDOT_Q running sums, so b is
 // read once per MDOT_Q vectors and the loads of MDOT_Q independent chains
-// overlap.  FP32 vectors: FP32 products and partial sums over runs of 32
-// elements, flushed into FP64 (FP64 throughput is a small fraction of FP32 on
-// this part); FP64 vectors: FP64 throughout.  A non-null flag holding 0
-// makes the launch a no-op.
+// overlap.  FP32 vectors are multiplied, summed and block-reduced in FP32 and
+// only the block totals enter FP64 (FP64 instructions issue at a small
+// fraction of the FP32 rate on this part, so even a per-thread FP64
+// reduction tree dominated the kernel); FP64 vectors run in FP64 with enough
+// elements per thread that the reduction tree is a small share.  A non-null
+// flag holding 0 makes the launch a no-op.
 #define MDOT_Q 8
 template <typename T>
 __global__ void __launch_bounds__(256) k_dots(int nq, size_t n, const T *const *__restrict__ a,
@@ -1838,40 +1837,32 @@ __global__ void __launch_bounds__(256) k_dots(int nq, size_t n, const T *const *
     if (flag && *flag == 0.0) return;
     const int q0 = blockIdx.y * MDOT_Q;
     const T *ap[MDOT_Q];
-    double acc[MDOT_Q];
     T part[MDOT_Q];
 #pragma unroll
     for (int j = 0; j < MDOT_Q; j++) {
         ap[j] = q0 + j < nq ? a[q0 + j] : nullptr;
-        acc[j] = 0.0;
         part[j] = T(0);
     }
     const size_t stride = (size_t)gridDim.x * blockDim.x;
-    int cnt = 0;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const T bi = b[i];
 #pragma unroll
         for (int j = 0; j < MDOT_Q; j++)
             if (ap[j]) part[j] += ap[j][i] * bi;
-        if (sizeof(T) == 8 || ++cnt == 32) {
-#pragma unroll
-            for (int j = 0; j < MDOT_Q; j++) { acc[j] += (double)part[j]; part[j] = T(0); }
-            cnt = 0;
-        }
     }
-    __shared__ double sh[MDOT_Q][8];
+    __shared__ T sh[MDOT_Q][8];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int j = 0; j < MDOT_Q; j++) {
-        double v = acc[j] + (double)part[j];
+        T v = part[j];
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lane == 0) sh[j][wid] = v;
     }
     __syncthreads();
     if (threadIdx.x < MDOT_Q && q0 + (int)threadIdx.x < nq) {
-        double v = 0.0;
+        T v = 0;
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += sh[threadIdx.x][w];
-        atomicAdd(out + q0 + threadIdx.x, v);
+        atomicAdd(out + q0 + threadIdx.x, (double)v);
     }
 }
 
@@ -1880,9 +1871,12 @@ static mdz_status dots_launch(mdz_ctx *ctx, gcr_space<T> &S, int q0, int nq, con
                               cudaStream_t st, const double *flag = nullptr) {
     if (nq <= 0) return MDZ_OK;
     MDZ_CUDA(ctx, cudaMemsetAsync(out, 0, sizeof(double) * nq, st));
+    // FP32: ~8 elements per thread (the FP32 sums stay short); FP64: at
+    // least 32 per thread, so the FP64 reduction tree is a small share
     const int tiles = (nq + MDOT_Q - 1) / MDOT_Q;
-    int bx = mdz_blocks((long long)S.n, 256), cap = (152 * 8) / tiles;
+    int bx = mdz_blocks((long long)S.n, 256 * (sizeof(T) == 4 ? 8 : 32)), cap = (152 * 8) / tiles;
     if (bx > cap) bx = cap;
+    if (bx < 1) bx = 1;
     k_dots<T><<<dim3(bx, tiles), 256, 0, st>>>(nq, S.n, S.dA0 + q0, b, out, flag);
     MDZ_LAUNCHED(ctx);
     return MDZ_OK;
@@ -2003,11 +1997,12 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
         // First pass: (w, W_q) q < k, (w, w), (w, r); the check decides on the
         // device whether a second pass runs.
         const int ng = nb < 152 * 8 ? nb : 152 * 8;
+        const int nw = mdz_blocks((long long)n, 256 * (sizeof(P) == 4 ? 8 : 32));
         if ((s = dots_launch<P>(ctx, SP, 0, k, SP.w, dots, st)) != MDZ_OK) return s;
         MDZ_CUDA(ctx, cudaMemsetAsync(dots + k, 0, 2 * sizeof(double), st));
         // (w, r) against the residual as the preconditioner saw it (SP.r: the
         // FP32 copy in the FP32 form, r itself otherwise)
-        k_gcr_wdots<P><<<ng, 256, 0, st>>>(n, SP.w, SP.r, dots + k, nullptr);
+        k_gcr_wdots<P><<<nw, 256, 0, st>>>(n, SP.w, SP.r, dots + k, nullptr);
         MDZ_LAUNCHED(ctx);
         k_gcr_check<<<1, 32, 0, st>>>(k, dots, sc);
         MDZ_LAUNCHED(ctx);
@@ -2016,7 +2011,7 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
             MDZ_LAUNCHED(ctx);
             if ((s = dots_launch<P>(ctx, SP, 0, k, SP.w, dots2, st, sc + 5)) != MDZ_OK) return s;
             MDZ_CUDA(ctx, cudaMemsetAsync(dots2 + k, 0, 2 * sizeof(double), st));
-            k_gcr_wdots<P><<<ng, 256, 0, st>>>(n, SP.w, SP.r, dots2 + k, sc + 5);
+            k_gcr_wdots<P><<<nw, 256, 0, st>>>(n, SP.w, SP.r, dots2 + k, sc + 5);
             MDZ_LAUNCHED(ctx);
             k_gcr_scalars2<<<1, 32, 0, st>>>(k, dots2, sc);
             MDZ_LAUNCHED(ctx);
