@@ -1695,6 +1695,7 @@ __device__ void gcr_scalars(int k, const double *dots, double *sc) {
     sc[1] = alpha;
     sc[2] = nrm2;
     sc[3] -= alpha * alpha;
+    sc[8 + k] = alpha;   // x = sum alpha_q Z_q is formed once per basis (k_gcr_xupdate)
 }
 
 __global__ void k_gcr_check(int k, const double *dots, double *sc) {
@@ -1736,13 +1737,17 @@ __global__ void k_set_scalar(double *dst, const double *src) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *dst = *src;
 }
 
-// basis Z, W and the new pair z, w in precision P; x, r in precision T.
-// With P = float the basis arithmetic is FP32 (FP64 throughput is a small
-// fraction of FP32 on this part; only the x, r updates are FP64).
+// Basis Z, W and the new pair z, w in precision P; r in precision T.  With
+// P = float the basis arithmetic is FP32 (FP64 throughput is a small fraction
+// of FP32 on this part); r is updated in FP64 and, in the FP32 form, its FP32
+// copy for the next preconditioner application is written in the same pass
+// (rp; null otherwise).  The iterate is not touched here: x = sum alpha_q Z_q
+// is formed once per basis by k_gcr_xupdate.
 template <typename P, typename T>
 __global__ void k_gcr_finish(size_t n, int k, P *__restrict__ Z, P *__restrict__ W, const double *__restrict__ dots1,
                              const double *__restrict__ dots2, const double *__restrict__ sc,
-                             const P *__restrict__ z, const P *__restrict__ w, T *__restrict__ x, T *__restrict__ r) {
+                             const P *__restrict__ z, const P *__restrict__ w, T *__restrict__ r,
+                             P *__restrict__ rp) {
     __shared__ P bsh[GCR_MAX_M];
     const double *__restrict__ beta = sc[5] != 0.0 ? dots2 : dots1;
     for (int q = threadIdx.x; q < k; q += blockDim.x) bsh[q] = (P)beta[q];
@@ -1756,13 +1761,28 @@ __global__ void k_gcr_finish(size_t n, int k, P *__restrict__ Z, P *__restrict__
         ws -= b * W[q * n + i];
     }
     const P inv = (P)sc[0];
-    const double alpha = sc[1];
     zs *= inv;
     ws *= inv;
     Z[(size_t)k * n + i] = zs;
     W[(size_t)k * n + i] = ws;
-    x[i] = (T)((double)x[i] + alpha * (double)zs);
-    r[i] = (T)((double)r[i] - alpha * (double)ws);
+    const T rn = (T)((double)r[i] - sc[1] * (double)ws);
+    r[i] = rn;
+    if (rp) rp[i] = (P)rn;
+}
+
+// x += sum_{q < k} alpha_q Z_q (alpha_q = sc[8 + q]): the basis part of the
+// iterate, once per basis (at a restart and at the end of the solve)
+template <typename P, typename T>
+__global__ void k_gcr_xupdate(size_t n, int k, const P *__restrict__ Z, const double *__restrict__ sc,
+                              T *__restrict__ x) {
+    __shared__ P ash[GCR_MAX_M];
+    for (int q = threadIdx.x; q < k; q += blockDim.x) ash[q] = (P)sc[8 + q];
+    __syncthreads();
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    P a = 0;
+    for (int q = 0; q < k; q++) a += ash[q] * Z[q * n + i];
+    x[i] = (T)((double)x[i] + (double)a);
 }
 
 // out[0] += (w, w), out[1] += (w, r): products, sums and the block reduction
@@ -1822,16 +1842,15 @@ static mdz_status remove_pressure_mean(mdz_ctx *ctx, double *p, cudaStream_t st)
 }
 
 // out[q] += (a_q, b) for the nq vectors of the pointer table (each of length
-// n, contiguous u|v|p like b).  One thread keeps MDOT_Q running sums, so b is
-// read once per MDOT_Q vectors and the loads of MDOT_Q independent chains
-// overlap.  FP32 vectors are multiplied, summed and block-reduced in FP32 and
-// only the block totals enter FP64 (FP64 instructions issue at a small
-// fraction of the FP32 rate on this part, so even a per-thread FP64
-// reduction tree dominated the kernel); FP64 vectors run in FP64 with enough
-// elements per thread that the reduction tree is a small share.  A non-null
-// flag holding 0 makes the launch a no-op.
-#define MDOT_Q 8
-template <typename T>
+// n, contiguous u|v|p like b).  FP32 vectors: one thread keeps Q = 8 running
+// sums, so b is read once per 8 vectors and the loads of 8 independent chains
+// overlap, and products, sums and the block reduction stay FP32 with only the
+// block totals entering FP64 (FP64 instructions issue at a small fraction of
+// the FP32 rate on this part, so even a per-thread FP64 reduction tree
+// dominated the kernel).  FP64 vectors: Q = 1, one vector per block row (the
+// per-element FP64 multiply-add is the bound there).  A non-null flag holding
+// 0 makes the launch a no-op.
+template <typename T, int MDOT_Q>
 __global__ void __launch_bounds__(256) k_dots(int nq, size_t n, const T *const *__restrict__ a,
                                               const T *__restrict__ b, double *out, const double *flag) {
     if (flag && *flag == 0.0) return;
@@ -1871,13 +1890,15 @@ static mdz_status dots_launch(mdz_ctx *ctx, gcr_space<T> &S, int q0, int nq, con
                               cudaStream_t st, const double *flag = nullptr) {
     if (nq <= 0) return MDZ_OK;
     MDZ_CUDA(ctx, cudaMemsetAsync(out, 0, sizeof(double) * nq, st));
-    // FP32: ~8 elements per thread (the FP32 sums stay short); FP64: at
-    // least 32 per thread, so the FP64 reduction tree is a small share
-    const int tiles = (nq + MDOT_Q - 1) / MDOT_Q;
-    int bx = mdz_blocks((long long)S.n, 256 * (sizeof(T) == 4 ? 8 : 32)), cap = (152 * 8) / tiles;
+    // FP32: 8 vectors per block row, ~8 elements per thread; FP64: one vector
+    // per block row, about 600 blocks in all
+    constexpr int Q = sizeof(T) == 4 ? 8 : 1;
+    const int tiles = (nq + Q - 1) / Q;
+    int bx = mdz_blocks((long long)S.n, 256 * (sizeof(T) == 4 ? 8 : 4));
+    const int cap = (sizeof(T) == 4 ? 152 * 8 : 152 * 4 + tiles - 1) / tiles;
     if (bx > cap) bx = cap;
-    if (bx < 1) bx = 1;
-    k_dots<T><<<dim3(bx, tiles), 256, 0, st>>>(nq, S.n, S.dA0 + q0, b, out, flag);
+    if (bx < 8) bx = 8;
+    k_dots<T, Q><<<dim3(bx, tiles), 256, 0, st>>>(nq, S.n, S.dA0 + q0, b, out, flag);
     MDZ_LAUNCHED(ctx);
     return MDZ_OK;
 }
@@ -1969,9 +1990,13 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
     int k = 0;
     const int check = SV->check > 0 ? SV->check : 1;
     for (it = 0; it < maxit; it++) {
-        if (k == S.m) k = 0;   // restart: keep x and r, drop the basis
+        if (k == S.m) {   // restart: fold the basis into x, keep r, drop the basis
+            k_gcr_xupdate<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, k, SP.Z, sc, S.x);
+            MDZ_LAUNCHED(ctx);
+            k = 0;
+        }
         cudaEvent_t ev;
-        if (mixed) {   // r (T) -> r (P) for the preconditioner
+        if (mixed && it == 0) {   // r (T) -> r (P) for the first preconditioner application
             k_convert<T, P><<<nb, MDZ_THREADS, 0, st>>>(n, S.r, SP.r);
             MDZ_LAUNCHED(ctx);
         }
@@ -1997,7 +2022,8 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
         // First pass: (w, W_q) q < k, (w, w), (w, r); the check decides on the
         // device whether a second pass runs.
         const int ng = nb < 152 * 8 ? nb : 152 * 8;
-        const int nw = mdz_blocks((long long)n, 256 * (sizeof(P) == 4 ? 8 : 32));
+        const int nw = mdz_blocks((long long)n, 256 * (sizeof(P) == 4 ? 8 : 4)) < 152 * 4
+                           ? mdz_blocks((long long)n, 256 * (sizeof(P) == 4 ? 8 : 4)) : 152 * 4;
         if ((s = dots_launch<P>(ctx, SP, 0, k, SP.w, dots, st)) != MDZ_OK) return s;
         MDZ_CUDA(ctx, cudaMemsetAsync(dots + k, 0, 2 * sizeof(double), st));
         // (w, r) against the residual as the preconditioner saw it (SP.r: the
@@ -2016,12 +2042,14 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
             k_gcr_scalars2<<<1, 32, 0, st>>>(k, dots2, sc);
             MDZ_LAUNCHED(ctx);
         }
-        k_gcr_finish<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, k, SP.Z, SP.W, dots, dots2, sc, SP.z, SP.w, S.x, S.r);
+        k_gcr_finish<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, k, SP.Z, SP.W, dots, dots2, sc, SP.z, SP.w, S.r,
+                                                        mixed ? SP.r : (P *)nullptr);
         MDZ_LAUNCHED(ctx);
         {   // algorithmic bytes (one Gram-Schmidt pass): the dots read W_q, w
-            // (k + 1 P vectors) and w, r; the finish reads Z_q, W_q, z, w (P),
-            // x, r (T) and writes Z_k, W_k (P), x, r (T)
-            double pv = (k > 0 ? k + 1.0 : 0.0) + 1.0 + (2.0 * k + 2.0) + 2.0, tv = 1.0 + 4.0;
+            // (k + 1 P vectors) and w, r (P); the finish reads Z_q, W_q, z, w
+            // (P), r (T) and writes Z_k, W_k (P), r (T) and its P copy; x is
+            // formed once per basis (k + 2 vectors, not counted per iteration)
+            double pv = (k > 0 ? k + 1.0 : 0.0) + 2.0 + (2.0 * k + 2.0) + 2.0 + (mixed ? 1.0 : 0.0), tv = 2.0;
             double bytes = (double)n * (sizeof(P) * pv + sizeof(T) * tv);
             mdz_prof_end(ctx, MDZ_PROF_KRYLOV, bytes, st, ev);
         }
@@ -2043,6 +2071,10 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
             rn2 = SV->sc[0];
             if (rn2 <= rtol * rtol * rn02) { it++; break; }
         }
+    }
+    if (k > 0) {   // the current basis' part of the iterate
+        k_gcr_xupdate<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, k, SP.Z, sc, S.x);
+        MDZ_LAUNCHED(ctx);
     }
     if (its_out) *its_out = it;
     if (rel_out) *rel_out = sqrt(rn2 > 0 ? rn2 : 0.0) / sqrt(rn02);
