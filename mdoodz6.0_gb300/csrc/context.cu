@@ -79,6 +79,7 @@ extern "C" mdz_status mdz_create(mdz_ctx **out, const mdz_grid_desc *d, int n_ph
     int Nx = d->Nx, Nz = d->Nz;
     g.Nx = Nx; g.Nz = Nz; g.ncx = Nx - 1; g.ncz = Nz - 1;
     g.dx = d->dx; g.dz = d->dz;
+    g.idx = 1.0 / d->dx; g.idz = 1.0 / d->dz;
     g.xmin = d->xmin; g.xmax = d->xmax; g.zmin = d->zmin; g.zmax = d->zmax;
     cudaError_t e = cudaSuccess;
 #define UP(dst, src, n) if (e == cudaSuccess) e = upload(&dst, src, n)

@@ -14,15 +14,15 @@
 
 // Nearest-node index along one line of a node set, as the reference computes
 // it: ceil(d/h + 0.5) - 1 with d measured from the first line, clamped.
-__device__ __forceinline__ int nearest_line(double x, double X0, double h, int n) {
-    int i = (int)ceil((x - X0) / h + 0.5) - 1;
+__device__ __forceinline__ int nearest_line(double x, double X0, double h, double ih, int n) {
+    int i = (int)ceil_quot(x - X0, h, ih, 0.5) - 1;
     i = i < 0 ? 0 : i;
     return i > n - 1 ? n - 1 : i;
 }
 
 // Lower-left cell index along one line (V2P / Interp_Grid2P): ceil(d/h) - 1.
-__device__ __forceinline__ int lower_line(double x, double X0, double h) {
-    return (int)ceil((x - X0) / h) - 1;
+__device__ __forceinline__ int lower_line(double x, double X0, double h, double ih) {
+    return (int)ceil_quot(x - X0, h, ih, 0.0) - 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -35,8 +35,8 @@ __global__ void k_bin_count(int n, const double *__restrict__ x, const double *_
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     if (phase[k] == -1) { cell[k] = -1; return; }
-    int ic = nearest_line(x[k], xc[0], dx, ncx);
-    int jc = nearest_line(z[k], zc[0], dz, ncz);
+    int ic = nearest_line(x[k], xc[0], dx, 1.0 / dx, ncx);
+    int jc = nearest_line(z[k], zc[0], dz, 1.0 / dz, ncz);
     int c = ic + jc * ncx;
     cell[k] = c;
     atomicAdd(&count[c], 1);
@@ -197,13 +197,14 @@ __global__ void __launch_bounds__(128) k_p2g_gather(
 #pragma unroll
     for (int p = 0; p < NPH; p++) Wph[p] = 0.0;
     const double X0 = X[0], Z0 = Z[0];
+    const double idx = 1.0 / dx, idz = 1.0 / dz, idxi = 1.0 / dx_itp, idzi = 1.0 / dz_itp;
     for (int r = rlo; r <= rhi; r++) {
         int b = start[clo + r * ncx], e = start[chi + r * ncx + 1];
         for (int q = b; q < e; q++) {
             int k = sorted[q];
             double xk = mx[k], zk = mz[k];
-            int ip = nearest_line(xk, X0, dx, nnx);
-            int jp = nearest_line(zk, Z0, dz, nnz);
+            int ip = nearest_line(xk, X0, dx, idx, nnx);
+            int jp = nearest_line(zk, Z0, dz, idz, nnz);
             int di = i - ip, dj = j - jp;
             if (di < -h || di > h || dj < -h || dj > h) continue;
             double Xn = X[ip], Zn = Z[jp];
@@ -212,7 +213,7 @@ __global__ void __launch_bounds__(128) k_p2g_gather(
             if (dj > 0) Zn = Z[jp] + dz;
             if (dj < 0) Zn = Z[jp] - dz;
             double dxm = fabs(Xn - xk), dzm = fabs(Zn - zk);
-            double w = (1.0 - dxm / dx_itp) * (1.0 - dzm / dz_itp);
+            double w = (1.0 - dxm * idxi) * (1.0 - dzm * idzi);
             int p = mphase[k];
             Wm += w;
 #pragma unroll
@@ -383,7 +384,8 @@ __global__ void k_count_nodes(int nnx, int nnz, int kindx, int kindz, const doub
         int b = start[clo + r * ncx], e = start[chi + r * ncx + 1];
         for (int q = b; q < e; q++) {
             int k = sorted[q];
-            if (nearest_line(mx[k], X[0], dx, nnx) != i || nearest_line(mz[k], Z[0], dz, nnz) != j) continue;
+            if (nearest_line(mx[k], X[0], dx, 1.0 / dx, nnx) != i || nearest_line(mz[k], Z[0], dz, 1.0 / dz, nnz) != j)
+                continue;
             int p = mphase[k];
             if (p < 0) continue;
             cnt++;
@@ -442,19 +444,21 @@ __device__ __forceinline__ bool air(signed char t) { return t == 30 || t == 31; 
 __device__ double g2p_bilinear(double xk, double zk, const double *__restrict__ F, const double *__restrict__ X,
                                const double *__restrict__ Z, int Nx, int Nz, const signed char *__restrict__ tag,
                                double dx, double dz) {
-    int jp = lower_line(xk, X[0], dx);
+    const double idx = 1.0 / dx, idz = 1.0 / dz;
+    int jp = lower_line(xk, X[0], dx, idx);
     if (jp < 0) jp = 0;
     if (jp > Nx - 2) jp = Nx - 2;
-    int ip = lower_line(zk, Z[0], dz);
+    int ip = lower_line(zk, Z[0], dz, idz);
     if (ip < 0) ip = 0;
     if (ip > Nz - 2) ip = Nz - 2;
     double dxm = fabs(xk - X[jp]), dzm = fabs(zk - Z[ip]);
     int iSW = jp + ip * Nx, iSE = iSW + 1, iNW = jp + (ip + 1) * Nx, iNE = iNW + 1;
     double v = 0.0;
-    v += (1.0 - dxm / dx) * (1.0 - dzm / dz) * (air(tag[iSW]) ? F[iNW] : F[iSW]);
-    v += (dxm / dx) * (1.0 - dzm / dz) * (air(tag[iSE]) ? F[iNE] : F[iSE]);
-    v += (1.0 - dxm / dx) * (dzm / dz) * (air(tag[iNW]) ? F[iSW] : F[iNW]);
-    v += (dxm / dx) * (dzm / dz) * (air(tag[iNE]) ? F[iSE] : F[iNE]);
+    const double wx = dxm * idx, wz = dzm * idz;
+    v += (1.0 - wx) * (1.0 - wz) * (air(tag[iSW]) ? F[iNW] : F[iSW]);
+    v += wx * (1.0 - wz) * (air(tag[iSE]) ? F[iNE] : F[iSE]);
+    v += (1.0 - wx) * wz * (air(tag[iNW]) ? F[iSW] : F[iNW]);
+    v += wx * wz * (air(tag[iNE]) ? F[iSE] : F[iNE]);
     return v;
 }
 
@@ -479,8 +483,9 @@ __global__ void k_g2p_centroids_ext(int n, const double *__restrict__ mx, const 
     if (k >= n) return;
     if (mphase[k] == -1) { out[k] = 0.0; return; }
     double xk = mx[k], zk = mz[k];
-    int jp = lower_line(xk, xvz[0], dx);
-    int ip = lower_line(zk, zvx[0], dz);
+    const double idx = 1.0 / dx, idz = 1.0 / dz;
+    int jp = lower_line(xk, xvz[0], dx, idx);
+    int ip = lower_line(zk, zvx[0], dz, idz);
     int jw, je, is, in_;   // centroid columns west/east and rows south/north
     if (jp > 0 && jp < ncx) { jw = jp - 1; je = jp; }
     else if (jp <= 0) { jw = 0; je = 0; }
@@ -494,10 +499,11 @@ __global__ void k_g2p_centroids_ext(int n, const double *__restrict__ mx, const 
     int iz = ip < 0 ? 0 : (ip > ncz ? ncz : ip);
     double dxm = xk - xvz[jx], dzm = zk - zvx[iz];
     double v = 0.0;
-    v += (1.0 - dxm / dx) * (1.0 - dzm / dz) * (air(tag[iSW]) ? F[iNW] : F[iSW]);
-    v += (dxm / dx) * (1.0 - dzm / dz) * (air(tag[iSE]) ? F[iNE] : F[iSE]);
-    v += (1.0 - dxm / dx) * (dzm / dz) * (air(tag[iNW]) ? F[iSW] : F[iNW]);
-    v += (dxm / dx) * (dzm / dz) * (air(tag[iNE]) ? F[iSE] : F[iNE]);
+    const double wx = dxm * idx, wz = dzm * idz;
+    v += (1.0 - wx) * (1.0 - wz) * (air(tag[iSW]) ? F[iNW] : F[iSW]);
+    v += wx * (1.0 - wz) * (air(tag[iSE]) ? F[iNE] : F[iSE]);
+    v += (1.0 - wx) * wz * (air(tag[iNW]) ? F[iSW] : F[iNW]);
+    v += wx * wz * (air(tag[iNE]) ? F[iSE] : F[iNE]);
     out[k] = v;
 }
 
@@ -535,13 +541,14 @@ extern "C" mdz_status mdz_Interp_Grid2P(mdz_ctx *ctx, const double *node_field, 
 __device__ void v2p(double xk, double zk, const double *__restrict__ u, const double *__restrict__ v,
                     const double *__restrict__ xg, const double *__restrict__ zg, const double *__restrict__ zvx,
                     const double *__restrict__ xvz, int Nx, int Nz, const signed char *__restrict__ tu,
-                    const double dx, const double dz, const signed char *__restrict__ tv, double &vxm, double &vzm) {
+                    const double dx, const double dz, const double idx, const double idz,
+                    const signed char *__restrict__ tv, double &vxm, double &vzm) {
     // Vx: Nx x (Nz+1)
     {
         int nx = Nx, nz = Nz + 1;
-        int jp = lower_line(xk, xg[0], dx);
+        int jp = lower_line(xk, xg[0], dx, idx);
         jp = jp < 0 ? 0 : (jp > nx - 2 ? nx - 2 : jp);
-        int ip = lower_line(zk, zvx[0], dz);
+        int ip = lower_line(zk, zvx[0], dz, idz);
         ip = ip < 0 ? 0 : (ip > nz - 2 ? nz - 2 : ip);
         double dxm = fabs(xk - xg[jp]), dzm = fabs(zk - zvx[ip]);
         int iSW = jp + ip * nx, iSE = iSW + 1, iNW = jp + (ip + 1) * nx, iNE = iNW + 1;
@@ -552,16 +559,17 @@ __device__ void v2p(double xk, double zk, const double *__restrict__ u, const do
         if (tu[iNE] == 30) VNE = u[iSE];
         if (tu[iNE] == 30 && tu[iSE] == 30) { VNE = VSW; VSE = VSW; }
         if (tu[iNW] == 30 && tu[iSW] == 30) { VNW = VSE; VSW = VSE; }
-        double v13 = VSW * (1.0 - dxm / dx) + VSE * dxm / dx;
-        double v24 = VNW * (1.0 - dxm / dx) + VNE * dxm / dx;
-        vxm = (1.0 - dzm / dz) * v13 + (dzm / dz) * v24;
+        const double wx = dxm * idx, wz = dzm * idz;
+        double v13 = VSW * (1.0 - wx) + VSE * wx;
+        double v24 = VNW * (1.0 - wx) + VNE * wx;
+        vxm = (1.0 - wz) * v13 + wz * v24;
     }
     // Vz: (Nx+1) x Nz
     {
         int nx = Nx + 1, nz = Nz;
-        int jp = lower_line(xk, xvz[0], dx);
+        int jp = lower_line(xk, xvz[0], dx, idx);
         jp = jp < 0 ? 0 : (jp > nx - 2 ? nx - 2 : jp);
-        int ip = lower_line(zk, zg[0], dz);
+        int ip = lower_line(zk, zg[0], dz, idz);
         ip = ip < 0 ? 0 : (ip > nz - 2 ? nz - 2 : ip);
         double dxm = fabs(xk - xvz[jp]), dzm = fabs(zk - zg[ip]);
         int iSW = jp + ip * nx, iSE = iSW + 1, iNW = jp + (ip + 1) * nx, iNE = iNW + 1;
@@ -572,9 +580,10 @@ __device__ void v2p(double xk, double zk, const double *__restrict__ u, const do
         if (tv[iNE] == 30) VNE = v[iSE];
         if (tv[iNE] == 30 && tv[iSE] == 30) { VNE = VSW; VSE = VSW; }
         if (tv[iNW] == 30 && tv[iSW] == 30) { VNW = VSE; VSW = VSE; }
-        double v12 = VSW * (1.0 - dzm / dz) + VNW * dzm / dz;
-        double v34 = VSE * (1.0 - dzm / dz) + VNE * dzm / dz;
-        vzm = (1.0 - dxm / dx) * v12 + (dxm / dx) * v34;
+        const double wx = dxm * idx, wz = dzm * idz;
+        double v12 = VSW * (1.0 - wz) + VNW * wz;
+        double v34 = VSE * (1.0 - wz) + VNE * wz;
+        vzm = (1.0 - wx) * v12 + wx * v34;
     }
 }
 
@@ -589,17 +598,18 @@ __global__ void k_rk4(int n, double *__restrict__ mx, double *__restrict__ mz, i
     int ph = mphase[k];
     double xA = mx[k], zA = mz[k], x = xA, z = zA;
     double VxA = 0, VzA = 0, VxB = 0, VzB = 0, VxC = 0, VzC = 0, VxD = 0, VzD = 0;
+    const double idx = 1.0 / dx, idz = 1.0 / dz;
 #define OUT_CHECK() if (x < xmin || x > xmax || z < zmin || z > zmax) ph = -1;
-    if (ph != -1) v2p(x, z, u, v, xg, zg, zvx, xvz, Nx, Nz, tu, dx, dz, tv, VxA, VzA);
+    if (ph != -1) v2p(x, z, u, v, xg, zg, zvx, xvz, Nx, Nz, tu, dx, dz, idx, idz, tv, VxA, VzA);
     if (ph != -1) { x = xA + 0.5 * dt * VxA; z = zA + 0.5 * dt * VzA; }
     OUT_CHECK();
-    if (ph != -1) v2p(x, z, u, v, xg, zg, zvx, xvz, Nx, Nz, tu, dx, dz, tv, VxB, VzB);
+    if (ph != -1) v2p(x, z, u, v, xg, zg, zvx, xvz, Nx, Nz, tu, dx, dz, idx, idz, tv, VxB, VzB);
     if (ph != -1) { x = xA + 0.5 * dt * VxB; z = zA + 0.5 * dt * VzB; }
     OUT_CHECK();
-    if (ph != -1) v2p(x, z, u, v, xg, zg, zvx, xvz, Nx, Nz, tu, dx, dz, tv, VxC, VzC);
+    if (ph != -1) v2p(x, z, u, v, xg, zg, zvx, xvz, Nx, Nz, tu, dx, dz, idx, idz, tv, VxC, VzC);
     if (ph != -1) { x = xA + 1.0 * dt * VxC; z = zA + 1.0 * dt * VzC; }
     OUT_CHECK();
-    if (ph != -1) v2p(x, z, u, v, xg, zg, zvx, xvz, Nx, Nz, tu, dx, dz, tv, VxD, VzD);
+    if (ph != -1) v2p(x, z, u, v, xg, zg, zvx, xvz, Nx, Nz, tu, dx, dz, idx, idz, tv, VxD, VzD);
     VxA = (1.0 / 6.0) * (VxA + 2.0 * VxB + 2.0 * VxC + VxD);
     VzA = (1.0 / 6.0) * (VzA + 2.0 * VzB + 2.0 * VzC + VzD);
     if (ph != -1) {

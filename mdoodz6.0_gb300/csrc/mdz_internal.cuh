@@ -20,10 +20,25 @@ void mdz_prof_end(mdz_ctx *ctx, int cls, double bytes, cudaStream_t st, cudaEven
 struct mdz_dgrid {
     int Nx, Nz, ncx, ncz;
     double dx, dz, xmin, xmax, zmin, zmax;
+    double idx, idz;   // 1/dx, 1/dz (marker kernels multiply; see ceil_quot)
     double *xg, *zg, *xc, *zc, *xvz, *zvx;
     signed char *BCu, *BCv, *BCp, *BCg;
     double *BCu_val, *BCv_val;
 };
+
+// ceil(d / h + add) exactly as the correctly rounded quotient d / h gives it,
+// from the product with ih = 1/h: the two differ by a few units in the last
+// place, so only a value that close to an integer pays for the division.  An
+// FP64 division is a long instruction sequence on this part, and the marker
+// kernels take several per marker where the reference divides by the grid
+// spacing; the cell indices must still match the reference's bit for bit.
+__device__ __forceinline__ double ceil_quot(double d, double h, double ih, double add) {
+    const double q = d * ih + add;
+    const double c = ceil(q);
+    const double tol = 16.0 * 2.220446049250313e-16 * (fabs(q) + 1.0);
+    if (c - q > tol && q - (c - 1.0) > tol) return c;
+    return ceil(d / h + add);
+}
 
 // Marker store: structure of arrays, FP64 positions, int32 phases.
 struct mdz_markers {

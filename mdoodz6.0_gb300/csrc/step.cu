@@ -171,11 +171,11 @@ __global__ void k_marker_update(int n, mdz_dgrid g, const double *__restrict__ m
                                 double *__restrict__ strain, double *__restrict__ strain_pl) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n || mph[k] == -1) return;
-    const double x = mx[k], z = mz[k], dx = g.dx, dz = g.dz;
+    const double x = mx[k], z = mz[k], dx = g.dx, dz = g.dz, idx = g.idx, idz = g.idz;
     const int ncx = g.ncx, ncz = g.ncz, Nx = g.Nx, Nz = g.Nz;
     // centroids, ghosted frame (Interp_Grid2P_centroids2, non-periodic)
     {
-        int jp = (int)ceil((x - g.xvz[0]) / dx) - 1, ip = (int)ceil((z - g.zvx[0]) / dz) - 1;
+        int jp = (int)ceil_quot(x - g.xvz[0], dx, idx, 0.0) - 1, ip = (int)ceil_quot(z - g.zvx[0], dz, idz, 0.0) - 1;
         int jw = jp - 1, je = jp, is = ip - 1, in_ = ip;
         if (jp <= 0) { jw = 0; je = 0; }
         if (jp >= ncx) { jw = ncx - 1; je = ncx - 1; }
@@ -184,8 +184,9 @@ __global__ void k_marker_update(int n, mdz_dgrid g, const double *__restrict__ m
         int jx = jp < 0 ? 0 : (jp > ncx ? ncx : jp), iz = ip < 0 ? 0 : (ip > ncz ? ncz : ip);
         double dxm = x - g.xvz[jx], dzm = z - g.zvx[iz];
         int SW = jw + is * ncx, SE = je + is * ncx, NW = jw + in_ * ncx, NE = je + in_ * ncx;
-        double wSW = (1.0 - dxm / dx) * (1.0 - dzm / dz), wSE = (dxm / dx) * (1.0 - dzm / dz);
-        double wNW = (1.0 - dxm / dx) * (dzm / dz), wNE = (dxm / dx) * (dzm / dz);
+        const double wx = dxm * idx, wz = dzm * idz;
+        double wSW = (1.0 - wx) * (1.0 - wz), wSE = wx * (1.0 - wz);
+        double wNW = (1.0 - wx) * wz, wNE = wx * wz;
         const signed char *t = g.BCp;
         int sSW = is_air(t[SW]) ? NW : SW, sSE = is_air(t[SE]) ? NE : SE;
         int sNW = is_air(t[NW]) ? SW : NW, sNE = is_air(t[NE]) ? SE : NE;
@@ -194,32 +195,34 @@ __global__ void k_marker_update(int n, mdz_dgrid g, const double *__restrict__ m
     }
     // vertices (Interp_Grid2P)
     {
-        int jp = (int)ceil((x - g.xg[0]) / dx) - 1, ip = (int)ceil((z - g.zg[0]) / dz) - 1;
+        int jp = (int)ceil_quot(x - g.xg[0], dx, idx, 0.0) - 1, ip = (int)ceil_quot(z - g.zg[0], dz, idz, 0.0) - 1;
         jp = jp < 0 ? 0 : (jp > Nx - 2 ? Nx - 2 : jp);
         ip = ip < 0 ? 0 : (ip > Nz - 2 ? Nz - 2 : ip);
         double dxm = fabs(x - g.xg[jp]), dzm = fabs(z - g.zg[ip]);
         int SW = jp + ip * Nx, SE = SW + 1, NW = jp + (ip + 1) * Nx, NE = NW + 1;
         const signed char *t = g.BCg;
         double v = 0.0;
-        v += (1.0 - dxm / dx) * (1.0 - dzm / dz) * dsxz[is_air(t[SW]) ? NW : SW];
-        v += (dxm / dx) * (1.0 - dzm / dz) * dsxz[is_air(t[SE]) ? NE : SE];
-        v += (1.0 - dxm / dx) * (dzm / dz) * dsxz[is_air(t[NW]) ? SW : NW];
-        v += (dxm / dx) * (dzm / dz) * dsxz[is_air(t[NE]) ? SE : NE];
+        const double wx = dxm * idx, wz = dzm * idz;
+        v += (1.0 - wx) * (1.0 - wz) * dsxz[is_air(t[SW]) ? NW : SW];
+        v += wx * (1.0 - wz) * dsxz[is_air(t[SE]) ? NE : SE];
+        v += (1.0 - wx) * wz * dsxz[is_air(t[NW]) ? SW : NW];
+        v += wx * wz * dsxz[is_air(t[NE]) ? SE : NE];
         sxz[k] += v;
     }
     // strain increments on centroid lines (AccumulatedStrainII :235-350)
     {
-        int jp = (int)ceil((x - g.xc[0]) / dx) - 1, ip = (int)ceil((z - g.zc[0]) / dz) - 1;
+        int jp = (int)ceil_quot(x - g.xc[0], dx, idx, 0.0) - 1, ip = (int)ceil_quot(z - g.zc[0], dz, idz, 0.0) - 1;
         jp = jp < 0 ? 0 : (jp > ncx - 2 ? ncx - 2 : jp);
         ip = ip < 0 ? 0 : (ip > ncz - 2 ? ncz - 2 : ip);
         double dxm = x - g.xc[jp], dzm = z - g.zc[ip];
         int SW = jp + ip * ncx, SE = SW + 1, NW = jp + (ip + 1) * ncx, NE = NW + 1;
         const signed char *t = g.BCp;
         double e = 0, ep = 0, s = 0, w;
-        if (!is_air(t[SW])) { w = (1.0 - dxm / dx) * (1.0 - dzm / dz); e += w * dstrain[SW]; ep += w * dstrain_pl[SW]; s += w; }
-        if (!is_air(t[SE])) { w = (dxm / dx) * (1.0 - dzm / dz); e += w * dstrain[SE]; ep += w * dstrain_pl[SE]; s += w; }
-        if (!is_air(t[NW])) { w = (1.0 - dxm / dx) * (dzm / dz); e += w * dstrain[NW]; ep += w * dstrain_pl[NW]; s += w; }
-        if (!is_air(t[NE])) { w = (dxm / dx) * (dzm / dz); e += w * dstrain[NE]; ep += w * dstrain_pl[NE]; s += w; }
+        const double wx = dxm * idx, wz = dzm * idz;
+        if (!is_air(t[SW])) { w = (1.0 - wx) * (1.0 - wz); e += w * dstrain[SW]; ep += w * dstrain_pl[SW]; s += w; }
+        if (!is_air(t[SE])) { w = wx * (1.0 - wz); e += w * dstrain[SE]; ep += w * dstrain_pl[SE]; s += w; }
+        if (!is_air(t[NW])) { w = (1.0 - wx) * wz; e += w * dstrain[NW]; ep += w * dstrain_pl[NW]; s += w; }
+        if (!is_air(t[NE])) { w = wx * wz; e += w * dstrain[NE]; ep += w * dstrain_pl[NE]; s += w; }
         if (s > 1e-13) { e /= s; ep /= s; }
         strain[k] += e;
         strain_pl[k] += ep;
