@@ -113,6 +113,7 @@ def train_guess(ctx, cfg, n=1 << 20, batch=65536, seed=1):
 
 
 def run_form(cfg_builder, precision, learned, steps, warmup, size):
+    import numpy as np
     import mdz
     import mdz_setups
     cfg = cfg_builder(precision, learned, size)
@@ -133,8 +134,25 @@ def run_form(cfg_builder, precision, learned, steps, warmup, size):
     launches = ctx.kernel_launches - l0
     gpu_ms = sum(r["ms_total"] for r in reps) / steps
     kern = ctx.kernel_timing()
+    g = cfg["grid"]
+    final = {"u": np.empty(g.size(-1)), "v": np.empty(g.size(-2)), "p": np.empty(g.size(1))}
+    ctx._check(ctx.L.mdz_get_velocity(ctx.h, mdz._dptr(final["u"]), mdz._dptr(final["v"]), mdz._dptr(final["p"])))
+    final["sxxd"] = ctx.get_marker_attr(mdz.M_SXXD)
+    final["sxz"] = ctx.get_marker_attr(mdz.M_SXZ)
     ctx.close()
-    return dict(ms_wall=wall, ms_gpu=gpu_ms, reports=reps, launches=launches, kernel=kern, cfg=cfg, train=train)
+    return dict(ms_wall=wall, ms_gpu=gpu_ms, reports=reps, launches=launches, kernel=kern, cfg=cfg, train=train,
+                final=final)
+
+
+def field_diffs(a, b):
+    import numpy as np
+    out = {}
+    for k in a:
+        x, y = a[k], b[k]
+        if k == "p":
+            x, y = x - x.mean(), y - y.mean()
+        out[k] = float(np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-300))
+    return out
 
 
 def mlp_workload():
@@ -325,7 +343,10 @@ def main():
                   "speedup_vs_plain_fp64": plain["ms_wall"] / fast["ms_wall"],
                   "plain_report": plain["reports"][-1], "learned_fp32_ir_report": fast["reports"][-1],
                   "guess_training_s": fast["train"][0], "guess_training_loss": fast["train"][1],
-                  "plain_fp64_classes": plain["kernel"]["classes"], "learned_fp32_ir_classes": fast["kernel"]["classes"]},
+                  "plain_fp64_classes": plain["kernel"]["classes"], "learned_fp32_ir_classes": fast["kernel"]["classes"],
+                  # relative 2-norm difference of each output field after the same steps (pressure
+                  # with its mean removed: the operator leaves it undetermined)
+                  "field_rel_diff_fp32_vs_fp64": field_diffs(fast["final"], plain["final"])},
         "e2e": {"value": e2e_ms, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "split": e2e_split},
         "gpu_launches": fast["launches"] // args.steps,
