@@ -194,32 +194,33 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     // sequence on this part, and the iterations below would take six each
     const double iEii = 1.0 / Eii, i2eta_el = 0.5 / eta_el, ifcst = constant ? 0.5 / (f_ani * eta_cst) : 0.0;
     if (guess) {
-        // Learned start eta = eta_up exp(y0) (the network predicts
-        // y0 = ln(eta_ve / eta_up), eta_up being the reference's start, the
-        // smallest viscosity of the active mechanisms; a start needs no FP64
-        // exp), polished by Halley steps on the reference's residual
-        // f(eta) = Eii - sum_k E_k(eta), every rate E_k = c_k eta^n_k, so with
-        // S0 = sum E_k, S1 = sum n_k E_k, S2 = sum n_k (n_k - 1) E_k:
-        // eta <- eta + 2 f S1 eta / (2 S1^2 + f S2).  Converged means the
-        // reference's own test below holds.
-        eta_ve = eta_up * (double)expf(guess[0]);
+        // Learned start s = log(eta_ve), polished by Halley steps on
+        // g(s) = log(sum of the strain rates) - log(Eii): every mechanism's
+        // rate is c_k exp(n_k s), so g' and g'' are rate-weighted means of n_k
+        // and n_k^2 (in s the residual is nearly linear; Halley in eta itself
+        // left 39 % of the solves unconverged after two steps).  Converged
+        // means the reference's own test below holds.  The network predicts
+        // ln(eta_ve / eta_up), eta_up being the reference's start (the
+        // smallest viscosity of the active mechanisms).
+        double s = log(eta_up) + (double)guess[0];
         for (it = 0; it <= MDZ_POLISH_STEPS; it++) {
+            eta_ve = exp(s);
             Tii = 2.0 * f_ani * eta_ve * Eii;
             const double Eel = elastic ? Tii * i2eta_el : 0.0;
             if (constant) Eii_cst = Tii * ifcst;
             if (dislocation) Eii_pwl = C_pwl * fpow(Tii, n_pwl);
             if (diffusion) Eii_lin = C_lin * fpow(Tii, n_lin) * dm_lin;
             const double S0 = Eel + Eii_pwl + Eii_lin + Eii_cst;
-            const double r = Eii - S0;
-            res = fabs(r * iEii);
+            res = fabs((Eii - S0) * iEii);
             if (res < tol / 100) { ve_done = true; break; }
             if (it == MDZ_POLISH_STEPS) break;
+            if (!(S0 > 0.0)) break;
             const double S1 = Eel + n_pwl * Eii_pwl + n_lin * Eii_lin + Eii_cst;
-            const double S2 = n_pwl * (n_pwl - 1.0) * Eii_pwl + n_lin * (n_lin - 1.0) * Eii_lin;
-            const double den = 2.0 * S1 * S1 + r * S2;
-            const double eta_n = eta_ve + (den > 0.0 ? 2.0 * r * S1 * eta_ve / den : r * eta_ve / S1);
-            if (!(eta_n > 0.0)) break;
-            eta_ve = eta_n;
+            const double S2 = Eel + n_pwl * n_pwl * Eii_pwl + n_lin * n_lin * Eii_lin + Eii_cst;
+            const double iS0 = 1.0 / S0;
+            const double g = log(S0 * iEii), g1 = S1 * iS0, g2 = S2 * iS0 - g1 * g1;
+            const double den = 2.0 * g1 * g1 - g * g2;
+            s -= den > 0.0 ? 2.0 * g * g1 / den : g / g1;
         }
         o.ve_its = it;
         if (!ve_done) {

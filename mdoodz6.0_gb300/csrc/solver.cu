@@ -158,7 +158,7 @@ __global__ void k_mg_diag(stokes_geom G, const T *__restrict__ D11, const T *__r
     int Nx = G.Nx, Nz = G.Nz, ncx = G.ncx, nu = Nx * (Nz + 1), nv = (Nx + 1) * Nz;
     // in the level's precision, with 1/dx^2, 1/dz^2 precomputed (FP64
     // divisions are long instruction sequences on this part)
-    const T celvol = (T)(G.dx * G.dz), idx2 = (T)(G.idx * G.idx), idz2 = (T)(G.idz * G.idz);
+    const T celvol = gc<T>(G, GC_CELVOL), idx2 = gc<T>(G, GC_IXX), idz2 = gc<T>(G, GC_IZZ);
     if (i < nu) {
         int k = i % Nx, l = i / Nx;
         T d = 0;
@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(256) k_mg_smooth(stokes_geom G, stokes_coefs<T
                                                    T *__restrict__ ov) {
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     const int Nx = G.Nx, Nz = G.Nz;
-    const T celvol = (T)(G.dx * G.dz);
+    const T celvol = gc<T>(G, GC_CELVOL);
     stokes_cvec<T> x{xu, xv, nullptr};
     if (i < Nx && j <= Nz) {
         int c = i + j * Nx;
@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(256) k_mg_residual(stokes_geom G, stokes_coefs
                                                      T *__restrict__ rv) {
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     const int Nx = G.Nx, Nz = G.Nz;
-    const T celvol = (T)(G.dx * G.dz);
+    const T celvol = gc<T>(G, GC_CELVOL);
     stokes_cvec<T> x{xu, xv, nullptr};
     if (i < Nx && j <= Nz) {
         int c = i + j * Nx;
@@ -562,7 +562,7 @@ __global__ void __launch_bounds__(256) k_mg_apply(stokes_geom G, stokes_coefs<T>
                                                   T *__restrict__ yu, T *__restrict__ yv) {
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     const int Nx = G.Nx, Nz = G.Nz;
-    const T celvol = (T)(G.dx * G.dz);
+    const T celvol = gc<T>(G, GC_CELVOL);
     stokes_cvec<T> x{xu, xv, NEWTON ? p0 : nullptr};
     if (i < Nx && j <= Nz) {
         int c = i + j * Nx;
@@ -634,8 +634,8 @@ __global__ void __launch_bounds__(256) k_picard_stencil(stokes_geom G, const T *
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     const int Nx = G.Nx, Nz = G.Nz, nx = Nx, ncx = G.ncx, nxvz = Nx + 1;
     const size_t nu = (size_t)Nx * (Nz + 1), nv = (size_t)(Nx + 1) * Nz;
-    const T celvol = (T)(G.dx * G.dz), ixx = (T)(G.idx * G.idx), izz = (T)(G.idz * G.idz),
-            ixz = (T)(G.idx * G.idz);
+    const T celvol = gc<T>(G, GC_CELVOL), ixx = gc<T>(G, GC_IXX), izz = gc<T>(G, GC_IZZ),
+            ixz = gc<T>(G, GC_IXZ);
     if (i < Nx && j <= Nz) {   // u-row (k, l) = (i, j)
         const int k = i, l = j, c1 = k + l * nx;
         T a[MG_NST];
@@ -1584,14 +1584,30 @@ static mdz_status vcycle(mdz_ctx *ctx, mg_hier<T> &H, int l, int nu1, int nu2, T
 
 // ---------------------------------------------------------------------------
 // Pressure mean over the pressure equations (sum, count) and its removal.
+// (sum in the vector's precision and an integer count per block, block totals
+// added in FP64: no FP64 instruction per element)
 template <typename T>
-__global__ void k_psum(int np, const signed char *__restrict__ tp, const T *__restrict__ p, double *out) {
-    double acc[2] = {0.0, 0.0};
+__global__ void __launch_bounds__(256) k_psum(int np, const signed char *__restrict__ tp, const T *__restrict__ p,
+                                              double *out) {
+    T acc = 0;
+    int cnt = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x)
-        if (tp[i] == -1) { acc[0] += (double)p[i]; acc[1] += 1.0; }
-    for (int q = 0; q < 2; q++)
-        for (int o = 16; o > 0; o >>= 1) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
-    if ((threadIdx.x & 31) == 0) { atomicAdd(&out[0], acc[0]); atomicAdd(&out[1], acc[1]); }
+        if (tp[i] == -1) { acc += p[i]; cnt++; }
+    for (int o = 16; o > 0; o >>= 1) {
+        acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    }
+    __shared__ T sa[8];
+    __shared__ int sn[8];
+    if ((threadIdx.x & 31) == 0) { sa[threadIdx.x >> 5] = acc; sn[threadIdx.x >> 5] = cnt; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        T a = 0;
+        int c = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) { a += sa[w]; c += sn[w]; }
+        atomicAdd(&out[0], (double)a);
+        atomicAdd(&out[1], (double)c);
+    }
 }
 
 // (the mean in the vector's precision: an FP64 division per thread is a long
@@ -1604,12 +1620,12 @@ __global__ void k_psub(int np, const signed char *__restrict__ tp, const double 
 
 // ---------------------------------------------------------------------------
 // Block preconditioner: zp = (eta_n / celvol) rp ; zu = V-cycle(ru - B zp).
+// (eta_n / celvol from the level-0 copy D11 = 2 eta_n in precision T)
 template <typename T>
-__global__ void k_precond_p(stokes_geom G, const double *__restrict__ eta_n, const T *__restrict__ rp,
-                            T *__restrict__ zp) {
+__global__ void k_precond_p(stokes_geom G, const T *__restrict__ D11, const T *__restrict__ rp, T *__restrict__ zp) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= G.ncx * G.ncz) return;
-    zp[i] = G.BCp[i] == -1 ? (T)(eta_n[i] * (G.idx * G.idz)) * rp[i] : T(0);
+    zp[i] = G.BCp[i] == -1 ? T(0.5) * gc<T>(G, GC_IXZ) * D11[i] * rp[i] : T(0);
 }
 
 // f = r_vel - B zp  on the fine MG level (B: celvol-scaled pressure gradient)
@@ -1623,7 +1639,7 @@ __global__ void k_precond_rhs(stokes_geom G, const T *__restrict__ ru, const T *
         T r = 0;
         if (G.BCu[c] == -1) {
             int c2 = i - 1 + (j - 1) * ncx;
-            r = ru[c] - (T)G.dz * (zp[c2 + 1] - zp[c2]);
+            r = ru[c] - gc<T>(G, GC_DZ) * (zp[c2 + 1] - zp[c2]);
         }
         fu[c] = r;
     }
@@ -1632,7 +1648,7 @@ __global__ void k_precond_rhs(stokes_geom G, const T *__restrict__ ru, const T *
         T r = 0;
         if (G.BCv[c] == -1) {
             int c2 = i - 1 + (j - 1) * ncx;
-            r = rv[c] - (T)G.dx * (zp[c2 + ncx] - zp[c2]);
+            r = rv[c] - gc<T>(G, GC_DX) * (zp[c2 + ncx] - zp[c2]);
         }
         fv[c] = r;
     }
@@ -1652,7 +1668,7 @@ static mdz_status precondition(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n,
     mg_level<T> &F = H.L[0];
     stokes_geom G = F.geom();
     const int np = F.ncx * F.ncz;
-    k_precond_p<T><<<mdz_blocks(np), MDZ_THREADS, 0, st>>>(G, eta_n, r + nu + nv, z + nu + nv);
+    k_precond_p<T><<<mdz_blocks(np), MDZ_THREADS, 0, st>>>(G, F.D11, r + nu + nv, z + nu + nv);
     MDZ_LAUNCHED(ctx);
     // zero-mean pressure block: constants are the operator's null space; left
     // in, they grow in the iterates and cost the FP32 gradients their accuracy

@@ -57,7 +57,7 @@ template <typename T>
 void stokes_apply_launch(const stokes_geom &G, const stokes_coefs<T> &D, stokes_cvec<T> x, stokes_vec<T> y,
                          const stokes_cvec<T> *b, bool newton, cudaStream_t st) {
     dim3 bl(32, 8), gr((G.Nx + 1 + 31) / 32, (G.Nz + 1 + 7) / 8);
-    T celvol = (T)(G.dx * G.dz);
+    T celvol = gc<T>(G, GC_CELVOL);
     stokes_cvec<T> bb = b ? *b : stokes_cvec<T>{nullptr, nullptr, nullptr};
     if (b) {
         if (newton) k_stokes_apply<T, true, true><<<gr, bl, 0, st>>>(G, D, x, y, bb, celvol);

@@ -40,17 +40,33 @@ struct stokes_cvec {
     const T *u, *v, *p;
 };
 
+// geometry constants in both precisions (gc<T>): a kernel in FP32 must not
+// convert an FP64 constant per thread, FP64 conversions issue at a small
+// fraction of the FP32 rate on this part
+enum { GC_DX = 0, GC_DZ, GC_IDX, GC_IDZ, GC_CELVOL, GC_IXX, GC_IZZ, GC_IXZ, GC_N };
+
 struct stokes_geom {
     int Nx, Nz, ncx, ncz;
     double dx, dz;
     const signed char *BCu, *BCv, *BCp, *BCg;
     double idx, idz;   // 1/dx, 1/dz: the stencils multiply (a division costs a
                        // long FP64 instruction sequence on this part)
+    double cd[GC_N];
+    float cf[GC_N];
 };
+
+template <typename T>
+__host__ __device__ __forceinline__ T gc(const stokes_geom &G, int k) {
+    if constexpr (sizeof(T) == 8) return G.cd[k];
+    else return G.cf[k];
+}
 
 inline stokes_geom make_geom(int Nx, int Nz, double dx, double dz, const signed char *BCu, const signed char *BCv,
                              const signed char *BCp, const signed char *BCg) {
-    return stokes_geom{Nx, Nz, Nx - 1, Nz - 1, dx, dz, BCu, BCv, BCp, BCg, 1.0 / dx, 1.0 / dz};
+    stokes_geom G{Nx, Nz, Nx - 1, Nz - 1, dx, dz, BCu, BCv, BCp, BCg, 1.0 / dx, 1.0 / dz, {0}, {0}};
+    const double c[GC_N] = {dx, dz, 1.0 / dx, 1.0 / dz, dx * dz, 1.0 / (dx * dx), 1.0 / (dz * dz), 1.0 / (dx * dz)};
+    for (int k = 0; k < GC_N; k++) { G.cd[k] = c[k]; G.cf[k] = (float)c[k]; }
+    return G;
 }
 
 // 1/w for the averaging weights w in {2, 3, 4}; w in {0, 1} stays (exact
@@ -66,7 +82,7 @@ __device__ __forceinline__ T xrow(const stokes_geom &G, const stokes_coefs<T> &D
                                   int l) {
     const int nx = G.Nx, ncx = G.ncx, nxvz = nx + 1;
     const int c1 = k + l * nx, c2 = k - 1 + (l - 1) * ncx, c3 = k + l * nxvz;
-    const T idx = (T)G.idx, idz = (T)G.idz;
+    const T idx = gc<T>(G, GC_IDX), idz = gc<T>(G, GC_IDZ);
     const int iPrW = c2, iPrE = c2 + 1, ixyN = c1, ixyS = c1 - nx;
     const T inW = G.BCp[iPrW] == -1 ? T(1) : T(0), inE = G.BCp[iPrE] == -1 ? T(1) : T(0);
     const T inS = (G.BCg[ixyS] != 30 && G.BCu[c1 - nx] != 13) ? T(1) : T(0);
@@ -152,7 +168,7 @@ __device__ __forceinline__ T zrow(const stokes_geom &G, const stokes_coefs<T> &D
                                   int l) {
     const int nx = G.Nx, ncx = G.ncx, nxvz = nx + 1;
     const int c3 = k + l * nxvz, c1 = k + l * nx, c2 = k - 1 + (l - 1) * ncx;
-    const T idx = (T)G.idx, idz = (T)G.idz;
+    const T idx = gc<T>(G, GC_IDX), idz = gc<T>(G, GC_IDZ);
     const int iPrS = c2, iPrN = c2 + ncx, ixyW = c1 - 1, ixyE = c1;
     T inS = 0, inN = 0;
     if (G.BCv[c3 - nxvz] != 30 && G.BCv[c3 + nxvz] != 30) { inS = 1; inN = 1; }
@@ -240,7 +256,7 @@ template <typename T>
 __device__ __forceinline__ T crow(const stokes_geom &G, const stokes_cvec<T> &x, int k, int l) {
     const int nx = G.Nx, nxvz = nx + 1;
     const int c1 = k + (l + 1) * nx, c3 = k + l * nxvz + 1;
-    const T idx = (T)G.idx, idz = (T)G.idz;
+    const T idx = gc<T>(G, GC_IDX), idz = gc<T>(G, GC_IDZ);
     T r = 0;
     if (G.BCu[c1] != 13) r += -x.u[c1] * idx;
     if (G.BCu[c1 + 1] != 13) r += x.u[c1 + 1] * idx;
