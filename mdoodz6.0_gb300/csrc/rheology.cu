@@ -150,25 +150,31 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     if (Eii * prm.scale_E < 1e-30) Eii = 1e-30 / prm.scale_E;
     if (Gii * prm.scale_E < 1e-30) Gii = 1e-30 / prm.scale_E;
     const double f_ani = Gii / Eii;
+    // reciprocals taken once per solve: an FP64 division is a long instruction
+    // sequence on this part, and the reference's formulas divide some fifty
+    // times per local solve
+    const double iEii = 1.0 / Eii, iGii = 1.0 / Gii;
     o.Pcorr = P;
     if (prm.step == 0) elastic = 0;
     o.d1 = m.gs_ref[p];
     if (elastic == 0) { G = 1e1; K = 1e1; dil = 0.0; }
     if (T < ZEROC / prm.scale_T) T = ZEROC / prm.scale_T;
+    const double iRT = 1.0 / (R * T);
     if (dislocation) {
-        double B_pwl = m.pref_pwl[p] * m.Fpwl[p] * fpow(m.Apwl[p], -1.0 / n_pwl) *
-                       exp((m.Qpwl[p] + P * Va_pwl) / R / n_pwl / T) * fpow(d, m.mpwl[p] / n_pwl) *
-                       fpow(m.fpwl[p], -m.rpwl[p] / n_pwl) * fexp(-m.apwl[p] * phi / n_pwl);
+        const double in = 1.0 / n_pwl;
+        double B_pwl = m.pref_pwl[p] * m.Fpwl[p] * fpow(m.Apwl[p], -in) * exp((m.Qpwl[p] + P * Va_pwl) * iRT * in) *
+                       fpow(d, m.mpwl[p] * in) * fpow(m.fpwl[p], -m.rpwl[p] * in) * fexp(-m.apwl[p] * phi * in);
         C_pwl = fpow(2.0 * f_ani * B_pwl, -n_pwl);
-        dCpwldP = -C_pwl * Va_pwl / R / T;
-        eta_pwl = B_pwl * fpow(Eii, 1.0 / n_pwl - 1.0);
+        dCpwldP = -C_pwl * Va_pwl * iRT;
+        eta_pwl = B_pwl * fpow(Eii, in - 1.0);
     }
     if (diffusion) {
-        B_lin = m.Flin[p] * fpow(m.Alin[p], -1.0 / n_lin) * exp((m.Qlin[p] + P * m.Vlin[p]) / R / n_lin / T) *
-                fpow(m.flin[p], -m.rlin[p] / n_lin) * fexp(-m.alin[p] * phi / n_lin);
+        const double in = 1.0 / n_lin;
+        B_lin = m.Flin[p] * fpow(m.Alin[p], -in) * exp((m.Qlin[p] + P * m.Vlin[p]) * iRT * in) *
+                fpow(m.flin[p], -m.rlin[p] * in) * fexp(-m.alin[p] * phi * in);
         C_lin = fpow(2.0 * f_ani * B_lin, -n_lin);
-        dClindP = -C_lin * m.Vlin[p] / R / T;
-        eta_lin = B_lin * fpow(Eii, 1.0 / n_lin - 1.0) * fpow(d, m_lin / n_lin);
+        dClindP = -C_lin * m.Vlin[p] * iRT;
+        eta_lin = B_lin * fpow(Eii, in - 1.0) * fpow(d, m_lin * in);
     }
     double cos_fric, sin_fric;
     sincos(fric, &sin_fric, &cos_fric);
@@ -190,9 +196,7 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     o.eta_up = eta_up;
     o.learned = guess != nullptr;
     o.fallback = 0;
-    // reciprocals taken once per solve: an FP64 division is a long instruction
-    // sequence on this part, and the iterations below would take six each
-    const double iEii = 1.0 / Eii, i2eta_el = 0.5 / eta_el, ifcst = constant ? 0.5 / (f_ani * eta_cst) : 0.0;
+    const double i2eta_el = 0.5 / eta_el, ifcst = constant ? 0.5 / (f_ani * eta_cst) : 0.0;
     if (guess) {
         // Learned start s = log(eta_ve), polished by Halley steps on
         // g(s) = log(sum of the strain rates) - log(Eii): every mechanism's
@@ -256,25 +260,32 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     const bool pwl_fresh = dislocation && (ve_done || res < tol / 100) && C_pwl > 0.0 && Eii_pwl > 0.0;
     Tii = 2.0 * eta_ve * f_ani * Eii;
     const double Tn = !dislocation ? 0.0 : (pwl_fresh ? Eii_pwl / C_pwl : fpow(Tii, n_pwl));   // Tii^n_pwl
-    double Txx = Gxx * Tii / f_ani / Eii, Tzz = Gzz * Tii / f_ani / Eii, Txz = Gxz * Tii / f_ani / Eii;
+    const double iTii = 1.0 / Tii, TG = Tii * iGii;   // Tii / (f_ani Eii) = Tii / Gii
+    double Txx = Gxx * TG, Tzz = Gzz * TG, Txz = Gxz * TG;
     double Exx_lin = 0, Ezz_lin = 0, Exz_lin = 0, Exx_cst = 0, Ezz_cst = 0, Exz_cst = 0;
-    if (dislocation) eta_pwl = fpow(2.0 * C_pwl, -1.0) * (Tii / Tn);   // (2 C)^-1 Tii^(1-n)
+    if (dislocation) eta_pwl = Tii / (2.0 * C_pwl * Tn);   // (2 C)^-1 Tii^(1-n)
     if (diffusion) {
-        eta_lin = B_lin * fpow(Eii_lin, 1.0 / n_lin - 1.0) * fpow(o.d1, m_lin / n_lin);
-        Exx_lin = Txx / 2.0 / eta_lin; Ezz_lin = Tzz / 2.0 / eta_lin; Exz_lin = Txz / 2.0 / eta_lin;
+        const double in = 1.0 / n_lin;
+        eta_lin = B_lin * fpow(Eii_lin, in - 1.0) * fpow(o.d1, m_lin * in);
+        const double h = 0.5 / eta_lin;
+        Exx_lin = Txx * h; Ezz_lin = Tzz * h; Exz_lin = Txz * h;
     }
-    if (constant) { Exx_cst = Txx / 2.0 / eta_cst; Ezz_cst = Tzz / 2.0 / eta_cst; Exz_cst = Txz / 2.0 / eta_cst; }
+    if (constant) {
+        const double h = 0.5 / eta_cst;
+        Exx_cst = Txx * h; Ezz_cst = Tzz * h; Exz_cst = Txz * h;
+    }
     // visco-elastic tangent
     double deta = 0.0;
-    if (dislocation) deta += -C_pwl * (Tn / (Tii * Tii * Tii)) * (n_pwl - 1.0);   // Tii^(n-3)
+    if (dislocation) deta += -C_pwl * (Tn * iTii * iTii * iTii) * (n_pwl - 1.0);   // Tii^(n-3)
     if (diffusion) deta += -C_lin * fpow(Tii, n_lin - 3.0) * (n_lin - 1.0) * dm_lin;
     const double e2 = fpow(eta_ve, 2.0);
     double dTxx = deta * (2.0 * Txx + Tzz) * e2, dTzz = deta * (2.0 * Tzz + Txx) * e2, dTxz = 2.0 * deta * Txz * e2;
     double den = 1.0 - 2.0 * (dTxx * Exx + dTzz * Ezz + dTxz * Exz);
-    double dve_dExx = dTxx * 2.0 * eta_ve / den, dve_dEzz = dTzz * 2.0 * eta_ve / den;
-    double dve_dExz = dTxz * 2.0 * eta_ve / den;
+    const double e2den = 2.0 * eta_ve / den;
+    double dve_dExx = dTxx * e2den, dve_dEzz = dTzz * e2den;
+    double dve_dExz = dTxz * e2den;
     double dummy = 0.0, Jii = Tii * Tii;
-    if (dislocation) dummy += -2.0 * (Tn / Tii) * dCpwldP;   // Jii^((n-1)/2) = Tii^(n-1)
+    if (dislocation) dummy += -2.0 * (Tn * iTii) * dCpwldP;   // Jii^((n-1)/2) = Tii^(n-1)
     if (diffusion) dummy += -2.0 * fpow(Jii, (1.0 / 2.0) * n_lin - 1.0 / 2.0) * fpow(d, -m_lin) * dClindP;
     double dve_dP = fpow(eta_ve, 2) * dummy;
     // plastic return mapping on gdot
@@ -284,10 +295,11 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     double F_trial = Tii - Tyield;
     const bool is_pl = F_trial > 1e-17;
     if (is_pl) {
-        eta_vp = eta_vp0 * fpow(Eii, 1.0 / n_vp - 1);
+        const double in_vp = 1.0 / n_vp;
+        eta_vp = eta_vp0 * fpow(Eii, in_vp - 1);
         gdot = F_trial / (eta_ve + eta_vp + K * dt * sin_fric * sin_dil);
-        dQdtxx = Txx / 2.0 / Tii; dQdtzz = Tzz / 2.0 / Tii; dQdtxz = Txz / 1.0 / Tii;
-        const double F_trial0 = F_trial;
+        dQdtxx = Txx * 0.5 * iTii; dQdtzz = Tzz * 0.5 * iTii; dQdtxz = Txz * iTii;
+        const double F_trial0 = F_trial, iF0 = 1.0 / F_trial0;
         bool vp_done = false;
         if (guess) {
             // learned start: gdot = fraction * 2 Eii, at most MDZ_POLISH_STEPS
@@ -300,13 +312,13 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
                 dQdP = -sin_dil;
                 divp = -gdot * dQdP;
                 Pc = P + K * dt * divp;
-                eta_vp = eta_vp0 * fpow(fabs(gdot), 1.0 / n_vp - 1.0);
+                eta_vp = eta_vp0 * fpow(fabs(gdot), in_vp - 1.0);
                 Tyield = C * cos_fric + Pc * sin_fric + gdot * eta_vp;
                 F_trial = Tii - eta_ve * gdot - Tyield;
                 res = fabs(F_trial);
-                if (res < tol || res / F_trial0 < tol) { vp_done = true; break; }
+                if (res < tol || res * iF0 < tol) { vp_done = true; break; }
                 if (it == MDZ_POLISH_STEPS) break;
-                double dFdgdot = -eta_ve - eta_vp / n_vp - K * dt * sin_fric * sin_dil;
+                double dFdgdot = -eta_ve - eta_vp * in_vp - K * dt * sin_fric * sin_dil;
                 gdot -= F_trial / dFdgdot;
             }
             o.vp_its = it;
@@ -319,46 +331,49 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
             dQdP = -sin_dil;
             divp = -gdot * dQdP;
             Pc = P + K * dt * divp;
-            eta_vp = eta_vp0 * fpow(fabs(gdot), 1.0 / n_vp - 1.0);
+            eta_vp = eta_vp0 * fpow(fabs(gdot), in_vp - 1.0);
             Tyield = C * cos_fric + Pc * sin_fric + gdot * eta_vp;
             F_trial = Tii - eta_ve * gdot - Tyield;
             res = fabs(F_trial);
-            if (res < tol || res / F_trial0 < tol) break;
-            double dFdgdot = -eta_ve - eta_vp / n_vp - K * dt * sin_fric * sin_dil;
+            if (res < tol || res * iF0 < tol) break;
+            double dFdgdot = -eta_ve - eta_vp * in_vp - K * dt * sin_fric * sin_dil;
             gdot -= F_trial / dFdgdot;
         }
         if (!vp_done) {
             o.vp_its = it + (guess ? MDZ_POLISH_STEPS : 0);
-            if (it == nitmax - 1 && (res > tol || res / F_trial0 > tol)) o.vp_fail = 1;
+            if (it == nitmax - 1 && (res > tol || res * iF0 > tol)) o.vp_fail = 1;
         }
         Txx = 2.0 * eta_ve * (Exx - gdot * dQdtxx);
         Tzz = 2.0 * eta_ve * (Ezz - gdot * dQdtzz);
         double Tyy = -(Txx + Tzz);
         Txz = 2.0 * eta_ve * (Exz - gdot * dQdtxz / 2.0);
         Tii = sqrt(0.5 * (fpow(Txx, 2.0) + fpow(Tzz, 2.0) + fpow(Tyy, 2.0)) + fpow(Txz, 2.0));
-        eta_vep = Tii / (2.0 * Eii);
+        eta_vep = Tii * 0.5 * iEii;
         o.Eii_pl = gdot / 2.0;
         Tii = 2.0 * eta_vep * Eii;
         o.OverS = eta_vp * gdot;
         o.Pcorr = Pc;
         // visco-elasto-plastic tangent
-        double dFdExx = (2.0 * Exx + Ezz) * eta_ve / Eii + 2.0 * Eii * dve_dExx;
-        double dFdEzz = (2.0 * Ezz + Exx) * eta_ve / Eii + 2.0 * Eii * dve_dEzz;
-        double dFdExz = 2.0 * Exz * eta_ve / Eii + 2.0 * Eii * dve_dExz;
+        const double ev = eta_ve * iEii;
+        double dFdExx = (2.0 * Exx + Ezz) * ev + 2.0 * Eii * dve_dExx;
+        double dFdEzz = (2.0 * Ezz + Exx) * ev + 2.0 * Eii * dve_dEzz;
+        double dFdExz = 2.0 * Exz * ev + 2.0 * Eii * dve_dExz;
         double dFdP = -sin_fric + 2.0 * Eii * dve_dP;
-        double gg = 1.0 / (eta_ve + eta_vp / n_vp + K * dt * sin_fric * sin_dil);
+        double gg = 1.0 / (eta_ve + eta_vp * in_vp + K * dt * sin_fric * sin_dil);
         dlamdExx = gg * (dFdExx - gdot * (dve_dExx + K * dt * sin_fric * 0.0));
         dlamdEzz = gg * (dFdEzz - gdot * (dve_dEzz + K * dt * sin_fric * 0.0));
         dlamdExz = gg * (dFdExz - gdot * (dve_dExz + K * dt * sin_fric * 0.0));
         dlamdP = gg * (dFdP - gdot * (dve_dP + K * dt * sin_fric * 0.0));
-        double q = 1.0 / n_vp - 1.0;
-        double dvp_dExx = eta_vp / gdot * dlamdExx * q, dvp_dEzz = eta_vp / gdot * dlamdEzz * q;
-        double dvp_dExz = eta_vp / gdot * dlamdExz * q, dvp_dP = eta_vp / gdot * dlamdP * q;
-        double a = eta_vp + K * dt * sin_fric * sin_dil, E3 = 2.0 * fpow(Eii, 3.0);
-        dvep_dExx = -0.5 * (2.0 * Exx + Ezz) * Tyield / E3 + (a * dlamdExx + gdot * dvp_dExx + gdot * K * dt * sin_fric * 0.0) / (2.0 * Eii);
-        dvep_dEzz = -0.5 * (2.0 * Ezz + Exx) * Tyield / E3 + (a * dlamdEzz + gdot * dvp_dEzz + gdot * K * dt * sin_fric * 0.0) / (2.0 * Eii);
-        dvep_dExz = -Exz * Tyield / E3 + (a * dlamdExz + gdot * dvp_dExz + gdot * K * dt * sin_fric * 0.0) / (2.0 * Eii);
-        dvep_dP = (sin_fric + a * dlamdP + gdot * dvp_dP + gdot * K * dt * sin_fric * 0.0) / (2.0 * Eii);
+        double q = in_vp - 1.0;
+        const double evg = eta_vp / gdot;
+        double dvp_dExx = evg * dlamdExx * q, dvp_dEzz = evg * dlamdEzz * q;
+        double dvp_dExz = evg * dlamdExz * q, dvp_dP = evg * dlamdP * q;
+        double a = eta_vp + K * dt * sin_fric * sin_dil;
+        const double TyE3 = Tyield * 0.5 * iEii * iEii * iEii, h2 = 0.5 * iEii;   // Tyield / (2 Eii^3), 1 / (2 Eii)
+        dvep_dExx = -0.5 * (2.0 * Exx + Ezz) * TyE3 + (a * dlamdExx + gdot * dvp_dExx + gdot * K * dt * sin_fric * 0.0) * h2;
+        dvep_dEzz = -0.5 * (2.0 * Ezz + Exx) * TyE3 + (a * dlamdEzz + gdot * dvp_dEzz + gdot * K * dt * sin_fric * 0.0) * h2;
+        dvep_dExz = -Exz * TyE3 + (a * dlamdExz + gdot * dvp_dExz + gdot * K * dt * sin_fric * 0.0) * h2;
+        dvep_dP = (sin_fric + a * dlamdP + gdot * dvp_dP + gdot * K * dt * sin_fric * 0.0) * h2;
     }
     o.gdot = gdot;
     double inv_eta_diss = 0.0;
@@ -381,21 +396,24 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     // eta_pwl is re-evaluated unconditionally in the reference (C_pwl = 0 when
     // dislocation creep is off, which makes the dislocation parts vanish); Tii
     // is still the visco-elastic one unless the plastic branch changed it
-    eta_pwl = fpow(2.0 * C_pwl, -1.0) * (dislocation && !is_pl ? Tii / Tn : fpow(Tii, 1.0 - n_pwl));
-    o.Exx_el = (double)elastic * (Txx - Txx0) / 2.0 / eta_el;
-    o.Ezz_el = (double)elastic * (Tzz - Tzz0) / 2.0 / eta_el;
-    o.Exz_el = (double)elastic * (Txz - Txz0) / 2.0 / eta_el;
-    o.Exx_diss = gdot * dQdtxx + Exx_lin + Txx / 2.0 / eta_pwl + Exx_cst;
-    o.Ezz_diss = gdot * dQdtzz + Ezz_lin + Tzz / 2.0 / eta_pwl + Ezz_cst;
-    o.Exz_diss = gdot * dQdtxz / 2.0 + Exz_lin + Txz / 2.0 / eta_pwl + Exz_cst;
-    o.Eii_el = (double)elastic * fabs(Tii - Tii0) / 2.0 / eta_el;
-    o.Eii_pwl = Tii / 2.0 / eta_pwl;
+    // 1 / (2 eta_pwl) = C_pwl Tii^(n-1): no division of the reference's
+    // fpow(2 C_pwl, -1) fpow(Tii, 1 - n) is needed where Tii^n is known
+    const double h_pwl = !(C_pwl > 0.0) ? 0.0 : (dislocation && !is_pl ? C_pwl * Tn * iTii : C_pwl * fpow(Tii, n_pwl - 1.0));
+    eta_pwl = 0.5 / h_pwl;
+    o.Exx_el = (double)elastic * (Txx - Txx0) * i2eta_el;
+    o.Ezz_el = (double)elastic * (Tzz - Tzz0) * i2eta_el;
+    o.Exz_el = (double)elastic * (Txz - Txz0) * i2eta_el;
+    o.Exx_diss = gdot * dQdtxx + Exx_lin + Txx * h_pwl + Exx_cst;
+    o.Ezz_diss = gdot * dQdtzz + Ezz_lin + Tzz * h_pwl + Ezz_cst;
+    o.Exz_diss = gdot * dQdtxz / 2.0 + Exz_lin + Txz * h_pwl + Exz_cst;
+    o.Eii_el = (double)elastic * fabs(Tii - Tii0) * i2eta_el;
+    o.Eii_pwl = Tii * h_pwl;
     o.Eii_lin = Eii_lin;
     o.Eii_cst = Eii_cst;
     o.div_pl = divp;
     o.div_el = -(Pc - P0) / (K * dt);
     double eta = 1.0 / inv_eta_diss;
-    o.VEcoeff = elastic == 0 ? 0.0 : eta_ve / eta_el;
+    o.VEcoeff = elastic == 0 ? 0.0 : 2.0 * eta_ve * i2eta_el;
     if (prm.step == 0) o.etaVE = eta;
     o.txx = Txx; o.tzz = Tzz; o.txz = Txz;
     if (eta > prm.maxeta) eta = prm.maxeta;
