@@ -703,7 +703,8 @@ __global__ void __launch_bounds__(256) k_picard_stencil(stokes_geom G, const T *
     }
 }
 
-// Coarse stencils = R A P, one thread per coarse row, accumulated in the
+// Coarse stencils = R A P, four threads per coarse row (one fine line of the
+// restriction each, summed in shared memory at the end), accumulated in the
 // level's precision (FP64 throughput is a small fraction of FP32 on this
 // part) in shared memory (plane-major, one column per thread).  Every level of the
 // hierarchy follows the tag rule (u_unknown / v_unknown), so the kernel
@@ -736,6 +737,7 @@ __device__ __forceinline__ void v_parents_ij(int i, int j, int ncxc, int *I, int
 }
 
 #define GAL_THREADS 128
+#define GAL_SPLIT 4   // threads per coarse row: each takes one of the 4 fine lines of the restriction
 template <typename T>
 __global__ void __launch_bounds__(GAL_THREADS) k_galerkin(stokes_geom F, const T *__restrict__ suF,
                                                           const T *__restrict__ svF, stokes_geom Cg,
@@ -743,7 +745,9 @@ __global__ void __launch_bounds__(GAL_THREADS) k_galerkin(stokes_geom F, const T
     __shared__ T acc_sh[MG_NST * GAL_THREADS];
     T *acc = acc_sh + threadIdx.x;
 #define ACC(q) acc[(q) * GAL_THREADS]
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = (int)(gt / GAL_SPLIT), sub = (int)(gt % GAL_SPLIT);   // coarse row, fine line of it
+    const int col0 = threadIdx.x - sub;                                  // the row's first column here
     const int Nxf = F.Nx, Nzf = F.Nz, Nxc = Cg.Nx, Nzc = Cg.Nz;
     const size_t nuf = (size_t)Nxf * (Nzf + 1), nvf = (size_t)(Nxf + 1) * Nzf;
     const int nuc = Nxc * (Nzc + 1), nvc = (Nxc + 1) * Nzc;
@@ -754,7 +758,7 @@ __global__ void __launch_bounds__(GAL_THREADS) k_galerkin(stokes_geom F, const T
         const int K = t % Nxc, L = t / Nxc;
         for (int q = 0; q < MG_NST; q++) ACC(q) = T(0);
         if (u_unknown(K, L, Nxc, Nzc)) {
-            for (int lf = 2 * L - 2; lf <= 2 * L + 1; lf++) {
+            for (int lf = 2 * L - 2 + sub; lf <= 2 * L - 2 + sub; lf++) {
                 if (lf < 1 || lf > F.ncz) continue;
                 int J0, J1;
                 float w0, w1;
@@ -796,13 +800,19 @@ __global__ void __launch_bounds__(GAL_THREADS) k_galerkin(stokes_geom F, const T
                 }
             }
         }
-        for (int q = 0; q < MG_NST; q++) suC[(size_t)q * nuc + t] = ACC(q);
     }
+    __syncthreads();
+    if (t < nuc)
+        for (int q = sub; q < MG_NST; q += GAL_SPLIT) {
+            const T *c = acc_sh + q * GAL_THREADS + col0;
+            suC[(size_t)q * nuc + t] = (c[0] + c[1]) + (c[2] + c[3]);
+        }
+    __syncthreads();
     if (t < nvc) {   // coarse v-row (I, J)
         const int I = t % (Nxc + 1), J = t / (Nxc + 1);
         for (int q = 0; q < MG_NST; q++) ACC(q) = T(0);
         if (v_unknown(I, J, Nxc, Nzc)) {
-            for (int i = 2 * I - 2; i <= 2 * I + 1; i++) {
+            for (int i = 2 * I - 2 + sub; i <= 2 * I - 2 + sub; i++) {
                 if (i < 1 || i > F.ncx) continue;
                 int I0, I1;
                 float w0, w1;
@@ -844,8 +854,13 @@ __global__ void __launch_bounds__(GAL_THREADS) k_galerkin(stokes_geom F, const T
                 }
             }
         }
-        for (int q = 0; q < MG_NST; q++) svC[(size_t)q * nvc + t] = ACC(q);
     }
+    __syncthreads();
+    if (t < nvc)
+        for (int q = sub; q < MG_NST; q += GAL_SPLIT) {
+            const T *c = acc_sh + q * GAL_THREADS + col0;
+            svC[(size_t)q * nvc + t] = (c[0] + c[1]) + (c[2] + c[3]);
+        }
 #undef ACC
 }
 
@@ -1472,7 +1487,7 @@ static mdz_status mg_setup(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n, con
     for (int l = 1; l < H.nlev; l++) {
         mg_level<T> &P = H.L[l - 1], &L = H.L[l];
         size_t n = L.nu() > L.nv() ? L.nu() : L.nv();
-        k_galerkin<T><<<mdz_blocks(n, GAL_THREADS), GAL_THREADS, 0, st>>>(P.geom(), P.su, P.sv, L.geom(), L.su, L.sv, status + 1);
+        k_galerkin<T><<<mdz_blocks((long long)n * GAL_SPLIT, GAL_THREADS), GAL_THREADS, 0, st>>>(P.geom(), P.su, P.sv, L.geom(), L.su, L.sv, status + 1);
         MDZ_LAUNCHED(ctx);
         k_st_diag<T><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(L.geom(), L.su, L.sv, L.idu, L.idv);
         MDZ_LAUNCHED(ctx);
