@@ -1635,12 +1635,36 @@ __global__ void k_psub(int np, const signed char *__restrict__ tp, const double 
 
 // ---------------------------------------------------------------------------
 // Block preconditioner: zp = (eta_n / celvol) rp ; zu = V-cycle(ru - B zp).
-// (eta_n / celvol from the level-0 copy D11 = 2 eta_n in precision T)
+// (eta_n / celvol from the level-0 copy D11 = 2 eta_n in precision T), and
+// the sum and count of zp over the pressure equations (as k_psum) for the
+// zero-mean projection applied by k_copy_out
 template <typename T>
-__global__ void k_precond_p(stokes_geom G, const T *__restrict__ D11, const T *__restrict__ rp, T *__restrict__ zp) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= G.ncx * G.ncz) return;
-    zp[i] = G.BCp[i] == -1 ? T(0.5) * gc<T>(G, GC_IXZ) * D11[i] * rp[i] : T(0);
+__global__ void __launch_bounds__(256) k_precond_p(stokes_geom G, const T *__restrict__ D11, const T *__restrict__ rp,
+                                                   T *__restrict__ zp, double *psum) {
+    const int np = G.ncx * G.ncz;
+    const T c = T(0.5) * gc<T>(G, GC_IXZ);
+    T acc = 0;
+    int cnt = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+        T v = 0;
+        if (G.BCp[i] == -1) { v = c * D11[i] * rp[i]; acc += v; cnt++; }
+        zp[i] = v;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    }
+    __shared__ T sa[8];
+    __shared__ int sn[8];
+    if ((threadIdx.x & 31) == 0) { sa[threadIdx.x >> 5] = acc; sn[threadIdx.x >> 5] = cnt; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        T a = 0;
+        int n = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) { a += sa[w]; n += sn[w]; }
+        atomicAdd(&psum[0], (double)a);
+        atomicAdd(&psum[1], (double)n);
+    }
 }
 
 // f = r_vel - B zp  on the fine MG level (B: celvol-scaled pressure gradient)
@@ -1669,12 +1693,17 @@ __global__ void k_precond_rhs(stokes_geom G, const T *__restrict__ ru, const T *
     }
 }
 
+// z velocity <- the V-cycle's result; z pressure <- zero mean over the
+// pressure equations (the mean cancels in the gradient of the right-hand side,
+// so it is removed only here)
 template <typename T>
-__global__ void k_copy_vel(size_t nu, size_t nv, const T *__restrict__ xu, const T *__restrict__ xv,
-                           T *__restrict__ zu, T *__restrict__ zv) {
+__global__ void k_copy_out(size_t nu, size_t nv, int np, const T *__restrict__ xu, const T *__restrict__ xv,
+                           const signed char *__restrict__ tp, const double *__restrict__ psum, T *__restrict__ zu,
+                           T *__restrict__ zv, T *__restrict__ zp) {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nu) zu[i] = xu[i];
     if (i < nv) zv[i] = xv[i];
+    if (i < (size_t)np && tp[i] == -1 && psum[1] > 0) zp[i] -= (T)psum[0] / (T)psum[1];
 }
 
 template <typename T>
@@ -1683,17 +1712,13 @@ static mdz_status precondition(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n,
     mg_level<T> &F = H.L[0];
     stokes_geom G = F.geom();
     const int np = F.ncx * F.ncz;
-    k_precond_p<T><<<mdz_blocks(np), MDZ_THREADS, 0, st>>>(G, F.D11, r + nu + nv, z + nu + nv);
-    MDZ_LAUNCHED(ctx);
     // zero-mean pressure block: constants are the operator's null space; left
     // in, they grow in the iterates and cost the FP32 gradients their accuracy
     MDZ_CUDA(ctx, cudaMemsetAsync(H.pmean, 0, 2 * sizeof(double), st));
     {
         int blocks = mdz_blocks(np, 256);
         if (blocks > 152 * 4) blocks = 152 * 4;
-        k_psum<T><<<blocks, 256, 0, st>>>(np, G.BCp, z + nu + nv, H.pmean);
-        MDZ_LAUNCHED(ctx);
-        k_psub<T><<<mdz_blocks(np), MDZ_THREADS, 0, st>>>(np, G.BCp, H.pmean, z + nu + nv);
+        k_precond_p<T><<<blocks, 256, 0, st>>>(G, F.D11, r + nu + nv, z + nu + nv, H.pmean);
         MDZ_LAUNCHED(ctx);
     }
     k_precond_rhs<T><<<box_grid(F.Nx, F.Nz), dim3(32, 8), 0, st>>>(G, r, r + nu, z + nu + nv, F.fu, F.fv);
@@ -1702,7 +1727,9 @@ static mdz_status precondition(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n,
     mdz_status s = vcycle<T>(ctx, H, 0, S->nu1, S->nu2, (T)S->omega, st);
     if (s != MDZ_OK) return s;
     size_t n = nu > nv ? nu : nv;
-    k_copy_vel<T><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(nu, nv, F.xu, F.xv, z, z + nu);
+    if ((size_t)np > n) n = np;
+    k_copy_out<T><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(nu, nv, np, F.xu, F.xv, G.BCp, H.pmean, z, z + nu,
+                                                         z + nu + nv);
     MDZ_LAUNCHED(ctx);
     return MDZ_OK;
 }
