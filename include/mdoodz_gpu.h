@@ -415,6 +415,12 @@ typedef struct mdz_model {
     int nit_pic_max;
     int newton_maxit;       /* Krylov cap of a Jacobian solve before the Picard operator takes
                                that iteration over (0: lin_maxit)                              */
+    /* 1: each defect solve asks only for the reduction the non-linear iteration
+     * can use (Eisenstat-Walker forcing, eta_k = 0.9 (r_k / r_k-1)^2 within
+     * [lin_rtol, 0.1], and no tighter than half the remaining distance to
+     * rel_tol); 0: every solve to lin_rtol.  No counterpart in the reference,
+     * whose direct solver has no tolerance. */
+    int adaptive_lin_tol;
 } mdz_model;
 
 #define MDZ_HISTORY 32
@@ -433,7 +439,7 @@ typedef struct mdz_step_report {
     int lin_its_history[MDZ_HISTORY];
     double lin_rel_history[MDZ_HISTORY];
     int newton_history[MDZ_HISTORY];
-    int precision_fallbacks;          /* FP32-refined solves that missed 10 x lin_rtol, redone in FP64 */
+    int precision_fallbacks;          /* FP32-refined solves that missed 10 x their tolerance, redone in FP64 */
 } mdz_step_report;
 
 /* One time step of Main_DOODZ.c's loop (SOURCE/Main_DOODZ.c:459-1320) on the

@@ -287,6 +287,17 @@ static mdz_status residual_norms(mdz_ctx *ctx, double *norms3, cudaStream_t st) 
 // Each block converges on its absolute or relative tolerance; a block whose
 // first residual is negligible next to the largest one (an initially
 // divergence-free velocity makes resp0 round-off) is measured against that one.
+// the largest block residual relative to its first value, with the block
+// selection of converged(): the distance still to go to rel_tol
+static double relative_residual(const double *r, const double *r0) {
+    double rmax = fmax(r0[0], fmax(r0[1], r0[2])), out = 0.0;
+    for (int q = 0; q < 3; q++) {
+        double ref = r0[q] > 1e-6 * rmax ? r0[q] : rmax;
+        if (ref > 0) out = fmax(out, r[q] / ref);
+    }
+    return out;
+}
+
 static bool converged(const mdz_model *M, const double *r, const double *r0) {
     double rmax = fmax(r0[0], fmax(r0[1], r0[2]));
     for (int q = 0; q < 3; q++) {
@@ -372,6 +383,7 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
     double r0[3] = {0, 0, 0}, r[3] = {0, 0, 0};
     int nit = 0;
     bool use_newton = M->newton && !M->picard2newton;
+    double rel_prev = -1.0, eta_prev = 0.1;   // forcing-term history (adaptive_lin_tol)
     MDZ_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(int) * 4, st));
     MDZ_CUDA(ctx, cudaMemsetAsync(ctx->d_counters + 48, 0, sizeof(unsigned long long), st));
     for (nit = 0; nit <= M->nit_max; nit++) {
@@ -402,18 +414,33 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
         }
         mdz_solve_stats ss{};
         bool newton_step = use_newton;
+        // tolerance of this defect solve: lin_rtol, or the Eisenstat-Walker
+        // forcing term (choice 2, gamma 0.9, alpha 2, with its safeguard) kept
+        // within [lin_rtol, 0.1] and no tighter than half the way to rel_tol
+        double eta = M->lin_rtol;
+        if (M->adaptive_lin_tol) {
+            const double rel = relative_residual(r, r0);
+            double e = rel_prev > 0.0 ? 0.9 * (rel / rel_prev) * (rel / rel_prev) : 0.1;
+            if (rel_prev > 0.0 && 0.9 * eta_prev * eta_prev > 0.1) e = fmax(e, 0.9 * eta_prev * eta_prev);
+            e = fmin(e, 0.1);
+            if (rel > 0.0) e = fmax(e, 0.5 * M->rel_tol / rel);
+            e = fmin(e, 0.1);
+            eta = fmax(e, M->lin_rtol);
+            rel_prev = rel;
+            eta_prev = eta;
+        }
         {
             step_timer T(st, &R.ms_solve);
             const int maxit = use_newton && M->newton_maxit > 0 ? M->newton_maxit : M->lin_maxit;
-            s = mdz_dev_solve(ctx, f, use_newton, M->precision, M->lin_rtol, maxit, B.F, B.dx, &ss, st);
+            s = mdz_dev_solve(ctx, f, use_newton, M->precision, eta, maxit, B.F, B.dx, &ss, st);
             if (s != MDZ_OK) return s;
             R.linear_its += ss.iterations;
             R.newton_its += use_newton ? 1 : 0;
             // an FP32-refined solve that stopped short of the tolerance (its
             // refinement stagnates where FP32 cannot resolve the correction) is
             // redone in FP64, so a missed digit never reaches the Newton update
-            if (M->precision == 32 && !(ss.rel_residual <= 10.0 * M->lin_rtol)) {
-                s = mdz_dev_solve(ctx, f, use_newton, 64, M->lin_rtol, maxit, B.F, B.dx, &ss, st);
+            if (M->precision == 32 && !(ss.rel_residual <= 10.0 * eta)) {
+                s = mdz_dev_solve(ctx, f, use_newton, 64, eta, maxit, B.F, B.dx, &ss, st);
                 if (s != MDZ_OK) return s;
                 R.linear_its += ss.iterations;
                 R.precision_fallbacks++;
@@ -421,9 +448,9 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
             // A Newton system whose pressure Schur complement the Picard-based
             // preconditioner cannot follow (strong pressure-dependent plasticity)
             // stalls the Krylov solve: take a Picard step for this iteration.
-            if (use_newton && !(ss.rel_residual <= 1e-2)) {
+            if (use_newton && !(ss.rel_residual <= fmax(1e-2, 2.0 * eta))) {
                 if ((s = mdz_dev_operators(ctx, &M->rheo, f, 0, st)) != MDZ_OK) return s;
-                s = mdz_dev_solve(ctx, f, false, M->precision, M->lin_rtol, M->lin_maxit, B.F, B.dx, &ss, st);
+                s = mdz_dev_solve(ctx, f, false, M->precision, eta, M->lin_maxit, B.F, B.dx, &ss, st);
                 if (s != MDZ_OK) return s;
                 R.linear_its += ss.iterations;
                 R.picard_fallbacks++;
