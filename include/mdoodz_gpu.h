@@ -439,7 +439,8 @@ typedef struct mdz_step_report {
     int lin_its_history[MDZ_HISTORY];
     double lin_rel_history[MDZ_HISTORY];
     int newton_history[MDZ_HISTORY];
-    int precision_fallbacks;          /* FP32-refined solves that missed 10 x their tolerance, redone in FP64 */
+    int precision_fallbacks;          /* FP32-refined solves that missed min(10 x their tolerance, 0.5),
+                                         redone in FP64 */
 } mdz_step_report;
 
 /* One time step of Main_DOODZ.c's loop (SOURCE/Main_DOODZ.c:459-1320) on the

@@ -438,8 +438,9 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
             R.newton_its += use_newton ? 1 : 0;
             // an FP32-refined solve that stopped short of the tolerance (its
             // refinement stagnates where FP32 cannot resolve the correction) is
-            // redone in FP64, so a missed digit never reaches the Newton update
-            if (M->precision == 32 && !(ss.rel_residual <= 10.0 * eta)) {
+            // redone in FP64, so a missed digit never reaches the Newton update;
+            // one that did not even halve the defect always is
+            if (M->precision == 32 && !(ss.rel_residual <= fmin(10.0 * eta, 0.5))) {
                 s = mdz_dev_solve(ctx, f, use_newton, 64, eta, maxit, B.F, B.dx, &ss, st);
                 if (s != MDZ_OK) return s;
                 R.linear_its += ss.iterations;

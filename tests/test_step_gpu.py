@@ -76,3 +76,23 @@ def test_vep_newton_step_vs_oracle(precision):
     for k in ("sxxd", "szzd", "sxz", "strain_pl", "x", "z"):
         assert _rel(mk[k], mo[k]) < 1e-8, k
     assert np.array_equal(mk["phase"], mo["phase"])
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_adaptive_linear_tolerance_same_step(precision):
+    """Eisenstat-Walker forcing (adaptive_lin_tol = 1) reaches the same
+    converged step as fixed-tolerance solves, with fewer Krylov iterations."""
+    g, m, u, v, p, mat = vep_case()
+    prm = mdz.RheoParams.make(dt=0.5, iselastic=1, step=1)
+    fixed = mdz.Model.make(prm, newton=1, nit_max=20, rel_tol=1e-11, lin_rtol=1e-9, line_search=0,
+                           precision=precision)
+    adapt = mdz.Model.make(prm, newton=1, nit_max=20, rel_tol=1e-11, lin_rtol=1e-9, line_search=0,
+                           precision=precision, adaptive_lin_tol=1)
+    out_f, mk_f, rep_f = run_gpu(g, dict((k, np.array(v_)) for k, v_ in m.items()), u, v, p, mat, fixed)
+    out_a, mk_a, rep_a = run_gpu(g, dict((k, np.array(v_)) for k, v_ in m.items()), u, v, p, mat, adapt)
+    assert rep_f.converged == 1 and rep_a.converged == 1, (rep_f.as_dict(), rep_a.as_dict())
+    assert rep_a.linear_its < rep_f.linear_its, (rep_a.linear_its, rep_f.linear_its)
+    assert _rel(out_a["u"], out_f["u"]) < 1e-8 and _rel(out_a["v"], out_f["v"]) < 1e-8
+    assert _rel(out_a["p"] - out_a["p"].mean(), out_f["p"] - out_f["p"].mean()) < 1e-8
+    for k in ("sxxd", "szzd", "sxz", "x", "z"):
+        assert _rel(mk_a[k], mk_f[k]) < 1e-8, k
