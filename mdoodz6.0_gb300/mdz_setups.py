@@ -153,10 +153,11 @@ def config_lithosphere(Nx=1025, Nz=513, nm=4, seed=12345, precision=64, learned=
                               scale_S=sc.S, scale_eta=sc.eta, scale_L=sc.L, clamp_tangent=1)
     # Picard iterations until resx or resz dropped tenfold, then Newton
     # (Picard2Newton of the reference); 30 iterations at most
-    # (no line search: the reference's default, line_search = 0)
+    # (no line search: the reference's default, line_search = 0; each defect
+    # solve asks only for the reduction the non-linear iteration can use)
     model = mdz.Model.make(prm, gz=-9.81 * L / S, newton=1, nit_max=30, rel_tol=1e-8, lin_rtol=1e-5,
                            line_search=0, precision=precision, learned_guess=learned, picard2newton=1,
-                           pic2newt_cond=1e-1, nit_pic_max=10, newton_maxit=200)
+                           pic2newt_cond=1e-1, nit_pic_max=10, newton_maxit=200, adaptive_lin_tol=1)
     u, v = pure_shear_velocity(g, eps / sc.E)
     m = _markers_dict(x, z, ph, T=T)
     # initial pressure: lithostatic column of the layered densities (the
