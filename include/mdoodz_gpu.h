@@ -421,6 +421,11 @@ typedef struct mdz_model {
      * rel_tol); 0: every solve to lin_rtol.  No counterpart in the reference,
      * whose direct solver has no tolerance. */
     int adaptive_lin_tol;
+    /* > 0: local rheology solves in FP32 (FP64 where one fails) while the
+     * largest relative block residual is above this value; the iterations that
+     * decide convergence, and the final update, always run in FP64.  0: FP64
+     * throughout.  No counterpart in the reference. */
+    double fp32_rheology_above;
 } mdz_model;
 
 #define MDZ_HISTORY 32

@@ -251,7 +251,7 @@ mdz_status mdz_check_materials(mdz_ctx *ctx, const mdz_materials *m);
 // starts.  learned: every local solve starts from the MLP's guess (weights
 // loaded in the context) and the plain solve reruns where the polish fails.
 mdz_status mdz_dev_viscosity(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm, const mdz_fields &f,
-                             int *d_counters, cudaStream_t st, bool learned = false);
+                             int *d_counters, cudaStream_t st, bool learned = false, bool fp32 = false);
 mdz_status mdz_dev_operators(mdz_ctx *ctx, const mdz_rheo_params *prm, const mdz_fields &f, int jacobian,
                              cudaStream_t st);
 mdz_status mdz_dev_rhs(mdz_ctx *ctx, const mdz_rheo_params *prm, double gx, double gz, const mdz_fields &f,

@@ -109,122 +109,143 @@ struct visc_res {
 // plain solve takes over.
 #define MDZ_POLISH_STEPS 2
 
-__device__ __forceinline__ double dmin(double a, double b) { return a <= b ? a : b; }
+// Precision-generic helpers of the local solve (FP64 or FP32 instances).
+__device__ __forceinline__ double msqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float msqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double mexp(double x) { return exp(x); }
+__device__ __forceinline__ float mexp(float x) { return expf(x); }
+__device__ __forceinline__ double mlog(double x) { return log(x); }
+__device__ __forceinline__ float mlog(float x) { return logf(x); }
+__device__ __forceinline__ double mfabs(double x) { return fabs(x); }
+__device__ __forceinline__ float mfabs(float x) { return fabsf(x); }
+__device__ __forceinline__ double msin(double x) { return sin(x); }
+__device__ __forceinline__ float msin(float x) { return sinf(x); }
+__device__ __forceinline__ void msincos(double x, double *s, double *c) { sincos(x, s, c); }
+__device__ __forceinline__ void msincos(float x, float *s, float *c) { sincosf(x, s, c); }
+__device__ __forceinline__ double mpow(double x, double y) { return pow(x, y); }
+__device__ __forceinline__ float mpow(float x, float y) { return powf(x, y); }
+
+template <typename Real>
+__device__ __forceinline__ Real dmin(Real a, Real b) { return a <= b ? a : b; }
 
 // pow with the exponents the creep laws make trivial (0, 1, 2, -1, -2:
 // grain-size and melt exponents switched off, linear diffusion creep and its
 // tangent, squares) taken exactly; each costs a full FP64 log/exp pair
 // otherwise, and FP64 throughput is what bounds the local solves on this part.
-__device__ __forceinline__ double fpow(double x, double y) {
-    if (y == 0.0) return 1.0;
-    if (y == 1.0) return x;
-    if (y == 2.0) return x * x;
-    if (y == -1.0) return 1.0 / x;
-    if (y == -2.0) return 1.0 / (x * x);
-    return pow(x, y);
+template <typename Real, typename Y>
+__device__ __forceinline__ Real fpow(Real x, Y y0) {
+    const Real y = Real(y0);
+    if (y == Real(0)) return Real(1);
+    if (y == Real(1)) return x;
+    if (y == Real(2)) return x * x;
+    if (y == Real(-1)) return Real(1) / x;
+    if (y == Real(-2)) return Real(1) / (x * x);
+    return mpow(x, y);
 }
 
 // exp with the zero argument of switched-off melt weakening taken exactly
-__device__ __forceinline__ double fexp(double x) { return x == 0.0 ? 1.0 : exp(x); }
+template <typename Real>
+__device__ __forceinline__ Real fexp(Real x) { return x == Real(0) ? Real(1) : mexp(x); }
 
-__device__ void visc_local(int p, double G, double T, double P, double d, double phi, double X0, double Exx,
-                           double Ezz, double Exz, double Gxx, double Gzz, double Gxz, double Txx0, double Tzz0,
-                           double Txz0, const mdz_materials &m, const mdz_rheo_params &prm, double dil, double fric,
-                           double C, double P0, double beta, visc_res &o, const float *guess = nullptr) {
-    const double R = m.R, dt = prm.dt, tol = 1.0e-11;
+template <typename Real>
+__device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Real X0, Real Exx,
+                           Real Ezz, Real Exz, Real Gxx, Real Gzz, Real Gxz, Real Txx0, Real Tzz0,
+                           Real Txz0, const mdz_materials &m, const mdz_rheo_params &prm, Real dil, Real fric,
+                           Real C, Real P0, Real beta, visc_res &o, const float *guess) {
+    const Real R = Real(m.R), dt = Real(prm.dt), tol = sizeof(Real) == 8 ? Real(1.0e-11) : Real(1.0e-4);
     const int nitmax = 20;
     int elastic = prm.iselastic, it;
-    const bool constant = m.cstv[p] != 0, dislocation = m.pwlv[p] != 0, diffusion = m.linv[p] != 0;
-    double K = 1.0 / beta, res = 0.0;
-    const double Tii0 = sqrt(Txx0 * Txx0 + Txz0 * Txz0);
-    const double n_pwl = m.npwl[p], Va_pwl = m.Vpwl[p], n_lin = m.nlin[p], m_lin = m.mlin[p];
-    double B_lin = 0, C_pwl = 0, C_lin = 0, dCpwldP = 0, dClindP = 0;
-    double eta_pwl = 0.0, eta_lin = 0.0, eta_cst = 0.0, eta_vep = 0.0, eta_vp = 0.0;
-    const double eta_vp0 = m.eta_vp[p], n_vp = m.n_vp[p];
-    double Eii_pwl = 0, Eii_lin = 0, Eii_cst = 0;
-    o.Eii_pl = 0.0; o.OverS = 0.0; o.ve_fail = 0; o.vp_fail = 0; o.vp_its = 0;
+    const bool constant = Real(m.cstv[p]) != 0, dislocation = Real(m.pwlv[p]) != 0, diffusion = Real(m.linv[p]) != 0;
+    Real K = Real(1.0) / beta, res = Real(0.0);
+    const Real Tii0 = msqrt(Txx0 * Txx0 + Txz0 * Txz0);
+    const Real n_pwl = Real(m.npwl[p]), Va_pwl = Real(m.Vpwl[p]), n_lin = Real(m.nlin[p]), m_lin = Real(m.mlin[p]);
+    Real B_lin = 0, C_pwl = 0, C_lin = 0, dCpwldP = 0, dClindP = 0;
+    Real eta_pwl = Real(0.0), eta_lin = Real(0.0), eta_cst = Real(0.0), eta_vep = Real(0.0), eta_vp = Real(0.0);
+    const Real eta_vp0 = Real(m.eta_vp[p]), n_vp = Real(m.n_vp[p]);
+    Real Eii_pwl = 0, Eii_lin = 0, Eii_cst = 0;
+    o.Eii_pl = Real(0.0); o.OverS = Real(0.0); o.ve_fail = 0; o.vp_fail = 0; o.vp_its = 0;
 
-    double Eyy = -(Exx + Ezz), Gyy = -(Gxx + Gzz);
-    double Eii = sqrt(1.0 / 2.0 * (Exx * Exx + Ezz * Ezz + Eyy * Eyy) + Exz * Exz);
-    double Gii = sqrt(1.0 / 2.0 * (Gxx * Gxx + Gzz * Gzz + Gyy * Gyy) + Gxz * Gxz);
-    if (Eii * prm.scale_E < 1e-30) Eii = 1e-30 / prm.scale_E;
-    if (Gii * prm.scale_E < 1e-30) Gii = 1e-30 / prm.scale_E;
-    const double f_ani = Gii / Eii;
+    Real Eyy = -(Exx + Ezz), Gyy = -(Gxx + Gzz);
+    Real Eii = msqrt(Real(1.0) / Real(2.0) * (Exx * Exx + Ezz * Ezz + Eyy * Eyy) + Exz * Exz);
+    Real Gii = msqrt(Real(1.0) / Real(2.0) * (Gxx * Gxx + Gzz * Gzz + Gyy * Gyy) + Gxz * Gxz);
+    if (Eii * Real(prm.scale_E) < Real(1e-30)) Eii = Real(1e-30) / Real(prm.scale_E);
+    if (Gii * Real(prm.scale_E) < Real(1e-30)) Gii = Real(1e-30) / Real(prm.scale_E);
+    const Real f_ani = Gii / Eii;
     // reciprocals taken once per solve: an FP64 division is a long instruction
     // sequence on this part, and the reference's formulas divide some fifty
     // times per local solve
-    const double iEii = 1.0 / Eii, iGii = 1.0 / Gii;
+    const Real iEii = Real(1.0) / Eii, iGii = Real(1.0) / Gii;
     o.Pcorr = P;
     if (prm.step == 0) elastic = 0;
-    o.d1 = m.gs_ref[p];
-    if (elastic == 0) { G = 1e1; K = 1e1; dil = 0.0; }
-    if (T < ZEROC / prm.scale_T) T = ZEROC / prm.scale_T;
-    const double iRT = 1.0 / (R * T);
+    o.d1 = Real(m.gs_ref[p]);
+    if (elastic == 0) { G = Real(1e1); K = Real(1e1); dil = Real(0.0); }
+    if (T < Real(ZEROC) / Real(prm.scale_T)) T = Real(ZEROC) / Real(prm.scale_T);
+    const Real iRT = Real(1.0) / (R * T);
     if (dislocation) {
-        const double in = 1.0 / n_pwl;
-        double B_pwl = m.pref_pwl[p] * m.Fpwl[p] * fpow(m.Apwl[p], -in) * exp((m.Qpwl[p] + P * Va_pwl) * iRT * in) *
-                       fpow(d, m.mpwl[p] * in) * fpow(m.fpwl[p], -m.rpwl[p] * in) * fexp(-m.apwl[p] * phi * in);
-        C_pwl = fpow(2.0 * f_ani * B_pwl, -n_pwl);
+        const Real in = Real(1.0) / n_pwl;
+        Real B_pwl = Real(m.pref_pwl[p]) * Real(m.Fpwl[p]) * fpow(Real(m.Apwl[p]), -in) * mexp((Real(m.Qpwl[p]) + P * Va_pwl) * iRT * in) *
+                       fpow(d, Real(m.mpwl[p]) * in) * fpow(Real(m.fpwl[p]), -Real(m.rpwl[p]) * in) * fexp(-Real(m.apwl[p]) * phi * in);
+        C_pwl = fpow(Real(2.0) * f_ani * B_pwl, -n_pwl);
         dCpwldP = -C_pwl * Va_pwl * iRT;
-        eta_pwl = B_pwl * fpow(Eii, in - 1.0);
+        eta_pwl = B_pwl * fpow(Eii, in - Real(1.0));
     }
     if (diffusion) {
-        const double in = 1.0 / n_lin;
-        B_lin = m.Flin[p] * fpow(m.Alin[p], -in) * exp((m.Qlin[p] + P * m.Vlin[p]) * iRT * in) *
-                fpow(m.flin[p], -m.rlin[p] * in) * fexp(-m.alin[p] * phi * in);
-        C_lin = fpow(2.0 * f_ani * B_lin, -n_lin);
-        dClindP = -C_lin * m.Vlin[p] * iRT;
-        eta_lin = B_lin * fpow(Eii, in - 1.0) * fpow(d, m_lin * in);
+        const Real in = Real(1.0) / n_lin;
+        B_lin = Real(m.Flin[p]) * fpow(Real(m.Alin[p]), -in) * mexp((Real(m.Qlin[p]) + P * Real(m.Vlin[p])) * iRT * in) *
+                fpow(Real(m.flin[p]), -Real(m.rlin[p]) * in) * fexp(-Real(m.alin[p]) * phi * in);
+        C_lin = fpow(Real(2.0) * f_ani * B_lin, -n_lin);
+        dClindP = -C_lin * Real(m.Vlin[p]) * iRT;
+        eta_lin = B_lin * fpow(Eii, in - Real(1.0)) * fpow(d, m_lin * in);
     }
-    double cos_fric, sin_fric;
-    sincos(fric, &sin_fric, &cos_fric);
-    double sin_dil = dil == 0.0 ? 0.0 : sin(dil);
-    double Tyield = C * cos_fric + P * sin_fric;
-    if (m.Slim[p] < Tyield) { sin_fric = 0.0; cos_fric = 1.0; sin_dil = 0.0; C = m.Slim[p]; Tyield = m.Slim[p]; }
+    Real cos_fric, sin_fric;
+    msincos(fric, &sin_fric, &cos_fric);
+    Real sin_dil = dil == Real(0.0) ? Real(0.0) : msin(dil);
+    Real Tyield = C * cos_fric + P * sin_fric;
+    if (Real(m.Slim[p]) < Tyield) { sin_fric = Real(0.0); cos_fric = Real(1.0); sin_dil = Real(0.0); C = Real(m.Slim[p]); Tyield = Real(m.Slim[p]); }
     o.X1 = X0;
-    const double eta_el = G * dt;
-    if (constant) eta_cst = m.eta0[p];
-    double eta_up = 1.0e100 / prm.scale_eta;
+    const Real eta_el = G * dt;
+    if (constant) eta_cst = Real(m.eta0[p]);
+    Real eta_up = Real(1.0e100) / Real(prm.scale_eta);
     if (constant) eta_up = dmin(eta_up, eta_cst);
     if (dislocation) eta_up = dmin(eta_up, eta_pwl);
     if (elastic) eta_up = dmin(eta_up, eta_el);
     if (diffusion) eta_up = dmin(eta_up, eta_lin);
     // local Newton on the visco-elastic viscosity
-    double eta_ve = eta_up, Tii;
-    const double dm_lin = fpow(o.d1, -m_lin);
+    Real eta_ve = eta_up, Tii;
+    const Real dm_lin = fpow(o.d1, -m_lin);
     bool ve_done = false;
     o.eta_up = eta_up;
     o.learned = guess != nullptr;
     o.fallback = 0;
-    const double i2eta_el = 0.5 / eta_el, ifcst = constant ? 0.5 / (f_ani * eta_cst) : 0.0;
+    const Real i2eta_el = Real(0.5) / eta_el, ifcst = constant ? Real(0.5) / (f_ani * eta_cst) : Real(0.0);
     if (guess) {
-        // Learned start s = log(eta_ve), polished by Halley steps on
-        // g(s) = log(sum of the strain rates) - log(Eii): every mechanism's
-        // rate is c_k exp(n_k s), so g' and g'' are rate-weighted means of n_k
+        // Learned start s = mlog(eta_ve), polished by Halley steps on
+        // g(s) = mlog(sum of the strain rates) - mlog(Eii): every mechanism's
+        // rate is c_k mexp(n_k s), so g' and g'' are rate-weighted means of n_k
         // and n_k^2 (in s the residual is nearly linear; Halley in eta itself
         // left 39 % of the solves unconverged after two steps).  Converged
         // means the reference's own test below holds.  The network predicts
         // ln(eta_ve / eta_up), eta_up being the reference's start (the
         // smallest viscosity of the active mechanisms).
-        double s = log(eta_up) + (double)guess[0];
+        Real s = mlog(eta_up) + (Real)guess[0];
         for (it = 0; it <= MDZ_POLISH_STEPS; it++) {
-            eta_ve = exp(s);
-            Tii = 2.0 * f_ani * eta_ve * Eii;
-            const double Eel = elastic ? Tii * i2eta_el : 0.0;
+            eta_ve = mexp(s);
+            Tii = Real(2.0) * f_ani * eta_ve * Eii;
+            const Real Eel = elastic ? Tii * i2eta_el : Real(0.0);
             if (constant) Eii_cst = Tii * ifcst;
             if (dislocation) Eii_pwl = C_pwl * fpow(Tii, n_pwl);
             if (diffusion) Eii_lin = C_lin * fpow(Tii, n_lin) * dm_lin;
-            const double S0 = Eel + Eii_pwl + Eii_lin + Eii_cst;
-            res = fabs((Eii - S0) * iEii);
+            const Real S0 = Eel + Eii_pwl + Eii_lin + Eii_cst;
+            res = mfabs((Eii - S0) * iEii);
             if (res < tol / 100) { ve_done = true; break; }
             if (it == MDZ_POLISH_STEPS) break;
-            if (!(S0 > 0.0)) break;
-            const double S1 = Eel + n_pwl * Eii_pwl + n_lin * Eii_lin + Eii_cst;
-            const double S2 = Eel + n_pwl * n_pwl * Eii_pwl + n_lin * n_lin * Eii_lin + Eii_cst;
-            const double iS0 = 1.0 / S0;
-            const double g = log(S0 * iEii), g1 = S1 * iS0, g2 = S2 * iS0 - g1 * g1;
-            const double den = 2.0 * g1 * g1 - g * g2;
-            s -= den > 0.0 ? 2.0 * g * g1 / den : g / g1;
+            if (!(S0 > Real(0.0))) break;
+            const Real S1 = Eel + n_pwl * Eii_pwl + n_lin * Eii_lin + Eii_cst;
+            const Real S2 = Eel + n_pwl * n_pwl * Eii_pwl + n_lin * n_lin * Eii_lin + Eii_cst;
+            const Real iS0 = Real(1.0) / S0;
+            const Real g = mlog(S0 * iEii), g1 = S1 * iS0, g2 = S2 * iS0 - g1 * g1;
+            const Real den = Real(2.0) * g1 * g1 - g * g2;
+            s -= den > Real(0.0) ? Real(2.0) * g * g1 / den : g / g1;
         }
         o.ve_its = it;
         if (!ve_done) {
@@ -233,17 +254,17 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
             Eii_pwl = 0; Eii_lin = 0; Eii_cst = 0;
         }
     }
-    const double dfel = elastic ? -Eii / eta_el : 0.0, dfcst = constant ? -Eii / eta_cst : 0.0;
+    const Real dfel = elastic ? -Eii / eta_el : Real(0.0), dfcst = constant ? -Eii / eta_cst : Real(0.0);
     for (it = 0; !ve_done && it < nitmax; it++) {
-        Tii = 2.0 * f_ani * eta_ve * Eii;
+        Tii = Real(2.0) * f_ani * eta_ve * Eii;
         if (constant) Eii_cst = Tii * ifcst;
         if (dislocation) Eii_pwl = C_pwl * fpow(Tii, n_pwl);
         if (diffusion) Eii_lin = C_lin * fpow(Tii, n_lin) * dm_lin;
-        double r = Eii - elastic * Tii * i2eta_el - (Eii_pwl + Eii_lin + Eii_cst);
-        res = fabs(r * iEii);
+        Real r = Eii - elastic * Tii * i2eta_el - (Eii_pwl + Eii_lin + Eii_cst);
+        res = mfabs(r * iEii);
         if (res < tol / 100) break;
-        const double ieta = 1.0 / eta_ve;
-        double dfdeta = dfel + dfcst;
+        const Real ieta = Real(1.0) / eta_ve;
+        Real dfdeta = dfel + dfcst;
         if (diffusion) dfdeta += -Eii_lin * n_lin * ieta;
         if (dislocation) dfdeta += -Eii_pwl * n_pwl * ieta;
         eta_ve -= r / dfdeta;
@@ -257,68 +278,68 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
     // iteration stopped on its convergence test (not when it ran out): then
     // Tii^n_pwl is Eii_pwl / C_pwl, and the powers of Tii below follow from it
     // without another FP64 pow each
-    const bool pwl_fresh = dislocation && (ve_done || res < tol / 100) && C_pwl > 0.0 && Eii_pwl > 0.0;
-    Tii = 2.0 * eta_ve * f_ani * Eii;
-    const double Tn = !dislocation ? 0.0 : (pwl_fresh ? Eii_pwl / C_pwl : fpow(Tii, n_pwl));   // Tii^n_pwl
-    const double iTii = 1.0 / Tii, TG = Tii * iGii;   // Tii / (f_ani Eii) = Tii / Gii
-    double Txx = Gxx * TG, Tzz = Gzz * TG, Txz = Gxz * TG;
-    double Exx_lin = 0, Ezz_lin = 0, Exz_lin = 0, Exx_cst = 0, Ezz_cst = 0, Exz_cst = 0;
-    if (dislocation) eta_pwl = Tii / (2.0 * C_pwl * Tn);   // (2 C)^-1 Tii^(1-n)
+    const bool pwl_fresh = dislocation && (ve_done || res < tol / 100) && C_pwl > Real(0.0) && Eii_pwl > Real(0.0);
+    Tii = Real(2.0) * eta_ve * f_ani * Eii;
+    const Real Tn = !dislocation ? Real(0.0) : (pwl_fresh ? Eii_pwl / C_pwl : fpow(Tii, n_pwl));   // Tii^n_pwl
+    const Real iTii = Real(1.0) / Tii, TG = Tii * iGii;   // Tii / (f_ani Eii) = Tii / Gii
+    Real Txx = Gxx * TG, Tzz = Gzz * TG, Txz = Gxz * TG;
+    Real Exx_lin = 0, Ezz_lin = 0, Exz_lin = 0, Exx_cst = 0, Ezz_cst = 0, Exz_cst = 0;
+    if (dislocation) eta_pwl = Tii / (Real(2.0) * C_pwl * Tn);   // (2 C)^-1 Tii^(1-n)
     if (diffusion) {
-        const double in = 1.0 / n_lin;
-        eta_lin = B_lin * fpow(Eii_lin, in - 1.0) * fpow(o.d1, m_lin * in);
-        const double h = 0.5 / eta_lin;
+        const Real in = Real(1.0) / n_lin;
+        eta_lin = B_lin * fpow(Eii_lin, in - Real(1.0)) * fpow(o.d1, m_lin * in);
+        const Real h = Real(0.5) / eta_lin;
         Exx_lin = Txx * h; Ezz_lin = Tzz * h; Exz_lin = Txz * h;
     }
     if (constant) {
-        const double h = 0.5 / eta_cst;
+        const Real h = Real(0.5) / eta_cst;
         Exx_cst = Txx * h; Ezz_cst = Tzz * h; Exz_cst = Txz * h;
     }
     // visco-elastic tangent
-    double deta = 0.0;
-    if (dislocation) deta += -C_pwl * (Tn * iTii * iTii * iTii) * (n_pwl - 1.0);   // Tii^(n-3)
-    if (diffusion) deta += -C_lin * fpow(Tii, n_lin - 3.0) * (n_lin - 1.0) * dm_lin;
-    const double e2 = fpow(eta_ve, 2.0);
-    double dTxx = deta * (2.0 * Txx + Tzz) * e2, dTzz = deta * (2.0 * Tzz + Txx) * e2, dTxz = 2.0 * deta * Txz * e2;
-    double den = 1.0 - 2.0 * (dTxx * Exx + dTzz * Ezz + dTxz * Exz);
-    const double e2den = 2.0 * eta_ve / den;
-    double dve_dExx = dTxx * e2den, dve_dEzz = dTzz * e2den;
-    double dve_dExz = dTxz * e2den;
-    double dummy = 0.0, Jii = Tii * Tii;
-    if (dislocation) dummy += -2.0 * (Tn * iTii) * dCpwldP;   // Jii^((n-1)/2) = Tii^(n-1)
-    if (diffusion) dummy += -2.0 * fpow(Jii, (1.0 / 2.0) * n_lin - 1.0 / 2.0) * fpow(d, -m_lin) * dClindP;
-    double dve_dP = fpow(eta_ve, 2) * dummy;
+    Real deta = Real(0.0);
+    if (dislocation) deta += -C_pwl * (Tn * iTii * iTii * iTii) * (n_pwl - Real(1.0));   // Tii^(n-3)
+    if (diffusion) deta += -C_lin * fpow(Tii, n_lin - Real(3.0)) * (n_lin - Real(1.0)) * dm_lin;
+    const Real e2 = fpow(eta_ve, Real(2.0));
+    Real dTxx = deta * (Real(2.0) * Txx + Tzz) * e2, dTzz = deta * (Real(2.0) * Tzz + Txx) * e2, dTxz = Real(2.0) * deta * Txz * e2;
+    Real den = Real(1.0) - Real(2.0) * (dTxx * Exx + dTzz * Ezz + dTxz * Exz);
+    const Real e2den = Real(2.0) * eta_ve / den;
+    Real dve_dExx = dTxx * e2den, dve_dEzz = dTzz * e2den;
+    Real dve_dExz = dTxz * e2den;
+    Real dummy = Real(0.0), Jii = Tii * Tii;
+    if (dislocation) dummy += -Real(2.0) * (Tn * iTii) * dCpwldP;   // Jii^((n-1)/2) = Tii^(n-1)
+    if (diffusion) dummy += -Real(2.0) * fpow(Jii, (Real(1.0) / Real(2.0)) * n_lin - Real(1.0) / Real(2.0)) * fpow(d, -m_lin) * dClindP;
+    Real dve_dP = fpow(eta_ve, 2) * dummy;
     // plastic return mapping on gdot
-    double gdot = 0.0, dQdtxx = 0, dQdtzz = 0, dQdtxz = 0, dQdP = 0, divp = 0.0, Pc = P;
-    double dlamdExx = 0, dlamdEzz = 0, dlamdExz = 0, dlamdP = 0;
-    double dvep_dExx = 0, dvep_dEzz = 0, dvep_dExz = 0, dvep_dP = 0;
-    double F_trial = Tii - Tyield;
-    const bool is_pl = F_trial > 1e-17;
+    Real gdot = Real(0.0), dQdtxx = 0, dQdtzz = 0, dQdtxz = 0, dQdP = 0, divp = Real(0.0), Pc = P;
+    Real dlamdExx = 0, dlamdEzz = 0, dlamdExz = 0, dlamdP = 0;
+    Real dvep_dExx = 0, dvep_dEzz = 0, dvep_dExz = 0, dvep_dP = 0;
+    Real F_trial = Tii - Tyield;
+    const bool is_pl = F_trial > Real(1e-17);
     if (is_pl) {
-        const double in_vp = 1.0 / n_vp;
+        const Real in_vp = Real(1.0) / n_vp;
         eta_vp = eta_vp0 * fpow(Eii, in_vp - 1);
         gdot = F_trial / (eta_ve + eta_vp + K * dt * sin_fric * sin_dil);
-        dQdtxx = Txx * 0.5 * iTii; dQdtzz = Tzz * 0.5 * iTii; dQdtxz = Txz * iTii;
-        const double F_trial0 = F_trial, iF0 = 1.0 / F_trial0;
+        dQdtxx = Txx * Real(0.5) * iTii; dQdtzz = Tzz * Real(0.5) * iTii; dQdtxz = Txz * iTii;
+        const Real F_trial0 = F_trial, iF0 = Real(1.0) / F_trial0;
         bool vp_done = false;
         if (guess) {
             // learned start: gdot = fraction * 2 Eii, at most MDZ_POLISH_STEPS
             // Newton updates, the reference's own convergence test
-            double frac = (double)guess[1];
-            frac = frac > 1e-6 ? (frac < 1.0 ? frac : 1.0) : 1e-6;
-            const double gdot_plain = gdot;
-            gdot = frac * 2.0 * Eii;
+            Real frac = (Real)guess[1];
+            frac = frac > Real(1e-6) ? (frac < Real(1.0) ? frac : Real(1.0)) : Real(1e-6);
+            const Real gdot_plain = gdot;
+            gdot = frac * Real(2.0) * Eii;
             for (it = 0; it <= MDZ_POLISH_STEPS; it++) {
                 dQdP = -sin_dil;
                 divp = -gdot * dQdP;
                 Pc = P + K * dt * divp;
-                eta_vp = eta_vp0 * fpow(fabs(gdot), in_vp - 1.0);
+                eta_vp = eta_vp0 * fpow(mfabs(gdot), in_vp - Real(1.0));
                 Tyield = C * cos_fric + Pc * sin_fric + gdot * eta_vp;
                 F_trial = Tii - eta_ve * gdot - Tyield;
-                res = fabs(F_trial);
+                res = mfabs(F_trial);
                 if (res < tol || res * iF0 < tol) { vp_done = true; break; }
                 if (it == MDZ_POLISH_STEPS) break;
-                double dFdgdot = -eta_ve - eta_vp * in_vp - K * dt * sin_fric * sin_dil;
+                Real dFdgdot = -eta_ve - eta_vp * in_vp - K * dt * sin_fric * sin_dil;
                 gdot -= F_trial / dFdgdot;
             }
             o.vp_its = it;
@@ -331,100 +352,136 @@ __device__ void visc_local(int p, double G, double T, double P, double d, double
             dQdP = -sin_dil;
             divp = -gdot * dQdP;
             Pc = P + K * dt * divp;
-            eta_vp = eta_vp0 * fpow(fabs(gdot), in_vp - 1.0);
+            eta_vp = eta_vp0 * fpow(mfabs(gdot), in_vp - Real(1.0));
             Tyield = C * cos_fric + Pc * sin_fric + gdot * eta_vp;
             F_trial = Tii - eta_ve * gdot - Tyield;
-            res = fabs(F_trial);
+            res = mfabs(F_trial);
             if (res < tol || res * iF0 < tol) break;
-            double dFdgdot = -eta_ve - eta_vp * in_vp - K * dt * sin_fric * sin_dil;
+            Real dFdgdot = -eta_ve - eta_vp * in_vp - K * dt * sin_fric * sin_dil;
             gdot -= F_trial / dFdgdot;
         }
         if (!vp_done) {
             o.vp_its = it + (guess ? MDZ_POLISH_STEPS : 0);
             if (it == nitmax - 1 && (res > tol || res * iF0 > tol)) o.vp_fail = 1;
         }
-        Txx = 2.0 * eta_ve * (Exx - gdot * dQdtxx);
-        Tzz = 2.0 * eta_ve * (Ezz - gdot * dQdtzz);
-        double Tyy = -(Txx + Tzz);
-        Txz = 2.0 * eta_ve * (Exz - gdot * dQdtxz / 2.0);
-        Tii = sqrt(0.5 * (fpow(Txx, 2.0) + fpow(Tzz, 2.0) + fpow(Tyy, 2.0)) + fpow(Txz, 2.0));
-        eta_vep = Tii * 0.5 * iEii;
-        o.Eii_pl = gdot / 2.0;
-        Tii = 2.0 * eta_vep * Eii;
+        Txx = Real(2.0) * eta_ve * (Exx - gdot * dQdtxx);
+        Tzz = Real(2.0) * eta_ve * (Ezz - gdot * dQdtzz);
+        Real Tyy = -(Txx + Tzz);
+        Txz = Real(2.0) * eta_ve * (Exz - gdot * dQdtxz / Real(2.0));
+        Tii = msqrt(Real(0.5) * (fpow(Txx, Real(2.0)) + fpow(Tzz, Real(2.0)) + fpow(Tyy, Real(2.0))) + fpow(Txz, Real(2.0)));
+        eta_vep = Tii * Real(0.5) * iEii;
+        o.Eii_pl = gdot / Real(2.0);
+        Tii = Real(2.0) * eta_vep * Eii;
         o.OverS = eta_vp * gdot;
         o.Pcorr = Pc;
         // visco-elasto-plastic tangent
-        const double ev = eta_ve * iEii;
-        double dFdExx = (2.0 * Exx + Ezz) * ev + 2.0 * Eii * dve_dExx;
-        double dFdEzz = (2.0 * Ezz + Exx) * ev + 2.0 * Eii * dve_dEzz;
-        double dFdExz = 2.0 * Exz * ev + 2.0 * Eii * dve_dExz;
-        double dFdP = -sin_fric + 2.0 * Eii * dve_dP;
-        double gg = 1.0 / (eta_ve + eta_vp * in_vp + K * dt * sin_fric * sin_dil);
-        dlamdExx = gg * (dFdExx - gdot * (dve_dExx + K * dt * sin_fric * 0.0));
-        dlamdEzz = gg * (dFdEzz - gdot * (dve_dEzz + K * dt * sin_fric * 0.0));
-        dlamdExz = gg * (dFdExz - gdot * (dve_dExz + K * dt * sin_fric * 0.0));
-        dlamdP = gg * (dFdP - gdot * (dve_dP + K * dt * sin_fric * 0.0));
-        double q = in_vp - 1.0;
-        const double evg = eta_vp / gdot;
-        double dvp_dExx = evg * dlamdExx * q, dvp_dEzz = evg * dlamdEzz * q;
-        double dvp_dExz = evg * dlamdExz * q, dvp_dP = evg * dlamdP * q;
-        double a = eta_vp + K * dt * sin_fric * sin_dil;
-        const double TyE3 = Tyield * 0.5 * iEii * iEii * iEii, h2 = 0.5 * iEii;   // Tyield / (2 Eii^3), 1 / (2 Eii)
-        dvep_dExx = -0.5 * (2.0 * Exx + Ezz) * TyE3 + (a * dlamdExx + gdot * dvp_dExx + gdot * K * dt * sin_fric * 0.0) * h2;
-        dvep_dEzz = -0.5 * (2.0 * Ezz + Exx) * TyE3 + (a * dlamdEzz + gdot * dvp_dEzz + gdot * K * dt * sin_fric * 0.0) * h2;
-        dvep_dExz = -Exz * TyE3 + (a * dlamdExz + gdot * dvp_dExz + gdot * K * dt * sin_fric * 0.0) * h2;
-        dvep_dP = (sin_fric + a * dlamdP + gdot * dvp_dP + gdot * K * dt * sin_fric * 0.0) * h2;
+        const Real ev = eta_ve * iEii;
+        Real dFdExx = (Real(2.0) * Exx + Ezz) * ev + Real(2.0) * Eii * dve_dExx;
+        Real dFdEzz = (Real(2.0) * Ezz + Exx) * ev + Real(2.0) * Eii * dve_dEzz;
+        Real dFdExz = Real(2.0) * Exz * ev + Real(2.0) * Eii * dve_dExz;
+        Real dFdP = -sin_fric + Real(2.0) * Eii * dve_dP;
+        Real gg = Real(1.0) / (eta_ve + eta_vp * in_vp + K * dt * sin_fric * sin_dil);
+        dlamdExx = gg * (dFdExx - gdot * (dve_dExx + K * dt * sin_fric * Real(0.0)));
+        dlamdEzz = gg * (dFdEzz - gdot * (dve_dEzz + K * dt * sin_fric * Real(0.0)));
+        dlamdExz = gg * (dFdExz - gdot * (dve_dExz + K * dt * sin_fric * Real(0.0)));
+        dlamdP = gg * (dFdP - gdot * (dve_dP + K * dt * sin_fric * Real(0.0)));
+        Real q = in_vp - Real(1.0);
+        const Real evg = eta_vp / gdot;
+        Real dvp_dExx = evg * dlamdExx * q, dvp_dEzz = evg * dlamdEzz * q;
+        Real dvp_dExz = evg * dlamdExz * q, dvp_dP = evg * dlamdP * q;
+        Real a = eta_vp + K * dt * sin_fric * sin_dil;
+        const Real TyE3 = Tyield * Real(0.5) * iEii * iEii * iEii, h2 = Real(0.5) * iEii;   // Tyield / (2 Eii^3), 1 / (2 Eii)
+        dvep_dExx = -Real(0.5) * (Real(2.0) * Exx + Ezz) * TyE3 + (a * dlamdExx + gdot * dvp_dExx + gdot * K * dt * sin_fric * Real(0.0)) * h2;
+        dvep_dEzz = -Real(0.5) * (Real(2.0) * Ezz + Exx) * TyE3 + (a * dlamdEzz + gdot * dvp_dEzz + gdot * K * dt * sin_fric * Real(0.0)) * h2;
+        dvep_dExz = -Exz * TyE3 + (a * dlamdExz + gdot * dvp_dExz + gdot * K * dt * sin_fric * Real(0.0)) * h2;
+        dvep_dP = (sin_fric + a * dlamdP + gdot * dvp_dP + gdot * K * dt * sin_fric * Real(0.0)) * h2;
     }
     o.gdot = gdot;
-    double inv_eta_diss = 0.0;
-    if (dislocation) inv_eta_diss += 1.0 / eta_pwl;
-    if (diffusion) inv_eta_diss += 1.0 / eta_lin;
-    if (constant) inv_eta_diss += 1.0 / eta_cst;
+    Real inv_eta_diss = Real(0.0);
+    if (dislocation) inv_eta_diss += Real(1.0) / eta_pwl;
+    if (diffusion) inv_eta_diss += Real(1.0) / eta_lin;
+    if (constant) inv_eta_diss += Real(1.0) / eta_cst;
     if (!is_pl) {
         o.detadexx = dve_dExx; o.detadezz = dve_dEzz; o.detadexz = dve_dExz; o.detadp = dve_dP;
         o.etaVE = eta_ve;
-        o.ddivpdexx = 0.0; o.ddivpdezz = 0.0; o.ddivpdexz = 0.0; o.ddivpdp = 0.0;
+        o.ddivpdexx = Real(0.0); o.ddivpdezz = Real(0.0); o.ddivpdexz = Real(0.0); o.ddivpdp = Real(0.0);
     } else {
         o.detadexx = dvep_dExx; o.detadezz = dvep_dEzz; o.detadexz = dvep_dExz; o.detadp = dvep_dP;
         o.etaVE = eta_vep;
-        o.ddivpdexx = -dQdP * dlamdExx + gdot * 0.0;
-        o.ddivpdezz = -dQdP * dlamdEzz + gdot * 0.0;
-        o.ddivpdexz = -dQdP * dlamdExz + gdot * 0.0;
-        o.ddivpdp = -dQdP * dlamdP + gdot * 0.0 + 0.0;
-        inv_eta_diss += 1.0 / eta_vep;
+        o.ddivpdexx = -dQdP * dlamdExx + gdot * Real(0.0);
+        o.ddivpdezz = -dQdP * dlamdEzz + gdot * Real(0.0);
+        o.ddivpdexz = -dQdP * dlamdExz + gdot * Real(0.0);
+        o.ddivpdp = -dQdP * dlamdP + gdot * Real(0.0) + Real(0.0);
+        inv_eta_diss += Real(1.0) / eta_vep;
     }
     // eta_pwl is re-evaluated unconditionally in the reference (C_pwl = 0 when
     // dislocation creep is off, which makes the dislocation parts vanish); Tii
     // is still the visco-elastic one unless the plastic branch changed it
     // 1 / (2 eta_pwl) = C_pwl Tii^(n-1): no division of the reference's
     // fpow(2 C_pwl, -1) fpow(Tii, 1 - n) is needed where Tii^n is known
-    const double h_pwl = !(C_pwl > 0.0) ? 0.0 : (dislocation && !is_pl ? C_pwl * Tn * iTii : C_pwl * fpow(Tii, n_pwl - 1.0));
-    eta_pwl = 0.5 / h_pwl;
-    o.Exx_el = (double)elastic * (Txx - Txx0) * i2eta_el;
-    o.Ezz_el = (double)elastic * (Tzz - Tzz0) * i2eta_el;
-    o.Exz_el = (double)elastic * (Txz - Txz0) * i2eta_el;
+    const Real h_pwl = !(C_pwl > Real(0.0)) ? Real(0.0) : (dislocation && !is_pl ? C_pwl * Tn * iTii : C_pwl * fpow(Tii, n_pwl - Real(1.0)));
+    eta_pwl = Real(0.5) / h_pwl;
+    o.Exx_el = (Real)elastic * (Txx - Txx0) * i2eta_el;
+    o.Ezz_el = (Real)elastic * (Tzz - Tzz0) * i2eta_el;
+    o.Exz_el = (Real)elastic * (Txz - Txz0) * i2eta_el;
     o.Exx_diss = gdot * dQdtxx + Exx_lin + Txx * h_pwl + Exx_cst;
     o.Ezz_diss = gdot * dQdtzz + Ezz_lin + Tzz * h_pwl + Ezz_cst;
-    o.Exz_diss = gdot * dQdtxz / 2.0 + Exz_lin + Txz * h_pwl + Exz_cst;
-    o.Eii_el = (double)elastic * fabs(Tii - Tii0) * i2eta_el;
+    o.Exz_diss = gdot * dQdtxz / Real(2.0) + Exz_lin + Txz * h_pwl + Exz_cst;
+    o.Eii_el = (Real)elastic * mfabs(Tii - Tii0) * i2eta_el;
     o.Eii_pwl = Tii * h_pwl;
     o.Eii_lin = Eii_lin;
     o.Eii_cst = Eii_cst;
     o.div_pl = divp;
     o.div_el = -(Pc - P0) / (K * dt);
-    double eta = 1.0 / inv_eta_diss;
-    o.VEcoeff = elastic == 0 ? 0.0 : 2.0 * eta_ve * i2eta_el;
+    Real eta = Real(1.0) / inv_eta_diss;
+    o.VEcoeff = elastic == 0 ? Real(0.0) : Real(2.0) * eta_ve * i2eta_el;
     if (prm.step == 0) o.etaVE = eta;
     o.txx = Txx; o.tzz = Tzz; o.txz = Txz;
-    if (eta > prm.maxeta) eta = prm.maxeta;
-    if (eta < prm.mineta) eta = prm.mineta;
-    const bool clamped = o.etaVE > prm.maxeta || o.etaVE < prm.mineta;
-    if (o.etaVE > prm.maxeta) o.etaVE = prm.maxeta;
-    if (o.etaVE < prm.mineta) o.etaVE = prm.mineta;
+    if (eta > Real(prm.maxeta)) eta = Real(prm.maxeta);
+    if (eta < Real(prm.mineta)) eta = Real(prm.mineta);
+    const bool clamped = o.etaVE > Real(prm.maxeta) || o.etaVE < Real(prm.mineta);
+    if (o.etaVE > Real(prm.maxeta)) o.etaVE = Real(prm.maxeta);
+    if (o.etaVE < Real(prm.mineta)) o.etaVE = Real(prm.mineta);
     if (clamped && prm.clamp_tangent) {   // the limiter is flat: its tangent is zero
-        o.detadexx = 0.0; o.detadezz = 0.0; o.detadexz = 0.0; o.detadp = 0.0;
+        o.detadexx = Real(0.0); o.detadezz = Real(0.0); o.detadexz = Real(0.0); o.detadp = Real(0.0);
     }
     o.eta = eta;
+}
+
+
+// The reference's local solve in FP64 (all call sites but the inexact FP32
+// evaluations of k_viscosity_* use this one).
+__device__ __forceinline__ void visc_local(int p, double G, double T, double P, double d, double phi, double X0,
+                                           double Exx, double Ezz, double Exz, double Gxx, double Gzz, double Gxz,
+                                           double Txx0, double Tzz0, double Txz0, const mdz_materials &m,
+                                           const mdz_rheo_params &prm, double dil, double fric, double C, double P0,
+                                           double beta, visc_res &o, const float *guess = nullptr) {
+    visc_local_t<double>(p, G, T, P, d, phi, X0, Exx, Ezz, Exz, Gxx, Gzz, Gxz, Txx0, Tzz0, Txz0, m, prm, dil, fric,
+                         C, P0, beta, o, guess);
+}
+
+// One (node, phase) local solve: in FP32 when asked (an inexact evaluation
+// for a non-linear iteration far from convergence; FP64 transcendental
+// functions issue at a small fraction of the FP32 rate on this part), with
+// the FP64 solve taking over wherever the FP32 one failed or overflowed;
+// otherwise the FP64 solve, from the learned start when one is given.
+__device__ __forceinline__ void visc_node_phase(bool fp32, int p, double G, double T, double P, double d, double phi,
+                                                double X0, const double *E, double Txx0, double Tzz0, double Txz0,
+                                                const mdz_materials &m, const mdz_rheo_params &prm, double dil,
+                                                double fric, double C, double P0, double beta, visc_res &o,
+                                                const float *guess) {
+    if (fp32) {
+        visc_local_t<float>(p, (float)G, (float)T, (float)P, (float)d, (float)phi, (float)X0, (float)E[0],
+                            (float)E[1], (float)E[2], (float)E[3], (float)E[4], (float)E[5], (float)Txx0,
+                            (float)Tzz0, (float)Txz0, m, prm, (float)dil, (float)fric, (float)C, (float)P0,
+                            (float)beta, o, nullptr);
+        const bool ok = !o.ve_fail && !o.vp_fail && isfinite(o.eta) && isfinite(o.etaVE) && isfinite(o.txx) &&
+                        isfinite(o.tzz) && isfinite(o.txz) && isfinite(o.detadexx) && isfinite(o.detadezz) &&
+                        isfinite(o.detadexz) && isfinite(o.detadp) && isfinite(o.Pcorr);
+        if (ok) return;
+    }
+    visc_local(p, G, T, P, d, phi, X0, E[0], E[1], E[2], E[3], E[4], E[5], Txx0, Tzz0, Txz0, m, prm, dil, fric, C,
+               P0, beta, o, guess);
 }
 
 // Effective rates entering the local solve (isotropic form of the elastic
@@ -469,7 +526,7 @@ __device__ __forceinline__ void count_local(int *counters, int fails, int fallba
 // One thread per centroid: loop over phases with a fraction above 1e-13.
 __global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_materials m, mdz_rheo_params prm,
                                                              mdz_fields f, int *__restrict__ counters,
-                                                             const float2 *__restrict__ guess) {
+                                                             const float2 *__restrict__ guess, int fp32) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     int nc = g.ncx * g.ncz;
     if (c >= nc) return;
@@ -497,8 +554,8 @@ __global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_ma
                 const float2 q = guess[(size_t)p * nc + c];
                 gs[0] = q.x; gs[1] = q.y;
             }
-            visc_local(p, mu, T, P, d0, phi0, X0, E[0], E[1], E[2], E[3], E[4], E[5], sxx0, szz0, sxz0, m, prm, dil,
-                       fric, Coh, P0, bet, o, guess ? gs : nullptr);
+            visc_node_phase(fp32 != 0, p, mu, T, P, d0, phi0, X0, E, sxx0, szz0, sxz0, m, prm, dil, fric, Coh, P0, bet, o,
+                            guess ? gs : nullptr);
             fails += o.ve_fail + o.vp_fail;
             fallbacks += o.fallback;
             iters += o.ve_its + o.vp_its;
@@ -557,7 +614,7 @@ __global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_ma
 
 __global__ void __launch_bounds__(128) k_viscosity_vertices(mdz_dgrid g, mdz_materials m, mdz_rheo_params prm,
                                                             mdz_fields f, int *__restrict__ counters,
-                                                            const float2 *__restrict__ guess) {
+                                                            const float2 *__restrict__ guess, int fp32) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     int nv = g.Nx * g.Nz;
     if (c >= nv) return;
@@ -582,8 +639,8 @@ __global__ void __launch_bounds__(128) k_viscosity_vertices(mdz_dgrid g, mdz_mat
                 const float2 q = guess[(size_t)p * nv + c];
                 gs[0] = q.x; gs[1] = q.y;
             }
-            visc_local(p, mu, T, P, d0, phi0, X0, E[0], E[1], E[2], E[3], E[4], E[5], sxx0, szz0, sxz0, m, prm, dil,
-                       fric, Coh, P0, bet, o, guess ? gs : nullptr);
+            visc_node_phase(fp32 != 0, p, mu, T, P, d0, phi0, X0, E, sxx0, szz0, sxz0, m, prm, dil, fric, Coh, P0, bet, o,
+                            guess ? gs : nullptr);
             fails += o.ve_fail + o.vp_fail;
             fallbacks += o.fallback;
             iters += o.ve_its + o.vp_its;
@@ -895,7 +952,7 @@ mdz_status mdz_dev_mlp_samples(mdz_ctx *ctx, const mdz_materials *m, const mdz_r
 }
 
 mdz_status mdz_dev_viscosity(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm, const mdz_fields &f,
-                             int *d_counters, cudaStream_t st, bool learned) {
+                             int *d_counters, cudaStream_t st, bool learned, bool fp32) {
     const mdz_dgrid &g = ctx->g;
     int nc = g.ncx * g.ncz, nv = g.Nx * g.Nz;
     // vertex copies of centroid fields (NonNewtonianViscosityGrid :979-983)
@@ -906,7 +963,7 @@ mdz_status mdz_dev_viscosity(mdz_ctx *ctx, const mdz_materials *m, const mdz_rhe
     if ((s = mdz_dev_c2v(ctx, f.d0_n, f.d0_s, st)) != MDZ_OK) return s;
     if ((s = mdz_dev_c2v(ctx, f.phi0_n, f.phi0_s, st)) != MDZ_OK) return s;
     const float2 *guess_n = nullptr, *guess_s = nullptr;
-    if (learned) {
+    if (learned && !fp32) {
         float2 *buf = mdz_mlp_guess_buffer(ctx, (size_t)m->n_phases * (nc + nv));
         if (!buf) return mdz_fail(ctx, MDZ_ERR_CUDA, "learned guess: buffer allocation failed");
         if ((s = mdz_dev_mlp_guess(ctx, m, prm, f, buf, buf + (size_t)m->n_phases * nc, st)) != MDZ_OK) return s;
@@ -915,9 +972,9 @@ mdz_status mdz_dev_viscosity(mdz_ctx *ctx, const mdz_materials *m, const mdz_rhe
     }
     cudaEvent_t ev;
     mdz_prof_begin(ctx, MDZ_PROF_VISCOSITY, st, &ev);
-    k_viscosity_centroids<<<mdz_blocks(nc, 128), 128, 0, st>>>(g, *m, *prm, f, d_counters, guess_n);
+    k_viscosity_centroids<<<mdz_blocks(nc, 128), 128, 0, st>>>(g, *m, *prm, f, d_counters, guess_n, fp32 ? 1 : 0);
     MDZ_LAUNCHED(ctx);
-    k_viscosity_vertices<<<mdz_blocks(nv, 128), 128, 0, st>>>(g, *m, *prm, f, d_counters, guess_s);
+    k_viscosity_vertices<<<mdz_blocks(nv, 128), 128, 0, st>>>(g, *m, *prm, f, d_counters, guess_s, fp32 ? 1 : 0);
     MDZ_LAUNCHED(ctx);
     // algorithmic bytes: per centroid 17 + n_phases FP64 inputs and 35 outputs,
     // per vertex 17 + n_phases inputs and 12 outputs, plus the tags

@@ -253,11 +253,13 @@ struct step_timer {
 
 // Local rheology + RHS + Picard operators of the current state (UpdateNonLinearity).
 static mdz_status update_nonlinearity(mdz_ctx *ctx, const mdz_materials *mat, const mdz_model *M,
-                                      mdz_step_report *rep, cudaStream_t st) {
+                                      mdz_step_report *rep, cudaStream_t st, bool fp32 = false) {
     mdz_fields &f = ctx->d;
     mdz_status s;
     if ((s = mdz_dev_strain_rates(ctx, f, st)) != MDZ_OK) return s;
-    if (M->learned_guess) {
+    if (fp32) {
+        if ((s = mdz_dev_viscosity(ctx, mat, &M->rheo, f, ctx->d_counters, st, false, true)) != MDZ_OK) return s;
+    } else if (M->learned_guess) {
         if ((s = mdz_dev_viscosity_learned(ctx, mat, &M->rheo, f, ctx->d_counters, st)) != MDZ_OK) return s;
     } else {
         if ((s = mdz_dev_viscosity(ctx, mat, &M->rheo, f, ctx->d_counters, st)) != MDZ_OK) return s;
@@ -384,20 +386,36 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
     int nit = 0;
     bool use_newton = M->newton && !M->picard2newton;
     double rel_prev = -1.0, eta_prev = 0.1;   // forcing-term history (adaptive_lin_tol)
+    double rel_last = 1.0;                     // relative residual of the latest evaluation
     MDZ_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(int) * 4, st));
     MDZ_CUDA(ctx, cudaMemsetAsync(ctx->d_counters + 48, 0, sizeof(unsigned long long), st));
     for (nit = 0; nit <= M->nit_max; nit++) {
+        // inexact FP32 rheology far from convergence (fp32_rheology_above)
+        bool fp32 = M->fp32_rheology_above > 0.0 && (nit == 0 || rel_last > M->fp32_rheology_above);
         {
             step_timer T(st, &R.ms_rheology);
-            if ((s = update_nonlinearity(ctx, mat, M, &R, st)) != MDZ_OK) return s;
+            if ((s = update_nonlinearity(ctx, mat, M, &R, st, fp32)) != MDZ_OK) return s;
         }
         {
             step_timer T(st, &R.ms_residual);
             if ((s = residual_norms(ctx, r, st)) != MDZ_OK) return s;
         }
         if (nit == 0) memcpy(r0, r, sizeof r0);
+        bool conv = converged(M, r, r0) && (nit > 0 || (r[0] < M->abs_tol && r[1] < M->abs_tol && r[2] < M->abs_tol));
+        if (conv && fp32) {   // convergence is only decided on an FP64 evaluation
+            {
+                step_timer T(st, &R.ms_rheology);
+                if ((s = update_nonlinearity(ctx, mat, M, &R, st, false)) != MDZ_OK) return s;
+            }
+            {
+                step_timer T(st, &R.ms_residual);
+                if ((s = residual_norms(ctx, r, st)) != MDZ_OK) return s;
+            }
+            conv = converged(M, r, r0);
+        }
+        rel_last = relative_residual(r, r0);
         if (nit < MDZ_HISTORY) memcpy(R.res_history[nit], r, sizeof r);
-        if (converged(M, r, r0) && (nit > 0 || (r[0] < M->abs_tol && r[1] < M->abs_tol && r[2] < M->abs_tol))) {
+        if (conv) {
             R.converged = 1;
             break;
         }
