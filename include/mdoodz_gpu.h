@@ -421,11 +421,13 @@ typedef struct mdz_model {
      * rel_tol); 0: every solve to lin_rtol.  No counterpart in the reference,
      * whose direct solver has no tolerance. */
     int adaptive_lin_tol;
-    /* > 0: local rheology solves in FP32 (FP64 where one fails) while the
-     * largest relative block residual is above this value; the iterations that
-     * decide convergence, and the final update, always run in FP64.  0: FP64
-     * throughout.  No counterpart in the reference. */
-    double fp32_rheology_above;
+    /* the first fp32_rheology_its non-linear iterations evaluate the local
+     * rheology in FP32 (FP64 where a solve fails); convergence decisions and
+     * the final update always run in FP64.  0: FP64 throughout.  (FP32 stresses
+     * put a floor of ~1e-7 of the stress level under the momentum residual, so
+     * only the first, Picard-type iterations can use them.)  No counterpart in
+     * the reference. */
+    int fp32_rheology_its;
 } mdz_model;
 
 #define MDZ_HISTORY 32

@@ -386,12 +386,11 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
     int nit = 0;
     bool use_newton = M->newton && !M->picard2newton;
     double rel_prev = -1.0, eta_prev = 0.1;   // forcing-term history (adaptive_lin_tol)
-    double rel_last = 1.0;                     // relative residual of the latest evaluation
     MDZ_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, sizeof(int) * 4, st));
     MDZ_CUDA(ctx, cudaMemsetAsync(ctx->d_counters + 48, 0, sizeof(unsigned long long), st));
     for (nit = 0; nit <= M->nit_max; nit++) {
-        // inexact FP32 rheology far from convergence (fp32_rheology_above)
-        bool fp32 = M->fp32_rheology_above > 0.0 && (nit == 0 || rel_last > M->fp32_rheology_above);
+        // inexact FP32 rheology in the first iterations (fp32_rheology_its)
+        bool fp32 = nit < M->fp32_rheology_its;
         {
             step_timer T(st, &R.ms_rheology);
             if ((s = update_nonlinearity(ctx, mat, M, &R, st, fp32)) != MDZ_OK) return s;
@@ -413,7 +412,6 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
             }
             conv = converged(M, r, r0);
         }
-        rel_last = relative_residual(r, r0);
         if (nit < MDZ_HISTORY) memcpy(R.res_history[nit], r, sizeof r);
         if (conv) {
             R.converged = 1;

@@ -155,12 +155,12 @@ def config_lithosphere(Nx=1025, Nz=513, nm=4, seed=12345, precision=64, learned=
     # (Picard2Newton of the reference); 30 iterations at most
     # (no line search: the reference's default, line_search = 0; each defect
     # solve asks only for the reduction the non-linear iteration can use; the
-    # FP32 form also evaluates the local rheology in FP32 while the residual
-    # is above 1e-4 of its first value)
+    # FP32 form also evaluates the local rheology of the first two non-linear
+    # iterations in FP32)
     model = mdz.Model.make(prm, gz=-9.81 * L / S, newton=1, nit_max=30, rel_tol=1e-8, lin_rtol=1e-5,
                            line_search=0, precision=precision, learned_guess=learned, picard2newton=1,
                            pic2newt_cond=1e-1, nit_pic_max=10, newton_maxit=200, adaptive_lin_tol=1,
-                           fp32_rheology_above=1e-4 if precision == 32 else 0.0)
+                           fp32_rheology_its=2 if precision == 32 else 0)
     u, v = pure_shear_velocity(g, eps / sc.E)
     m = _markers_dict(x, z, ph, T=T)
     # initial pressure: lithostatic column of the layered densities (the
