@@ -101,6 +101,10 @@ LO_MLP, HI_MLP = [-18.0, 273.0, 0.0, 9.0], [-12.0, 1600.0, 5e9, 12.0]
 
 GUESS_STEPS = [3000]
 
+# DRAM bytes (read + write) per launch of a kernel class at 1025x513, from one
+# ncu capture of the FP32 form (profiles/vcycle_traffic_lithosphere_1025x513_fp32.md)
+TRAFFIC_PER_LAUNCH = {"mg_vcycle": 88.5e6}
+
 
 def train_guess(ctx, cfg, n=1 << 20, batch=65536, seed=1):
     """Tuples labelled by the plain local solve of the model's materials, then
@@ -351,7 +355,8 @@ def main():
                 "split": e2e_split},
         "gpu_launches": fast["launches"] // args.steps,
         "roofline": {"bound": "hbm", "kernel": k["name"], "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                     "frac": (achieved / hbm) if achieved else None,
+                     "traffic": TRAFFIC_PER_LAUNCH.get(k["name"]) if not size else None,
                      "peak_kind": peak_kind},
         "clocks": clk.summary(),
     }

@@ -28,6 +28,7 @@
 
 #define MG_MAX_LEVELS 16
 #define MG_DENSE_MAX 256
+#define MG_DENSE_SMEM (96 * 1024)   // [A | I] of the coarsest level in shared memory up to this size (n <= 78)
 #define MG_NST 31        // stencil coefficients per velocity row (15 same-component + 16 cross)
 #define MG_CENTER 7      // plane of the diagonal entry in both layouts
 #define GCR_MAX_M 48
@@ -953,8 +954,13 @@ __device__ __forceinline__ int dense_v(int Nx, int Nz, int i, int j) {
 template <typename T>
 __global__ void __launch_bounds__(512) k_coarse_dense_setup(stokes_geom G, const T *__restrict__ su,
                                                             const T *__restrict__ sv, int n,
-                                                            const int *__restrict__ map, double *A,
+                                                            const int *__restrict__ map, double *Ag,
                                                             T *__restrict__ AinvT, int *status) {
+    // [A | I] in shared memory when it fits (the launch passes the dynamic
+    // size), else in the global work array: each of the n elimination steps
+    // reads and writes all of it between barriers
+    extern __shared__ double dsm[];
+    double *A = (size_t)2 * n * n * sizeof(double) <= MG_DENSE_SMEM ? dsm : Ag;
     __shared__ double col[MG_DENSE_MAX];
     __shared__ int bad;
     const int Nx = G.Nx, Nz = G.Nz;
@@ -1359,6 +1365,10 @@ mdz_status mdz_solver_ensure(mdz_ctx *ctx) {
     memset(S->sc, 0, 64 * sizeof(double));
     S->bottom_cs[0] = mg_bottom_cluster_size<double>();
     S->bottom_cs[1] = mg_bottom_cluster_size<float>();
+    MDZ_CUDA(ctx, cudaFuncSetAttribute(k_coarse_dense_setup<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       MG_DENSE_SMEM));
+    MDZ_CUDA(ctx, cudaFuncSetAttribute(k_coarse_dense_setup<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       MG_DENSE_SMEM));
     MDZ_CUDA(ctx, cudaDeviceSynchronize());
     S->ready = true;
     return MDZ_OK;
@@ -1494,7 +1504,9 @@ static mdz_status mg_setup(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n, con
     }
     mg_level<T> &C = H.L[H.nlev - 1];
     if (C.ndense) {
-        k_coarse_dense_setup<T><<<1, 512, 0, st>>>(C.geom(), C.su, C.sv, C.ndense, C.dmap, C.Awork, C.AinvT, status);
+        const size_t smem = (size_t)2 * C.ndense * C.ndense * sizeof(double);
+        k_coarse_dense_setup<T><<<1, 512, smem <= MG_DENSE_SMEM ? smem : 0, st>>>(C.geom(), C.su, C.sv, C.ndense,
+                                                                              C.dmap, C.Awork, C.AinvT, status);
         MDZ_LAUNCHED(ctx);
     }
     {   // algorithmic bytes: viscosities in, D11 / D33 out; level-0 stencils
