@@ -102,7 +102,8 @@ LO_MLP, HI_MLP = [-18.0, 273.0, 0.0, 9.0], [-12.0, 1600.0, 5e9, 12.0]
 GUESS_STEPS = [3000]
 
 # DRAM bytes (read + write) per launch of a kernel class at 1025x513, from one
-# ncu capture of the FP32 form (profiles/vcycle_traffic_lithosphere_1025x513_fp32.md)
+# ncu capture of the FP32 form (dram__bytes_read.sum + dram__bytes_write.sum
+# over the kernels of 8 preconditioner applications, caches left warm)
 TRAFFIC_PER_LAUNCH = {"mg_vcycle": 88.5e6}
 
 
