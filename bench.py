@@ -265,7 +265,7 @@ def cpu_reference(size, budget_s=20.0):
     import mdz_setups
     import oracle_step
     nx, nz = size if size else (1025, 513)
-    strip_nz = 17
+    strip_nz = 9   # 8 cell rows: about 30 s of one core per sample
     cfg = mdz_setups.config_lithosphere(Nx=nx, Nz=strip_nz, precision=64)
     m = cfg["markers"]
     t0 = time.perf_counter()
