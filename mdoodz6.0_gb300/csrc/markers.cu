@@ -30,13 +30,13 @@ __device__ __forceinline__ int lower_line(double x, double X0, double h, double 
 // clamps as P2Mastah on centroids), per-cell counts.
 __global__ void k_bin_count(int n, const double *__restrict__ x, const double *__restrict__ z,
                             const int *__restrict__ phase, const double *__restrict__ xc,
-                            const double *__restrict__ zc, double dx, double dz, int ncx, int ncz,
-                            int *__restrict__ cell, int *__restrict__ count) {
+                            const double *__restrict__ zc, double dx, double dz, double idx, double idz, int ncx,
+                            int ncz, int *__restrict__ cell, int *__restrict__ count) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     if (phase[k] == -1) { cell[k] = -1; return; }
-    int ic = nearest_line(x[k], xc[0], dx, 1.0 / dx, ncx);
-    int jc = nearest_line(z[k], zc[0], dz, 1.0 / dz, ncz);
+    int ic = nearest_line(x[k], xc[0], dx, idx, ncx);
+    int jc = nearest_line(z[k], zc[0], dz, idz, ncz);
     int c = ic + jc * ncx;
     cell[k] = c;
     atomicAdd(&count[c], 1);
@@ -134,7 +134,7 @@ mdz_status mdz_ensure_bins(mdz_ctx *ctx, cudaStream_t st) {
     MDZ_CUDA(ctx, cudaMemsetAsync(B.cursor, 0, sizeof(int) * (nc + 1), st));
     if (n > 0) {
         k_bin_count<<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, ctx->m.x, ctx->m.z, ctx->m.phase, g.xc, g.zc, g.dx, g.dz,
-                                                           g.ncx, g.ncz, B.cell, B.count);
+                                                           g.idx, g.idz, g.ncx, g.ncz, B.cell, B.count);
         MDZ_LAUNCHED(ctx);
     }
     int nb = (nc + 1023) / 1024;
