@@ -1110,7 +1110,7 @@ struct mg_bottom_args {
 };
 
 // points a bottom launch of `cs` CTAs takes on per level
-static inline long long mg_bottom_points(int cs) { return (long long)cs * MG_BOTTOM_THREADS * (cs == 1 ? 4 : 3); }
+static inline long long mg_bottom_points(int cs) { return (long long)cs * MG_BOTTOM_THREADS * (cs == 1 ? 4 : 2); }
 
 template <typename T>
 __global__ void __launch_bounds__(MG_BOTTOM_THREADS) k_mg_bottom(const __grid_constant__ mg_bottom_args<T> A) {
