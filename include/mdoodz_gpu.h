@@ -428,6 +428,12 @@ typedef struct mdz_model {
      * only the first, Picard-type iterations can use them.)  No counterpart in
      * the reference. */
     int fp32_rheology_its;
+    /* > 0: a defect solve whose non-linear iteration has its largest relative
+     * block residual below this value keeps the multigrid hierarchy of the
+     * previous solve (the viscosities have nearly converged) instead of
+     * rebuilding it.  0: rebuilt for every solve.  No counterpart in the
+     * reference. */
+    double mg_reuse_below;
 } mdz_model;
 
 #define MDZ_HISTORY 32

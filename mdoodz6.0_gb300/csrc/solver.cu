@@ -80,6 +80,7 @@ template <typename T>
 struct mg_hier {
     int nlev = 0;
     bool newton = false;          // level 0 is the probed Newton block (smoothed by its stencil)
+    bool built = false;           // mg_setup has filled the levels at least once
     double *pmean = nullptr;      // preconditioner scratch: pressure sum and count
     mg_level<T> L[MG_MAX_LEVELS];
 };
@@ -1461,6 +1462,7 @@ static mdz_status mg_setup(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n, con
     mg_level<T> &F = H.L[0];
     int nc = F.ncx * F.ncz, nv = F.Nx * F.Nz;
     H.newton = newton;
+    H.built = true;
     cudaEvent_t ev;
     mdz_prof_begin(ctx, MDZ_PROF_MG_SETUP, st, &ev);
     k_fill_D11_D33<T><<<mdz_blocks(nv > nc ? nv : nc), MDZ_THREADS, 0, st>>>(nc, nv, eta_n, eta_s, F.D11, F.D33);
@@ -2158,7 +2160,7 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
 // contiguous, length n), FP64.  precision 64: plain FP64 GCR + FP64 V-cycle;
 // precision 32: FP64 defect correction around FP32 GCR + FP32 V-cycle.
 mdz_status mdz_dev_solve(mdz_ctx *ctx, const mdz_fields &f, bool newton, int precision, double rtol, int maxit,
-                         const double *F, double *dx, mdz_solve_stats *stats, cudaStream_t st) {
+                         const double *F, double *dx, mdz_solve_stats *stats, cudaStream_t st, bool reuse_mg) {
     mdz_status s = mdz_solver_ensure(ctx);
     if (s != MDZ_OK) return s;
     mdz_solver *SV = ctx->solver;
@@ -2169,8 +2171,9 @@ mdz_status mdz_dev_solve(mdz_ctx *ctx, const mdz_fields &f, bool newton, int pre
     int its = 0, total = 0, cycles = 0;
     double rel = 1.0;
     if (precision == 64) {
-        if ((s = mg_setup<double>(ctx, SV->mg64, f.eta_n, f.eta_s, K64, newton && SV->mg_jacobian, st)) != MDZ_OK)
-            return s;
+        const bool nh = newton && SV->mg_jacobian;
+        if (!(reuse_mg && SV->mg64.built && SV->mg64.newton == nh))
+            if ((s = mg_setup<double>(ctx, SV->mg64, f.eta_n, f.eta_s, K64, nh, st)) != MDZ_OK) return s;
         MDZ_CUDA(ctx, cudaMemcpyAsync(S64.r, F, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
         if ((s = gcr_solve<double, double>(ctx, S64, S64, SV->mg64, K64, newton, f.eta_n, rtol, maxit, &its, &rel,
                                            st)) != MDZ_OK)
@@ -2191,8 +2194,9 @@ mdz_status mdz_dev_solve(mdz_ctx *ctx, const mdz_fields &f, bool newton, int pre
         }
         stokes_coefs<float> K32{S32.Dc[0], S32.Dc[1], S32.Dc[2], S32.Dc[3], S32.Dc[4], S32.Dc[5], S32.Dc[6],
                                 S32.Dc[7], S32.Dc[8], S32.Dc[9], S32.Dc[10], S32.Dc[11]};
-        if ((s = mg_setup<float>(ctx, SV->mg32, f.eta_n, f.eta_s, K32, newton && SV->mg_jacobian, st)) != MDZ_OK)
-            return s;
+        const bool nh = newton && SV->mg_jacobian;
+        if (!(reuse_mg && SV->mg32.built && SV->mg32.newton == nh))
+            if ((s = mg_setup<float>(ctx, SV->mg32, f.eta_n, f.eta_s, K32, nh, st)) != MDZ_OK) return s;
         // defect correction: r64 = F - K64 dx64 ; solve K32 e = r64 ; dx64 += e
         MDZ_CUDA(ctx, cudaMemsetAsync(dx, 0, sizeof(double) * n, st));
         MDZ_CUDA(ctx, cudaMemcpyAsync(S64.r, F, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));

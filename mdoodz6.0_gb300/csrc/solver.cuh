@@ -13,5 +13,8 @@ mdz_status mdz_solver_ensure(mdz_ctx *ctx);
 void mdz_solver_free(mdz_ctx *ctx);
 int mdz_solver_levels(const mdz_ctx *ctx);
 // K dx = F on device arrays (u | v | p contiguous grid layout).
+// reuse_mg: keep the multigrid hierarchy of the previous solve of this
+// precision (if it was built for the same operator) instead of rebuilding it
+// from the current viscosities.
 mdz_status mdz_dev_solve(mdz_ctx *ctx, const mdz_fields &f, bool newton, int precision, double rtol, int maxit,
-                         const double *F, double *dx, mdz_solve_stats *stats, cudaStream_t st);
+                         const double *F, double *dx, mdz_solve_stats *stats, cudaStream_t st, bool reuse_mg = false);

@@ -434,6 +434,7 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
         // forcing term (choice 2, gamma 0.9, alpha 2, with its safeguard) kept
         // within [lin_rtol, 0.1] and no tighter than half the way to rel_tol
         double eta = M->lin_rtol;
+        const bool reuse_mg = M->mg_reuse_below > 0.0 && nit > 0 && relative_residual(r, r0) < M->mg_reuse_below;
         if (M->adaptive_lin_tol) {
             const double rel = relative_residual(r, r0);
             double e = rel_prev > 0.0 ? 0.9 * (rel / rel_prev) * (rel / rel_prev) : 0.1;
@@ -448,7 +449,7 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
         {
             step_timer T(st, &R.ms_solve);
             const int maxit = use_newton && M->newton_maxit > 0 ? M->newton_maxit : M->lin_maxit;
-            s = mdz_dev_solve(ctx, f, use_newton, M->precision, eta, maxit, B.F, B.dx, &ss, st);
+            s = mdz_dev_solve(ctx, f, use_newton, M->precision, eta, maxit, B.F, B.dx, &ss, st, reuse_mg);
             if (s != MDZ_OK) return s;
             R.linear_its += ss.iterations;
             R.newton_its += use_newton ? 1 : 0;

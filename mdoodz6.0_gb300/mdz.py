@@ -551,16 +551,16 @@ class Model(C.Structure):
                 ("precision", C.c_int), ("learned_guess", C.c_int), ("itp_stencil", C.c_int),
                 ("softening", C.c_int), ("advect", C.c_int), ("picard2newton", C.c_int),
                 ("pic2newt_cond", C.c_double), ("nit_pic_max", C.c_int), ("newton_maxit", C.c_int),
-                ("adaptive_lin_tol", C.c_int), ("fp32_rheology_its", C.c_int)]
+                ("adaptive_lin_tol", C.c_int), ("fp32_rheology_its", C.c_int), ("mg_reuse_below", C.c_double)]
 
     @classmethod
     def make(cls, rheo, gx=0.0, gz=0.0, newton=1, nit_max=10, rel_tol=1e-8, abs_tol=1e-300, lin_rtol=1e-5,
              lin_maxit=500, line_search=0, line_search_min=0.0, precision=64, learned_guess=0, itp_stencil=1,
              softening=0, advect=1, picard2newton=0, pic2newt_cond=1e-1, nit_pic_max=10, newton_maxit=0,
-             adaptive_lin_tol=0, fp32_rheology_its=0):
+             adaptive_lin_tol=0, fp32_rheology_its=0, mg_reuse_below=0.0):
         return cls(rheo, gx, gz, newton, nit_max, rel_tol, abs_tol, lin_rtol, lin_maxit, line_search,
                    line_search_min, precision, learned_guess, itp_stencil, softening, advect, picard2newton,
-                   pic2newt_cond, nit_pic_max, newton_maxit, adaptive_lin_tol, fp32_rheology_its)
+                   pic2newt_cond, nit_pic_max, newton_maxit, adaptive_lin_tol, fp32_rheology_its, mg_reuse_below)
 
 
 class StepReport(C.Structure):
