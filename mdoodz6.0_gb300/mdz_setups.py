@@ -156,11 +156,12 @@ def config_lithosphere(Nx=1025, Nz=513, nm=4, seed=12345, precision=64, learned=
     # (no line search: the reference's default, line_search = 0; each defect
     # solve asks only for the reduction the non-linear iteration can use; the
     # FP32 form also evaluates the local rheology of the first two non-linear
-    # iterations in FP32)
+    # iterations in FP32; once the residual is below 1e-2 of its first value
+    # the multigrid hierarchy of the previous solve is kept)
     model = mdz.Model.make(prm, gz=-9.81 * L / S, newton=1, nit_max=30, rel_tol=1e-8, lin_rtol=1e-5,
                            line_search=0, precision=precision, learned_guess=learned, picard2newton=1,
                            pic2newt_cond=1e-1, nit_pic_max=10, newton_maxit=200, adaptive_lin_tol=1,
-                           fp32_rheology_its=2 if precision == 32 else 0)
+                           fp32_rheology_its=2 if precision == 32 else 0, mg_reuse_below=1e-2)
     u, v = pure_shear_velocity(g, eps / sc.E)
     m = _markers_dict(x, z, ph, T=T)
     # initial pressure: lithostatic column of the layered densities (the
