@@ -81,7 +81,8 @@ typedef struct mdz_ctx mdz_ctx;
 /* Create a context on the current CUDA device: copies the grid description to
  * the device and reserves room for `max_markers` markers.  Replaces the
  * reference's GridAlloc/PartAlloc (SOURCE/MemoryAllocFree.c:182,333) for the
- * device mirrors; the host arrays stay owned by the caller. */
+ * device mirrors; the host arrays stay owned by the caller.  Grids of 3 to
+ * 65 535 lines a side (MDZ_ERR_ARG otherwise). */
 mdz_status mdz_create(mdz_ctx **ctx, const mdz_grid_desc *grid, int n_phases, long long max_markers);
 void mdz_destroy(mdz_ctx *ctx);
 const char *mdz_last_error(const mdz_ctx *ctx);

@@ -53,8 +53,10 @@ extern "C" mdz_status mdz_create(mdz_ctx **out, const mdz_grid_desc *d, int n_ph
     if (!out || !d) return MDZ_ERR_ARG;
     *out = nullptr;
     mdz_ctx *ctx = new mdz_ctx();
-    if (d->Nx < 3 || d->Nz < 3 || n_phases < 1 || n_phases > MDZ_MAX_PHASES || max_markers < 0 ||
-        max_markers > (1LL << 31) - 1) {
+    // (grids up to 65 535 lines a side: the marker kernels' index fast path,
+    // ceil_quot, is exact up to quotients of 2^16)
+    if (d->Nx < 3 || d->Nz < 3 || d->Nx > 65535 || d->Nz > 65535 || n_phases < 1 || n_phases > MDZ_MAX_PHASES ||
+        max_markers < 0 || max_markers > (1LL << 31) - 1) {
         mdz_fail(ctx, MDZ_ERR_ARG, "mdz_create: bad grid size, phase count or marker capacity");
         delete ctx;
         return MDZ_ERR_ARG;

@@ -32,11 +32,13 @@ struct mdz_dgrid {
 // FP64 division is a long instruction sequence on this part, and the marker
 // kernels take several per marker where the reference divides by the grid
 // spacing; the cell indices must still match the reference's bit for bit.
+// The margin is fixed for |q| up to 2^16 (grids have fewer lines; a quotient
+// beyond that lies outside the grid, where every caller clamps the index).
+#define MDZ_CEIL_QUOT_TOL (16.0 * 2.220446049250313e-16 * 65538.0)
 __device__ __forceinline__ double ceil_quot(double d, double h, double ih, double add) {
     const double q = d * ih + add;
-    const double c = ceil(q);
-    const double tol = 16.0 * 2.220446049250313e-16 * (fabs(q) + 1.0);
-    if (c - q > tol && q - (c - 1.0) > tol) return c;
+    const double c = ceil(q), f = c - q;
+    if (f > MDZ_CEIL_QUOT_TOL && f < 1.0 - MDZ_CEIL_QUOT_TOL) return c;
     return ceil(d / h + add);
 }
 

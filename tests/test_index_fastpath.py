@@ -13,8 +13,9 @@ EPS = np.finfo(np.float64).eps
 def ceil_quot(d, h, ih, add, fma):
     q = (np.longdouble(d) * np.longdouble(ih) + np.longdouble(add)).astype(np.float64) if fma else d * ih + add
     c = np.ceil(q)
-    tol = 16.0 * EPS * (np.abs(q) + 1.0)
-    fast = (c - q > tol) & (q - (c - 1.0) > tol)
+    tol = 16.0 * EPS * 65538.0
+    f = c - q
+    fast = (f > tol) & (f < 1.0 - tol)
     return np.where(fast, c, np.ceil(d / h + add))
 
 
