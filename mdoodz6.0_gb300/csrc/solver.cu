@@ -1104,6 +1104,7 @@ struct mg_bottom_level {
 template <typename T>
 struct mg_bottom_args {
     int nlev, nu1, nu2, ndense;   // nlev levels, the last one the dense coarsest
+    int lsplit;                   // first level run by CTA 0 alone (nlev: none)
     T omega;
     const int *dmap;
     const T *AinvT;
@@ -1118,75 +1119,93 @@ __global__ void __launch_bounds__(MG_BOTTOM_THREADS) k_mg_bottom(const __grid_co
     __shared__ T fs[MG_DENSE_MAX];
     T *xu[MG_BOTTOM_MAX], *xv[MG_BOTTOM_MAX], *yu[MG_BOTTOM_MAX], *yv[MG_BOTTOM_MAX];
     for (int l = 0; l < A.nlev; l++) { xu[l] = A.L[l].xu; xv[l] = A.L[l].xv; yu[l] = A.L[l].yu; yv[l] = A.L[l].yv; }
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
     // barrier over every thread of the launch: the grid is one cluster (or one CTA);
     // release / acquire at cluster scope orders the global-memory phases
-    auto bar = [&]() {
+    auto cbar = [&]() {
         if (gridDim.x > 1) cooperative_groups::this_cluster().sync();
         else __syncthreads();
     };
+    auto tbar = [&]() { __syncthreads(); };
     auto swap_xy = [&](int l) {
         T *t = xu[l]; xu[l] = yu[l]; yu[l] = t;
         t = xv[l]; xv[l] = yv[l]; yv[l] = t;
     };
-    for (int l = 0; l < A.nlev - 1; l++) {   // descent
+    // One level's descent (pre-smoothing, residual, restriction) or ascent
+    // (prolongation, post-smoothing) by a team of threads t0, t0 + nt, ...
+    // (act = false: the thread only keeps its pointer swaps in step) with the
+    // team's barrier after each phase.
+    auto down = [&](int l, bool act, int t0, int nt, auto &&sync) {
         const mg_bottom_level<T> &L = A.L[l];
         const int W = L.G.Nx + 1, npt = W * (L.G.Nz + 1);
-        for (int p = tid; p < npt; p += nthr)
+        for (int p = t0; act && p < npt; p += nt)
             st_smooth_pt<T>(L.G, L.su, L.sv, nullptr, nullptr, L.fu, L.fv, L.idu, L.idv, A.omega, xu[l], xv[l],
                             p % W, p / W);
-        bar();
+        sync();
         for (int s = 1; s < A.nu1; s++) {
-            for (int p = tid; p < npt; p += nthr)
+            for (int p = t0; act && p < npt; p += nt)
                 st_smooth_pt<T>(L.G, L.su, L.sv, xu[l], xv[l], L.fu, L.fv, L.idu, L.idv, A.omega, yu[l], yv[l],
                                 p % W, p / W);
-            bar();
+            sync();
             swap_xy(l);
         }
-        for (int p = tid; p < npt; p += nthr)
+        for (int p = t0; act && p < npt; p += nt)
             st_residual_pt<T>(L.G, L.su, L.sv, xu[l], xv[l], L.fu, L.fv, L.ru, L.rv, p % W, p / W);
-        bar();
+        sync();
         const mg_bottom_level<T> &C = A.L[l + 1];
         const int Wc = C.G.Nx + 1, nptc = Wc * (C.G.Nz + 1);
-        for (int p = tid; p < nptc; p += nthr)
+        for (int p = t0; act && p < nptc; p += nt)
             mg_restrict_pt<T>(L.G, C.G, L.ru, L.rv, C.fu, C.fv, p % Wc, p / Wc);
-        bar();
-    }
-    {   // dense coarsest: x = A^-1 f (zero outside the unknowns); every CTA
-        // gathers f into its own shared memory
+        sync();
+    };
+    auto up = [&](int l, bool act, int t0, int nt, auto &&sync) {
+        const mg_bottom_level<T> &L = A.L[l];
+        const mg_bottom_level<T> &C = A.L[l + 1];
+        const int W = L.G.Nx + 1, npt = W * (L.G.Nz + 1);
+        for (int p = t0; act && p < npt; p += nt)
+            mg_prolong_pt<T>(L.G, C.G, xu[l + 1], xv[l + 1], xu[l], xv[l], p % W, p / W);
+        sync();
+        for (int s = 0; s < A.nu2; s++) {
+            for (int p = t0; act && p < npt; p += nt)
+                st_smooth_pt<T>(L.G, L.su, L.sv, xu[l], xv[l], L.fu, L.fv, L.idu, L.idv, A.omega, yu[l], yv[l],
+                                p % W, p / W);
+            sync();
+            swap_xy(l);
+        }
+    };
+    auto dense = [&](bool act, int t0, int nt, auto &&sync) {   // x = A^-1 f on the coarsest level
         const int lc = A.nlev - 1, n = A.ndense;
         const mg_bottom_level<T> &C = A.L[lc];
         const int nu = C.G.Nx * (C.G.Nz + 1), nv = (C.G.Nx + 1) * C.G.Nz;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        for (int i = threadIdx.x; act && i < n; i += blockDim.x) {   // every active CTA gathers f for itself
             const int m = A.dmap[i];
             fs[i] = m < nu ? C.fu[m] : C.fv[m - nu];
         }
-        for (int i = tid; i < nu; i += nthr) xu[lc][i] = T(0);
-        for (int i = tid; i < nv; i += nthr) xv[lc][i] = T(0);
-        bar();
-        for (int r = tid; r < n; r += nthr) {
+        for (int i = t0; act && i < nu; i += nt) xu[lc][i] = T(0);
+        for (int i = t0; act && i < nv; i += nt) xv[lc][i] = T(0);
+        sync();
+        for (int r = t0; act && r < n; r += nt) {
             T s = 0;
             for (int j = 0; j < n; j++) s += A.AinvT[(size_t)j * n + r] * fs[j];
             const int m = A.dmap[r];
             if (m < nu) xu[lc][m] = s; else xv[lc][m - nu] = s;
         }
-        bar();
+        sync();
+    };
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
+    // levels lsplit .. nlev-1 are small enough for CTA 0 alone: their phases end
+    // in CTA barriers instead of cluster barriers (the other CTAs wait once)
+    const int ls = A.lsplit;
+    for (int l = 0; l < ls && l < A.nlev - 1; l++) down(l, true, tid, nthr, cbar);
+    if (ls < A.nlev) {
+        const bool act = blockIdx.x == 0;
+        for (int l = ls; l < A.nlev - 1; l++) down(l, act, threadIdx.x, blockDim.x, tbar);
+        dense(act, threadIdx.x, blockDim.x, tbar);
+        for (int l = A.nlev - 2; l >= ls; l--) up(l, act, threadIdx.x, blockDim.x, tbar);
+        cbar();
+    } else {
+        dense(true, tid, nthr, cbar);
     }
-    for (int l = A.nlev - 2; l >= 0; l--) {   // ascent
-        const mg_bottom_level<T> &L = A.L[l];
-        const mg_bottom_level<T> &C = A.L[l + 1];
-        const int W = L.G.Nx + 1, npt = W * (L.G.Nz + 1);
-        for (int p = tid; p < npt; p += nthr)
-            mg_prolong_pt<T>(L.G, C.G, xu[l + 1], xv[l + 1], xu[l], xv[l], p % W, p / W);
-        bar();
-        for (int s = 0; s < A.nu2; s++) {
-            for (int p = tid; p < npt; p += nthr)
-                st_smooth_pt<T>(L.G, L.su, L.sv, xu[l], xv[l], L.fu, L.fv, L.idu, L.idv, A.omega, yu[l], yv[l],
-                                p % W, p / W);
-            bar();
-            swap_xy(l);
-        }
-    }
+    for (int l = (ls < A.nlev - 1 ? ls : A.nlev - 1) - 1; l >= 0; l--) up(l, true, tid, nthr, cbar);
     if (xu[0] != A.L[0].xu) {   // odd number of swaps on the first level: copy back
         const mg_bottom_level<T> &L = A.L[0];
         const int nu = L.G.Nx * (L.G.Nz + 1), nv = (L.G.Nx + 1) * L.G.Nz;
@@ -1555,6 +1574,9 @@ static mdz_status vcycle(mdz_ctx *ctx, mg_hier<T> &H, int l, int nu1, int nu2, T
         (long long)(L.Nx + 1) * (L.Nz + 1) <= mg_bottom_points(cs)) {   // this level and all below in one launch
         mg_bottom_args<T> A;
         A.nlev = H.nlev - l; A.nu1 = nu1; A.nu2 = nu2; A.ndense = Cd.ndense; A.omega = omega;
+        A.lsplit = A.nlev;
+        for (int q = 0; q < A.nlev; q++)   // levels of at most one point per thread of one CTA
+            if ((long long)(H.L[l + q].Nx + 1) * (H.L[l + q].Nz + 1) <= MG_BOTTOM_THREADS) { A.lsplit = q; break; }
         A.dmap = Cd.dmap; A.AinvT = Cd.AinvT;
         for (int q = 0; q < A.nlev; q++) {
             const mg_level<T> &B = H.L[l + q];
