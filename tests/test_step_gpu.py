@@ -98,3 +98,20 @@ def test_adaptive_linear_tolerance_same_step(precision):
     assert _rel(out_a["p"] - out_a["p"].mean(), out_f["p"] - out_f["p"].mean()) < 1e-8
     for k in ("sxxd", "szzd", "sxz", "x", "z"):
         assert _rel(mk_a[k], mk_f[k]) < 1e-8, k
+
+
+def test_multigrid_reuse_same_step():
+    """Keeping the multigrid hierarchy for nearly converged iterations
+    (mg_reuse_below) reaches the same converged step."""
+    g, m, u, v, p, mat = vep_case()
+    prm = mdz.RheoParams.make(dt=0.5, iselastic=1, step=1)
+    base = dict(newton=1, nit_max=20, rel_tol=1e-11, lin_rtol=1e-9, line_search=0, precision=32, adaptive_lin_tol=1)
+    fresh = mdz.Model.make(prm, **base)
+    reuse = mdz.Model.make(prm, mg_reuse_below=1e-2, **base)
+    out_f, mk_f, rep_f = run_gpu(g, dict((k, np.array(v_)) for k, v_ in m.items()), u, v, p, mat, fresh)
+    out_r, mk_r, rep_r = run_gpu(g, dict((k, np.array(v_)) for k, v_ in m.items()), u, v, p, mat, reuse)
+    assert rep_f.converged == 1 and rep_r.converged == 1, (rep_f.as_dict(), rep_r.as_dict())
+    assert _rel(out_r["u"], out_f["u"]) < 1e-8 and _rel(out_r["v"], out_f["v"]) < 1e-8
+    assert _rel(out_r["p"] - out_r["p"].mean(), out_f["p"] - out_f["p"].mean()) < 1e-8
+    for k in ("sxxd", "szzd", "sxz", "x", "z"):
+        assert _rel(mk_r[k], mk_f[k]) < 1e-8, k
