@@ -490,11 +490,11 @@ __device__ __forceinline__ void visc_node_phase(bool fp32, int p, double G, doub
 // for ani = 0 (iDa11 = iDa22 = 1/2, iDa33 = 1, off-diagonals 0).
 __device__ __forceinline__ void eff_rates(double exx, double ezz, double exz, double sxx0, double szz0, double sxz0,
                                           double etae, double *E) {
-    const double i11 = 0.5, i22 = 0.5, i33 = 1.0, z = 0.0;
-    double Exx = exx + (i11 * sxx0 + z * szz0 + z * sxz0) / etae;
-    double Ezz = ezz + (z * sxx0 + i22 * szz0 + z * sxz0) / etae;
-    double Exz = exz + (z * sxx0 + z * szz0 + i33 * sxz0) / 2.0 / etae;
-    double gxz = 2.0 * exz + (z * sxx0 + z * szz0 + i33 * sxz0) / etae;
+    const double i11 = 0.5, i22 = 0.5, i33 = 1.0, z = 0.0, ie = 1.0 / etae;   // one division, not four
+    double Exx = exx + (i11 * sxx0 + z * szz0 + z * sxz0) * ie;
+    double Ezz = ezz + (z * sxx0 + i22 * szz0 + z * sxz0) * ie;
+    double Exz = exz + (z * sxx0 + z * szz0 + i33 * sxz0) * 0.5 * ie;
+    double gxz = 2.0 * exz + (z * sxx0 + z * szz0 + i33 * sxz0) * ie;
     E[0] = Exx; E[1] = Ezz; E[2] = Exz;
     E[3] = Exx * 1.0 + Ezz * z + gxz * z;
     E[4] = Ezz * 1.0 + Exx * z - gxz * z;
@@ -746,10 +746,10 @@ __global__ void k_rhs(mdz_dgrid g, mdz_rheo_params prm, double gx, double gz, md
             double inN = (g.BCg[ixyN] != 30 && g.BCu[c + Nx] != 13) ? 1.0 : 0.0;
             r = -gx * (0.5 * (f.rho_s[ixyS] + f.rho_s[ixyN]));
             if (prm.iselastic == 1 && k > 0 && k < Nx - 1) {
-                if (inE) r -= 1.0 / dx * (f.eta_n[iPrE] / (f.mu_n[iPrE] * dt) * f.sxxd0[iPrE]);
-                if (inW) r -= 1.0 / dx * (-f.eta_n[iPrW] / (f.mu_n[iPrW] * dt) * f.sxxd0[iPrW]);
-                if (inN) r -= 1.0 / dz * (f.eta_s[ixyN] / (f.mu_s[ixyN] * dt) * f.sxz0[ixyN]);
-                if (inS) r -= 1.0 / dz * (-f.eta_s[ixyS] / (f.mu_s[ixyS] * dt) * f.sxz0[ixyS]);
+                if (inE) r -= g.idx * (f.eta_n[iPrE] / (f.mu_n[iPrE] * dt) * f.sxxd0[iPrE]);
+                if (inW) r -= g.idx * (-f.eta_n[iPrW] / (f.mu_n[iPrW] * dt) * f.sxxd0[iPrW]);
+                if (inN) r -= g.idz * (f.eta_s[ixyN] / (f.mu_s[ixyN] * dt) * f.sxz0[ixyN]);
+                if (inS) r -= g.idz * (-f.eta_s[ixyS] / (f.mu_s[ixyS] * dt) * f.sxz0[ixyS]);
             }
         }
         f.roger_x[c] = -r;
@@ -765,10 +765,10 @@ __global__ void k_rhs(mdz_dgrid g, mdz_rheo_params prm, double gx, double gz, md
             double inE = (g.BCg[ixyE] != 30 && g.BCv[c + 1] != 13) ? 1.0 : 0.0;
             r = -gz * (0.5 * ((l > 0 ? f.rho_n[iPrS] : 0.0) + (l < Nz - 1 ? f.rho_n[iPrN] : 0.0)));
             if (prm.iselastic == 1 && l > 0 && l < Nz - 1) {
-                if (inN) r -= 1.0 / dz * (f.eta_n[iPrN] / (f.mu_n[iPrN] * dt) * (f.szzd0[iPrN]));
-                if (inS) r -= 1.0 / dz * (-f.eta_n[iPrS] / (f.mu_n[iPrS] * dt) * (f.szzd0[iPrS]));
-                if (inE) r -= 1.0 / dx * (f.eta_s[ixyE] / (f.mu_s[ixyE] * dt) * f.sxz0[ixyE]);
-                if (inW) r -= 1.0 / dx * (-f.eta_s[ixyW] / (f.mu_s[ixyW] * dt) * f.sxz0[ixyW]);
+                if (inN) r -= g.idz * (f.eta_n[iPrN] / (f.mu_n[iPrN] * dt) * (f.szzd0[iPrN]));
+                if (inS) r -= g.idz * (-f.eta_n[iPrS] / (f.mu_n[iPrS] * dt) * (f.szzd0[iPrS]));
+                if (inE) r -= g.idx * (f.eta_s[ixyE] / (f.mu_s[ixyE] * dt) * f.sxz0[ixyE]);
+                if (inW) r -= g.idx * (-f.eta_s[ixyW] / (f.mu_s[ixyW] * dt) * f.sxz0[ixyW]);
             }
         }
         f.roger_z[c] = -r;
