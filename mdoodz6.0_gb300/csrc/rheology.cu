@@ -28,10 +28,11 @@ __global__ void k_strain_centroids(mdz_dgrid g, const double *__restrict__ u, co
     int k = c0 % ncx, l = c0 / ncx, c1 = k + l * Nx, c2 = k + l * (Nx + 1);
     signed char t = g.BCp[c0];
     if (t != 30 && t != 31) {
-        double d = (u[c1 + 1 + Nx] - u[c1 + Nx]) / g.dx + (v[c2 + Nx + 1 + 1] - v[c2 + 1]) / g.dz;
+        double dudx = (u[c1 + 1 + Nx] - u[c1 + Nx]) * g.idx, dvdz = (v[c2 + 1 + (Nx + 1)] - v[c2 + 1]) * g.idz;
+        double d = dudx + dvdz;
         div[c0] = d;
-        exx[c0] = (u[c1 + 1 + Nx] - u[c1 + Nx]) / g.dx - 1.0 / 3.0 * d;
-        ezz[c0] = (v[c2 + 1 + (Nx + 1)] - v[c2 + 1]) / g.dz - 1.0 / 3.0 * d;
+        exx[c0] = dudx - 1.0 / 3.0 * d;
+        ezz[c0] = dvdz - 1.0 / 3.0 * d;
     } else {
         div[c0] = 0.0; exx[c0] = 0.0; ezz[c0] = 0.0;
     }
@@ -45,8 +46,8 @@ __global__ void k_strain_vertices(mdz_dgrid g, const double *__restrict__ u, con
     int k = c1 % Nx, l = c1 / Nx, c2 = k + l * (Nx + 1);
     double e = 0.0;
     if (g.BCg[c1] != 30) {
-        if (g.BCu[c1] != 30 && g.BCu[c1 + Nx] != 30) e += 0.5 * (u[c1 + Nx] - u[c1]) / g.dz;
-        if (g.BCv[c2] != 30 && g.BCv[c2 + 1] != 30) e += 0.5 * (v[c2 + 1] - v[c2]) / g.dx;
+        if (g.BCu[c1] != 30 && g.BCu[c1 + Nx] != 30) e += 0.5 * (u[c1 + Nx] - u[c1]) * g.idz;
+        if (g.BCv[c2] != 30 && g.BCv[c2 + 1] != 30) e += 0.5 * (v[c2 + 1] - v[c2]) * g.idx;
     }
     exz[c1] = e;
 }
@@ -128,6 +129,40 @@ __device__ __forceinline__ float mpow(float x, float y) { return powf(x, y); }
 template <typename Real>
 __device__ __forceinline__ Real dmin(Real a, Real b) { return a <= b ? a : b; }
 
+// Materials as the local solves read them: the public parameters plus
+// lnK_pwl = ln(pref F A^(-1/n) f^(-r/n)), the part of the logarithm of the
+// dislocation prefactor B_pwl (Viscosity, SOURCE/RheologyDensity.c:153-154)
+// that depends on neither the node nor the iteration.  Taken once per
+// launch on the host; NaN where the product is not positive and finite, and the
+// solve then multiplies the reference's factors out as they stand.
+struct mdz_mat_k : mdz_materials {
+    double lnK_pwl[MDZ_MAX_PHASES];
+};
+
+static mdz_mat_k mat_k(const mdz_materials &m) {
+    mdz_mat_k k;
+    static_cast<mdz_materials &>(k) = m;
+    for (int p = 0; p < MDZ_MAX_PHASES; p++) {
+        double v = NAN;
+        const double n = m.npwl[p], pf = m.pref_pwl[p] * m.Fpwl[p], A = m.Apwl[p], f = m.fpwl[p], r = m.rpwl[p];
+        if (p < m.n_phases && m.pwlv[p] != 0 && n != 0 && pf > 0 && A > 0 && (r == 0 || f > 0)) {
+            v = std::log(pf) - std::log(A) / n;
+            if (r != 0) v -= r / n * std::log(f);
+            if (!std::isfinite(v)) v = NAN;
+        }
+        k.lnK_pwl[p] = v;
+    }
+    return k;
+}
+
+// ln(1 + x) by its Mercator series through x^7, for |x| < 1/32 (truncation
+// below x^8 / 8 < 2^-43): the Halley update of the learned start needs only
+// its root at x = 0 to be exact, and the FP64 logarithm costs several times
+// these seven multiply-adds on this part.
+__device__ __forceinline__ double ln1p_series(double x) {
+    return x * (1.0 + x * (-0.5 + x * (1.0 / 3.0 + x * (-0.25 + x * (0.2 + x * (-1.0 / 6.0 + x * (1.0 / 7.0)))))));
+}
+
 // pow with the exponents the creep laws make trivial (0, 1, 2, -1, -2:
 // grain-size and melt exponents switched off, linear diffusion creep and its
 // tangent, squares) taken exactly; each costs a full FP64 log/exp pair
@@ -150,7 +185,7 @@ __device__ __forceinline__ Real fexp(Real x) { return x == Real(0) ? Real(1) : m
 template <typename Real>
 __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Real X0, Real Exx,
                            Real Ezz, Real Exz, Real Gxx, Real Gzz, Real Gxz, Real Txx0, Real Tzz0,
-                           Real Txz0, const mdz_materials &m, const mdz_rheo_params &prm, Real dil, Real fric,
+                           Real Txz0, const mdz_mat_k &m, const mdz_rheo_params &prm, Real dil, Real fric,
                            Real C, Real P0, Real beta, visc_res &o, const float *guess) {
     const Real R = Real(m.R), dt = Real(prm.dt), tol = sizeof(Real) == 8 ? Real(1.0e-11) : Real(1.0e-4);
     const int nitmax = 20;
@@ -181,13 +216,33 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
     if (elastic == 0) { G = Real(1e1); K = Real(1e1); dil = Real(0.0); }
     if (T < Real(ZEROC) / Real(prm.scale_T)) T = Real(ZEROC) / Real(prm.scale_T);
     const Real iRT = Real(1.0) / (R * T);
+    // FP64 dislocation creep in log form: ln B_pwl from the per-phase constant,
+    // then C_pwl = (2 f_ani B_pwl)^-n and eta_pwl = B_pwl Eii^(1/n - 1) as two
+    // exponentials after one logarithm (the product form takes three pow and an
+    // exp), and in the learned polish Eii_pwl = exp(ln C_pwl + n ln Tii) with
+    // ln Tii = lnTE + ln eta_ve known.  FP32 keeps the product form: rounding of
+    // the logarithms' sums there is at the size of its convergence test.
+    const bool logform = sizeof(Real) == 8 && dislocation && isfinite(m.lnK_pwl[p]);
+    Real lnC_pwl = Real(0.0), lnTE = Real(0.0), ln_eta_pwl = Real(0.0);
     if (dislocation) {
         const Real in = Real(1.0) / n_pwl;
-        Real B_pwl = Real(m.pref_pwl[p]) * Real(m.Fpwl[p]) * fpow(Real(m.Apwl[p]), -in) * mexp((Real(m.Qpwl[p]) + P * Va_pwl) * iRT * in) *
-                       fpow(d, Real(m.mpwl[p]) * in) * fpow(Real(m.fpwl[p]), -Real(m.rpwl[p]) * in) * fexp(-Real(m.apwl[p]) * phi * in);
-        C_pwl = fpow(Real(2.0) * f_ani * B_pwl, -n_pwl);
+        if (logform) {
+            Real lnB = Real(m.lnK_pwl[p]) + (Real(m.Qpwl[p]) + P * Va_pwl) * iRT * in;
+            if (Real(m.mpwl[p]) != Real(0.0)) lnB += Real(m.mpwl[p]) * in * mlog(d);
+            if (Real(m.apwl[p]) != Real(0.0)) lnB -= Real(m.apwl[p]) * phi * in;
+            const Real LE = mlog(Eii), LF = f_ani == Real(1.0) ? Real(0.69314718055994530942) : mlog(Real(2.0) * f_ani);   // ln 2
+            lnTE = LF + LE;   // ln(2 f_ani Eii) = ln Tii - ln eta_ve
+            lnC_pwl = -n_pwl * (LF + lnB);
+            C_pwl = mexp(lnC_pwl);
+            ln_eta_pwl = lnB + (in - Real(1.0)) * LE;
+            eta_pwl = mexp(ln_eta_pwl);
+        } else {
+            Real B_pwl = Real(m.pref_pwl[p]) * Real(m.Fpwl[p]) * fpow(Real(m.Apwl[p]), -in) * mexp((Real(m.Qpwl[p]) + P * Va_pwl) * iRT * in) *
+                           fpow(d, Real(m.mpwl[p]) * in) * fpow(Real(m.fpwl[p]), -Real(m.rpwl[p]) * in) * fexp(-Real(m.apwl[p]) * phi * in);
+            C_pwl = fpow(Real(2.0) * f_ani * B_pwl, -n_pwl);
+            eta_pwl = B_pwl * fpow(Eii, in - Real(1.0));
+        }
         dCpwldP = -C_pwl * Va_pwl * iRT;
-        eta_pwl = B_pwl * fpow(Eii, in - Real(1.0));
     }
     if (diffusion) {
         const Real in = Real(1.0) / n_lin;
@@ -227,13 +282,13 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
         // means the reference's own test below holds.  The network predicts
         // ln(eta_ve / eta_up), eta_up being the reference's start (the
         // smallest viscosity of the active mechanisms).
-        Real s = mlog(eta_up) + (Real)guess[0];
+        Real s = (logform && eta_up == eta_pwl ? ln_eta_pwl : mlog(eta_up)) + (Real)guess[0];
         for (it = 0; it <= MDZ_POLISH_STEPS; it++) {
             eta_ve = mexp(s);
             Tii = Real(2.0) * f_ani * eta_ve * Eii;
             const Real Eel = elastic ? Tii * i2eta_el : Real(0.0);
             if (constant) Eii_cst = Tii * ifcst;
-            if (dislocation) Eii_pwl = C_pwl * fpow(Tii, n_pwl);
+            if (dislocation) Eii_pwl = logform ? mexp(lnC_pwl + n_pwl * (lnTE + s)) : C_pwl * fpow(Tii, n_pwl);
             if (diffusion) Eii_lin = C_lin * fpow(Tii, n_lin) * dm_lin;
             const Real S0 = Eel + Eii_pwl + Eii_lin + Eii_cst;
             res = mfabs((Eii - S0) * iEii);
@@ -243,7 +298,9 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
             const Real S1 = Eel + n_pwl * Eii_pwl + n_lin * Eii_lin + Eii_cst;
             const Real S2 = Eel + n_pwl * n_pwl * Eii_pwl + n_lin * n_lin * Eii_lin + Eii_cst;
             const Real iS0 = Real(1.0) / S0;
-            const Real g = mlog(S0 * iEii), g1 = S1 * iS0, g2 = S2 * iS0 - g1 * g1;
+            const Real q = S0 * iEii;
+            const Real g = (sizeof(Real) == 8 && mfabs(q - Real(1.0)) < Real(0.03125)) ? Real(ln1p_series(double(q - Real(1.0)))) : mlog(q);
+            const Real g1 = S1 * iS0, g2 = S2 * iS0 - g1 * g1;
             const Real den = Real(2.0) * g1 * g1 - g * g2;
             s -= den > Real(0.0) ? Real(2.0) * g * g1 / den : g / g1;
         }
@@ -453,7 +510,7 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
 // evaluations of k_viscosity_* use this one).
 __device__ __forceinline__ void visc_local(int p, double G, double T, double P, double d, double phi, double X0,
                                            double Exx, double Ezz, double Exz, double Gxx, double Gzz, double Gxz,
-                                           double Txx0, double Tzz0, double Txz0, const mdz_materials &m,
+                                           double Txx0, double Tzz0, double Txz0, const mdz_mat_k &m,
                                            const mdz_rheo_params &prm, double dil, double fric, double C, double P0,
                                            double beta, visc_res &o, const float *guess = nullptr) {
     visc_local_t<double>(p, G, T, P, d, phi, X0, Exx, Ezz, Exz, Gxx, Gzz, Gxz, Txx0, Tzz0, Txz0, m, prm, dil, fric,
@@ -467,7 +524,7 @@ __device__ __forceinline__ void visc_local(int p, double G, double T, double P, 
 // otherwise the FP64 solve, from the learned start when one is given.
 __device__ __forceinline__ void visc_node_phase(bool fp32, int p, double G, double T, double P, double d, double phi,
                                                 double X0, const double *E, double Txx0, double Tzz0, double Txz0,
-                                                const mdz_materials &m, const mdz_rheo_params &prm, double dil,
+                                                const mdz_mat_k &m, const mdz_rheo_params &prm, double dil,
                                                 double fric, double C, double P0, double beta, visc_res &o,
                                                 const float *guess) {
     if (fp32) {
@@ -524,7 +581,7 @@ __device__ __forceinline__ void count_local(int *counters, int fails, int fallba
 }
 
 // One thread per centroid: loop over phases with a fraction above 1e-13.
-__global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_materials m, mdz_rheo_params prm,
+__global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_mat_k m, mdz_rheo_params prm,
                                                              mdz_fields f, int *__restrict__ counters,
                                                              const float2 *__restrict__ guess, int fp32) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -612,7 +669,7 @@ __global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_ma
     count_local(counters, fails, fallbacks, learned, iters);
 }
 
-__global__ void __launch_bounds__(128) k_viscosity_vertices(mdz_dgrid g, mdz_materials m, mdz_rheo_params prm,
+__global__ void __launch_bounds__(128) k_viscosity_vertices(mdz_dgrid g, mdz_mat_k m, mdz_rheo_params prm,
                                                             mdz_fields f, int *__restrict__ counters,
                                                             const float2 *__restrict__ guess, int fp32) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -915,7 +972,7 @@ __device__ __forceinline__ double mlp_u01(unsigned long long seed, long long i, 
     return (double)(z >> 11) * (1.0 / 9007199254740992.0);
 }
 
-__global__ void __launch_bounds__(128) k_mlp_samples(long long n, unsigned long long seed, mdz_materials m,
+__global__ void __launch_bounds__(128) k_mlp_samples(long long n, unsigned long long seed, mdz_mat_k m,
                                                      mdz_rheo_params prm, double lo0, double hi0, double lo1,
                                                      double hi1, double lo2, double hi2, double lo3, double hi3,
                                                      mdz_mlp_norm nm, uint4 *__restrict__ X, float2 *__restrict__ Y) {
@@ -945,7 +1002,7 @@ __global__ void __launch_bounds__(128) k_mlp_samples(long long n, unsigned long 
 mdz_status mdz_dev_mlp_samples(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm, long long n,
                                unsigned long long seed, const double lo[4], const double hi[4],
                                const mdz_mlp_norm &norm, uint4 *X, float2 *Y, cudaStream_t st) {
-    k_mlp_samples<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, seed, *m, *prm, lo[0], hi[0], lo[1], hi[1], lo[2],
+    k_mlp_samples<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, seed, mat_k(*m), *prm, lo[0], hi[0], lo[1], hi[1], lo[2],
                                                                 hi[2], lo[3], hi[3], norm, X, Y);
     MDZ_LAUNCHED(ctx);
     return MDZ_OK;
@@ -972,9 +1029,10 @@ mdz_status mdz_dev_viscosity(mdz_ctx *ctx, const mdz_materials *m, const mdz_rhe
     }
     cudaEvent_t ev;
     mdz_prof_begin(ctx, MDZ_PROF_VISCOSITY, st, &ev);
-    k_viscosity_centroids<<<mdz_blocks(nc, 128), 128, 0, st>>>(g, *m, *prm, f, d_counters, guess_n, fp32 ? 1 : 0);
+    const mdz_mat_k mk = mat_k(*m);
+    k_viscosity_centroids<<<mdz_blocks(nc, 128), 128, 0, st>>>(g, mk, *prm, f, d_counters, guess_n, fp32 ? 1 : 0);
     MDZ_LAUNCHED(ctx);
-    k_viscosity_vertices<<<mdz_blocks(nv, 128), 128, 0, st>>>(g, *m, *prm, f, d_counters, guess_s, fp32 ? 1 : 0);
+    k_viscosity_vertices<<<mdz_blocks(nv, 128), 128, 0, st>>>(g, mk, *prm, f, d_counters, guess_s, fp32 ? 1 : 0);
     MDZ_LAUNCHED(ctx);
     // algorithmic bytes: per centroid 17 + n_phases FP64 inputs and 35 outputs,
     // per vertex 17 + n_phases inputs and 12 outputs, plus the tags
