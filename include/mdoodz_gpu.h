@@ -403,7 +403,11 @@ typedef struct mdz_model {
     int line_search;        /* 1: LineSearchDecoupled (6 trial steps)                      */
     double line_search_min;
     int precision;          /* 64: plain FP64; 32: FP32 stencils + V-cycles in FP64 refinement */
-    int learned_guess;      /* 1: MLP initial guess for the local rheology (mdz_mlp_*)       */
+    int learned_guess;      /* local rheology starts (MLP weights loaded with mdz_mlp_*):
+                               1: the MLP's guess in the first FP64 evaluation of the step,
+                                  then each evaluation polishes the solutions the previous
+                                  one converged to; 2: the MLP's guess in every evaluation;
+                                  0: the reference's start                                  */
     int itp_stencil;        /* 1 or 9                                                        */
     int softening;          /* 0: smooth erfc law (reference); 1: linear law                 */
     int advect;             /* 1: update marker stress/strain and advect (RK4)               */

@@ -250,10 +250,14 @@ mdz_status mdz_dev_v2c(mdz_ctx *ctx, double *cen, const double *ver, cudaStream_
 mdz_status mdz_check_materials(mdz_ctx *ctx, const mdz_materials *m);
 // Local rheology on centroids and vertices.  d_counters: [0] local solves not
 // converged, [1] learned starts that fell back to the plain solve, [2] learned
-// starts.  learned: every local solve starts from the MLP's guess (weights
-// loaded in the context) and the plain solve reruns where the polish fails.
+// starts.  learned: every local solve starts from a guess and the plain solve
+// reruns where the polish fails; the guess is the MLP's (weights loaded in the
+// context) unless warm = 2, which starts from the solutions the previous
+// evaluation recorded (same phase fractions: within one time step).  warm >= 1
+// records each converged solve in the guess buffer for the next evaluation.
 mdz_status mdz_dev_viscosity(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm, const mdz_fields &f,
-                             int *d_counters, cudaStream_t st, bool learned = false, bool fp32 = false);
+                             int *d_counters, cudaStream_t st, bool learned = false, bool fp32 = false,
+                             int warm = 0);
 mdz_status mdz_dev_operators(mdz_ctx *ctx, const mdz_rheo_params *prm, const mdz_fields &f, int jacobian,
                              cudaStream_t st);
 mdz_status mdz_dev_rhs(mdz_ctx *ctx, const mdz_rheo_params *prm, double gx, double gz, const mdz_fields &f,

@@ -625,8 +625,8 @@ extern "C" mdz_status mdz_mlp_benchmark(mdz_ctx *ctx, int batch, int reps, doubl
 // NonNewtonianViscosityGrid with the MLP start: guesses for every (phase,
 // node), then the local solves polish them (rheology.cu).
 mdz_status mdz_dev_viscosity_learned(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm,
-                                     const mdz_fields &f, int *d_counters, cudaStream_t st) {
+                                     const mdz_fields &f, int *d_counters, cudaStream_t st, int warm) {
     if (!mdz_mlp_ready(ctx)) return mdz_fail(ctx, MDZ_ERR_STATE, "learned guess: no MLP weights loaded");
     if (m->n_phases > 4) return mdz_fail(ctx, MDZ_ERR_UNSUPPORTED, "learned guess: at most 4 phases");
-    return mdz_dev_viscosity(ctx, m, prm, f, d_counters, st, true);
+    return mdz_dev_viscosity(ctx, m, prm, f, d_counters, st, true, false, warm);
 }

@@ -69,7 +69,7 @@ void mdz_mlp_free(mdz_ctx *ctx);
 // guess buffer for n_phases x (nc + nv) nodes (allocated on first use)
 float2 *mdz_mlp_guess_buffer(mdz_ctx *ctx, size_t n);
 mdz_status mdz_dev_viscosity_learned(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm,
-                                     const mdz_fields &f, int *d_counters, cudaStream_t st);
+                                     const mdz_fields &f, int *d_counters, cudaStream_t st, int warm = 0);
 
 // Labelled tuples by the plain local solve (rheology.cu).
 mdz_status mdz_dev_mlp_samples(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm, long long n,

@@ -104,6 +104,7 @@ struct visc_res {
     double eta_up;          // the reference's start of the visco-elastic iteration
     int ve_fail, vp_fail, ve_its, vp_its;
     int learned, fallback;  // started from a learned guess; polish failed and the plain solve reran
+    float lab_x, lab_y;     // the converged solve as a start: ln(eta_ve / eta_up), gdot / (2 Eii)
 };
 
 // Polish budget of a learned start: Newton-type updates allowed before the
@@ -503,6 +504,10 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
         o.detadexx = Real(0.0); o.detadezz = Real(0.0); o.detadexz = Real(0.0); o.detadp = Real(0.0);
     }
     o.eta = eta;
+    // the start the next evaluation of this (node, phase) can polish from, in
+    // the learned guess's encoding; FP32 logarithms suffice for a start
+    o.lab_x = logf((float)eta_ve) - logf((float)o.eta_up);
+    o.lab_y = (float)(gdot * Real(0.5) * iEii);
 }
 
 
@@ -583,7 +588,7 @@ __device__ __forceinline__ void count_local(int *counters, int fails, int fallba
 // One thread per centroid: loop over phases with a fraction above 1e-13.
 __global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_mat_k m, mdz_rheo_params prm,
                                                              mdz_fields f, int *__restrict__ counters,
-                                                             const float2 *__restrict__ guess, int fp32) {
+                                                             const float2 *guess, float2 *labels, int fp32) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     int nc = g.ncx * g.ncz;
     if (c >= nc) return;
@@ -613,6 +618,8 @@ __global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_ma
             }
             visc_node_phase(fp32 != 0, p, mu, T, P, d0, phi0, X0, E, sxx0, szz0, sxz0, m, prm, dil, fric, Coh, P0, bet, o,
                             guess ? gs : nullptr);
+            // labels may be the guess buffer itself: this thread read its entry above
+            if (labels) labels[(size_t)p * nc + c] = make_float2(o.lab_x, o.lab_y);
             fails += o.ve_fail + o.vp_fail;
             fallbacks += o.fallback;
             iters += o.ve_its + o.vp_its;
@@ -671,7 +678,7 @@ __global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_ma
 
 __global__ void __launch_bounds__(128) k_viscosity_vertices(mdz_dgrid g, mdz_mat_k m, mdz_rheo_params prm,
                                                             mdz_fields f, int *__restrict__ counters,
-                                                            const float2 *__restrict__ guess, int fp32) {
+                                                            const float2 *guess, float2 *labels, int fp32) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
     int nv = g.Nx * g.Nz;
     if (c >= nv) return;
@@ -698,6 +705,8 @@ __global__ void __launch_bounds__(128) k_viscosity_vertices(mdz_dgrid g, mdz_mat
             }
             visc_node_phase(fp32 != 0, p, mu, T, P, d0, phi0, X0, E, sxx0, szz0, sxz0, m, prm, dil, fric, Coh, P0, bet, o,
                             guess ? gs : nullptr);
+            // labels may be the guess buffer itself: this thread read its entry above
+            if (labels) labels[(size_t)p * nv + c] = make_float2(o.lab_x, o.lab_y);
             fails += o.ve_fail + o.vp_fail;
             fallbacks += o.fallback;
             iters += o.ve_its + o.vp_its;
@@ -1009,7 +1018,7 @@ mdz_status mdz_dev_mlp_samples(mdz_ctx *ctx, const mdz_materials *m, const mdz_r
 }
 
 mdz_status mdz_dev_viscosity(mdz_ctx *ctx, const mdz_materials *m, const mdz_rheo_params *prm, const mdz_fields &f,
-                             int *d_counters, cudaStream_t st, bool learned, bool fp32) {
+                             int *d_counters, cudaStream_t st, bool learned, bool fp32, int warm) {
     const mdz_dgrid &g = ctx->g;
     int nc = g.ncx * g.ncz, nv = g.Nx * g.Nz;
     // vertex copies of centroid fields (NonNewtonianViscosityGrid :979-983)
@@ -1020,19 +1029,22 @@ mdz_status mdz_dev_viscosity(mdz_ctx *ctx, const mdz_materials *m, const mdz_rhe
     if ((s = mdz_dev_c2v(ctx, f.d0_n, f.d0_s, st)) != MDZ_OK) return s;
     if ((s = mdz_dev_c2v(ctx, f.phi0_n, f.phi0_s, st)) != MDZ_OK) return s;
     const float2 *guess_n = nullptr, *guess_s = nullptr;
+    float2 *lab_n = nullptr, *lab_s = nullptr;
     if (learned && !fp32) {
         float2 *buf = mdz_mlp_guess_buffer(ctx, (size_t)m->n_phases * (nc + nv));
         if (!buf) return mdz_fail(ctx, MDZ_ERR_CUDA, "learned guess: buffer allocation failed");
-        if ((s = mdz_dev_mlp_guess(ctx, m, prm, f, buf, buf + (size_t)m->n_phases * nc, st)) != MDZ_OK) return s;
+        if (warm != 2)
+            if ((s = mdz_dev_mlp_guess(ctx, m, prm, f, buf, buf + (size_t)m->n_phases * nc, st)) != MDZ_OK) return s;
         guess_n = buf;
         guess_s = buf + (size_t)m->n_phases * nc;
+        if (warm >= 1) { lab_n = buf; lab_s = buf + (size_t)m->n_phases * nc; }
     }
     cudaEvent_t ev;
     mdz_prof_begin(ctx, MDZ_PROF_VISCOSITY, st, &ev);
     const mdz_mat_k mk = mat_k(*m);
-    k_viscosity_centroids<<<mdz_blocks(nc, 128), 128, 0, st>>>(g, mk, *prm, f, d_counters, guess_n, fp32 ? 1 : 0);
+    k_viscosity_centroids<<<mdz_blocks(nc, 128), 128, 0, st>>>(g, mk, *prm, f, d_counters, guess_n, lab_n, fp32 ? 1 : 0);
     MDZ_LAUNCHED(ctx);
-    k_viscosity_vertices<<<mdz_blocks(nv, 128), 128, 0, st>>>(g, mk, *prm, f, d_counters, guess_s, fp32 ? 1 : 0);
+    k_viscosity_vertices<<<mdz_blocks(nv, 128), 128, 0, st>>>(g, mk, *prm, f, d_counters, guess_s, lab_s, fp32 ? 1 : 0);
     MDZ_LAUNCHED(ctx);
     // algorithmic bytes: per centroid 17 + n_phases FP64 inputs and 35 outputs,
     // per vertex 17 + n_phases inputs and 12 outputs, plus the tags

@@ -252,21 +252,25 @@ struct step_timer {
 };
 
 // Local rheology + RHS + Picard operators of the current state (UpdateNonLinearity).
+// labels: whether an FP64 evaluation of this time step recorded its converged
+// local solves (learned_guess = 1 then starts the next one from them instead
+// of the MLP: the phase fractions are those of the step's projection).
 static mdz_status update_nonlinearity(mdz_ctx *ctx, const mdz_materials *mat, const mdz_model *M,
-                                      mdz_step_report *rep, cudaStream_t st, bool fp32 = false) {
+                                      bool &labels, cudaStream_t st, bool fp32 = false) {
     mdz_fields &f = ctx->d;
     mdz_status s;
     if ((s = mdz_dev_strain_rates(ctx, f, st)) != MDZ_OK) return s;
     if (fp32) {
         if ((s = mdz_dev_viscosity(ctx, mat, &M->rheo, f, ctx->d_counters, st, false, true)) != MDZ_OK) return s;
     } else if (M->learned_guess) {
-        if ((s = mdz_dev_viscosity_learned(ctx, mat, &M->rheo, f, ctx->d_counters, st)) != MDZ_OK) return s;
+        const int warm = M->learned_guess == 1 ? (labels ? 2 : 1) : 0;
+        if ((s = mdz_dev_viscosity_learned(ctx, mat, &M->rheo, f, ctx->d_counters, st, warm)) != MDZ_OK) return s;
+        labels = warm >= 1;
     } else {
         if ((s = mdz_dev_viscosity(ctx, mat, &M->rheo, f, ctx->d_counters, st)) != MDZ_OK) return s;
     }
     if ((s = mdz_dev_rhs(ctx, &M->rheo, M->gx, M->gz, f, st)) != MDZ_OK) return s;
     if ((s = mdz_dev_operators(ctx, &M->rheo, f, 0, st)) != MDZ_OK) return s;
-    (void)rep;
     return MDZ_OK;
 }
 
@@ -342,6 +346,7 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
                              cudaStream_t st) {
     mdz_status s;
     mdz_step_report R{};
+    bool labels = false;
     const mdz_dgrid &g = ctx->g;
     mdz_fields &f = ctx->d;
     const int nu = g.Nx * (g.Nz + 1), nv = (g.Nx + 1) * g.Nz, np = g.ncx * g.ncz, nvert = g.Nx * g.Nz;
@@ -393,7 +398,7 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
         bool fp32 = nit < M->fp32_rheology_its;
         {
             step_timer T(st, &R.ms_rheology);
-            if ((s = update_nonlinearity(ctx, mat, M, &R, st, fp32)) != MDZ_OK) return s;
+            if ((s = update_nonlinearity(ctx, mat, M, labels, st, fp32)) != MDZ_OK) return s;
         }
         {
             step_timer T(st, &R.ms_residual);
@@ -404,7 +409,7 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
         if (conv && fp32) {   // convergence is only decided on an FP64 evaluation
             {
                 step_timer T(st, &R.ms_rheology);
-                if ((s = update_nonlinearity(ctx, mat, M, &R, st, false)) != MDZ_OK) return s;
+                if ((s = update_nonlinearity(ctx, mat, M, labels, st, false)) != MDZ_OK) return s;
             }
             {
                 step_timer T(st, &R.ms_residual);
@@ -499,7 +504,7 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
                 MDZ_LAUNCHED(ctx);
                 k_mirror_ghosts<<<mdz_blocks(g.Nx > g.Nz ? g.Nx : g.Nz), MDZ_THREADS, 0, st>>>(g, f.u, f.v);
                 MDZ_LAUNCHED(ctx);
-                if ((s = update_nonlinearity(ctx, mat, M, &R, st)) != MDZ_OK) return s;
+                if ((s = update_nonlinearity(ctx, mat, M, labels, st)) != MDZ_OK) return s;
                 double t[3];
                 if ((s = residual_norms(ctx, t, st)) != MDZ_OK) return s;
                 rx[kk] = t[0]; rz[kk] = t[1]; rp[kk] = t[2];
@@ -539,7 +544,7 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
     // ---- 3. final rheology update, p <- p_corr ----------------------------------
     {
         step_timer T(st, &R.ms_rheology);
-        if ((s = update_nonlinearity(ctx, mat, M, &R, st)) != MDZ_OK) return s;
+        if ((s = update_nonlinearity(ctx, mat, M, labels, st)) != MDZ_OK) return s;
         MDZ_CUDA(ctx, cudaMemcpyAsync(f.p, f.p_corr, sizeof(double) * np, cudaMemcpyDeviceToDevice, st));
     }
     // ---- 4. markers ---------------------------------------------------------------

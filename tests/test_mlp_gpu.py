@@ -106,3 +106,44 @@ def test_learned_start_ablation():
     assert learned["fallbacks"] <= 0.05 * learned["learned"], learned
     assert learned["iterations"] < 0.8 * plain["iterations"], (plain, learned)
     ctx.close()
+
+
+def test_warm_start_same_step():
+    """learned_guess = 1 (the MLP's start in the step's first FP64 evaluation,
+    then each evaluation polishes the solutions the previous one converged to)
+    against learned_guess = 2 (the MLP's start in every evaluation) and the
+    reference's start: the same time step within the local tolerance, and the
+    warm start needs fewer local updates than the MLP's start every time."""
+    cfg = mdz_setups.config_lithosphere(Nx=129, Nz=65, precision=32)
+    cfg["model"].rel_tol = 1e-10
+    w, res = None, {}
+    for mode in (0, 2, 1):
+        ctx = mdz_setups.load_context(cfg)
+        if w is None:
+            ctx.mlp_init(1)
+            ctx.mlp_generate(cfg["mat"], cfg["model"].rheo, 1 << 18, 3, LO_C3, HI_C3)
+            ctx.mlp_train(3000, 16384, 2e-3)
+            w = ctx.mlp_get_weights()
+        else:
+            ctx.mlp_set_weights(w)
+        cfg["model"].learned_guess = mode
+        rep = ctx.time_step(cfg["mat"], cfg["model"])
+        f = mdz.GridFields(cfg["grid"], cfg["mat"].n_phases)
+        ctx.download_fields(f)
+        res[mode] = (rep, {k: f[k].copy() for k in ("u", "v", "p", "eta_n", "sxxd", "sxz")},
+                     ctx.get_marker_attr(mdz.M_SXXD))
+        ctx.close()
+    cfg["model"].learned_guess = 0
+    for mode in (2, 1):
+        rep, fields, sxx_m = res[mode]
+        assert rep.converged and rep.local_failures == 0, (mode, rep.as_dict())
+        assert abs(rep.nonlinear_its - res[0][0].nonlinear_its) <= 1, (mode, rep.nonlinear_its, res[0][0].nonlinear_its)
+        for k, v in fields.items():
+            ref = res[0][1][k]
+            if k == "p":
+                v, ref = v - v.mean(), ref - ref.mean()
+            assert _rel(v, ref) < 1e-7, (mode, k, _rel(v, ref))
+        assert _rel(sxx_m, res[0][2]) < 1e-7, mode
+    warm, every = res[1][0], res[2][0]
+    assert warm.local_fallbacks <= every.local_fallbacks, (warm.local_fallbacks, every.local_fallbacks)
+    assert warm.local_iterations < 0.9 * every.local_iterations, (warm.local_iterations, every.local_iterations)
