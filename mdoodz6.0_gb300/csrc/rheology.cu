@@ -109,7 +109,7 @@ struct visc_res {
 
 // Polish budget of a learned start: Newton-type updates allowed before the
 // plain solve takes over.
-#define MDZ_POLISH_STEPS 2
+#define MDZ_POLISH_STEPS 3
 
 // Precision-generic helpers of the local solve (FP64 or FP32 instances).
 __device__ __forceinline__ double msqrt(double x) { return sqrt(x); }
@@ -293,7 +293,11 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
             if (diffusion) Eii_lin = C_lin * fpow(Tii, n_lin) * dm_lin;
             const Real S0 = Eel + Eii_pwl + Eii_lin + Eii_cst;
             res = mfabs((Eii - S0) * iEii);
-            if (res < tol / 100) { ve_done = true; break; }
+            // a start is accepted only after one update: a warm start can
+            // pass the test as it stands, with an error the size of the change
+            // in strain rate since it was recorded (the reference's iteration
+            // always ends one quadratic step past the test)
+            if (it > 0 && res < tol / 100) { ve_done = true; break; }
             if (it == MDZ_POLISH_STEPS) break;
             if (!(S0 > Real(0.0))) break;
             const Real S1 = Eel + n_pwl * Eii_pwl + n_lin * Eii_lin + Eii_cst;
@@ -395,7 +399,7 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
                 Tyield = C * cos_fric + Pc * sin_fric + gdot * eta_vp;
                 F_trial = Tii - eta_ve * gdot - Tyield;
                 res = mfabs(F_trial);
-                if (res < tol || res * iF0 < tol) { vp_done = true; break; }
+                if (it > 0 && (res < tol || res * iF0 < tol)) { vp_done = true; break; }
                 if (it == MDZ_POLISH_STEPS) break;
                 Real dFdgdot = -eta_ve - eta_vp * in_vp - K * dt * sin_fric * sin_dil;
                 gdot -= F_trial / dFdgdot;
