@@ -225,3 +225,177 @@ int orc_rk4(const mdz_grid_desc *g, int n, double *x, double *z, int *phase, dou
     }
     return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Marker reseeding: CountPartCell with RESEED = 1 on one OpenMP thread
+ * (SOURCE/ParticleRoutines.c:3543-4480).  Quarter-cell binning of the active
+ * markers on the grid extended by one cell (:3905-3950); every quarter cell
+ * of the inner region whose centroid is not air and that holds fewer than
+ * (int)(ceil(min_part_cell) / 4) markers gets one marker at its centre
+ * (AddPartCell2, :977-1030), which copies the nearest of the markers in the
+ * 5x5 quarter cells around it (FindClosestPhase2, :841-890; candidates in the
+ * reference's visiting order :4105-4283, a later one wins only when strictly
+ * closer); new markers, numbered quarter-column by quarter-column, first fill
+ * the slots of inactive markers in index order, then append (:4285-4330);
+ * AssignMarkerProperties (:648-762) copies phase, velocity and strains, and
+ * T and the stresses from the neighbour (direct = 1) or from the grid
+ * (Centers2Particle :259-455, Vertices2Particle :461-520; direct = 0).  The
+ * air test reads BCp (the reference reads BCt, whose air tag 30 sits on the
+ * same cells).  attr: the MDZ_M_* marker attributes; the cohesion multiplier
+ * is copied.  Returns the new marker count; -1 when a deficient quarter cell
+ * has no marker within two quarter cells (the reference exits with 333), -2
+ * when the new markers would not fit in cap. */
+static double orc_c2p(const mdz_grid_desc *g, double x, double z, const double *F) {
+    const int Nx = g->Nx - 1, Nz = g->Nz - 1;   /* centroid counts */
+    const double *X = g->xvz, *Z = g->zvx, dx = g->dx, dz = g->dz;
+    const int j = (int)(ceil((x - X[0]) / dx) - 1), i = (int)(ceil((z - Z[0]) / dz) - 1);
+    int iSW, iSE, iNW, iNE, ic, jc;
+    if (j > 0 && j < Nx && i > 0 && i < Nz) {
+        ic = i - 1; jc = j - 1;
+        iSW = jc + ic * Nx; iSE = iSW + 1; iNW = jc + (ic + 1) * Nx; iNE = iNW + 1;
+    } else if (j == 0 && i > 0 && i < Nz) {
+        ic = i - 1; iSW = iSE = ic * Nx; iNW = iNE = (ic + 1) * Nx;
+    } else if (j == Nx && i > 0 && i < Nz) {
+        ic = i - 1; jc = Nx - 1; iSW = iSE = jc + ic * Nx; iNW = iNE = jc + (ic + 1) * Nx;
+    } else if (i == 0 && j > 0 && j < Nx) {
+        jc = j - 1; iSW = iNW = jc; iSE = iNE = jc + 1;
+    } else if (i == Nz && j > 0 && j < Nx) {
+        ic = Nz - 1; jc = j - 1; iSW = iNW = jc + ic * Nx; iSE = iNE = jc + ic * Nx + 1;
+    } else if (i == 0 && j == 0) {
+        iSW = iSE = iNW = iNE = 0;
+    } else if (i == 0 && j == Nx) {
+        iSW = iSE = iNW = iNE = Nx - 1;
+    } else if (i == Nz && j == 0) {
+        iSW = iSE = iNW = iNE = (Nz - 1) * Nx;
+    } else if (i == Nz && j == Nx) {
+        iSW = iSE = iNW = iNE = (Nx - 1) + (Nz - 1) * Nx;
+    } else {
+        return 0.0;   /* outside the extended frame: not reached for markers inside the box */
+    }
+    const double dxm = x - X[j], dzm = z - Z[i];
+    const signed char *t = g->BCp_type;
+    double val = 0.0, sw = 0.0, w;
+    if (t[iSW] != 30 && t[iSW] != 31) { w = (1.0 - dxm / dx) * (1.0 - dzm / dz); val += w * F[iSW]; sw += w; }
+    if (t[iSE] != 30 && t[iSE] != 31) { w = (dxm / dx) * (1.0 - dzm / dz); val += w * F[iSE]; sw += w; }
+    if (t[iNW] != 30 && t[iNW] != 31) { w = (1.0 - dxm / dx) * (dzm / dz); val += w * F[iNW]; sw += w; }
+    if (t[iNE] != 30 && t[iNE] != 31) { w = (dxm / dx) * (dzm / dz); val += w * F[iNE]; sw += w; }
+    if (sw > 1e-13) val /= sw;
+    return val;
+}
+
+static double orc_v2p_vert(const mdz_grid_desc *g, double x, double z, const double *F) {
+    const int Nx = g->Nx;
+    const double dx = g->dx, dz = g->dz;
+    const int j = (int)(ceil(fabs(x - g->xg[0]) / dx) - 1), i = (int)(ceil(fabs(z - g->zg[0]) / dz) - 1);
+    const double dxm = x - g->xg[j], dzm = z - g->zg[i];
+    const int iSW = j + i * Nx, iSE = iSW + 1, iNW = j + (i + 1) * Nx, iNE = iNW + 1;
+    const signed char *t = g->BCg_type;
+    double val = 0.0, sw = 0.0, w;
+    if (t[iSW] != 30 && t[iSW] != 31) { w = (1.0 - dxm / dx) * (1.0 - dzm / dz); val += w * F[iSW]; sw += w; }
+    if (t[iSE] != 30 && t[iSE] != 31) { w = (dxm / dx) * (1.0 - dzm / dz); val += w * F[iSE]; sw += w; }
+    if (t[iNW] != 30 && t[iNW] != 31) { w = (1.0 - dxm / dx) * (dzm / dz); val += w * F[iNW]; sw += w; }
+    if (t[iNE] != 30 && t[iNE] != 31) { w = (dxm / dx) * (dzm / dz); val += w * F[iNE]; sw += w; }
+    if (sw > 1e-13) val /= sw;
+    return val;
+}
+
+int orc_reseed(const mdz_grid_desc *g, int n, int cap, double *x, double *z, int *phase, double *vx, double *vz,
+               double *const *attr, int min_part_cell, int direct, const double *T_n, const double *sxxd_n,
+               const double *szzd_n, const double *sxz_s, int *n_added) {
+    const double dx = g->dx, dz = g->dz;
+    const int Ncx = g->Nx - 1, Ncz = g->Nz - 1, nxl = 2 * (Ncx + 2), nzl = 2 * (Ncz + 2), nq = nxl * nzl;
+    const double xge = g->xg[0] - dx, zge = g->zg[0] - dz;
+    const double xce = 0.5 * (xge + (xge + dx)), zce = 0.5 * (zge + (zge + dz));
+    int *cnt = calloc((size_t)nq, sizeof(int)), *start = calloc((size_t)nq + 1, sizeof(int));
+    int *list = malloc(sizeof(int) * (size_t)(n > 0 ? n : 1)), *qk = malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    /* quarter-cell bins, marker indices ascending inside each */
+    for (int k = 0; k < n; k++) {
+        qk[k] = -1;
+        if (phase[k] < 0) continue;
+        int ic = (int)(ceil((x[k] - (xce - dx / 4.0)) / dx * 2.0 + 0.5) - 1);
+        int jc = (int)(ceil((z[k] - (zce - dz / 4.0)) / dz * 2.0 + 0.5) - 1);
+        ic = ic < 0 ? 0 : (ic > nxl - 1 ? nxl - 1 : ic);
+        jc = jc < 0 ? 0 : (jc > nzl - 1 ? nzl - 1 : jc);
+        qk[k] = ic + jc * nxl;
+        cnt[qk[k]]++;
+    }
+    for (int q = 0; q < nq; q++) start[q + 1] = start[q] + cnt[q];
+    {
+        int *cur = calloc((size_t)nq, sizeof(int));
+        for (int k = 0; k < n; k++)
+            if (qk[k] >= 0) list[start[qk[k]] + cur[qk[k]]++] = k;
+        free(cur);
+    }
+    const int thr = (int)(ceil((double)min_part_cell) / 4.0);
+    /* window visiting order (dk, dl) */
+    static const int W[25][2] = {{0, 0}, {-1, 0}, {1, 0}, {0, -1}, {0, 1}, {-1, -1}, {1, -1}, {-1, 1}, {1, 1},
+                                 {-2, 0}, {2, 0}, {0, -2}, {0, 2}, {-2, -2}, {2, -2}, {-2, 2}, {2, 2},
+                                 {-1, -2}, {1, -2}, {-1, 2}, {1, 2}, {-2, -1}, {-2, 1}, {2, -1}, {2, 1}};
+    int nnew = 0, cap_new = 4 * Ncx * Ncz;
+    double *nx_ = malloc(sizeof(double) * (size_t)cap_new), *nz_ = malloc(sizeof(double) * (size_t)cap_new);
+    int *src = malloc(sizeof(int) * (size_t)cap_new), status = 0;
+    for (int k = 2; k < nxl - 2 && !status; k++)
+        for (int l = 2; l < nzl - 2; l++) {
+            const int kd = k + l * nxl;
+            int ic = (int)(ceil(((xge + dx / 4.0 + k * dx / 2.0) - g->xc[0]) / dx + 0.5) - 1);
+            int jc = (int)(ceil(((zge + dz / 4.0 + l * dz / 2.0) - g->zc[0]) / dz + 0.5) - 1);
+            ic = ic < 0 ? 0 : (ic > Ncx - 1 ? Ncx - 1 : ic);
+            jc = jc < 0 ? 0 : (jc > Ncz - 1 ? Ncz - 1 : jc);
+            if (g->BCp_type[ic + jc * Ncx] == 30) continue;
+            if (!(cnt[kd] < thr)) continue;
+            int neighs = 0;
+            for (int w = 0; w < 25; w++) neighs += cnt[kd + W[w][0] + W[w][1] * nxl];
+            if (neighs == 0) { status = -1; break; }
+            const double xn = g->xg[0] + (k - 2) * dx / 2.0 + dx / 4.0, zn = g->zg[0] + (l - 2) * dz / 2.0 + dz / 4.0;
+            if (!(xn > g->xmin && zn > g->zmin && zn < g->zmax)) continue;
+            double best = g->xmax - g->xmin;
+            int bi = -1;
+            for (int w = 0; w < 25; w++) {
+                const int q = kd + W[w][0] + W[w][1] * nxl;
+                for (int s = start[q]; s < start[q + 1]; s++) {
+                    const int m = list[s];
+                    if (bi < 0) bi = m;   /* the reference's start: the first candidate */
+                    /* squares by pow as the reference writes them (libm's pow(a, 2) and
+                     * a * a can differ in the last bit) */
+                    const double d = sqrt(pow(xn - x[m], 2.0) + pow(zn - z[m], 2.0));
+                    if (d < best) { best = d; bi = m; }
+                }
+            }
+            nx_[nnew] = xn; nz_[nnew] = zn; src[nnew] = bi; nnew++;
+        }
+    int out = status;
+    if (!status) {
+        int nreuse = 0;
+        for (int k = 0; k < n; k++) nreuse += phase[k] == -1;
+        const int n_final = n + (nnew > nreuse ? nnew - nreuse : 0);
+        if (n_final > cap) out = -2;
+        else {
+            int *reuse = malloc(sizeof(int) * (size_t)(nreuse > 0 ? nreuse : 1)), r = 0;
+            for (int k = 0; k < n; k++) if (phase[k] == -1) reuse[r++] = k;
+            for (int q = 0; q < nnew; q++) {
+                const int slot = q < nreuse ? reuse[q] : n + (q - nreuse), m = src[q];
+                x[slot] = nx_[q]; z[slot] = nz_[q];
+                phase[slot] = phase[m]; vx[slot] = vx[m]; vz[slot] = vz[m];
+                attr[MDZ_M_STRAIN][slot] = attr[MDZ_M_STRAIN][m];
+                attr[MDZ_M_STRAIN_PL][slot] = attr[MDZ_M_STRAIN_PL][m];
+                attr[MDZ_M_CMUL][slot] = attr[MDZ_M_CMUL][m];
+                if (direct) {
+                    attr[MDZ_M_T][slot] = attr[MDZ_M_T][m];
+                    attr[MDZ_M_SXXD][slot] = attr[MDZ_M_SXXD][m];
+                    attr[MDZ_M_SZZD][slot] = attr[MDZ_M_SZZD][m];
+                    attr[MDZ_M_SXZ][slot] = attr[MDZ_M_SXZ][m];
+                } else {
+                    attr[MDZ_M_T][slot] = orc_c2p(g, x[slot], z[slot], T_n);
+                    attr[MDZ_M_SXXD][slot] = orc_c2p(g, x[slot], z[slot], sxxd_n);
+                    attr[MDZ_M_SZZD][slot] = orc_c2p(g, x[slot], z[slot], szzd_n);
+                    attr[MDZ_M_SXZ][slot] = orc_v2p_vert(g, x[slot], z[slot], sxz_s);
+                }
+            }
+            free(reuse);
+            out = n_final;
+            if (n_added) *n_added = nnew;
+        }
+    }
+    free(cnt); free(start); free(list); free(qk); free(nx_); free(nz_); free(src);
+    return out;
+}

@@ -39,6 +39,15 @@ int orc_g2p(const mdz_grid_desc *g, int n, const double *x, const double *z, con
 int orc_rk4(const mdz_grid_desc *g, int n, double *x, double *z, int *phase, double *vx, double *vz,
             const double *u, const double *v, double dt);
 
+/* Marker reseeding: CountPartCell with RESEED = 1, one OpenMP thread
+ * (SOURCE/ParticleRoutines.c:3543-4480, 977-1030, 841-890, 648-762, 259-520).
+ * attr: the MDZ_M_NATTR marker attribute arrays, all of length cap.  Returns
+ * the new marker count, -1 for a deficient quarter cell without neighbours,
+ * -2 when cap is too small; n_added receives the number of new markers. */
+int orc_reseed(const mdz_grid_desc *g, int n, int cap, double *x, double *z, int *phase, double *vx, double *vz,
+               double *const *attr, int min_part_cell, int direct, const double *T_n, const double *sxxd_n,
+               const double *szzd_n, const double *sxz_s, int *n_added);
+
 #ifdef __cplusplus
 }
 #endif

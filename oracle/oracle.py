@@ -97,6 +97,40 @@ class Oracle:
         return vx, vz
 
 
+# marker attribute order of include/mdoodz_gpu.h (MDZ_M_SXXD ... MDZ_M_CMUL)
+MARKER_ATTRS = ("sxxd", "szzd", "sxz", "strain_pl", "strain", "T", "cmul")
+
+
+def reseed(grid, markers, cap, min_part_cell=16, direct=0, T_n=None, sxxd_n=None, szzd_n=None, sxz_s=None):
+    """Marker reseeding of CountPartCell (RESEED = 1, one thread): returns a
+    new markers dict (keys x, z, phase, vx, vz and MARKER_ATTRS, length = the
+    new count) and the number of markers created.  Raises RuntimeError where
+    the reference exits."""
+    n = len(markers["x"])
+    out = {}
+    for k in ("x", "z", "vx", "vz") + MARKER_ATTRS:
+        a = np.zeros(cap)
+        a[:n] = markers[k]
+        out[k] = a
+    out["phase"] = np.full(cap, -1, np.int32)
+    out["phase"][:n] = markers["phase"]
+    attrs = (_dp * len(MARKER_ATTRS))(*[_d(out[k]) for k in MARKER_ATTRS])
+    g = grid
+    nc, nv = (g.Nx - 1) * (g.Nz - 1), g.Nx * g.Nz
+    z0 = np.zeros(max(nc, nv))
+    fld = [np.ascontiguousarray(a if a is not None else z0, np.float64) for a in (T_n, sxxd_n, szzd_n, sxz_s)]
+    added = C.c_int(0)
+    desc = grid.desc()
+    r = lib().orc_reseed(C.byref(desc), C.c_int(n), C.c_int(cap), _d(out["x"]), _d(out["z"]), _i(out["phase"]),
+                         _d(out["vx"]), _d(out["vz"]), attrs, C.c_int(min_part_cell), C.c_int(direct),
+                         _d(fld[0]), _d(fld[1]), _d(fld[2]), _d(fld[3]), C.byref(added))
+    if r == -1:
+        raise RuntimeError("reseed: a deficient quarter cell has no marker within two quarter cells")
+    if r == -2:
+        raise RuntimeError("reseed: capacity exceeded")
+    return {k: v[:r].copy() for k, v in out.items()}, added.value
+
+
 def strain_rates(grid, fields):
     s = fields.struct()
     lib().orc_strain_rates(C.byref(grid.desc()), C.byref(s))

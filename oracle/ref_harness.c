@@ -28,11 +28,13 @@
  *   SOURCE/StokesAssemblyDecoupled.c:1573 BuildStokesOperatorDecoupled
  *   SOURCE/StokesAssemblyDecoupled.c:3834 BuildJacobianOperatorDecoupled
  *   SOURCE/RheologyParticles.c:1124  UpdateParticleStress
+ *   SOURCE/ParticleRoutines.c:3543   CountPartCell (RESEED = 1: marker reseeding)
  */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <math.h>
+#include <omp.h>
 #include "header_MDOODZ.h"
 
 /* Reference functions used here whose prototypes are not in its header. */
@@ -187,6 +189,39 @@ int ref_set_markers(int n, const double *x, const double *z, const int *phase) {
     memcpy(g_parts.phase, phase, sizeof(int) * n);
     g_have_parts = 1;
     return 0;
+}
+
+/* Markers with room for cap of them (reseeding writes new markers up to cap). */
+int ref_set_markers_cap(int n, int cap, const double *x, const double *z, const int *phase) {
+    if (g_have_parts) PartFree(&g_parts, &g_model);
+    memset(&g_parts, 0, sizeof g_parts);
+    g_parts.Nb_part = n; g_parts.Nb_part_max = cap > n ? cap : (n > 0 ? n : 1);
+    PartAlloc(&g_parts, &g_model);
+    memcpy(g_parts.x, x, sizeof(double) * n);
+    memcpy(g_parts.z, z, sizeof(double) * n);
+    memcpy(g_parts.phase, phase, sizeof(int) * n);
+    g_have_parts = 1;
+    return 0;
+}
+
+/* CountPartCell with RESEED = 1 on ONE OpenMP thread: the reference splits the
+ * domain into per-thread x-slabs whose overlap decides which markers a new one
+ * may copy from, so only the one-thread result is thread-count independent.
+ * No free surface, no sedimentation, no finite strain / P-T recording /
+ * anisotropy.  Returns the new Nb_part. */
+int ref_reseed(int direct_neighbour, int min_part_cell) {
+    surface topo, topo_ini;
+    memset(&topo, 0, sizeof topo);
+    memset(&topo_ini, 0, sizeof topo_ini);
+    g_model.DirectNeighbour = direct_neighbour;
+    g_model.free_surf = 0; g_model.surf_processes = 0; g_model.fstrain = 0; g_model.rec_T_P_x_z = 0;
+    g_model.aniso = 0; g_model.isperiodic_x = 0;
+    g_parts.min_part_cell = min_part_cell;
+    const int nt = omp_get_max_threads();
+    omp_set_num_threads(1);
+    CountPartCell(&g_parts, &g_mesh, g_model, topo, topo_ini, 1, g_scale);
+    omp_set_num_threads(nt);
+    return g_parts.Nb_part;
 }
 
 double *ref_marker_field(const char *name) {

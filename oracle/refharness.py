@@ -114,6 +114,21 @@ class RefMDOODZ:
         self.lib.ref_set_markers(C.c_int(len(x)), x.ctypes.data_as(_dp), z.ctypes.data_as(_dp),
                                  phase.ctypes.data_as(_ip))
 
+    def set_markers_cap(self, x, z, phase, cap):
+        """Markers with room for cap of them (reseeding)."""
+        x = np.ascontiguousarray(x, np.float64)
+        z = np.ascontiguousarray(z, np.float64)
+        phase = np.ascontiguousarray(phase, np.int32)
+        self.n_markers = len(x)
+        self.cap = cap
+        self.lib.ref_set_markers_cap(C.c_int(len(x)), C.c_int(cap), x.ctypes.data_as(_dp), z.ctypes.data_as(_dp),
+                                     phase.ctypes.data_as(_ip))
+
+    def reseed(self, direct, min_part_cell):
+        """CountPartCell(RESEED = 1) on one thread; returns the new marker count."""
+        self.n_markers = self.lib.ref_reseed(C.c_int(direct), C.c_int(min_part_cell))
+        return self.n_markers
+
     def marker_field(self, name):
         ptr = self.lib.ref_marker_field(name.encode())
         return np.ctypeslib.as_array(ptr, shape=(self.n_markers,))

@@ -243,8 +243,76 @@ def _v2c_np(g, ver):
     return (0.25 * (V[:-1, :-1] + V[:-1, 1:] + V[1:, :-1] + V[1:, 1:])).ravel()
 
 
+RESEED_ATTRS = (("Vx", "vx"), ("Vz", "vz"), ("sxxd", "sxxd"), ("szzd", "szzd"), ("sxz", "sxz"),
+                ("strain", "strain"), ("strain_pl", "strain_pl"), ("T", "T"))
+
+
+def reseed_inputs(g, seed=11):
+    """Markers thinned at random, one cell emptied and some made inactive
+    (their slots are reused), random attributes and grid fields."""
+    rng = np.random.default_rng(seed)
+    x, z = mdz_setups.seed_markers(g, 4, 4, 0.5, seed)
+    keep = rng.random(len(x)) > 0.25
+    keep &= ~((x > g.xc[6] - 0.5 * g.dx) & (x < g.xc[6] + 0.5 * g.dx) & (z > g.zc[5] - 0.5 * g.dz) &
+              (z < g.zc[5] + 0.5 * g.dz))
+    x, z = x[keep], z[keep]
+    ph = mdz_setups.inclusion_phase(x, z, 0.05, -0.02, 0.18)
+    ph[(z > 0.25) & (x < -0.2)] = 2
+    ph[::53] = -1
+    m = dict(x=x, z=z, phase=ph.astype(np.int32))
+    for _, k in RESEED_ATTRS:
+        m[k] = rng.normal(size=len(x))
+    nc, nv = (g.Nx - 1) * (g.Nz - 1), g.Nx * g.Nz
+    fields = dict(T_n=rng.normal(size=nc), sxxd_n=rng.normal(size=nc), szzd_n=rng.normal(size=nc),
+                  sxz_s=rng.normal(size=nv))
+    return m, fields
+
+
+def make_reseed_fixture():
+    g = _grid()
+    m, fields = reseed_inputs(g)
+    out = dict(Nx=NX, Nz=NZ, box=np.array([XMIN, XMAX, ZMIN, ZMAX]), **{"in_" + k: v for k, v in m.items()},
+               **fields)
+    n = len(m["x"])
+    cap = n + 4 * (NX - 1) * (NZ - 1)
+    for direct in (1, 0):
+        for mpc in (16, 9):
+            r = RefMDOODZ(NX, NZ, XMIN, XMAX, ZMIN, ZMAX, 3)
+            r.set_bc_pureshear(1.0)
+            r.set_markers_cap(m["x"], m["z"], m["phase"], cap)
+            for ref_name, key in RESEED_ATTRS:
+                r.marker_field(ref_name)[:] = m[key]
+            r.field("T")[:] = fields["T_n"]
+            r.field("sxxd")[:] = fields["sxxd_n"]
+            r.field("szzd")[:] = fields["szzd_n"]
+            r.field("sxz")[:] = fields["sxz_s"]
+            n_new = r.reseed(direct, mpc)
+            tag = "d%d_m%d_" % (direct, mpc)
+            # only the slots the reseeding wrote (inactive ones reused, then
+            # appended ones) are stored; every other marker is unchanged
+            ph_out = r.marker_phase().copy()
+            written = np.concatenate([np.flatnonzero(m["phase"] == -1), np.arange(n, n_new)])
+            written = written[(written >= n) | (ph_out[np.minimum(written, n_new - 1)] != -1)]
+            untouched = np.setdiff1d(np.arange(n), written)
+            assert np.array_equal(r.marker_field("x")[untouched], m["x"][untouched])
+            assert np.array_equal(ph_out[untouched], m["phase"][untouched])
+            out[tag + "n"] = n_new
+            out[tag + "slots"] = written
+            out[tag + "x"] = r.marker_field("x")[written].copy()
+            out[tag + "z"] = r.marker_field("z")[written].copy()
+            out[tag + "phase"] = ph_out[written]
+            for ref_name, key in RESEED_ATTRS:
+                vals = r.marker_field(ref_name)
+                assert np.array_equal(vals[untouched], m[key][untouched]), key
+                out[tag + key] = vals[written].copy()
+            print("reseed direct=%d min_part_cell=%d: %d -> %d markers" % (direct, mpc, n, n_new))
+    np.savez_compressed(os.path.join(HERE, "reseed_ref.npz"), **out)
+
+
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["markers", "rheology"]
+    what = sys.argv[1:] or ["markers", "rheology", "reseed"]
+    if "reseed" in what:
+        make_reseed_fixture()
     if "markers" in what:
         make_markers_fixture()
     if "rheology" in what:

@@ -1,0 +1,61 @@
+"""Pin the CPU oracle's marker reseeding (CountPartCell with RESEED = 1, one
+thread: quarter-cell counts, AddPartCell2, FindClosestPhase2, slot reuse,
+AssignMarkerProperties) against golden vectors produced by the reference's
+own compiled CountPartCell (tests/golden/make_golden.py)."""
+import numpy as np
+import pytest
+
+import mdz
+import oracle
+
+ATTRS = ("vx", "vz", "sxxd", "szzd", "sxz", "strain", "strain_pl", "T")
+
+
+@pytest.fixture(scope="module")
+def ref(golden):
+    return golden("reseed_ref.npz")
+
+
+def reseed_case(ref):
+    """Grid and input markers of the fixture (the cohesion multiplier, which
+    the reference does not carry, is the marker index)."""
+    xmin, xmax, zmin, zmax = ref["box"]
+    g = mdz.Grid(int(ref["Nx"]), int(ref["Nz"]), xmin, xmax, zmin, zmax).set_bc_pureshear(1.0)
+    m = {k: np.array(ref["in_" + k]) for k in ("x", "z", "phase") + ATTRS}
+    m["cmul"] = np.arange(len(m["x"]), dtype=np.float64)
+    return g, m
+
+
+@pytest.mark.parametrize("direct", [1, 0])
+@pytest.mark.parametrize("mpc", [16, 9])
+def test_reseed_matches_reference(ref, direct, mpc):
+    g, m = reseed_case(ref)
+    n = len(m["x"])
+    cap = n + 4 * (g.Nx - 1) * (g.Nz - 1)
+    out, added = oracle.reseed(g, m, cap, mpc, direct, ref["T_n"], ref["sxxd_n"], ref["szzd_n"], ref["sxz_s"])
+    tag = "d%d_m%d_" % (direct, mpc)
+    assert len(out["x"]) == int(ref[tag + "n"])
+    slots = ref[tag + "slots"]
+    assert added >= len(slots) - np.count_nonzero(slots < n) and added > 0
+    for k in ("x", "z", "phase") + ATTRS:     # bit for bit, copies and interpolations alike
+        assert np.array_equal(out[k][slots], ref[tag + k]), k
+    untouched = np.setdiff1d(np.arange(n), slots)
+    for k in ("x", "z", "phase", "cmul") + ATTRS:
+        assert np.array_equal(out[k][untouched], m[k][untouched]), k
+    # the cohesion multiplier (not a reference attribute) travels with the copied marker
+    src = out["cmul"][slots].astype(np.int64)
+    assert np.array_equal(out["phase"][slots], m["phase"][src])
+
+
+def test_reseed_no_neighbours_raises(ref):
+    g, m = reseed_case(ref)
+    keep = m["x"] > 0.0           # the west half is empty: its quarter cells have no neighbours
+    mm = {k: v[keep] for k, v in m.items()}
+    with pytest.raises(RuntimeError):
+        oracle.reseed(g, mm, len(mm["x"]) + 4 * (g.Nx - 1) * (g.Nz - 1), 16, 1)
+
+
+def test_reseed_capacity(ref):
+    g, m = reseed_case(ref)
+    with pytest.raises(RuntimeError):
+        oracle.reseed(g, m, len(m["x"]) + 1, 16, 1)
