@@ -92,6 +92,12 @@ long long mdz_kernel_launches(const mdz_ctx *ctx);
 /* Upload markers (positions and phase) to the context's resident marker store
  * and mark the cell binning stale.  n <= max_markers. */
 mdz_status mdz_set_markers(mdz_ctx *ctx, int n, const double *x, const double *z, const int *phase);
+/* Number of resident markers (particles.Nb_part): the count set by
+ * mdz_set_markers, grown by reseeding (mdz_CountPartCell, mdz_time_step). */
+int mdz_marker_count(const mdz_ctx *ctx);
+/* Upload the resident markers' velocities (particles.Vx, Vz; RK4 writes them,
+ * reseeding copies them), e.g. when markers are restored from a saved state. */
+mdz_status mdz_set_marker_velocity(mdz_ctx *ctx, int n, const double *vx, const double *vz);
 /* Download resident marker positions / phases (any pointer may be NULL). */
 mdz_status mdz_get_markers(mdz_ctx *ctx, int n, double *x, double *z, int *phase, double *vx, double *vz);
 
@@ -133,6 +139,30 @@ mdz_status mdz_dev_p2g(mdz_ctx *ctx, int n_fields, const double *const *d_values
  * int32.  Any output may be NULL.  Host buffers. */
 mdz_status mdz_count_markers(mdz_ctx *ctx, int *nb_part_cell, int *nb_part_vert, int *phase_count_cell,
                              int *phase_count_vert);
+
+/* Marker reseeding: CountPartCell(particles, mesh, model, topo, topo_ini,
+ * RESEED, scaling) (SOURCE/ParticleRoutines.c:3543-4480) on the resident
+ * markers, with the result the reference gives on one OpenMP thread (its
+ * thread slabs change which markers a new one may copy from).  reseed = 0
+ * returns at once: the phase fractions CountPartCell also computes come from
+ * mdz_P2Mastah with prop = 1.  reseed = 1: every quarter cell whose centroid
+ * is not air and that holds fewer than (int)(ceil(min_part_cell) / 4) active
+ * markers (particles.min_part_cell) gets one marker at its centre
+ * (AddPartCell2 :977-1030).  The new marker copies the phase, velocity and
+ * strains of the nearest marker within two quarter cells (FindClosestPhase2
+ * :841-890); its T and stresses come from that marker (direct_neighbour = 1)
+ * or from the grid fields T_n, sxxd_n, szzd_n (centroids) and sxz_s
+ * (vertices) (direct_neighbour = 0, model.DirectNeighbour; host arrays, which
+ * may be NULL when direct_neighbour = 1) (AssignMarkerProperties :648-762).
+ * New markers fill the slots of inactive markers (phase -1) first and are
+ * then appended; n_added (may be NULL) receives their number.
+ * MDZ_ERR_CAPACITY if they do not fit in the context's capacity (the
+ * reference exits), MDZ_ERR_STATE if a deficient quarter cell has no marker
+ * within two quarter cells (the reference exits with code 333); the markers
+ * are unchanged then.  Free surface, sedimentation and periodic x are not
+ * implemented (the context rejects them). */
+mdz_status mdz_CountPartCell(mdz_ctx *ctx, int reseed, int min_part_cell, int direct_neighbour, const double *T_n,
+                             const double *sxxd_n, const double *szzd_n, const double *sxz_s, int *n_added);
 
 /* ---- grid -> marker interpolation ---------------------------------------- */
 
@@ -439,6 +469,13 @@ typedef struct mdz_model {
      * rebuilding it.  0: rebuilt for every solve.  No counterpart in the
      * reference. */
     double mg_reuse_below;
+    /* 1: after the advection, reseed the markers as CountPartCell(RESEED = 1)
+     * (model.Reseed with cpc = 1, Main_DOODZ.c:1235; mdz_CountPartCell) with
+     * particles.min_part_cell and model.DirectNeighbour; T and the stresses of
+     * new markers then come from the step's grid fields T, sxxd, szzd, sxz. */
+    int reseed;
+    int min_part_cell;
+    int direct_neighbour;
 } mdz_model;
 
 #define MDZ_HISTORY 32
@@ -459,6 +496,7 @@ typedef struct mdz_step_report {
     int newton_history[MDZ_HISTORY];
     int precision_fallbacks;          /* FP32-refined solves that missed min(10 x their tolerance, 0.5),
                                          redone in FP64 */
+    int markers_added;                /* markers created by the reseeding (model.reseed)      */
 } mdz_step_report;
 
 /* One time step of Main_DOODZ.c's loop (SOURCE/Main_DOODZ.c:459-1320) on the

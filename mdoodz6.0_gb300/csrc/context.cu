@@ -121,6 +121,7 @@ extern "C" void mdz_destroy(mdz_ctx *ctx) {
     if (!ctx) return;
     mdz_solver_free(ctx);
     mdz_mlp_free(ctx);
+    mdz_reseed_free(ctx);
     mdz_free_fields(ctx);
     mdz_dgrid &g = ctx->g;
     void *ptrs[] = {g.xg, g.zg, g.xc, g.zc, g.xvz, g.zvx, g.BCu, g.BCv, g.BCp, g.BCg, g.BCu_val, g.BCv_val,
@@ -138,6 +139,7 @@ extern "C" void mdz_destroy(mdz_ctx *ctx) {
 
 extern "C" const char *mdz_last_error(const mdz_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 extern "C" long long mdz_kernel_launches(const mdz_ctx *ctx) { return ctx ? ctx->launches : 0; }
+extern "C" int mdz_marker_count(const mdz_ctx *ctx) { return ctx ? ctx->m.n : 0; }
 
 extern "C" mdz_status mdz_set_markers(mdz_ctx *ctx, int n, const double *x, const double *z, const int *phase) {
     if (!ctx) return MDZ_ERR_ARG;
@@ -152,6 +154,19 @@ extern "C" mdz_status mdz_set_markers(mdz_ctx *ctx, int n, const double *x, cons
     MDZ_CUDA(ctx, cudaStreamSynchronize(st));
     ctx->m.n = n;
     ctx->bins.valid = false;
+    return MDZ_OK;
+}
+
+extern "C" mdz_status mdz_set_marker_velocity(mdz_ctx *ctx, int n, const double *vx, const double *vz) {
+    if (!ctx) return MDZ_ERR_ARG;
+    if (n < 0 || n > ctx->m.n || (n > 0 && (!vx || !vz)))
+        return mdz_fail(ctx, MDZ_ERR_ARG, "mdz_set_marker_velocity: bad arguments (n=%d, resident %d)", n, ctx->m.n);
+    cudaStream_t st = ctx->stream;
+    if (n) {
+        MDZ_CUDA(ctx, cudaMemcpyAsync(ctx->m.vx, vx, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+        MDZ_CUDA(ctx, cudaMemcpyAsync(ctx->m.vz, vz, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    }
+    MDZ_CUDA(ctx, cudaStreamSynchronize(st));
     return MDZ_OK;
 }
 

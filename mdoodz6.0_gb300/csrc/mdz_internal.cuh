@@ -83,6 +83,7 @@ struct mdz_ctx {
     long long prof_n[8] = {0};
     struct mdz_solver *solver = nullptr;   // Krylov / multigrid workspace (solver.cu)
     struct mdz_mlp *mlp = nullptr;         // learned local-rheology guess (mlp.cu)
+    struct mdz_reseed_ws *reseed = nullptr;   // quarter-cell workspace of the reseeding (reseed.cu)
     std::string err;
     // host-call staging buffers (grown on demand)
     void *stage[8] = {nullptr};
@@ -121,8 +122,23 @@ struct mdz_nodeset {
 };
 mdz_nodeset mdz_get_nodeset(const mdz_ctx *ctx, int centroid);
 
-// Binning (markers.cu)
+// Binning (markers.cu): the cell bins, and the scan / scatter / per-bin
+// sort kernels the quarter-cell bins of the reseeding reuse.
 mdz_status mdz_ensure_bins(mdz_ctx *ctx, cudaStream_t st);
+__global__ void k_scan_blocks(int n, const int *__restrict__ in, int *__restrict__ out, int *__restrict__ partial);
+__global__ void k_scan_partials(int nb, int *partial);
+__global__ void k_scan_add(int n, int *__restrict__ out, const int *__restrict__ partial);
+__global__ void k_bin_scatter(int n, const int *__restrict__ cell, const int *__restrict__ start,
+                              int *__restrict__ cursor, int *__restrict__ sorted);
+__global__ void k_bin_sort_segments(int ncells, const int *__restrict__ start, int *__restrict__ sorted);
+
+// Marker reseeding (reseed.cu): the reseeding of CountPartCell on the resident
+// markers; T_n, sxxd_n, szzd_n (centroids) and sxz_s (vertices) are device
+// fields, read when direct = 0.
+struct mdz_attr_ptrs { double *a[MDZ_M_NATTR]; };
+mdz_status mdz_dev_reseed(mdz_ctx *ctx, int min_part_cell, int direct, const double *T_n, const double *sxxd_n,
+                          const double *szzd_n, const double *sxz_s, cudaStream_t st, int *n_added);
+void mdz_reseed_free(mdz_ctx *ctx);
 
 // Every mdz_fields member with its node set (X-macro): VX / VZ velocity nodes,
 // CEN centroids, VER vertices, PPN / PPS phase fractions (n_phases rows).

@@ -563,6 +563,11 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
             MDZ_LAUNCHED(ctx);
         }
         if ((s = mdz_dev_rk4(ctx, f.u, f.v, M->rheo.dt, st)) != MDZ_OK) return s;
+        // reseeding after the advection (Main_DOODZ.c:1233-1236)
+        if (M->reseed)
+            if ((s = mdz_dev_reseed(ctx, M->min_part_cell, M->direct_neighbour, f.T, f.sxxd, f.szzd, f.sxz, st,
+                                    &R.markers_added)) != MDZ_OK)
+                return s;
     }
     cudaEventRecord(t1, st);
     MDZ_CUDA(ctx, cudaEventSynchronize(t1));

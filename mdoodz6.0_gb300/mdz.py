@@ -53,6 +53,7 @@ def load_library(path=LIB_PATH):
     L = C.CDLL(path)
     L.mdz_last_error.restype = C.c_char_p
     L.mdz_kernel_launches.restype = C.c_longlong
+    L.mdz_marker_count.restype = C.c_int
     L.mdz_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(GridDesc), C.c_int, C.c_longlong]
     L.mdz_host_register.argtypes = [C.c_void_p, C.c_size_t]
     L.mdz_host_unregister.argtypes = [C.c_void_p]
@@ -190,7 +191,6 @@ class Context:
         if st != 0:
             raise MdzError(st, "mdz_create failed (no usable CUDA device or bad grid)")
         self.h = h
-        self.n_markers = 0
 
     def close(self):
         if getattr(self, "h", None):
@@ -217,7 +217,16 @@ class Context:
         z = np.ascontiguousarray(z, np.float64)
         phase = np.ascontiguousarray(phase, np.int32)
         self._check(self.L.mdz_set_markers(self.h, C.c_int(len(x)), _dptr(x), _dptr(z), _iptr(phase)))
-        self.n_markers = len(x)
+
+    def set_marker_velocity(self, vx, vz):
+        vx = np.ascontiguousarray(vx, np.float64)
+        vz = np.ascontiguousarray(vz, np.float64)
+        self._check(self.L.mdz_set_marker_velocity(self.h, C.c_int(len(vx)), _dptr(vx), _dptr(vz)))
+
+    @property
+    def n_markers(self):
+        """Resident marker count (grows when reseeding appends markers)."""
+        return int(self.L.mdz_marker_count(self.h)) if self.h else 0
 
     def get_markers(self, out=None):
         """(x, z, phase, vx, vz) of the resident markers; `out` may hold five
@@ -254,6 +263,17 @@ class Context:
         pc, pv = np.zeros((self.n_phases, nc), np.int32), np.zeros((self.n_phases, nv), np.int32)
         self._check(self.L.mdz_count_markers(self.h, _iptr(c), _iptr(v), _iptr(pc), _iptr(pv)))
         return c, v, pc, pv
+
+    def CountPartCell(self, reseed=1, min_part_cell=16, direct_neighbour=0, T_n=None, sxxd_n=None, szzd_n=None,
+                      sxz_s=None):
+        """CountPartCell (SOURCE/ParticleRoutines.c:3543) with RESEED = reseed
+        on the resident markers; returns the number of markers created."""
+        a = [None if v is None else np.ascontiguousarray(v, np.float64) for v in (T_n, sxxd_n, szzd_n, sxz_s)]
+        added = C.c_int(0)
+        self._check(self.L.mdz_CountPartCell(self.h, C.c_int(reseed), C.c_int(min_part_cell),
+                                             C.c_int(direct_neighbour), *[_dptr(v) if v is not None else None for v in a],
+                                             C.byref(added)))
+        return added.value
 
     def Interp_Grid2P(self, node_field, node_set):
         nf = np.ascontiguousarray(node_field, np.float64)
@@ -551,16 +571,19 @@ class Model(C.Structure):
                 ("precision", C.c_int), ("learned_guess", C.c_int), ("itp_stencil", C.c_int),
                 ("softening", C.c_int), ("advect", C.c_int), ("picard2newton", C.c_int),
                 ("pic2newt_cond", C.c_double), ("nit_pic_max", C.c_int), ("newton_maxit", C.c_int),
-                ("adaptive_lin_tol", C.c_int), ("fp32_rheology_its", C.c_int), ("mg_reuse_below", C.c_double)]
+                ("adaptive_lin_tol", C.c_int), ("fp32_rheology_its", C.c_int), ("mg_reuse_below", C.c_double),
+                ("reseed", C.c_int), ("min_part_cell", C.c_int), ("direct_neighbour", C.c_int)]
 
     @classmethod
     def make(cls, rheo, gx=0.0, gz=0.0, newton=1, nit_max=10, rel_tol=1e-8, abs_tol=1e-300, lin_rtol=1e-5,
              lin_maxit=500, line_search=0, line_search_min=0.0, precision=64, learned_guess=0, itp_stencil=1,
              softening=0, advect=1, picard2newton=0, pic2newt_cond=1e-1, nit_pic_max=10, newton_maxit=0,
-             adaptive_lin_tol=0, fp32_rheology_its=0, mg_reuse_below=0.0):
+             adaptive_lin_tol=0, fp32_rheology_its=0, mg_reuse_below=0.0, reseed=0, min_part_cell=16,
+             direct_neighbour=0):
         return cls(rheo, gx, gz, newton, nit_max, rel_tol, abs_tol, lin_rtol, lin_maxit, line_search,
                    line_search_min, precision, learned_guess, itp_stencil, softening, advect, picard2newton,
-                   pic2newt_cond, nit_pic_max, newton_maxit, adaptive_lin_tol, fp32_rheology_its, mg_reuse_below)
+                   pic2newt_cond, nit_pic_max, newton_maxit, adaptive_lin_tol, fp32_rheology_its, mg_reuse_below,
+                   reseed, min_part_cell, direct_neighbour)
 
 
 class StepReport(C.Structure):
@@ -572,7 +595,7 @@ class StepReport(C.Structure):
                 ("ms_total", C.c_double), ("newton_its", C.c_int), ("local_iterations", C.c_longlong),
                 ("res_history", (C.c_double * 3) * 32), ("lin_its_history", C.c_int * 32),
                 ("lin_rel_history", C.c_double * 32), ("newton_history", C.c_int * 32),
-                ("precision_fallbacks", C.c_int)]
+                ("precision_fallbacks", C.c_int), ("markers_added", C.c_int)]
 
     def as_dict(self):
         def plain(v):

@@ -269,8 +269,14 @@ def time_step(g, mat, model, markers, u, v, p, fields_out=None):
         e, ep = _accumulated_strain(g, markers, dstr, dstr_pl)
         markers["strain"] += e
         markers["strain_pl"] += ep
-        o.RogerGuntherII(u, v, dt)
+        markers["vx"], markers["vz"] = o.RogerGuntherII(u, v, dt)
         markers["x"], markers["z"], markers["phase"] = o.x, o.z, o.phase
+        rep["markers_added"] = 0
+        if getattr(model, "reseed", 0):   # CountPartCell(RESEED = 1) after the advection
+            cap = len(markers["x"]) + 4 * (g.Nx - 1) * (g.Nz - 1)
+            new, rep["markers_added"] = orc.reseed(g, markers, cap, model.min_part_cell, model.direct_neighbour,
+                                                   f["T"], f["sxxd"], f["szzd"], f["sxz"])
+            markers.update(new)
     if fields_out is not None:
         fields_out.update({k: f[k].copy() for k in f.a})
     return u, v, p, rep

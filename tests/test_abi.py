@@ -40,3 +40,31 @@ def test_every_declared_symbol_is_exported(lib):
     missing = [n for n in _declared() if not hasattr(lib, n)]
     assert not missing, missing
 
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """The ctypes mirrors of the header's structs have the C compiler's size
+    and field offsets (a C program built here against include/mdoodz_gpu.h
+    prints them)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    mirrors = {"mdz_grid_desc": mdz.GridDesc, "mdz_fields": mdz.FieldsStruct, "mdz_materials": mdz.Materials,
+               "mdz_rheo_params": mdz.RheoParams, "mdz_model": mdz.Model, "mdz_step_report": mdz.StepReport}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "mdoodz_gpu.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for fname, _ in py._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    lines.append("return 0; }")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = dict(l.split() for l in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n") if l)
+    for cname, py in mirrors.items():
+        assert int(out[cname]) == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert int(out[cname + "." + fname]) == getattr(py, fname).offset, (cname, fname)

@@ -33,8 +33,8 @@ def vep_case(N=33, nm=4, seed=5):
     return g, m, u, v, p, mat
 
 
-def run_gpu(g, m, u, v, p, mat, model):
-    ctx = mdz.Context(g, mat.n_phases, len(m["x"]))
+def run_gpu(g, m, u, v, p, mat, model, cap=None):
+    ctx = mdz.Context(g, mat.n_phases, cap or len(m["x"]))
     ctx.set_markers(m["x"], m["z"], m["phase"])
     for attr, key in ((mdz.M_SXXD, "sxxd"), (mdz.M_SZZD, "szzd"), (mdz.M_SXZ, "sxz"), (mdz.M_STRAIN_PL, "strain_pl"),
                       (mdz.M_STRAIN, "strain"), (mdz.M_T, "T"), (mdz.M_CMUL, "cmul")):
@@ -49,9 +49,11 @@ def run_gpu(g, m, u, v, p, mat, model):
     rep = ctx.time_step(mat, model)
     out = mdz.GridFields(g, mat.n_phases)
     ctx.download_fields(out)
-    x, z, ph, _, _ = ctx.get_markers()
-    mk = dict(x=x, z=z, phase=ph, sxxd=ctx.get_marker_attr(mdz.M_SXXD), szzd=ctx.get_marker_attr(mdz.M_SZZD),
-              sxz=ctx.get_marker_attr(mdz.M_SXZ), strain_pl=ctx.get_marker_attr(mdz.M_STRAIN_PL))
+    x, z, ph, vx, vz = ctx.get_markers()
+    mk = dict(x=x, z=z, phase=ph, vx=vx, vz=vz, sxxd=ctx.get_marker_attr(mdz.M_SXXD),
+              szzd=ctx.get_marker_attr(mdz.M_SZZD), sxz=ctx.get_marker_attr(mdz.M_SXZ),
+              strain_pl=ctx.get_marker_attr(mdz.M_STRAIN_PL), strain=ctx.get_marker_attr(mdz.M_STRAIN),
+              T=ctx.get_marker_attr(mdz.M_T), cmul=ctx.get_marker_attr(mdz.M_CMUL))
     ctx.close()
     return out, mk, rep
 
@@ -98,6 +100,29 @@ def test_adaptive_linear_tolerance_same_step(precision):
     assert _rel(out_a["p"] - out_a["p"].mean(), out_f["p"] - out_f["p"].mean()) < 1e-8
     for k in ("sxxd", "szzd", "sxz", "x", "z"):
         assert _rel(mk_a[k], mk_f[k]) < 1e-8, k
+
+
+@pytest.mark.parametrize("direct", [1, 0])
+def test_vep_step_with_reseeding_vs_oracle(direct):
+    """model.reseed: CountPartCell(RESEED = 1) after the advection; the same
+    markers are created (count, slots, positions, phases) as by the oracle
+    step followed by the oracle reseeding, with the same attributes.  A short
+    step (dt = 0.02 at unit pure-shear rate): a long one empties bands along
+    the walls wider than two quarter cells, where the reference stops."""
+    g, m, u, v, p, mat = vep_case()
+    prm = mdz.RheoParams.make(dt=0.02, iselastic=1, step=1)
+    model = mdz.Model.make(prm, newton=1, nit_max=12, rel_tol=1e-11, lin_rtol=1e-9, line_search=0, precision=64,
+                           reseed=1, min_part_cell=16, direct_neighbour=direct)
+    cap = len(m["x"]) + 4 * g.ncx * g.ncz
+    out, mk, rep = run_gpu(g, dict((k, np.array(v_)) for k, v_ in m.items()), u, v, p, mat, model, cap=cap)
+    mo = dict((k, np.array(v_)) for k, v_ in m.items())
+    uo, vo, po, ro = oracle_step.time_step(g, mat, model, mo, u, v, p)
+    assert rep.converged == 1 and ro["converged"] == 1
+    assert rep.markers_added == ro["markers_added"] > 0, (rep.markers_added, ro["markers_added"])
+    assert len(mk["x"]) == len(mo["x"])
+    assert np.array_equal(mk["phase"], mo["phase"])
+    for k in ("x", "z", "vx", "vz", "sxxd", "szzd", "sxz", "strain_pl", "strain", "T", "cmul"):
+        assert _rel(mk[k], mo[k]) < 1e-8, (k, _rel(mk[k], mo[k]))
 
 
 def test_multigrid_reuse_same_step():
