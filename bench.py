@@ -117,12 +117,14 @@ def train_guess(ctx, cfg, n=1 << 20, batch=65536, seed=1):
     return time.perf_counter() - t0, loss
 
 
-def run_form(cfg_builder, precision, learned, steps, warmup, size):
+def run_form(cfg_builder, precision, learned, steps, warmup, size, reseed=False):
     import numpy as np
     import mdz
     import mdz_setups
     cfg = cfg_builder(precision, learned, size)
-    ctx = mdz_setups.load_context(cfg)
+    g = cfg["grid"]
+    # room for one reseeding pass (one marker per quarter cell at most)
+    ctx = mdz_setups.load_context(cfg, max_markers=len(cfg["markers"]["x"]) + 4 * g.ncx * g.ncz)
     model, mat = cfg["model"], cfg["mat"]
     train = train_guess(ctx, cfg) if learned else None
     reps = []
@@ -144,9 +146,42 @@ def run_form(cfg_builder, precision, learned, steps, warmup, size):
     ctx._check(ctx.L.mdz_get_velocity(ctx.h, mdz._dptr(final["u"]), mdz._dptr(final["v"]), mdz._dptr(final["p"])))
     final["sxxd"] = ctx.get_marker_attr(mdz.M_SXXD)
     final["sxz"] = ctx.get_marker_attr(mdz.M_SXZ)
+    rs = reseed_pass(ctx, cfg) if reseed else None
     ctx.close()
     return dict(ms_wall=wall, ms_gpu=gpu_ms, reports=reps, launches=launches, kernel=kern, cfg=cfg, train=train,
-                final=final)
+                final=final, reseed=rs)
+
+
+def reseed_pass(ctx, cfg, min_part_cell=16):
+    """One reseeding pass (CountPartCell with RESEED = 1, DirectNeighbour = 1)
+    of the resident markers after the timed steps, through the C ABI: wall
+    time of the synchronous call (a pass with min_part_cell = 0, which adds
+    nothing, sets up its workspace first).  The CPU side is the oracle's
+    one-thread restatement on the same markers."""
+    import mdz
+    import oracle
+    x, z, ph, vx, vz = ctx.get_markers()
+    m = dict(x=x, z=z, phase=ph, vx=vx, vz=vz)
+    for k, a in zip(oracle.MARKER_ATTRS, range(mdz.M_NATTR)):
+        m[k] = ctx.get_marker_attr(a)
+    n = len(x)
+    ctx.CountPartCell(1, 0, 1)
+    ctx.L.mdz_sync(ctx.h)
+    t0 = time.perf_counter()
+    added = ctx.CountPartCell(1, min_part_cell, 1)
+    ms = (time.perf_counter() - t0) * 1e3
+    g = cfg["grid"]
+    t0 = time.perf_counter()
+    _, added_cpu = oracle.reseed(g, m, n + 4 * g.ncx * g.ncz, min_part_cell, 1)
+    ms_cpu = (time.perf_counter() - t0) * 1e3
+    # algorithmic bytes: marker x, z, phase read twice (bins, candidates), one
+    # int bin index written and read, quarter-cell counts, and the new markers
+    # written with their 12 copied values
+    nq = (2 * g.ncx + 4) * (2 * g.ncz + 4)
+    byts = n * (2 * 20 + 8) + nq * 16 + added * (12 * 8 + 16)
+    return {"markers": n, "added": added, "ms": ms, "GB/s": byts / (ms * 1e-3) / 1e9,
+            "cpu_baseline": {"value": ms_cpu, "unit": "ms", "cores": 1, "kind": "port", "added": added_cpu,
+                             "sample": "the same markers, one pass"}}
 
 
 def field_diffs(a, b):
@@ -326,7 +361,7 @@ def main():
     GUESS_STEPS[0] = args.guess_steps
     with ClockSampler(local) as clk:
         plain = run_form(b, 64, 0, args.steps, args.warmup, size)
-        fast = run_form(b, 32, 1, args.steps, args.warmup, size)
+        fast = run_form(b, 32, 1, args.steps, args.warmup, size, reseed=rank == 0 and not args.no_cpu)
     ms = fast["ms_wall"]
     if world > 1:
         t = torch.tensor([ms], device="cuda")
@@ -361,6 +396,8 @@ def main():
                      "peak_kind": peak_kind},
         "clocks": clk.summary(),
     }
+    if fast["reseed"]:
+        line["reseed"] = fast["reseed"]
     if rank == 0 and not args.no_mlp:
         line["mlp"] = mlp_workload()
     if rank == 0 and not args.no_cpu:

@@ -561,6 +561,7 @@ class RheoParams(C.Structure):
 
 # marker attributes (enum in include/mdoodz_gpu.h)
 M_SXXD, M_SZZD, M_SXZ, M_STRAIN_PL, M_STRAIN, M_T, M_CMUL = range(7)
+M_NATTR = 7
 
 
 class Model(C.Structure):
