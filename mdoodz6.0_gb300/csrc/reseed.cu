@@ -105,52 +105,53 @@ __constant__ signed char c_window[25][2] = {
     {-2, 0},  {2, 0},  {0, -2}, {0, 2},  {-2, -2}, {2, -2}, {-2, 2}, {2, 2},
     {-1, -2}, {1, -2}, {-1, 2}, {1, 2},  {-2, -1}, {-2, 1}, {2, -1}, {2, 1}};
 
-// New-marker position of inner quarter cell (k, l): xg[0] + ic dx/2 + dx/4 with ic = k - 2.
+// New-marker position of inner quarter cell (k, l): xg[0] + ic dx/2 + dx/4 with
+// ic = k - 2 (halving and quartering are exact as products with 0.5, 0.25).
 __device__ __forceinline__ double new_pos(double o, int i, double h) {
-    return __dadd_rn(__dadd_rn(o, __ddiv_rn(__dmul_rn((double)i, h), 2.0)), __ddiv_rn(h, 4.0));
+    return __dadd_rn(__dadd_rn(o, __dmul_rn(__dmul_rn((double)i, h), 0.5)), __dmul_rn(h, 0.25));
 }
 
 // One thread per inner quarter cell; t runs over (k, l) with k fastest, the
-// outputs are stored in the reference's creation order q = (k-2) (nzl-4) + (l-2).
+// flags are stored in the reference's creation order q = (k-2) (nzl-4) + (l-2).
+// The count test comes first (integer), then the air test of the cell's
+// centroid, the neighbour count and the box test of the new position.
 __global__ void k_reseed_cells(quarter_geom q, const signed char *__restrict__ tagp, const int *__restrict__ qstart,
-                               const int *__restrict__ qsorted, const double *__restrict__ x,
-                               const double *__restrict__ z, int thr, int *__restrict__ flag,
-                               int *__restrict__ src, int *__restrict__ status) {
+                               int thr, int *__restrict__ flag, int *__restrict__ status) {
     const int wi = q.nxl - 4, wj = q.nzl - 4;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= wi * wj) return;
     const int k = 2 + t % wi, l = 2 + t / wi, qo = (k - 2) * wj + (l - 2), kd = k + l * q.nxl;
-    flag[qo] = 0;
-    // centroid of the quarter cell's coarse cell, for the air test
-    const double cx = __dadd_rn(__dadd_rn(q.xge, __ddiv_rn(q.dx, 4.0)), __ddiv_rn(__dmul_rn((double)k, q.dx), 2.0));
-    const double cz = __dadd_rn(__dadd_rn(q.zge, __ddiv_rn(q.dz, 4.0)), __ddiv_rn(__dmul_rn((double)l, q.dz), 2.0));
-    int ic = nearest_of(__ddiv_rn(cx - q.xc0, q.dx)), jc = nearest_of(__ddiv_rn(cz - q.zc0, q.dz));
-    ic = ic < 0 ? 0 : (ic > q.Ncx - 1 ? q.Ncx - 1 : ic);
-    jc = jc < 0 ? 0 : (jc > q.Ncz - 1 ? q.Ncz - 1 : jc);
-    if (tagp[ic + jc * q.Ncx] == 30) return;
-    if (!(qstart[kd + 1] - qstart[kd] < thr)) return;
-    int neighs = 0;
-    for (int w = 0; w < 25; w++) {
-        const int c = kd + c_window[w][0] + c_window[w][1] * q.nxl;
-        neighs += qstart[c + 1] - qstart[c];
-    }
-    if (neighs == 0) { atomicOr(status, 1); return; }
-    const double xn = new_pos(q.xg0, k - 2, q.dx), zn = new_pos(q.zg0, l - 2, q.dz);
-    if (!(xn > q.xmin && zn > q.zmin && zn < q.zmax)) return;
-    double best = q.xmax - q.xmin;
-    int bi = -1;
-    for (int w = 0; w < 25; w++) {
-        const int c = kd + c_window[w][0] + c_window[w][1] * q.nxl;
-        for (int s = qstart[c], e = qstart[c + 1]; s < e; s++) {
-            const int m = qsorted[s];
-            if (bi < 0) bi = m;
-            const double ax = xn - x[m], az = zn - z[m];
-            const double d = sqrt(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(az, az)));
-            if (d < best) { best = d; bi = m; }
+    int f = 0;
+    if (qstart[kd + 1] - qstart[kd] < thr) {
+        // centroid of the quarter cell's coarse cell, for the air test
+        const double cx = __dadd_rn(__dadd_rn(q.xge, __dmul_rn(q.dx, 0.25)), __dmul_rn(__dmul_rn((double)k, q.dx), 0.5));
+        const double cz = __dadd_rn(__dadd_rn(q.zge, __dmul_rn(q.dz, 0.25)), __dmul_rn(__dmul_rn((double)l, q.dz), 0.5));
+        int ic = nearest_of(__ddiv_rn(cx - q.xc0, q.dx)), jc = nearest_of(__ddiv_rn(cz - q.zc0, q.dz));
+        ic = ic < 0 ? 0 : (ic > q.Ncx - 1 ? q.Ncx - 1 : ic);
+        jc = jc < 0 ? 0 : (jc > q.Ncz - 1 ? q.Ncz - 1 : jc);
+        if (tagp[ic + jc * q.Ncx] != 30) {
+            int neighs = 0;
+            for (int w = 0; w < 25; w++) {
+                const int c = kd + c_window[w][0] + c_window[w][1] * q.nxl;
+                neighs += qstart[c + 1] - qstart[c];
+            }
+            if (neighs == 0) {
+                atomicOr(status, 1);
+            } else {
+                const double xn = new_pos(q.xg0, k - 2, q.dx), zn = new_pos(q.zg0, l - 2, q.dz);
+                f = xn > q.xmin && zn > q.zmin && zn < q.zmax;
+            }
         }
     }
-    flag[qo] = 1;
-    src[qo] = bi;
+    flag[qo] = f;
+}
+
+// Inverse of the ranks: list[rank] = quarter cell, so that the search below
+// runs one thread per new marker.
+__global__ void k_reseed_list(int ni, const int *__restrict__ flag, const int *__restrict__ rank,
+                              int *__restrict__ list) {
+    const int qo = blockIdx.x * blockDim.x + threadIdx.x;
+    if (qo < ni && flag[qo]) list[rank[qo]] = qo;
 }
 
 __global__ void k_inactive_flags(int n, const int *__restrict__ phase, int *__restrict__ inact) {
@@ -222,17 +223,36 @@ struct reseed_fields {
     const double *T_n, *sxxd_n, *szzd_n, *sxz_s;
 };
 
-__global__ void k_reseed_write(quarter_geom q, mdz_dgrid g, int n, int nreuse, const int *__restrict__ flag,
-                               const int *__restrict__ rank, const int *__restrict__ src,
+// One thread per new marker r: its quarter cell, the nearest of the markers
+// in the 5x5 quarter cells around it (the reference's visiting order; a
+// candidate replaces the best only when strictly closer: the square test
+// skips the square root of every candidate that cannot be), and the copy.
+__global__ void k_reseed_write(quarter_geom q, mdz_dgrid g, int n, int nnew, int nreuse, const int *__restrict__ list,
+                               const int *__restrict__ qstart, const int *__restrict__ qsorted,
                                const int *__restrict__ reuse, double *x, double *z, int *phase, double *vx,
                                double *vz, mdz_attr_ptrs A, int direct, reseed_fields F) {
-    const int wj = q.nzl - 4, ni = (q.nxl - 4) * wj;
-    const int qo = blockIdx.x * blockDim.x + threadIdx.x;
-    if (qo >= ni || !flag[qo]) return;
-    const int r = rank[qo], m = src[qo];
-    const int slot = r < nreuse ? reuse[r] : n + (r - nreuse);
-    const int k = 2 + qo / wj, l = 2 + qo % wj;
+    const int wj = q.nzl - 4;
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nnew) return;
+    const int qo = list[r];
+    const int k = 2 + qo / wj, l = 2 + qo % wj, kd = k + l * q.nxl;
     const double xn = new_pos(q.xg0, k - 2, q.dx), zn = new_pos(q.zg0, l - 2, q.dz);
+    double best = q.xmax - q.xmin, best2 = INFINITY;
+    int m = -1;
+    for (int w = 0; w < 25; w++) {
+        const int c = kd + c_window[w][0] + c_window[w][1] * q.nxl;
+        for (int s = qstart[c], e = qstart[c + 1]; s < e; s++) {
+            const int j = qsorted[s];
+            if (m < 0) m = j;
+            const double ax = xn - x[j], az = zn - z[j];
+            const double d2 = __dadd_rn(__dmul_rn(ax, ax), __dmul_rn(az, az));
+            if (d2 < best2) {   // sqrt is monotone: d2 >= best2 cannot give d < best
+                const double d = sqrt(d2);
+                if (d < best) { best = d; best2 = d2; m = j; }
+            }
+        }
+    }
+    const int slot = r < nreuse ? reuse[r] : n + (r - nreuse);
     x[slot] = xn;
     z[slot] = zn;
     phase[slot] = phase[m];
@@ -283,7 +303,7 @@ static mdz_status reseed_ws(mdz_ctx *ctx, const quarter_geom &q, mdz_reseed_ws *
     MDZ_CUDA(ctx, A(W->qpart, (nq + 1023) / 1024 + 1));
     MDZ_CUDA(ctx, A(W->flag, ni));
     MDZ_CUDA(ctx, A(W->rank, ni + 1));
-    MDZ_CUDA(ctx, A(W->src, ni));
+    MDZ_CUDA(ctx, A(W->src, ni));   // list: quarter cell of each new marker
     MDZ_CUDA(ctx, A(W->ipart, (ni + 1023) / 1024 + 1));
     MDZ_CUDA(ctx, A(W->inact, cap));
     MDZ_CUDA(ctx, A(W->islot, cap + 1));
@@ -325,10 +345,11 @@ mdz_status mdz_dev_reseed(mdz_ctx *ctx, int min_part_cell, int direct, const dou
     MDZ_LAUNCHED(ctx);
     // deficient quarter cells and their nearest markers, then the ranks
     const int thr = (int)(std::ceil((double)min_part_cell) / 4.0);
-    k_reseed_cells<<<mdz_blocks(ni), MDZ_THREADS, 0, st>>>(q, ctx->g.BCp, W->qstart, W->qsorted, ctx->m.x,
-                                                          ctx->m.z, thr, W->flag, W->src, W->status);
+    k_reseed_cells<<<mdz_blocks(ni), MDZ_THREADS, 0, st>>>(q, ctx->g.BCp, W->qstart, thr, W->flag, W->status);
     MDZ_LAUNCHED(ctx);
     if ((s = scan_ints(ctx, ni, W->flag, W->rank, W->ipart, st)) != MDZ_OK) return s;
+    k_reseed_list<<<mdz_blocks(ni), MDZ_THREADS, 0, st>>>(ni, W->flag, W->rank, W->src);
+    MDZ_LAUNCHED(ctx);
     // inactive slots in index order
     int nreuse = 0;
     if (n > 0) {
@@ -353,10 +374,10 @@ mdz_status mdz_dev_reseed(mdz_ctx *ctx, int min_part_cell, int direct, const dou
     if (nnew > 0) {
         mdz_attr_ptrs A;
         for (int a = 0; a < MDZ_M_NATTR; a++) A.a[a] = ctx->m.attr[a];
-        k_reseed_write<<<mdz_blocks(ni), MDZ_THREADS, 0, st>>>(q, ctx->g, n, nreuse, W->flag, W->rank, W->src,
-                                                               W->reuse, ctx->m.x, ctx->m.z, ctx->m.phase, ctx->m.vx,
-                                                               ctx->m.vz, A, direct,
-                                                               reseed_fields{T_n, sxxd_n, szzd_n, sxz_s});
+        k_reseed_write<<<mdz_blocks(nnew), MDZ_THREADS, 0, st>>>(q, ctx->g, n, nnew, nreuse, W->src, W->qstart,
+                                                                 W->qsorted, W->reuse, ctx->m.x, ctx->m.z,
+                                                                 ctx->m.phase, ctx->m.vx, ctx->m.vz, A, direct,
+                                                                 reseed_fields{T_n, sxxd_n, szzd_n, sxz_s});
         MDZ_LAUNCHED(ctx);
     }
     ctx->m.n = (int)n_final;
