@@ -95,6 +95,19 @@ mdz_status mdz_set_markers(mdz_ctx *ctx, int n, const double *x, const double *z
 /* Number of resident markers (particles.Nb_part): the count set by
  * mdz_set_markers, grown by reseeding (mdz_CountPartCell, mdz_time_step). */
 int mdz_marker_count(const mdz_ctx *ctx);
+/* Breakpoint of the resident state (MakeBreakpointParticles /
+ * LoadBreakpointParticles, SOURCE/InputOutput.c:515-1007, 160-514, for what
+ * this library keeps between steps): markers (x, z, phase, Vx, Vz and the
+ * MDZ_M_* attributes) and the grid u, v, p that start the next step, from
+ * the device mirrors to one binary file ("MDZBRK01" header with the grid
+ * sizes, then the arrays in host byte order) and back into a context of the
+ * same grid and phase count.  A restart from it continues as the
+ * uninterrupted run; the learned guess's weights are saved separately
+ * (mdz_mlp_get_weights).  MDZ_ERR_ARG for an unreadable, foreign or
+ * truncated file (the context is unchanged then), MDZ_ERR_CAPACITY when its
+ * markers exceed the capacity. */
+mdz_status mdz_save_breakpoint(mdz_ctx *ctx, const char *path);
+mdz_status mdz_load_breakpoint(mdz_ctx *ctx, const char *path);
 /* Upload the resident markers' velocities (particles.Vx, Vz; RK4 writes them,
  * reseeding copies them), e.g. when markers are restored from a saved state. */
 mdz_status mdz_set_marker_velocity(mdz_ctx *ctx, int n, const double *vx, const double *vz);

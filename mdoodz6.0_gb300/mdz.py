@@ -218,6 +218,12 @@ class Context:
         phase = np.ascontiguousarray(phase, np.int32)
         self._check(self.L.mdz_set_markers(self.h, C.c_int(len(x)), _dptr(x), _dptr(z), _iptr(phase)))
 
+    def save_breakpoint(self, path):
+        self._check(self.L.mdz_save_breakpoint(self.h, os.fsencode(path)))
+
+    def load_breakpoint(self, path):
+        self._check(self.L.mdz_load_breakpoint(self.h, os.fsencode(path)))
+
     def set_marker_velocity(self, vx, vz):
         vx = np.ascontiguousarray(vx, np.float64)
         vz = np.ascontiguousarray(vz, np.float64)

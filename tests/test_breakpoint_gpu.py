@@ -1,0 +1,88 @@
+"""Breakpoint of the resident state (mdz_save_breakpoint / mdz_load_breakpoint,
+the counterpart of MakeBreakpointParticles / LoadBreakpointParticles): a run
+restarted from a breakpoint continues as the uninterrupted one, and a
+breakpoint of another grid or a truncated file is refused without touching
+the context."""
+import numpy as np
+import pytest
+
+import mdz
+from test_step_gpu import vep_case, _rel
+
+pytestmark = pytest.mark.gpu
+
+
+def _context(g, m, u, v, p, mat, cap):
+    ctx = mdz.Context(g, mat.n_phases, cap)
+    ctx.set_markers(m["x"], m["z"], m["phase"])
+    for attr, key in ((mdz.M_SXXD, "sxxd"), (mdz.M_SZZD, "szzd"), (mdz.M_SXZ, "sxz"), (mdz.M_STRAIN_PL, "strain_pl"),
+                      (mdz.M_STRAIN, "strain"), (mdz.M_T, "T"), (mdz.M_CMUL, "cmul")):
+        ctx.set_marker_attr(attr, m[key])
+    f = mdz.GridFields(g, mat.n_phases)
+    f["u"], f["v"], f["p"] = u, v, p
+    s = f.struct()
+    for name in mdz.FIELD_NAMES:
+        if name not in ("u", "v", "p"):
+            setattr(s, name, None)
+    ctx._check(ctx.L.mdz_sync_fields(ctx.h, mdz.C.byref(s), 1))
+    return ctx
+
+
+def _state(ctx, g, nph):
+    out = mdz.GridFields(g, nph)
+    ctx.download_fields(out)
+    x, z, ph, vx, vz = ctx.get_markers()
+    return dict(u=out["u"], v=out["v"], p=out["p"] - out["p"].mean(), x=x, z=z, phase=ph, vx=vx,
+                sxxd=ctx.get_marker_attr(mdz.M_SXXD), strain_pl=ctx.get_marker_attr(mdz.M_STRAIN_PL))
+
+
+def test_restart_continues_as_uninterrupted(tmp_path):
+    g, m, u, v, p, mat = vep_case()
+    prm = mdz.RheoParams.make(dt=0.05, iselastic=1, step=1)
+    model = mdz.Model.make(prm, newton=1, nit_max=12, rel_tol=1e-11, lin_rtol=1e-9, line_search=0, precision=64,
+                           reseed=1, min_part_cell=16, direct_neighbour=0)
+    cap = len(m["x"]) + 8 * g.ncx * g.ncz
+    path = str(tmp_path / "step1.brk")
+    a = _context(g, m, u, v, p, mat, cap)
+    a.time_step(mat, model)
+    a.save_breakpoint(path)
+    n1 = a.n_markers
+    ra = a.time_step(mat, model)
+    sa = _state(a, g, mat.n_phases)
+    a.close()
+    # a fresh context of the same grid, nothing uploaded but the breakpoint
+    b = mdz.Context(g, mat.n_phases, cap)
+    b.load_breakpoint(path)
+    assert b.n_markers == n1
+    rb = b.time_step(mat, model)
+    sb = _state(b, g, mat.n_phases)
+    b.close()
+    assert ra.converged == 1 and rb.converged == 1
+    assert ra.nonlinear_its == rb.nonlinear_its and ra.markers_added == rb.markers_added
+    assert np.array_equal(sa["phase"], sb["phase"])
+    for k in ("u", "v", "p", "x", "z", "vx", "sxxd", "strain_pl"):
+        assert _rel(sb[k], sa[k]) < 1e-12, (k, _rel(sb[k], sa[k]))
+
+
+def test_breakpoint_refused(tmp_path):
+    g, m, u, v, p, mat = vep_case()
+    path = str(tmp_path / "b.brk")
+    a = _context(g, m, u, v, p, mat, len(m["x"]))
+    a.save_breakpoint(path)
+    before = a.get_markers()
+    other = mdz.Grid(g.Nx + 2, g.Nz, g.xmin, g.xmax, g.zmin, g.zmax).set_bc_pureshear(1.0)
+    c = mdz.Context(other, mat.n_phases, len(m["x"]))
+    with pytest.raises(mdz.MdzError) as e:
+        c.load_breakpoint(path)
+    assert e.value.status == 1
+    c.close()
+    raw = open(path, "rb").read()
+    short = str(tmp_path / "short.brk")
+    open(short, "wb").write(raw[:len(raw) // 2])
+    with pytest.raises(mdz.MdzError) as e:
+        a.load_breakpoint(short)
+    assert e.value.status == 1
+    after = a.get_markers()
+    for x, y in zip(before, after):
+        assert np.array_equal(x, y)
+    a.close()
