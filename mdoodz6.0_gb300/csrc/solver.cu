@@ -1342,7 +1342,7 @@ static mdz_status alloc_gcr(mdz_ctx *ctx, gcr_space<T> &S, int m) {
     if (e == cudaSuccess) e = cudaMalloc((void **)&S.dA0, sizeof(T *) * (GCR_MAX_M + 4));
     if (e == cudaSuccess) e = cudaMalloc((void **)&S.dA1, sizeof(T *) * (GCR_MAX_M + 4));
     if (e == cudaSuccess) e = cudaMalloc((void **)&S.dA2, sizeof(T *) * (GCR_MAX_M + 4));
-    if (e == cudaSuccess) e = alloc0(&S.dots, 4 * (GCR_MAX_M + 8));
+    if (e == cudaSuccess) e = alloc0(&S.dots, 8 * (GCR_MAX_M + 8));   // see the layout in gcr_solve
     if (e != cudaSuccess) return mdz_cuda_check(ctx, e, "GCR allocation");
     // pointer tables: rows 0..m-1 = W_i, row m = w, row m+1 = r
     std::vector<const T *> a0(m + 2), a1(m + 2), a2(m + 2);
@@ -1776,8 +1776,8 @@ static mdz_status precondition(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n,
 // the first removed all but 1e-3 of w's squared norm (a DGKS-type test; with
 // the usual 1/2 the second pass ran in almost every FP32 iteration and made
 // the plain FP64 solve 7 % slower for the same iteration counts),
-// decided on the device: k_gcr_check sets sc[5] = 1 for a second pass, and
-// the second-pass kernels return at once when it is 0.
+// decided on the device: the first pass's k_gcr_dots sets sc[5] = 1 for a
+// second pass, and the second-pass kernels return at once when it is 0.
 // dots[0..k-1] = (w, W_q), dots[k] = (w, w), dots[k+1] = (w, r) of the pass
 // whose coefficients the finish applies; sc[0] = 1/||w||, sc[1] = alpha,
 // sc[2] = ||w||^2, sc[3] = running ||r||^2 (so the host reads it only every
@@ -1794,19 +1794,7 @@ __device__ void gcr_scalars(int k, const double *dots, double *sc) {
     sc[8 + k] = alpha;   // x = sum alpha_q Z_q is formed once per basis (k_gcr_xupdate)
 }
 
-__global__ void k_gcr_check(int k, const double *dots, double *sc) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double nrm2 = dots[k];
-    for (int q = 0; q < k; q++) nrm2 -= dots[q] * dots[q];
-    if (k > 0 && !(nrm2 > 1e-3 * dots[k])) { sc[5] = 1.0; return; }
-    sc[5] = 0.0;
-    gcr_scalars(k, dots, sc);
-}
 
-__global__ void k_gcr_scalars2(int k, const double *dots2, double *sc) {
-    if (threadIdx.x != 0 || blockIdx.x != 0 || sc[5] == 0.0) return;
-    gcr_scalars(k, dots2, sc);
-}
 
 // first-pass correction z -= sum beta_q Z_q, w -= sum beta_q W_q, only when
 // sc[5] asks for a second pass (grid-stride, so a skipped launch is short)
@@ -1843,7 +1831,11 @@ template <typename P, typename T>
 __global__ void k_gcr_finish(size_t n, int k, P *__restrict__ Z, P *__restrict__ W, const double *__restrict__ dots1,
                              const double *__restrict__ dots2, const double *__restrict__ sc,
                              const P *__restrict__ z, const P *__restrict__ w, T *__restrict__ r,
-                             P *__restrict__ rp) {
+                             P *__restrict__ rp, double *__restrict__ next1, double *__restrict__ next2) {
+    // the next iteration accumulates into the other parity's buffers, which
+    // no kernel of this iteration reads: clear them here instead of by memsets
+    if (blockIdx.x == 0 && next1)
+        for (int q = threadIdx.x; q < k + 3; q += blockDim.x) { next1[q] = 0.0; next2[q] = 0.0; }
     __shared__ P bsh[GCR_MAX_M];
     const double *__restrict__ beta = sc[5] != 0.0 ? dots2 : dots1;
     for (int q = threadIdx.x; q < k; q += blockDim.x) bsh[q] = (P)beta[q];
@@ -1884,28 +1876,6 @@ __global__ void k_gcr_xupdate(size_t n, int k, const P *__restrict__ Z, const do
 // out[0] += (w, w), out[1] += (w, r): products, sums and the block reduction
 // in the vectors' precision, block totals added in FP64 (as k_dots); a
 // non-null flag holding 0 makes the launch a no-op
-template <typename P>
-__global__ void __launch_bounds__(256) k_gcr_wdots(size_t n, const P *__restrict__ w, const P *__restrict__ r,
-                                                   double *out, const double *flag) {
-    if (flag && *flag == 0.0) return;
-    P a[2] = {0, 0};
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const P wi = w[i];
-        a[0] += wi * wi;
-        a[1] += wi * r[i];
-    }
-    __shared__ P sh[2][8];
-    for (int q = 0; q < 2; q++) {
-        for (int o = 16; o > 0; o >>= 1) a[q] += __shfl_xor_sync(0xffffffffu, a[q], o);
-        if ((threadIdx.x & 31) == 0) sh[q][threadIdx.x >> 5] = a[q];
-    }
-    __syncthreads();
-    if (threadIdx.x < 2) {
-        P t = 0;
-        for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += sh[threadIdx.x][q];
-        atomicAdd(out + threadIdx.x, (double)t);
-    }
-}
 
 template <typename T>
 __global__ void k_axpby(size_t n, double a, const T *__restrict__ x, double b, T *__restrict__ y) {
@@ -1979,6 +1949,85 @@ __global__ void __launch_bounds__(256) k_dots(int nq, size_t n, const T *const *
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += sh[threadIdx.x][w];
         atomicAdd(out + q0 + threadIdx.x, (double)v);
     }
+}
+
+// One Gram-Schmidt pass's sums in one launch: (w, W_q) for q < k, then
+// (w, w) and (w, r) as vectors k and k + 1 (b = w), accumulated as k_dots
+// does; the last block to finish (a device-scope counter) then runs the
+// pass's scalar step: mode 1 the check of the first pass (sc[5] = 1 asks for
+// a second pass, else the scalars), mode 2 the scalars of the second pass.
+// With flag (mode 2) every block returns at once when *flag is 0.
+template <typename T, int MDOT_Q>
+__global__ void __launch_bounds__(256) k_gcr_dots(int k, size_t n, const T *const *__restrict__ a,
+                                                  const T *__restrict__ w, const T *__restrict__ r, double *out,
+                                                  const double *flag, int mode, double *sc,
+                                                  unsigned int *counter) {
+    if (flag && *flag == 0.0) return;
+    const int nq = k + 2, q0 = blockIdx.y * MDOT_Q;
+    const T *ap[MDOT_Q];
+    T part[MDOT_Q];
+#pragma unroll
+    for (int j = 0; j < MDOT_Q; j++) {
+        const int q = q0 + j;
+        ap[j] = q < k ? a[q] : (q == k ? w : (q == k + 1 ? r : nullptr));
+        part[j] = T(0);
+    }
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const T bi = w[i];
+#pragma unroll
+        for (int j = 0; j < MDOT_Q; j++)
+            if (ap[j]) part[j] += ap[j][i] * bi;
+    }
+    __shared__ T sh[MDOT_Q][8];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < MDOT_Q; j++) {
+        T v = part[j];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[j][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < MDOT_Q && q0 + (int)threadIdx.x < nq) {
+        T v = 0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) v += sh[threadIdx.x][q];
+        atomicAdd(out + q0 + threadIdx.x, (double)v);
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int total = gridDim.x * gridDim.y;
+        last = atomicAdd(counter, 1u) == total - 1;
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    double d[GCR_MAX_M + 2];
+    const volatile double *vo = out;
+    for (int q = 0; q < nq; q++) d[q] = vo[q];
+    *counter = 0u;   // for the next launch (stream order)
+    if (mode == 1) {
+        double nrm2 = d[k];
+        for (int q = 0; q < k; q++) nrm2 -= d[q] * d[q];
+        if (k > 0 && !(nrm2 > 1e-3 * d[k])) { sc[5] = 1.0; return; }
+        sc[5] = 0.0;
+    }
+    gcr_scalars(k, d, sc);
+}
+
+template <typename T>
+static mdz_status gcr_dots_launch(mdz_ctx *ctx, gcr_space<T> &S, int k, const T *w, const T *r, double *out,
+                                  const double *flag, int mode, double *sc, unsigned int *counter, cudaStream_t st) {
+    constexpr int Q = sizeof(T) == 4 ? 8 : 1;
+    const int tiles = (k + 2 + Q - 1) / Q;
+    int bx = mdz_blocks((long long)S.n, 256 * (sizeof(T) == 4 ? 8 : 4));
+    const int cap = (sizeof(T) == 4 ? 152 * 8 : 152 * 4 + tiles - 1) / tiles;
+    if (bx > cap) bx = cap;
+    if (bx < 8) bx = 8;
+    k_gcr_dots<T, Q><<<dim3(bx, tiles), 256, 0, st>>>(k, S.n, S.dA0, w, r, out, flag, mode, sc, counter);
+    MDZ_LAUNCHED(ctx);
+    return MDZ_OK;
 }
 
 template <typename T>
@@ -2064,7 +2113,17 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
     int nb = mdz_blocks(n);
     MDZ_CUDA(ctx, cudaMemsetAsync(S.x, 0, sizeof(T) * n, st));
     // ||r0||
-    double *dots = S.dots, *sc = S.dots + (GCR_MAX_M + 4), *dots2 = S.dots + 2 * (GCR_MAX_M + 8);
+    // S.dots layout (doubles, B = GCR_MAX_M + 8): first-pass sums of even / odd
+    // iterations at 0 / 4B, the scalars sc at GCR_MAX_M + 4, second-pass sums
+    // at 2B / 5B, a scratch sum at 3B, the fused kernels' block counter at 6B
+    const int B = GCR_MAX_M + 8;
+    double *sc = S.dots + (GCR_MAX_M + 4), *dots = S.dots + 3 * B;
+    double *dots1p[2] = {S.dots, S.dots + 4 * B}, *dots2p[2] = {S.dots + 2 * B, S.dots + 5 * B};
+    unsigned int *counter = reinterpret_cast<unsigned int *>(S.dots + 6 * B);
+    for (int q = 0; q < 2; q++) {
+        MDZ_CUDA(ctx, cudaMemsetAsync(dots1p[q], 0, sizeof(double) * (GCR_MAX_M + 3), st));
+        MDZ_CUDA(ctx, cudaMemsetAsync(dots2p[q], 0, sizeof(double) * (GCR_MAX_M + 3), st));
+    }
     mdz_status s;
     cudaGraphExec_t pre = nullptr;
     long long pre_launches = 0;
@@ -2118,28 +2177,19 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
         // First pass: (w, W_q) q < k, (w, w), (w, r); the check decides on the
         // device whether a second pass runs.
         const int ng = nb < 152 * 8 ? nb : 152 * 8;
-        const int nw = mdz_blocks((long long)n, 256 * (sizeof(P) == 4 ? 8 : 4)) < 152 * 4
-                           ? mdz_blocks((long long)n, 256 * (sizeof(P) == 4 ? 8 : 4)) : 152 * 4;
-        if ((s = dots_launch<P>(ctx, SP, 0, k, SP.w, dots, st)) != MDZ_OK) return s;
-        MDZ_CUDA(ctx, cudaMemsetAsync(dots + k, 0, 2 * sizeof(double), st));
-        // (w, r) against the residual as the preconditioner saw it (SP.r: the
-        // FP32 copy in the FP32 form, r itself otherwise)
-        k_gcr_wdots<P><<<nw, 256, 0, st>>>(n, SP.w, SP.r, dots + k, nullptr);
-        MDZ_LAUNCHED(ctx);
-        k_gcr_check<<<1, 32, 0, st>>>(k, dots, sc);
-        MDZ_LAUNCHED(ctx);
+        // one launch per pass: (w, W_q), (w, w) and (w, r) against the residual
+        // as the preconditioner saw it (SP.r: the FP32 copy in the FP32 form,
+        // r itself otherwise), then the check / scalars in its last block
+        double *d1 = dots1p[it & 1], *d2 = dots2p[it & 1];
+        if ((s = gcr_dots_launch<P>(ctx, SP, k, SP.w, SP.r, d1, nullptr, 1, sc, counter, st)) != MDZ_OK) return s;
         if (k > 0) {   // second pass (each launch returns at once unless sc[5] = 1)
-            k_gcr_orth_if<P><<<ng, MDZ_THREADS, 0, st>>>(n, k, SP.Z, SP.W, dots, sc, SP.z, SP.w);
+            k_gcr_orth_if<P><<<ng, MDZ_THREADS, 0, st>>>(n, k, SP.Z, SP.W, d1, sc, SP.z, SP.w);
             MDZ_LAUNCHED(ctx);
-            if ((s = dots_launch<P>(ctx, SP, 0, k, SP.w, dots2, st, sc + 5)) != MDZ_OK) return s;
-            MDZ_CUDA(ctx, cudaMemsetAsync(dots2 + k, 0, 2 * sizeof(double), st));
-            k_gcr_wdots<P><<<nw, 256, 0, st>>>(n, SP.w, SP.r, dots2 + k, sc + 5);
-            MDZ_LAUNCHED(ctx);
-            k_gcr_scalars2<<<1, 32, 0, st>>>(k, dots2, sc);
-            MDZ_LAUNCHED(ctx);
+            if ((s = gcr_dots_launch<P>(ctx, SP, k, SP.w, SP.r, d2, sc + 5, 2, sc, counter, st)) != MDZ_OK) return s;
         }
-        k_gcr_finish<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, k, SP.Z, SP.W, dots, dots2, sc, SP.z, SP.w, S.r,
-                                                        mixed ? SP.r : (P *)nullptr);
+        k_gcr_finish<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, k, SP.Z, SP.W, d1, d2, sc, SP.z, SP.w, S.r,
+                                                        mixed ? SP.r : (P *)nullptr, dots1p[(it + 1) & 1],
+                                                        dots2p[(it + 1) & 1]);
         MDZ_LAUNCHED(ctx);
         {   // algorithmic bytes (one Gram-Schmidt pass): the dots read W_q, w
             // (k + 1 P vectors) and w, r (P); the finish reads Z_q, W_q, z, w
