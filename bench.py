@@ -134,10 +134,13 @@ def run_form(cfg_builder, precision, learned, steps, warmup, size, reseed=False)
     ctx.set_profiling(True)
     l0 = ctx.kernel_launches
     t0 = time.perf_counter()
+    marks = []
     for _ in range(steps):
-        reps.append(ctx.time_step(mat, model).as_dict())
+        reps.append(ctx.time_step(mat, model).as_dict())   # synchronous: returns when the step is done
+        marks.append(time.perf_counter())
     ctx.L.mdz_sync(ctx.h)
     wall = (time.perf_counter() - t0) * 1e3 / steps
+    step_ms = [(b - a) * 1e3 for a, b in zip([t0] + marks[:-1], marks)]
     launches = ctx.kernel_launches - l0
     gpu_ms = sum(r["ms_total"] for r in reps) / steps
     kern = ctx.kernel_timing()
@@ -149,7 +152,7 @@ def run_form(cfg_builder, precision, learned, steps, warmup, size, reseed=False)
     rs = reseed_pass(ctx, cfg) if reseed else None
     ctx.close()
     return dict(ms_wall=wall, ms_gpu=gpu_ms, reports=reps, launches=launches, kernel=kern, cfg=cfg, train=train,
-                final=final, reseed=rs)
+                final=final, reseed=rs, step_ms=step_ms)
 
 
 def reseed_pass(ctx, cfg, min_part_cell=16):
@@ -380,6 +383,10 @@ def main():
                    "l2": "inputs larger than L2 (markers %.0f MB)" % (len(fast["cfg"]["markers"]["x"]) * 84 / 1e6),
                    "parallelism": "replicas" if world > 1 else "single"},
         "forms": {"plain_fp64_ms": plain["ms_wall"], "learned_fp32_ir_ms": fast["ms_wall"],
+                  # wall time of each timed step and its device time (CUDA events inside the step)
+                  "plain_step_ms": plain["step_ms"], "learned_fp32_ir_step_ms": fast["step_ms"],
+                  "plain_step_device_ms": [r["ms_total"] for r in plain["reports"]],
+                  "learned_fp32_ir_step_device_ms": [r["ms_total"] for r in fast["reports"]],
                   "speedup_vs_plain_fp64": plain["ms_wall"] / fast["ms_wall"],
                   "plain_report": plain["reports"][-1], "learned_fp32_ir_report": fast["reports"][-1],
                   "guess_training_s": fast["train"][0], "guess_training_loss": fast["train"][1],
