@@ -2,8 +2,8 @@
 oracle/_build/libmdz_oracle.so).
 
 Test infrastructure only: imported by tests/, __graft_entry__.smoke() and the
-CPU-baseline leg of bench.py, always as the checker / reported baseline and
-never as the thing measured or shipped.
+CPU-baseline legs of bench.py, always as the reference the GPU results are
+compared with or as the reported CPU time, never as the thing measured or shipped.
 """
 import ctypes as C
 import os
