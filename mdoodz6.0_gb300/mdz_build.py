@@ -72,7 +72,7 @@ def build_cuda(verbose=False, extra_flags=()):
 
 
 def build_oracle():
-    """CPU restatement used as the checker (plain gcc; builds on x86 and Arm)."""
+    """The oracle: the CPU restatement the tests compare with (plain gcc; builds on x86 and Arm)."""
     _run(["make", "-s", "-C", ORACLE_DIR, "port"])
     return ORACLE_LIB
 

@@ -1,6 +1,6 @@
 /*
  * CPU oracle: a plain-C restatement of the MDOODZ 6.0 hot-path algorithms,
- * used ONLY as the checker in tests/, __graft_entry__.smoke() and the CPU
+ * used ONLY as the reference for comparisons in tests/, __graft_entry__.smoke() and the CPU
  * baseline leg of bench.py.  The product library never links or calls it.
  *
  * Each function cites the reference function (path:line inside the MDOODZ 6.0
