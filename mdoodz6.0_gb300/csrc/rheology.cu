@@ -231,7 +231,14 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
             Real lnB = Real(m.lnK_pwl[p]) + (Real(m.Qpwl[p]) + P * Va_pwl) * iRT * in;
             if (Real(m.mpwl[p]) != Real(0.0)) lnB += Real(m.mpwl[p]) * in * mlog(d);
             if (Real(m.apwl[p]) != Real(0.0)) lnB -= Real(m.apwl[p]) * phi * in;
-            const Real LE = mlog(Eii), LF = f_ani == Real(1.0) ? Real(0.69314718055994530942) : mlog(Real(2.0) * f_ani);   // ln 2
+            // ln(2 f_ani): f_ani = Gii / Eii is 1 up to rounding for isotropic rates,
+            // where ln 2 + x - x^2/2 + x^3/3 (x = f_ani - 1, |x| < 2^-20) is exact
+            // to rounding and spares an FP64 logarithm
+            const Real xf = f_ani - Real(1.0);
+            const Real LE = mlog(Eii),
+                       LF = mfabs(xf) < Real(9.5367431640625e-07)
+                                ? Real(0.69314718055994530942) + xf * (Real(1.0) + xf * (Real(-0.5) + xf * Real(1.0 / 3.0)))
+                                : mlog(Real(2.0) * f_ani);   // ln 2; 2^-20
             lnTE = LF + LE;   // ln(2 f_ani Eii) = ln Tii - ln eta_ve
             lnC_pwl = -n_pwl * (LF + lnB);
             C_pwl = mexp(lnC_pwl);
