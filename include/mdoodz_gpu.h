@@ -399,7 +399,7 @@ mdz_status mdz_SolveStokesDefect(mdz_ctx *ctx, mdz_fields *f, int jacobian, int 
  * number of Krylov iterations between host-side convergence checks (1..64), and
  * mg_jacobian = 1 to build the multigrid hierarchy of a Newton solve from the
  * Jacobian's velocity block instead of the Picard block.
- * Defaults 2, 1, 0.7, 30, 4, 0. */
+ * Defaults 2, 1, 0.7, 30, 1, 0. */
 mdz_status mdz_set_solver_options(mdz_ctx *ctx, int nu1, int nu2, double omega, int restart, int check,
                                   int mg_jacobian);
 

@@ -94,7 +94,8 @@ struct mdz_solver {
     bool ready = false;
     int nu1 = 2, nu2 = 1;        // fewer sweeps, a few more Krylov iterations: faster overall at 1025x513
     double omega = 0.7;
-    int check = 4;               // GCR iterations between host convergence checks
+    int check = 1;               // GCR iterations between host convergence checks (one read-back
+                                 // each: cheaper at 1025x513 than the iterations a sparser check overshoots)
     int restart = 30;            // GCR basis size
     int mg_jacobian = 0;         // 1: multigrid on the Newton Jacobian's velocity block (else Picard)
     int bottom_cs[2] = {1, 1};   // cluster size of the V-cycle bottom kernel ([0] FP64, [1] FP32)

@@ -432,7 +432,7 @@ class Context:
                                                  _dptr(du), _dptr(dv), _dptr(dp), C.byref(its), C.byref(rel)))
         return du, dv, dp, its.value, rel.value
 
-    def set_solver_options(self, nu1=2, nu2=1, omega=0.7, restart=30, check=4, mg_jacobian=0):
+    def set_solver_options(self, nu1=2, nu2=1, omega=0.7, restart=30, check=1, mg_jacobian=0):
         self._check(self.L.mdz_set_solver_options(self.h, C.c_int(nu1), C.c_int(nu2), C.c_double(omega),
                                                   C.c_int(restart), C.c_int(check), C.c_int(mg_jacobian)))
 
