@@ -168,13 +168,16 @@ __global__ void k_marker_update(int n, mdz_dgrid g, const double *__restrict__ m
                                 const double *__restrict__ dszz, const double *__restrict__ dsxz,
                                 const double *__restrict__ dstrain, const double *__restrict__ dstrain_pl,
                                 double *__restrict__ sxx, double *__restrict__ szz, double *__restrict__ sxz,
-                                double *__restrict__ strain, double *__restrict__ strain_pl) {
+                                double *__restrict__ strain, double *__restrict__ strain_pl, int what) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n || mph[k] == -1) return;
     const double x = mx[k], z = mz[k], dx = g.dx, dz = g.dz, idx = g.idx, idz = g.idz;
     const int ncx = g.ncx, ncz = g.ncz, Nx = g.Nx, Nz = g.Nz;
+    // what & 1: stress increments (UpdateParticleStress, before the advection);
+    // what & 2: strain increments (AccumulatedStrainII, after it, at the
+    // advected positions; markers that left the box are skipped)
     // centroids, ghosted frame (Interp_Grid2P_centroids2, non-periodic)
-    {
+    if (what & 1) {
         int jp = (int)ceil_quot(x - g.xvz[0], dx, idx, 0.0) - 1, ip = (int)ceil_quot(z - g.zvx[0], dz, idz, 0.0) - 1;
         int jw = jp - 1, je = jp, is = ip - 1, in_ = ip;
         if (jp <= 0) { jw = 0; je = 0; }
@@ -194,7 +197,7 @@ __global__ void k_marker_update(int n, mdz_dgrid g, const double *__restrict__ m
         szz[k] += wSW * dszz[sSW] + wSE * dszz[sSE] + wNW * dszz[sNW] + wNE * dszz[sNE];
     }
     // vertices (Interp_Grid2P)
-    {
+    if (what & 1) {
         int jp = (int)ceil_quot(x - g.xg[0], dx, idx, 0.0) - 1, ip = (int)ceil_quot(z - g.zg[0], dz, idz, 0.0) - 1;
         jp = jp < 0 ? 0 : (jp > Nx - 2 ? Nx - 2 : jp);
         ip = ip < 0 ? 0 : (ip > Nz - 2 ? Nz - 2 : ip);
@@ -210,7 +213,7 @@ __global__ void k_marker_update(int n, mdz_dgrid g, const double *__restrict__ m
         sxz[k] += v;
     }
     // strain increments on centroid lines (AccumulatedStrainII :235-350)
-    {
+    if (what & 2) {
         int jp = (int)ceil_quot(x - g.xc[0], dx, idx, 0.0) - 1, ip = (int)ceil_quot(z - g.zc[0], dz, idz, 0.0) - 1;
         jp = jp < 0 ? 0 : (jp > ncx - 2 ? ncx - 2 : jp);
         ip = ip < 0 ? 0 : (ip > ncz - 2 ? ncz - 2 : ip);
@@ -559,10 +562,18 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
             k_marker_update<<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(
                 n, g, ctx->m.x, ctx->m.z, ctx->m.phase, B.dsxx, B.dszz, B.dsxz, B.dstr, B.dstr_pl,
                 ctx->m.attr[MDZ_M_SXXD], ctx->m.attr[MDZ_M_SZZD], ctx->m.attr[MDZ_M_SXZ], ctx->m.attr[MDZ_M_STRAIN],
-                ctx->m.attr[MDZ_M_STRAIN_PL]);
+                ctx->m.attr[MDZ_M_STRAIN_PL], 1);
             MDZ_LAUNCHED(ctx);
         }
         if ((s = mdz_dev_rk4(ctx, f.u, f.v, M->rheo.dt, st)) != MDZ_OK) return s;
+        // AccumulatedStrainII after the advection (Main_DOODZ.c:1134-1140)
+        if (n > 0) {
+            k_marker_update<<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(
+                n, g, ctx->m.x, ctx->m.z, ctx->m.phase, B.dsxx, B.dszz, B.dsxz, B.dstr, B.dstr_pl,
+                ctx->m.attr[MDZ_M_SXXD], ctx->m.attr[MDZ_M_SZZD], ctx->m.attr[MDZ_M_SXZ], ctx->m.attr[MDZ_M_STRAIN],
+                ctx->m.attr[MDZ_M_STRAIN_PL], 2);
+            MDZ_LAUNCHED(ctx);
+        }
         // reseeding after the advection (Main_DOODZ.c:1233-1236)
         if (M->reseed)
             if ((s = mdz_dev_reseed(ctx, M->min_part_cell, M->direct_neighbour, f.T, f.sxxd, f.szzd, f.sxz, st,

@@ -266,11 +266,12 @@ def time_step(g, mat, model, markers, u, v, p, fields_out=None):
         markers["sxxd"] += np.where(act, o.Interp_Grid2P(dsxx, 1), 0.0)
         markers["szzd"] += np.where(act, o.Interp_Grid2P(dszz, 1), 0.0)
         markers["sxz"] += np.where(act, o.Interp_Grid2P(dsxz, 0), 0.0)
+        markers["vx"], markers["vz"] = o.RogerGuntherII(u, v, dt)
+        markers["x"], markers["z"], markers["phase"] = o.x, o.z, o.phase
+        # AccumulatedStrainII after the advection (Main_DOODZ.c:1134-1140)
         e, ep = _accumulated_strain(g, markers, dstr, dstr_pl)
         markers["strain"] += e
         markers["strain_pl"] += ep
-        markers["vx"], markers["vz"] = o.RogerGuntherII(u, v, dt)
-        markers["x"], markers["z"], markers["phase"] = o.x, o.z, o.phase
         rep["markers_added"] = 0
         if getattr(model, "reseed", 0):   # CountPartCell(RESEED = 1) after the advection
             cap = len(markers["x"]) + 4 * (g.Nx - 1) * (g.Nz - 1)
