@@ -29,6 +29,7 @@
  *   SOURCE/StokesAssemblyDecoupled.c:3834 BuildJacobianOperatorDecoupled
  *   SOURCE/RheologyParticles.c:1124  UpdateParticleStress
  *   SOURCE/ParticleRoutines.c:3543   CountPartCell (RESEED = 1: marker reseeding)
+ *   SOURCE/RheologyParticles.c:191   AccumulatedStrainII
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -275,6 +276,11 @@ int ref_strain_rates(void) { StrainRateComponents(&g_mesh, g_scale, &g_model); r
 int ref_viscosity_grid(void) { NonNewtonianViscosityGrid(&g_mesh, &g_mat, &g_model, g_nmodel, &g_scale); return 0; }
 int ref_rheo_operators(int jacobian) { RheologicalOperators(&g_mesh, &g_model, &g_scale, jacobian); return 0; }
 int ref_rhs(void) { EvaluateRHS(&g_mesh, g_model, g_scale, g_mat.rho[0]); return 0; }
+int ref_accumulated_strain(void) {
+    AccumulatedStrainII(&g_mesh, g_scale, g_model, &g_parts, g_mesh.xc_coord, g_mesh.zc_coord, g_mesh.Nx - 1,
+                        g_mesh.Nz - 1, g_mesh.BCp.type);
+    return 0;
+}
 int ref_update_particle_stress(void) { UpdateParticleStress(&g_mesh, &g_parts, &g_model, &g_mat, &g_scale); return 0; }
 
 static void free_blocks(SparseMat *A, SparseMat *B, SparseMat *C, SparseMat *D) {

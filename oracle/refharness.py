@@ -124,6 +124,10 @@ class RefMDOODZ:
         self.lib.ref_set_markers_cap(C.c_int(len(x)), C.c_int(cap), x.ctypes.data_as(_dp), z.ctypes.data_as(_dp),
                                      phase.ctypes.data_as(_ip))
 
+    def accumulated_strain(self):
+        """AccumulatedStrainII on the current markers (adds to strain, strain_pl)."""
+        self.lib.ref_accumulated_strain()
+
     def reseed(self, direct, min_part_cell):
         """CountPartCell(RESEED = 1) on one thread; returns the new marker count."""
         self.n_markers = self.lib.ref_reseed(C.c_int(direct), C.c_int(min_part_cell))

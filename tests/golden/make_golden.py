@@ -268,6 +268,30 @@ def reseed_inputs(g, seed=11):
     return m, fields
 
 
+def make_strain_fixture():
+    """AccumulatedStrainII: random non-negative strain rates on the centroids,
+    the markers of the markers fixture (some inactive) with random strains."""
+    g = _grid()
+    x, z, ph = _markers(g)
+    rng = np.random.default_rng(17)
+    nc = (NX - 1) * (NZ - 1)
+    rates = {k: np.abs(rng.normal(size=nc)) for k in ("eII_el", "eII_pl", "eII_pwl", "eII_lin", "eII_cst")}
+    strain0, strain_pl0 = rng.random(len(x)), rng.random(len(x))
+    r = RefMDOODZ(NX, NZ, XMIN, XMAX, ZMIN, ZMAX, 3)
+    r.set_bc_pureshear(1.0)
+    r.set_param("dt", 0.3)
+    r.set_markers(x, z, ph)
+    r.marker_field("strain")[:] = strain0
+    r.marker_field("strain_pl")[:] = strain_pl0
+    for k, v in rates.items():
+        r.field(k)[:] = v
+    r.accumulated_strain()
+    np.savez_compressed(os.path.join(HERE, "strain_ref.npz"), Nx=NX, Nz=NZ, box=np.array([XMIN, XMAX, ZMIN, ZMAX]),
+                        x=x, z=z, phase=ph, dt=0.3, strain0=strain0, strain_pl0=strain_pl0,
+                        strain=r.marker_field("strain").copy(), strain_pl=r.marker_field("strain_pl").copy(),
+                        **rates)
+
+
 def make_reseed_fixture():
     g = _grid()
     m, fields = reseed_inputs(g)
@@ -310,7 +334,9 @@ def make_reseed_fixture():
 
 
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["markers", "rheology", "reseed"]
+    what = sys.argv[1:] or ["markers", "rheology", "reseed", "strain"]
+    if "strain" in what:
+        make_strain_fixture()
     if "reseed" in what:
         make_reseed_fixture()
     if "markers" in what:

@@ -59,3 +59,21 @@ def test_reseed_capacity(ref):
     g, m = reseed_case(ref)
     with pytest.raises(RuntimeError):
         oracle.reseed(g, m, len(m["x"]) + 1, 16, 1)
+
+
+def test_accumulated_strain_matches_reference(golden):
+    """The oracle step's AccumulatedStrainII restatement against the
+    reference's own AccumulatedStrainII (RheologyParticles.c:191-537)."""
+    import oracle_step
+    ref = golden("strain_ref.npz")
+    xmin, xmax, zmin, zmax = ref["box"]
+    g = mdz.Grid(int(ref["Nx"]), int(ref["Nz"]), xmin, xmax, zmin, zmax).set_bc_pureshear(1.0)
+    dt = float(ref["dt"])
+    dstr = dt * (ref["eII_pl"] + ref["eII_pwl"] + ref["eII_lin"] + ref["eII_el"] + ref["eII_cst"])
+    dstr_pl = dt * ref["eII_pl"]
+    m = dict(x=ref["x"], z=ref["z"], phase=ref["phase"])
+    e, ep = oracle_step._accumulated_strain(g, m, dstr, dstr_pl)
+    for got, key, base in ((e, "strain", "strain0"), (ep, "strain_pl", "strain_pl0")):
+        want = ref[key] - ref[base]
+        assert np.allclose(got, want, rtol=1e-13, atol=1e-15), (key, np.abs(got - want).max())
+    assert (e[ref["phase"] == -1] == 0).all() and (e > 0).any()
