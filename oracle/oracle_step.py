@@ -256,16 +256,9 @@ def time_step(g, mat, model, markers, u, v, p, fields_out=None):
     p = f["p_corr"].copy()
     if model.advect:
         dt = prm.dt
-        act_n = (g.BCp != 30) & (g.BCp != 31)
-        dsxx = np.where(act_n, f["sxxd"] - f["sxxd0"], 0.0)
-        dszz = np.where(act_n, f["szzd"] - f["szzd0"], 0.0)
-        dsxz = np.where(g.BCg != 30, f["sxz"] - f["sxz0"], 0.0)
+        update_particle_stress(g, o, f, markers)
         dstr = dt * (f["eII_pl"] + f["eII_pwl"] + f["eII_lin"] + f["eII_el"] + f["eII_cst"])
         dstr_pl = dt * f["eII_pl"]
-        act = markers["phase"] != -1
-        markers["sxxd"] += np.where(act, o.Interp_Grid2P(dsxx, 1), 0.0)
-        markers["szzd"] += np.where(act, o.Interp_Grid2P(dszz, 1), 0.0)
-        markers["sxz"] += np.where(act, o.Interp_Grid2P(dsxz, 0), 0.0)
         markers["vx"], markers["vz"] = o.RogerGuntherII(u, v, dt)
         markers["x"], markers["z"], markers["phase"] = o.x, o.z, o.phase
         # AccumulatedStrainII after the advection (Main_DOODZ.c:1134-1140)
@@ -311,6 +304,22 @@ def _trial(g, u0, v0, p0, dx, a):
     p = np.where(g.BCp == -1, p0 + a * dx[nu + nv:], p0)
     _mirror(g, u, v)
     return u, v, p
+
+
+def update_particle_stress(g, o, f, markers):
+    """UpdateParticleStress without rotation and subgrid diffusion
+    (SOURCE/RheologyParticles.c:1124-1447): the grid stress increments
+    (centroids sxxd - sxxd0, szzd - szzd0; vertices sxz - sxz0) interpolated to
+    the active markers (Interp_Grid2P_centroids2 / Interp_Grid2P) and added.
+    o: an Oracle holding the markers' positions and phases."""
+    act_n = (g.BCp != 30) & (g.BCp != 31)
+    dsxx = np.where(act_n, f["sxxd"] - f["sxxd0"], 0.0)
+    dszz = np.where(act_n, f["szzd"] - f["szzd0"], 0.0)
+    dsxz = np.where(g.BCg != 30, f["sxz"] - f["sxz0"], 0.0)
+    act = markers["phase"] != -1
+    markers["sxxd"] += np.where(act, o.Interp_Grid2P(dsxx, 1), 0.0)
+    markers["szzd"] += np.where(act, o.Interp_Grid2P(dszz, 1), 0.0)
+    markers["sxz"] += np.where(act, o.Interp_Grid2P(dsxz, 0), 0.0)
 
 
 def _accumulated_strain(g, m, dstr, dstr_pl):

@@ -292,6 +292,32 @@ def make_strain_fixture():
                         **rates)
 
 
+def make_stress_fixture():
+    """UpdateParticleStress (StressUpdate 0, no rotation, no subgrid
+    diffusion): random grid stresses before and after, markers with random
+    stresses, zero velocity."""
+    g = _grid()
+    x, z, ph = _markers(g)
+    rng = np.random.default_rng(23)
+    nc, nv = (NX - 1) * (NZ - 1), NX * NZ
+    flds = dict(sxxd=rng.normal(size=nc), szzd=rng.normal(size=nc), sxxd0=rng.normal(size=nc),
+                szzd0=rng.normal(size=nc), sxz=rng.normal(size=nv), sxz0=rng.normal(size=nv))
+    m0 = {k: rng.normal(size=len(x)) for k in ("sxxd", "szzd", "sxz")}
+    r = RefMDOODZ(NX, NZ, XMIN, XMAX, ZMIN, ZMAX, 3)
+    r.set_bc_pureshear(1.0)
+    for name, v in (("dt", 0.3), ("StressUpdate", 0), ("StressRotation", 0), ("subgrid_diff", 0)):
+        r.set_param(name, v)
+    r.set_markers(x, z, ph)
+    for k, v in m0.items():
+        r.marker_field(k)[:] = v
+    for k, v in flds.items():
+        r.field(k)[:] = v
+    r.update_particle_stress()
+    np.savez_compressed(os.path.join(HERE, "stress_ref.npz"), Nx=NX, Nz=NZ, box=np.array([XMIN, XMAX, ZMIN, ZMAX]),
+                        x=x, z=z, phase=ph, **flds, **{"m0_" + k: v for k, v in m0.items()},
+                        **{"m_" + k: r.marker_field(k).copy() for k in m0})
+
+
 def make_reseed_fixture():
     g = _grid()
     m, fields = reseed_inputs(g)
@@ -334,7 +360,9 @@ def make_reseed_fixture():
 
 
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["markers", "rheology", "reseed", "strain"]
+    what = sys.argv[1:] or ["markers", "rheology", "reseed", "strain", "stress"]
+    if "stress" in what:
+        make_stress_fixture()
     if "strain" in what:
         make_strain_fixture()
     if "reseed" in what:

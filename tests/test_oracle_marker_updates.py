@@ -1,7 +1,8 @@
-"""Pin the CPU oracle's marker reseeding (CountPartCell with RESEED = 1, one
-thread: quarter-cell counts, AddPartCell2, FindClosestPhase2, slot reuse,
-AssignMarkerProperties) against golden vectors produced by the reference's
-own compiled CountPartCell (tests/golden/make_golden.py)."""
+"""Pin the CPU oracle's marker updates against golden vectors produced by the
+reference's own compiled functions (tests/golden/make_golden.py): the
+reseeding (CountPartCell with RESEED = 1 on one thread: quarter-cell counts,
+AddPartCell2, FindClosestPhase2, slot reuse, AssignMarkerProperties),
+UpdateParticleStress and AccumulatedStrainII."""
 import numpy as np
 import pytest
 
@@ -77,3 +78,22 @@ def test_accumulated_strain_matches_reference(golden):
         want = ref[key] - ref[base]
         assert np.allclose(got, want, rtol=1e-13, atol=1e-15), (key, np.abs(got - want).max())
     assert (e[ref["phase"] == -1] == 0).all() and (e > 0).any()
+
+
+def test_update_particle_stress_matches_reference(golden):
+    """The oracle step's UpdateParticleStress (no rotation, no subgrid
+    diffusion) against the reference's own (RheologyParticles.c:1124-1447)."""
+    import oracle_step
+    from oracle import Oracle
+    ref = golden("stress_ref.npz")
+    xmin, xmax, zmin, zmax = ref["box"]
+    g = mdz.Grid(int(ref["Nx"]), int(ref["Nz"]), xmin, xmax, zmin, zmax).set_bc_pureshear(1.0)
+    o = Oracle(g, 3)
+    o.set_markers(ref["x"], ref["z"], ref["phase"])
+    f = {k: ref[k] for k in ("sxxd", "szzd", "sxxd0", "szzd0", "sxz", "sxz0")}
+    m = {"phase": ref["phase"], **{k: np.array(ref["m0_" + k]) for k in ("sxxd", "szzd", "sxz")}}
+    oracle_step.update_particle_stress(g, o, f, m)
+    for k in ("sxxd", "szzd", "sxz"):
+        want = ref["m_" + k]
+        assert np.allclose(m[k], want, rtol=1e-13, atol=1e-14), (k, np.abs(m[k] - want).max())
+        assert not np.array_equal(want, ref["m0_" + k])
