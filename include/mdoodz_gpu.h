@@ -173,7 +173,8 @@ mdz_status mdz_count_markers(mdz_ctx *ctx, int *nb_part_cell, int *nb_part_vert,
  * reference exits), MDZ_ERR_STATE if a deficient quarter cell has no marker
  * within two quarter cells (the reference exits with code 333); the markers
  * are unchanged then.  Free surface, sedimentation and periodic x are not
- * implemented (the context rejects them). */
+ * implemented (the context rejects them); MDZ_ERR_UNSUPPORTED for grids whose
+ * (2 (Nx - 1) + 4)(2 (Nz - 1) + 4) quarter cells exceed 2^31. */
 mdz_status mdz_CountPartCell(mdz_ctx *ctx, int reseed, int min_part_cell, int direct_neighbour, const double *T_n,
                              const double *sxxd_n, const double *szzd_n, const double *sxz_s, int *n_added);
 

@@ -323,6 +323,9 @@ mdz_status mdz_dev_reseed(mdz_ctx *ctx, int min_part_cell, int direct, const dou
     if (!direct && (!T_n || !sxxd_n || !szzd_n || !sxz_s))
         return mdz_fail(ctx, MDZ_ERR_ARG, "CountPartCell: DirectNeighbour = 0 needs T, sxxd, szzd and sxz");
     const quarter_geom q = make_quarter_geom(ctx);
+    // quarter-cell indices are 32-bit: (2 Ncx + 4)(2 Ncz + 4) must stay below 2^31
+    if ((long long)q.nxl * q.nzl > 2147483000LL)
+        return mdz_fail(ctx, MDZ_ERR_UNSUPPORTED, "CountPartCell: %d x %d quarter cells exceed 2^31", q.nxl, q.nzl);
     mdz_reseed_ws *W = nullptr;
     mdz_status s = reseed_ws(ctx, q, W);
     if (s != MDZ_OK) return s;
