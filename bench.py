@@ -92,9 +92,6 @@ def peaks():
         return 6800.0, 1900.0, "fallback"
 
 
-# ranges of the learned guess's training tuples for the lithosphere model:
-# log10 strain rate [1/s], T [K], P [Pa], log10 dt [s]
-LO_LITHO, HI_LITHO = [-18.0, 273.0, 0.0, 9.0], [-12.0, 1800.0, 15e9, 12.0]
 # the local-rheology MLP workload: 2^24 tuples over these ranges, batch 65536
 LO_MLP, HI_MLP = [-18.0, 273.0, 0.0, 9.0], [-12.0, 1600.0, 5e9, 12.0]
 
@@ -107,13 +104,12 @@ GUESS_STEPS = [3000]
 TRAFFIC_PER_LAUNCH = {"mg_vcycle": 88.5e6}
 
 
-def train_guess(ctx, cfg, n=1 << 20, batch=65536, seed=1):
-    """Tuples labelled by the plain local solve of the model's materials, then
-    Adam on the device; returns (seconds, final loss)."""
+def train_guess(ctx, cfg):
+    """The learned start of the model (mdz_setups.train_guess); returns
+    (seconds, final loss)."""
+    import mdz_setups
     t0 = time.perf_counter()
-    ctx.mlp_init(seed)
-    ctx.mlp_generate(cfg["mat"], cfg["model"].rheo, n, seed, LO_LITHO, HI_LITHO)
-    loss = ctx.mlp_train(GUESS_STEPS[0], batch, 2e-3)
+    loss = mdz_setups.train_guess(ctx, cfg, steps=GUESS_STEPS[0])
     return time.perf_counter() - t0, loss
 
 
@@ -123,8 +119,7 @@ def run_form(cfg_builder, precision, learned, steps, warmup, size, reseed=False)
     import mdz_setups
     cfg = cfg_builder(precision, learned, size)
     g = cfg["grid"]
-    # room for one reseeding pass (one marker per quarter cell at most)
-    ctx = mdz_setups.load_context(cfg, max_markers=len(cfg["markers"]["x"]) + 4 * g.ncx * g.ncz)
+    ctx = mdz_setups.load_context(cfg, max_markers=marker_capacity(cfg))
     model, mat = cfg["model"], cfg["mat"]
     train = train_guess(ctx, cfg) if learned else None
     reps = []
@@ -149,20 +144,28 @@ def run_form(cfg_builder, precision, learned, steps, warmup, size, reseed=False)
     ctx._check(ctx.L.mdz_get_velocity(ctx.h, mdz._dptr(final["u"]), mdz._dptr(final["v"]), mdz._dptr(final["p"])))
     final["sxxd"] = ctx.get_marker_attr(mdz.M_SXXD)
     final["sxz"] = ctx.get_marker_attr(mdz.M_SXZ)
-    rs = reseed_pass(ctx, cfg) if reseed else None
+    n_final = ctx.n_markers
     ctx.close()
+    rs = reseed_pass(cfg) if reseed else None
     return dict(ms_wall=wall, ms_gpu=gpu_ms, reports=reps, launches=launches, kernel=kern, cfg=cfg, train=train,
-                final=final, reseed=rs, step_ms=step_ms)
+                final=final, reseed=rs, step_ms=step_ms, n_markers_final=n_final)
 
 
-def reseed_pass(ctx, cfg, min_part_cell=16):
+def marker_capacity(cfg):
+    import mdz_setups
+    return mdz_setups.marker_capacity(cfg)
+
+
+def reseed_pass(cfg, min_part_cell=16):
     """One reseeding pass (CountPartCell with RESEED = 1, DirectNeighbour = 1)
-    of the resident markers after the timed steps, through the C ABI: wall
-    time of the synchronous call (a pass with min_part_cell = 0, which adds
-    nothing, sets up its workspace first).  The CPU side is the oracle's
-    one-thread restatement on the same markers."""
+    of the configuration's seeded markers, through the C ABI: wall time of the
+    synchronous call (a pass with min_part_cell = 0, which adds nothing, sets
+    up its workspace first).  The CPU side is the oracle's one-thread
+    restatement on the same markers."""
     import mdz
+    import mdz_setups
     import oracle
+    ctx = mdz_setups.load_context(cfg, max_markers=marker_capacity(cfg))
     x, z, ph, vx, vz = ctx.get_markers()
     m = dict(x=x, z=z, phase=ph, vx=vx, vz=vz)
     for k, a in zip(oracle.MARKER_ATTRS, range(mdz.M_NATTR)):
@@ -173,9 +176,10 @@ def reseed_pass(ctx, cfg, min_part_cell=16):
     t0 = time.perf_counter()
     added = ctx.CountPartCell(1, min_part_cell, 1)
     ms = (time.perf_counter() - t0) * 1e3
+    ctx.close()
     g = cfg["grid"]
     t0 = time.perf_counter()
-    _, added_cpu = oracle.reseed(g, m, n + 4 * g.ncx * g.ncz, min_part_cell, 1)
+    _, added_cpu = oracle.reseed(g, m, marker_capacity(cfg), min_part_cell, 1)
     ms_cpu = (time.perf_counter() - t0) * 1e3
     # algorithmic bytes: marker x, z, phase read twice (bins, candidates), one
     # int bin index written and read, quarter-cell counts, and the new markers
@@ -227,14 +231,17 @@ def e2e_form(cfg_builder, precision, learned, steps, size, warmup):
     (positions, phases, the seven attributes), runs the step and downloads the
     advected markers, their velocities, the updated attributes and the grid
     velocity into the same host arrays, which the next step uploads again.
-    The host arrays are page-locked once with host_register (as a caller
-    would register its marker arrays), so the copies are DMA transfers."""
+    The host arrays hold the run's marker capacity (reseeding changes the
+    count from step to step) and are page-locked once with host_register (as
+    a caller would register its marker arrays), so the copies are DMA
+    transfers."""
     import numpy as np
     import mdz
     import mdz_setups
     cfg = cfg_builder(precision, learned, size)
     m = cfg["markers"]
-    ctx = mdz_setups.load_context(cfg)
+    cap = marker_capacity(cfg)
+    ctx = mdz_setups.load_context(cfg, max_markers=cap)
     model, mat = cfg["model"], cfg["mat"]
     if learned:
         train_guess(ctx, cfg)
@@ -242,27 +249,30 @@ def e2e_form(cfg_builder, precision, learned, steps, size, warmup):
     n = len(m["x"])
     attrs = ((mdz.M_SXXD, "sxxd"), (mdz.M_SZZD, "szzd"), (mdz.M_SXZ, "sxz"), (mdz.M_STRAIN_PL, "strain_pl"),
              (mdz.M_STRAIN, "strain"), (mdz.M_T, "T"), (mdz.M_CMUL, "cmul"))
-    hin = {"x": np.array(m["x"], np.float64), "z": np.array(m["z"], np.float64),
-           "phase": np.array(m["phase"], np.int32)}   # copies: the caller's own host arrays
+    hin = {"x": np.zeros(cap), "z": np.zeros(cap), "phase": np.full(cap, -1, np.int32)}   # the caller's arrays
     for _, key in attrs:
-        hin[key] = np.array(m[key], np.float64)
-    hvx, hvz = np.empty(n), np.empty(n)
+        hin[key] = np.zeros(cap)
+    for key in hin:
+        hin[key][:n] = m[key]
+    hvx, hvz = np.zeros(cap), np.zeros(cap)
     hout = [hin["x"], hin["z"], hin["phase"], hvx, hvz]
     hu = np.empty(g.size(-1))
     pinned = list(hin.values()) + [hvx, hvz, hu]
     for a in pinned:
         mdz.host_register(a)
     times, parts, reps = [], [0.0, 0.0, 0.0, 0.0], []
+    h2d = d2h = 0
     for step in range(warmup + steps):   # the same steps as the device-resident form; the last `steps` timed
         t0 = time.perf_counter()
-        ctx.set_markers(hin["x"], hin["z"], hin["phase"])
+        ctx.set_markers(hin["x"][:n], hin["z"][:n], hin["phase"][:n])
         for attr, key in attrs:
-            ctx.set_marker_attr(attr, hin[key])
+            ctx.set_marker_attr(attr, hin[key][:n])
         t1 = time.perf_counter()
         rep = ctx.time_step(mat, model)
         t2 = time.perf_counter()
+        n_in, n = n, ctx.n_markers
         reps.append({k: rep.as_dict()[k] for k in ("nonlinear_its", "linear_its", "ms_solve", "ms_rheology",
-                                                    "ms_total")})
+                                                    "ms_total", "markers_added")})
         ctx.get_markers(out=hout)
         for attr, key in attrs:
             ctx.get_marker_attr(attr, out=hin[key])
@@ -272,16 +282,17 @@ def e2e_form(cfg_builder, precision, learned, steps, size, warmup):
             reps.pop()
             continue
         times.append((t3 - t0) * 1e3)
+        h2d += (n_in * (8 * 2 + 4) + n_in * 8 * len(attrs)) / steps
+        d2h += (n * (8 * 4 + 4) + n * 8 * len(attrs) + g.size(-1) * 8) / steps
         for q, v in enumerate(((t1 - t0) * 1e3, (t2 - t1) * 1e3, (t3 - t2) * 1e3, rep.ms_total)):
             parts[q] += v / steps
     for a in pinned:
         mdz.host_unregister(a)
-    h2d = n * (8 * 2 + 4) + n * 8 * len(attrs)
-    d2h = n * (8 * 4 + 4) + n * 8 * len(attrs) + g.size(-1) * 8
     ctx.close()
     split = dict(zip(("upload_ms", "step_ms", "download_ms", "step_device_ms"), parts))
     split["reports"] = reps
-    return sum(times) / len(times), h2d, d2h, split
+    split["markers_final"] = n
+    return sum(times) / len(times), int(h2d), int(d2h), split
 
 
 def builder(size):

@@ -165,6 +165,7 @@ struct p2g_fields {
     int per_phase[MDZ_P2G_MAX_FIELDS];       // 1: val is indexed by phase (flag 0)
     int avg[MDZ_P2G_MAX_FIELDS];
     double *out[MDZ_P2G_MAX_FIELDS];
+    int *empty;   // when set, counts active nodes that received no marker weight (phase fractions only)
 };
 
 // Candidate cell range along one direction for node i of a node set whose
@@ -228,7 +229,9 @@ __global__ void __launch_bounds__(128) k_p2g_gather(
             }
         }
     }
-    bool skip = fabs(Wm) < 1e-30 || tag[node] == 30 || tag[node] == 31;
+    const bool air = tag[node] == 30 || tag[node] == 31;
+    bool skip = fabs(Wm) < 1e-30 || air;
+    if (F.empty && phase_perc && !air && fabs(Wm) < 1e-30) atomicAdd(F.empty, 1);
 #pragma unroll
     for (int f = 0; f < NF; f++) {
         if (skip) continue;
@@ -282,8 +285,10 @@ static mdz_status p2g_core(mdz_ctx *ctx, const p2g_fields &F, int nf, double *d_
     int nn = ns.nx * ns.nz;
     dim3 bl(128), gr(mdz_blocks(nn, 128));
     int nph = d_phase_perc ? ctx->n_phases : 0;
+    p2g_fields Fc = F;
+    Fc.empty = d_phase_perc ? ctx->p2g_empty : nullptr;
     switch (nf) {
-#define CASE(N) case N: launch_p2g_nf<N>(nph, gr, bl, st, ns.nx, ns.nz, ns.X, ns.Z, ns.tag, kx, kz, h, g.dx, g.dz, dxi, dzi, g.ncx, g.ncz, ctx, F, d_phase_perc); break;
+#define CASE(N) case N: launch_p2g_nf<N>(nph, gr, bl, st, ns.nx, ns.nz, ns.X, ns.Z, ns.tag, kx, kz, h, g.dx, g.dz, dxi, dzi, g.ncx, g.ncz, ctx, Fc, d_phase_perc); break;
         CASE(0) CASE(1) CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8)
 #undef CASE
     }

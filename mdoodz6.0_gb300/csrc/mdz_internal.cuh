@@ -74,6 +74,9 @@ struct mdz_ctx {
     mdz_fields d{};              // device mirrors of every grid field (allocated on first use)
     bool fields_ready = false;
     int *d_counters = nullptr;   // small device scratch: failure counters etc.
+    // set by the time step around its projections: phase-fraction projections
+    // count there the active nodes that received no marker weight
+    int *p2g_empty = nullptr;
     bool bcs_checked = false, bcs_ok = false;
     // optional per-launch event timing of the main kernel classes (bench roofline)
     bool profiling = false;

@@ -361,6 +361,13 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
     cudaEventCreate(&t1);
     cudaEventRecord(t0, st);
     // ---- 1. projections ------------------------------------------------------
+    // Active nodes that receive no marker weight (cells emptied by the flow when
+    // reseeding is off) would get zero phase fractions, a zero viscosity and a
+    // NaN later in the Krylov solve; the phase-fraction projections count them
+    // and the step refuses such a state here.
+    int *d_empty = ctx->d_counters + 3;
+    MDZ_CUDA(ctx, cudaMemsetAsync(d_empty, 0, sizeof(int), st));
+    ctx->p2g_empty = d_empty;
     {
         step_timer T(st, &R.ms_projection);
         const double *cv[5] = {ctx->m.attr[MDZ_M_SXXD], ctx->m.attr[MDZ_M_SZZD], ctx->m.attr[MDZ_M_T],
@@ -388,6 +395,16 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
         MDZ_LAUNCHED(ctx);
         k_mirror_ghosts<<<mdz_blocks(g.Nx > g.Nz ? g.Nx : g.Nz), MDZ_THREADS, 0, st>>>(g, f.u, f.v);
         MDZ_LAUNCHED(ctx);
+    }
+    ctx->p2g_empty = nullptr;
+    {
+        int empty = 0;
+        MDZ_CUDA(ctx, cudaMemcpyAsync(&empty, d_empty, sizeof(int), cudaMemcpyDeviceToHost, st));
+        MDZ_CUDA(ctx, cudaStreamSynchronize(st));
+        if (empty > 0)
+            return mdz_fail(ctx, MDZ_ERR_STATE,
+                            "time step: %d active centroids/vertices received no marker weight (emptied cells: "
+                            "enable reseeding, mdz_model.reseed = 1)", empty);
     }
     // ---- 2. non-linear iterations -----------------------------------------------
     double r0[3] = {0, 0, 0}, r[3] = {0, 0, 0};
@@ -615,6 +632,7 @@ extern "C" mdz_status mdz_time_step(mdz_ctx *ctx, const mdz_materials *mat, cons
     if ((s = mdz_solver_ensure(ctx)) != MDZ_OK) return s;
     if ((s = mdz_ensure_bins(ctx, ctx->stream)) != MDZ_OK) return s;
     s = mdz_dev_time_step(ctx, mat, model, rep, ctx->stream);
+    ctx->p2g_empty = nullptr;
     ctx->bins.valid = false;
     return s;
 }

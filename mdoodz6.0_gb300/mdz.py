@@ -383,10 +383,11 @@ class Context:
         self._check(self.L.mdz_set_marker_attr(self.h, C.c_int(attr), C.c_int(len(v)), _dptr(v)))
 
     def get_marker_attr(self, attr, out=None):
-        v = np.zeros(self.n_markers) if out is None else out
-        if v.dtype != np.float64 or v.size < self.n_markers or not v.flags.c_contiguous:
+        n = self.n_markers
+        v = np.zeros(n) if out is None else out
+        if v.dtype != np.float64 or v.size < n or not v.flags.c_contiguous:
             raise MdzError(1, "get_marker_attr: out must be a contiguous float64 array of the marker count")
-        self._check(self.L.mdz_get_marker_attr(self.h, C.c_int(attr), C.c_int(len(v)), _dptr(v)))
+        self._check(self.L.mdz_get_marker_attr(self.h, C.c_int(attr), C.c_int(n), _dptr(v)))
         return v
 
     def upload_fields(self, fields):

@@ -100,7 +100,8 @@ def config_vep(N=401, nm=4, seed=12345, noise=0.01):
                    eta_vp=0.05, n_vp=1.0, gs_ref=1.0, pls_start=0.0, pls_end=1.0)]
     mat = mdz.Materials.from_phases(phases)
     prm = mdz.RheoParams.make(dt=1e-2, iselastic=1, step=1, eta_avg=0)
-    model = mdz.Model.make(prm, newton=1, nit_max=10, rel_tol=1e-8, lin_rtol=1e-6, line_search=1)
+    model = mdz.Model.make(prm, newton=1, nit_max=10, rel_tol=1e-8, lin_rtol=1e-6, line_search=1,
+                           reseed=1, min_part_cell=16, direct_neighbour=0)
     u, v = pure_shear_velocity(g, 1.0)
     m = _markers_dict(x, z, ph, cmul=1.0 + noise * rng.standard_normal(len(x)))
     return dict(name="vep", grid=g, markers=m, mat=mat, model=model, u=u, v=v, p=np.zeros(g.size(1)))
@@ -157,11 +158,16 @@ def config_lithosphere(Nx=1025, Nz=513, nm=4, seed=12345, precision=64, learned=
     # solve asks only for the reduction the non-linear iteration can use; the
     # FP32 form also evaluates the local rheology of the first two non-linear
     # iterations in FP32; once the residual is below 1e-2 of its first value
-    # the multigrid hierarchy of the previous solve is kept)
+    # the multigrid hierarchy of the previous solve is kept; markers are
+    # reseeded after every advection, CountPartCell with RESEED = 1 and the
+    # reference's defaults Reseed = 1, min_part_cell = 16, DirectNeighbour = 0:
+    # the extension's inflow through the bottom wall empties the lowest cells
+    # of markers within a few tens of steps otherwise)
     model = mdz.Model.make(prm, gz=-9.81 * L / S, newton=1, nit_max=30, rel_tol=1e-8, lin_rtol=1e-5,
                            line_search=0, precision=precision, learned_guess=learned, picard2newton=1,
                            pic2newt_cond=1e-1, nit_pic_max=10, newton_maxit=200, adaptive_lin_tol=1,
-                           fp32_rheology_its=2 if precision == 32 else 0, mg_reuse_below=1e-2)
+                           fp32_rheology_its=2 if precision == 32 else 0, mg_reuse_below=1e-2,
+                           reseed=1, min_part_cell=16, direct_neighbour=0)
     u, v = pure_shear_velocity(g, eps / sc.E)
     m = _markers_dict(x, z, ph, T=T)
     # initial pressure: lithostatic column of the layered densities (the
@@ -192,11 +198,39 @@ def config_shear_band(N=2049, nm=4, seed=12345, noise=0.01, precision=64, learne
     return cfg
 
 
+# ranges of the learned guess's training tuples for the lithosphere model:
+# log10 strain rate [1/s], T [K], P [Pa], log10 dt [s]
+LO_LITHO, HI_LITHO = [-18.0, 273.0, 0.0, 9.0], [-12.0, 1800.0, 15e9, 12.0]
+
+
+def train_guess(ctx, cfg, steps=3000, n=1 << 20, batch=65536, seed=1, lo=LO_LITHO, hi=HI_LITHO):
+    """The learned local-rheology start of a configuration: n tuples drawn
+    over [lo, hi] and labelled by the plain local solve of the model's
+    materials on the device, then `steps` Adam steps; returns the final loss."""
+    ctx.mlp_init(seed)
+    ctx.mlp_generate(cfg["mat"], cfg["model"].rheo, n, seed, lo, hi)
+    return ctx.mlp_train(steps, batch, 2e-3)
+
+
+def marker_capacity(cfg):
+    """Marker slots of a run: twice the seeded markers.  Reseeding adds one
+    marker to every quarter cell that holds fewer than min_part_cell / 4 and
+    never removes any, so a quarter cell that a marker leaves gets a new one
+    while the cell the marker entered keeps it: the count creeps up over the
+    steps (by about a quarter over the first 25 steps of the 1025 x 513
+    lithosphere model) before the quarter cells hold enough spare markers.
+    Markers that leave the box free their slots for the next pass."""
+    g = cfg["grid"]
+    n = len(cfg["markers"]["x"])
+    return 2 * n + 4 * g.ncx * g.ncz
+
+
 def load_context(cfg, max_markers=None):
-    """Context with the configuration's markers, attributes and initial fields resident."""
+    """Context with the configuration's markers, attributes and initial fields
+    resident; room for max_markers markers (default: marker_capacity)."""
     import mdz
     g, m = cfg["grid"], cfg["markers"]
-    ctx = mdz.Context(g, cfg["mat"].n_phases, max_markers or len(m["x"]))
+    ctx = mdz.Context(g, cfg["mat"].n_phases, max_markers or marker_capacity(cfg))
     ctx.set_markers(m["x"], m["z"], m["phase"])
     for attr, key in ((mdz.M_SXXD, "sxxd"), (mdz.M_SZZD, "szzd"), (mdz.M_SXZ, "sxz"), (mdz.M_STRAIN_PL, "strain_pl"),
                       (mdz.M_STRAIN, "strain"), (mdz.M_T, "T"), (mdz.M_CMUL, "cmul")):
