@@ -103,6 +103,8 @@ extern "C" mdz_status mdz_create(mdz_ctx **out, const mdz_grid_desc *d, int n_ph
     UP(ctx->bins.count, (const int *)nullptr, ncells + 1); UP(ctx->bins.start, (const int *)nullptr, ncells + 1);
     UP(ctx->bins.cursor, (const int *)nullptr, ncells + 1);
     UP(ctx->bins.scan_partials, (const int *)nullptr, (ncells + 1) / 1024 + 2);
+    UP(ctx->red_part, (const double *)nullptr, MDZ_RED_PART);
+    UP(ctx->red_cnt, (const unsigned int *)nullptr, MDZ_RED_COUNTERS);
 #undef UP
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
@@ -126,7 +128,8 @@ extern "C" void mdz_destroy(mdz_ctx *ctx) {
     mdz_dgrid &g = ctx->g;
     void *ptrs[] = {g.xg, g.zg, g.xc, g.zc, g.xvz, g.zvx, g.BCu, g.BCv, g.BCp, g.BCg, g.BCu_val, g.BCv_val,
                     ctx->m.x, ctx->m.z, ctx->m.vx, ctx->m.vz, ctx->m.phase, ctx->bins.cell, ctx->bins.sorted,
-                    ctx->bins.count, ctx->bins.start, ctx->bins.cursor, ctx->bins.scan_partials};
+                    ctx->bins.count, ctx->bins.start, ctx->bins.cursor, ctx->bins.scan_partials,
+                    ctx->red_part, ctx->red_cnt};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int a = 0; a < MDZ_M_NATTR; a++)

@@ -5,6 +5,7 @@
 #include <string>
 #include <vector>
 #include "mdoodz_gpu.h"
+#include "reduce.cuh"
 
 // kernel classes timed when profiling is on
 enum { MDZ_PROF_VISCOSITY = 0, MDZ_PROF_STOKES_APPLY = 1, MDZ_PROF_MG_SMOOTH = 2, MDZ_PROF_P2G = 3, MDZ_PROF_MLP = 4,
@@ -77,6 +78,10 @@ struct mdz_ctx {
     // set by the time step around its projections: phase-fraction projections
     // count there the active nodes that received no marker weight
     int *p2g_empty = nullptr;
+    // deterministic reductions (reduce.cuh): per-block partial slots and the
+    // arrival counters of the last-block sums
+    double *red_part = nullptr;
+    unsigned int *red_cnt = nullptr;
     bool bcs_checked = false, bcs_ok = false;
     // optional per-launch event timing of the main kernel classes (bench roofline)
     bool profiling = false;

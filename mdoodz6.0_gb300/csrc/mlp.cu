@@ -15,7 +15,7 @@
 
 static size_t train_smem_bytes() {
     return MLP_PACK_BYTES + (size_t)(16 + 64 * 4 + 16) * MLP_RS * 2 + 4 * 32 * MLP_S1 * 2 + MLP_TILE * 2 * 4 +
-           136 * 4;
+           4 * 136 * 4;
 }
 static size_t infer_smem_bytes() { return MLP_PACK_BYTES + 8 * 32 * MLP_S1 * 2 + 8 * 64 * 4; }
 
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(128) k_mlp_train(const unsigned char *__restri
     mlp_load_weights(sm, packed);
     for (int i = threadIdx.x; i < 16 * MLP_RS; i += blockDim.x) { XT[i] = __float2bfloat16_rn(0.f); DYT[i] = XT[i]; }
     for (int i = threadIdx.x; i < 4 * 32 * MLP_S1; i += blockDim.x) XR[i] = __float2bfloat16_rn(0.f);
-    for (int i = threadIdx.x; i < 136; i += blockDim.x) BACC[i] = 0.f;
+    for (int i = threadIdx.x; i < 4 * 136; i += blockDim.x) BACC[i] = 0.f;
     __syncthreads();
     const mlp_w W = mlp_views(sm);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
@@ -191,7 +191,10 @@ __global__ void __launch_bounds__(128) k_mlp_train(const unsigned char *__restri
         }
         __syncthreads();
     }
-    // bias and loss sums: lanes with the same t hold the same columns
+    // bias and loss sums: lanes with the same t hold the same columns; each
+    // warp writes its own slot and the slots are added in warp order below
+    // (no shared-memory atomics: the partials are the same bits every run)
+    float *BW = BACC + 136 * warp;
 #pragma unroll
     for (int j = 0; j < 8; j++)
 #pragma unroll
@@ -202,18 +205,21 @@ __global__ void __launch_bounds__(128) k_mlp_train(const unsigned char *__restri
                 b += __shfl_xor_sync(0xffffffffu, b, o);
             }
             if (g == 0) {
-                atomicAdd(&BACC[8 * j + 2 * t + h], a);
-                atomicAdd(&BACC[64 + 8 * j + 2 * t + h], b);
+                BW[8 * j + 2 * t + h] = a;
+                BW[64 + 8 * j + 2 * t + h] = b;
             }
         }
 #pragma unroll
     for (int h = 0; h < 2; h++) {
         float a = db3[h];
         for (int o = 4; o < 32; o <<= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-        if (lane == 0) atomicAdd(&BACC[128 + h], a);
+        if (lane == 0) BW[128 + h] = a;
     }
     for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
-    if (lane == 0) atomicAdd(&BACC[130], loss);
+    if (lane == 0) BW[130] = loss;
+    __syncthreads();
+    for (int i = threadIdx.x; i < 131; i += blockDim.x)
+        BACC[i] = ((BACC[i] + BACC[136 + i]) + BACC[272 + i]) + BACC[408 + i];
     __syncthreads();
     float *P = partials + (size_t)blockIdx.x * (MLP_NPARAM + 1);
 #pragma unroll

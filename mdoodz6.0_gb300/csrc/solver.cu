@@ -1636,30 +1636,18 @@ static mdz_status vcycle(mdz_ctx *ctx, mg_hier<T> &H, int l, int nu1, int nu2, T
 
 // ---------------------------------------------------------------------------
 // Pressure mean over the pressure equations (sum, count) and its removal.
-// (sum in the vector's precision and an integer count per block, block totals
-// added in FP64: no FP64 instruction per element)
+// (sum in the vector's precision and an integer count per thread, warp sums
+// in that precision, then a fixed-order FP64 sum of the block partials:
+// reduce.cuh)
 template <typename T>
 __global__ void __launch_bounds__(256) k_psum(int np, const signed char *__restrict__ tp, const T *__restrict__ p,
-                                              double *out) {
+                                              double *part, unsigned int *counter, double *out) {
     T acc = 0;
     int cnt = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x)
         if (tp[i] == -1) { acc += p[i]; cnt++; }
-    for (int o = 16; o > 0; o >>= 1) {
-        acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    }
-    __shared__ T sa[8];
-    __shared__ int sn[8];
-    if ((threadIdx.x & 31) == 0) { sa[threadIdx.x >> 5] = acc; sn[threadIdx.x >> 5] = cnt; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        T a = 0;
-        int c = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) { a += sa[w]; c += sn[w]; }
-        atomicAdd(&out[0], (double)a);
-        atomicAdd(&out[1], (double)c);
-    }
+    const T v[2] = {acc, (T)cnt};   // (counts per thread are small integers: exact in T)
+    mdz_grid_sum<2, T>(v, part, counter, out);
 }
 
 // (the mean in the vector's precision: an FP64 division per thread is a long
@@ -1677,7 +1665,8 @@ __global__ void k_psub(int np, const signed char *__restrict__ tp, const double 
 // zero-mean projection applied by k_copy_out
 template <typename T>
 __global__ void __launch_bounds__(256) k_precond_p(stokes_geom G, const T *__restrict__ D11, const T *__restrict__ rp,
-                                                   T *__restrict__ zp, double *psum) {
+                                                   T *__restrict__ zp, double *part, unsigned int *counter,
+                                                   double *psum) {
     const int np = G.ncx * G.ncz;
     const T c = T(0.5) * gc<T>(G, GC_IXZ);
     T acc = 0;
@@ -1687,21 +1676,8 @@ __global__ void __launch_bounds__(256) k_precond_p(stokes_geom G, const T *__res
         if (G.BCp[i] == -1) { v = c * D11[i] * rp[i]; acc += v; cnt++; }
         zp[i] = v;
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    }
-    __shared__ T sa[8];
-    __shared__ int sn[8];
-    if ((threadIdx.x & 31) == 0) { sa[threadIdx.x >> 5] = acc; sn[threadIdx.x >> 5] = cnt; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        T a = 0;
-        int n = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) { a += sa[w]; n += sn[w]; }
-        atomicAdd(&psum[0], (double)a);
-        atomicAdd(&psum[1], (double)n);
-    }
+    const T v[2] = {acc, (T)cnt};
+    mdz_grid_sum<2, T>(v, part, counter, psum);
 }
 
 // f = r_vel - B zp  on the fine MG level (B: celvol-scaled pressure gradient)
@@ -1751,11 +1727,11 @@ static mdz_status precondition(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n,
     const int np = F.ncx * F.ncz;
     // zero-mean pressure block: constants are the operator's null space; left
     // in, they grow in the iterates and cost the FP32 gradients their accuracy
-    MDZ_CUDA(ctx, cudaMemsetAsync(H.pmean, 0, 2 * sizeof(double), st));
     {
         int blocks = mdz_blocks(np, 256);
         if (blocks > 152 * 4) blocks = 152 * 4;
-        k_precond_p<T><<<blocks, 256, 0, st>>>(G, F.D11, r + nu + nv, z + nu + nv, H.pmean);
+        k_precond_p<T><<<blocks, 256, 0, st>>>(G, F.D11, r + nu + nv, z + nu + nv, ctx->red_part + MDZ_RP_PRECP,
+                                               ctx->red_cnt + MDZ_RC_PRECP, H.pmean);
         MDZ_LAUNCHED(ctx);
     }
     k_precond_rhs<T><<<box_grid(F.Nx, F.Nz), dim3(32, 8), 0, st>>>(G, r, r + nu, z + nu + nv, F.fu, F.fv);
@@ -1898,116 +1874,97 @@ static mdz_status remove_pressure_mean(mdz_ctx *ctx, double *p, cudaStream_t st)
     const mdz_dgrid &g = ctx->g;
     int np = g.ncx * g.ncz;
     double *d = (double *)(ctx->d_counters + 24);
-    MDZ_CUDA(ctx, cudaMemsetAsync(d, 0, 2 * sizeof(double), st));
     int blocks = mdz_blocks(np, 256);
     if (blocks > 152 * 4) blocks = 152 * 4;
-    k_psum<double><<<blocks, 256, 0, st>>>(np, g.BCp, p, d);
+    k_psum<double><<<blocks, 256, 0, st>>>(np, g.BCp, p, ctx->red_part + MDZ_RP_PSUM, ctx->red_cnt + MDZ_RC_PSUM, d);
     MDZ_LAUNCHED(ctx);
     k_psub<double><<<mdz_blocks(np), MDZ_THREADS, 0, st>>>(np, g.BCp, d, p);
     MDZ_LAUNCHED(ctx);
     return MDZ_OK;
 }
 
-// out[q] += (a_q, b) for the nq vectors of the pointer table (each of length
+// out[q] = (a_q, b) for the nq vectors of the pointer table (each of length
 // n, contiguous u|v|p like b).  FP32 vectors: one thread keeps Q = 8 running
 // sums, so b is read once per 8 vectors and the loads of 8 independent chains
-// overlap, and products, sums and the block reduction stay FP32 with only the
-// block totals entering FP64 (FP64 instructions issue at a small fraction of
+// overlap, and products, sums and the warp reductions stay FP32 with only the
+// warp sums entering FP64 (FP64 instructions issue at a small fraction of
 // the FP32 rate on this part, so even a per-thread FP64 reduction tree
 // dominated the kernel).  FP64 vectors: Q = 1, one vector per block row (the
-// per-element FP64 multiply-add is the bound there).  A non-null flag holding
-// 0 makes the launch a no-op.
+// per-element FP64 multiply-add is the bound there).  Block row y handles
+// vectors y Q .. y Q + Q - 1; its blocks write their partials to
+// part[q * gridDim.x + blockIdx.x] and the last block of the row to finish
+// adds them up in block order (reduce.cuh): deterministic.  cnt: one arrival
+// counter per block row.  A non-null flag holding 0 makes the launch a no-op.
 template <typename T, int MDOT_Q>
-__global__ void __launch_bounds__(256) k_dots(int nq, size_t n, const T *const *__restrict__ a,
-                                              const T *__restrict__ b, double *out, const double *flag) {
-    if (flag && *flag == 0.0) return;
-    const int q0 = blockIdx.y * MDOT_Q;
-    const T *ap[MDOT_Q];
-    T part[MDOT_Q];
+__device__ __forceinline__ void dots_block(int nq, size_t n, const T *const *ap, const T *__restrict__ b,
+                                           double *part, double (&bs)[MDOT_Q], double *sh) {
+    T p[MDOT_Q];
 #pragma unroll
-    for (int j = 0; j < MDOT_Q; j++) {
-        ap[j] = q0 + j < nq ? a[q0 + j] : nullptr;
-        part[j] = T(0);
-    }
+    for (int j = 0; j < MDOT_Q; j++) p[j] = T(0);
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         const T bi = b[i];
 #pragma unroll
         for (int j = 0; j < MDOT_Q; j++)
-            if (ap[j]) part[j] += ap[j][i] * bi;
+            if (ap[j]) p[j] += ap[j][i] * bi;
     }
-    __shared__ T sh[MDOT_Q][8];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    mdz_block_sum<MDOT_Q, T>(p, bs, sh);
+    const int q0 = blockIdx.y * MDOT_Q;
+    if (threadIdx.x == 0) {
 #pragma unroll
-    for (int j = 0; j < MDOT_Q; j++) {
-        T v = part[j];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) sh[j][wid] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < MDOT_Q && q0 + (int)threadIdx.x < nq) {
-        T v = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += sh[threadIdx.x][w];
-        atomicAdd(out + q0 + threadIdx.x, (double)v);
+        for (int j = 0; j < MDOT_Q; j++)
+            if (q0 + j < nq) part[(size_t)(q0 + j) * gridDim.x + blockIdx.x] = bs[j];
     }
 }
 
+template <typename T, int MDOT_Q>
+__global__ void __launch_bounds__(256) k_dots(int nq, size_t n, const T *const *__restrict__ a,
+                                              const T *__restrict__ b, double *part, unsigned int *cnt,
+                                              double *out, const double *flag) {
+    if (flag && *flag == 0.0) return;
+    __shared__ double sh[32 * MDOT_Q];
+    const int q0 = blockIdx.y * MDOT_Q;
+    const T *ap[MDOT_Q];
+#pragma unroll
+    for (int j = 0; j < MDOT_Q; j++) ap[j] = q0 + j < nq ? a[q0 + j] : nullptr;
+    double bs[MDOT_Q];
+    dots_block<T, MDOT_Q>(nq, n, ap, b, part, bs, sh);
+    if (!mdz_arrive_last(cnt + blockIdx.y, gridDim.x)) return;
+    const int nrow = nq - q0 < MDOT_Q ? nq - q0 : MDOT_Q;
+    mdz_sum_partials(part + (size_t)q0 * gridDim.x, gridDim.x, nrow, out + q0);
+}
+
 // One Gram-Schmidt pass's sums in one launch: (w, W_q) for q < k, then
-// (w, w) and (w, r) as vectors k and k + 1 (b = w), accumulated as k_dots
-// does; the last block to finish (a device-scope counter) then runs the
-// pass's scalar step: mode 1 the check of the first pass (sc[5] = 1 asks for
-// a second pass, else the scalars), mode 2 the scalars of the second pass.
+// (w, w) and (w, r) as vectors k and k + 1 (b = w), summed as k_dots does
+// (the last block of each block row adds its row's partials in block order);
+// the last row to finish (a second arrival counter) then runs the pass's
+// scalar step: mode 1 the check of the first pass (sc[5] = 1 asks for a
+// second pass, else the scalars), mode 2 the scalars of the second pass.
 // With flag (mode 2) every block returns at once when *flag is 0.
+// cnt[0]: rows finished, cnt[1 + y]: blocks of row y finished.
 template <typename T, int MDOT_Q>
 __global__ void __launch_bounds__(256) k_gcr_dots(int k, size_t n, const T *const *__restrict__ a,
-                                                  const T *__restrict__ w, const T *__restrict__ r, double *out,
-                                                  const double *flag, int mode, double *sc,
-                                                  unsigned int *counter) {
+                                                  const T *__restrict__ w, const T *__restrict__ r, double *part,
+                                                  double *out, const double *flag, int mode, double *sc,
+                                                  unsigned int *cnt) {
     if (flag && *flag == 0.0) return;
+    __shared__ double sh[32 * MDOT_Q];
     const int nq = k + 2, q0 = blockIdx.y * MDOT_Q;
     const T *ap[MDOT_Q];
-    T part[MDOT_Q];
 #pragma unroll
     for (int j = 0; j < MDOT_Q; j++) {
         const int q = q0 + j;
         ap[j] = q < k ? a[q] : (q == k ? w : (q == k + 1 ? r : nullptr));
-        part[j] = T(0);
     }
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const T bi = w[i];
-#pragma unroll
-        for (int j = 0; j < MDOT_Q; j++)
-            if (ap[j]) part[j] += ap[j][i] * bi;
-    }
-    __shared__ T sh[MDOT_Q][8];
-    __shared__ bool last;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int j = 0; j < MDOT_Q; j++) {
-        T v = part[j];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) sh[j][wid] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < MDOT_Q && q0 + (int)threadIdx.x < nq) {
-        T v = 0;
-        for (int q = 0; q < (int)(blockDim.x >> 5); q++) v += sh[threadIdx.x][q];
-        atomicAdd(out + q0 + threadIdx.x, (double)v);
-        __threadfence();
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        const unsigned int total = gridDim.x * gridDim.y;
-        last = atomicAdd(counter, 1u) == total - 1;
-    }
-    __syncthreads();
-    if (!last || threadIdx.x != 0) return;
-    __threadfence();
+    double bs[MDOT_Q];
+    dots_block<T, MDOT_Q>(nq, n, ap, w, part, bs, sh);
+    if (!mdz_arrive_last(cnt + 1 + blockIdx.y, gridDim.x)) return;
+    const int nrow = nq - q0 < MDOT_Q ? nq - q0 : MDOT_Q;
+    mdz_sum_partials(part + (size_t)q0 * gridDim.x, gridDim.x, nrow, out + q0);
+    if (!mdz_arrive_last(cnt, gridDim.y)) return;
+    if (threadIdx.x != 0) return;
     double d[GCR_MAX_M + 2];
-    const volatile double *vo = out;
-    for (int q = 0; q < nq; q++) d[q] = vo[q];
-    *counter = 0u;   // for the next launch (stream order)
+    for (int q = 0; q < nq; q++) d[q] = __ldcg(out + q);
     if (mode == 1) {
         double nrm2 = d[k];
         for (int q = 0; q < k; q++) nrm2 -= d[q] * d[q];
@@ -2019,14 +1976,15 @@ __global__ void __launch_bounds__(256) k_gcr_dots(int k, size_t n, const T *cons
 
 template <typename T>
 static mdz_status gcr_dots_launch(mdz_ctx *ctx, gcr_space<T> &S, int k, const T *w, const T *r, double *out,
-                                  const double *flag, int mode, double *sc, unsigned int *counter, cudaStream_t st) {
+                                  const double *flag, int mode, double *sc, cudaStream_t st) {
     constexpr int Q = sizeof(T) == 4 ? 8 : 1;
     const int tiles = (k + 2 + Q - 1) / Q;
     int bx = mdz_blocks((long long)S.n, 256 * (sizeof(T) == 4 ? 8 : 4));
     const int cap = (sizeof(T) == 4 ? 152 * 8 : 152 * 4 + tiles - 1) / tiles;
     if (bx > cap) bx = cap;
     if (bx < 8) bx = 8;
-    k_gcr_dots<T, Q><<<dim3(bx, tiles), 256, 0, st>>>(k, S.n, S.dA0, w, r, out, flag, mode, sc, counter);
+    k_gcr_dots<T, Q><<<dim3(bx, tiles), 256, 0, st>>>(k, S.n, S.dA0, w, r, ctx->red_part + MDZ_RP_DOTS, out, flag,
+                                                       mode, sc, ctx->red_cnt + MDZ_RC_GCR);
     MDZ_LAUNCHED(ctx);
     return MDZ_OK;
 }
@@ -2035,7 +1993,6 @@ template <typename T>
 static mdz_status dots_launch(mdz_ctx *ctx, gcr_space<T> &S, int q0, int nq, const T *b, double *out,
                               cudaStream_t st, const double *flag = nullptr) {
     if (nq <= 0) return MDZ_OK;
-    MDZ_CUDA(ctx, cudaMemsetAsync(out, 0, sizeof(double) * nq, st));
     // FP32: 8 vectors per block row, ~8 elements per thread; FP64: one vector
     // per block row, about 600 blocks in all
     constexpr int Q = sizeof(T) == 4 ? 8 : 1;
@@ -2044,7 +2001,8 @@ static mdz_status dots_launch(mdz_ctx *ctx, gcr_space<T> &S, int q0, int nq, con
     const int cap = (sizeof(T) == 4 ? 152 * 8 : 152 * 4 + tiles - 1) / tiles;
     if (bx > cap) bx = cap;
     if (bx < 8) bx = 8;
-    k_dots<T, Q><<<dim3(bx, tiles), 256, 0, st>>>(nq, S.n, S.dA0 + q0, b, out, flag);
+    k_dots<T, Q><<<dim3(bx, tiles), 256, 0, st>>>(nq, S.n, S.dA0 + q0, b, ctx->red_part + MDZ_RP_DOTS,
+                                                   ctx->red_cnt + MDZ_RC_DOTS, out, flag);
     MDZ_LAUNCHED(ctx);
     return MDZ_OK;
 }
@@ -2116,11 +2074,10 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
     // ||r0||
     // S.dots layout (doubles, B = GCR_MAX_M + 8): first-pass sums of even / odd
     // iterations at 0 / 4B, the scalars sc at GCR_MAX_M + 4, second-pass sums
-    // at 2B / 5B, a scratch sum at 3B, the fused kernels' block counter at 6B
+    // at 2B / 5B, a scratch sum at 3B
     const int B = GCR_MAX_M + 8;
     double *sc = S.dots + (GCR_MAX_M + 4), *dots = S.dots + 3 * B;
     double *dots1p[2] = {S.dots, S.dots + 4 * B}, *dots2p[2] = {S.dots + 2 * B, S.dots + 5 * B};
-    unsigned int *counter = reinterpret_cast<unsigned int *>(S.dots + 6 * B);
     for (int q = 0; q < 2; q++) {
         MDZ_CUDA(ctx, cudaMemsetAsync(dots1p[q], 0, sizeof(double) * (GCR_MAX_M + 3), st));
         MDZ_CUDA(ctx, cudaMemsetAsync(dots2p[q], 0, sizeof(double) * (GCR_MAX_M + 3), st));
@@ -2182,11 +2139,11 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
         // as the preconditioner saw it (SP.r: the FP32 copy in the FP32 form,
         // r itself otherwise), then the check / scalars in its last block
         double *d1 = dots1p[it & 1], *d2 = dots2p[it & 1];
-        if ((s = gcr_dots_launch<P>(ctx, SP, k, SP.w, SP.r, d1, nullptr, 1, sc, counter, st)) != MDZ_OK) return s;
+        if ((s = gcr_dots_launch<P>(ctx, SP, k, SP.w, SP.r, d1, nullptr, 1, sc, st)) != MDZ_OK) return s;
         if (k > 0) {   // second pass (each launch returns at once unless sc[5] = 1)
             k_gcr_orth_if<P><<<ng, MDZ_THREADS, 0, st>>>(n, k, SP.Z, SP.W, d1, sc, SP.z, SP.w);
             MDZ_LAUNCHED(ctx);
-            if ((s = gcr_dots_launch<P>(ctx, SP, k, SP.w, SP.r, d2, sc + 5, 2, sc, counter, st)) != MDZ_OK) return s;
+            if ((s = gcr_dots_launch<P>(ctx, SP, k, SP.w, SP.r, d2, sc + 5, 2, sc, st)) != MDZ_OK) return s;
         }
         k_gcr_finish<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, k, SP.Z, SP.W, d1, d2, sc, SP.z, SP.w, S.r,
                                                         mixed ? SP.r : (P *)nullptr, dots1p[(it + 1) & 1],

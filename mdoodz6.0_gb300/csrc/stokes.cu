@@ -73,39 +73,13 @@ template void stokes_apply_launch<float>(const stokes_geom &, const stokes_coefs
                                          stokes_vec<float>, const stokes_cvec<float> *, bool, cudaStream_t);
 
 // ---------------------------------------------------------------------------
-// Reductions: block-level warp-shuffle sums, one FP64 atomicAdd per block.
-__device__ __forceinline__ double warp_sum(double v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-template <int NV>
-__device__ __forceinline__ void block_sum_atomic(double (&v)[NV], double *out) {
-    __shared__ double sh[NV][32];
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-    for (int q = 0; q < NV; q++) {
-        double s = warp_sum(v[q]);
-        if (lane == 0) sh[q][wid] = s;
-    }
-    __syncthreads();
-    if (wid == 0) {
-#pragma unroll
-        for (int q = 0; q < NV; q++) {
-            double s = lane < nw ? sh[q][lane] : 0.0;
-            s = warp_sum(s);
-            if (lane == 0) atomicAdd(&out[q], s);
-        }
-    }
-}
-
 // Sums of squares per equation block and counts of equations: out[0..2] = sum F^2
 // over x-momentum, z-momentum, continuity rows; out[3..5] = row counts.
 template <typename T>
 __global__ void k_residual_norms(int nu, int nv, int np, const T *__restrict__ fu, const T *__restrict__ fv,
                                  const T *__restrict__ fp, const signed char *__restrict__ tu,
                                  const signed char *__restrict__ tv, const signed char *__restrict__ tp,
-                                 double *out) {
+                                 double *part, unsigned int *counter, double *out) {
     double acc[6] = {0, 0, 0, 0, 0, 0};
     int n = nu > nv ? nu : nv;
     n = n > np ? n : np;
@@ -114,18 +88,18 @@ __global__ void k_residual_norms(int nu, int nv, int np, const T *__restrict__ f
         if (i < nv && tv[i] == -1) { double f = fv[i]; acc[1] += f * f; acc[4] += 1; }
         if (i < np && tp[i] == -1) { double f = fp[i]; acc[2] += f * f; acc[5] += 1; }
     }
-    block_sum_atomic<6>(acc, out);
+    mdz_grid_sum<6, double>(acc, part, counter, out);   // fixed order: the same bits every run
 }
 
 template <typename T>
 mdz_status stokes_norms_launch(mdz_ctx *ctx, stokes_cvec<T> f, double *d_out6, cudaStream_t st) {
     const mdz_dgrid &g = ctx->g;
     int nu = g.Nx * (g.Nz + 1), nv = (g.Nx + 1) * g.Nz, np = g.ncx * g.ncz;
-    MDZ_CUDA(ctx, cudaMemsetAsync(d_out6, 0, 6 * sizeof(double), st));
     int n = nu > nv ? nu : nv;
     int blocks = mdz_blocks(n, 256);
     if (blocks > 152 * 8) blocks = 152 * 8;
-    k_residual_norms<T><<<blocks, 256, 0, st>>>(nu, nv, np, f.u, f.v, f.p, g.BCu, g.BCv, g.BCp, d_out6);
+    k_residual_norms<T><<<blocks, 256, 0, st>>>(nu, nv, np, f.u, f.v, f.p, g.BCu, g.BCv, g.BCp,
+                                                ctx->red_part + MDZ_RP_NORMS, ctx->red_cnt + MDZ_RC_NORMS, d_out6);
     MDZ_LAUNCHED(ctx);
     return MDZ_OK;
 }

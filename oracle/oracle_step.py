@@ -48,44 +48,55 @@ def assemble(g, f, jacobian, period=5):
                 yu, yv, yp = orc.stokes_apply(g, f, jacobian, x[:nu], x[nu:nu + nv], x[nu + nv:])
                 y = np.concatenate([yu, yv, yp])
                 # owner of each response: the probed node of this colour nearest to the row
-                for r in np.flatnonzero(y):
-                    if idx[r] < 0:
-                        continue
-                    rows.append(idx[r])
-                    cols.append(_owner(r, sel, comp, offs, widths, period, cx, cz))
-                    vals.append(y[r])
-    cols = np.array([idx[c] for c in cols])
+                r = np.flatnonzero(y)
+                r = r[idx[r] >= 0]
+                rows.append(idx[r])
+                cols.append(idx[_owner(r, comp, offs, widths, period, cx, cz)])
+                vals.append(y[r])
+    rows, cols, vals = np.concatenate(rows), np.concatenate(cols), np.concatenate(vals)
     return sp.csr_matrix((vals, (rows, cols)), shape=(n, n)), idx, n, len(ep)
 
 
-def _owner(r, sel, comp, offs, widths, period, cx, cz):
-    # position of row r in its own component's index box
-    for c in (2, 1, 0):
-        if r >= offs[c]:
-            rc = c
-            break
-    W, _ = widths[rc]
-    rk, rl = (r - offs[rc]) % W, (r - offs[rc]) // W
+def _owner(r, comp, offs, widths, period, cx, cz):
+    """Column of each response row r: the unique probed node of colour
+    (cx, cz) of component comp within two nodes of the row's position."""
+    rc = np.zeros(len(r), int)
+    rc[r >= offs[1]] = 1
+    rc[r >= offs[2]] = 2
+    Wr = np.array([w for w, _ in widths])[rc]
+    loc = r - np.array(offs)[rc]
+    rk, rl = loc % Wr, loc // Wr
     W2, _ = widths[comp]
-    # the unique probed node with k = cx (mod period), |k - rk| <= 2 (same for l)
     k = rk - ((rk - cx) % period)
-    if rk - k > 2:
-        k += period
+    k[rk - k > 2] += period
     l = rl - ((rl - cz) % period)
-    if rl - l > 2:
-        l += period
+    l[rl - l > 2] += period
     return offs[comp] + k + l * W2
 
 
 def solve_defect(g, f, jacobian, F):
+    """Solve K x = F on the equation nodes with the pressure mean fixed to
+    zero: the bordered system [K e; e^T 0] [x; lam] = [F; 0] (e: ones on the
+    pressure equations).  Factorised as M = K + c u u^T (u: one pressure
+    unknown; nonsingular where K's null space is the constant pressure) by
+    sparse LU without the dense border, then the border and the rank-one term
+    resolved from three solves with M (2 x 2 system)."""
     K, idx, n, n_p = assemble(g, f, jacobian)
     b = F[idx >= 0][np.argsort(idx[idx >= 0])]
     b = b.copy()
     b[n - n_p:] -= b[n - n_p:].mean()
     e = np.zeros(n)
     e[n - n_p:] = 1.0
-    Kb = sp.bmat([[K, sp.csr_matrix(e).T], [sp.csr_matrix(e), None]]).tocsc()
-    x = spla.spsolve(Kb, np.concatenate([b, [0.0]]))[:n]
+    r = n - 1
+    c = np.abs(K.diagonal()[:n - n_p]).mean()
+    u = np.zeros(n)
+    u[r] = 1.0
+    M = (K + sp.csr_matrix(([c], ([r], [r])), shape=(n, n))).tocsc()
+    lu = spla.splu(M, permc_spec="COLAMD")
+    yb, yu, ye = lu.solve(b), lu.solve(u), lu.solve(e)
+    A2 = np.array([[1.0 - c * yu[r], ye[r]], [c * (e @ yu), -(e @ ye)]])
+    s_, lam = np.linalg.solve(A2, np.array([yb[r], -(e @ yb)]))
+    x = yb + c * s_ * yu - lam * ye
     out = np.zeros(len(F))
     out[idx >= 0] = x[idx[idx >= 0]]
     return out
