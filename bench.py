@@ -202,6 +202,45 @@ def field_diffs(a, b):
     return out
 
 
+PARITY_GRID = (129, 65)
+
+
+def parity_vs_oracle(nx=PARITY_GRID[0], nz=PARITY_GRID[1]):
+    """Each output field of both GPU forms after one time step of the
+    lithosphere model at nx x nz, against the oracle's FP64 time step on the
+    same inputs (restated reference functions, exact defect solves): relative
+    2-norm errors (pressure with its mean removed: the operator leaves it
+    undetermined)."""
+    import numpy as np
+    import mdz
+    import mdz_setups
+    import oracle_step
+    cfg = mdz_setups.config_lithosphere(Nx=nx, Nz=nz, precision=64)
+    m = {k: v.copy() for k, v in cfg["markers"].items()}
+    u, v, p, rep = oracle_step.time_step(cfg["grid"], cfg["mat"], cfg["model"], m, cfg["u"], cfg["v"], cfg["p"])
+    ref = dict(u=u, v=v, p=p - p.mean(), sxxd=m["sxxd"], szzd=m["szzd"], sxz=m["sxz"], x=m["x"], z=m["z"])
+    out = {"grid": "%dx%d" % (nx, nz), "step": 1, "oracle_nonlinear_its": rep["nonlinear_its"]}
+    for name, prec, learned in (("plain_fp64", 64, 0), ("learned_fp32_ir", 32, 1)):
+        c = mdz_setups.config_lithosphere(Nx=nx, Nz=nz, precision=prec, learned=learned)
+        ctx = mdz_setups.load_context(c)
+        if learned:
+            mdz_setups.train_guess(ctx, c, steps=GUESS_STEPS[0])
+        r = ctx.time_step(c["mat"], c["model"])
+        g = c["grid"]
+        uu, vv, pp = np.empty(g.size(-1)), np.empty(g.size(-2)), np.empty(g.size(1))
+        ctx._check(ctx.L.mdz_get_velocity(ctx.h, mdz._dptr(uu), mdz._dptr(vv), mdz._dptr(pp)))
+        x, z, ph, _, _ = ctx.get_markers()
+        got = dict(u=uu, v=vv, p=pp - pp.mean(), sxxd=ctx.get_marker_attr(mdz.M_SXXD),
+                   szzd=ctx.get_marker_attr(mdz.M_SZZD), sxz=ctx.get_marker_attr(mdz.M_SXZ), x=x, z=z)
+        ctx.close()
+        e = {k: (float(np.linalg.norm(got[k] - ref[k]) / max(np.linalg.norm(ref[k]), 1e-300))
+                 if len(got[k]) == len(ref[k]) else None) for k in ref}
+        e["phases_equal"] = bool(len(ph) == len(m["phase"]) and np.array_equal(ph, m["phase"]))
+        e["nonlinear_its"] = r.nonlinear_its
+        out[name] = e
+    return out
+
+
 def mlp_workload():
     """The local-rheology MLP on its own: 2^24 tuples of the lithosphere
     phases, one epoch of training at batch 65536, inference over 2^24 cells."""
@@ -306,24 +345,77 @@ def builder(size):
     return b
 
 
-def cpu_reference(size, budget_s=20.0):
-    """The oracle's CPU time step (restated reference functions + SuperLU) on a
-    bounded strip of the same model: full width, a few cells deep, timed and
-    scaled to the full grid by the cell count."""
-    import numpy as np
-    import mdz_setups
-    import oracle_step
+# The CPU time step is sampled on the same model at 1/64 of the cells (same
+# domain, layering, rheology, markers per cell and time step), scaled by the
+# cell count to the full grid; SAMPLE_CHECK is a second resolution (1/16 of
+# the cells) whose first steps test that scaling.
+SAMPLE_GRID = (129, 65)
+SAMPLE_CHECK = (257, 129)
+
+
+def _cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+class CpuModel:
+    """Consecutive oracle time steps (the restated reference functions in C,
+    threaded over nodes and markers with OpenMP, plus SciPy SuperLU for each
+    defect solve in place of CHOLMOD) of the lithosphere model at one grid
+    size.  step() returns the wall time of one step in ms and its report."""
+
+    def __init__(self, nx, nz):
+        import mdz_setups
+        self.cfg = mdz_setups.config_lithosphere(Nx=nx, Nz=nz, precision=64)
+        c = self.cfg
+        self.m = {k: v.copy() for k, v in c["markers"].items()}
+        self.u, self.v, self.p = c["u"].copy(), c["v"].copy(), c["p"].copy()
+        self.cells = (nx - 1) * (nz - 1)
+
+    def step(self):
+        import oracle_step
+        c = self.cfg
+        t0 = time.perf_counter()
+        self.u, self.v, self.p, rep = oracle_step.time_step(c["grid"], c["mat"], c["model"], self.m, self.u, self.v,
+                                                            self.p)
+        return (time.perf_counter() - t0) * 1e3, rep
+
+
+def cpu_sample(steps, warmup, size=None, check=True):
+    """CPU reference time per full-grid step: `warmup` untimed and `steps`
+    timed consecutive steps of the model at SAMPLE_GRID (the same step indices
+    as the GPU forms time), scaled by cells; then the first two steps at
+    SAMPLE_CHECK against the first two at SAMPLE_GRID, per cell."""
     nx, nz = size if size else (1025, 513)
-    strip_nz = 9   # 8 cell rows: about 30 s of one core per sample
-    cfg = mdz_setups.config_lithosphere(Nx=nx, Nz=strip_nz, precision=64)
-    m = cfg["markers"]
-    t0 = time.perf_counter()
-    oracle_step.time_step(cfg["grid"], cfg["mat"], cfg["model"], m, cfg["u"], cfg["v"], cfg["p"])
-    dt = time.perf_counter() - t0
-    scale = ((nx - 1) * (nz - 1)) / ((nx - 1) * (strip_nz - 1))
-    return dict(value=dt * 1e3 * scale, unit=UNIT, cores=1, kind="port",
-                sample="one oracle time step on a %dx%d strip of the model (%.1f s), scaled by cells x%.1f"
-                       % (nx, strip_nz, dt, scale))
+    full = (nx - 1) * (nz - 1)
+    os.environ.setdefault("OMP_NUM_THREADS", str(_cpu_threads()))
+    a = CpuModel(*SAMPLE_GRID)
+    scale = full / a.cells
+    first, times, reps = [], [], []
+    for k in range(warmup + steps):
+        ms, rep = a.step()
+        if k < 2:
+            first.append(ms)
+        if k >= warmup:
+            times.append(ms)
+            reps.append(rep["nonlinear_its"])
+    value = scale * sum(times) / len(times)
+    out = dict(value=value, unit=UNIT, cores=int(os.environ["OMP_NUM_THREADS"]), kind="port",
+                sample=("%d consecutive time steps (after %d untimed) of the same lithosphere model at %dx%d "
+                        "(%d cells, 16 markers per cell), scaled by cells x%.0f to %dx%d; oracle C functions "
+                        "threaded with OpenMP, defect solves by SciPy SuperLU on one thread (CHOLMOD unavailable)"
+                        % (steps, warmup, SAMPLE_GRID[0], SAMPLE_GRID[1], a.cells, scale, nx, nz)),
+                sample_step_ms=times, sample_nonlinear_its=reps)
+    if check:
+        b = CpuModel(*SAMPLE_CHECK)
+        t2 = [b.step()[0] for _ in range(2)]
+        per_cell_a = sum(first) / a.cells
+        per_cell_b = sum(t2) / b.cells
+        out["scaling_check"] = {"grid": "%dx%d" % SAMPLE_CHECK, "first_two_steps_ms": t2, "ms_per_cell": per_cell_b,
+                                "ms_per_cell_at_%dx%d" % SAMPLE_GRID: per_cell_a, "ratio": per_cell_b / per_cell_a}
+    return out
 
 
 def main():
@@ -344,16 +436,16 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return 0
-        times = []
-        for _ in range(args.warmup + args.steps):
-            times.append(cpu_reference(size))
-        ref = times[-1]
-        val = sum(t["value"] for t in times[args.warmup:]) / args.steps
+        ref = cpu_sample(args.steps, args.warmup, size)
+        val = ref["value"]
         line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": val, "higher_is_better": False,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": {"workload": "lithosphere 1025x513, 4 phases, 16 markers/cell, one Newton time step"},
-                "cpu_baseline": dict(ref, value=val),
+                "config": {"workload": "lithosphere %s, 4 phases, 16 markers/cell, one Newton time step"
+                                       % ("x".join(map(str, size)) if size else "1025x513"),
+                           "timed": "each step is one time step of the model at %dx%d, scaled by cells"
+                                    % SAMPLE_GRID},
+                "cpu_baseline": ref,
                 "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return 0
@@ -419,7 +511,9 @@ def main():
     if rank == 0 and not args.no_mlp:
         line["mlp"] = mlp_workload()
     if rank == 0 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_reference(size)
+        line["field_rel_err_vs_oracle"] = parity_vs_oracle()
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_sample(3, 0, size, check=False)
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -331,6 +331,19 @@ mdz_status mdz_mlp_benchmark(mdz_ctx *ctx, int batch, int reps, double *ms_infer
 mdz_status mdz_NonNewtonianViscosityGrid_learned(mdz_ctx *ctx, const mdz_materials *mat, const mdz_rheo_params *prm,
                                                  mdz_fields *f, int learned, long long *stats);
 
+/* ShearModCompExpGrid (SOURCE/RheologyDensity.c:1666-1791): harmonic phase
+ * averages of the shear modulus and compressibility from phase_perc_n /
+ * phase_perc_s -> mu_n, mu_s, bet_n, bet_s (0 on air nodes). */
+mdz_status mdz_ShearModCompExpGrid(mdz_ctx *ctx, const mdz_materials *mat, mdz_fields *f);
+
+/* CohesionFrictionDilationGrid (SOURCE/RheologyDensity.c:1422-1665): the
+ * resident markers' plastic strain projected to the centroids (P2Mastah with
+ * itp_stencil 1 or 9) and to the vertices (Interp_P2N, one-cell tent), the
+ * smooth (erfc) softening of cohesion, friction and dilation per phase, and
+ * arithmetic phase averages from phase_perc_n / phase_perc_s -> C_n, C_s,
+ * fric_n, fric_s, dil_n, dil_s, strain_n, strain_s (0 on air nodes). */
+mdz_status mdz_CohesionFrictionDilationGrid(mdz_ctx *ctx, const mdz_materials *mat, int itp_stencil, mdz_fields *f);
+
 /* RheologicalOperators (SOURCE/RheologyDensity.c:713-954), isotropic:
  * Picard (jacobian = 0) or Newton (jacobian = 1) D11..D24 at centroids and
  * D31..D34 at vertices. */

@@ -85,7 +85,7 @@ __global__ void k_grid_props(int n, int nph, mdz_materials m, int law, const sig
         }
         imu = 1.0 / imu;
         ibet = 1.0 / ibet;
-        Cs *= cmul[c];
+        if (cmul) Cs *= cmul[c];
     }
     mu[c] = imu; bet[c] = ibet; rho[c] = r;
     if (d0) d0[c] = d;
@@ -376,9 +376,15 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
         int avg[5] = {0, 0, 0, 0, 0};
         if ((s = mdz_dev_p2g(ctx, 5, cv, avg, co, f.phase_perc_n, MDZ_NODES_CENTROIDS, M->itp_stencil, st)) != MDZ_OK)
             return s;
+        // vertices: the softening reads the plastic strain as Interp_P2N gives it
+        // (RheologyDensity.c:1545, the one-cell stencil whatever itp_stencil),
+        // and the cohesion multiplier travels with it
         const double *vv[3] = {ctx->m.attr[MDZ_M_SXZ], ctx->m.attr[MDZ_M_STRAIN_PL], ctx->m.attr[MDZ_M_CMUL]};
         double *vo[3] = {f.sxz0, f.strain_s, B.cmul_s};
-        if ((s = mdz_dev_p2g(ctx, 3, vv, avg, vo, f.phase_perc_s, MDZ_NODES_VERTICES, M->itp_stencil, st)) != MDZ_OK)
+        const int nv1 = M->itp_stencil == 1 ? 3 : 1;
+        if ((s = mdz_dev_p2g(ctx, nv1, vv, avg, vo, f.phase_perc_s, MDZ_NODES_VERTICES, M->itp_stencil, st)) != MDZ_OK)
+            return s;
+        if (nv1 == 1 && (s = mdz_dev_p2g(ctx, 2, vv + 1, avg, vo + 1, nullptr, MDZ_NODES_VERTICES, 1, st)) != MDZ_OK)
             return s;
         if ((s = mdz_dev_c2v(ctx, f.sxxd0, f.sxxd0_s, st)) != MDZ_OK) return s;
         if ((s = mdz_dev_c2v(ctx, f.szzd0, f.szzd0_s, st)) != MDZ_OK) return s;
@@ -635,6 +641,65 @@ extern "C" mdz_status mdz_time_step(mdz_ctx *ctx, const mdz_materials *mat, cons
     ctx->p2g_empty = nullptr;
     ctx->bins.valid = false;
     return s;
+}
+
+// ShearModCompExpGrid (SOURCE/RheologyDensity.c:1666-1791): harmonic shear
+// modulus and compressibility at centroids and vertices from the phase
+// fractions f->phase_perc_n / phase_perc_s (host); writes f->mu_n, mu_s,
+// bet_n, bet_s.  Air nodes (tag 30, and 31 at centroids) get 0.
+// CohesionFrictionDilationGrid (:1422-1665): the resident markers' plastic
+// strain projected to the centroids (P2Mastah with itp_stencil) and to the
+// vertices (Interp_P2N: nearest vertex, one-cell tent), the smooth softening
+// law per phase, arithmetic phase average; writes f->C_n, C_s, fric_n, fric_s,
+// dil_n, dil_s (and strain_n, strain_s).  Both run on the device mirrors and
+// copy the outputs back (synchronous).
+static mdz_status grid_props_host(mdz_ctx *ctx, const mdz_materials *mat, int itp_stencil, mdz_fields *h,
+                                  bool cohesion) {
+    if (!ctx || !mat || !h || !h->phase_perc_n || !h->phase_perc_s)
+        return ctx ? mdz_fail(ctx, MDZ_ERR_ARG, "grid properties: null argument") : MDZ_ERR_ARG;
+    mdz_status s = mdz_check_materials(ctx, mat);
+    if (s != MDZ_OK) return s;
+    if (itp_stencil != 1 && itp_stencil != 9)
+        return mdz_fail(ctx, MDZ_ERR_ARG, "CohesionFrictionDilationGrid: itp_stencil must be 1 or 9");
+    if ((s = mdz_ensure_fields(ctx)) != MDZ_OK) return s;
+    const mdz_dgrid &g = ctx->g;
+    mdz_fields &f = ctx->d;
+    cudaStream_t st = ctx->stream;
+    const int np = g.ncx * g.ncz, nvert = g.Nx * g.Nz, nph = mat->n_phases;
+    MDZ_CUDA(ctx, cudaMemcpyAsync(f.phase_perc_n, h->phase_perc_n, sizeof(double) * np * nph, cudaMemcpyHostToDevice,
+                                  st));
+    MDZ_CUDA(ctx, cudaMemcpyAsync(f.phase_perc_s, h->phase_perc_s, sizeof(double) * nvert * nph,
+                                  cudaMemcpyHostToDevice, st));
+    if (cohesion) {
+        const double *val[1] = {ctx->m.attr[MDZ_M_STRAIN_PL]};
+        int avg[1] = {0};
+        double *on[1] = {f.strain_n}, *os[1] = {f.strain_s};
+        if ((s = mdz_dev_p2g(ctx, 1, val, avg, on, nullptr, MDZ_NODES_CENTROIDS, itp_stencil, st)) != MDZ_OK) return s;
+        if ((s = mdz_dev_p2g(ctx, 1, val, avg, os, nullptr, MDZ_NODES_VERTICES, 1, st)) != MDZ_OK) return s;
+    }
+    k_grid_props<<<mdz_blocks(np), MDZ_THREADS, 0, st>>>(np, nph, *mat, 0, g.BCp, 1, f.phase_perc_n, f.strain_n,
+                                                         nullptr, f.mu_n, f.bet_n, f.rho_n, f.d0_n, f.C_n, f.fric_n,
+                                                         f.dil_n);
+    MDZ_LAUNCHED(ctx);
+    k_grid_props<<<mdz_blocks(nvert), MDZ_THREADS, 0, st>>>(nvert, nph, *mat, 0, g.BCg, 0, f.phase_perc_s,
+                                                            f.strain_s, nullptr, f.mu_s, f.bet_s, f.rho_s, nullptr,
+                                                            f.C_s, f.fric_s, f.dil_s);
+    MDZ_LAUNCHED(ctx);
+    if (cohesion) {
+        static const char *const names[] = {"C_n", "C_s", "fric_n", "fric_s", "dil_n", "dil_s", "strain_n", "strain_s"};
+        return mdz_download_fields(ctx, h, names, 8, st);
+    }
+    static const char *const names[] = {"mu_n", "mu_s", "bet_n", "bet_s"};
+    return mdz_download_fields(ctx, h, names, 4, st);
+}
+
+extern "C" mdz_status mdz_ShearModCompExpGrid(mdz_ctx *ctx, const mdz_materials *mat, mdz_fields *f) {
+    return grid_props_host(ctx, mat, 1, f, false);
+}
+
+extern "C" mdz_status mdz_CohesionFrictionDilationGrid(mdz_ctx *ctx, const mdz_materials *mat, int itp_stencil,
+                                                       mdz_fields *f) {
+    return grid_props_host(ctx, mat, itp_stencil, f, true);
 }
 
 extern "C" mdz_status mdz_sync_fields(mdz_ctx *ctx, mdz_fields *f, int to_device) {

@@ -363,6 +363,19 @@ class Context:
                                              C.byref(c)))
         return dict(ms_infer=a.value, ms_train_step=b.value, rms_error=c.value)
 
+    def ShearModCompExpGrid(self, mat, fields):
+        """ShearModCompExpGrid (SOURCE/RheologyDensity.c:1666): mu_n, mu_s,
+        bet_n, bet_s of `fields` from its phase fractions."""
+        s = fields.struct()
+        self._check(self.L.mdz_ShearModCompExpGrid(self.h, C.byref(mat), C.byref(s)))
+
+    def CohesionFrictionDilationGrid(self, mat, itp_stencil, fields):
+        """CohesionFrictionDilationGrid (SOURCE/RheologyDensity.c:1422): C, fric,
+        dil (and strain) at centroids and vertices of `fields` from its phase
+        fractions and the resident markers' plastic strain."""
+        s = fields.struct()
+        self._check(self.L.mdz_CohesionFrictionDilationGrid(self.h, C.byref(mat), C.c_int(itp_stencil), C.byref(s)))
+
     def RheologicalOperators(self, prm, fields, jacobian):
         s = fields.struct()
         self._check(self.L.mdz_RheologicalOperators(self.h, C.byref(prm), C.byref(s), C.c_int(jacobian)))

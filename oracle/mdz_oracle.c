@@ -119,6 +119,7 @@ static const signed char *nodeset_tags(const mdz_grid_desc *g, int centroid) {
 int orc_g2p(const mdz_grid_desc *g, int n, const double *x, const double *z, const int *phase,
             const double *F, int node_set, double *out) {
     double dx = g->dx, dz = g->dz;
+#pragma omp parallel for schedule(static)
     for (int k = 0; k < n; k++) {
         out[k] = 0.0;
         if (phase[k] == -1) continue;
@@ -200,6 +201,7 @@ static void orc_v2p(const mdz_grid_desc *g, double xk, double zk, const double *
 /* RogerGuntherII: SOURCE/AdvectionRoutines.c:569-628. */
 int orc_rk4(const mdz_grid_desc *g, int n, double *x, double *z, int *phase, double *vx, double *vz,
             const double *u, const double *v, double dt) {
+#pragma omp parallel for schedule(static)
     for (int k = 0; k < n; k++) {
         double xA = x[k], zA = z[k];
         double VA[2] = {0, 0}, VB[2] = {0, 0}, VC[2] = {0, 0}, VD[2] = {0, 0};

@@ -376,7 +376,9 @@ int orc_viscosity_grid(const mdz_grid_desc *g, const mdz_materials *mat, const m
     orc_c2v(g, f->p, f->P_s);
     orc_c2v(g, f->d0_n, f->d0_s);
     orc_c2v(g, f->phi0_n, f->phi0_s);
-    /* centroids :987-1240 */
+    /* centroids :987-1240 (nodes are independent: the threads' results are
+     * those of the serial loop, bit for bit) */
+#pragma omp parallel for private(p) reduction(+ : ve_fail, vp_fail) schedule(dynamic, 256)
     for (c = 0; c < nc; c++) {
         double eta = 0, eta_phys = 0, VE = 0, sxx = 0, szz = 0, sxz = 0, eel = 0, epl = 0, epwl = 0, elin = 0,
                ecst = 0, dn = 0, xel = 0, xdi = 0, zel = 0, zdi = 0, dexx = 0, dezz = 0, dgxz = 0, dp = 0,
@@ -446,6 +448,7 @@ int orc_viscosity_grid(const mdz_grid_desc *g, const mdz_materials *mat, const m
         SETF(f->OverS_n, c, OS);
     }
     /* vertices :1246-1410 */
+#pragma omp parallel for private(p) reduction(+ : ve_fail, vp_fail) schedule(dynamic, 256)
     for (c = 0; c < nv; c++) {
         double VE = 0, sxz = 0, eta_phys = 0, eta = 0, zel = 0, zdi = 0, dexx = 0, dezz = 0, dgxz = 0, dp = 0, X = 0,
                OS = 0;

@@ -183,6 +183,8 @@ int orc_stokes_apply(const mdz_grid_desc *g, const mdz_fields *f, int jacobian, 
     double celvol = g->dx * g->dz;
     rates_t R = {0, 0, 0};
     if (jacobian) R = rates(g, u, v);
+    /* rows are independent: threaded loops give the serial loop's bits */
+#pragma omp parallel for schedule(static)
     for (int l = 0; l <= nz; l++)
         for (int k = 0; k < nx; k++) {
             int c = k + l * nx;
@@ -194,6 +196,7 @@ int orc_stokes_apply(const mdz_grid_desc *g, const mdz_fields *f, int jacobian, 
             }
             yu[c] = r;
         }
+#pragma omp parallel for schedule(static)
     for (int l = 0; l < nz; l++)
         for (int k = 0; k <= nx; k++) {
             int c = k + l * nxvz;
@@ -205,6 +208,7 @@ int orc_stokes_apply(const mdz_grid_desc *g, const mdz_fields *f, int jacobian, 
             }
             yv[c] = r;
         }
+#pragma omp parallel for schedule(static)
     for (int l = 0; l < ncz; l++)
         for (int k = 0; k < ncx; k++) {
             int c = k + l * ncx;

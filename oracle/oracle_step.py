@@ -151,9 +151,10 @@ def grid_props(g, mat, nph, pp, strain, cmul, tags, law):
     return 1.0 / imu, 1.0 / ibet, rho, d0, Cs * cmul, fs, ds
 
 
-def time_step(g, mat, model, markers, u, v, p, fields_out=None):
-    """markers: dict with x, z, phase, sxxd, szzd, sxz, strain_pl, strain, T, cmul (updated in place).
-    Returns (u, v, p, report dict)."""
+def project(g, mat, model, markers):
+    """The projections of a time step (P2Mastah calls of Main_DOODZ.c:501-594)
+    and the grid properties (ShearModCompExpGrid, CohesionFrictionDilationGrid):
+    returns (GridFields, Oracle holding the markers)."""
     import mdz
     nph = mat.n_phases
     f = mdz.GridFields(g, nph)
@@ -182,6 +183,35 @@ def time_step(g, mat, model, markers, u, v, p, fields_out=None):
         g, mat, nph, pn, f["strain_n"], cmul_n, g.BCp, model.softening)
     (f["mu_s"], f["bet_s"], f["rho_s"], _, f["C_s"], f["fric_s"], f["dil_s"]) = grid_props(
         g, mat, nph, ps, f["strain_s"], cmul_s, g.BCg, model.softening)
+    return f, o
+
+
+def first_defect(g, mat, model, markers, u, v, p, jacobian):
+    """State of a time step's first non-linear iteration: projections, BCs,
+    UpdateNonLinearity and the residual F (grid layout u | v | p), with the
+    Picard (jacobian 0) or Newton (jacobian 1) D-tensor in the fields."""
+    f, _ = project(g, mat, model, markers)
+    u = np.array(u, np.float64)
+    v = np.array(v, np.float64)
+    u[g.BCu == 0] = g.BCu_val[g.BCu == 0]
+    v[g.BCv == 0] = g.BCv_val[g.BCv == 0]
+    _mirror(g, u, v)
+    f["u"], f["v"], f["p"] = u, v, np.array(p, np.float64)
+    prm = model.rheo
+    orc.strain_rates(g, f)
+    orc.viscosity_grid(g, mat, prm, f)
+    orc.rhs(g, prm, model.gx, model.gz, f)
+    orc.rheo_operators(g, prm, f, 0)
+    orc.residual(g, f)
+    if jacobian:
+        orc.rheo_operators(g, prm, f, 1)
+    return f, np.concatenate([f["ru"], f["rv"], f["rp"]])
+
+
+def time_step(g, mat, model, markers, u, v, p, fields_out=None):
+    """markers: dict with x, z, phase, sxxd, szzd, sxz, strain_pl, strain, T, cmul (updated in place).
+    Returns (u, v, p, report dict)."""
+    f, o = project(g, mat, model, markers)
     u = np.array(u, np.float64)
     v = np.array(v, np.float64)
     p = np.array(p, np.float64)

@@ -30,6 +30,9 @@
  *   SOURCE/RheologyParticles.c:1124  UpdateParticleStress
  *   SOURCE/ParticleRoutines.c:3543   CountPartCell (RESEED = 1: marker reseeding)
  *   SOURCE/RheologyParticles.c:191   AccumulatedStrainII
+ *   SOURCE/RheologyParticles.c:1004  UpdateParticlePressure
+ *   SOURCE/RheologyDensity.c:1422    CohesionFrictionDilationGrid
+ *   SOURCE/RheologyDensity.c:1666    ShearModCompExpGrid
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -115,7 +118,7 @@ int ref_set_param(const char *name, double v) {
     P_D(dt) P_D(mineta) P_D(maxeta) P_D(gx) P_D(gz) P_D(EpsBG)
     P_I(iselastic) P_I(step) P_I(eta_avg) P_I(itp_stencil) P_I(compressible) P_I(Newton)
     P_I(isperiodic_x) P_I(StressUpdate) P_I(StressRotation) P_I(subgrid_diff) P_I(ConservInterp)
-    P_I(free_surf) P_I(aniso) P_I(loc_iter)
+    P_I(free_surf) P_I(aniso) P_I(loc_iter) P_I(Plith_trick)
 #undef P_D
 #undef P_I
     if (!strcmp(name, "scale_eta")) { g_scale.eta = v; return 0; }
@@ -157,7 +160,7 @@ double *ref_field(const char *name) {
     F(detadexx_n) F(detadezz_n) F(detadgxz_n) F(detadp_n) F(ddivpdexx_n) F(ddivpdezz_n) F(ddivpdgxz_n) F(ddivpdp_n)
     F(detadexx_s) F(detadezz_s) F(detadgxz_s) F(detadp_s)
     F(roger_x) F(roger_z) F(rhs_p) F(ru) F(rv) F(rp) F(gx) F(gz)
-    F(xg_coord) F(zg_coord) F(xc_coord) F(zc_coord) F(xvz_coord) F(zvx_coord)
+    F(xg_coord) F(zg_coord) F(xc_coord) F(zc_coord) F(xvz_coord) F(zvx_coord) F(dp) F(p_lith) F(p_lith0)
 #undef F
     if (!strcmp(name, "BCu_val")) return g_mesh.BCu.val;
     if (!strcmp(name, "BCv_val")) return g_mesh.BCv.val;
@@ -282,6 +285,13 @@ int ref_accumulated_strain(void) {
     return 0;
 }
 int ref_update_particle_stress(void) { UpdateParticleStress(&g_mesh, &g_parts, &g_model, &g_mat, &g_scale); return 0; }
+/* ShearModCompExpGrid and CohesionFrictionDilationGrid from the phase
+ * fractions already on the grid and the markers' strain_pl. */
+int ref_shear_mod_grid(void) { ShearModCompExpGrid(&g_mesh, g_mat, g_model, g_scale); return 0; }
+int ref_cohesion_grid(void) { CohesionFrictionDilationGrid(&g_mesh, &g_parts, g_mat, g_model, g_scale); return 0; }
+/* UpdateParticlePressure (no subgrid diffusion when subgrid_diff < 2) from
+ * p_in, p0_n and, with Plith_trick = 1, p_lith and p_lith0. */
+int ref_update_particle_pressure(void) { UpdateParticlePressure(&g_mesh, g_scale, g_model, &g_parts, &g_mat); return 0; }
 
 static void free_blocks(SparseMat *A, SparseMat *B, SparseMat *C, SparseMat *D) {
     FreeMat(A); FreeMat(B); FreeMat(C); FreeMat(D);

@@ -176,6 +176,15 @@ class RefMDOODZ:
     def update_particle_stress(self):
         self.lib.ref_update_particle_stress()
 
+    def update_particle_pressure(self):
+        self.lib.ref_update_particle_pressure()
+
+    def shear_mod_grid(self):
+        self.lib.ref_shear_mod_grid()
+
+    def cohesion_grid(self):
+        self.lib.ref_cohesion_grid()
+
     def setup_equations(self):
         self.lib.ref_setup_equations()
 

@@ -359,8 +359,84 @@ def make_reseed_fixture():
     np.savez_compressed(os.path.join(HERE, "reseed_ref.npz"), **out)
 
 
+# ---- grid properties (ShearModCompExpGrid, CohesionFrictionDilationGrid) ------------
+GRIDPROP_PHASES = [
+    # friction, dilation and cohesion all soften
+    dict(mu=1.0, bet=1e-2, C=1.0, phi=0.5, psi=0.1, C_end=0.5, phi_end=0.3, psi_end=0.0, pls_start=0.1, pls_end=0.9,
+         coh_soft=1, phi_soft=1, psi_soft=1),
+    # cohesion softening only, another strain window
+    dict(mu=2.0, bet=2e-2, C=2.0, phi=0.6, psi=0.0, C_end=0.2, phi_end=0.6, psi_end=0.0, pls_start=0.0, pls_end=0.5,
+         coh_soft=1, phi_soft=0, psi_soft=0),
+    # no softening
+    dict(mu=0.5, bet=5e-3, C=0.7, phi=0.4, psi=0.05, C_end=0.7, phi_end=0.4, psi_end=0.05, pls_start=0.0,
+         pls_end=1.0, coh_soft=0, phi_soft=0, psi_soft=0),
+]
+
+
+def make_gridprops_fixture():
+    """Phase fractions projected from the markers, then the reference's
+    ShearModCompExpGrid (harmonic shear modulus and compressibility) and
+    CohesionFrictionDilationGrid (smooth softening by the markers' plastic
+    strain: P2Mastah to the centroids, Interp_P2N to the vertices), for
+    itp_stencil 1 and 9."""
+    g = _grid()
+    x, z, ph = _markers(g)
+    rng = np.random.default_rng(31)
+    strain_pl = np.abs(rng.normal(0.5, 0.4, len(x)))
+    out = dict(Nx=NX, Nz=NZ, box=np.array([XMIN, XMAX, ZMIN, ZMAX]), x=x, z=z, phase=ph, strain_pl=strain_pl)
+    for stencil in (1, 9):
+        r = RefMDOODZ(NX, NZ, XMIN, XMAX, ZMIN, ZMAX, 3)
+        r.set_bc_pureshear(1.0)
+        r.set_param("itp_stencil", stencil)
+        for p, props in enumerate(GRIDPROP_PHASES):
+            for k, v in props.items():
+                r.set_mat(k, p, v)
+        r.set_markers(x, z, ph)
+        r.marker_field("strain_pl")[:] = strain_pl
+        for centroid in (1, 0):
+            r.p2g(np.zeros(3), 0, 0, 1, centroid, stencil)
+            out["s%d_pp_c%d" % (stencil, centroid)] = np.array([r.phase_perc(centroid, p).copy() for p in range(3)])
+        r.shear_mod_grid()
+        r.cohesion_grid()
+        for k in ("mu_n", "mu_s", "bet_n", "bet_s", "C_n", "C_s", "fric_n", "fric_s", "dil_n", "dil_s"):
+            out["s%d_%s" % (stencil, k)] = r.field(k).copy()
+    np.savez_compressed(os.path.join(HERE, "gridprops_ref.npz"), **out)
+    print("gridprops_ref.npz:", len(out), "arrays")
+
+
+def make_pressure_fixture():
+    """UpdateParticlePressure: marker pressures plus the centroid increment
+    p_in - p0_n (Plith_trick 0) or its dynamic part (Plith_trick 1), without
+    subgrid diffusion."""
+    g = _grid()
+    x, z, ph = _markers(g)
+    rng = np.random.default_rng(41)
+    nc = (NX - 1) * (NZ - 1)
+    flds = dict(p_in=rng.normal(size=nc), p0_n=rng.normal(size=nc), p_lith=rng.normal(size=nc),
+                p_lith0=rng.normal(size=nc))
+    P0 = rng.normal(size=len(x))
+    out = dict(Nx=NX, Nz=NZ, box=np.array([XMIN, XMAX, ZMIN, ZMAX]), x=x, z=z, phase=ph, P0=P0, **flds)
+    for trick in (0, 1):
+        r = RefMDOODZ(NX, NZ, XMIN, XMAX, ZMIN, ZMAX, 3)
+        r.set_bc_pureshear(1.0)
+        r.set_param("Plith_trick", trick)
+        r.set_param("subgrid_diff", 0)
+        r.set_markers(x, z, ph)
+        r.marker_field("P")[:] = P0
+        for k, v in flds.items():
+            r.field(k)[:] = v
+        r.update_particle_pressure()
+        out["P_trick%d" % trick] = r.marker_field("P").copy()
+    np.savez_compressed(os.path.join(HERE, "pressure_ref.npz"), **out)
+    print("pressure_ref.npz:", len(out), "arrays")
+
+
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["markers", "rheology", "reseed", "strain", "stress"]
+    what = sys.argv[1:] or ["markers", "rheology", "reseed", "strain", "stress", "gridprops", "pressure"]
+    if "gridprops" in what:
+        make_gridprops_fixture()
+    if "pressure" in what:
+        make_pressure_fixture()
     if "stress" in what:
         make_stress_fixture()
     if "strain" in what:

@@ -101,3 +101,31 @@ def test_fp32_refined_matches_fp64():
     assert a[4] <= 1e-10 and b[4] <= 1e-4
     for x, y in zip(a[:2], b[:2]):
         assert _rel(y, x) < 1e-3
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_newton_defect_solve_vs_direct(precision):
+    """The Newton-Jacobian defect equation of the lithosphere model's first
+    non-linear iteration (dislocation + diffusion creep with their viscosity
+    tangents, elasticity; plasticity off so that the Jacobian's pressure Schur
+    complement stays definite): the matrix-free GCR solve against a direct
+    solve of the oracle's assembled Jacobian, pressure mean fixed to zero."""
+    import mdz_setups
+    import oracle_step
+    cfg = mdz_setups.config_lithosphere(Nx=65, Nz=33, precision=precision)
+    for p in range(cfg["mat"].n_phases):
+        cfg["mat"].C[p] = 1e90
+    g = cfg["grid"]
+    f, F = oracle_step.first_defect(g, cfg["mat"], cfg["model"], cfg["markers"], cfg["u"], cfg["v"], cfg["p"], 1)
+    assert np.abs(f["detadexx_n"]).max() > 0   # the tangent is in the operator
+    want = oracle_step.solve_defect(g, f, 1, F)
+    nu, nv = g.size(-1), g.size(-2)
+    Fu, Fv, Fp = F[:nu], F[nu:nu + nv], F[nu + nv:].copy()
+    Fp[g.BCp == -1] -= Fp[g.BCp == -1].mean()
+    ctx = mdz.Context(g, cfg["mat"].n_phases, 1)
+    du, dv, dp, its, rel = ctx.SolveStokesDefect(f, 1, precision, 1e-11, 400, Fu, Fv, Fp)
+    ctx.close()
+    assert rel <= 1e-11, (rel, its)
+    wu, wv, wp = want[:nu], want[nu:nu + nv], want[nu + nv:]
+    assert _rel(du, wu) < 1e-8 and _rel(dv, wv) < 1e-8
+    assert _rel(dp - dp.mean(), wp - wp.mean()) < 1e-8
