@@ -267,7 +267,7 @@ def mlp_workload():
 def e2e_form(cfg_builder, precision, learned, steps, size, warmup):
     """Same step through the public API with the marker state owned by the
     host, as in the reference's time loop: every step uploads the markers
-    (positions, phases, the seven attributes), runs the step and downloads the
+    (positions, phases, the eight attributes), runs the step and downloads the
     advected markers, their velocities, the updated attributes and the grid
     velocity into the same host arrays, which the next step uploads again.
     The host arrays hold the run's marker capacity (reseeding changes the
@@ -287,7 +287,7 @@ def e2e_form(cfg_builder, precision, learned, steps, size, warmup):
     g = cfg["grid"]
     n = len(m["x"])
     attrs = ((mdz.M_SXXD, "sxxd"), (mdz.M_SZZD, "szzd"), (mdz.M_SXZ, "sxz"), (mdz.M_STRAIN_PL, "strain_pl"),
-             (mdz.M_STRAIN, "strain"), (mdz.M_T, "T"), (mdz.M_CMUL, "cmul"))
+             (mdz.M_STRAIN, "strain"), (mdz.M_T, "T"), (mdz.M_CMUL, "cmul"), (mdz.M_P, "P"))
     hin = {"x": np.zeros(cap), "z": np.zeros(cap), "phase": np.full(cap, -1, np.int32)}   # the caller's arrays
     for _, key in attrs:
         hin[key] = np.zeros(cap)

@@ -163,10 +163,11 @@ mdz_status mdz_count_markers(mdz_ctx *ctx, int *nb_part_cell, int *nb_part_vert,
  * markers (particles.min_part_cell) gets one marker at its centre
  * (AddPartCell2 :977-1030).  The new marker copies the phase, velocity and
  * strains of the nearest marker within two quarter cells (FindClosestPhase2
- * :841-890); its T and stresses come from that marker (direct_neighbour = 1)
- * or from the grid fields T_n, sxxd_n, szzd_n (centroids) and sxz_s
- * (vertices) (direct_neighbour = 0, model.DirectNeighbour; host arrays, which
- * may be NULL when direct_neighbour = 1) (AssignMarkerProperties :648-762).
+ * :841-890); its T, pressure and stresses come from that marker
+ * (direct_neighbour = 1) or from the grid fields T_n, sxxd_n, szzd_n, p_n
+ * (centroids: p_n is the grid pressure p_in) and sxz_s (vertices)
+ * (direct_neighbour = 0, model.DirectNeighbour; host arrays, which may be NULL
+ * when direct_neighbour = 1) (AssignMarkerProperties :648-762).
  * New markers fill the slots of inactive markers (phase -1) first and are
  * then appended; n_added (may be NULL) receives their number.
  * MDZ_ERR_CAPACITY if they do not fit in the context's capacity (the
@@ -176,7 +177,8 @@ mdz_status mdz_count_markers(mdz_ctx *ctx, int *nb_part_cell, int *nb_part_vert,
  * implemented (the context rejects them); MDZ_ERR_UNSUPPORTED for grids whose
  * (2 (Nx - 1) + 4)(2 (Nz - 1) + 4) quarter cells exceed 2^31. */
 mdz_status mdz_CountPartCell(mdz_ctx *ctx, int reseed, int min_part_cell, int direct_neighbour, const double *T_n,
-                             const double *sxxd_n, const double *szzd_n, const double *sxz_s, int *n_added);
+                             const double *sxxd_n, const double *szzd_n, const double *sxz_s, const double *p_n,
+                             int *n_added);
 
 /* ---- grid -> marker interpolation ---------------------------------------- */
 
@@ -371,15 +373,21 @@ mdz_status mdz_EvaluateStokesResidualDecoupled(mdz_ctx *ctx, mdz_fields *f, doub
  * rp ((Nx-1)*(Nz-1)) and their tag arrays; norms3 is a device array of 3
  * doubles written on `stream` (a cudaStream_t; NULL = legacy default stream).
  * Scratch: a static device array of 8192 * 6 doubles (384 KiB), one slot per
- * index-box row; grids with Nz + 1 > 8192 rows are rejected with
- * MDZ_ERR_CAPACITY.  No scratch value has to start at zero (every slot a call
- * reads is written by that call first) and the result is bitwise
- * reproducible.  The first call on a device looks the scratch address up
- * (cudaGetSymbolAddress, with that device current): make it once before any
- * stream capture.  The scratch is shared, so calls that overlap in time
- * (several streams or host threads on one device) race and must be
- * serialised.  Status only (no context for a message): MDZ_ERR_ARG for a
- * null pointer or Nx, Nz < 3, MDZ_ERR_CUDA for a launch error. */
+ * index-box row; grids with Nz + 1 > 8192 rows, or whose Vx/Vz index
+ * boxes exceed 32-bit indices, are rejected with MDZ_ERR_CAPACITY.  No
+ * scratch value has to start at zero (every slot a call reads is written by
+ * that call first) and the result is bitwise reproducible.  The first call on
+ * a device looks the scratch address up (cudaGetSymbolAddress, with that
+ * device current): make it once before any stream capture.  That address is
+ * kept for the life of the process; after a cudaDeviceReset (or anything else
+ * that tears down the device's primary context) it is stale, and this entry
+ * point must not be called again in that process.  The scratch is shared, so
+ * calls that overlap in time (several streams or host threads on one device)
+ * race and must be serialised.  Status only (no context for a message):
+ * MDZ_ERR_ARG for a null pointer or Nx, Nz < 3, MDZ_ERR_CAPACITY for a grid
+ * above the limits, MDZ_ERR_CUDA for a launch error -- including an earlier
+ * asynchronous error still pending on the device, which the launch check
+ * reports (and clears) here. */
 mdz_status mdz_dev_residual_norms_noalloc(int Nx, int Nz, const double *ru, const double *rv, const double *rp,
                                           const signed char *BCu, const signed char *BCv, const signed char *BCp,
                                           double *norms3, void *stream);
@@ -436,11 +444,31 @@ mdz_status mdz_mg_stencils(mdz_ctx *ctx, int precision, int level, int *levels, 
 /* Per-marker attributes kept on the device next to x, z, phase (the marker
  * arrays of the reference, SOURCE/header_MDOODZ.h:66-78).  MDZ_M_CMUL is a
  * per-marker cohesion multiplier (harness extension: seeded cohesion noise;
- * 1 reproduces the reference). */
+ * 1 reproduces the reference).  MDZ_M_P is the marker pressure
+ * (particles.P): the time step projects it to p0_n and adds the step's
+ * pressure increment to it (UpdateParticlePressure). */
 enum {
     MDZ_M_SXXD = 0, MDZ_M_SZZD = 1, MDZ_M_SXZ = 2, MDZ_M_STRAIN_PL = 3, MDZ_M_STRAIN = 4, MDZ_M_T = 5,
-    MDZ_M_CMUL = 6, MDZ_M_NATTR = 7
+    MDZ_M_CMUL = 6, MDZ_M_P = 7, MDZ_M_NATTR = 8
 };
+/* UpdateParticlePressure (SOURCE/RheologyParticles.c:1004-1123) with
+ * Plith_trick = 0 and no subgrid diffusion (subgrid_diff < 2, the reference's
+ * defaults): dp = p - p0_n on every centroid whose tag is not 30 (f->p is the
+ * reference's p_in, f->p0_n the pressure projected from the markers at the
+ * start of the step; host arrays), interpolated to the resident active
+ * markers (Interp_Grid2P_centroids2) and added to their MDZ_M_P. */
+mdz_status mdz_UpdateParticlePressure(mdz_ctx *ctx, mdz_fields *f);
+/* UpdateParticleStress (SOURCE/RheologyParticles.c:1124-1447), StressUpdate =
+ * 0 without rotation and subgrid diffusion: the increments sxxd - sxxd0,
+ * szzd - szzd0 (centroids, not on air) and sxz - sxz0 (vertices) of the host
+ * fields in f, interpolated to the resident markers and added to MDZ_M_SXXD,
+ * MDZ_M_SZZD, MDZ_M_SXZ. */
+mdz_status mdz_UpdateParticleStress(mdz_ctx *ctx, mdz_fields *f);
+/* AccumulatedStrainII (SOURCE/RheologyParticles.c:191-537): dt times the
+ * centroid strain-rate invariants of f (eII_el + eII_pl + eII_pwl + eII_lin +
+ * eII_cst, and eII_pl alone), interpolated to the resident markers and added
+ * to MDZ_M_STRAIN and MDZ_M_STRAIN_PL. */
+mdz_status mdz_AccumulatedStrainII(mdz_ctx *ctx, mdz_fields *f, double dt);
 mdz_status mdz_set_marker_attr(mdz_ctx *ctx, int attr, int n, const double *values);
 mdz_status mdz_get_marker_attr(mdz_ctx *ctx, int attr, int n, double *values);
 

@@ -121,6 +121,12 @@ extern "C" mdz_status mdz_load_breakpoint(mdz_ctx *ctx, const char *path) {
         MDZ_CUDA(ctx, cudaMemcpy(ctx->d.u, fl.data(), sizeof(double) * nu, cudaMemcpyHostToDevice));
         MDZ_CUDA(ctx, cudaMemcpy(ctx->d.v, fl.data() + nu, sizeof(double) * nv, cudaMemcpyHostToDevice));
         MDZ_CUDA(ctx, cudaMemcpy(ctx->d.p, fl.data() + nu + nv, sizeof(double) * np, cudaMemcpyHostToDevice));
+    } else if (ctx->fields_ready) {
+        // saved before any field existed: the saving context's u, v, p were
+        // zero, so a context that has stepped since must not keep its own
+        MDZ_CUDA(ctx, cudaMemset(ctx->d.u, 0, sizeof(double) * nu));
+        MDZ_CUDA(ctx, cudaMemset(ctx->d.v, 0, sizeof(double) * nv));
+        MDZ_CUDA(ctx, cudaMemset(ctx->d.p, 0, sizeof(double) * np));
     }
     ctx->m.n = n;
     ctx->bins.valid = false;

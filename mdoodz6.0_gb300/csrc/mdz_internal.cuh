@@ -141,11 +141,12 @@ __global__ void k_bin_scatter(int n, const int *__restrict__ cell, const int *__
 __global__ void k_bin_sort_segments(int ncells, const int *__restrict__ start, int *__restrict__ sorted);
 
 // Marker reseeding (reseed.cu): the reseeding of CountPartCell on the resident
-// markers; T_n, sxxd_n, szzd_n (centroids) and sxz_s (vertices) are device
-// fields, read when direct = 0.
+// markers; T_n, sxxd_n, szzd_n, p_n (centroids) and sxz_s (vertices) are
+// device fields, read when direct = 0.
 struct mdz_attr_ptrs { double *a[MDZ_M_NATTR]; };
 mdz_status mdz_dev_reseed(mdz_ctx *ctx, int min_part_cell, int direct, const double *T_n, const double *sxxd_n,
-                          const double *szzd_n, const double *sxz_s, cudaStream_t st, int *n_added);
+                          const double *szzd_n, const double *sxz_s, const double *p_n, cudaStream_t st,
+                          int *n_added);
 void mdz_reseed_free(mdz_ctx *ctx);
 
 // Every mdz_fields member with its node set (X-macro): VX / VZ velocity nodes,

@@ -77,7 +77,8 @@ __global__ void __launch_bounds__(256) k_noalloc_norms(int nrows, const double *
     }
 }
 
-// Scratch address per device, looked up once with that device current.
+// Scratch address per device, looked up once with that device current (kept
+// for the process: stale after the device's primary context is torn down).
 static double *g_noalloc_ptr[64];
 
 extern "C" mdz_status mdz_dev_residual_norms_noalloc(int Nx, int Nz, const double *ru, const double *rv,
@@ -86,6 +87,7 @@ extern "C" mdz_status mdz_dev_residual_norms_noalloc(int Nx, int Nz, const doubl
                                                      double *norms3, void *stream) {
     if (Nx < 3 || Nz < 3 || !ru || !rv || !rp || !BCu || !BCv || !BCp || !norms3) return MDZ_ERR_ARG;
     if (Nz + 1 > NOALLOC_MAX_ROWS) return MDZ_ERR_CAPACITY;   // scratch holds NOALLOC_MAX_ROWS index-box rows
+    if ((long long)(Nx + 1) * (Nz + 1) > 2147483647LL) return MDZ_ERR_CAPACITY;   // the kernels' 32-bit indices
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return MDZ_ERR_CUDA;
     if (!g_noalloc_ptr[dev]) {

@@ -21,7 +21,7 @@
 //                  (the reference's k-outer, l-inner loop); the first ones
 //                  take the slots of inactive markers in index order, the
 //                  rest are appended (:4285-4330): two scans;
-//   properties     phase, velocity and strains are copied, T and the stresses
+//   properties     phase, velocity and strains are copied, T, P and the stresses
 //                  copied (DirectNeighbour = 1) or interpolated from the grid
 //                  (Centers2Particle :259-455, Vertices2Particle :461-520)
 //                  (AssignMarkerProperties :648-762).  The cohesion multiplier
@@ -220,7 +220,7 @@ __device__ double v2p_vertices(const mdz_dgrid &g, double x, double z, const dou
 }
 
 struct reseed_fields {
-    const double *T_n, *sxxd_n, *szzd_n, *sxz_s;
+    const double *T_n, *sxxd_n, *szzd_n, *sxz_s, *p_n;
 };
 
 // One thread per new marker r: its quarter cell, the nearest of the markers
@@ -263,11 +263,13 @@ __global__ void k_reseed_write(quarter_geom q, mdz_dgrid g, int n, int nnew, int
     A.a[MDZ_M_CMUL][slot] = A.a[MDZ_M_CMUL][m];
     if (direct) {
         A.a[MDZ_M_T][slot] = A.a[MDZ_M_T][m];
+        A.a[MDZ_M_P][slot] = A.a[MDZ_M_P][m];
         A.a[MDZ_M_SXXD][slot] = A.a[MDZ_M_SXXD][m];
         A.a[MDZ_M_SZZD][slot] = A.a[MDZ_M_SZZD][m];
         A.a[MDZ_M_SXZ][slot] = A.a[MDZ_M_SXZ][m];
     } else {
         A.a[MDZ_M_T][slot] = c2p(g, xn, zn, F.T_n);
+        A.a[MDZ_M_P][slot] = c2p(g, xn, zn, F.p_n);
         A.a[MDZ_M_SXXD][slot] = c2p(g, xn, zn, F.sxxd_n);
         A.a[MDZ_M_SZZD][slot] = c2p(g, xn, zn, F.szzd_n);
         A.a[MDZ_M_SXZ][slot] = v2p_vertices(g, xn, zn, F.sxz_s);
@@ -317,11 +319,12 @@ static mdz_status reseed_ws(mdz_ctx *ctx, const quarter_geom &q, mdz_reseed_ws *
 }
 
 mdz_status mdz_dev_reseed(mdz_ctx *ctx, int min_part_cell, int direct, const double *T_n, const double *sxxd_n,
-                          const double *szzd_n, const double *sxz_s, cudaStream_t st, int *n_added) {
+                          const double *szzd_n, const double *sxz_s, const double *p_n, cudaStream_t st,
+                          int *n_added) {
     if (n_added) *n_added = 0;
     if (min_part_cell < 0) return mdz_fail(ctx, MDZ_ERR_ARG, "CountPartCell: min_part_cell < 0");
-    if (!direct && (!T_n || !sxxd_n || !szzd_n || !sxz_s))
-        return mdz_fail(ctx, MDZ_ERR_ARG, "CountPartCell: DirectNeighbour = 0 needs T, sxxd, szzd and sxz");
+    if (!direct && (!T_n || !sxxd_n || !szzd_n || !sxz_s || !p_n))
+        return mdz_fail(ctx, MDZ_ERR_ARG, "CountPartCell: DirectNeighbour = 0 needs T, sxxd, szzd, sxz and p");
     const quarter_geom q = make_quarter_geom(ctx);
     // quarter-cell indices are 32-bit: (2 Ncx + 4)(2 Ncz + 4) must stay below 2^31
     if ((long long)q.nxl * q.nzl > 2147483000LL)
@@ -380,7 +383,7 @@ mdz_status mdz_dev_reseed(mdz_ctx *ctx, int min_part_cell, int direct, const dou
         k_reseed_write<<<mdz_blocks(nnew), MDZ_THREADS, 0, st>>>(q, ctx->g, n, nnew, nreuse, W->src, W->qstart,
                                                                  W->qsorted, W->reuse, ctx->m.x, ctx->m.z,
                                                                  ctx->m.phase, ctx->m.vx, ctx->m.vz, A, direct,
-                                                                 reseed_fields{T_n, sxxd_n, szzd_n, sxz_s});
+                                                                 reseed_fields{T_n, sxxd_n, szzd_n, sxz_s, p_n});
         MDZ_LAUNCHED(ctx);
     }
     ctx->m.n = (int)n_final;
@@ -391,28 +394,29 @@ mdz_status mdz_dev_reseed(mdz_ctx *ctx, int min_part_cell, int direct, const dou
 
 extern "C" mdz_status mdz_CountPartCell(mdz_ctx *ctx, int reseed, int min_part_cell, int direct_neighbour,
                                         const double *T_n, const double *sxxd_n, const double *szzd_n,
-                                        const double *sxz_s, int *n_added) {
+                                        const double *sxz_s, const double *p_n, int *n_added) {
     if (!ctx) return MDZ_ERR_ARG;
     if (n_added) *n_added = 0;
     if (!reseed) return MDZ_OK;
     cudaStream_t st = ctx->stream;
     const mdz_dgrid &g = ctx->g;
     const size_t nc = (size_t)g.ncx * g.ncz, nv = (size_t)g.Nx * g.Nz;
-    const double *d[4] = {nullptr, nullptr, nullptr, nullptr};
+    const double *d[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     if (!direct_neighbour) {
-        if (!T_n || !sxxd_n || !szzd_n || !sxz_s)
-            return mdz_fail(ctx, MDZ_ERR_ARG, "CountPartCell: DirectNeighbour = 0 needs T, sxxd, szzd and sxz");
-        const double *hsrc[4] = {T_n, sxxd_n, szzd_n, sxz_s};
-        for (int i = 0; i < 4; i++) {
+        if (!T_n || !sxxd_n || !szzd_n || !sxz_s || !p_n)
+            return mdz_fail(ctx, MDZ_ERR_ARG, "CountPartCell: DirectNeighbour = 0 needs T, sxxd, szzd, sxz and p");
+        const double *hsrc[5] = {T_n, sxxd_n, szzd_n, sxz_s, p_n};
+        static const int slot[5] = {0, 1, 2, 3, 6};   // staging slots (5 holds the time step's workspace)
+        for (int i = 0; i < 5; i++) {
             const size_t cnt = i == 3 ? nv : nc;
-            double *p = (double *)mdz_stage(ctx, i, sizeof(double) * cnt);
+            double *p = (double *)mdz_stage(ctx, slot[i], sizeof(double) * cnt);
             if (!p) return mdz_fail(ctx, MDZ_ERR_CUDA, "CountPartCell: staging allocation failed");
             MDZ_CUDA(ctx, cudaMemcpyAsync(p, hsrc[i], sizeof(double) * cnt, cudaMemcpyHostToDevice, st));
             d[i] = p;
         }
     }
     int added = 0;
-    mdz_status s = mdz_dev_reseed(ctx, min_part_cell, direct_neighbour, d[0], d[1], d[2], d[3], st, &added);
+    mdz_status s = mdz_dev_reseed(ctx, min_part_cell, direct_neighbour, d[0], d[1], d[2], d[3], d[4], st, &added);
     if (s != MDZ_OK) return s;
     MDZ_CUDA(ctx, cudaStreamSynchronize(st));
     if (n_added) *n_added = added;

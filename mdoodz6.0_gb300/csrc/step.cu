@@ -144,13 +144,16 @@ __global__ void k_copy3(int nu, int nv, int np, const double *__restrict__ a, co
 
 // stress increments on the grid (UpdateParticleStress, no-subgrid branch :1397-1420)
 // and strain increments (AccumulatedStrainII :205-219)
+// and the pressure increment of UpdateParticlePressure (RheologyParticles.c:
+// 1004-1030, Plith_trick = 0: p_in - p0_n where the tag is not 30)
 __global__ void k_increments(mdz_dgrid g, double dt, mdz_fields f, double *__restrict__ dsxx,
                              double *__restrict__ dszz, double *__restrict__ dsxz, double *__restrict__ dstrain,
-                             double *__restrict__ dstrain_pl) {
+                             double *__restrict__ dstrain_pl, double *__restrict__ dp) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int nc = g.ncx * g.ncz, nv = g.Nx * g.Nz;
     if (i < nc) {
         bool act = g.BCp[i] != 30 && g.BCp[i] != 31;
+        dp[i] = g.BCp[i] != 30 ? f.p[i] - f.p0_n[i] : 0.0;
         dsxx[i] = act ? f.sxxd[i] - f.sxxd0[i] : 0.0;
         dszz[i] = act ? f.szzd[i] - f.szzd0[i] : 0.0;
         dstrain[i] = dt * (f.eII_pl[i] + f.eII_pwl[i] + f.eII_lin[i] + f.eII_el[i] + f.eII_cst[i]);
@@ -167,17 +170,19 @@ __global__ void k_marker_update(int n, mdz_dgrid g, const double *__restrict__ m
                                 const int *__restrict__ mph, const double *__restrict__ dsxx,
                                 const double *__restrict__ dszz, const double *__restrict__ dsxz,
                                 const double *__restrict__ dstrain, const double *__restrict__ dstrain_pl,
-                                double *__restrict__ sxx, double *__restrict__ szz, double *__restrict__ sxz,
-                                double *__restrict__ strain, double *__restrict__ strain_pl, int what) {
+                                const double *__restrict__ dp, double *__restrict__ sxx, double *__restrict__ szz,
+                                double *__restrict__ sxz, double *__restrict__ strain, double *__restrict__ strain_pl,
+                                double *__restrict__ P, int what) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n || mph[k] == -1) return;
     const double x = mx[k], z = mz[k], dx = g.dx, dz = g.dz, idx = g.idx, idz = g.idz;
     const int ncx = g.ncx, ncz = g.ncz, Nx = g.Nx, Nz = g.Nz;
     // what & 1: stress increments (UpdateParticleStress, before the advection);
     // what & 2: strain increments (AccumulatedStrainII, after it, at the
-    // advected positions; markers that left the box are skipped)
+    // advected positions; markers that left the box are skipped);
+    // what & 4: pressure increment (UpdateParticlePressure, before the advection)
     // centroids, ghosted frame (Interp_Grid2P_centroids2, non-periodic)
-    if (what & 1) {
+    if (what & 5) {
         int jp = (int)ceil_quot(x - g.xvz[0], dx, idx, 0.0) - 1, ip = (int)ceil_quot(z - g.zvx[0], dz, idz, 0.0) - 1;
         int jw = jp - 1, je = jp, is = ip - 1, in_ = ip;
         if (jp <= 0) { jw = 0; je = 0; }
@@ -193,8 +198,11 @@ __global__ void k_marker_update(int n, mdz_dgrid g, const double *__restrict__ m
         const signed char *t = g.BCp;
         int sSW = is_air(t[SW]) ? NW : SW, sSE = is_air(t[SE]) ? NE : SE;
         int sNW = is_air(t[NW]) ? SW : NW, sNE = is_air(t[NE]) ? SE : NE;
-        sxx[k] += wSW * dsxx[sSW] + wSE * dsxx[sSE] + wNW * dsxx[sNW] + wNE * dsxx[sNE];
-        szz[k] += wSW * dszz[sSW] + wSE * dszz[sSE] + wNW * dszz[sNW] + wNE * dszz[sNE];
+        if (what & 1) {
+            sxx[k] += wSW * dsxx[sSW] + wSE * dsxx[sSE] + wNW * dsxx[sNW] + wNE * dsxx[sNE];
+            szz[k] += wSW * dszz[sSW] + wSE * dszz[sSE] + wNW * dszz[sNW] + wNE * dszz[sNE];
+        }
+        if (what & 4) P[k] += wSW * dp[sSW] + wSE * dp[sSE] + wNW * dp[sNW] + wNE * dp[sNE];
     }
     // vertices (Interp_Grid2P)
     if (what & 1) {
@@ -320,14 +328,14 @@ static bool converged(const mdz_model *M, const double *r, const double *r0) {
 struct step_buffers {
     double *F = nullptr, *dx = nullptr, *u0 = nullptr, *v0 = nullptr, *p0 = nullptr;
     double *cmul_n = nullptr, *cmul_s = nullptr;
-    double *dsxx = nullptr, *dszz = nullptr, *dsxz = nullptr, *dstr = nullptr, *dstr_pl = nullptr;
+    double *dsxx = nullptr, *dszz = nullptr, *dsxz = nullptr, *dstr = nullptr, *dstr_pl = nullptr, *dp = nullptr;
 };
 
 static mdz_status step_buffers_get(mdz_ctx *ctx, step_buffers &B) {
     const mdz_dgrid &g = ctx->g;
     size_t nu = (size_t)g.Nx * (g.Nz + 1), nv = (size_t)(g.Nx + 1) * g.Nz, np = (size_t)g.ncx * g.ncz;
     size_t ng = (size_t)g.Nx * g.Nz, n = nu + nv + np;
-    size_t total = 2 * n + nu + nv + np + np + ng + 3 * np + ng + np;
+    size_t total = 2 * n + nu + nv + np + np + ng + 3 * np + ng + np + np;
     double *b = (double *)mdz_stage(ctx, 5, sizeof(double) * total);
     if (!b) return mdz_fail(ctx, MDZ_ERR_CUDA, "time step: workspace allocation failed");
     B.F = b; b += n;
@@ -342,6 +350,7 @@ static mdz_status step_buffers_get(mdz_ctx *ctx, step_buffers &B) {
     B.dstr = b; b += np;
     B.dsxz = b; b += ng;
     B.dstr_pl = b; b += np;
+    B.dp = b; b += np;
     return MDZ_OK;
 }
 
@@ -370,11 +379,13 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
     ctx->p2g_empty = d_empty;
     {
         step_timer T(st, &R.ms_projection);
-        const double *cv[5] = {ctx->m.attr[MDZ_M_SXXD], ctx->m.attr[MDZ_M_SZZD], ctx->m.attr[MDZ_M_T],
-                               ctx->m.attr[MDZ_M_STRAIN_PL], ctx->m.attr[MDZ_M_CMUL]};
-        double *co[5] = {f.sxxd0, f.szzd0, f.T, f.strain_n, B.cmul_n};
-        int avg[5] = {0, 0, 0, 0, 0};
-        if ((s = mdz_dev_p2g(ctx, 5, cv, avg, co, f.phase_perc_n, MDZ_NODES_CENTROIDS, M->itp_stencil, st)) != MDZ_OK)
+        // centroids: old stresses, T, plastic strain, cohesion multiplier and the
+        // markers' pressure (p0_n, Main_DOODZ.c:593)
+        const double *cv[6] = {ctx->m.attr[MDZ_M_SXXD], ctx->m.attr[MDZ_M_SZZD], ctx->m.attr[MDZ_M_T],
+                               ctx->m.attr[MDZ_M_STRAIN_PL], ctx->m.attr[MDZ_M_CMUL], ctx->m.attr[MDZ_M_P]};
+        double *co[6] = {f.sxxd0, f.szzd0, f.T, f.strain_n, B.cmul_n, f.p0_n};
+        int avg[6] = {0, 0, 0, 0, 0, 0};
+        if ((s = mdz_dev_p2g(ctx, 6, cv, avg, co, f.phase_perc_n, MDZ_NODES_CENTROIDS, M->itp_stencil, st)) != MDZ_OK)
             return s;
         // vertices: the softening reads the plastic strain as Interp_P2N gives it
         // (RheologyDensity.c:1545, the one-cell stencil whatever itp_stencil),
@@ -578,28 +589,29 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
         step_timer T(st, &R.ms_markers);
         int nn = np > nvert ? np : nvert;
         k_increments<<<mdz_blocks(nn), MDZ_THREADS, 0, st>>>(g, M->rheo.dt, f, B.dsxx, B.dszz, B.dsxz, B.dstr,
-                                                            B.dstr_pl);
+                                                            B.dstr_pl, B.dp);
         MDZ_LAUNCHED(ctx);
         int n = ctx->m.n;
         if (n > 0) {
+            // UpdateParticleStress and UpdateParticlePressure (Main_DOODZ.c:1010-1013)
             k_marker_update<<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(
-                n, g, ctx->m.x, ctx->m.z, ctx->m.phase, B.dsxx, B.dszz, B.dsxz, B.dstr, B.dstr_pl,
+                n, g, ctx->m.x, ctx->m.z, ctx->m.phase, B.dsxx, B.dszz, B.dsxz, B.dstr, B.dstr_pl, B.dp,
                 ctx->m.attr[MDZ_M_SXXD], ctx->m.attr[MDZ_M_SZZD], ctx->m.attr[MDZ_M_SXZ], ctx->m.attr[MDZ_M_STRAIN],
-                ctx->m.attr[MDZ_M_STRAIN_PL], 1);
+                ctx->m.attr[MDZ_M_STRAIN_PL], ctx->m.attr[MDZ_M_P], 1 | 4);
             MDZ_LAUNCHED(ctx);
         }
         if ((s = mdz_dev_rk4(ctx, f.u, f.v, M->rheo.dt, st)) != MDZ_OK) return s;
         // AccumulatedStrainII after the advection (Main_DOODZ.c:1134-1140)
         if (n > 0) {
             k_marker_update<<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(
-                n, g, ctx->m.x, ctx->m.z, ctx->m.phase, B.dsxx, B.dszz, B.dsxz, B.dstr, B.dstr_pl,
+                n, g, ctx->m.x, ctx->m.z, ctx->m.phase, B.dsxx, B.dszz, B.dsxz, B.dstr, B.dstr_pl, B.dp,
                 ctx->m.attr[MDZ_M_SXXD], ctx->m.attr[MDZ_M_SZZD], ctx->m.attr[MDZ_M_SXZ], ctx->m.attr[MDZ_M_STRAIN],
-                ctx->m.attr[MDZ_M_STRAIN_PL], 2);
+                ctx->m.attr[MDZ_M_STRAIN_PL], nullptr, 2);
             MDZ_LAUNCHED(ctx);
         }
         // reseeding after the advection (Main_DOODZ.c:1233-1236)
         if (M->reseed)
-            if ((s = mdz_dev_reseed(ctx, M->min_part_cell, M->direct_neighbour, f.T, f.sxxd, f.szzd, f.sxz, st,
+            if ((s = mdz_dev_reseed(ctx, M->min_part_cell, M->direct_neighbour, f.T, f.sxxd, f.szzd, f.sxz, f.p, st,
                                     &R.markers_added)) != MDZ_OK)
                 return s;
     }
@@ -691,6 +703,62 @@ static mdz_status grid_props_host(mdz_ctx *ctx, const mdz_materials *mat, int it
     }
     static const char *const names[] = {"mu_n", "mu_s", "bet_n", "bet_s"};
     return mdz_download_fields(ctx, h, names, 4, st);
+}
+
+// Host drop-ins of the marker updates on the resident markers: the grid
+// fields named are uploaded from h, the increments formed on the device and
+// interpolated to the markers (what: 1 stresses, 2 strains, 4 pressure).
+static mdz_status marker_update_host(mdz_ctx *ctx, mdz_fields *h, const char *const *need, int nneed, int what,
+                                     double dt) {
+    mdz_status s = mdz_ensure_fields(ctx);
+    if (s != MDZ_OK) return s;
+    mdz_fields up{};   // upload exactly the fields this update reads
+    for (int i = 0; i < nneed; i++) {
+#define PICK(name, kind)                                                                         \
+        if (!strcmp(need[i], #name)) {                                                          \
+            if (!h->name) return mdz_fail(ctx, MDZ_ERR_ARG, "marker update: needs %s", #name);  \
+            up.name = h->name;                                                                  \
+        }
+        MDZ_FIELD_LIST(PICK)
+#undef PICK
+    }
+    cudaStream_t st = ctx->stream;
+    if ((s = mdz_upload_fields(ctx, &up, st)) != MDZ_OK) return s;
+    const mdz_dgrid &g = ctx->g;
+    const int np = g.ncx * g.ncz, nvert = g.Nx * g.Nz, nn = np > nvert ? np : nvert;
+    step_buffers B;
+    if ((s = step_buffers_get(ctx, B)) != MDZ_OK) return s;
+    k_increments<<<mdz_blocks(nn), MDZ_THREADS, 0, st>>>(g, dt, ctx->d, B.dsxx, B.dszz, B.dsxz, B.dstr, B.dstr_pl,
+                                                          B.dp);
+    MDZ_LAUNCHED(ctx);
+    const int n = ctx->m.n;
+    if (n > 0) {
+        k_marker_update<<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(
+            n, g, ctx->m.x, ctx->m.z, ctx->m.phase, B.dsxx, B.dszz, B.dsxz, B.dstr, B.dstr_pl, B.dp,
+            ctx->m.attr[MDZ_M_SXXD], ctx->m.attr[MDZ_M_SZZD], ctx->m.attr[MDZ_M_SXZ], ctx->m.attr[MDZ_M_STRAIN],
+            ctx->m.attr[MDZ_M_STRAIN_PL], ctx->m.attr[MDZ_M_P], what);
+        MDZ_LAUNCHED(ctx);
+    }
+    MDZ_CUDA(ctx, cudaStreamSynchronize(st));
+    return MDZ_OK;
+}
+
+extern "C" mdz_status mdz_UpdateParticlePressure(mdz_ctx *ctx, mdz_fields *h) {
+    if (!ctx || !h) return ctx ? mdz_fail(ctx, MDZ_ERR_ARG, "UpdateParticlePressure: null argument") : MDZ_ERR_ARG;
+    static const char *const need[] = {"p", "p0_n"};
+    return marker_update_host(ctx, h, need, 2, 4, 1.0);
+}
+
+extern "C" mdz_status mdz_UpdateParticleStress(mdz_ctx *ctx, mdz_fields *h) {
+    if (!ctx || !h) return ctx ? mdz_fail(ctx, MDZ_ERR_ARG, "UpdateParticleStress: null argument") : MDZ_ERR_ARG;
+    static const char *const need[] = {"sxxd", "szzd", "sxz", "sxxd0", "szzd0", "sxz0"};
+    return marker_update_host(ctx, h, need, 6, 1, 1.0);
+}
+
+extern "C" mdz_status mdz_AccumulatedStrainII(mdz_ctx *ctx, mdz_fields *h, double dt) {
+    if (!ctx || !h) return ctx ? mdz_fail(ctx, MDZ_ERR_ARG, "AccumulatedStrainII: null argument") : MDZ_ERR_ARG;
+    static const char *const need[] = {"eII_pl", "eII_pwl", "eII_lin", "eII_el", "eII_cst"};
+    return marker_update_host(ctx, h, need, 5, 2, dt);
 }
 
 extern "C" mdz_status mdz_ShearModCompExpGrid(mdz_ctx *ctx, const mdz_materials *mat, mdz_fields *f) {

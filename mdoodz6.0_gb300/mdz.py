@@ -271,15 +271,21 @@ class Context:
         return c, v, pc, pv
 
     def CountPartCell(self, reseed=1, min_part_cell=16, direct_neighbour=0, T_n=None, sxxd_n=None, szzd_n=None,
-                      sxz_s=None):
+                      sxz_s=None, p_n=None):
         """CountPartCell (SOURCE/ParticleRoutines.c:3543) with RESEED = reseed
         on the resident markers; returns the number of markers created."""
-        a = [None if v is None else np.ascontiguousarray(v, np.float64) for v in (T_n, sxxd_n, szzd_n, sxz_s)]
+        a = [None if v is None else np.ascontiguousarray(v, np.float64) for v in (T_n, sxxd_n, szzd_n, sxz_s, p_n)]
         added = C.c_int(0)
         self._check(self.L.mdz_CountPartCell(self.h, C.c_int(reseed), C.c_int(min_part_cell),
                                              C.c_int(direct_neighbour), *[_dptr(v) if v is not None else None for v in a],
                                              C.byref(added)))
         return added.value
+
+    def UpdateParticlePressure(self, fields):
+        """UpdateParticlePressure (SOURCE/RheologyParticles.c:1004): the resident
+        markers' pressure += the centroid increment p - p0_n of `fields`."""
+        s = fields.struct()
+        self._check(self.L.mdz_UpdateParticlePressure(self.h, C.byref(s)))
 
     def Interp_Grid2P(self, node_field, node_set):
         nf = np.ascontiguousarray(node_field, np.float64)
@@ -580,8 +586,8 @@ class RheoParams(C.Structure):
 
 
 # marker attributes (enum in include/mdoodz_gpu.h)
-M_SXXD, M_SZZD, M_SXZ, M_STRAIN_PL, M_STRAIN, M_T, M_CMUL = range(7)
-M_NATTR = 7
+M_SXXD, M_SZZD, M_SXZ, M_STRAIN_PL, M_STRAIN, M_T, M_CMUL, M_P = range(8)
+M_NATTR = 8
 
 
 class Model(C.Structure):

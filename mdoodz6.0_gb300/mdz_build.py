@@ -2,6 +2,7 @@
 oracle.  Compiles in-tree; outputs are git-ignored.
 
     libmdoodz_gb300.so   mdoodz6.0_gb300/lib/   product: CUDA kernels + C ABI
+    libmdoodz_refshim.so mdoodz6.0_gb300/lib/   product: reference-signature drop-ins over that ABI
     libmdz_oracle.so     oracle/_build/         checker only (tests, smoke, bench's CPU leg)
     libmdoodz_ref.so     oracle/_ref/           reference compiled in place (only where its sources exist)
 """
@@ -18,9 +19,12 @@ INCLUDE = os.path.join(ROOT, "include")
 OBJ = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libmdoodz_gb300.so")
+REFSHIM_LIB = os.path.join(LIBDIR, "libmdoodz_refshim.so")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "_build", "libmdz_oracle.so")
-REF_SRC = "/root/reference/SOURCE"
+# the reference's SOURCE directory (for the oracle's in-place build and the
+# layout check): MDZ_REF_SRC, else the location it has in this container
+REF_SRC = os.environ.get("MDZ_REF_SRC", "/root/reference/SOURCE")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC,
@@ -66,9 +70,23 @@ def build_cuda(verbose=False, extra_flags=()):
     objs = [os.path.join(OBJ, os.path.basename(s)[:-3] + ".o") for s in sources]
     if jobs or not os.path.exists(LIB):
         _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
+    build_refshim()
     if verbose:
         print("".join(logs))
     return LIB
+
+
+def build_refshim():
+    """The reference-signature drop-ins (refshim/mdz_refshim.c) against the
+    generated layout view of the reference's structures, linked to the CUDA
+    library: lib/libmdoodz_refshim.so."""
+    src = os.path.join(PKG, "refshim", "mdz_refshim.c")
+    deps = [src, LIB] + glob.glob(os.path.join(INCLUDE, "*.h"))
+    if os.path.exists(REFSHIM_LIB) and all(os.path.getmtime(REFSHIM_LIB) >= os.path.getmtime(d) for d in deps):
+        return REFSHIM_LIB
+    _run(["gcc", "-std=gnu99", "-O2", "-fPIC", "-shared", "-Wall", "-I" + INCLUDE, src, "-o", REFSHIM_LIB,
+          "-L" + LIBDIR, "-lmdoodz_gb300", "-Wl,-rpath,$ORIGIN", "-lm"])
+    return REFSHIM_LIB
 
 
 def build_oracle():

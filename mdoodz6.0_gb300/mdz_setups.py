@@ -10,19 +10,19 @@ import numpy as np
 def seed_markers(grid, nmx, nmz, jitter=0.5, seed=12345):
     """nmx x nmz markers per cell, each displaced uniformly by up to
     +/- jitter x (marker spacing) in x and z, clipped into the box.
-    Returned in cell-major order (all markers of cell 0, then cell 1, ...)."""
+    Returned in cell-major order (all markers of cell 0, then cell 1, ...;
+    inside a cell by sub-row, then sub-column)."""
     rng = np.random.default_rng(seed)
     ncx, ncz = grid.ncx, grid.ncz
     hx, hz = grid.dx / nmx, grid.dz / nmz
-    # sub-grid of the whole box, then reorder cell-major
-    ix = np.arange(ncx * nmx)
-    iz = np.arange(ncz * nmz)
-    X, Z = np.meshgrid(grid.xmin + (ix + 0.5) * hx, grid.zmin + (iz + 0.5) * hz)
-    cx = (ix // nmx)[None, :].repeat(len(iz), 0)
-    cz = (iz // nmz)[:, None].repeat(len(ix), 1)
-    order = np.lexsort((X.ravel(), Z.ravel(), cx.ravel(), cz.ravel()))
-    x = X.ravel()[order]
-    z = Z.ravel()[order]
+    # sub-grid indices in (cell row, cell column, sub-row, sub-column) order
+    cz = np.arange(ncz)[:, None, None, None]
+    cx = np.arange(ncx)[None, :, None, None]
+    j = np.arange(nmz)[None, None, :, None]
+    i = np.arange(nmx)[None, None, None, :]
+    shape = (ncz, ncx, nmz, nmx)
+    x = np.broadcast_to(grid.xmin + ((cx * nmx + i) + 0.5) * hx, shape).ravel()
+    z = np.broadcast_to(grid.zmin + ((cz * nmz + j) + 0.5) * hz, shape).ravel()
     n = x.size
     x = x + rng.uniform(-jitter, jitter, n) * hx
     z = z + rng.uniform(-jitter, jitter, n) * hz
@@ -57,7 +57,7 @@ class Scales:
 def _markers_dict(x, z, ph, **attrs):
     n = len(x)
     m = dict(x=x, z=z, phase=ph.astype(np.int32))
-    for k in ("sxxd", "szzd", "sxz", "strain_pl", "strain", "T"):
+    for k in ("sxxd", "szzd", "sxz", "strain_pl", "strain", "T", "P"):
         m[k] = np.zeros(n)
     m["cmul"] = np.ones(n)
     m.update(attrs)
@@ -178,6 +178,9 @@ def config_lithosphere(Nx=1025, Nz=513, nm=4, seed=12345, precision=64, learned=
     rho_c = rho_of(-zc * L)
     col = np.cumsum((rho_c * (-model.gz) * dz)[::-1])[::-1] - 0.5 * rho_c * (-model.gz) * dz
     p0 = np.repeat(col[:, None], g.ncx, axis=1).ravel()
+    # markers start at the lithostatic pressure of their depth (the reference
+    # interpolates p_lith to them, Main_DOODZ.c:297)
+    m["P"] = np.interp(z, zc, col)
     return dict(name="lithosphere", grid=g, markers=m, mat=mat, model=model, u=u, v=v, p=p0, scales=sc)
 
 
@@ -233,7 +236,7 @@ def load_context(cfg, max_markers=None):
     ctx = mdz.Context(g, cfg["mat"].n_phases, max_markers or marker_capacity(cfg))
     ctx.set_markers(m["x"], m["z"], m["phase"])
     for attr, key in ((mdz.M_SXXD, "sxxd"), (mdz.M_SZZD, "szzd"), (mdz.M_SXZ, "sxz"), (mdz.M_STRAIN_PL, "strain_pl"),
-                      (mdz.M_STRAIN, "strain"), (mdz.M_T, "T"), (mdz.M_CMUL, "cmul")):
+                      (mdz.M_STRAIN, "strain"), (mdz.M_T, "T"), (mdz.M_CMUL, "cmul"), (mdz.M_P, "P")):
         ctx.set_marker_attr(attr, m[key])
     f = mdz.GridFields(g, cfg["mat"].n_phases)
     f["u"], f["v"], f["p"] = cfg["u"], cfg["v"], cfg["p"]

@@ -303,7 +303,7 @@ static double orc_v2p_vert(const mdz_grid_desc *g, double x, double z, const dou
 
 int orc_reseed(const mdz_grid_desc *g, int n, int cap, double *x, double *z, int *phase, double *vx, double *vz,
                double *const *attr, int min_part_cell, int direct, const double *T_n, const double *sxxd_n,
-               const double *szzd_n, const double *sxz_s, int *n_added) {
+               const double *szzd_n, const double *sxz_s, const double *p_n, int *n_added) {
     const double dx = g->dx, dz = g->dz;
     const int Ncx = g->Nx - 1, Ncz = g->Nz - 1, nxl = 2 * (Ncx + 2), nzl = 2 * (Ncz + 2), nq = nxl * nzl;
     const double xge = g->xg[0] - dx, zge = g->zg[0] - dz;
@@ -383,11 +383,13 @@ int orc_reseed(const mdz_grid_desc *g, int n, int cap, double *x, double *z, int
                 attr[MDZ_M_CMUL][slot] = attr[MDZ_M_CMUL][m];
                 if (direct) {
                     attr[MDZ_M_T][slot] = attr[MDZ_M_T][m];
+                    attr[MDZ_M_P][slot] = attr[MDZ_M_P][m];
                     attr[MDZ_M_SXXD][slot] = attr[MDZ_M_SXXD][m];
                     attr[MDZ_M_SZZD][slot] = attr[MDZ_M_SZZD][m];
                     attr[MDZ_M_SXZ][slot] = attr[MDZ_M_SXZ][m];
                 } else {
                     attr[MDZ_M_T][slot] = orc_c2p(g, x[slot], z[slot], T_n);
+                    attr[MDZ_M_P][slot] = orc_c2p(g, x[slot], z[slot], p_n);   /* mesh->p_in :672 */
                     attr[MDZ_M_SXXD][slot] = orc_c2p(g, x[slot], z[slot], sxxd_n);
                     attr[MDZ_M_SZZD][slot] = orc_c2p(g, x[slot], z[slot], szzd_n);
                     attr[MDZ_M_SXZ][slot] = orc_v2p_vert(g, x[slot], z[slot], sxz_s);

@@ -46,7 +46,7 @@ int orc_rk4(const mdz_grid_desc *g, int n, double *x, double *z, int *phase, dou
  * -2 when cap is too small; n_added receives the number of new markers. */
 int orc_reseed(const mdz_grid_desc *g, int n, int cap, double *x, double *z, int *phase, double *vx, double *vz,
                double *const *attr, int min_part_cell, int direct, const double *T_n, const double *sxxd_n,
-               const double *szzd_n, const double *sxz_s, int *n_added);
+               const double *szzd_n, const double *sxz_s, const double *p_n, int *n_added);
 
 #ifdef __cplusplus
 }

@@ -97,11 +97,12 @@ class Oracle:
         return vx, vz
 
 
-# marker attribute order of include/mdoodz_gpu.h (MDZ_M_SXXD ... MDZ_M_CMUL)
-MARKER_ATTRS = ("sxxd", "szzd", "sxz", "strain_pl", "strain", "T", "cmul")
+# marker attribute order of include/mdoodz_gpu.h (MDZ_M_SXXD ... MDZ_M_P)
+MARKER_ATTRS = ("sxxd", "szzd", "sxz", "strain_pl", "strain", "T", "cmul", "P")
 
 
-def reseed(grid, markers, cap, min_part_cell=16, direct=0, T_n=None, sxxd_n=None, szzd_n=None, sxz_s=None):
+def reseed(grid, markers, cap, min_part_cell=16, direct=0, T_n=None, sxxd_n=None, szzd_n=None, sxz_s=None,
+           p_n=None):
     """Marker reseeding of CountPartCell (RESEED = 1, one thread): returns a
     new markers dict (keys x, z, phase, vx, vz and MARKER_ATTRS, length = the
     new count) and the number of markers created.  Raises RuntimeError where
@@ -118,12 +119,12 @@ def reseed(grid, markers, cap, min_part_cell=16, direct=0, T_n=None, sxxd_n=None
     g = grid
     nc, nv = (g.Nx - 1) * (g.Nz - 1), g.Nx * g.Nz
     z0 = np.zeros(max(nc, nv))
-    fld = [np.ascontiguousarray(a if a is not None else z0, np.float64) for a in (T_n, sxxd_n, szzd_n, sxz_s)]
+    fld = [np.ascontiguousarray(a if a is not None else z0, np.float64) for a in (T_n, sxxd_n, szzd_n, sxz_s, p_n)]
     added = C.c_int(0)
     desc = grid.desc()
     r = lib().orc_reseed(C.byref(desc), C.c_int(n), C.c_int(cap), _d(out["x"]), _d(out["z"]), _i(out["phase"]),
                          _d(out["vx"]), _d(out["vz"]), attrs, C.c_int(min_part_cell), C.c_int(direct),
-                         _d(fld[0]), _d(fld[1]), _d(fld[2]), _d(fld[3]), C.byref(added))
+                         _d(fld[0]), _d(fld[1]), _d(fld[2]), _d(fld[3]), _d(fld[4]), C.byref(added))
     if r == -1:
         raise RuntimeError("reseed: a deficient quarter cell has no marker within two quarter cells")
     if r == -2:

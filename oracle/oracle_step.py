@@ -164,7 +164,7 @@ def project(g, mat, model, markers):
     # 1. projections
     f["phase_perc_n"] = o.P2Mastah(np.zeros(nph), None, g.tags(1), 0, 0, 1, 1, st)
     f["phase_perc_s"] = o.P2Mastah(np.zeros(nph), None, g.tags(0), 0, 0, 1, 0, st)
-    for name, key in (("sxxd0", "sxxd"), ("szzd0", "szzd"), ("T", "T"), ("strain_n", "strain_pl")):
+    for name, key in (("sxxd0", "sxxd"), ("szzd0", "szzd"), ("T", "T"), ("strain_n", "strain_pl"), ("p0_n", "P")):
         f[name] = o.P2Mastah(markers[key], f[name], g.tags(1), 1, 0, 0, 1, st)
     cmul_n = o.P2Mastah(markers["cmul"], np.zeros(g.size(1)), g.tags(1), 1, 0, 0, 1, st)
     f["sxz0"] = o.P2Mastah(markers["sxz"], f["sxz0"], g.tags(0), 1, 0, 0, 0, st)
@@ -298,6 +298,7 @@ def time_step(g, mat, model, markers, u, v, p, fields_out=None):
     if model.advect:
         dt = prm.dt
         update_particle_stress(g, o, f, markers)
+        update_particle_pressure(g, o, f["p0_n"], p, markers)
         dstr = dt * (f["eII_pl"] + f["eII_pwl"] + f["eII_lin"] + f["eII_el"] + f["eII_cst"])
         dstr_pl = dt * f["eII_pl"]
         markers["vx"], markers["vz"] = o.RogerGuntherII(u, v, dt)
@@ -310,7 +311,7 @@ def time_step(g, mat, model, markers, u, v, p, fields_out=None):
         if getattr(model, "reseed", 0):   # CountPartCell(RESEED = 1) after the advection
             cap = len(markers["x"]) + 4 * (g.Nx - 1) * (g.Nz - 1)
             new, rep["markers_added"] = orc.reseed(g, markers, cap, model.min_part_cell, model.direct_neighbour,
-                                                   f["T"], f["sxxd"], f["szzd"], f["sxz"])
+                                                   f["T"], f["sxxd"], f["szzd"], f["sxz"], p)
             markers.update(new)
     if fields_out is not None:
         fields_out.update({k: f[k].copy() for k in f.a})
@@ -361,6 +362,16 @@ def update_particle_stress(g, o, f, markers):
     markers["sxxd"] += np.where(act, o.Interp_Grid2P(dsxx, 1), 0.0)
     markers["szzd"] += np.where(act, o.Interp_Grid2P(dszz, 1), 0.0)
     markers["sxz"] += np.where(act, o.Interp_Grid2P(dsxz, 0), 0.0)
+
+
+def update_particle_pressure(g, o, p0_n, p, markers):
+    """UpdateParticlePressure (SOURCE/RheologyParticles.c:1004-1123) with
+    Plith_trick = 0 and no subgrid diffusion: dp = p_in - p0_n where the
+    centroid tag is not 30, interpolated to the active markers
+    (Interp_Grid2P_centroids2) and added to their pressure.  o: an Oracle
+    holding the markers' positions and phases."""
+    dp = np.where(g.BCp != 30, p - p0_n, 0.0)
+    markers["P"] += np.where(markers["phase"] != -1, o.Interp_Grid2P(dp, 1), 0.0)
 
 
 def _accumulated_strain(g, m, dstr, dstr_pl):

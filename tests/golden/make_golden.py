@@ -244,7 +244,7 @@ def _v2c_np(g, ver):
 
 
 RESEED_ATTRS = (("Vx", "vx"), ("Vz", "vz"), ("sxxd", "sxxd"), ("szzd", "szzd"), ("sxz", "sxz"),
-                ("strain", "strain"), ("strain_pl", "strain_pl"), ("T", "T"))
+                ("strain", "strain"), ("strain_pl", "strain_pl"), ("T", "T"), ("P", "P"))
 
 
 def reseed_inputs(g, seed=11):
@@ -264,7 +264,7 @@ def reseed_inputs(g, seed=11):
         m[k] = rng.normal(size=len(x))
     nc, nv = (g.Nx - 1) * (g.Nz - 1), g.Nx * g.Nz
     fields = dict(T_n=rng.normal(size=nc), sxxd_n=rng.normal(size=nc), szzd_n=rng.normal(size=nc),
-                  sxz_s=rng.normal(size=nv))
+                  sxz_s=rng.normal(size=nv), p_n=rng.normal(size=nc))
     return m, fields
 
 
@@ -336,6 +336,7 @@ def make_reseed_fixture():
             r.field("sxxd")[:] = fields["sxxd_n"]
             r.field("szzd")[:] = fields["szzd_n"]
             r.field("sxz")[:] = fields["sxz_s"]
+            r.field("p_in")[:] = fields["p_n"]
             n_new = r.reseed(direct, mpc)
             tag = "d%d_m%d_" % (direct, mpc)
             # only the slots the reseeding wrote (inactive ones reused, then

@@ -64,6 +64,45 @@ def test_restart_continues_as_uninterrupted(tmp_path):
         assert _rel(sb[k], sa[k]) < 1e-12, (k, _rel(sb[k], sa[k]))
 
 
+def test_restart_into_a_context_that_has_stepped(tmp_path):
+    """Loading into a context that already ran steps of its own (other
+    markers, fields and multigrid hierarchy) gives the same next step as the
+    uninterrupted run; a breakpoint saved before any field existed zeroes the
+    loaded context's u, v, p as well."""
+    g, m, u, v, p, mat = vep_case()
+    prm = mdz.RheoParams.make(dt=0.05, iselastic=1, step=1)
+    model = mdz.Model.make(prm, newton=1, nit_max=12, rel_tol=1e-11, lin_rtol=1e-9, line_search=0, precision=64,
+                           reseed=1, min_part_cell=16, direct_neighbour=0)
+    cap = len(m["x"]) + 8 * g.ncx * g.ncz
+    path = str(tmp_path / "step1.brk")
+    a = _context(g, m, u, v, p, mat, cap)
+    a.time_step(mat, model)
+    a.save_breakpoint(path)
+    ra = a.time_step(mat, model)
+    sa = _state(a, g, mat.n_phases)
+    a.close()
+    c = _context(g, m, u, v, p, mat, cap)
+    for _ in range(3):
+        c.time_step(mat, model)
+    c.load_breakpoint(path)
+    rc = c.time_step(mat, model)
+    sc = _state(c, g, mat.n_phases)
+    assert rc.nonlinear_its == ra.nonlinear_its and rc.markers_added == ra.markers_added
+    for k in ("u", "v", "p", "x", "z", "vx", "sxxd", "strain_pl"):
+        assert _rel(sc[k], sa[k]) < 1e-12, (k, _rel(sc[k], sa[k]))
+    # a field-less breakpoint (saved by a context that never had fields)
+    empty = str(tmp_path / "markers_only.brk")
+    d = mdz.Context(g, mat.n_phases, cap)
+    d.set_markers(m["x"], m["z"], m["phase"])
+    d.save_breakpoint(empty)
+    d.close()
+    c.load_breakpoint(empty)
+    out = mdz.GridFields(g, mat.n_phases)
+    c.download_fields(out)
+    c.close()
+    assert not out["u"].any() and not out["v"].any() and not out["p"].any()
+
+
 def test_breakpoint_refused(tmp_path):
     g, m, u, v, p, mat = vep_case()
     path = str(tmp_path / "b.brk")

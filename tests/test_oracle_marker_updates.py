@@ -9,7 +9,7 @@ import pytest
 import mdz
 import oracle
 
-ATTRS = ("vx", "vz", "sxxd", "szzd", "sxz", "strain", "strain_pl", "T")
+ATTRS = ("vx", "vz", "sxxd", "szzd", "sxz", "strain", "strain_pl", "T", "P")
 
 
 @pytest.fixture(scope="module")
@@ -33,7 +33,8 @@ def test_reseed_matches_reference(ref, direct, mpc):
     g, m = reseed_case(ref)
     n = len(m["x"])
     cap = n + 4 * (g.Nx - 1) * (g.Nz - 1)
-    out, added = oracle.reseed(g, m, cap, mpc, direct, ref["T_n"], ref["sxxd_n"], ref["szzd_n"], ref["sxz_s"])
+    out, added = oracle.reseed(g, m, cap, mpc, direct, ref["T_n"], ref["sxxd_n"], ref["szzd_n"], ref["sxz_s"],
+                                 ref["p_n"])
     tag = "d%d_m%d_" % (direct, mpc)
     assert len(out["x"]) == int(ref[tag + "n"])
     slots = ref[tag + "slots"]
@@ -97,3 +98,17 @@ def test_update_particle_stress_matches_reference(golden):
         want = ref["m_" + k]
         assert np.allclose(m[k], want, rtol=1e-13, atol=1e-14), (k, np.abs(m[k] - want).max())
         assert not np.array_equal(want, ref["m0_" + k])
+
+
+def test_update_particle_pressure_matches_reference(golden):
+    """UpdateParticlePressure (Plith_trick = 0, no subgrid diffusion): the
+    oracle's centroid increment p_in - p0_n interpolated to the markers."""
+    import oracle_step
+    ref = golden("pressure_ref.npz")
+    xmin, xmax, zmin, zmax = ref["box"]
+    g = mdz.Grid(int(ref["Nx"]), int(ref["Nz"]), xmin, xmax, zmin, zmax).set_bc_pureshear(1.0)
+    o = oracle.Oracle(g, 3)
+    o.set_markers(ref["x"], ref["z"], ref["phase"])
+    m = dict(phase=np.array(ref["phase"]), P=np.array(ref["P0"]))
+    oracle_step.update_particle_pressure(g, o, ref["p0_n"], ref["p_in"], m)
+    np.testing.assert_allclose(m["P"], ref["P_trick0"], rtol=1e-13, atol=1e-13)

@@ -14,8 +14,8 @@ import oracle
 pytestmark = pytest.mark.gpu
 
 ATTR_IDS = (("sxxd", mdz.M_SXXD), ("szzd", mdz.M_SZZD), ("sxz", mdz.M_SXZ), ("strain_pl", mdz.M_STRAIN_PL),
-            ("strain", mdz.M_STRAIN), ("T", mdz.M_T), ("cmul", mdz.M_CMUL))
-INTERP = ("T", "sxxd", "szzd", "sxz")
+            ("strain", mdz.M_STRAIN), ("T", mdz.M_T), ("cmul", mdz.M_CMUL), ("P", mdz.M_P))
+INTERP = ("T", "sxxd", "szzd", "sxz", "P")
 INTERP_TOL = 1e-14
 
 
@@ -50,7 +50,7 @@ def _case(ref):
     xmin, xmax, zmin, zmax = ref["box"]
     g = mdz.Grid(int(ref["Nx"]), int(ref["Nz"]), xmin, xmax, zmin, zmax).set_bc_pureshear(1.0)
     m = {k: np.array(ref["in_" + k]) for k in ("x", "z", "phase", "vx", "vz", "sxxd", "szzd", "sxz", "strain",
-                                                "strain_pl", "T")}
+                                                "strain_pl", "T", "P")}
     m["cmul"] = np.arange(len(m["x"]), dtype=np.float64)
     return g, m
 
@@ -63,16 +63,18 @@ def test_reseed_matches_reference_golden(golden, direct, mpc):
     n = len(m["x"])
     cap = n + 4 * g.ncx * g.ncz
     ctx = _load(g, m, cap, 3)
-    added = ctx.CountPartCell(1, mpc, direct, ref["T_n"], ref["sxxd_n"], ref["szzd_n"], ref["sxz_s"])
+    added = ctx.CountPartCell(1, mpc, direct, ref["T_n"], ref["sxxd_n"], ref["szzd_n"], ref["sxz_s"], ref["p_n"])
     tag = "d%d_m%d_" % (direct, mpc)
     assert ctx.n_markers == int(ref[tag + "n"]) and added > 0
     out = _read(ctx)
     slots = ref[tag + "slots"]
     _compare({k: out[k][slots] for k in out}, {k: ref[tag + k] for k in ("x", "z", "phase", "vx", "vz", "sxxd",
-                                                                         "szzd", "sxz", "strain", "strain_pl", "T")},
+                                                                         "szzd", "sxz", "strain", "strain_pl", "T",
+                                                                         "P")},
              direct)
     # the whole marker store against the oracle, the cohesion multiplier included
-    o, o_added = oracle.reseed(g, m, cap, mpc, direct, ref["T_n"], ref["sxxd_n"], ref["szzd_n"], ref["sxz_s"])
+    o, o_added = oracle.reseed(g, m, cap, mpc, direct, ref["T_n"], ref["sxxd_n"], ref["szzd_n"], ref["sxz_s"],
+                               ref["p_n"])
     assert o_added == added
     _compare(out, o, direct)
     ctx.close()
@@ -86,10 +88,10 @@ def _random_case(Nx, Nz, nm, thin, seed, nph=4):
     x, z = x[keep], z[keep]
     m = dict(x=x, z=z, phase=rng.integers(0, nph, len(x)).astype(np.int32))
     m["phase"][rng.random(len(x)) < 0.01] = -1          # markers that left the box: slots to reuse
-    for k in ("vx", "vz", "sxxd", "szzd", "sxz", "strain", "strain_pl", "T", "cmul"):
+    for k in ("vx", "vz", "sxxd", "szzd", "sxz", "strain", "strain_pl", "T", "cmul", "P"):
         m[k] = rng.normal(size=len(x))
     nc, nv = g.ncx * g.ncz, Nx * Nz
-    flds = [rng.normal(size=nc), rng.normal(size=nc), rng.normal(size=nc), rng.normal(size=nv)]
+    flds = [rng.normal(size=nc), rng.normal(size=nc), rng.normal(size=nc), rng.normal(size=nv), rng.normal(size=nc)]
     return g, m, flds
 
 
