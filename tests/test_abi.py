@@ -12,9 +12,14 @@ import mdz
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def _declared():
+REFSHIM_HEADER = "mdoodz_refshim.h"   # declared by the drop-in library, libmdoodz_refshim.so
+
+
+def _declared(refshim=False):
     names = set()
     for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        if (os.path.basename(h) == REFSHIM_HEADER) != refshim:
+            continue
         src = open(h).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
         for m in re.finditer(r"\b(mdz_[A-Za-z0-9_]+)\s*\(", src):
@@ -40,6 +45,20 @@ def test_every_declared_symbol_is_exported(lib):
     missing = [n for n in _declared() if not hasattr(lib, n)]
     assert not missing, missing
 
+
+def test_refshim_exports_its_symbols(lib):
+    """libmdoodz_refshim.so exports the mdz_gpu_* entry points of its header
+    and the reference-named drop-ins."""
+    import mdz_build
+    if not os.path.exists(mdz_build.REFSHIM_LIB):
+        mdz_build.build_refshim()
+    shim = ctypes.CDLL(mdz_build.REFSHIM_LIB)
+    names = _declared(refshim=True) + ["P2Mastah", "CountPartCell", "NonNewtonianViscosityGrid",
+                                       "EvaluateStokesResidualDecoupled", "SolveStokesDefectDecoupled",
+                                       "RogerGuntherII", "Interp_Grid2P", "UpdateParticleStress"]
+    assert "mdz_gpu_init" in names
+    missing = [n for n in names if not hasattr(shim, n)]
+    assert not missing, missing
 
 
 def test_struct_layouts_match_header(tmp_path):
