@@ -99,9 +99,11 @@ int mdz_marker_count(const mdz_ctx *ctx);
  * LoadBreakpointParticles, SOURCE/InputOutput.c:515-1007, 160-514, for what
  * this library keeps between steps): markers (x, z, phase, Vx, Vz and the
  * MDZ_M_* attributes) and the grid u, v, p that start the next step, from
- * the device mirrors to one binary file ("MDZBRK01" header with the grid
- * sizes, then the arrays in host byte order) and back into a context of the
- * same grid and phase count.  A restart from it continues as the
+ * the device mirrors to one binary file ("MDZBRK02" header with the grid
+ * sizes and the box, then the arrays in host byte order) and back into a
+ * context of the same grid sizes and phase count; loading moves the
+ * context's box to the saved one (a box moved by PureShearALE), as the
+ * reference restores model.xmin..zmax.  A restart from it continues as the
  * uninterrupted run; the learned guess's weights are saved separately
  * (mdz_mlp_get_weights).  MDZ_ERR_ARG for an unreadable, foreign or
  * truncated file (the context is unchanged then), MDZ_ERR_CAPACITY when its
@@ -199,10 +201,12 @@ mdz_status mdz_RogerGuntherII(mdz_ctx *ctx, const double *u, const double *v, do
 /* Per-phase material parameters: the subset of the reference's mat_prop
  * (SOURCE/header_MDOODZ.h:46-63) used by the implemented creep laws.
  * Implemented: constant viscosity (cstv), dislocation creep (pwlv), diffusion
- * creep (linv, constant grain size), Maxwell elasticity, Drucker-Prager /
- * von Mises plasticity with the viscoplastic regularisation eta_vp, n_vp.
- * Not implemented (rejected with MDZ_ERR_UNSUPPORTED): Peierls (expv), GBS
- * (gbsv), grain-size evolution (gs), reaction mixing, tension cut-off. */
+ * creep (linv, constant grain size), Peierls creep (expv, below 1200 C),
+ * grain-boundary sliding (gbsv), Maxwell elasticity, Drucker-Prager / von
+ * Mises plasticity with the viscoplastic regularisation eta_vp, n_vp, and the
+ * tension cut-off (is_tensile, tension pressure -25 MPa).
+ * Not implemented (rejected with MDZ_ERR_UNSUPPORTED): grain-size evolution
+ * (gs), reaction mixing (reac_soft, phase_mix). */
 typedef struct mdz_materials {
     int n_phases;
     double R;                                           /* gas constant (mat_prop.R)           */
@@ -225,6 +229,15 @@ typedef struct mdz_materials {
     double C_end[MDZ_MAX_PHASES], phi_end[MDZ_MAX_PHASES], psi_end[MDZ_MAX_PHASES];
     double pls_start[MDZ_MAX_PHASES], pls_end[MDZ_MAX_PHASES];
     int coh_soft[MDZ_MAX_PHASES], phi_soft[MDZ_MAX_PHASES], psi_soft[MDZ_MAX_PHASES];
+    /* Peierls creep (expv): activation energy Qexp, Peierls stress Sexp,
+     * reference strain rate Eexp, gamma Gexp (0 < Gexp < 1), stress exponent
+     * nexp (Viscosity, SOURCE/RheologyDensity.c:181-199) */
+    double Qexp[MDZ_MAX_PHASES], Sexp[MDZ_MAX_PHASES], Eexp[MDZ_MAX_PHASES], Gexp[MDZ_MAX_PHASES];
+    double nexp[MDZ_MAX_PHASES];
+    /* grain-boundary sliding (gbsv), a creep law of the dislocation form */
+    double ngbs[MDZ_MAX_PHASES], Agbs[MDZ_MAX_PHASES], Qgbs[MDZ_MAX_PHASES], Vgbs[MDZ_MAX_PHASES];
+    double mgbs[MDZ_MAX_PHASES], rgbs[MDZ_MAX_PHASES], fgbs[MDZ_MAX_PHASES], agbs[MDZ_MAX_PHASES];
+    double Fgbs[MDZ_MAX_PHASES];
 } mdz_materials;
 
 /* Model switches and scales read by the rheology (params / scale in the reference). */
@@ -266,6 +279,7 @@ typedef struct mdz_fields {
     double *D31_s, *D32_s, *D33_s, *D34_s;
     double *roger_x, *roger_z, *rhs_p, *gx, *gz;
     double *ru, *rv, *rp;
+    double *eII_exp, *eII_gbs;   /* centroid Peierls and grain-boundary-sliding rates */
 } mdz_fields;
 
 /* Host-pointer drop-ins for the grid-side reference functions.  Each reads the
@@ -476,6 +490,27 @@ mdz_status mdz_get_marker_attr(mdz_ctx *ctx, int attr, int n, double *values);
  * mirrors: to_device = 1 uploads every non-NULL member, 0 downloads them. */
 mdz_status mdz_sync_fields(mdz_ctx *ctx, mdz_fields *f, int to_device);
 
+/* PureShearALE (SOURCE/AdvectionRoutines.c:634-734, ispureshear_ale = 1,
+ * no free surface): the mean Vx of the Dirichlet nodes (tag 0) of the west and
+ * east walls (Vx rows 0..Nz-1) and the mean Vz of the Dirichlet nodes of the
+ * south (tag 0) and north (tag 0 or 30) walls (Vz columns 0..Nx-1), each summed
+ * in the reference's loop order, move xmin, xmax, zmin, zmax by dt times that
+ * velocity; the grid lines are then regenerated over the new box as
+ * SetGridCoordinates accumulates them.  u_in / v_in: host velocities, or NULL
+ * for the resident ones.  bounds (4 doubles, may be NULL) receives the new
+ * xmin, xmax, zmin, zmax.  The Dirichlet values are not changed
+ * (mdz_set_boundary_values). */
+mdz_status mdz_PureShearALE(mdz_ctx *ctx, const double *u_in, const double *v_in, double dt, double *bounds);
+/* Replace the Dirichlet values of the Vx and Vz nodes (the BCu.val / BCv.val
+ * arrays of the grid description; either may be NULL to keep it), as the
+ * reference's SetBCs rewrites them at the start of every step. */
+mdz_status mdz_set_boundary_values(mdz_ctx *ctx, const double *BCu_val, const double *BCv_val);
+/* The grid the context works on now (after any PureShearALE): box[6] =
+ * xmin, xmax, zmin, zmax, dx, dz, and the coordinate lines xg (Nx), zg (Nz),
+ * xc (Nx-1), zc (Nz-1), xvz (Nx+1), zvx (Nz+1); any pointer may be NULL. */
+mdz_status mdz_get_grid(mdz_ctx *ctx, double *box, double *xg, double *zg, double *xc, double *zc, double *xvz,
+                        double *zvx);
+
 /* Switches of one time step (the reference's params / Nparams keys). */
 typedef struct mdz_model {
     mdz_rheo_params rheo;   /* dt, elasticity, averaging, viscosity limits, scales        */
@@ -531,6 +566,15 @@ typedef struct mdz_model {
     int reseed;
     int min_part_cell;
     int direct_neighbour;
+    /* 1: the box deforms with the flow (model.ispureshear_ale = 1, PureShearALE,
+     * SOURCE/AdvectionRoutines.c:634-734, called before the marker advection,
+     * Main_DOODZ.c:1107-1109): each wall moves by dt times the mean velocity of
+     * its Dirichlet nodes and the grid lines are regenerated over the new box
+     * (SetGridCoordinates, SOURCE/GridRoutines.c:230-300) before the markers are
+     * advected on it.  The report returns the new box; the Dirichlet values of
+     * the next step follow from it (the reference's SetBCs runs again on the new
+     * coordinates): mdz_set_boundary_values.  0: fixed box. */
+    int ispureshear_ale;
 } mdz_model;
 
 #define MDZ_HISTORY 32
@@ -552,6 +596,7 @@ typedef struct mdz_step_report {
     int precision_fallbacks;          /* FP32-refined solves that missed min(10 x their tolerance, 0.5),
                                          redone in FP64 */
     int markers_added;                /* markers created by the reseeding (model.reseed)      */
+    double xmin, xmax, zmin, zmax;    /* the box after the step (moves with ispureshear_ale)  */
 } mdz_step_report;
 
 /* One time step of Main_DOODZ.c's loop (SOURCE/Main_DOODZ.c:459-1320) on the

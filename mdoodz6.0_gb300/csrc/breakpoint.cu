@@ -8,22 +8,25 @@
 // (projections, rheology, multigrid hierarchy); the learned guess's weights
 // have their own entry points (mdz_mlp_get_weights / mdz_mlp_set_weights).
 //
-// File: "MDZBRK01", int32 Nx, Nz, n_phases, n_markers, n_attr, has_fields,
-// double dx, dz, xmin, zmin, then x, z, vx, vz (double), phase (int32), the
-// n_attr attribute arrays (double) and, when has_fields, u, v, p (double), in
-// the byte order of the host that wrote it.
+// File: "MDZBRK02", int32 Nx, Nz, n_phases, n_markers, n_attr, has_fields,
+// double xmin, xmax, zmin, zmax (the box, which PureShearALE moves), then x,
+// z, vx, vz (double), phase (int32), the n_attr attribute arrays (double) and,
+// when has_fields, u, v, p (double), in the byte order of the host that wrote
+// it.  Loading restores the box and regenerates the grid lines over it, as
+// the reference reads model.xmin..zmax back and calls SetGridCoordinates
+// (Main_DOODZ.c:446).
 #include <cstdio>
 #include <cstring>
 #include <vector>
 #include "mdz_internal.cuh"
 
 namespace {
-const char kMagic[8] = {'M', 'D', 'Z', 'B', 'R', 'K', '0', '1'};
+const char kMagic[8] = {'M', 'D', 'Z', 'B', 'R', 'K', '0', '2'};
 
 struct brk_header {
     char magic[8];
     int Nx, Nz, n_phases, n_markers, n_attr, has_fields;
-    double dx, dz, xmin, zmin;
+    double xmin, xmax, zmin, zmax;
 };
 
 struct file_closer {
@@ -42,7 +45,8 @@ extern "C" mdz_status mdz_save_breakpoint(mdz_ctx *ctx, const char *path) {
     memcpy(h.magic, kMagic, 8);
     h.Nx = g.Nx; h.Nz = g.Nz; h.n_phases = ctx->n_phases; h.n_markers = n; h.n_attr = MDZ_M_NATTR;
     h.has_fields = ctx->fields_ready ? 1 : 0;
-    h.dx = g.dx; h.dz = g.dz; h.xmin = ctx->host_desc.xmin; h.zmin = ctx->host_desc.zmin;
+    h.xmin = ctx->host_desc.xmin; h.xmax = ctx->host_desc.xmax;
+    h.zmin = ctx->host_desc.zmin; h.zmax = ctx->host_desc.zmax;
     // one host staging buffer, filled array by array from the device
     const size_t big = (size_t)n > nu + nv + np ? (size_t)n : nu + nv + np;
     std::vector<double> buf(big > 0 ? big : 1);
@@ -86,8 +90,8 @@ extern "C" mdz_status mdz_load_breakpoint(mdz_ctx *ctx, const char *path) {
     brk_header h;
     if (fread(&h, sizeof h, 1, fc.f) != 1 || memcmp(h.magic, kMagic, 8) != 0)
         return mdz_fail(ctx, MDZ_ERR_ARG, "mdz_load_breakpoint: %s is not a breakpoint of this library", path);
-    if (h.Nx != g.Nx || h.Nz != g.Nz || h.n_phases != ctx->n_phases || h.n_attr != MDZ_M_NATTR || h.dx != g.dx ||
-        h.dz != g.dz || h.xmin != ctx->host_desc.xmin || h.zmin != ctx->host_desc.zmin)
+    if (h.Nx != g.Nx || h.Nz != g.Nz || h.n_phases != ctx->n_phases || h.n_attr != MDZ_M_NATTR ||
+        !(h.xmax > h.xmin) || !(h.zmax > h.zmin))
         return mdz_fail(ctx, MDZ_ERR_ARG, "mdz_load_breakpoint: %s holds another grid (%dx%d, %d phases)", path, h.Nx,
                         h.Nz, h.n_phases);
     if (h.n_markers < 0 || h.n_markers > ctx->m.cap)
@@ -130,5 +134,8 @@ extern "C" mdz_status mdz_load_breakpoint(mdz_ctx *ctx, const char *path) {
     }
     ctx->m.n = n;
     ctx->bins.valid = false;
+    const mdz_grid_desc &d = ctx->host_desc;
+    if (h.xmin != d.xmin || h.xmax != d.xmax || h.zmin != d.zmin || h.zmax != d.zmax)
+        return mdz_set_box(ctx, h.xmin, h.xmax, h.zmin, h.zmax, ctx->stream);
     return MDZ_OK;
 }

@@ -76,6 +76,22 @@ extern "C" mdz_status mdz_create(mdz_ctx **out, const mdz_grid_desc *d, int n_ph
         return MDZ_ERR_CUDA;
     }
     ctx->host_desc = *d;
+    {
+        const double *src[6] = {d->xg, d->zg, d->xc, d->zc, d->xvz, d->zvx};
+        const size_t len[6] = {(size_t)d->Nx, (size_t)d->Nz, (size_t)d->Nx - 1, (size_t)d->Nz - 1,
+                               (size_t)d->Nx + 1, (size_t)d->Nz + 1};
+        for (int i = 0; i < 6; i++) ctx->hline[i].assign(src[i], src[i] + len[i]);
+        const signed char *tsrc[4] = {d->BCu_type, d->BCv_type, d->BCp_type, d->BCg_type};
+        const size_t tlen[4] = {(size_t)d->Nx * (d->Nz + 1), (size_t)(d->Nx + 1) * d->Nz,
+                                (size_t)(d->Nx - 1) * (d->Nz - 1), (size_t)d->Nx * d->Nz};
+        for (int i = 0; i < 4; i++) ctx->htag[i].assign(tsrc[i], tsrc[i] + tlen[i]);
+        mdz_grid_desc &h = ctx->host_desc;
+        h.xg = ctx->hline[0].data(); h.zg = ctx->hline[1].data(); h.xc = ctx->hline[2].data();
+        h.zc = ctx->hline[3].data(); h.xvz = ctx->hline[4].data(); h.zvx = ctx->hline[5].data();
+        h.BCu_type = ctx->htag[0].data(); h.BCv_type = ctx->htag[1].data();
+        h.BCp_type = ctx->htag[2].data(); h.BCg_type = ctx->htag[3].data();
+        h.BCu_val = nullptr; h.BCv_val = nullptr;
+    }
     ctx->n_phases = n_phases;
     mdz_dgrid &g = ctx->g;
     int Nx = d->Nx, Nz = d->Nz;
@@ -129,7 +145,7 @@ extern "C" void mdz_destroy(mdz_ctx *ctx) {
     void *ptrs[] = {g.xg, g.zg, g.xc, g.zc, g.xvz, g.zvx, g.BCu, g.BCv, g.BCp, g.BCg, g.BCu_val, g.BCv_val,
                     ctx->m.x, ctx->m.z, ctx->m.vx, ctx->m.vz, ctx->m.phase, ctx->bins.cell, ctx->bins.sorted,
                     ctx->bins.count, ctx->bins.start, ctx->bins.cursor, ctx->bins.scan_partials,
-                    ctx->red_part, ctx->red_cnt};
+                    ctx->red_part, ctx->red_cnt, ctx->ale_sums};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     for (int a = 0; a < MDZ_M_NATTR; a++)

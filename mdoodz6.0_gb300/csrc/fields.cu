@@ -112,7 +112,8 @@ static mdz_status viscosity_grid(mdz_ctx *ctx, const mdz_materials *m, const mdz
     }
     const int fails = cnt[0];
     NAMES("div_u_s", "T_s", "P_s", "d0_s", "phi0_s", "eta_n", "eta_s", "eta_phys_n", "eta_phys_s", "VE_n", "VE_s",
-          "sxxd", "szzd", "sxz", "sxz_n", "eII_el", "eII_pl", "eII_pwl", "eII_lin", "eII_cst", "d_n", "exx_el",
+          "sxxd", "szzd", "sxz", "sxz_n", "eII_el", "eII_pl", "eII_pwl", "eII_lin", "eII_cst", "eII_exp", "eII_gbs",
+          "d_n", "exx_el",
           "ezz_el", "exz_el", "exx_diss", "ezz_diss", "exz_diss", "detadexx_n", "detadezz_n", "detadgxz_n",
           "detadp_n", "ddivpdexx_n", "ddivpdezz_n", "ddivpdgxz_n", "ddivpdp_n", "detadexx_s", "detadezz_s",
           "detadgxz_s", "detadp_s", "p_corr", "div_u_el", "div_u_pl", "div_u_r", "Wtot", "Wel", "Wdiss", "X_n",

@@ -65,7 +65,13 @@ struct mdz_bins {
 };
 
 struct mdz_ctx {
+    // the grid description with the context's own copies of its coordinate
+    // lines and tags (host_desc points at these; the Dirichlet values live on
+    // the device only): PureShearALE rewrites the lines and bounds
     mdz_grid_desc host_desc{};
+    std::vector<double> hline[6];        // xg, zg, xc, zc, xvz, zvx
+    std::vector<signed char> htag[4];    // BCu, BCv, BCp, BCg
+    double *ale_sums = nullptr;          // device: wall sums and counts of PureShearALE
     mdz_dgrid g{};
     int n_phases = 0;
     mdz_markers m;
@@ -144,6 +150,12 @@ __global__ void k_bin_sort_segments(int ncells, const int *__restrict__ start, i
 // markers; T_n, sxxd_n, szzd_n, p_n (centroids) and sxz_s (vertices) are
 // device fields, read when direct = 0.
 struct mdz_attr_ptrs { double *a[MDZ_M_NATTR]; };
+// PureShearALE on device velocities u, v (stream st): moves the box, rewrites
+// the grid lines (host copies and device), the spacings and the solver levels.
+mdz_status mdz_dev_pure_shear_ale(mdz_ctx *ctx, const double *u, const double *v, double dt, cudaStream_t st);
+mdz_status mdz_solver_regrid(mdz_ctx *ctx);
+// Move the box to the given bounds and regenerate the grid lines over it.
+mdz_status mdz_set_box(mdz_ctx *ctx, double xmin, double xmax, double zmin, double zmax, cudaStream_t st);
 mdz_status mdz_dev_reseed(mdz_ctx *ctx, int min_part_cell, int direct, const double *T_n, const double *sxxd_n,
                           const double *szzd_n, const double *sxz_s, const double *p_n, cudaStream_t st,
                           int *n_added);
@@ -260,7 +272,9 @@ void mdz_reseed_free(mdz_ctx *ctx);
     X(gz, VZ) \
     X(ru, VX) \
     X(rv, VZ) \
-    X(rp, CEN)
+    X(rp, CEN) \
+    X(eII_exp, CEN) \
+    X(eII_gbs, CEN)
 
 enum mdz_field_kind { MDZ_K_VX, MDZ_K_VZ, MDZ_K_CEN, MDZ_K_VER, MDZ_K_PPN, MDZ_K_PPS };
 size_t mdz_field_count(const mdz_ctx *ctx, int kind);

@@ -96,7 +96,7 @@ __global__ void k_v2c(mdz_dgrid g, double *__restrict__ cen, const double *__res
 // ---------------------------------------------------------------------------
 // Local solve.  Outputs of one (node, phase) solve.
 struct visc_res {
-    double eta, txx, tzz, txz, etaVE, VEcoeff, Eii_el, Eii_pl, Eii_pwl, Eii_lin, Eii_cst;
+    double eta, txx, tzz, txz, etaVE, VEcoeff, Eii_el, Eii_pl, Eii_pwl, Eii_lin, Eii_cst, Eii_exp, Eii_gbs;
     double Exx_el, Ezz_el, Exz_el, Exx_diss, Ezz_diss, Exz_diss, d1;
     double detadexx, detadezz, detadexz, detadp, X1, OverS;
     double ddivpdexx, ddivpdezz, ddivpdexz, ddivpdp, Pcorr, div_el, div_pl;
@@ -192,13 +192,19 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
     const int nitmax = 20;
     int elastic = prm.iselastic, it;
     const bool constant = Real(m.cstv[p]) != 0, dislocation = Real(m.pwlv[p]) != 0, diffusion = Real(m.linv[p]) != 0;
+    // Peierls creep only below 1200 C (tested before the 0 C clamp, :137),
+    // grain-boundary sliding, tension cut-off; the learned start models none
+    // of them, so their solves take the reference's start
+    const bool peierls = m.expv[p] != 0 && T < Real((1200.0 + ZEROC) / prm.scale_T);
+    const bool gbs = m.gbsv[p] != 0, tensile = m.is_tensile[p] != 0;
+    if (peierls || gbs || tensile) guess = nullptr;
     Real K = Real(1.0) / beta, res = Real(0.0);
     const Real Tii0 = msqrt(Txx0 * Txx0 + Txz0 * Txz0);
     const Real n_pwl = Real(m.npwl[p]), Va_pwl = Real(m.Vpwl[p]), n_lin = Real(m.nlin[p]), m_lin = Real(m.mlin[p]);
     Real B_lin = 0, C_pwl = 0, C_lin = 0, dCpwldP = 0, dClindP = 0;
     Real eta_pwl = Real(0.0), eta_lin = Real(0.0), eta_cst = Real(0.0), eta_vep = Real(0.0), eta_vp = Real(0.0);
     const Real eta_vp0 = Real(m.eta_vp[p]), n_vp = Real(m.n_vp[p]);
-    Real Eii_pwl = 0, Eii_lin = 0, Eii_cst = 0;
+    Real Eii_pwl = 0, Eii_lin = 0, Eii_cst = 0, Eii_exp = 0, Eii_gbs = 0;
     o.Eii_pl = Real(0.0); o.OverS = Real(0.0); o.ve_fail = 0; o.vp_fail = 0; o.vp_its = 0;
 
     Real Eyy = -(Exx + Ezz), Gyy = -(Gxx + Gzz);
@@ -260,11 +266,48 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
         dClindP = -C_lin * Real(m.Vlin[p]) * iRT;
         eta_lin = B_lin * fpow(Eii, in - Real(1.0)) * fpow(d, m_lin * in);
     }
+    // grain-boundary sliding: a creep law of the dislocation form (:176-180)
+    const Real n_gbs = Real(m.ngbs[p]);
+    Real C_gbs = Real(0.0), eta_gbs = Real(0.0);
+    if (gbs) {
+        const Real in = Real(1.0) / n_gbs;
+        const Real B_gbs = Real(m.Fgbs[p]) * fpow(Real(m.Agbs[p]), -in) *
+                           mexp((Real(m.Qgbs[p]) + P * Real(m.Vgbs[p])) * iRT * in) * fpow(d, Real(m.mgbs[p]) * in) *
+                           fpow(Real(m.fgbs[p]), -Real(m.rgbs[p]) * in) * fexp(-Real(m.agbs[p]) * phi * in);
+        C_gbs = fpow(Real(2.0) * f_ani * B_gbs, -n_gbs);
+        eta_gbs = B_gbs * fpow(Eii, in - Real(1.0));
+    }
+    // Peierls creep, exponential law as a power law of exponent ST + n
+    // (:181-199): ST = Q / RT 2 gamma (1 - gamma)
+    const Real n_exp = Real(m.nexp[p]);
+    Real ST = Real(0.0), B_exp = Real(0.0), C_exp = Real(0.0), eta_exp = Real(0.0);
+    if (peierls) {
+        const Real gam = Real(m.Gexp[p]), Ea = Real(m.Qexp[p]);
+        ST = Ea * iRT * Real(2.0) * gam * (Real(1.0) - gam);
+        const Real sn = ST + n_exp, isn = Real(1.0) / sn;
+        const Real Arr = mexp(-Ea * iRT * (Real(1.0) - gam) * (Real(1.0) - gam));
+        const Real F_exp = mpow(mpow(Real(2.0), Real(1.0) - ST - n_exp) / mpow(msqrt(Real(3.0)), sn + Real(1.0)), isn);
+        B_exp = F_exp * (mpow(gam * Real(m.Sexp[p]), ST * isn) / mpow(Real(m.Eexp[p]) * Arr, isn));
+        C_exp = mpow(Real(2.0) * f_ani * B_exp, -sn);
+        eta_exp = B_exp * mpow(Eii, isn - Real(1.0));
+    }
     Real cos_fric, sin_fric;
     msincos(fric, &sin_fric, &cos_fric);
     Real sin_dil = dil == Real(0.0) ? Real(0.0) : msin(dil);
     Real Tyield = C * cos_fric + P * sin_fric;
     if (Real(m.Slim[p]) < Tyield) { sin_fric = Real(0.0); cos_fric = Real(1.0); sin_dil = Real(0.0); C = Real(m.Slim[p]); Tyield = Real(m.Slim[p]); }
+    // tension cut-off (:204-213): below the tension pressure -25 MPa the yield
+    // line turns to pass through (P_tens, 0)
+    bool tens = false;
+    if (tensile) {
+        const Real P_tens = Real(-25e6) / Real(prm.scale_S);
+        const Real sin_fric_tens = -C * cos_fric / P_tens;
+        if (C * cos_fric + P * sin_fric_tens < Tyield) {
+            sin_fric = sin_fric_tens;
+            Tyield = C * cos_fric + P * sin_fric_tens;
+            tens = true;
+        }
+    }
     o.X1 = X0;
     const Real eta_el = G * dt;
     if (constant) eta_cst = Real(m.eta0[p]);
@@ -272,7 +315,9 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
     if (constant) eta_up = dmin(eta_up, eta_cst);
     if (dislocation) eta_up = dmin(eta_up, eta_pwl);
     if (elastic) eta_up = dmin(eta_up, eta_el);
+    if (peierls) eta_up = dmin(eta_up, eta_exp);
     if (diffusion) eta_up = dmin(eta_up, eta_lin);
+    if (gbs) eta_up = dmin(eta_up, eta_gbs);
     // local Newton on the visco-elastic viscosity
     Real eta_ve = eta_up, Tii;
     const Real dm_lin = fpow(o.d1, -m_lin);
@@ -328,12 +373,16 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
         Tii = Real(2.0) * f_ani * eta_ve * Eii;
         if (constant) Eii_cst = Tii * ifcst;
         if (dislocation) Eii_pwl = C_pwl * fpow(Tii, n_pwl);
+        if (gbs) Eii_gbs = C_gbs * fpow(Tii, n_gbs);
+        if (peierls) Eii_exp = C_exp * mpow(Tii, ST + n_exp);
         if (diffusion) Eii_lin = C_lin * fpow(Tii, n_lin) * dm_lin;
-        Real r = Eii - elastic * Tii * i2eta_el - (Eii_pwl + Eii_lin + Eii_cst);
+        Real r = Eii - elastic * Tii * i2eta_el - (Eii_pwl + Eii_exp + Eii_lin + Eii_gbs + Eii_cst);
         res = mfabs(r * iEii);
         if (res < tol / 100) break;
         const Real ieta = Real(1.0) / eta_ve;
         Real dfdeta = dfel + dfcst;
+        // (grain-boundary sliding has no term here in the reference)
+        if (peierls) dfdeta += -Eii_exp * (ST + n_exp) * ieta;
         if (diffusion) dfdeta += -Eii_lin * n_lin * ieta;
         if (dislocation) dfdeta += -Eii_pwl * n_pwl * ieta;
         eta_ve -= r / dfdeta;
@@ -353,6 +402,12 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
     const Real iTii = Real(1.0) / Tii, TG = Tii * iGii;   // Tii / (f_ani Eii) = Tii / Gii
     Real Txx = Gxx * TG, Tzz = Gzz * TG, Txz = Gxz * TG;
     Real Exx_lin = 0, Ezz_lin = 0, Exz_lin = 0, Exx_cst = 0, Ezz_cst = 0, Exz_cst = 0;
+    Real Exx_exp = 0, Ezz_exp = 0, Exz_exp = 0;
+    if (peierls) {
+        eta_exp = B_exp * mpow(Eii_exp, Real(1.0) / (ST + n_exp) - Real(1.0));
+        const Real h = Real(0.5) / eta_exp;
+        Exx_exp = Txx * h; Ezz_exp = Tzz * h; Exz_exp = Txz * h;
+    }
     if (dislocation) eta_pwl = Tii / (Real(2.0) * C_pwl * Tn);   // (2 C)^-1 Tii^(1-n)
     if (diffusion) {
         const Real in = Real(1.0) / n_lin;
@@ -367,6 +422,7 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
     // visco-elastic tangent
     Real deta = Real(0.0);
     if (dislocation) deta += -C_pwl * (Tn * iTii * iTii * iTii) * (n_pwl - Real(1.0));   // Tii^(n-3)
+    if (peierls) deta += -C_exp * mpow(Tii, n_exp + ST - Real(3.0)) * (n_exp + ST - Real(1.0));
     if (diffusion) deta += -C_lin * fpow(Tii, n_lin - Real(3.0)) * (n_lin - Real(1.0)) * dm_lin;
     const Real e2 = fpow(eta_ve, Real(2.0));
     Real dTxx = deta * (Real(2.0) * Txx + Tzz) * e2, dTzz = deta * (Real(2.0) * Tzz + Txx) * e2, dTxz = Real(2.0) * deta * Txz * e2;
@@ -383,7 +439,16 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
     Real dlamdExx = 0, dlamdEzz = 0, dlamdExz = 0, dlamdP = 0;
     Real dvep_dExx = 0, dvep_dEzz = 0, dvep_dExz = 0, dvep_dP = 0;
     Real F_trial = Tii - Tyield;
+    // tensile domain: the dilation angle that returns the stress to the
+    // tension corner (:456-465, SimpleYields.m of the reference)
+    if (tens) {
+        eta_vp = eta_vp0 * fpow(Eii, Real(1.0) / n_vp - Real(1.0));
+        const Real Pc_chk = -(C * cos_fric) / (-Tii / P + sin_fric);
+        sin_dil = (P * eta_ve + P * eta_vp - Pc_chk * eta_ve - Pc_chk * eta_vp) /
+                  (K * dt * (C * cos_fric + Pc_chk * sin_fric - Tii));
+    }
     const bool is_pl = F_trial > Real(1e-17);
+    Real dsdExx = Real(0.0), dsdEzz = Real(0.0), dsdExz = Real(0.0), dsdP = Real(0.0);   // d sin_dil / d .
     if (is_pl) {
         const Real in_vp = Real(1.0) / n_vp;
         eta_vp = eta_vp0 * fpow(Eii, in_vp - 1);
@@ -444,29 +509,48 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
         o.OverS = eta_vp * gdot;
         o.Pcorr = Pc;
         // visco-elasto-plastic tangent
+        if (tens) {   // derivatives of the tensile dilation angle (:578-587)
+            const Real dEii_dExx = (Real(2.0) * Exx + Ezz) * Real(0.5) * iEii, dEii_dEzz = (Real(2.0) * Ezz + Exx) * Real(0.5) * iEii;
+            const Real dEii_dExz = Exz * iEii;
+            const Real Ccf = C * cos_fric, A = Real(2.0) * Eii * eta_ve - P * sin_fric, A2 = A * A;
+            const Real iden = Real(1.0) / (K * dt * A * (C * P * cos_fric * sin_fric + (Ccf - Real(2.0) * Eii * eta_ve) * A));
+            const Real Q = C * P * cos_fric * sin_fric + A2;
+            auto dsd = [&](Real dve, Real dE) {
+                const Real dT = Eii * dve + dE * eta_ve;
+                return (Real(2.0) * K * dt * sin_dil * dT * Q +
+                        P * (-Ccf * dve * A + Real(2.0) * Ccf * (eta_ve + eta_vp) * dT + dve * A2)) * iden;
+            };
+            dsdExx = dsd(dve_dExx, dEii_dExx);
+            dsdEzz = dsd(dve_dEzz, dEii_dEzz);
+            dsdExz = dsd(dve_dExz, dEii_dExz);
+            dsdP = (Real(2.0) * C * Eii * cos_fric * (eta_ve + eta_vp) * (P * dve_dP - eta_ve) - C * P * cos_fric * dve_dP * A +
+                    Real(2.0) * Eii * K * dt * sin_dil * (C * cos_fric * sin_fric * (P * dve_dP - eta_ve) + dve_dP * A2) +
+                    A2 * (P * dve_dP + eta_ve + eta_vp)) * iden;
+        }
         const Real ev = eta_ve * iEii;
         Real dFdExx = (Real(2.0) * Exx + Ezz) * ev + Real(2.0) * Eii * dve_dExx;
         Real dFdEzz = (Real(2.0) * Ezz + Exx) * ev + Real(2.0) * Eii * dve_dEzz;
         Real dFdExz = Real(2.0) * Exz * ev + Real(2.0) * Eii * dve_dExz;
         Real dFdP = -sin_fric + Real(2.0) * Eii * dve_dP;
         Real gg = Real(1.0) / (eta_ve + eta_vp * in_vp + K * dt * sin_fric * sin_dil);
-        dlamdExx = gg * (dFdExx - gdot * (dve_dExx + K * dt * sin_fric * Real(0.0)));
-        dlamdEzz = gg * (dFdEzz - gdot * (dve_dEzz + K * dt * sin_fric * Real(0.0)));
-        dlamdExz = gg * (dFdExz - gdot * (dve_dExz + K * dt * sin_fric * Real(0.0)));
-        dlamdP = gg * (dFdP - gdot * (dve_dP + K * dt * sin_fric * Real(0.0)));
+        dlamdExx = gg * (dFdExx - gdot * (dve_dExx + K * dt * sin_fric * dsdExx));
+        dlamdEzz = gg * (dFdEzz - gdot * (dve_dEzz + K * dt * sin_fric * dsdEzz));
+        dlamdExz = gg * (dFdExz - gdot * (dve_dExz + K * dt * sin_fric * dsdExz));
+        dlamdP = gg * (dFdP - gdot * (dve_dP + K * dt * sin_fric * dsdP));
         Real q = in_vp - Real(1.0);
         const Real evg = eta_vp / gdot;
         Real dvp_dExx = evg * dlamdExx * q, dvp_dEzz = evg * dlamdEzz * q;
         Real dvp_dExz = evg * dlamdExz * q, dvp_dP = evg * dlamdP * q;
         Real a = eta_vp + K * dt * sin_fric * sin_dil;
         const Real TyE3 = Tyield * Real(0.5) * iEii * iEii * iEii, h2 = Real(0.5) * iEii;   // Tyield / (2 Eii^3), 1 / (2 Eii)
-        dvep_dExx = -Real(0.5) * (Real(2.0) * Exx + Ezz) * TyE3 + (a * dlamdExx + gdot * dvp_dExx + gdot * K * dt * sin_fric * Real(0.0)) * h2;
-        dvep_dEzz = -Real(0.5) * (Real(2.0) * Ezz + Exx) * TyE3 + (a * dlamdEzz + gdot * dvp_dEzz + gdot * K * dt * sin_fric * Real(0.0)) * h2;
-        dvep_dExz = -Exz * TyE3 + (a * dlamdExz + gdot * dvp_dExz + gdot * K * dt * sin_fric * Real(0.0)) * h2;
-        dvep_dP = (sin_fric + a * dlamdP + gdot * dvp_dP + gdot * K * dt * sin_fric * Real(0.0)) * h2;
+        dvep_dExx = -Real(0.5) * (Real(2.0) * Exx + Ezz) * TyE3 + (a * dlamdExx + gdot * dvp_dExx + gdot * K * dt * sin_fric * dsdExx) * h2;
+        dvep_dEzz = -Real(0.5) * (Real(2.0) * Ezz + Exx) * TyE3 + (a * dlamdEzz + gdot * dvp_dEzz + gdot * K * dt * sin_fric * dsdEzz) * h2;
+        dvep_dExz = -Exz * TyE3 + (a * dlamdExz + gdot * dvp_dExz + gdot * K * dt * sin_fric * dsdExz) * h2;
+        dvep_dP = (sin_fric + a * dlamdP + gdot * dvp_dP + gdot * K * dt * sin_fric * dsdP) * h2;
     }
     o.gdot = gdot;
     Real inv_eta_diss = Real(0.0);
+    if (peierls) inv_eta_diss += Real(1.0) / eta_exp;
     if (dislocation) inv_eta_diss += Real(1.0) / eta_pwl;
     if (diffusion) inv_eta_diss += Real(1.0) / eta_lin;
     if (constant) inv_eta_diss += Real(1.0) / eta_cst;
@@ -477,10 +561,10 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
     } else {
         o.detadexx = dvep_dExx; o.detadezz = dvep_dEzz; o.detadexz = dvep_dExz; o.detadp = dvep_dP;
         o.etaVE = eta_vep;
-        o.ddivpdexx = -dQdP * dlamdExx + gdot * Real(0.0);
-        o.ddivpdezz = -dQdP * dlamdEzz + gdot * Real(0.0);
-        o.ddivpdexz = -dQdP * dlamdExz + gdot * Real(0.0);
-        o.ddivpdp = -dQdP * dlamdP + gdot * Real(0.0) + Real(0.0);
+        o.ddivpdexx = -dQdP * dlamdExx + gdot * dsdExx;
+        o.ddivpdezz = -dQdP * dlamdEzz + gdot * dsdEzz;
+        o.ddivpdexz = -dQdP * dlamdExz + gdot * dsdExz;
+        o.ddivpdp = -dQdP * dlamdP + gdot * dsdP + Real(0.0);
         inv_eta_diss += Real(1.0) / eta_vep;
     }
     // eta_pwl is re-evaluated unconditionally in the reference (C_pwl = 0 when
@@ -493,13 +577,15 @@ __device__ void visc_local_t(int p, Real G, Real T, Real P, Real d, Real phi, Re
     o.Exx_el = (Real)elastic * (Txx - Txx0) * i2eta_el;
     o.Ezz_el = (Real)elastic * (Tzz - Tzz0) * i2eta_el;
     o.Exz_el = (Real)elastic * (Txz - Txz0) * i2eta_el;
-    o.Exx_diss = gdot * dQdtxx + Exx_lin + Txx * h_pwl + Exx_cst;
-    o.Ezz_diss = gdot * dQdtzz + Ezz_lin + Tzz * h_pwl + Ezz_cst;
-    o.Exz_diss = gdot * dQdtxz / Real(2.0) + Exz_lin + Txz * h_pwl + Exz_cst;
+    o.Exx_diss = gdot * dQdtxx + Exx_lin + Txx * h_pwl + Exx_exp + Exx_cst;
+    o.Ezz_diss = gdot * dQdtzz + Ezz_lin + Tzz * h_pwl + Ezz_exp + Ezz_cst;
+    o.Exz_diss = gdot * dQdtxz / Real(2.0) + Exz_lin + Txz * h_pwl + Exz_exp + Exz_cst;
     o.Eii_el = (Real)elastic * mfabs(Tii - Tii0) * i2eta_el;
     o.Eii_pwl = Tii * h_pwl;
     o.Eii_lin = Eii_lin;
     o.Eii_cst = Eii_cst;
+    o.Eii_exp = Eii_exp;
+    o.Eii_gbs = Eii_gbs;
     o.div_pl = divp;
     o.div_el = -(Pc - P0) / (K * dt);
     Real eta = Real(1.0) / inv_eta_diss;
@@ -605,6 +691,7 @@ __global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_ma
     if (c >= nc) return;
     const int avg = prm.eta_avg, nph = m.n_phases;
     double eta = 0, eta_phys = 0, VE = 0, sxx = 0, szz = 0, sxz = 0, eel = 0, epl = 0, epwl = 0, elin = 0, ecst = 0,
+           eexp = 0, egbs = 0,
            dn = 0, xel = 0, xdi = 0, zel = 0, zdi = 0, dexx = 0, dezz = 0, dgxz = 0, dp = 0, vxx = 0, vzz = 0,
            vxz = 0, vp = 0, pc = 0, del = 0, dpl = 0, Wt = 0, We = 0, Wd = 0, X = 0, OS = 0;
     int fails = 0, fallbacks = 0, learned = 0, iters = 0;
@@ -642,6 +729,7 @@ __global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_ma
             if (avg == 0 || avg == 2) { sxx += w * o.txx; szz += w * o.tzz; sxz += w * o.txz; }
             VE += w * o.VEcoeff; eel += w * o.Eii_el; epl += w * o.Eii_pl; epwl += w * o.Eii_pwl;
             elin += w * o.Eii_lin; ecst += w * o.Eii_cst; dn += w * 1.0 / o.d1;
+            eexp += w * o.Eii_exp; egbs += w * o.Eii_gbs;
             xel += w * o.Exx_el; xdi += w * o.Exx_diss; zel += w * o.Ezz_el; zdi += w * o.Ezz_diss;
             Wt += w * (o.txx * exx + o.tzz * ezz + (o.txx + o.tzz) * (exx + ezz) + 2.0 * o.txz * exz);
             Wd += w * (o.txx * o.Exx_diss + o.tzz * o.Ezz_diss + (o.txx + o.tzz) * (o.Exx_diss + o.Ezz_diss) +
@@ -678,7 +766,7 @@ __global__ void __launch_bounds__(128) k_viscosity_centroids(mdz_dgrid g, mdz_ma
     put(f.eta_n, c, eta); put(f.eta_phys_n, c, eta_phys); put(f.VE_n, c, VE);
     put(f.sxxd, c, sxx); put(f.szzd, c, szz); put(f.sxz_n, c, sxz);
     put(f.eII_el, c, eel); put(f.eII_pl, c, epl); put(f.eII_pwl, c, epwl); put(f.eII_lin, c, elin);
-    put(f.eII_cst, c, ecst); put(f.d_n, c, dn);
+    put(f.eII_cst, c, ecst); put(f.d_n, c, dn); put(f.eII_exp, c, eexp); put(f.eII_gbs, c, egbs);
     put(f.exx_el, c, xel); put(f.exx_diss, c, xdi); put(f.ezz_el, c, zel); put(f.ezz_diss, c, zdi);
     put(f.detadexx_n, c, dexx); put(f.detadezz_n, c, dezz); put(f.detadgxz_n, c, dgxz); put(f.detadp_n, c, dp);
     put(f.ddivpdexx_n, c, vxx); put(f.ddivpdezz_n, c, vzz); put(f.ddivpdgxz_n, c, vxz); put(f.ddivpdp_n, c, vp);
@@ -887,10 +975,12 @@ mdz_status mdz_check_materials(mdz_ctx *ctx, const mdz_materials *m) {
     if (m->n_phases < 1 || m->n_phases > MDZ_MAX_PHASES || m->n_phases > ctx->n_phases)
         return mdz_fail(ctx, MDZ_ERR_ARG, "materials: %d phases (context has %d)", m->n_phases, ctx->n_phases);
     for (int p = 0; p < m->n_phases; p++) {
-        if (m->expv[p] || m->gbsv[p] || m->gs[p] || m->reac_soft[p] || m->phase_mix[p] || m->is_tensile[p])
+        if (m->gs[p] || m->reac_soft[p] || m->phase_mix[p])
             return mdz_fail(ctx, MDZ_ERR_UNSUPPORTED,
-                            "phase %d: Peierls, GBS, grain-size evolution, reaction mixing and the tension cut-off "
-                            "are not implemented", p);
+                            "phase %d: grain-size evolution and reaction mixing are not implemented", p);
+        if (m->gbsv[p] && m->ngbs[p] <= 0) return mdz_fail(ctx, MDZ_ERR_ARG, "phase %d: ngbs must be > 0", p);
+        if (m->expv[p] && !(m->Gexp[p] > 0 && m->Gexp[p] < 1 && m->Eexp[p] > 0 && m->Sexp[p] > 0))
+            return mdz_fail(ctx, MDZ_ERR_ARG, "phase %d: Peierls creep needs 0 < Gexp < 1, Eexp > 0, Sexp > 0", p);
         if (m->pwlv[p] && m->npwl[p] <= 0) return mdz_fail(ctx, MDZ_ERR_ARG, "phase %d: npwl must be > 0", p);
         if (m->linv[p] && m->nlin[p] <= 0) return mdz_fail(ctx, MDZ_ERR_ARG, "phase %d: nlin must be > 0", p);
         if (m->n_vp[p] <= 0) return mdz_fail(ctx, MDZ_ERR_ARG, "phase %d: n_vp must be > 0", p);

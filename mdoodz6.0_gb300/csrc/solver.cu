@@ -1458,6 +1458,25 @@ extern "C" mdz_status mdz_set_solver_options(mdz_ctx *ctx, int nu1, int nu2, dou
     return MDZ_OK;
 }
 
+// The grid spacing changed (PureShearALE): every level's spacing follows the
+// fine one (doubling per level, as the hierarchy was built) and the captured
+// preconditioner graphs, which hold the old spacings as kernel arguments, are
+// dropped (recaptured on their next use).
+mdz_status mdz_solver_regrid(mdz_ctx *ctx) {
+    mdz_solver *S = ctx->solver;
+    if (!S) return MDZ_OK;
+    MDZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int q = 0; q < 4; q++)
+        if (S->pre[q]) { cudaGraphExecDestroy(S->pre[q]); S->pre[q] = nullptr; S->pre_eta[q] = nullptr; }
+    S->mg64.built = false;   // no solve may keep operators of the old spacing
+    S->mg32.built = false;
+    double dx = ctx->g.dx, dz = ctx->g.dz;
+    for (int lev = 0; lev < S->mg64.nlev; lev++, dx *= 2, dz *= 2) { S->mg64.L[lev].dx = dx; S->mg64.L[lev].dz = dz; }
+    dx = ctx->g.dx; dz = ctx->g.dz;
+    for (int lev = 0; lev < S->mg32.nlev; lev++, dx *= 2, dz *= 2) { S->mg32.L[lev].dx = dx; S->mg32.L[lev].dz = dz; }
+    return MDZ_OK;
+}
+
 void mdz_solver_free(mdz_ctx *ctx) {
     if (!ctx->solver) return;
     mdz_solver *S = ctx->solver;

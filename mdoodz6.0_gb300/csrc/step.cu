@@ -600,6 +600,10 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
                 ctx->m.attr[MDZ_M_STRAIN_PL], ctx->m.attr[MDZ_M_P], 1 | 4);
             MDZ_LAUNCHED(ctx);
         }
+        // PureShearALE before the marker advection (Main_DOODZ.c:1107-1109): the
+        // markers then move through the velocities on the new grid lines
+        if (M->ispureshear_ale == 1)
+            if ((s = mdz_dev_pure_shear_ale(ctx, f.u, f.v, M->rheo.dt, st)) != MDZ_OK) return s;
         if ((s = mdz_dev_rk4(ctx, f.u, f.v, M->rheo.dt, st)) != MDZ_OK) return s;
         // AccumulatedStrainII after the advection (Main_DOODZ.c:1134-1140)
         if (n > 0) {
@@ -630,6 +634,8 @@ mdz_status mdz_dev_time_step(mdz_ctx *ctx, const mdz_materials *mat, const mdz_m
     unsigned long long li = 0;
     MDZ_CUDA(ctx, cudaMemcpy(&li, ctx->d_counters + 48, sizeof li, cudaMemcpyDeviceToHost));
     R.local_iterations = (long long)li;
+    R.xmin = ctx->host_desc.xmin; R.xmax = ctx->host_desc.xmax;
+    R.zmin = ctx->host_desc.zmin; R.zmax = ctx->host_desc.zmax;
     if (rep) *rep = R;
     return MDZ_OK;
 }
@@ -644,6 +650,8 @@ extern "C" mdz_status mdz_time_step(mdz_ctx *ctx, const mdz_materials *mat, cons
     if (model->itp_stencil != 1 && model->itp_stencil != 9)
         return mdz_fail(ctx, MDZ_ERR_ARG, "mdz_time_step: itp_stencil must be 1 or 9");
     if (model->rheo.dt <= 0) return mdz_fail(ctx, MDZ_ERR_ARG, "mdz_time_step: dt must be > 0");
+    if (model->ispureshear_ale != 0 && model->ispureshear_ale != 1)
+        return mdz_fail(ctx, MDZ_ERR_ARG, "mdz_time_step: ispureshear_ale must be 0 or 1");
     if (model->learned_guess && !mdz_mlp_ready(ctx))
         return mdz_fail(ctx, MDZ_ERR_STATE, "mdz_time_step: learned guess requested but no MLP weights loaded");
     if ((s = mdz_ensure_fields(ctx)) != MDZ_OK) return s;

@@ -95,21 +95,33 @@ class Grid:
 
     def __init__(self, Nx, Nz, xmin, xmax, zmin, zmax):
         self.Nx, self.Nz = int(Nx), int(Nz)
-        self.xmin, self.xmax, self.zmin, self.zmax = float(xmin), float(xmax), float(zmin), float(zmax)
-        self.dx = (self.xmax - self.xmin) / (Nx - 1)
-        self.dz = (self.zmax - self.zmin) / (Nz - 1)
-        self.xg = self._accum(self.xmin, self.dx, Nx)
-        self.zg = self._accum(self.zmin, self.dz, Nz)
-        self.xc = self._accum(self.xmin + self.dx / 2.0, self.dx, Nx - 1)
-        self.zc = self._accum(self.zmin + self.dz / 2.0, self.dz, Nz - 1)
-        self.xvz = self._accum(self.xmin - self.dx / 2.0, self.dx, Nx + 1)
-        self.zvx = self._accum(self.zmin - self.dz / 2.0, self.dz, Nz + 1)
+        self.regrid(xmin, xmax, zmin, zmax)
         self.BCu = np.full(Nx * (Nz + 1), -1, np.int8)
         self.BCv = np.full((Nx + 1) * Nz, -1, np.int8)
         self.BCp = np.full((Nx - 1) * (Nz - 1), -1, np.int8)
         self.BCg = np.full(Nx * Nz, -1, np.int8)
         self.BCu_val = np.zeros(Nx * (Nz + 1))
         self.BCv_val = np.zeros((Nx + 1) * Nz)
+
+    def regrid(self, xmin, xmax, zmin, zmax):
+        """Move the box to the given bounds and regenerate the grid lines over
+        it (SetGridCoordinates; PureShearALE calls it after moving the walls).
+        Tags and Dirichlet values are kept."""
+        Nx, Nz = self.Nx, self.Nz
+        self.xmin, self.xmax, self.zmin, self.zmax = float(xmin), float(xmax), float(zmin), float(zmax)
+        self.dx = (self.xmax - self.xmin) / (Nx - 1)
+        self.dz = (self.zmax - self.zmin) / (Nz - 1)
+        lines = dict(xg=self._accum(self.xmin, self.dx, Nx), zg=self._accum(self.zmin, self.dz, Nz),
+                     xc=self._accum(self.xmin + self.dx / 2.0, self.dx, Nx - 1),
+                     zc=self._accum(self.zmin + self.dz / 2.0, self.dz, Nz - 1),
+                     xvz=self._accum(self.xmin - self.dx / 2.0, self.dx, Nx + 1),
+                     zvx=self._accum(self.zmin - self.dz / 2.0, self.dz, Nz + 1))
+        for k, a in lines.items():   # in place: descriptions made earlier keep valid pointers
+            if hasattr(self, k):
+                getattr(self, k)[:] = a
+            else:
+                setattr(self, k, a)
+        return self
 
     @staticmethod
     def _accum(x0, h, n):
@@ -222,7 +234,38 @@ class Context:
         self._check(self.L.mdz_save_breakpoint(self.h, os.fsencode(path)))
 
     def load_breakpoint(self, path):
+        """Restore a breakpoint; the context's grid (and self.grid) move to
+        the box it was saved with."""
         self._check(self.L.mdz_load_breakpoint(self.h, os.fsencode(path)))
+        self._follow_box()
+
+    # the box (PureShearALE) ---------------------------------------------------
+    def get_box(self):
+        """(xmin, xmax, zmin, zmax, dx, dz) of the grid the context works on."""
+        b = (C.c_double * 6)()
+        self._check(self.L.mdz_get_grid(self.h, b, None, None, None, None, None, None))
+        return tuple(b)
+
+    def _follow_box(self):
+        b = self.get_box()
+        g = self.grid
+        if (b[0], b[1], b[2], b[3]) != (g.xmin, g.xmax, g.zmin, g.zmax):
+            g.regrid(*b[:4])
+
+    def pure_shear_ale(self, dt, u=None, v=None):
+        """mdz_PureShearALE on host velocities u, v (or the resident ones):
+        returns the new (xmin, xmax, zmin, zmax); self.grid follows."""
+        b = (C.c_double * 4)()
+        uu = None if u is None else np.ascontiguousarray(u, np.float64)
+        vv = None if v is None else np.ascontiguousarray(v, np.float64)
+        self._check(self.L.mdz_PureShearALE(self.h, _dptr(uu), _dptr(vv), C.c_double(dt), b))
+        self._follow_box()
+        return tuple(b)
+
+    def set_boundary_values(self, grid=None):
+        """Upload the Dirichlet values of `grid` (default self.grid)."""
+        g = grid or self.grid
+        self._check(self.L.mdz_set_boundary_values(self.h, _dptr(g.BCu_val), _dptr(g.BCv_val)))
 
     def set_marker_velocity(self, vx, vz):
         vx = np.ascontiguousarray(vx, np.float64)
@@ -437,8 +480,13 @@ class Context:
         return d
 
     def time_step(self, mat, model):
+        """mdz_time_step; with model.ispureshear_ale the box moves and
+        self.grid follows it (its Dirichlet values for the next step are the
+        setup's to renew: set_boundary_values)."""
         rep = StepReport()
         self._check(self.L.mdz_time_step(self.h, C.byref(mat), C.byref(model), C.byref(rep)))
+        if model.ispureshear_ale:
+            self._follow_box()
         return rep
 
     def SolveStokesDefect(self, fields, jacobian, precision, rtol, maxit, Fu, Fv, Fp):
@@ -495,7 +543,7 @@ FIELD_NAMES = [
     "D11_n", "D12_n", "D13_n", "D14_n", "D21_n", "D22_n", "D23_n", "D24_n",
     "D31_s", "D32_s", "D33_s", "D34_s",
     "roger_x", "roger_z", "rhs_p", "gx", "gz",
-    "ru", "rv", "rp",
+    "ru", "rv", "rp", "eII_exp", "eII_gbs",
 ]
 
 VERTEX_FIELDS = {"div_u_s", "exz", "exxd_s", "ezzd_s", "sxz0", "sxxd0_s", "szzd0_s", "mu_s", "T_s", "P_s", "d0_s",
@@ -552,6 +600,8 @@ MAT_DBL = ["eta0", "rho", "alp", "gs_ref", "Slim", "eta_vp", "n_vp",
            "nlin", "Alin", "Qlin", "Vlin", "mlin", "rlin", "flin", "alin", "Flin"]
 MAT_DBL2 = ["mu", "bet", "C", "phi", "psi", "C_end", "phi_end", "psi_end", "pls_start", "pls_end"]
 MAT_INT2 = ["coh_soft", "phi_soft", "psi_soft"]
+MAT_DBL3 = ["Qexp", "Sexp", "Eexp", "Gexp", "nexp",
+            "ngbs", "Agbs", "Qgbs", "Vgbs", "mgbs", "rgbs", "fgbs", "agbs", "Fgbs"]
 
 
 class Materials(C.Structure):
@@ -559,7 +609,8 @@ class Materials(C.Structure):
                 + [(n, C.c_int * MDZ_MAX_PHASES) for n in MAT_INT]
                 + [(n, C.c_double * MDZ_MAX_PHASES) for n in MAT_DBL]
                 + [(n, C.c_double * MDZ_MAX_PHASES) for n in MAT_DBL2]
-                + [(n, C.c_int * MDZ_MAX_PHASES) for n in MAT_INT2])
+                + [(n, C.c_int * MDZ_MAX_PHASES) for n in MAT_INT2]
+                + [(n, C.c_double * MDZ_MAX_PHASES) for n in MAT_DBL3])
 
     @classmethod
     def from_phases(cls, phases, R=8.314510):
@@ -599,18 +650,19 @@ class Model(C.Structure):
                 ("softening", C.c_int), ("advect", C.c_int), ("picard2newton", C.c_int),
                 ("pic2newt_cond", C.c_double), ("nit_pic_max", C.c_int), ("newton_maxit", C.c_int),
                 ("adaptive_lin_tol", C.c_int), ("fp32_rheology_its", C.c_int), ("mg_reuse_below", C.c_double),
-                ("reseed", C.c_int), ("min_part_cell", C.c_int), ("direct_neighbour", C.c_int)]
+                ("reseed", C.c_int), ("min_part_cell", C.c_int), ("direct_neighbour", C.c_int),
+                ("ispureshear_ale", C.c_int)]
 
     @classmethod
     def make(cls, rheo, gx=0.0, gz=0.0, newton=1, nit_max=10, rel_tol=1e-8, abs_tol=1e-300, lin_rtol=1e-5,
              lin_maxit=500, line_search=0, line_search_min=0.0, precision=64, learned_guess=0, itp_stencil=1,
              softening=0, advect=1, picard2newton=0, pic2newt_cond=1e-1, nit_pic_max=10, newton_maxit=0,
              adaptive_lin_tol=0, fp32_rheology_its=0, mg_reuse_below=0.0, reseed=0, min_part_cell=16,
-             direct_neighbour=0):
+             direct_neighbour=0, ispureshear_ale=0):
         return cls(rheo, gx, gz, newton, nit_max, rel_tol, abs_tol, lin_rtol, lin_maxit, line_search,
                    line_search_min, precision, learned_guess, itp_stencil, softening, advect, picard2newton,
                    pic2newt_cond, nit_pic_max, newton_maxit, adaptive_lin_tol, fp32_rheology_its, mg_reuse_below,
-                   reseed, min_part_cell, direct_neighbour)
+                   reseed, min_part_cell, direct_neighbour, ispureshear_ale)
 
 
 class StepReport(C.Structure):
@@ -622,7 +674,8 @@ class StepReport(C.Structure):
                 ("ms_total", C.c_double), ("newton_its", C.c_int), ("local_iterations", C.c_longlong),
                 ("res_history", (C.c_double * 3) * 32), ("lin_its_history", C.c_int * 32),
                 ("lin_rel_history", C.c_double * 32), ("newton_history", C.c_int * 32),
-                ("precision_fallbacks", C.c_int), ("markers_added", C.c_int)]
+                ("precision_fallbacks", C.c_int), ("markers_added", C.c_int),
+                ("xmin", C.c_double), ("xmax", C.c_double), ("zmin", C.c_double), ("zmax", C.c_double)]
 
     def as_dict(self):
         def plain(v):

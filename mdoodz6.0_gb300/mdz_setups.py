@@ -81,7 +81,10 @@ def config_inclusion(N=101, nm=4, seed=12345):
               dict(cstv=1, eta0=1e3, mu=1.0, bet=1.0, C=1e90, phi=0.0, rho=1.0, Slim=1e90, n_vp=1.0, gs_ref=1.0)]
     mat = mdz.Materials.from_phases(phases)
     prm = mdz.RheoParams.make(dt=1e-3, iselastic=0, step=1, eta_avg=0)
-    model = mdz.Model.make(prm, newton=0, nit_max=4, rel_tol=1e-8, lin_rtol=1e-9, line_search=0)
+    # a linear problem: one defect solve, to 1e-12 (the pressure around a 1e3
+    # inclusion is conditioned far worse than the velocity: a 1e-9 solve leaves
+    # ~1e-6 relative pressure error)
+    model = mdz.Model.make(prm, newton=0, nit_max=4, rel_tol=1e-8, lin_rtol=1e-12, line_search=0)
     u, v = pure_shear_velocity(g, 1.0)
     return dict(name="inclusion", grid=g, markers=_markers_dict(x, z, ph), mat=mat, model=model, u=u, v=v,
                 p=np.zeros(g.size(1)))
@@ -90,7 +93,19 @@ def config_inclusion(N=101, nm=4, seed=12345):
 def config_vep(N=401, nm=4, seed=12345, noise=0.01):
     """Visco-elasto-plastic Drucker-Prager pure shear: G = 1, eta = 1e3, C = 1
     with 1 % seeded per-marker noise, phi = 30 deg, psi = 0, dt = 1e-2,
-    eps_BG = 1; viscoplastic regularisation eta_vp = 0.05."""
+    eps_BG = 1; viscoplastic regularisation eta_vp = 0.05.
+
+    The box deforms with the flow (ispureshear_ALE = 1, as the reference's
+    shear-band setup BENCHMARKS_old_input/SH_Duretz14.txt runs it): at
+    dt = 1e-2 the inflow through fixed walls would move markers two cells
+    (401 x 401) to ten cells (2049 x 2049) per step, more than the reseeding's
+    two-quarter-cell neighbourhood (CountPartCell) can refill.  The material
+    is homogeneous, so until the stress reaches the yield stress the
+    pure-shear start is the solution (residual at round-off, ~1e-19): the
+    absolute tolerance abs_tol = 1e-14 (the reference's abs_tol_u / abs_tol_p
+    test, Main_DOODZ.c:830) accepts it; relative tolerance 1e-8 otherwise.
+    Loading is elastic, tau_II = 2 G t to first order, so yielding
+    (C cos phi = 0.866) starts near step 44."""
     import mdz
     g = mdz.Grid(N, N, -0.5, 0.5, -0.5, 0.5).set_bc_pureshear(1.0)
     x, z = seed_markers(g, nm, nm, 0.5, seed)
@@ -100,11 +115,11 @@ def config_vep(N=401, nm=4, seed=12345, noise=0.01):
                    eta_vp=0.05, n_vp=1.0, gs_ref=1.0, pls_start=0.0, pls_end=1.0)]
     mat = mdz.Materials.from_phases(phases)
     prm = mdz.RheoParams.make(dt=1e-2, iselastic=1, step=1, eta_avg=0)
-    model = mdz.Model.make(prm, newton=1, nit_max=10, rel_tol=1e-8, lin_rtol=1e-6, line_search=1,
-                           reseed=1, min_part_cell=16, direct_neighbour=0)
+    model = mdz.Model.make(prm, newton=1, nit_max=10, rel_tol=1e-8, abs_tol=1e-14, lin_rtol=1e-6, line_search=1,
+                           reseed=1, min_part_cell=16, direct_neighbour=0, ispureshear_ale=1)
     u, v = pure_shear_velocity(g, 1.0)
     m = _markers_dict(x, z, ph, cmul=1.0 + noise * rng.standard_normal(len(x)))
-    return dict(name="vep", grid=g, markers=m, mat=mat, model=model, u=u, v=v, p=np.zeros(g.size(1)))
+    return dict(name="vep", grid=g, markers=m, mat=mat, model=model, u=u, v=v, p=np.zeros(g.size(1)), eps_bg=1.0)
 
 
 def config_lithosphere(Nx=1025, Nz=513, nm=4, seed=12345, precision=64, learned=0):
@@ -187,12 +202,25 @@ def config_lithosphere(Nx=1025, Nz=513, nm=4, seed=12345, precision=64, learned=
 def config_shear_band(N=2049, nm=4, seed=12345, noise=0.01, precision=64, learned=0):
     """Shear-band localisation: VEP pure shear with cohesion softening linearly
     from 1 to 0.5 over accumulated plastic strain 0-1, 1 % seeded cohesion
-    noise, 16 markers per cell."""
+    noise, 16 markers per cell, box deforming with the flow.
+
+    The time step is the Courant step of the walls (Courant number 0.5 at
+    |v| = 0.5: dt = dx), the reference's default criterion (Courant = 0.5,
+    EvaluateCourantCriterion): with the deforming box each step loses the
+    markers of a band 0.5 dt |v| wide at the inflowing walls (the midpoint
+    stage of RogerGuntherII leaves the box), which the reseeding refills only
+    while the band is at most two quarter cells (dt <= 4 dx); the 1e-2 step
+    of the 401 x 401 model is twenty times that at 2049 x 2049.  The shear
+    modulus is 100 so that the elastic loading, 2 G dt per step, reaches the
+    yield stress (C cos phi = 0.87) after some nine steps and leaves forty for
+    yielding, softening and localisation."""
     cfg = config_vep(N=N, nm=nm, seed=seed, noise=noise)
     import mdz
-    phases = [dict(cstv=1, eta0=1e3, mu=1.0, bet=1e-2, C=1.0, C_end=0.5, coh_soft=1, phi=np.pi / 6, psi=0.0,
+    g = cfg["grid"]
+    phases = [dict(cstv=1, eta0=1e3, mu=100.0, bet=1e-2, C=1.0, C_end=0.5, coh_soft=1, phi=np.pi / 6, psi=0.0,
                    rho=1.0, Slim=1e10, eta_vp=0.05, n_vp=1.0, gs_ref=1.0, pls_start=0.0, pls_end=1.0)]
     cfg["mat"] = mdz.Materials.from_phases(phases)
+    cfg["model"].rheo.dt = min(g.dx, g.dz) * 0.5 / 0.5
     cfg["model"].softening = 1
     cfg["model"].nit_max = 15
     cfg["model"].precision = precision
@@ -226,6 +254,25 @@ def marker_capacity(cfg):
     g = cfg["grid"]
     n = len(cfg["markers"]["x"])
     return 2 * n + 4 * g.ncx * g.ncz
+
+
+def renew_bcs(cfg):
+    """The setup's SetBCs for the next step: with a deforming box
+    (ispureshear_ale) the pure-shear Dirichlet values follow the moved walls.
+    Returns True when they changed."""
+    if not cfg["model"].ispureshear_ale:
+        return False
+    cfg["grid"].set_bc_pureshear(cfg["eps_bg"])
+    return True
+
+
+def time_step(ctx, cfg):
+    """One time step of a configuration on a context from load_context: the
+    library's step, then the setup's boundary values for the next one."""
+    rep = ctx.time_step(cfg["mat"], cfg["model"])
+    if renew_bcs(cfg):
+        ctx.set_boundary_values(cfg["grid"])
+    return rep
 
 
 def load_context(cfg, max_markers=None):

@@ -60,7 +60,8 @@ MEMBERS = {
                                             "Qpwl", "Vpwl", "npwl", "mpwl", "Apwl", "apwl", "fpwl", "rpwl", "Fpwl",
                                             "pref_pwl", "Qlin", "Vlin", "nlin", "mlin", "Alin", "alin", "flin",
                                             "rlin", "Flin", "gs_ref", "C_end", "phi_end", "psi_end", "pls_start",
-                                            "pls_end", "eta_vp", "n_vp")]
+                                            "pls_end", "eta_vp", "n_vp", "Qexp", "Sexp", "Eexp", "Gexp", "nexp",
+                                            "Qgbs", "Vgbs", "ngbs", "mgbs", "Agbs", "agbs", "fgbs", "rgbs", "Fgbs")]
                 + [(I + "[20]", n) for n in ("gs", "cstv", "pwlv", "linv", "expv", "gbsv", "phi_soft", "psi_soft",
                                             "coh_soft", "is_tensile", "reac_soft", "phase_mix")],
     "grid": [(I, "Nx"), (I, "Nz"), (D, "dx"), (D, "dz")]

@@ -51,6 +51,10 @@
 #endif
 #include "mdoodz_refshim.h"
 
+/* BC tags are plain char in the reference's structures: signed on x86-64,
+ * unsigned on AArch64, so every comparison reads them as signed char. */
+#define TAG(t) ((signed char)(t))
+
 static mdz_ctx *g_ctx = NULL;
 static mdz_grid_desc g_desc;         /* the grid of the context (the caller's arrays) */
 static int g_nph = 0;
@@ -230,6 +234,7 @@ static void fields_of(grid *m, mdz_fields *f, int nph, int with_pp) {
     f->rho_s = m->rho_s; f->eta_n = m->eta_n; f->eta_s = m->eta_s; f->eta_phys_n = m->eta_phys_n;
     f->eta_phys_s = m->eta_phys_s; f->VE_n = m->VE_n; f->VE_s = m->VE_s; f->sxxd = m->sxxd; f->szzd = m->szzd;
     f->sxz = m->sxz; f->sxz_n = m->sxz_n; f->eII_el = m->eII_el; f->eII_pl = m->eII_pl; f->eII_pwl = m->eII_pwl;
+    f->eII_exp = m->eII_exp; f->eII_gbs = m->eII_gbs;
     f->eII_lin = m->eII_lin; f->eII_cst = m->eII_cst; f->d_n = m->d_n; f->exx_el = m->exx_el;
     f->ezz_el = m->ezz_el; f->exz_el = m->exz_el; f->exx_diss = m->exx_diss; f->ezz_diss = m->ezz_diss;
     f->exz_diss = m->exz_diss; f->detadexx_n = m->detadexx_n; f->detadezz_n = m->detadezz_n;
@@ -269,7 +274,7 @@ static void keep_only(mdz_fields *f, const char *names) {
     KEEP(strain_n) KEEP(strain_s) KEEP(dil_n) KEEP(dil_s) KEEP(fric_n) KEEP(fric_s) KEEP(C_n) KEEP(C_s) KEEP(p0_n)
     KEEP(p0_s) KEEP(bet_n) KEEP(bet_s) KEEP(rho_n) KEEP(rho_s) KEEP(phase_perc_n) KEEP(phase_perc_s) KEEP(eta_n)
     KEEP(eta_s) KEEP(eta_phys_n) KEEP(eta_phys_s) KEEP(VE_n) KEEP(VE_s) KEEP(sxxd) KEEP(szzd) KEEP(sxz) KEEP(sxz_n)
-    KEEP(eII_el) KEEP(eII_pl) KEEP(eII_pwl) KEEP(eII_lin) KEEP(eII_cst) KEEP(d_n) KEEP(exx_el) KEEP(ezz_el)
+    KEEP(eII_el) KEEP(eII_pl) KEEP(eII_pwl) KEEP(eII_lin) KEEP(eII_cst) KEEP(eII_exp) KEEP(eII_gbs) KEEP(d_n) KEEP(exx_el) KEEP(ezz_el)
     KEEP(exz_el) KEEP(exx_diss) KEEP(ezz_diss) KEEP(exz_diss) KEEP(detadexx_n) KEEP(detadezz_n) KEEP(detadgxz_n)
     KEEP(detadp_n) KEEP(ddivpdexx_n) KEEP(ddivpdezz_n) KEEP(ddivpdgxz_n) KEEP(ddivpdp_n) KEEP(detadexx_s)
     KEEP(detadezz_s) KEEP(detadgxz_s) KEEP(detadp_s) KEEP(div_u_el) KEEP(div_u_pl) KEEP(div_u_r) KEEP(Wtot)
@@ -299,6 +304,11 @@ static void materials_of(const mat_prop *mp, int nph, mdz_materials *m) {
         m->psi[p] = mp->psi[p]; m->C_end[p] = mp->C_end[p]; m->phi_end[p] = mp->phi_end[p];
         m->psi_end[p] = mp->psi_end[p]; m->pls_start[p] = mp->pls_start[p]; m->pls_end[p] = mp->pls_end[p];
         m->coh_soft[p] = mp->coh_soft[p]; m->phi_soft[p] = mp->phi_soft[p]; m->psi_soft[p] = mp->psi_soft[p];
+        m->Qexp[p] = mp->Qexp[p]; m->Sexp[p] = mp->Sexp[p]; m->Eexp[p] = mp->Eexp[p]; m->Gexp[p] = mp->Gexp[p];
+        m->nexp[p] = mp->nexp[p];
+        m->ngbs[p] = mp->ngbs[p]; m->Agbs[p] = mp->Agbs[p]; m->Qgbs[p] = mp->Qgbs[p]; m->Vgbs[p] = mp->Vgbs[p];
+        m->mgbs[p] = mp->mgbs[p]; m->rgbs[p] = mp->rgbs[p]; m->fgbs[p] = mp->fgbs[p]; m->agbs[p] = mp->agbs[p];
+        m->Fgbs[p] = mp->Fgbs[p];
     }
 }
 
@@ -365,10 +375,10 @@ void UpdateNonLinearity(grid *mesh, markers *particles, markers *topo_chain, sur
 static void rows_to_eqn(const grid *m, const SparseMat *S, const double *ru, const double *rv, const double *rp,
                         double *Fm, double *Fc) {
     const int nu = m->Nx * (m->Nz + 1), nv = (m->Nx + 1) * m->Nz, np = (m->Nx - 1) * (m->Nz - 1);
-    for (int c = 0; c < nu; c++) if (S->eqn_u[c] >= 0 && m->BCu.type[c] == -1) Fm[S->eqn_u[c]] = ru[c];
-    for (int c = 0; c < nv; c++) if (S->eqn_v[c] >= 0 && m->BCv.type[c] == -1) Fm[S->eqn_v[c]] = rv[c];
+    for (int c = 0; c < nu; c++) if (S->eqn_u[c] >= 0 && TAG(m->BCu.type[c]) == -1) Fm[S->eqn_u[c]] = ru[c];
+    for (int c = 0; c < nv; c++) if (S->eqn_v[c] >= 0 && TAG(m->BCv.type[c]) == -1) Fm[S->eqn_v[c]] = rv[c];
     for (int c = 0; c < np; c++)
-        if (S->eqn_p[c] >= 0 && m->BCp.type[c] == -1) Fc[S->eqn_p[c] - S->neq_mom] = rp[c];
+        if (S->eqn_p[c] >= 0 && TAG(m->BCp.type[c]) == -1) Fc[S->eqn_p[c] - S->neq_mom] = rp[c];
 }
 
 /* Assemble = 1 records the operator for the next defect solve (matrix-free);
@@ -422,18 +432,18 @@ static void extract(grid *m, const params *model, const double *du, const double
                     double alpha) {
     const int Nx = m->Nx, Nz = m->Nz, nu = Nx * (Nz + 1), nv = (Nx + 1) * Nz, np = (Nx - 1) * (Nz - 1);
     (void)model;
-    for (int c = 0; c < nu; c++) if (m->BCu.type[c] == -1) m->u_in[c] += alpha * du[c];
-    for (int c = 0; c < nv; c++) if (m->BCv.type[c] == -1) m->v_in[c] += alpha * dv[c];
-    for (int c = 0; c < np; c++) if (m->BCp.type[c] == -1) m->p_in[c] += alpha * dp[c];
-    for (int c = 0; c < nu; c++) if (m->BCu.type[c] == 0) m->u_in[c] = m->BCu.val[c];
-    for (int c = 0; c < nv; c++) if (m->BCv.type[c] == 0) m->v_in[c] = m->BCv.val[c];
+    for (int c = 0; c < nu; c++) if (TAG(m->BCu.type[c]) == -1) m->u_in[c] += alpha * du[c];
+    for (int c = 0; c < nv; c++) if (TAG(m->BCv.type[c]) == -1) m->v_in[c] += alpha * dv[c];
+    for (int c = 0; c < np; c++) if (TAG(m->BCp.type[c]) == -1) m->p_in[c] += alpha * dp[c];
+    for (int c = 0; c < nu; c++) if (TAG(m->BCu.type[c]) == 0) m->u_in[c] = m->BCu.val[c];
+    for (int c = 0; c < nv; c++) if (TAG(m->BCv.type[c]) == 0) m->v_in[c] = m->BCv.val[c];
     for (int k = 0; k < Nx; k++) {
-        if (m->BCu.type[k] == 13) m->u_in[k] = m->u_in[k + Nx];
-        if (m->BCu.type[k + Nz * Nx] == 13) m->u_in[k + Nz * Nx] = m->u_in[k + (Nz - 1) * Nx];
+        if (TAG(m->BCu.type[k]) == 13) m->u_in[k] = m->u_in[k + Nx];
+        if (TAG(m->BCu.type[k + Nz * Nx]) == 13) m->u_in[k + Nz * Nx] = m->u_in[k + (Nz - 1) * Nx];
     }
     for (int l = 0; l < Nz; l++) {
-        if (m->BCv.type[l * (Nx + 1)] == 13) m->v_in[l * (Nx + 1)] = m->v_in[l * (Nx + 1) + 1];
-        if (m->BCv.type[l * (Nx + 1) + Nx] == 13) m->v_in[l * (Nx + 1) + Nx] = m->v_in[l * (Nx + 1) + Nx - 1];
+        if (TAG(m->BCv.type[l * (Nx + 1)]) == 13) m->v_in[l * (Nx + 1)] = m->v_in[l * (Nx + 1) + 1];
+        if (TAG(m->BCv.type[l * (Nx + 1) + Nx]) == 13) m->v_in[l * (Nx + 1) + Nx] = m->v_in[l * (Nx + 1) + Nx - 1];
     }
 }
 
@@ -452,11 +462,11 @@ static double *solve_defect(grid *mesh, params *model, SparseMat *Stokes, Sparse
     double *F = g_dx + n, *dx = g_dx;
     memset(F, 0, sizeof(double) * n);
     /* F from the equation-numbered StokesA->F / StokesC->F */
-    for (int c = 0; c < nu; c++) if (Stokes->eqn_u[c] >= 0 && mesh->BCu.type[c] == -1) F[c] = StokesA->F[Stokes->eqn_u[c]];
+    for (int c = 0; c < nu; c++) if (Stokes->eqn_u[c] >= 0 && TAG(mesh->BCu.type[c]) == -1) F[c] = StokesA->F[Stokes->eqn_u[c]];
     for (int c = 0; c < nv; c++)
-        if (Stokes->eqn_v[c] >= 0 && mesh->BCv.type[c] == -1) F[nu + c] = StokesA->F[Stokes->eqn_v[c]];
+        if (Stokes->eqn_v[c] >= 0 && TAG(mesh->BCv.type[c]) == -1) F[nu + c] = StokesA->F[Stokes->eqn_v[c]];
     for (int c = 0; c < np; c++)
-        if (Stokes->eqn_p[c] >= 0 && mesh->BCp.type[c] == -1)
+        if (Stokes->eqn_p[c] >= 0 && TAG(mesh->BCp.type[c]) == -1)
             F[nu + nv + c] = StokesC->F[Stokes->eqn_p[c] - Stokes->neq_mom];
     mdz_fields f;
     fields_of(mesh, &f, model->Nb_phases, 0);
@@ -532,11 +542,11 @@ double LineSearchDecoupled(SparseMat *Stokes, SparseMat *StokesA, SparseMat *Sto
     const int Nx = mesh->Nx, Nz = mesh->Nz, nu = Nx * (Nz + 1), nv = (Nx + 1) * Nz, np = (Nx - 1) * (Nz - 1);
     double *dx = (double *)calloc((size_t)nu + nv + np, sizeof(double));
     if (!dx) { fprintf(stderr, "mdz_refshim: out of host memory\n"); exit(1); }
-    for (int c = 0; c < nu; c++) if (Stokes->eqn_u[c] >= 0 && mesh->BCu.type[c] == -1) dx[c] = sol[Stokes->eqn_u[c]];
+    for (int c = 0; c < nu; c++) if (Stokes->eqn_u[c] >= 0 && TAG(mesh->BCu.type[c]) == -1) dx[c] = sol[Stokes->eqn_u[c]];
     for (int c = 0; c < nv; c++)
-        if (Stokes->eqn_v[c] >= 0 && mesh->BCv.type[c] == -1) dx[nu + c] = sol[Stokes->eqn_v[c]];
+        if (Stokes->eqn_v[c] >= 0 && TAG(mesh->BCv.type[c]) == -1) dx[nu + c] = sol[Stokes->eqn_v[c]];
     for (int c = 0; c < np; c++)
-        if (Stokes->eqn_p[c] >= 0 && mesh->BCp.type[c] == -1) dx[nu + nv + c] = sol[Stokes->eqn_p[c]];
+        if (Stokes->eqn_p[c] >= 0 && TAG(mesh->BCp.type[c]) == -1) dx[nu + nv + c] = sol[Stokes->eqn_p[c]];
     const double a = line_search(mesh, model, Nmodel, Stokes, StokesA, StokesB, StokesC, StokesD, materials, scaling,
                                  dx);
     free(dx);

@@ -96,7 +96,7 @@ int orc_strain_rates(const mdz_grid_desc *g, mdz_fields *f) {
 /* ------------------------------------------------------------------------ */
 /* Outputs of one local solve (the pointer arguments of Viscosity()). */
 typedef struct {
-    double eta, txx, tzz, txz, etaVE, VEcoeff, Eii_el, Eii_pl, Eii_pwl, Eii_lin, Eii_cst;
+    double eta, txx, tzz, txz, etaVE, VEcoeff, Eii_el, Eii_pl, Eii_pwl, Eii_lin, Eii_cst, Eii_exp, Eii_gbs;
     double Exx_el, Ezz_el, Exz_el, Exx_diss, Ezz_diss, Exz_diss, d1;
     double detadexx, detadezz, detadexz, detadp, X1, OverS;
     double ddivpdexx, ddivpdezz, ddivpdexz, ddivpdp, Pcorr, drhodp, rho, div_el, div_pl, div_r;
@@ -105,8 +105,9 @@ typedef struct {
 
 static double dmin(double a, double b) { return a <= b ? a : b; }
 
-/* Viscosity (RheologyDensity.c:44-707) for constant, dislocation and diffusion
- * creep, elasticity and Drucker-Prager / von Mises plasticity. */
+/* Viscosity (RheologyDensity.c:44-707) for constant, dislocation, diffusion
+ * and Peierls creep, grain-boundary sliding, elasticity and Drucker-Prager /
+ * von Mises plasticity with the tension cut-off. */
 static void orc_visc(int p, double G, double T, double P, double d, double phi, double X0, double Exx, double Ezz,
                      double Exz, double Gxx, double Gzz, double Gxz, double Txx0, double Tzz0, double Txz0,
                      const mdz_materials *m, const mdz_rheo_params *prm, double dil, double fric, double C, double P0,
@@ -114,6 +115,16 @@ static void orc_visc(int p, double G, double T, double P, double d, double phi, 
     double R = m->R, dt = prm->dt, minEta = prm->mineta, maxEta = prm->maxeta;
     int nitmax = 20, it, elastic = prm->iselastic;
     int constant = m->cstv[p] != 0, dislocation = m->pwlv[p] != 0, diffusion = m->linv[p] != 0;
+    /* :135-141 (Peierls tested before the 0 C clamp) */
+    int peierls = m->expv[p] != 0 && T < (1200.0 + ZEROC) / prm->scale_T, gbs = m->gbsv[p] != 0;
+    double Ea_gbs = m->Qgbs[p], Va_gbs = m->Vgbs[p], n_gbs = m->ngbs[p], m_gbs = m->mgbs[p], r_gbs = m->rgbs[p];
+    double A_gbs = m->Agbs[p], f_gbs = m->fgbs[p], a_gbs = m->agbs[p], F_gbs = m->Fgbs[p];
+    double B_gbs = 0, C_gbs = 0, eta_gbs = 0, Eii_gbs = 0;
+    double Ea_exp = m->Qexp[p], S_exp = m->Sexp[p], E_exp = m->Eexp[p], gamma = m->Gexp[p], n_exp = m->nexp[p];
+    double ST = 0, B_exp = 0, C_exp = 0, F_exp = 0, eta_exp = 0, Eii_exp = 0;
+    double Exx_exp = 0, Ezz_exp = 0, Exz_exp = 0;
+    int tens = 0;
+    double dsin_dildExx = 0.0, dsin_dildEzz = 0.0, dsin_dildExz = 0.0, dsin_dildP = 0.0;
     double tol = 1.0e-11, res = 0.0, res0 = 0.0, dfdeta, Txx, Tzz, Txz, Tii, ieta_sum;
     double Tii0 = sqrt(Txx0 * Txx0 + Txz0 * Txz0);
     double eta_up, eta_lo, eta_ve, eta_pwl = 0.0, eta_lin = 0.0, eta_el, eta_cst = 0.0, eta_vep = 0.0;
@@ -159,23 +170,48 @@ static void orc_visc(int p, double G, double T, double P, double d, double phi, 
         C_lin = pow(2.0 * f_ani * B_lin, -n_lin);
         dClindP = -C_lin * Va_lin / R / T;
     }
+    if (gbs) {
+        B_gbs = F_gbs * pow(A_gbs, -1.0 / n_gbs) * exp((Ea_gbs + P * Va_gbs) / R / n_gbs / T) * pow(d, m_gbs / n_gbs) *
+                pow(f_gbs, -r_gbs / n_gbs) * exp(-a_gbs * phi / n_gbs);
+        C_gbs = pow(2.0 * f_ani * B_gbs, -n_gbs);
+    }
+    if (peierls) {   /* :181-199, the "new" form */
+        ST = Ea_exp / R / T * 2.0 * gamma * (1 - gamma);
+        double Arr_exp = exp(-Ea_exp / R / T * pow(1.0 - gamma, 2.0));
+        F_exp = pow(pow(2.0, 1.0 - ST - n_exp) / pow(sqrt(3.0), ST + n_exp + 1.0), 1.0 / (ST + n_exp));
+        B_exp = F_exp * (pow(gamma * S_exp, ST / (ST + n_exp)) / pow(E_exp * Arr_exp, 1.0 / (ST + n_exp)));
+        C_exp = pow(2.0 * f_ani * B_exp, -(ST + n_exp));
+    }
     /* yield :214-225 */
     double cos_fric = cos(fric), sin_fric = sin(fric), sin_dil = sin(dil);
     Tyield = C * cos_fric + P * sin_fric;
     if (m->Slim[p] < Tyield) { sin_fric = 0.0; cos_fric = 1.0; sin_dil = 0.0; C = m->Slim[p]; Tyield = m->Slim[p]; }
+    {   /* tension cut-off :204-213 */
+        double P_tens = -25e6 / prm->scale_S;
+        double sin_fric_tens = -C * cos_fric / P_tens;
+        if (C * cos_fric + P * sin_fric_tens < Tyield && m->is_tensile[p] == 1) {
+            sin_fric = sin_fric_tens;
+            Tyield = C * cos_fric + P * sin_fric_tens;
+            tens = 1;
+        }
+    }
     o->X1 = X0;
     /* isolated viscosities :320-330 */
     eta_el = G * dt;
     if (constant) eta_cst = m->eta0[p];
     if (dislocation) eta_pwl = B_pwl * pow(Eii, 1.0 / n_pwl - 1.0);
     if (diffusion) eta_lin = B_lin * pow(Eii, 1.0 / n_lin - 1.0) * pow(d, m_lin / n_lin);
+    if (gbs) eta_gbs = B_gbs * pow(Eii, 1.0 / n_gbs - 1.0);
+    if (peierls) eta_exp = B_exp * pow(Eii, 1.0 / (ST + n_exp) - 1.0);
     /* bounds :340-378 */
     eta_up = 1.0e100 / prm->scale_eta;
     ieta_sum = 0.0;
     if (constant) { eta_up = dmin(eta_up, eta_cst); ieta_sum += 1.0 / eta_cst; }
     if (dislocation) { eta_up = dmin(eta_up, eta_pwl); ieta_sum += 1.0 / eta_pwl; }
     if (elastic) { eta_up = dmin(eta_up, eta_el); ieta_sum += 1.0 / eta_el; }
+    if (peierls) { eta_up = dmin(eta_up, eta_exp); ieta_sum += 1.0 / eta_exp; }
     if (diffusion) { eta_up = dmin(eta_up, eta_lin); ieta_sum += 1.0 / eta_lin; }
+    if (gbs) { eta_up = dmin(eta_up, eta_gbs); ieta_sum += 1.0 / eta_gbs; }
     eta_lo = 1.0 / ieta_sum;
     (void)eta_lo;
     /* local Newton on eta_ve :384-415 */
@@ -184,14 +220,17 @@ static void orc_visc(int p, double G, double T, double P, double d, double phi, 
         Tii = 2.0 * f_ani * eta_ve * Eii;
         if (constant) Eii_cst = Tii / f_ani / 2.0 / eta_cst;
         if (dislocation) Eii_pwl = C_pwl * pow(Tii, n_pwl);
+        if (gbs) Eii_gbs = C_gbs * pow(Tii, n_gbs);
+        if (peierls) Eii_exp = C_exp * pow(Tii, ST + n_exp);
         if (diffusion) Eii_lin = C_lin * pow(Tii, n_lin) * pow(o->d1, -m_lin);
-        double Eii_vis = Eii_pwl + Eii_lin + Eii_cst;
+        double Eii_vis = Eii_pwl + Eii_exp + Eii_lin + Eii_gbs + Eii_cst;
         double r = Eii - elastic * Tii / (2.0 * eta_el) - Eii_vis;
         res = fabs(r / Eii);
         if (it == 0) res0 = res;
         if (res < tol / 100) break;
         dfdeta = 0.0;
         if (elastic) dfdeta += -Eii / eta_el;
+        if (peierls) dfdeta += -Eii_exp * (ST + n_exp) / eta_ve;
         if (diffusion) dfdeta += -Eii_lin * n_lin / eta_ve;
         if (dislocation) dfdeta += -Eii_pwl * n_pwl / eta_ve;
         if (constant) dfdeta += -Eii / eta_cst;
@@ -208,10 +247,13 @@ static void orc_visc(int p, double G, double T, double P, double d, double phi, 
     if (dislocation) eta_pwl = pow(2.0 * C_pwl, -1.0) * pow(Tii, 1.0 - n_pwl);
     if (diffusion) eta_lin = B_lin * pow(Eii_lin, 1.0 / n_lin - 1.0) * pow(o->d1, m_lin / n_lin);
     if (diffusion) { Exx_lin = Txx / 2.0 / eta_lin; Ezz_lin = Tzz / 2.0 / eta_lin; Exz_lin = Txz / 2.0 / eta_lin; }
+    if (peierls) eta_exp = B_exp * pow(Eii_exp, 1.0 / (ST + n_exp) - 1.0);
+    if (peierls) { Exx_exp = Txx / 2.0 / eta_exp; Ezz_exp = Tzz / 2.0 / eta_exp; Exz_exp = Txz / 2.0 / eta_exp; }
     if (constant) { Exx_cst = Txx / 2.0 / eta_cst; Ezz_cst = Tzz / 2.0 / eta_cst; Exz_cst = Txz / 2.0 / eta_cst; }
     /* VE tangent :449-471 */
     deta = 0.0;
     if (dislocation) deta += -C_pwl * pow(Tii, n_pwl - 3.0) * (n_pwl - 1.0);
+    if (peierls) deta += -C_exp * pow(Tii, n_exp + ST - 3.0) * (n_exp + ST - 1.0);
     if (diffusion) deta += -C_lin * pow(Tii, n_lin - 3.0) * (n_lin - 1.0) * pow(o->d1, -m_lin);
     detadTxx = deta * (2.0 * Txx + Tzz) * pow(eta_ve, 2.0);
     detadTzz = deta * (2.0 * Tzz + Txx) * pow(eta_ve, 2.0);
@@ -227,6 +269,12 @@ static void orc_visc(int p, double G, double T, double P, double d, double phi, 
     dve_dP = pow(eta_ve, 2) * dummy;
     /* plasticity :482-560 */
     F_trial = Tii - Tyield;
+    if (tens == 1) {   /* :456-465 */
+        eta_vp = eta_vp0 * pow(Eii, 1.0 / n_vp - 1);
+        double Pc_chk = -(C * cos_fric) / (-Tii / P + sin_fric);
+        sin_dil = (P * eta_ve + P * eta_vp - Pc_chk * eta_ve - Pc_chk * eta_vp) /
+                  (K * dt * (C * cos_fric + Pc_chk * sin_fric - Tii));
+    }
     if (F_trial > 1e-17) {
         is_pl = 1;
         eta_vp = eta_vp0 * pow(Eii, 1.0 / n_vp - 1);
@@ -262,35 +310,55 @@ static void orc_visc(int p, double G, double T, double P, double d, double phi, 
         o->Pcorr = Pc;
     }
     (void)Tyy;
-    /* VEP tangent :573-603 (tension branch not implemented) */
+    /* VEP tangent :573-603 */
     if (is_pl) {
+        if (tens == 1) {   /* :578-587 */
+            double dEii_dExx = (2.0 * Exx + Ezz) / 2.0 / Eii;
+            double dEii_dEzz = (2.0 * Ezz + Exx) / 2.0 / Eii;
+            double dEii_dExz = Exz / 1.0 / Eii;
+            double A = 2 * Eii * eta_ve - P * sin_fric;
+            double den = K * dt * A * (C * P * cos_fric * sin_fric + (C * cos_fric - 2 * Eii * eta_ve) * A);
+            dsin_dildExx = (2 * K * dt * sin_dil * (Eii * dve_dExx + dEii_dExx * eta_ve) * (C * P * cos_fric * sin_fric + pow(A, 2)) +
+                            P * (-C * cos_fric * dve_dExx * A + 2 * C * cos_fric * (eta_ve + eta_vp) * (Eii * dve_dExx + dEii_dExx * eta_ve) +
+                                 dve_dExx * pow(A, 2))) / den;
+            dsin_dildEzz = (2 * K * dt * sin_dil * (Eii * dve_dEzz + dEii_dEzz * eta_ve) * (C * P * cos_fric * sin_fric + pow(A, 2)) +
+                            P * (-C * cos_fric * dve_dEzz * A + 2 * C * cos_fric * (eta_ve + eta_vp) * (Eii * dve_dEzz + dEii_dEzz * eta_ve) +
+                                 dve_dEzz * pow(A, 2))) / den;
+            dsin_dildExz = (2 * K * dt * sin_dil * (Eii * dve_dExz + dEii_dExz * eta_ve) * (C * P * cos_fric * sin_fric + pow(A, 2)) +
+                            P * (-C * cos_fric * dve_dExz * A + 2 * C * cos_fric * (eta_ve + eta_vp) * (Eii * dve_dExz + dEii_dExz * eta_ve) +
+                                 dve_dExz * pow(A, 2))) / den;
+            dsin_dildP = (2 * C * Eii * cos_fric * (eta_ve + eta_vp) * (P * dve_dP - eta_ve) - C * P * cos_fric * dve_dP * A +
+                          2 * Eii * K * dt * sin_dil * (C * cos_fric * sin_fric * (P * dve_dP - eta_ve) + dve_dP * pow(A, 2)) +
+                          pow(A, 2) * (P * dve_dP + eta_ve + eta_vp)) / den;
+        }
         double dFdExx = (2.0 * Exx + Ezz) * eta_ve / Eii + 2.0 * Eii * dve_dExx;
         double dFdEzz = (2.0 * Ezz + Exx) * eta_ve / Eii + 2.0 * Eii * dve_dEzz;
         double dFdExz = 2.0 * Exz * eta_ve / Eii + 2.0 * Eii * dve_dExz;
         double dFdP = -sin_fric + 2.0 * Eii * dve_dP;
         double gg = 1.0 / (eta_ve + eta_vp / n_vp + K * dt * sin_fric * sin_dil);
-        dlamdExx = gg * (dFdExx - gdot * (dve_dExx + K * dt * sin_fric * 0.0));
-        dlamdEzz = gg * (dFdEzz - gdot * (dve_dEzz + K * dt * sin_fric * 0.0));
-        dlamdExz = gg * (dFdExz - gdot * (dve_dExz + K * dt * sin_fric * 0.0));
-        dlamdP = gg * (dFdP - gdot * (dve_dP + K * dt * sin_fric * 0.0));
+        dlamdExx = gg * (dFdExx - gdot * (dve_dExx + K * dt * sin_fric * dsin_dildExx));
+        dlamdEzz = gg * (dFdEzz - gdot * (dve_dEzz + K * dt * sin_fric * dsin_dildEzz));
+        dlamdExz = gg * (dFdExz - gdot * (dve_dExz + K * dt * sin_fric * dsin_dildExz));
+        dlamdP = gg * (dFdP - gdot * (dve_dP + K * dt * sin_fric * dsin_dildP));
         double dvp_dExx = eta_vp / gdot * dlamdExx * (1.0 / n_vp - 1.0);
         double dvp_dEzz = eta_vp / gdot * dlamdEzz * (1.0 / n_vp - 1.0);
         double dvp_dExz = eta_vp / gdot * dlamdExz * (1.0 / n_vp - 1.0);
         double dvp_dP = eta_vp / gdot * dlamdP * (1.0 / n_vp - 1.0);
         double a = eta_vp + K * dt * sin_fric * sin_dil;
         dvep_dExx = -0.5 * (2.0 * Exx + Ezz) * Tyield / (2.0 * pow(Eii, 3.0)) +
-                    (a * dlamdExx + gdot * dvp_dExx + gdot * K * dt * sin_fric * 0.0) / (2.0 * Eii);
+                    (a * dlamdExx + gdot * dvp_dExx + gdot * K * dt * sin_fric * dsin_dildExx) / (2.0 * Eii);
         dvep_dEzz = -0.5 * (2.0 * Ezz + Exx) * Tyield / (2.0 * pow(Eii, 3.0)) +
-                    (a * dlamdEzz + gdot * dvp_dEzz + gdot * K * dt * sin_fric * 0.0) / (2.0 * Eii);
+                    (a * dlamdEzz + gdot * dvp_dEzz + gdot * K * dt * sin_fric * dsin_dildEzz) / (2.0 * Eii);
         dvep_dExz = -Exz * Tyield / (2.0 * pow(Eii, 3.0)) +
-                    (a * dlamdExz + gdot * dvp_dExz + gdot * K * dt * sin_fric * 0.0) / (2.0 * Eii);
-        dvep_dP = (sin_fric + a * dlamdP + gdot * dvp_dP + gdot * K * dt * sin_fric * 0.0) / (2.0 * Eii);
+                    (a * dlamdExz + gdot * dvp_dExz + gdot * K * dt * sin_fric * dsin_dildExz) / (2.0 * Eii);
+        dvep_dP = (sin_fric + a * dlamdP + gdot * dvp_dP + gdot * K * dt * sin_fric * dsin_dildP) / (2.0 * Eii);
     }
     /* density :632-640 (non-reactive branch) */
     o->rho = m->rho[p] * exp(1.0 / K * Pc - m->alp[p] * T);
     o->drhodp = o->rho / K;
     /* outputs :657-707 */
     double inv_eta_diss = 0.0;
+    if (peierls) inv_eta_diss += 1.0 / eta_exp;
     if (dislocation) inv_eta_diss += 1.0 / eta_pwl;
     if (diffusion) inv_eta_diss += 1.0 / eta_lin;
     if (constant) inv_eta_diss += 1.0 / eta_cst;
@@ -302,10 +370,10 @@ static void orc_visc(int p, double G, double T, double P, double d, double phi, 
     } else {
         o->detadexx = dvep_dExx; o->detadezz = dvep_dEzz; o->detadexz = dvep_dExz; o->detadp = dvep_dP;
         o->etaVE = eta_vep;
-        o->ddivpdexx = -dQdP * dlamdExx + gdot * 0.0;
-        o->ddivpdezz = -dQdP * dlamdEzz + gdot * 0.0;
-        o->ddivpdexz = -dQdP * dlamdExz + gdot * 0.0;
-        o->ddivpdp = -dQdP * dlamdP + gdot * 0.0 + 0.0;
+        o->ddivpdexx = -dQdP * dlamdExx + gdot * dsin_dildExx;
+        o->ddivpdezz = -dQdP * dlamdEzz + gdot * dsin_dildEzz;
+        o->ddivpdexz = -dQdP * dlamdExz + gdot * dsin_dildExz;
+        o->ddivpdp = -dQdP * dlamdP + gdot * dsin_dildP + 0.0;
         inv_eta_diss += 1.0 / eta_vep;
     }
     eta_pwl = pow(2.0 * C_pwl, -1.0) * pow(Tii, 1.0 - n_pwl);
@@ -314,13 +382,15 @@ static void orc_visc(int p, double G, double T, double P, double d, double phi, 
     o->Exz_el = (double)elastic * (Txz - Txz0) / 2.0 / eta_el;
     Exx_pl = gdot * dQdtxx; Ezz_pl = gdot * dQdtzz; Exz_pl = gdot * dQdtxz / 2.0;
     Exx_pwl = Txx / 2.0 / eta_pwl; Ezz_pwl = Tzz / 2.0 / eta_pwl; Exz_pwl = Txz / 2.0 / eta_pwl;
-    o->Exx_diss = Exx_pl + Exx_lin + Exx_pwl + Exx_cst;
-    o->Ezz_diss = Ezz_pl + Ezz_lin + Ezz_pwl + Ezz_cst;
-    o->Exz_diss = Exz_pl + Exz_lin + Exz_pwl + Exz_cst;
+    o->Exx_diss = Exx_pl + Exx_lin + Exx_pwl + Exx_exp + 0.0 + Exx_cst;   /* Exx_gbs stays 0 (:678) */
+    o->Ezz_diss = Ezz_pl + Ezz_lin + Ezz_pwl + Ezz_exp + 0.0 + Ezz_cst;
+    o->Exz_diss = Exz_pl + Exz_lin + Exz_pwl + Exz_exp + 0.0 + Exz_cst;
     o->Eii_el = (double)elastic * fabs(Tii - Tii0) / 2.0 / eta_el;
     o->Eii_pwl = Tii / 2.0 / eta_pwl;
     o->Eii_lin = Eii_lin;
     o->Eii_cst = Eii_cst;
+    o->Eii_exp = Eii_exp;
+    o->Eii_gbs = Eii_gbs;
     o->div_pl = divp;
     o->div_el = -(Pc - P0) / (K * dt);
     o->div_r = 0.0;
@@ -380,6 +450,7 @@ int orc_viscosity_grid(const mdz_grid_desc *g, const mdz_materials *mat, const m
      * those of the serial loop, bit for bit) */
 #pragma omp parallel for private(p) reduction(+ : ve_fail, vp_fail) schedule(dynamic, 256)
     for (c = 0; c < nc; c++) {
+        double eexp = 0, egbs = 0;
         double eta = 0, eta_phys = 0, VE = 0, sxx = 0, szz = 0, sxz = 0, eel = 0, epl = 0, epwl = 0, elin = 0,
                ecst = 0, dn = 0, xel = 0, xdi = 0, zel = 0, zdi = 0, dexx = 0, dezz = 0, dgxz = 0, dp = 0,
                vxx = 0, vzz = 0, vxz = 0, vp = 0, pc = 0, del = 0, dpl = 0, dr = 0, Wt = 0, We = 0, Wd = 0, X = 0,
@@ -402,6 +473,7 @@ int orc_viscosity_grid(const mdz_grid_desc *g, const mdz_materials *mat, const m
                 if (avg == 0 || avg == 2) { sxx += w * o.txx; szz += w * o.tzz; sxz += w * o.txz; }
                 VE += w * o.VEcoeff; eel += w * o.Eii_el; epl += w * o.Eii_pl; epwl += w * o.Eii_pwl;
                 elin += w * o.Eii_lin; ecst += w * o.Eii_cst; dn += w * 1.0 / o.d1;
+                eexp += w * o.Eii_exp; egbs += w * o.Eii_gbs;
                 xel += w * o.Exx_el; xdi += w * o.Exx_diss; zel += w * o.Ezz_el; zdi += w * o.Ezz_diss;
                 Wt += w * (o.txx * f->exxd[c] + o.tzz * f->ezzd[c] + (o.txx + o.tzz) * (f->exxd[c] + f->ezzd[c]) +
                            2.0 * o.txz * f->exz_n[c]);
@@ -437,7 +509,7 @@ int orc_viscosity_grid(const mdz_grid_desc *g, const mdz_materials *mat, const m
         SETF(f->eta_n, c, eta); SETF(f->eta_phys_n, c, eta_phys); SETF(f->VE_n, c, VE);
         SETF(f->sxxd, c, sxx); SETF(f->szzd, c, szz); SETF(f->sxz_n, c, sxz);
         SETF(f->eII_el, c, eel); SETF(f->eII_pl, c, epl); SETF(f->eII_pwl, c, epwl); SETF(f->eII_lin, c, elin);
-        SETF(f->eII_cst, c, ecst); SETF(f->d_n, c, dn);
+        SETF(f->eII_cst, c, ecst); SETF(f->d_n, c, dn); SETF(f->eII_exp, c, eexp); SETF(f->eII_gbs, c, egbs);
         SETF(f->exx_el, c, xel); SETF(f->exx_diss, c, xdi); SETF(f->ezz_el, c, zel); SETF(f->ezz_diss, c, zdi);
         SETF(f->detadexx_n, c, dexx); SETF(f->detadezz_n, c, dezz); SETF(f->detadgxz_n, c, dgxz);
         SETF(f->detadp_n, c, dp);

@@ -80,7 +80,11 @@ def solve_defect(g, f, jacobian, F):
     pressure equations).  Factorised as M = K + c u u^T (u: one pressure
     unknown; nonsingular where K's null space is the constant pressure) by
     sparse LU without the dense border, then the border and the rank-one term
-    resolved from three solves with M (2 x 2 system)."""
+    resolved from three solves with M (2 x 2 system).  Two steps of iterative
+    refinement with the same factors follow: the pressure of a strong
+    viscosity contrast is conditioned far worse than the residual (a 1e3
+    inclusion at 101 x 101 keeps ~1e-7 relative pressure error after the
+    direct solve alone, at a 2e-14 relative residual; ~1e-12 after them)."""
     K, idx, n, n_p = assemble(g, f, jacobian)
     b = F[idx >= 0][np.argsort(idx[idx >= 0])]
     b = b.copy()
@@ -93,10 +97,18 @@ def solve_defect(g, f, jacobian, F):
     u[r] = 1.0
     M = (K + sp.csr_matrix(([c], ([r], [r])), shape=(n, n))).tocsc()
     lu = spla.splu(M, permc_spec="COLAMD")
-    yb, yu, ye = lu.solve(b), lu.solve(u), lu.solve(e)
+    yu, ye = lu.solve(u), lu.solve(e)
     A2 = np.array([[1.0 - c * yu[r], ye[r]], [c * (e @ yu), -(e @ ye)]])
-    s_, lam = np.linalg.solve(A2, np.array([yb[r], -(e @ yb)]))
-    x = yb + c * s_ * yu - lam * ye
+
+    def solve(rhs):
+        yb = lu.solve(rhs)
+        s_, lam = np.linalg.solve(A2, np.array([yb[r], -(e @ yb)]))
+        return yb + c * s_ * yu - lam * ye
+    x = solve(b)
+    for _ in range(2):
+        res = b - K @ x
+        res[n - n_p:] -= res[n - n_p:].mean()
+        x = x + solve(res)
     out = np.zeros(len(F))
     out[idx >= 0] = x[idx[idx >= 0]]
     return out
@@ -208,6 +220,33 @@ def first_defect(g, mat, model, markers, u, v, p, jacobian):
     return f, np.concatenate([f["ru"], f["rv"], f["rp"]])
 
 
+def pure_shear_ale(g, u, v, dt):
+    """PureShearALE (SOURCE/AdvectionRoutines.c:634-734, no free surface):
+    each wall moves by dt times the mean velocity of its Dirichlet nodes,
+    summed in the reference's loop order (west / east: Vx rows 0..Nz-1 of the
+    first / last column, tag 0; south / north: Vz columns 0..Nx-1 of the first
+    / last row, tag 0, or 0 and 30 on the north), then the grid lines are
+    regenerated over the new box (g.regrid, SetGridCoordinates).  g changes in
+    place; returns the new (xmin, xmax, zmin, zmax)."""
+    Nx, Nz = g.Nx, g.Nz
+    uu, bu = np.asarray(u).reshape(Nz + 1, Nx), g.BCu.reshape(Nz + 1, Nx)
+    vv, bv = np.asarray(v).reshape(Nz, Nx + 1), g.BCv.reshape(Nz, Nx + 1)
+
+    def mean(vals, take):
+        s, c = 0.0, 0
+        for x, t in zip(vals.tolist(), take.tolist()):
+            if t:
+                s += x
+                c += 1
+        return s / c if c > 0 else s
+    VxW = mean(uu[:Nz, 0], bu[:Nz, 0] == 0)
+    VxE = mean(uu[:Nz, Nx - 1], bu[:Nz, Nx - 1] == 0)
+    VzS = mean(vv[0, :Nx], bv[0, :Nx] == 0)
+    VzN = mean(vv[Nz - 1, :Nx], (bv[Nz - 1, :Nx] == 0) | (bv[Nz - 1, :Nx] == 30))
+    g.regrid(g.xmin + VxW * dt, g.xmax + VxE * dt, g.zmin + VzS * dt, g.zmax + VzN * dt)
+    return g.xmin, g.xmax, g.zmin, g.zmax
+
+
 def time_step(g, mat, model, markers, u, v, p, fields_out=None):
     """markers: dict with x, z, phase, sxxd, szzd, sxz, strain_pl, strain, T, cmul (updated in place).
     Returns (u, v, p, report dict)."""
@@ -301,6 +340,9 @@ def time_step(g, mat, model, markers, u, v, p, fields_out=None):
         update_particle_pressure(g, o, f["p0_n"], p, markers)
         dstr = dt * (f["eII_pl"] + f["eII_pwl"] + f["eII_lin"] + f["eII_el"] + f["eII_cst"])
         dstr_pl = dt * f["eII_pl"]
+        if getattr(model, "ispureshear_ale", 0) == 1:   # before the advection (Main_DOODZ.c:1107-1109)
+            pure_shear_ale(g, u, v, dt)
+            o._desc = g.desc()
         markers["vx"], markers["vz"] = o.RogerGuntherII(u, v, dt)
         markers["x"], markers["z"], markers["phase"] = o.x, o.z, o.phase
         # AccumulatedStrainII after the advection (Main_DOODZ.c:1134-1140)

@@ -138,6 +138,8 @@ int ref_set_mat(const char *name, int p, double v) {
     M_D(tpwl) M_D(Qpwl) M_D(Vpwl) M_D(npwl) M_D(mpwl) M_D(Apwl) M_D(apwl) M_D(fpwl) M_D(rpwl) M_D(Fpwl) M_D(pref_pwl)
     M_D(tlin) M_D(Qlin) M_D(Vlin) M_D(nlin) M_D(mlin) M_D(Alin) M_D(alin) M_D(flin) M_D(rlin) M_D(Flin)
     M_D(gs_ref) M_D(C_end) M_D(phi_end) M_D(psi_end) M_D(pls_start) M_D(pls_end) M_D(eta_vp) M_D(n_vp)
+    M_D(Qexp) M_D(Sexp) M_D(Eexp) M_D(Gexp) M_D(nexp)
+    M_D(Qgbs) M_D(Vgbs) M_D(ngbs) M_D(mgbs) M_D(Agbs) M_D(agbs) M_D(fgbs) M_D(rgbs) M_D(Fgbs)
     M_I(cstv) M_I(pwlv) M_I(linv) M_I(expv) M_I(gbsv) M_I(gs) M_I(is_tensile)
     M_I(coh_soft) M_I(phi_soft) M_I(psi_soft)
 #undef M_D
@@ -154,7 +156,7 @@ double *ref_field(const char *name) {
     F(eta_n) F(eta_s) F(eta_phys_n) F(eta_phys_s) F(VE_n) F(VE_s) F(mu_n) F(mu_s) F(T) F(T_s) F(P_s)
     F(d0_n) F(d0_s) F(phi0_n) F(phi0_s) F(X0_n) F(X0_s) F(strain_n) F(strain_s) F(p0_n) F(p0_s)
     F(bet_n) F(bet_s) F(rho_n) F(rho_s) F(C_n) F(C_s) F(fric_n) F(fric_s) F(dil_n) F(dil_s)
-    F(eII_el) F(eII_pl) F(eII_pwl) F(eII_lin) F(eII_cst) F(exx_el) F(ezz_el) F(exz_el) F(exx_diss) F(ezz_diss) F(exz_diss)
+    F(eII_el) F(eII_pl) F(eII_pwl) F(eII_lin) F(eII_cst) F(eII_exp) F(eII_gbs) F(exx_el) F(ezz_el) F(exz_el) F(exx_diss) F(ezz_diss) F(exz_diss)
     F(d_n) F(OverS_n) F(OverS_s) F(X_n) F(X_s) F(div_u_el) F(div_u_pl) F(div_u_r) F(Wtot) F(Wel) F(Wdiss)
     F(D11_n) F(D12_n) F(D13_n) F(D14_n) F(D21_n) F(D22_n) F(D23_n) F(D24_n) F(D31_s) F(D32_s) F(D33_s) F(D34_s)
     F(detadexx_n) F(detadezz_n) F(detadgxz_n) F(detadp_n) F(ddivpdexx_n) F(ddivpdezz_n) F(ddivpdgxz_n) F(ddivpdp_n)

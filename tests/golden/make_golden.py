@@ -111,6 +111,24 @@ RHEO_PHASES = [
 ]
 RHEO_MODEL = dict(dt=0.5, iselastic=1, step=1, eta_avg=0, mineta=1e-3, maxeta=1e6)
 RHEO_R = 8.314
+# the other mechanisms of Viscosity(): Peierls creep, grain-boundary sliding
+# and the tension cut-off (tension pressure -25 MPa / scale_S = -0.5 here, so
+# that the fixture's pressures, -0.2 .. 1.4, straddle it)
+RHEO_PHASES_MECH = [
+    # constant viscosity + Peierls creep + elasticity + Drucker-Prager with the tension cut-off
+    dict(cstv=1, eta0=3.0, expv=1, Qexp=5.4e4, Sexp=10.0, Eexp=1.0, Gexp=0.1, nexp=2.0, is_tensile=1,
+         rho=1.0, Slim=1e10, eta_vp=0.02, n_vp=1.0, gs_ref=1.0),
+    # dislocation creep + grain-boundary sliding + tension cut-off
+    dict(pwlv=1, npwl=3.0, Apwl=2.0e-3, Qpwl=1.2e4, Vpwl=0.05, mpwl=0.0, rpwl=0.0, fpwl=1.0, apwl=0.0, Fpwl=1.0,
+         pref_pwl=1.0, gbsv=1, ngbs=2.0, Agbs=1.0e-2, Qgbs=1.0e4, Vgbs=0.02, mgbs=0.0, rgbs=0.0, fgbs=1.0, agbs=0.0,
+         Fgbs=1.0, is_tensile=1, rho=1.1, Slim=1e10, eta_vp=0.02, n_vp=1.0, gs_ref=1.0),
+    # diffusion creep + Peierls + grain-boundary sliding, von Mises cap
+    dict(linv=1, nlin=1.0, Alin=0.3, Qlin=5.0e3, Vlin=0.0, mlin=0.0, rlin=0.0, flin=1.0, alin=0.0, Flin=1.0,
+         expv=1, Qexp=4.0e4, Sexp=5.0, Eexp=2.0, Gexp=0.2, nexp=1.5,
+         gbsv=1, ngbs=2.5, Agbs=5.0e-3, Qgbs=8.0e3, Vgbs=0.0, mgbs=0.0, rgbs=0.0, fgbs=1.0, agbs=0.0, Fgbs=1.0,
+         rho=0.9, Slim=1.3, eta_vp=0.0, n_vp=1.0, gs_ref=1.0),
+]
+RHEO_MODEL_MECH = dict(RHEO_MODEL, scale_S=5e7)
 
 
 def rheology_inputs(g, rng):
@@ -139,15 +157,15 @@ def rheology_inputs(g, rng):
     return f
 
 
-def make_rheology_fixture(avg=0, tag=""):
+def make_rheology_fixture(avg=0, tag="", phases=None, model=None):
     g = _grid()
     r = RefMDOODZ(NX, NZ, XMIN, XMAX, ZMIN, ZMAX, 3)
     r.set_bc_pureshear(1.0)
-    for k, v in RHEO_MODEL.items():
+    for k, v in (model or RHEO_MODEL).items():
         r.set_param(k, v)
     r.set_param("eta_avg", avg)
     r.set_param("R", RHEO_R)
-    for p, props in enumerate(RHEO_PHASES):
+    for p, props in enumerate(phases or RHEO_PHASES):
         for k, v in props.items():
             r.set_mat(k, p, v)
     x, z, ph = _markers(g, seed=11)
@@ -188,7 +206,7 @@ def make_rheology_fixture(avg=0, tag=""):
                  "exx_diss", "ezz_diss", "exz_diss", "detadexx_n", "detadezz_n", "detadgxz_n", "detadp_n",
                  "ddivpdexx_n", "ddivpdezz_n", "ddivpdgxz_n", "ddivpdp_n", "detadexx_s", "detadezz_s",
                  "detadgxz_s", "detadp_s", "p_corr", "div_u_el", "div_u_pl", "div_u_r", "Wtot", "Wel", "Wdiss",
-                 "OverS_n", "OverS_s", "T_s", "P_s", "div_u_s"):
+                 "OverS_n", "OverS_s", "T_s", "P_s", "div_u_s") + (("eII_exp", "eII_gbs") if phases else ()):
         out["vg_" + name] = r.field(name).copy()
     r.rheo_operators(0)
     for name in ("D11_n", "D12_n", "D13_n", "D14_n", "D21_n", "D22_n", "D23_n", "D24_n", "D31_s", "D32_s", "D33_s",
@@ -450,3 +468,5 @@ if __name__ == "__main__":
         make_rheology_fixture(0)
         make_rheology_fixture(1, "_harm")
         make_rheology_fixture(2, "_geom")
+    if "rheology" in what or "mech" in what:
+        make_rheology_fixture(0, "_mech", RHEO_PHASES_MECH, RHEO_MODEL_MECH)

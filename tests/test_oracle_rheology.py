@@ -12,17 +12,21 @@ RHEO_TOL = 1e-11   # local Newton stops at |r/Eii| < 1e-13: results agree to far
 PHASES = None
 
 
-def rheology_case(ref, avg):
-    from golden.make_golden import RHEO_PHASES, RHEO_MODEL, RHEO_R, NX, NZ, XMIN, XMAX, ZMIN, ZMAX
+def rheology_case(ref, avg, mech=False):
+    """Grid, input fields, materials and parameters of a rheology fixture;
+    mech: the fixture of Peierls creep, grain-boundary sliding and the
+    tension cut-off (rheology_ref_mech.npz)."""
+    from golden.make_golden import (RHEO_PHASES, RHEO_MODEL, RHEO_R, RHEO_PHASES_MECH, RHEO_MODEL_MECH, NX, NZ, XMIN,
+                                    XMAX, ZMIN, ZMAX)
     g = mdz.Grid(NX, NZ, XMIN, XMAX, ZMIN, ZMAX).set_bc_pureshear(1.0)
     f = mdz.GridFields(g, 3)
     for k in ref:
         if k.startswith("in_"):
             f[k[3:]] = ref[k]
-    m = dict(RHEO_MODEL)
+    m = dict(RHEO_MODEL_MECH if mech else RHEO_MODEL)
     m["eta_avg"] = avg
     prm = mdz.RheoParams.make(**m)
-    mat = mdz.Materials.from_phases(RHEO_PHASES, R=RHEO_R)
+    mat = mdz.Materials.from_phases(RHEO_PHASES_MECH if mech else RHEO_PHASES, R=RHEO_R)
     return g, f, mat, prm
 
 
@@ -32,10 +36,10 @@ def _check(got, want, name, tol=RHEO_TOL):
     assert err < tol, "%s: max rel err %.3e" % (name, err)
 
 
-@pytest.mark.parametrize("avg,tag", [(0, ""), (1, "_harm"), (2, "_geom")])
+@pytest.mark.parametrize("avg,tag", [(0, ""), (1, "_harm"), (2, "_geom"), (0, "_mech")])
 def test_rheology_chain_matches_reference(golden, avg, tag):
     ref = golden("rheology_ref%s.npz" % tag)
-    g, f, mat, prm = rheology_case(ref, avg)
+    g, f, mat, prm = rheology_case(ref, avg, mech=tag == "_mech")
     oracle.strain_rates(g, f)
     for k in ("div_u", "exxd", "ezzd", "exz", "exz_n", "exxd_s", "ezzd_s"):
         _check(f[k], ref["sr_" + k], k, 1e-13)

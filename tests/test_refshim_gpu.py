@@ -28,8 +28,12 @@ def shim():
 
 
 def _grid(ref):
-    xmin, xmax, zmin, zmax = ref["box"]
-    return mdz.Grid(int(ref["Nx"]), int(ref["Nz"]), xmin, xmax, zmin, zmax).set_bc_pureshear(1.0)
+    if "box" in ref:
+        xmin, xmax, zmin, zmax = ref["box"]
+        return mdz.Grid(int(ref["Nx"]), int(ref["Nz"]), xmin, xmax, zmin, zmax).set_bc_pureshear(1.0)
+    # fixtures without the box were made on the generator's standard grid
+    from golden.make_golden import NX, NZ, XMIN, XMAX, ZMIN, ZMAX
+    return mdz.Grid(NX, NZ, XMIN, XMAX, ZMIN, ZMAX).set_bc_pureshear(1.0)
 
 
 def _params(g, nph, **kw):

@@ -25,7 +25,7 @@ def vep_case(N=33, nm=4, seed=5):
     rng = np.random.default_rng(seed)
     m = dict(x=x, z=z, phase=ph, sxxd=np.full(len(x), -0.7), szzd=np.full(len(x), 0.7),
              sxz=0.05 * rng.standard_normal(len(x)), strain_pl=np.zeros(len(x)), strain=np.zeros(len(x)),
-             T=np.zeros(len(x)), cmul=1.0 + 0.01 * rng.standard_normal(len(x)))
+             T=np.zeros(len(x)), cmul=1.0 + 0.01 * rng.standard_normal(len(x)), P=np.zeros(len(x)))
     u = (-g.xg[None, :] + 0 * g.zvx[:, None]).ravel()
     v = (g.zg[:, None] + 0 * g.xvz[None, :]).ravel()
     p = np.zeros(g.size(1))
@@ -37,7 +37,7 @@ def run_gpu(g, m, u, v, p, mat, model, cap=None):
     ctx = mdz.Context(g, mat.n_phases, cap or len(m["x"]))
     ctx.set_markers(m["x"], m["z"], m["phase"])
     for attr, key in ((mdz.M_SXXD, "sxxd"), (mdz.M_SZZD, "szzd"), (mdz.M_SXZ, "sxz"), (mdz.M_STRAIN_PL, "strain_pl"),
-                      (mdz.M_STRAIN, "strain"), (mdz.M_T, "T"), (mdz.M_CMUL, "cmul")):
+                      (mdz.M_STRAIN, "strain"), (mdz.M_T, "T"), (mdz.M_CMUL, "cmul"), (mdz.M_P, "P")):
         ctx.set_marker_attr(attr, m[key])
     f = mdz.GridFields(g, mat.n_phases)
     f["u"], f["v"], f["p"] = u, v, p
@@ -53,7 +53,7 @@ def run_gpu(g, m, u, v, p, mat, model, cap=None):
     mk = dict(x=x, z=z, phase=ph, vx=vx, vz=vz, sxxd=ctx.get_marker_attr(mdz.M_SXXD),
               szzd=ctx.get_marker_attr(mdz.M_SZZD), sxz=ctx.get_marker_attr(mdz.M_SXZ),
               strain_pl=ctx.get_marker_attr(mdz.M_STRAIN_PL), strain=ctx.get_marker_attr(mdz.M_STRAIN),
-              T=ctx.get_marker_attr(mdz.M_T), cmul=ctx.get_marker_attr(mdz.M_CMUL))
+              T=ctx.get_marker_attr(mdz.M_T), cmul=ctx.get_marker_attr(mdz.M_CMUL), P=ctx.get_marker_attr(mdz.M_P))
     ctx.close()
     return out, mk, rep
 
@@ -121,7 +121,7 @@ def test_vep_step_with_reseeding_vs_oracle(direct):
     assert rep.markers_added == ro["markers_added"] > 0, (rep.markers_added, ro["markers_added"])
     assert len(mk["x"]) == len(mo["x"])
     assert np.array_equal(mk["phase"], mo["phase"])
-    for k in ("x", "z", "vx", "vz", "sxxd", "szzd", "sxz", "strain_pl", "strain", "T", "cmul"):
+    for k in ("x", "z", "vx", "vz", "sxxd", "szzd", "sxz", "strain_pl", "strain", "T", "cmul", "P"):
         assert _rel(mk[k], mo[k]) < 1e-8, (k, _rel(mk[k], mo[k]))
 
 
