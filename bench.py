@@ -256,12 +256,17 @@ def mlp_workload():
     t0 = time.perf_counter()
     loss = ctx.mlp_train(n // 65536, 65536, 2e-3)
     t_epoch = time.perf_counter() - t0
-    b = ctx.mlp_benchmark(65536, 5)
+    ctx.mlp_set_engine(0)
+    b = ctx.mlp_benchmark(65536, 5)               # tcgen05 inference (the default)
+    ctx.mlp_set_engine(1)
+    b1 = ctx.mlp_benchmark(65536, 5)              # warp-level mma.sync inference
     ctx.close()
-    flops = 2.0 * (16 * 64 + 64 * 64 + 64 * 8)   # per row, padded tensor-core shapes
+    flops = 2.0 * (8 * 64 + 64 * 64 + 64 * 2)     # algorithmic FLOP per row (9472)
     return {"tuples": n, "batch": 65536, "generate_s": t_gen, "epoch_s": t_epoch, "loss": loss,
             "ms_infer_2^24": b["ms_infer"], "ms_train_step": b["ms_train_step"], "rms_error": b["rms_error"],
-            "infer_tflops": flops * n / (b["ms_infer"] * 1e-3) / 1e12}
+            "infer_tflops": flops * n / (b["ms_infer"] * 1e-3) / 1e12, "infer_engine": "tcgen05",
+            "mma_sync": {"ms_infer_2^24": b1["ms_infer"], "infer_tflops": flops * n / (b1["ms_infer"] * 1e-3) / 1e12,
+                         "rms_error": b1["rms_error"]}}
 
 
 def e2e_form(cfg_builder, precision, learned, steps, size, warmup):
@@ -430,6 +435,8 @@ def main():
     ap.add_argument("--forms", default="both", choices=["both", "fast"],
                     help="fast: run only the learned FP32-refined form and print nothing (profiling)")
     ap.add_argument("--guess-steps", type=int, default=3000, help="Adam steps of the learned guess")
+    ap.add_argument("--mlp-only", action="store_true",
+                    help="run only the MLP workload (2^24 tuples, one epoch, inference) and print its object")
     args = ap.parse_args()
     rank, world, local = _dist()
     size = tuple(int(s) for s in args.size.split("x")) if args.size else None
@@ -456,6 +463,9 @@ def main():
         dist.init_process_group("nccl")
     import mdz
     mdz.load_library()
+    if args.mlp_only:
+        print(json.dumps(mlp_workload()))
+        return 0
     b = builder(size)
     if world > 1:
         torch.distributed.barrier()

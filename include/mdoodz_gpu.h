@@ -280,6 +280,10 @@ typedef struct mdz_fields {
     double *roger_x, *roger_z, *rhs_p, *gx, *gz;
     double *ru, *rv, *rp;
     double *eII_exp, *eII_gbs;   /* centroid Peierls and grain-boundary-sliding rates */
+    /* energy equation: conductivity on the Vx / Vz faces (kx, kz), heat
+     * capacity Cv, radiogenic heat Qr, temperature increment dT and thermal
+     * expansivity alp at the centroids */
+    double *kx, *kz, *Cv, *Qr, *dT, *alp;
 } mdz_fields;
 
 /* Host-pointer drop-ins for the grid-side reference functions.  Each reads the
@@ -321,6 +325,11 @@ mdz_status mdz_mlp_get_weights(mdz_ctx *ctx, float *params);
  * x = 2 (v - lo) / (hi - lo) - 1, temperature as 1000 / T over
  * [1000 / hi, 1000 / lo]. */
 mdz_status mdz_mlp_set_ranges(mdz_ctx *ctx, const double *lo, const double *hi);
+/* Kernel of mdz_mlp_infer and mdz_mlp_benchmark's inference: 0 (default)
+ * tcgen05.mma on 128-row tiles with the accumulators in tensor memory,
+ * 1 the warp-level mma.sync kernel.  Both compute the same BF16 network with
+ * FP32 accumulation. */
+mdz_status mdz_mlp_set_engine(mdz_ctx *ctx, int engine);
 /* n training tuples on the device, drawn uniformly in the ranges (phase
  * uniform among the materials' phases) and labelled by the plain local solve
  * of these materials and switches (dt per tuple). */
@@ -392,8 +401,7 @@ mdz_status mdz_EvaluateStokesResidualDecoupled(mdz_ctx *ctx, mdz_fields *f, doub
  * scratch value has to start at zero (every slot a call reads is written by
  * that call first) and the result is bitwise reproducible.  The first call on
  * a device looks the scratch address up (cudaGetSymbolAddress, with that
- * device current): make it once before any stream capture.  That address is
- * kept for the life of the process; after a cudaDeviceReset (or anything else
+ * device current).  That address is kept for the life of the process; after a cudaDeviceReset (or anything else
  * that tears down the device's primary context) it is stale, and this entry
  * point must not be called again in that process.  The scratch is shared, so
  * calls that overlap in time (several streams or host threads on one device)
@@ -489,6 +497,38 @@ mdz_status mdz_get_marker_attr(mdz_ctx *ctx, int attr, int n, double *values);
 /* Copy grid fields between the caller's host arrays and the context's device
  * mirrors: to_device = 1 uploads every non-NULL member, 0 downloads them. */
 mdz_status mdz_sync_fields(mdz_ctx *ctx, mdz_fields *f, int to_device);
+
+/* ---- energy equation ------------------------------------------------------ */
+
+/* Thermal boundary description (the reference's BCT BCt): centroid tags
+ * (-1 active, 30 air; ncx*ncz) and, per wall, a type and a value per
+ * boundary cell: typS / typN / valS / valN over the Nx-1 columns, typW / typE
+ * / valW / valE over the Nz-1 rows.  Type 1: Dirichlet temperature at the
+ * wall; type 2 on the south wall: prescribed flux; type 0: zero flux. */
+typedef struct mdz_thermal_bc {
+    const signed char *type;
+    const signed char *typW, *typE, *typS, *typN;
+    const double *valW, *valE, *valS, *valN;
+} mdz_thermal_bc;
+
+/* EnergyDirectSolve (SOURCE/ThermalRoutines.c:72-551, one iteration, polar =
+ * 0): the implicit (theta = 1) energy step rho Cv (T_new - T) / dt =
+ * div(k grad T_new) + Qr [+ Wdiss with shear_heating = 1] [+ adiabatic heat,
+ * adiab_heating = 1: T alp v gz rho_n, 2: T alp (p - p0_n) / dt] on the
+ * centroids, with the reference's five-point conductances (kx on the west /
+ * east faces, kz on the south / north faces) and boundary rows.  The
+ * symmetric positive definite system is solved matrix-free by Jacobi-
+ * preconditioned conjugate gradients in FP64 to a relative residual of
+ * rel_tol (<= 0: 1e-13), in place of the reference's CHOLMOD factorisation.
+ * Reads f->T, rho_n, Cv, Qr, kx, kz (and Wdiss, alp, v, p, p0_n as the
+ * heating switches ask); writes f->T (the new temperature; zeroC / scale_T on
+ * air cells) and f->dT.  iterations and rel_residual (may be NULL) report the
+ * solve.  MDZ_ERR_UNSUPPORTED for centroid tags other than -1 / 30 (free
+ * surface, periodic), MDZ_ERR_NOT_CONVERGED when max_iterations pass,
+ * MDZ_ERR_STATE for a negative temperature (the reference exits there). */
+mdz_status mdz_EnergyDirectSolve(mdz_ctx *ctx, mdz_fields *f, const mdz_thermal_bc *bc, double dt, double gz,
+                                 int shear_heating, int adiab_heating, double scale_T, double rel_tol,
+                                 int max_iterations, int *iterations, double *rel_residual);
 
 /* PureShearALE (SOURCE/AdvectionRoutines.c:634-734, ispureshear_ale = 1,
  * no free surface): the mean Vx of the Dirichlet nodes (tag 0) of the west and

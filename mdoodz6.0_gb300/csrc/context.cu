@@ -150,7 +150,7 @@ extern "C" void mdz_destroy(mdz_ctx *ctx) {
         if (p) cudaFree(p);
     for (int a = 0; a < MDZ_M_NATTR; a++)
         if (ctx->m.attr[a]) cudaFree(ctx->m.attr[a]);
-    for (int i = 0; i < 8; i++)
+    for (int i = 0; i < 9; i++)
         if (ctx->stage[i]) cudaFree(ctx->stage[i]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;

@@ -88,7 +88,7 @@ struct mdz_ctx {
     // arrival counters of the last-block sums
     double *red_part = nullptr;
     unsigned int *red_cnt = nullptr;
-    bool bcs_checked = false, bcs_ok = false;
+    bool bcs_checked = false, bcs_ok = false, bcs_neumann = false;
     // optional per-launch event timing of the main kernel classes (bench roofline)
     bool profiling = false;
     struct prof_rec { int cls; cudaEvent_t a, b; double bytes; };
@@ -100,8 +100,8 @@ struct mdz_ctx {
     struct mdz_reseed_ws *reseed = nullptr;   // quarter-cell workspace of the reseeding (reseed.cu)
     std::string err;
     // host-call staging buffers (grown on demand)
-    void *stage[8] = {nullptr};
-    size_t stage_bytes[8] = {0};
+    void *stage[9] = {nullptr};
+    size_t stage_bytes[9] = {0};
 };
 
 // ---- helpers -------------------------------------------------------------
@@ -274,7 +274,13 @@ void mdz_reseed_free(mdz_ctx *ctx);
     X(rv, VZ) \
     X(rp, CEN) \
     X(eII_exp, CEN) \
-    X(eII_gbs, CEN)
+    X(eII_gbs, CEN) \
+    X(kx, VX) \
+    X(kz, VZ) \
+    X(Cv, CEN) \
+    X(Qr, CEN) \
+    X(dT, CEN) \
+    X(alp, CEN)
 
 enum mdz_field_kind { MDZ_K_VX, MDZ_K_VZ, MDZ_K_CEN, MDZ_K_VER, MDZ_K_PPN, MDZ_K_PPS };
 size_t mdz_field_count(const mdz_ctx *ctx, int kind);

@@ -316,6 +316,8 @@ static mdz_status mlp_ensure(mdz_ctx *ctx) {
     if (e == cudaSuccess) e = cudaMemset(M->packed, 0, MLP_PACK_BYTES);
     if (e == cudaSuccess) e = cudaMalloc((void **)&M->partials, sizeof(float) * (MLP_NPARAM + 1) * M->max_blocks);
     if (e == cudaSuccess) e = cudaMalloc((void **)&M->grad, sizeof(float) * (MLP_NPARAM + 1));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&M->tc_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(M->tc_err, 0, sizeof(int));
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem_bytes());
     if (e == cudaSuccess)
@@ -327,7 +329,7 @@ static mdz_status mlp_ensure(mdz_ctx *ctx) {
 void mdz_mlp_free(mdz_ctx *ctx) {
     if (!ctx->mlp) return;
     mdz_mlp *M = ctx->mlp;
-    void *p[] = {M->params, M->adam_m, M->adam_v, M->packed, M->partials, M->grad, M->X, M->Y, M->guess};
+    void *p[] = {M->params, M->adam_m, M->adam_v, M->packed, M->partials, M->grad, M->X, M->Y, M->guess, M->tc_err};
     for (void *q : p)
         if (q) cudaFree(q);
     delete M;
@@ -540,7 +542,17 @@ extern "C" mdz_status mdz_mlp_gradients(mdz_ctx *ctx, int n, const float *x, con
     return MDZ_OK;
 }
 
+// The tcgen05 kernel's time-out flag (read after a synchronisation; cleared).
+static mdz_status mlp_tc_status(mdz_ctx *ctx) {
+    int e = 0;
+    MDZ_CUDA(ctx, cudaMemcpy(&e, ctx->mlp->tc_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (!e) return MDZ_OK;
+    MDZ_CUDA(ctx, cudaMemset(ctx->mlp->tc_err, 0, sizeof(int)));
+    return mdz_fail(ctx, MDZ_ERR_STATE, "mlp inference: a tensor-core commit did not arrive (time-out)");
+}
+
 static mdz_status mlp_infer_dev(mdz_ctx *ctx, const uint4 *X, long long n, float2 *Y, cudaStream_t st) {
+    if (ctx->mlp->engine == 0) return mdz_mlp_infer_tc(ctx, ctx->mlp->packed, X, n, Y, ctx->mlp->tc_err, st);
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -569,6 +581,14 @@ extern "C" mdz_status mdz_mlp_infer(mdz_ctx *ctx, long long n, const float *x, f
     if (s != MDZ_OK) return s;
     MDZ_CUDA(ctx, cudaMemcpyAsync(y, Y, sizeof(float2) * n, cudaMemcpyDeviceToHost, st));
     MDZ_CUDA(ctx, cudaStreamSynchronize(st));
+    return mlp_tc_status(ctx);
+}
+
+extern "C" mdz_status mdz_mlp_set_engine(mdz_ctx *ctx, int engine) {
+    if (!ctx || (engine != 0 && engine != 1)) return ctx ? mdz_fail(ctx, MDZ_ERR_ARG, "mlp_set_engine: 0 or 1") : MDZ_ERR_ARG;
+    mdz_status s = mlp_ensure(ctx);
+    if (s != MDZ_OK) return s;
+    ctx->mlp->engine = engine;
     return MDZ_OK;
 }
 
@@ -596,6 +616,7 @@ extern "C" mdz_status mdz_mlp_benchmark(mdz_ctx *ctx, int batch, int reps, doubl
     float ms = 0.f;
     cudaEventElapsedTime(&ms, a, b);
     if (ms_infer) *ms_infer = ms / reps;
+    if ((s = mlp_tc_status(ctx)) != MDZ_OK) return s;
     if (rms_error) {   // RMS of the outputs against the labels over the tuples
         std::vector<float2> h(M->n), l(M->n);
         MDZ_CUDA(ctx, cudaMemcpy(h.data(), Y, sizeof(float2) * M->n, cudaMemcpyDeviceToHost));

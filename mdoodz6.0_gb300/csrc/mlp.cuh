@@ -62,9 +62,15 @@ struct mdz_mlp {
     float2 *guess = nullptr;             // n_phases x (centroids + vertices)
     size_t guess_cap = 0;
     double last_loss = 0.0;
+    int engine = 0;                      // inference: 0 tcgen05 (mlp_tc.cu), 1 warp-level mma.sync
+    int *tc_err = nullptr;               // device flag: a tcgen05 commit timed out
 };
 
 bool mdz_mlp_ready(const mdz_ctx *ctx);
+// tcgen05 inference of n BF16 input rows (mlp_tc.cu); d_err is raised if a
+// tensor-core commit never arrived
+mdz_status mdz_mlp_infer_tc(mdz_ctx *ctx, const unsigned char *packed, const uint4 *X, long long n, float2 *Y,
+                            int *d_err, cudaStream_t st);
 void mdz_mlp_free(mdz_ctx *ctx);
 // guess buffer for n_phases x (nc + nv) nodes (allocated on first use)
 float2 *mdz_mlp_guess_buffer(mdz_ctx *ctx, size_t n);

@@ -20,12 +20,14 @@ enum {
     MDZ_RC_PRECP = 2,     // preconditioner pressure block sum and count
     MDZ_RC_DOTS = 8,      // k_dots: one counter per tile row (up to 40)
     MDZ_RC_GCR = 64,      // k_gcr_dots: [0] across tile rows, [1 + y] per tile row (up to 40)
+    MDZ_RC_ENERGY = 112,  // energy-equation conjugate gradients: 3 counters
 };
 enum {
     MDZ_RP_NORMS = 0,         // 6 x 2048
     MDZ_RP_PSUM = 12288,      // 2 x 2048
     MDZ_RP_PRECP = 16384,     // 2 x 2048
     MDZ_RP_DOTS = 20480,      // up to 48 x 2048
+    MDZ_RP_ENERGY = 118784,   // 3 x 2048 (energy-equation conjugate gradients)
 };
 
 template <typename T>

@@ -84,8 +84,9 @@ __global__ void k_residual_norms(int nu, int nv, int np, const T *__restrict__ f
     int n = nu > nv ? nu : nv;
     n = n > np ? n : np;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        if (i < nu && tu[i] == -1) { double f = fu[i]; acc[0] += f * f; acc[3] += 1; }
-        if (i < nv && tv[i] == -1) { double f = fv[i]; acc[1] += f * f; acc[4] += 1; }
+        // equations: inner (-1) and Neumann (2) velocity nodes
+        if (i < nu && (tu[i] == -1 || tu[i] == 2)) { double f = fu[i]; acc[0] += f * f; acc[3] += 1; }
+        if (i < nv && (tv[i] == -1 || tv[i] == 2)) { double f = fv[i]; acc[1] += f * f; acc[4] += 1; }
         if (i < np && tp[i] == -1) { double f = fp[i]; acc[2] += f * f; acc[5] += 1; }
     }
     mdz_grid_sum<6, double>(acc, part, counter, out);   // fixed order: the same bits every run
@@ -108,12 +109,22 @@ template mdz_status stokes_norms_launch<float>(mdz_ctx *, stokes_cvec<float>, do
 
 // ---------------------------------------------------------------------------
 // Host drop-ins.
-static bool supported_bcs(const mdz_ctx *ctx) {
-    // inner (-1), Dirichlet on the boundary (0) and free-slip ghosts (13) only
+static bool supported_bcs(const mdz_ctx *ctx, bool *neumann) {
+    // inner (-1), Dirichlet on the boundary (0), free-slip ghosts (13), and
+    // Neumann (2) on the west / east Vx lines and the south / north Vz lines
     const mdz_grid_desc &d = ctx->host_desc;
     size_t nu = (size_t)d.Nx * (d.Nz + 1), nv = (size_t)(d.Nx + 1) * d.Nz, np = (size_t)(d.Nx - 1) * (d.Nz - 1);
-    for (size_t i = 0; i < nu; i++) if (d.BCu_type[i] != -1 && d.BCu_type[i] != 0 && d.BCu_type[i] != 13) return false;
-    for (size_t i = 0; i < nv; i++) if (d.BCv_type[i] != -1 && d.BCv_type[i] != 0 && d.BCv_type[i] != 13) return false;
+    *neumann = false;
+    for (size_t i = 0; i < nu; i++) {
+        const int t = d.BCu_type[i], k = (int)(i % d.Nx), l = (int)(i / d.Nx);
+        if (t == 2 && (k == 0 || k == d.Nx - 1) && l > 0 && l < d.Nz) { *neumann = true; continue; }
+        if (t != -1 && t != 0 && t != 13) return false;
+    }
+    for (size_t i = 0; i < nv; i++) {
+        const int t = d.BCv_type[i], k = (int)(i % (d.Nx + 1)), l = (int)(i / (d.Nx + 1));
+        if (t == 2 && (l == 0 || l == d.Nz - 1) && k > 0 && k < d.Nx) { *neumann = true; continue; }
+        if (t != -1 && t != 0 && t != 13) return false;
+    }
     for (size_t i = 0; i < np; i++) if (d.BCp_type[i] != -1) return false;
     for (size_t i = 0; i < (size_t)d.Nx * d.Nz; i++) if (d.BCg_type[i] == 30) return false;
     // equations only on inner nodes: boundary rows/columns must not be -1
@@ -132,12 +143,13 @@ static bool supported_bcs(const mdz_ctx *ctx) {
 
 mdz_status mdz_check_stokes_bcs(mdz_ctx *ctx) {
     if (!ctx->bcs_checked) {
-        ctx->bcs_ok = supported_bcs(ctx);
+        ctx->bcs_ok = supported_bcs(ctx, &ctx->bcs_neumann);
         ctx->bcs_checked = true;
     }
     if (!ctx->bcs_ok)
         return mdz_fail(ctx, MDZ_ERR_UNSUPPORTED,
-                        "Stokes: only inner equations with Dirichlet (0) / free-slip (13) boundaries are implemented");
+                        "Stokes: only inner equations with Dirichlet (0), free-slip (13) and wall Neumann (2) "
+                        "boundaries are implemented");
     return MDZ_OK;
 }
 
@@ -146,12 +158,203 @@ stokes_coefs<double> mdz_coefs64(const mdz_fields &f) {
                                 f.D31_s, f.D32_s, f.D33_s, f.D34_s};
 }
 
+// ---------------------------------------------------------------------------
+// Neumann rows (tag 2): Xmomentum_WestNeumannDecoupled / _EastNeumannDecoupled
+// and Zmomentum_SouthNeumannDecoupled / _NorthNeumannDecoupled
+// (SOURCE/StokesAssemblyDecoupled.c:476-795, 1168-1428).  The reference calls
+// the same functions from its Picard and its Jacobian builders, but the
+// Jacobian builder sets comp = 1 (:3851), which adds the 2/3 compressible
+// terms to these rows; the Picard operator and the residual use comp = 0
+// (the incompressible model).  Viscosities eta_n, eta_s are taken directly,
+// the prescribed traction BC*.val / h moves to the right-hand side.  Each row is a list of (unknown, coefficient) entries with
+// the reference's two selections: the assembled entries (AddCoeff2), whose
+// Dirichlet-like neighbours (tags 0, 31, 11, 13) go to the right-hand side as
+// coefficient x value (twice the value for tag 11), and the entries its
+// residual sums directly.  Residual: F = (-b + sum over Dirichlet-like assembled
+// entries of c val + sum over residual entries of c x) x cell volume, with
+// b = roger (west / south: minus, east / north: plus the traction over h);
+// the reference takes the Dirichlet part from its last assembly, identical to
+// this where that assembly saw the same state.  Operator: the assembled entries
+// that are unknowns.  The north row's residual reads the pressure one cell
+// below the one its assembled row uses (c2 - ncx, :1418), kept as it is.
+namespace {
+struct nrow_entry {
+    double c;
+    int kind, idx;        // 0 u, 1 v, 2 p
+    bool assembled, residual;
+    double mult;          // Dirichlet value multiplier of the assembled entry
+};
+
+__device__ __forceinline__ bool dirlike(int t) { return t == 0 || t == 31 || t == 11 || t == 13; }
+
+struct nrow {
+    nrow_entry e[11];
+    int n = 0;
+    __device__ void add(int kind, int idx, double c, bool assembled, bool residual, double mult = 1.0) {
+        e[n++] = nrow_entry{c, kind, idx, assembled, residual, mult};
+    }
+};
+
+__device__ void neumann_x(const stokes_geom &G, const double *eta_n, const double *eta_s, int k, int l, bool west,
+                          double comp, nrow &R) {
+    const int nx = G.Nx, ncx = G.ncx, nxvz = nx + 1;
+    const int c1 = k + l * nx, c2 = k - 1 + (l - 1) * ncx, c3 = k + l * nxvz;
+    const double ixx = G.cd[GC_IXX], izz = G.cd[GC_IZZ], ixz = G.cd[GC_IXZ], idx = G.cd[GC_IDX];
+    const double etaC = west ? eta_n[c2 + 1] : eta_n[c2], etaN = eta_s[c1], etaS = eta_s[c1 - nx];
+    const int tS = G.BCu[c1 - nx], tN = G.BCu[c1 + nx], tO = west ? G.BCu[c1 + 1] : G.BCu[c1 - 1];
+    double uC = 0, uO = 0, uS = 0, uN = 0, vSW = 0, vSE = 0, vNW = 0, vNE = 0, pO = 0;
+    const double c23 = comp * 2.0 / 3.0;
+    if (tO != 30) { uC = -2.0 * ixx * etaC + c23 * ixx * etaC; uO = 2.0 * ixx * etaC - c23 * ixx * etaC; }
+    if (tS != 30 && tN != 30) {
+        if (tS != 13) { uS = izz * etaS; uC += -izz * etaS; }
+        if (tN != 13) { uN = izz * etaN; uC += -izz * etaN; }
+    }
+    if (tS == 30 && tN != 30 && tN != 13) { uC += -izz * etaN; uN = izz * etaN; }
+    if (tS != 30 && tN == 30 && tS != 13) { uC += -izz * etaS; uS = izz * etaS; }
+    if (tS == 11) uC += -izz * etaS;
+    if (tN == 11) uC += -izz * etaN;
+    const bool sp = G.BCv[c3 - nxvz] != 30 && G.BCv[c3 - nxvz + 1] != 30;
+    const bool np_ = G.BCv[c3 + 1] != 30 && G.BCv[c3] != 30;
+    if (sp) { vSE = -ixz * etaS + c23 * ixz * etaC; vSW = ixz * etaS - c23 * ixz * etaC; }
+    if (np_) { vNE = ixz * etaN - c23 * ixz * etaC; vNW = -ixz * etaN + c23 * ixz * etaC; }
+    const int ip = west ? c2 + 1 : c2;
+    const bool pin = G.BCp[ip] != 30;
+    if (pin) pO = west ? -idx : idx;
+    R.add(0, c1, -uC, true, true);
+    R.add(0, c1 - nx, -uS, tS != 30, tS != 30 && tS != 11, tS == 11 ? 2.0 : 1.0);
+    R.add(0, west ? c1 + 1 : c1 - 1, -uO, tO != 30, tO != 30);
+    R.add(0, c1 + nx, -uN, tN != 30, tN != 30 && tN != 11, tN == 11 ? 2.0 : 1.0);
+    const int vi[4] = {c3 - nxvz, c3 - nxvz + 1, c3, c3 + 1};
+    const double vc[4] = {-vSW, -vSE, -vNW, -vNE};
+    for (int q = 0; q < 4; q++) {
+        const bool pair = q < 2 ? sp : np_;
+        const int t = G.BCv[vi[q]];
+        R.add(1, vi[q], vc[q], pair, pair && t != 11 && t != 0);
+    }
+    R.add(2, ip, -pO, pin, pin);
+}
+
+__device__ void neumann_z(const stokes_geom &G, const double *eta_n, const double *eta_s, int k, int l, bool south,
+                          double comp, nrow &R) {
+    const int nx = G.Nx, ncx = G.ncx, nxvz = nx + 1;
+    const int c1 = k + l * nx, c2 = k - 1 + (l - 1) * ncx, c3 = k + l * nxvz;
+    const double ixx = G.cd[GC_IXX], izz = G.cd[GC_IZZ], ixz = G.cd[GC_IXZ], idz = G.cd[GC_IDZ];
+    const double etaC = south ? eta_n[c2 + ncx] : eta_n[c2], etaE = eta_s[c1], etaW = eta_s[c1 - 1];
+    const int tW = G.BCv[c3 - 1], tE = G.BCv[c3 + 1], tO = south ? G.BCv[c3 + nxvz] : G.BCv[c3 - nxvz];
+    double uSW = 0, uSE = 0, uNW = 0, uNE = 0, vC = 0, vO = 0, vW = 0, vE = 0, pO = 0;
+    const bool sp = G.BCu[c1 - 1] != 30 && G.BCu[c1] != 30;
+    const bool np_ = G.BCu[c1 + nx - 1] != 30 && G.BCu[c1 + nx] != 30;
+    const double c23 = comp * 2.0 / 3.0;   // etaS = etaN = etaC in these rows
+    if (sp) { uSW = ixz * etaW - c23 * etaC * ixz; uSE = -ixz * etaE + c23 * etaC * ixz; }
+    if (np_) { uNW = -ixz * etaW + c23 * etaC * ixz; uNE = ixz * etaE - c23 * etaC * ixz; }
+    if (tO != 30) { vC = -2.0 * izz * etaC + c23 * etaC * izz; vO = 2.0 * izz * etaC - c23 * etaC * izz; }
+    if (tW != 30 && tE != 30) {
+        if (tW != 13) { vW = ixx * etaW; vC += -ixx * etaW; }
+        if (tE != 13) { vE = ixx * etaE; vC += -ixx * etaE; }
+    }
+    if (tW == 30 && tE != 30 && tE != 13) { vE = ixx * etaE; vC += -ixx * etaE; }
+    if (tW != 30 && tE == 30 && tW != 13) { vW = ixx * etaW; vC += -ixx * etaW; }
+    if (tW == 11) vC += -ixx * etaW;
+    if (tE == 11) vC += -ixx * etaE;
+    const int ip = south ? c2 + ncx : c2;
+    const bool pin = G.BCp[ip] != 30;
+    if (pin) pO = south ? -idz : idz;
+    const int ui[4] = {c1 - 1, c1, c1 + nx - 1, c1 + nx};
+    const double uc[4] = {-uSW, -uSE, -uNW, -uNE};
+    for (int q = 0; q < 4; q++) {
+        const bool pair = q < 2 ? sp : np_;
+        const int t = G.BCu[ui[q]];
+        R.add(0, ui[q], uc[q], pair, pair && t != 11 && t != 0);
+    }
+    R.add(1, c3 - 1, -vW, tW != 30, tW != 30 && tW != 11, tW == 11 ? 2.0 : 1.0);
+    R.add(1, c3, -vC, true, true);
+    R.add(1, c3 + 1, -vE, tE != 30, tE != 30 && tE != 11, tE == 11 ? 2.0 : 1.0);
+    R.add(1, south ? c3 + nxvz : c3 - nxvz, -vO, tO != 30, tO != 30);
+    if (south) {
+        R.add(2, ip, -pO, pin, pin);
+    } else {   // assembled on c2, summed by the residual on c2 - ncx
+        R.add(2, ip, -pO, pin, false);
+        const bool pin2 = G.BCp[c2 - ncx] != 30;
+        R.add(2, c2 - ncx, -pO, false, pin2);
+    }
+}
+
+// One thread per wall node: west / east Vx lines (l = 1..Nz-1), south /
+// north Vz lines (k = 1..Nx-1).  RES: y = residual rows (b = roger_x /
+// roger_z, bu / bv = the Dirichlet values); else y = operator rows.
+template <bool RES>
+__global__ void k_neumann_rows(stokes_geom G, const double *__restrict__ eta_n, const double *__restrict__ eta_s,
+                               stokes_cvec<double> x, const double *__restrict__ bx, const double *__restrict__ bz,
+                               const double *__restrict__ bu, const double *__restrict__ bv, double *__restrict__ yu,
+                               double *__restrict__ yv, double comp) {
+    const int Nx = G.Nx, Nz = G.Nz, nxvz = Nx + 1;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nX = 2 * (Nz - 1), nZ = 2 * (Nx - 1);
+    if (t >= nX + nZ) return;
+    nrow R;
+    int row, kind;
+    double b;
+    if (t < nX) {
+        const bool west = t < Nz - 1;
+        const int l = 1 + (west ? t : t - (Nz - 1)), k = west ? 0 : Nx - 1;
+        row = k + l * Nx;
+        if (G.BCu[row] != 2) return;
+        kind = 0;
+        neumann_x(G, eta_n, eta_s, k, l, west, comp, R);
+        b = RES ? bx[row] + (west ? -bu[row] : bu[row]) * G.cd[GC_IDX] : 0.0;
+    } else {
+        const int q = t - nX;
+        const bool south = q < Nx - 1;
+        const int k = 1 + (south ? q : q - (Nx - 1)), l = south ? 0 : Nz - 1;
+        row = k + l * nxvz;
+        if (G.BCv[row] != 2) return;
+        kind = 1;
+        neumann_z(G, eta_n, eta_s, k, l, south, comp, R);
+        b = RES ? bz[row] + (south ? -bv[row] : bv[row]) * G.cd[GC_IDZ] : 0.0;
+    }
+    double r = RES ? -b : 0.0;
+    for (int q = 0; q < R.n; q++) {
+        const nrow_entry &e = R.e[q];
+        const int tag = e.kind == 0 ? G.BCu[e.idx] : (e.kind == 1 ? G.BCv[e.idx] : G.BCp[e.idx]);
+        const double xv = e.kind == 0 ? x.u[e.idx] : (e.kind == 1 ? x.v[e.idx] : x.p[e.idx]);
+        if (RES) {
+            if (e.assembled && e.kind != 2 && dirlike(tag))
+                r += e.c * e.mult * (e.kind == 0 ? bu[e.idx] : bv[e.idx]);
+            if (e.residual) r += e.c * xv;
+        } else if (e.assembled && !dirlike(tag)) {
+            r += e.c * xv;
+        }
+    }
+    r *= G.cd[GC_CELVOL];
+    if (kind == 0) yu[row] = r;
+    else yv[row] = r;
+}
+}  // namespace
+
+static mdz_status neumann_launch(mdz_ctx *ctx, bool res, bool jacobian, const mdz_fields &f, stokes_cvec<double> x,
+                                 double *yu, double *yv, cudaStream_t st) {
+    if (!ctx->bcs_neumann) return MDZ_OK;
+    const mdz_dgrid &g = ctx->g;
+    const int n = 2 * (g.Nz - 1) + 2 * (g.Nx - 1);
+    stokes_geom G = mdz_stokes_geom(ctx);
+    if (res)
+        k_neumann_rows<true><<<mdz_blocks(n, 128), 128, 0, st>>>(G, f.eta_n, f.eta_s, x, f.roger_x, f.roger_z,
+                                                                  g.BCu_val, g.BCv_val, yu, yv, 0.0);
+    else
+        k_neumann_rows<false><<<mdz_blocks(n, 128), 128, 0, st>>>(G, f.eta_n, f.eta_s, x, nullptr, nullptr, nullptr,
+                                                                   nullptr, yu, yv, jacobian ? 1.0 : 0.0);
+    MDZ_LAUNCHED(ctx);
+    return MDZ_OK;
+}
+
 mdz_status mdz_dev_residual(mdz_ctx *ctx, const mdz_fields &f, double *d_norms6, cudaStream_t st) {
     stokes_geom G = mdz_stokes_geom(ctx);
     stokes_cvec<double> x{f.u, f.v, f.p_corr}, b{f.roger_x, f.roger_z, f.rhs_p};
     stokes_vec<double> y{f.ru, f.rv, f.rp};
     stokes_apply_launch<double>(G, mdz_coefs64(f), x, y, &b, false, st);
     MDZ_LAUNCHED(ctx);
+    mdz_status s = neumann_launch(ctx, true, false, f, x, f.ru, f.rv, st);
+    if (s != MDZ_OK) return s;
     if (d_norms6) return stokes_norms_launch<double>(ctx, stokes_cvec<double>{f.ru, f.rv, f.rp}, d_norms6, st);
     return MDZ_OK;
 }
@@ -198,6 +401,9 @@ extern "C" mdz_status mdz_StokesOperatorApply(mdz_ctx *ctx, mdz_fields *f, int j
     stokes_apply_launch<double>(mdz_stokes_geom(ctx), mdz_coefs64(ctx->d), stokes_cvec<double>{dxu, dxv, dxp},
                                 stokes_vec<double>{dyu, dyv, dyp}, nullptr, jacobian != 0, st);
     MDZ_LAUNCHED(ctx);
+    if ((s = neumann_launch(ctx, false, jacobian != 0, ctx->d, stokes_cvec<double>{dxu, dxv, dxp}, dyu, dyv, st)) !=
+        MDZ_OK)
+        return s;
     MDZ_CUDA(ctx, cudaMemcpyAsync(yu, dyu, nu * 8, cudaMemcpyDeviceToHost, st));
     MDZ_CUDA(ctx, cudaMemcpyAsync(yv, dyv, nv * 8, cudaMemcpyDeviceToHost, st));
     MDZ_CUDA(ctx, cudaMemcpyAsync(yp, dyp, np * 8, cudaMemcpyDeviceToHost, st));

@@ -191,7 +191,7 @@ __device__ __forceinline__ T zrow(const stokes_geom &G, const stokes_coefs<T> &D
     };
     pair2<T> eS = exx_c(k - 1, l - 1), eN = exx_c(k - 1, l);
     T gW = gxz_v(k - 1, l), gE = gxz_v(k, l);
-    T TzzN, TzzS, TxzE, TxzW;
+    T TzzN, TzzS, TxzE, TxzW, ndrop = 0;
     if (!NEWTON) {
         TzzN = D.D22[iPrN] * eN.y;
         TzzS = D.D22[iPrS] * eS.y;
@@ -246,9 +246,31 @@ __device__ __forceinline__ T zrow(const stokes_geom &G, const stokes_coefs<T> &D
         T pE_ = wE * (inN * p[iPrN] + inS * p[iPrS] + inNEc * pNE + inSEc * pSE);
         TxzW = D.D31[ixyW] * exxW + D.D32[ixyW] * ezzW + D.D33[ixyW] * gW + D.D34[ixyW] * pW_;
         TxzE = D.D31[ixyE] * exxE + D.D32[ixyE] * ezzE + D.D33[ixyE] * gE + D.D34[ixyE] * pE_;
+        // The reference's Jacobian assembles the diagonal Vz neighbours only
+        // where they are plain unknowns (tag -1, StokesAssemblyDecoupled.c:
+        // 3669-3711): a Neumann wall node (tag 2) diagonal to the first or the
+        // last inner row has no entry there, so its coupling (the coefficients
+        // of :3573-3576 with comp = 1) is taken out of this row.
+        if (l == 1 || l == nz - 2) {
+            const T ixz = idx * idz, third = T(1.0 / 3.0);
+            T drop = 0;
+            if (l == 1 && G.BCv[c3 - nxvz - 1] == 2)
+                drop += (T(-3) * D.D23[iPrS] * inS * inSWv * wS + D.D31[ixyW] * inSWc * inW * wW -
+                         T(2) * D.D32[ixyW] * inSWc * inW * wW) * third * ixz * v[c3 - nxvz - 1];
+            if (l == 1 && G.BCv[c3 - nxvz + 1] == 2)
+                drop += (T(3) * D.D23[iPrS] * inS * inSEv * wS - D.D31[ixyE] * inE * inSEc * wE +
+                         T(2) * D.D32[ixyE] * inE * inSEc * wE) * third * ixz * v[c3 - nxvz + 1];
+            if (l == nz - 2 && G.BCv[c3 + nxvz - 1] == 2)
+                drop += (T(3) * D.D23[iPrN] * inN * inNWv * wN - D.D31[ixyW] * inNWc * inW * wW +
+                         T(2) * D.D32[ixyW] * inNWc * inW * wW) * third * ixz * v[c3 + nxvz - 1];
+            if (l == nz - 2 && G.BCv[c3 + nxvz + 1] == 2)
+                drop += (T(-3) * D.D23[iPrN] * inN * inNEv * wN + D.D31[ixyE] * inE * inNEc * wE -
+                         T(2) * D.D32[ixyE] * inE * inNEc * wE) * third * ixz * v[c3 + nxvz + 1];
+            ndrop = drop;
+        }
     }
     T grad = (p && G.BCp[iPrS] != 30 && G.BCp[iPrN] != 30) ? (p[iPrN] - p[iPrS]) * idz : T(0);
-    return -(inN * TzzN - inS * TzzS) * idz - (inE * TxzE - inW * TxzW) * idx + grad;
+    return -(inN * TzzN - inS * TzzS) * idz - (inE * TxzE - inW * TxzW) * idx + grad - ndrop;
 }
 
 // continuity row at centroid (k, l)

@@ -190,6 +190,12 @@ class Grid:
         return d
 
 
+class ThermalBC(C.Structure):
+    """mdz_thermal_bc (the reference's BCT BCt)."""
+    _fields_ = [("type", _sp), ("typW", _sp), ("typE", _sp), ("typS", _sp), ("typN", _sp),
+                ("valW", _dp), ("valE", _dp), ("valS", _dp), ("valN", _dp)]
+
+
 class Context:
     """One device context: grid mirror + resident markers (mdz_create)."""
 
@@ -406,6 +412,27 @@ class Context:
         self._check(self.L.mdz_mlp_infer(self.h, C.c_longlong(len(x)), x.ctypes.data_as(fp), y.ctypes.data_as(fp)))
         return y
 
+    def EnergyDirectSolve(self, fields, bc, dt, gz=0.0, shear_heating=0, adiab_heating=0, scale_T=1.0, rel_tol=0.0,
+                          max_iterations=0):
+        """mdz_EnergyDirectSolve: one implicit energy step on `fields` (T and
+        dT are written back); bc: dict of the thermal boundary arrays (type,
+        typW, typE, typS, typN as int8, valW, valE, valS, valN).  Returns
+        (iterations, relative residual)."""
+        arrs = {k: np.ascontiguousarray(bc[k], np.int8) for k in ("type", "typW", "typE", "typS", "typN")}
+        arrs.update({k: np.ascontiguousarray(bc[k], np.float64) for k in ("valW", "valE", "valS", "valN")})
+        b = ThermalBC(*[(_sptr if k.startswith("t") else _dptr)(arrs[k]) for k, _ in ThermalBC._fields_])
+        s = fields.struct()
+        its, rel = C.c_int(0), C.c_double(0)
+        self._check(self.L.mdz_EnergyDirectSolve(self.h, C.byref(s), C.byref(b), C.c_double(dt), C.c_double(gz),
+                                                 C.c_int(shear_heating), C.c_int(adiab_heating),
+                                                 C.c_double(scale_T), C.c_double(rel_tol), C.c_int(max_iterations),
+                                                 C.byref(its), C.byref(rel)))
+        return its.value, rel.value
+
+    def mlp_set_engine(self, engine):
+        """Inference kernel: 0 tcgen05 (tensor memory accumulators), 1 mma.sync."""
+        self._check(self.L.mdz_mlp_set_engine(self.h, C.c_int(engine)))
+
     def mlp_benchmark(self, batch, reps):
         a, b, c = C.c_double(0), C.c_double(0), C.c_double(0)
         self._check(self.L.mdz_mlp_benchmark(self.h, C.c_int(batch), C.c_int(reps), C.byref(a), C.byref(b),
@@ -504,6 +531,7 @@ class Context:
         self._check(self.L.mdz_set_solver_options(self.h, C.c_int(nu1), C.c_int(nu2), C.c_double(omega),
                                                   C.c_int(restart), C.c_int(check), C.c_int(mg_jacobian)))
 
+
     def mg_stencils(self, precision, level):
         """(levels, Nx, Nz, su[31, Nx*(Nz+1)], sv[31, (Nx+1)*Nz]) of one multigrid level."""
         nl, nx, nz = C.c_int(0), C.c_int(0), C.c_int(0)
@@ -544,14 +572,15 @@ FIELD_NAMES = [
     "D31_s", "D32_s", "D33_s", "D34_s",
     "roger_x", "roger_z", "rhs_p", "gx", "gz",
     "ru", "rv", "rp", "eII_exp", "eII_gbs",
+    "kx", "kz", "Cv", "Qr", "dT", "alp",
 ]
 
 VERTEX_FIELDS = {"div_u_s", "exz", "exxd_s", "ezzd_s", "sxz0", "sxxd0_s", "szzd0_s", "mu_s", "T_s", "P_s", "d0_s",
                  "phi0_s", "X0_s", "strain_s", "dil_s", "fric_s", "C_s", "p0_s", "bet_s", "rho_s", "eta_s",
                  "eta_phys_s", "VE_s", "sxz", "exz_el", "exz_diss", "detadexx_s", "detadezz_s", "detadgxz_s",
                  "detadp_s", "X_s", "OverS_s", "D31_s", "D32_s", "D33_s", "D34_s"}
-VX_FIELDS = {"u", "roger_x", "gx", "ru"}
-VZ_FIELDS = {"v", "roger_z", "gz", "rv"}
+VX_FIELDS = {"u", "roger_x", "gx", "ru", "kx"}
+VZ_FIELDS = {"v", "roger_z", "gz", "rv", "kz"}
 
 
 def field_size(grid, name, n_phases=1):

@@ -389,7 +389,7 @@ static void build_operator(grid *mesh, params model, SparseMat *Stokes, SparseMa
     if (Assemble == 1) { g_jacobian = jacobian; return; }
     mdz_fields f;
     fields_of(mesh, &f, model.Nb_phases, 0);
-    keep_only(&f, " u v p_corr D11_n D22_n D33_s roger_x roger_z rhs_p ru rv rp ");
+    keep_only(&f, " u v p_corr D11_n D22_n D33_s roger_x roger_z rhs_p ru rv rp eta_n eta_s ");
     double norms[3];
     check(mdz_EvaluateStokesResidualDecoupled(g_ctx, &f, norms), "BuildStokesOperatorDecoupled");
     rows_to_eqn(mesh, Stokes, mesh->ru, mesh->rv, mesh->rp, StokesA->F, StokesC->F);
@@ -416,7 +416,7 @@ void EvaluateStokesResidualDecoupled(SparseMat *Stokes, SparseMat *StokesA, Spar
     ensure(&model, mesh, NULL);
     mdz_fields f;
     fields_of(mesh, &f, model.Nb_phases, 0);
-    keep_only(&f, " u v p_corr D11_n D22_n D33_s roger_x roger_z rhs_p ru rv rp ");
+    keep_only(&f, " u v p_corr D11_n D22_n D33_s roger_x roger_z rhs_p ru rv rp eta_n eta_s ");
     double norms[3];
     check(mdz_EvaluateStokesResidualDecoupled(g_ctx, &f, norms), "EvaluateStokesResidualDecoupled");
     rows_to_eqn(mesh, Stokes, mesh->ru, mesh->rv, mesh->rp, StokesA->F, StokesC->F);

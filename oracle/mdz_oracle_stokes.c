@@ -90,7 +90,7 @@ static double cont_row(const mdz_grid_desc *g, const double *u, const double *v,
 }
 
 /* Newton rows: strain rates of the input first (exx', ezz' per centroid, gxz per vertex). */
-typedef struct { double *exx, *ezz, *gxz; } rates_t;
+typedef struct { double *exx, *ezz, *gxz; const double *v; } rates_t;
 
 static rates_t rates(const mdz_grid_desc *g, const double *u, const double *v) {
     int nx = g->Nx, nz = g->Nz, ncx = nx - 1, ncz = nz - 1, nxvz = nx + 1;
@@ -98,6 +98,7 @@ static rates_t rates(const mdz_grid_desc *g, const double *u, const double *v) {
     r.exx = calloc((size_t)ncx * ncz, sizeof(double));
     r.ezz = calloc((size_t)ncx * ncz, sizeof(double));
     r.gxz = calloc((size_t)nx * nz, sizeof(double));
+    r.v = v;
     for (int l = 0; l < ncz; l++)
         for (int k = 0; k < ncx; k++) {
             int cu = k + (l + 1) * nx, cv = k + 1 + l * nxvz;
@@ -174,14 +175,38 @@ static double newton_z(const mdz_grid_desc *g, const mdz_fields *f, const rates_
     double TxzW = f->D31_s[Wv] * exW + f->D32_s[Wv] * ezW + f->D33_s[Wv] * gx[Wv] + f->D34_s[Wv] * pW;
     double TxzE = f->D31_s[Ev] * exE + f->D32_s[Ev] * ezE + f->D33_s[Ev] * gx[Ev] + f->D34_s[Ev] * pE;
 #undef CV
-    return -(inN * TzzN - inS * TzzS) / g->dz - (inE * TxzE - inW * TxzW) / g->dx + (p[N] - p[S]) / g->dz;
+    double r = -(inN * TzzN - inS * TzzS) / g->dz - (inE * TxzE - inW * TxzW) / g->dx + (p[N] - p[S]) / g->dz;
+    /* The reference's Jacobian assembles the diagonal Vz neighbours only where
+     * they are plain unknowns (tag -1, StokesAssemblyDecoupled.c:3669-3711):
+     * a Neumann wall node (tag 2) south-west / south-east of the first inner
+     * row, or north-west / north-east of the last, has no entry in that row.
+     * Its coupling (the coefficients of :3573-3576, comp = 1) is taken out. */
+    const double *vv = R->v;
+    const double ixz = 1.0 / (g->dx * g->dz);
+    if (l == 1) {
+        if (g->BCv_type[c3 - nxvz - 1] == 2)
+            r -= (-3.0 * f->D23_n[S] * inS * inSWv * wS + f->D31_s[Wv] * inSWc * inW * wW -
+                  2.0 * f->D32_s[Wv] * inSWc * inW * wW) / 3.0 * ixz * vv[c3 - nxvz - 1];
+        if (g->BCv_type[c3 - nxvz + 1] == 2)
+            r -= (3.0 * f->D23_n[S] * inS * inSEv * wS - f->D31_s[Ev] * inE * inSEc * wE +
+                  2.0 * f->D32_s[Ev] * inE * inSEc * wE) / 3.0 * ixz * vv[c3 - nxvz + 1];
+    }
+    if (l == nz - 2) {
+        if (g->BCv_type[c3 + nxvz - 1] == 2)
+            r -= (3.0 * f->D23_n[N] * inN * inNWv * wN - f->D31_s[Wv] * inNWc * inW * wW +
+                  2.0 * f->D32_s[Wv] * inNWc * inW * wW) / 3.0 * ixz * vv[c3 + nxvz - 1];
+        if (g->BCv_type[c3 + nxvz + 1] == 2)
+            r -= (-3.0 * f->D23_n[N] * inN * inNEv * wN + f->D31_s[Ev] * inE * inNEc * wE -
+                  2.0 * f->D32_s[Ev] * inE * inNEc * wE) / 3.0 * ixz * vv[c3 + nxvz + 1];
+    }
+    return r;
 }
 
 int orc_stokes_apply(const mdz_grid_desc *g, const mdz_fields *f, int jacobian, int residual, const double *u,
                      const double *v, const double *p, double *yu, double *yv, double *yp) {
     int nx = g->Nx, nz = g->Nz, ncx = nx - 1, ncz = nz - 1, nxvz = nx + 1;
     double celvol = g->dx * g->dz;
-    rates_t R = {0, 0, 0};
+    rates_t R = {0, 0, 0, 0};
     if (jacobian) R = rates(g, u, v);
     /* rows are independent: threaded loops give the serial loop's bits */
 #pragma omp parallel for schedule(static)

@@ -163,6 +163,7 @@ double *ref_field(const char *name) {
     F(detadexx_s) F(detadezz_s) F(detadgxz_s) F(detadp_s)
     F(roger_x) F(roger_z) F(rhs_p) F(ru) F(rv) F(rp) F(gx) F(gz)
     F(xg_coord) F(zg_coord) F(xc_coord) F(zc_coord) F(xvz_coord) F(zvx_coord) F(dp) F(p_lith) F(p_lith0)
+    F(kx) F(kz) F(Cv) F(Qr) F(dT) F(alp)
 #undef F
     if (!strcmp(name, "BCu_val")) return g_mesh.BCu.val;
     if (!strcmp(name, "BCv_val")) return g_mesh.BCv.val;
@@ -352,4 +353,112 @@ int ref_block(int jacobian, int b, int **Ic, int **J, double **A, double **bbc) 
                             : (b == 0 ? &g_SA : b == 1 ? &g_SB : b == 2 ? &g_SC : &g_SD);
     *Ic = M->Ic; *J = M->J; *A = M->A; *bbc = M->bbc;
     return M->neq;
+}
+
+
+/* ------------------------------------------------------------------------ */
+/* Energy equation.  ThermalSolver.c (the CHOLMOD factorisation and solve of
+ * EnergyDirectSolve) is not built; these stand-ins keep a copy of the matrix
+ * the reference assembled and of its right-hand side, and solve the system by
+ * dense Gaussian elimination with partial pivoting (fixture sizes, a few
+ * hundred unknowns), so that EnergyDirectSolve runs to its end.  Test
+ * infrastructure only. */
+static int g_en_n = 0, g_en_nnz = 0;
+static int *g_en_ia = NULL, *g_en_ja = NULL;
+static double *g_en_a = NULL, *g_en_b = NULL, *g_en_x = NULL;
+static cholmod_factor g_en_factor;
+
+int cholmod_start(cholmod_common *c) { (void)c; return 1; }
+int cholmod_finish(cholmod_common *c) { (void)c; return 1; }
+int cholmod_free_factor(cholmod_factor **f, cholmod_common *c) { (void)f; (void)c; return 1; }
+cs_di *cs_spfree(cs_di *A) { (void)A; return NULL; }
+cs_di *TransposeA(cholmod_common *c, double *A, int *Ic, int *J, int neq, int nnz) {
+    (void)c; (void)A; (void)Ic; (void)J; (void)neq; (void)nnz;
+    return NULL;   /* used by the polar mode only */
+}
+
+cholmod_factor *FactorEnergyCHOLMOD(cholmod_common *c, cs_di *At, double *a, int *ia, int *ja, int n, int nnz,
+                                    int polar_mode) {
+    (void)c; (void)At; (void)polar_mode;
+    free(g_en_ia); free(g_en_ja); free(g_en_a);
+    g_en_n = n; g_en_nnz = nnz;
+    g_en_ia = malloc(sizeof(int) * (n + 1));
+    g_en_ja = malloc(sizeof(int) * (nnz > 0 ? nnz : 1));
+    g_en_a = malloc(sizeof(double) * (nnz > 0 ? nnz : 1));
+    memcpy(g_en_ia, ia, sizeof(int) * (n + 1));
+    memcpy(g_en_ja, ja, sizeof(int) * nnz);
+    memcpy(g_en_a, a, sizeof(double) * nnz);
+    return &g_en_factor;
+}
+
+void SolveEnergyCHOLMOD(cholmod_common *c, cs_di *At, cholmod_factor *F, double *x, double *b, int n, int nnz,
+                        int polar_mode) {
+    (void)c; (void)At; (void)F; (void)nnz; (void)polar_mode;
+    int i, j, k;
+    free(g_en_b); free(g_en_x);
+    g_en_b = malloc(sizeof(double) * n);
+    g_en_x = malloc(sizeof(double) * n);
+    memcpy(g_en_b, b, sizeof(double) * n);
+    double *M = calloc((size_t)n * (n + 1), sizeof(double));
+    for (i = 0; i < n; i++) {
+        for (k = g_en_ia[i]; k < g_en_ia[i + 1]; k++) M[(size_t)i * (n + 1) + g_en_ja[k]] += g_en_a[k];
+        M[(size_t)i * (n + 1) + n] = b[i];
+    }
+    for (j = 0; j < n; j++) {
+        int piv = j;
+        for (i = j + 1; i < n; i++)
+            if (fabs(M[(size_t)i * (n + 1) + j]) > fabs(M[(size_t)piv * (n + 1) + j])) piv = i;
+        if (piv != j)
+            for (k = 0; k <= n; k++) {
+                double t = M[(size_t)j * (n + 1) + k];
+                M[(size_t)j * (n + 1) + k] = M[(size_t)piv * (n + 1) + k];
+                M[(size_t)piv * (n + 1) + k] = t;
+            }
+        for (i = j + 1; i < n; i++) {
+            double f = M[(size_t)i * (n + 1) + j] / M[(size_t)j * (n + 1) + j];
+            if (f == 0.0) continue;
+            for (k = j; k <= n; k++) M[(size_t)i * (n + 1) + k] -= f * M[(size_t)j * (n + 1) + k];
+        }
+    }
+    for (i = n - 1; i >= 0; i--) {
+        double s = M[(size_t)i * (n + 1) + n];
+        for (k = i + 1; k < n; k++) s -= M[(size_t)i * (n + 1) + k] * x[k];
+        x[i] = s / M[(size_t)i * (n + 1) + i];
+    }
+    memcpy(g_en_x, x, sizeof(double) * n);
+    free(M);
+}
+
+/* One implicit energy step (EnergyDirectSolve, ThermalRoutines.c:72-551,
+ * nit = 1) on the harness grid: mesh T, rho_n, Cv, Qr, kx, kz, Wdiss, alp,
+ * BCt. */
+int ref_energy_solve(double dt, int shear_heating, int adiab_heating) {
+    EnergyDirectSolve(&g_mesh, g_model, g_mesh.T, g_mesh.dT, NULL, g_mesh.T, &g_parts, dt, shear_heating,
+                      adiab_heating, g_scale, 1);
+    return 0;
+}
+
+/* The last assembled energy system: n rows, CSR (ia, ja, a), right-hand side
+ * b (b + bbc as solved) and solution x. */
+int ref_energy_system(int **ia, int **ja, double **a, double **b, double **x) {
+    *ia = g_en_ia; *ja = g_en_ja; *a = g_en_a; *b = g_en_b; *x = g_en_x;
+    return g_en_n;
+}
+
+/* Thermal boundary arrays (BCT BCt): tags "type" (centroids), "typW",
+ * "typE" (Nz-1), "typS", "typN" (Nx-1); values "valW" ... "valN". */
+char *ref_bct_tags(const char *name) {
+    if (!strcmp(name, "type")) return g_mesh.BCt.type;
+    if (!strcmp(name, "typW")) return g_mesh.BCt.typW;
+    if (!strcmp(name, "typE")) return g_mesh.BCt.typE;
+    if (!strcmp(name, "typS")) return g_mesh.BCt.typS;
+    if (!strcmp(name, "typN")) return g_mesh.BCt.typN;
+    return NULL;
+}
+double *ref_bct_vals(const char *name) {
+    if (!strcmp(name, "valW")) return g_mesh.BCt.valW;
+    if (!strcmp(name, "valE")) return g_mesh.BCt.valE;
+    if (!strcmp(name, "valS")) return g_mesh.BCt.valS;
+    if (!strcmp(name, "valN")) return g_mesh.BCt.valN;
+    return NULL;
 }

@@ -41,6 +41,8 @@ class RefMDOODZ:
         L.ref_eqn.restype = _ip
         L.ref_residual_vec.restype = _dp
         L.ref_rhs_vec.restype = _dp
+        L.ref_bct_tags.restype = _cp
+        L.ref_bct_vals.restype = _dp
         L.ref_set_param.argtypes = [C.c_char_p, C.c_double]
         L.ref_set_mat.argtypes = [C.c_char_p, C.c_int, C.c_double]
         L.ref_setup(C.c_int(Nx), C.c_int(Nz), C.c_double(xmin), C.c_double(xmax), C.c_double(zmin),
@@ -55,7 +57,7 @@ class RefMDOODZ:
                 "xg": Nx, "zg": Nz, "xc": Nx - 1, "zc": Nz - 1, "xvz": Nx + 1, "zvx": Nz + 1}[kind]
 
     _KIND = {
-        "u_in": "u", "v_in": "v", "roger_x": "u", "ru": "u", "BCu_val": "u", "gx": "u",
+        "u_in": "u", "v_in": "v", "roger_x": "u", "ru": "u", "BCu_val": "u", "gx": "u", "kx": "u", "kz": "v",
         "roger_z": "v", "rv": "v", "BCv_val": "v", "gz": "v",
         "xg_coord": "xg", "zg_coord": "zg", "xc_coord": "xc", "zc_coord": "zc", "xvz_coord": "xvz",
         "zvx_coord": "zvx",
@@ -219,3 +221,29 @@ class RefMDOODZ:
             a = np.ctypeslib.as_array(A, shape=(max(nnz, 1),))[:nnz].copy() if nnz else np.zeros(0)
             out.append(sp.csr_matrix((a, j, ic), shape=(nr, ncol)))
         return out
+
+    # ---- energy equation (EnergyDirectSolve with the harness's dense stand-in solve)
+    def bct_tags(self, name):
+        """numpy int8 view of BCt.type (centroids) or BCt.typW/E (Nz-1), typS/N (Nx-1)."""
+        n = {"type": self.size("n"), "typW": self.Nz - 1, "typE": self.Nz - 1, "typS": self.Nx - 1,
+             "typN": self.Nx - 1}[name]
+        return np.ctypeslib.as_array(C.cast(self.lib.ref_bct_tags(name.encode()), C.POINTER(C.c_int8)), shape=(n,))
+
+    def bct_vals(self, name):
+        n = {"valW": self.Nz - 1, "valE": self.Nz - 1, "valS": self.Nx - 1, "valN": self.Nx - 1}[name]
+        return np.ctypeslib.as_array(self.lib.ref_bct_vals(name.encode()), shape=(n,))
+
+    def energy_solve(self, dt, shear_heating, adiab_heating):
+        self.lib.ref_energy_solve(C.c_double(dt), C.c_int(shear_heating), C.c_int(adiab_heating))
+
+    def energy_system(self):
+        """(CSR matrix, right-hand side b + bbc, solution) of the last energy solve."""
+        import scipy.sparse as sp
+        ia, ja, a, b, x = _ip(), _ip(), _dp(), _dp(), _dp()
+        n = self.lib.ref_energy_system(C.byref(ia), C.byref(ja), C.byref(a), C.byref(b), C.byref(x))
+        ic = np.ctypeslib.as_array(ia, shape=(n + 1,)).copy()
+        nnz = int(ic[-1])
+        j = np.ctypeslib.as_array(ja, shape=(nnz,)).copy()
+        v = np.ctypeslib.as_array(a, shape=(nnz,)).copy()
+        return (sp.csr_matrix((v, j, ic), shape=(n, n)), np.ctypeslib.as_array(b, shape=(n,)).copy(),
+                np.ctypeslib.as_array(x, shape=(n,)).copy())

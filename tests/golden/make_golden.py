@@ -157,10 +157,27 @@ def rheology_inputs(g, rng):
     return f
 
 
-def make_rheology_fixture(avg=0, tag="", phases=None, model=None):
+def set_neumann_walls(tu, vu, tv, vv, seed=21):
+    """Neumann (tag 2) west and east Vx lines and south Vz line with seeded
+    tractions; the north wall stays Dirichlet (arrays in grid layout, changed
+    in place)."""
+    rng = np.random.default_rng(seed)
+    Nx, Nz = NX, NZ
+    tu, vu = tu.reshape(Nz + 1, Nx), vu.reshape(Nz + 1, Nx)
+    tv, vv = tv.reshape(Nz, Nx + 1), vv.reshape(Nz, Nx + 1)
+    for k in (0, Nx - 1):
+        tu[1:Nz, k] = 2
+        vu[1:Nz, k] = 0.3 * rng.standard_normal(Nz - 1)
+    tv[0, 1:Nx] = 2
+    vv[0, 1:Nx] = 0.2 * rng.standard_normal(Nx - 1)
+
+
+def make_rheology_fixture(avg=0, tag="", phases=None, model=None, neumann=False):
     g = _grid()
     r = RefMDOODZ(NX, NZ, XMIN, XMAX, ZMIN, ZMAX, 3)
     r.set_bc_pureshear(1.0)
+    if neumann:
+        set_neumann_walls(r.tags("BCu"), r.field("BCu_val"), r.tags("BCv"), r.field("BCv_val"))
     for k, v in (model or RHEO_MODEL).items():
         r.set_param(k, v)
     r.set_param("eta_avg", avg)
@@ -217,14 +234,23 @@ def make_rheology_fixture(avg=0, tag="", phases=None, model=None):
                  "D34_s"):
         out["op1_" + name] = r.field(name).copy()
     r.set_param("gz", -1.0)
+    if neumann:
+        r.set_param("gx", 0.2)
     r.rhs()
     for name in ("roger_x", "roger_z", "rhs_p"):
         out["rhs_" + name] = r.field(name).copy()
     out["gz"] = -1.0
+    out["gx"] = 0.2 if neumann else 0.0
+    if neumann:
+        for name in ("BCu", "BCv"):
+            out["bc_" + name] = r.tags(name).copy()
+            out["bc_" + name + "_val"] = r.field(name + "_val").copy()
     if avg == 0:
         # decoupled Stokes: non-linear residual (Picard operator, p_corr) and
         # the assembled Picard and Newton blocks in the reference's numbering
         r.rheo_operators(0)
+        if neumann:   # the Neumann rows take their Dirichlet terms from the last assembly
+            r.assemble(0)
         norms, Fm, Fc = r.residual()
         out["st_norms"] = norms
         for name in ("ru", "rv", "rp"):
@@ -242,6 +268,63 @@ def make_rheology_fixture(avg=0, tag="", phases=None, model=None):
                 out["st_J%d_%s_shape" % (jac, b)] = np.array(M.shape)
     np.savez_compressed(os.path.join(HERE, "rheology_ref%s.npz" % tag), **out)
     print("rheology_ref%s.npz: plastic centroids %d / %d" % (tag, (out["vg_eII_pl"] > 0).sum(), out["vg_eII_pl"].size))
+
+
+THERMAL_CASES = [dict(dt=0.05, shear_heating=1, adiab_heating=1, gz=-1.0),
+                 dict(dt=0.2, shear_heating=0, adiab_heating=2, gz=0.0)]
+
+
+def thermal_inputs(rng, ncx, ncz, Nx, Nz):
+    """Seeded energy-equation inputs and thermal boundaries: Dirichlet south
+    and north walls (a few south cells with a prescribed flux instead), a
+    Dirichlet west wall on the lower half, zero flux elsewhere."""
+    Xc, Zc = np.meshgrid(np.arange(ncx), np.arange(ncz))
+    f = dict(T=(1.0 + 0.3 * np.sin(0.4 * Xc) * np.cos(0.3 * Zc) + 0.05 * rng.random(Xc.shape)).ravel(),
+             rho_n=1.0 + 0.1 * rng.random(ncx * ncz), Cv=0.8 + 0.4 * rng.random(ncx * ncz),
+             Qr=0.1 * rng.random(ncx * ncz), Wdiss=0.2 * rng.random(ncx * ncz), alp=0.05 * rng.random(ncx * ncz),
+             kx=np.exp(0.5 * rng.standard_normal(Nx * (Nz + 1))), kz=np.exp(0.5 * rng.standard_normal((Nx + 1) * Nz)),
+             p=rng.standard_normal(ncx * ncz), p0_n=rng.standard_normal(ncx * ncz),
+             v=rng.standard_normal((Nx + 1) * Nz))
+    bc = dict(type=np.full(ncx * ncz, -1, np.int8), typS=np.ones(ncx, np.int8), typN=np.ones(ncx, np.int8),
+              typW=np.zeros(ncz, np.int8), typE=np.zeros(ncz, np.int8),
+              valS=1.0 + 0.1 * rng.random(ncx), valN=0.5 + 0.1 * rng.random(ncx), valW=0.8 + 0.1 * rng.random(ncz),
+              valE=np.zeros(ncz))
+    bc["typS"][3:6] = 2
+    bc["typW"][:ncz // 2] = 1
+    return f, bc
+
+
+def make_thermal_fixture():
+    """EnergyDirectSolve (one implicit step) for two settings of the heating
+    switches: the matrix and right-hand side it assembled and the new T."""
+    Nx, Nz = NX, NZ
+    ncx, ncz = Nx - 1, Nz - 1
+    out = dict(Nx=Nx, Nz=Nz, box=np.array([XMIN, XMAX, ZMIN, ZMAX]))
+    for q, case in enumerate(THERMAL_CASES):
+        r = RefMDOODZ(NX, NZ, XMIN, XMAX, ZMIN, ZMAX, 1)
+        r.set_bc_pureshear(1.0)
+        rng = np.random.default_rng(40 + q)
+        f, bc = thermal_inputs(rng, ncx, ncz, Nx, Nz)
+        for name, arr in f.items():
+            r.field({"p": "p_in", "v": "v_in"}.get(name, name))[:] = arr
+        for name in ("type", "typW", "typE", "typS", "typN"):
+            r.bct_tags(name)[:] = bc[name]
+        for name in ("valW", "valE", "valS", "valN"):
+            r.bct_vals(name)[:] = bc[name]
+        r.set_param("gz", case["gz"])
+        r.set_param("dt", case["dt"])
+        r.energy_solve(case["dt"], case["shear_heating"], case["adiab_heating"])
+        A, b, x = r.energy_system()
+        pre = "c%d_" % q
+        out.update({pre + "in_" + k: v for k, v in f.items()})
+        out.update({pre + "bc_" + k: v for k, v in bc.items()})
+        out[pre + "T"] = r.field("T").copy()
+        out[pre + "dT"] = r.field("dT").copy()
+        out[pre + "A_data"], out[pre + "A_indices"], out[pre + "A_indptr"] = A.data, A.indices, A.indptr
+        out[pre + "rhs"], out[pre + "x"] = b, x
+        out[pre + "case"] = np.array([case["dt"], case["shear_heating"], case["adiab_heating"], case["gz"]])
+    np.savez_compressed(os.path.join(HERE, "thermal_ref.npz"), **out)
+    print("thermal_ref.npz: %d unknowns" % (ncx * ncz))
 
 
 def _c2v_np(g, cen):
@@ -451,7 +534,7 @@ def make_pressure_fixture():
 
 
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["markers", "rheology", "reseed", "strain", "stress", "gridprops", "pressure"]
+    what = sys.argv[1:] or ["markers", "rheology", "reseed", "strain", "stress", "gridprops", "pressure", "thermal"]
     if "gridprops" in what:
         make_gridprops_fixture()
     if "pressure" in what:
@@ -470,3 +553,7 @@ if __name__ == "__main__":
         make_rheology_fixture(2, "_geom")
     if "rheology" in what or "mech" in what:
         make_rheology_fixture(0, "_mech", RHEO_PHASES_MECH, RHEO_MODEL_MECH)
+    if "thermal" in what:
+        make_thermal_fixture()
+    if "rheology" in what or "neumann" in what:
+        make_rheology_fixture(0, "_neumann", neumann=True)

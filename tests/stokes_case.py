@@ -11,8 +11,12 @@ def reference_state(ref, jacobian):
     p_corr, RHS and the Picard (jacobian=0) or Newton (jacobian=1) D tensor."""
     from golden.make_golden import NX, NZ, XMIN, XMAX, ZMIN, ZMAX
     g = mdz.Grid(NX, NZ, XMIN, XMAX, ZMIN, ZMAX).set_bc_pureshear(1.0)
+    if "bc_BCu" in ref:   # a fixture with its own boundary tags and values (Neumann walls)
+        g.BCu[:], g.BCu_val[:] = ref["bc_BCu"], ref["bc_BCu_val"]
+        g.BCv[:], g.BCv_val[:] = ref["bc_BCv"], ref["bc_BCv_val"]
     f = mdz.GridFields(g, 3)
     f["u"], f["v"], f["p"] = ref["in_u"], ref["in_v"], ref["in_p"]
+    f["eta_n"], f["eta_s"] = ref["vg_eta_n"], ref["vg_eta_s"]   # read by the Neumann rows
     f["p_corr"] = ref["vg_p_corr"]
     for k in ref:
         if k.startswith("op%d_" % jacobian):

@@ -51,14 +51,38 @@ def test_gradients_match_cpu_oracle(n):
     ctx.close()
 
 
-def test_inference_matches_cpu_oracle():
+@pytest.mark.parametrize("engine", [0, 1])   # tcgen05 / mma.sync
+def test_inference_matches_cpu_oracle(engine):
     ctx = _ctx()
     ctx.mlp_init(2)
     p = ctx.mlp_get_weights().astype(np.float64)
-    x, _ = _rows(5000, 9)
-    y = ctx.mlp_infer(x)
-    ref = mo.forward(p, x.astype(np.float64), bf=True)[3]
-    assert np.max(np.abs(y - ref)) <= 1e-3 * (1.0 + np.max(np.abs(ref)))
+    rng = np.random.default_rng(4)
+    p[mo.SLICES["b1"][0]:mo.SLICES["b1"][0] + 64] = rng.normal(0, 0.1, 64)   # non-zero biases
+    p[mo.SLICES["b2"][0]:mo.SLICES["b2"][0] + 64] = rng.normal(0, 0.1, 64)
+    p[mo.SLICES["b3"][0]:mo.SLICES["b3"][0] + 2] = rng.normal(0, 0.1, 2)
+    ctx.mlp_set_weights(p)
+    ctx.mlp_set_engine(engine)
+    for n in (5000, 128, 1):   # ragged tail, one full tile, one row
+        x, _ = _rows(n, 9 + n)
+        y = ctx.mlp_infer(x)
+        ref = mo.forward(p, x.astype(np.float64), bf=True)[3]
+        assert np.max(np.abs(y - ref)) <= 1e-3 * (1.0 + np.max(np.abs(ref))), n
+    ctx.close()
+
+
+def test_tensor_core_engines_agree():
+    """The tcgen05 kernel (128-row tiles, TMEM accumulators) and the mma.sync
+    kernel give the same network output to FP32 accumulation-order rounding on
+    70 000 rows (grid-stride over many CTAs)."""
+    ctx = _ctx()
+    ctx.mlp_init(7)
+    x, _ = _rows(70000, 3)
+    ctx.mlp_set_engine(0)
+    y0 = ctx.mlp_infer(x)
+    ctx.mlp_set_engine(1)
+    y1 = ctx.mlp_infer(x)
+    assert np.max(np.abs(y0 - y1)) <= 2e-2 * (1.0 + np.max(np.abs(y1)))
+    assert np.mean(np.abs(y0 - y1)) <= 1e-3 * (1.0 + np.max(np.abs(y1)))
     ctx.close()
 
 

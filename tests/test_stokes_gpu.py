@@ -11,8 +11,11 @@ from stokes_case import assembled, eqn_maps, reference_state, to_eqn, to_grid
 pytestmark = pytest.mark.gpu
 
 
-def test_residual_vs_reference(golden):
-    ref = golden("rheology_ref.npz")
+@pytest.mark.parametrize("fixture", ["rheology_ref.npz", "rheology_ref_neumann.npz"])
+def test_residual_vs_reference(golden, fixture):
+    """Residual rows and norms; the second fixture has Neumann (tag 2) west,
+    east and south walls with prescribed tractions and gravity along x."""
+    ref = golden(fixture)
     g, f = reference_state(ref, 0)
     ctx = mdz.Context(g, 3, 1)
     norms = ctx.EvaluateStokesResidualDecoupled(f)
@@ -22,9 +25,10 @@ def test_residual_vs_reference(golden):
     ctx.close()
 
 
+@pytest.mark.parametrize("fixture", ["rheology_ref.npz", "rheology_ref_neumann.npz"])
 @pytest.mark.parametrize("jacobian", [0, 1])
-def test_operator_vs_assembled_blocks(golden, jacobian):
-    ref = golden("rheology_ref.npz")
+def test_operator_vs_assembled_blocks(golden, jacobian, fixture):
+    ref = golden(fixture)
     g, f = reference_state(ref, jacobian)
     K = assembled(ref, jacobian)
     maps = eqn_maps(ref)
