@@ -514,6 +514,11 @@ def main():
                      "frac": (achieved / hbm) if achieved else None,
                      "traffic": TRAFFIC_PER_LAUNCH.get(k["name"]) if not size else None,
                      "peak_kind": peak_kind},
+        # every instrumented kernel class of the FP32 form: live CUDA-event time per step, algorithmic
+        # bytes over that time and its fraction of the measured copy bandwidth
+        "class_bandwidth": {name: {"ms_per_step": c["ms"] / args.steps, "GB/s": c["bytes"] / (c["ms"] * 1e-3) / 1e9,
+                                   "frac": c["bytes"] / (c["ms"] * 1e-3) / 1e9 / hbm}
+                            for name, c in fast["kernel"]["classes"].items() if c["ms"] > 0},
         "clocks": clk.summary(),
     }
     if fast["reseed"]:

@@ -447,6 +447,14 @@ mdz_status mdz_SolveStokesDefect(mdz_ctx *ctx, mdz_fields *f, int jacobian, int 
 mdz_status mdz_set_solver_options(mdz_ctx *ctx, int nu1, int nu2, double omega, int restart, int check,
                                   int mg_jacobian);
 
+/* Pressure block of the preconditioner in Newton (Jacobian) solves: mode 0
+ * (default) scales the pressure residual by eta_n / cell volume, as in the
+ * Picard solves; mode 1 by the Jacobian's own D11 / 2 (the tangent viscosity,
+ * which the plastic part of the Newton tangent lowers below eta_n) wherever
+ * that is positive, eta_n elsewhere.  No counterpart in the reference (its
+ * defect solves are direct). */
+mdz_status mdz_set_schur_scaling(mdz_ctx *ctx, int mode);
+
 /* Multigrid stencils of one level after a solve (diagnostics and tests; no
  * counterpart in the reference).  31 coefficient planes per velocity row,
  * structure of arrays: su[31][Nx*(Nz+1)] for Vx rows, sv[31][(Nx+1)*Nz] for Vz

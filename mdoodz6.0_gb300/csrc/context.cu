@@ -116,6 +116,7 @@ extern "C" mdz_status mdz_create(mdz_ctx **out, const mdz_grid_desc *d, int n_ph
     int ncells = (Nx - 1) * (Nz - 1);
     ctx->bins.ncells = ncells;
     UP(ctx->bins.cell, (const int *)nullptr, cap); UP(ctx->bins.sorted, (const int *)nullptr, cap);
+    UP(ctx->bins.qvert, (const int *)nullptr, cap);
     UP(ctx->bins.count, (const int *)nullptr, ncells + 1); UP(ctx->bins.start, (const int *)nullptr, ncells + 1);
     UP(ctx->bins.cursor, (const int *)nullptr, ncells + 1);
     UP(ctx->bins.scan_partials, (const int *)nullptr, (ncells + 1) / 1024 + 2);
@@ -144,7 +145,7 @@ extern "C" void mdz_destroy(mdz_ctx *ctx) {
     mdz_dgrid &g = ctx->g;
     void *ptrs[] = {g.xg, g.zg, g.xc, g.zc, g.xvz, g.zvx, g.BCu, g.BCv, g.BCp, g.BCg, g.BCu_val, g.BCv_val,
                     ctx->m.x, ctx->m.z, ctx->m.vx, ctx->m.vz, ctx->m.phase, ctx->bins.cell, ctx->bins.sorted,
-                    ctx->bins.count, ctx->bins.start, ctx->bins.cursor, ctx->bins.scan_partials,
+                    ctx->bins.qvert, ctx->bins.count, ctx->bins.start, ctx->bins.cursor, ctx->bins.scan_partials,
                     ctx->red_part, ctx->red_cnt, ctx->ale_sums};
     for (void *p : ptrs)
         if (p) cudaFree(p);

@@ -125,6 +125,23 @@ __global__ void k_bin_sort_segments(int ncells, const int *__restrict__ start, i
     }
 }
 
+// Nearest vertex of the marker at each sorted position (the projection onto
+// vertices tests every marker of its four candidate cells against the node:
+// with the index stored once per binning the three markers in four that
+// belong to another vertex cost an integer compare instead of two FP64 index
+// computations, FP64 being a small fraction of the FP32 rate on this part).
+// Same formula, lines and clamps as the projection's own nearest_line.
+__global__ void k_bin_vertices(int n, const int *__restrict__ nbinned, const int *__restrict__ sorted,
+                               const double *__restrict__ x, const double *__restrict__ z,
+                               const double *__restrict__ xg, const double *__restrict__ zg, double dx, double dz,
+                               double idx, double idz, int Nx, int Nz, int *__restrict__ qvert) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n || q >= *nbinned) return;
+    const int k = sorted[q];
+    const int ip = nearest_line(x[k], xg[0], dx, idx, Nx), jp = nearest_line(z[k], zg[0], dz, idz, Nz);
+    qvert[q] = ip | (jp << 16);
+}
+
 mdz_status mdz_ensure_bins(mdz_ctx *ctx, cudaStream_t st) {
     mdz_bins &B = ctx->bins;
     if (B.valid) return MDZ_OK;
@@ -150,6 +167,11 @@ mdz_status mdz_ensure_bins(mdz_ctx *ctx, cudaStream_t st) {
     }
     k_bin_sort_segments<<<mdz_blocks(nc), MDZ_THREADS, 0, st>>>(nc, B.start, B.sorted);
     MDZ_LAUNCHED(ctx);
+    if (n > 0) {
+        k_bin_vertices<<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, B.start + nc, B.sorted, ctx->m.x, ctx->m.z, g.xg,
+                                                              g.zg, g.dx, g.dz, g.idx, g.idz, g.Nx, g.Nz, B.qvert);
+        MDZ_LAUNCHED(ctx);
+    }
     B.valid = true;
     return MDZ_OK;
 }
@@ -183,9 +205,9 @@ template <int NF, int NPH>
 __global__ void __launch_bounds__(128) k_p2g_gather(
     int nnx, int nnz, const double *__restrict__ X, const double *__restrict__ Z, const signed char *__restrict__ tag,
     int kindx, int kindz, int h, double dx, double dz, double dx_itp, double dz_itp, int ncx, int ncz,
-    const int *__restrict__ start, const int *__restrict__ sorted, const double *__restrict__ mx,
-    const double *__restrict__ mz, const int *__restrict__ mphase, p2g_fields F, int nph_rt,
-    double *__restrict__ phase_perc) {
+    const int *__restrict__ start, const int *__restrict__ sorted, const int *__restrict__ qvert,
+    const double *__restrict__ mx, const double *__restrict__ mz, const int *__restrict__ mphase, p2g_fields F,
+    int nph_rt, double *__restrict__ phase_perc) {
     int node = blockIdx.x * blockDim.x + threadIdx.x;
     if (node >= nnx * nnz) return;
     int i = node % nnx, j = node / nnx;
@@ -199,34 +221,57 @@ __global__ void __launch_bounds__(128) k_p2g_gather(
     for (int p = 0; p < NPH; p++) Wph[p] = 0.0;
     const double X0 = X[0], Z0 = Z[0];
     const double idx = 1.0 / dx, idz = 1.0 / dz, idxi = 1.0 / dx_itp, idzi = 1.0 / dz_itp;
+    // contribution of marker k, whose nearest node (ip, jp) is within h of this one
+    auto add = [&](int k, int ip, int jp, int di, int dj) {
+        const double xk = mx[k], zk = mz[k];
+        double Xn = X[ip], Zn = Z[jp];
+        if (di > 0) Xn = X[ip] + dx;
+        if (di < 0) Xn = X[ip] - dx;
+        if (dj > 0) Zn = Z[jp] + dz;
+        if (dj < 0) Zn = Z[jp] - dz;
+        double dxm = fabs(Xn - xk), dzm = fabs(Zn - zk);
+        double w = (1.0 - dxm * idxi) * (1.0 - dzm * idzi);
+        int p = mphase[k];
+        Wm += w;
+#pragma unroll
+        for (int pp = 0; pp < NPH; pp++)
+            if (p == pp) Wph[pp] += w;
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            double v = F.per_phase[f] ? F.val[f][p] : F.val[f][k];
+            if (F.avg[f] == 1) v = 1.0 / v;
+            if (F.avg[f] == 2) v = log(v);
+            BmWm[f] += v * w;
+        }
+    };
+    // Markers in the order the reference's loop meets them: cell rows
+    // upwards, cells left to right, markers by index inside a cell.
+    const bool cellnode = kindx == 0 && kindz == 0;   // centroids: the bin cell is the nearest centroid
     for (int r = rlo; r <= rhi; r++) {
+        if (cellnode) {
+            for (int c = clo; c <= chi; c++) {
+                const int di = i - c, dj = j - r;
+                if (di < -h || di > h || dj < -h || dj > h) continue;
+                const int cell = c + r * ncx;
+                for (int q = start[cell], e = start[cell + 1]; q < e; q++) add(sorted[q], c, r, di, dj);
+            }
+            continue;
+        }
         int b = start[clo + r * ncx], e = start[chi + r * ncx + 1];
         for (int q = b; q < e; q++) {
-            int k = sorted[q];
-            double xk = mx[k], zk = mz[k];
-            int ip = nearest_line(xk, X0, dx, idx, nnx);
-            int jp = nearest_line(zk, Z0, dz, idz, nnz);
+            int ip, jp;
+            if (qvert) {   // vertices: the stored nearest vertex
+                const int pk = qvert[q];
+                ip = pk & 0xffff;
+                jp = pk >> 16;
+            } else {
+                const int k = sorted[q];
+                ip = nearest_line(mx[k], X0, dx, idx, nnx);
+                jp = nearest_line(mz[k], Z0, dz, idz, nnz);
+            }
             int di = i - ip, dj = j - jp;
             if (di < -h || di > h || dj < -h || dj > h) continue;
-            double Xn = X[ip], Zn = Z[jp];
-            if (di > 0) Xn = X[ip] + dx;
-            if (di < 0) Xn = X[ip] - dx;
-            if (dj > 0) Zn = Z[jp] + dz;
-            if (dj < 0) Zn = Z[jp] - dz;
-            double dxm = fabs(Xn - xk), dzm = fabs(Zn - zk);
-            double w = (1.0 - dxm * idxi) * (1.0 - dzm * idzi);
-            int p = mphase[k];
-            Wm += w;
-#pragma unroll
-            for (int pp = 0; pp < NPH; pp++)
-                if (p == pp) Wph[pp] += w;
-#pragma unroll
-            for (int f = 0; f < NF; f++) {
-                double v = F.per_phase[f] ? F.val[f][p] : F.val[f][k];
-                if (F.avg[f] == 1) v = 1.0 / v;
-                if (F.avg[f] == 2) v = log(v);
-                BmWm[f] += v * w;
-            }
+            add(sorted[q], ip, jp, di, dj);
         }
     }
     const bool air = tag[node] == 30 || tag[node] == 31;
@@ -254,16 +299,17 @@ static void launch_p2g_nf(int nph, dim3 gr, dim3 bl, cudaStream_t st, int nnx, i
                           double dxi, double dzi, int ncx, int ncz, const mdz_ctx *ctx, const p2g_fields &F,
                           double *pp) {
     const mdz_bins &B = ctx->bins;
+    const int *qv = kx == 1 && kz == 1 ? B.qvert : nullptr;   // vertex lines in both directions
     if (pp == nullptr || nph <= 0)
         k_p2g_gather<NF, 0><<<gr, bl, 0, st>>>(nnx, nnz, X, Z, tag, kx, kz, h, dx, dz, dxi, dzi, ncx, ncz, B.start,
-                                               B.sorted, ctx->m.x, ctx->m.z, ctx->m.phase, F, 0, nullptr);
+                                               B.sorted, qv, ctx->m.x, ctx->m.z, ctx->m.phase, F, 0, nullptr);
     else if (nph <= 4)
         k_p2g_gather<NF, 4><<<gr, bl, 0, st>>>(nnx, nnz, X, Z, tag, kx, kz, h, dx, dz, dxi, dzi, ncx, ncz, B.start,
-                                               B.sorted, ctx->m.x, ctx->m.z, ctx->m.phase, F, nph, pp);
+                                               B.sorted, qv, ctx->m.x, ctx->m.z, ctx->m.phase, F, nph, pp);
     else
         k_p2g_gather<NF, MDZ_MAX_PHASES><<<gr, bl, 0, st>>>(nnx, nnz, X, Z, tag, kx, kz, h, dx, dz, dxi, dzi, ncx,
-                                                            ncz, B.start, B.sorted, ctx->m.x, ctx->m.z,
-                                                            ctx->m.phase, F, nph, pp);
+                                                            ncz, B.start, B.sorted, qv, ctx->m.x,
+                                                            ctx->m.z, ctx->m.phase, F, nph, pp);
 }
 
 // Core projection on the resident markers (device pointers everywhere).
@@ -287,12 +333,21 @@ static mdz_status p2g_core(mdz_ctx *ctx, const p2g_fields &F, int nf, double *d_
     int nph = d_phase_perc ? ctx->n_phases : 0;
     p2g_fields Fc = F;
     Fc.empty = d_phase_perc ? ctx->p2g_empty : nullptr;
+    cudaEvent_t ev;
+    mdz_prof_begin(ctx, MDZ_PROF_P2G, st, &ev);
     switch (nf) {
 #define CASE(N) case N: launch_p2g_nf<N>(nph, gr, bl, st, ns.nx, ns.nz, ns.X, ns.Z, ns.tag, kx, kz, h, g.dx, g.dz, dxi, dzi, g.ncx, g.ncz, ctx, Fc, d_phase_perc); break;
         CASE(0) CASE(1) CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8)
 #undef CASE
     }
     MDZ_LAUNCHED(ctx);
+    {   // algorithmic bytes: each marker's position, phase and per-marker
+        // fields read once; each node's fields and phase fractions written once
+        int nfm = 0;
+        for (int f = 0; f < nf; f++) nfm += F.per_phase[f] ? 0 : 1;
+        const double bytes = (double)ctx->m.n * (20.0 + 8.0 * nfm) + 8.0 * (double)nn * (nf + nph);
+        mdz_prof_end(ctx, MDZ_PROF_P2G, bytes, st, ev);
+    }
     return MDZ_OK;
 }
 

@@ -61,6 +61,7 @@ struct mdz_bins {
     int *start = nullptr;       // per cell + 1: exclusive scan of count
     int *cursor = nullptr;      // scratch for the scatter
     int *sorted = nullptr;      // marker indices grouped by cell, ascending inside a cell
+    int *qvert = nullptr;       // per sorted position: the marker's nearest vertex, ip | jp << 16
     int *scan_partials = nullptr;
 };
 

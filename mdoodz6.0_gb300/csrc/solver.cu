@@ -85,6 +85,7 @@ struct mg_hier {
     mg_level<T> L[MG_MAX_LEVELS];
 };
 
+#define MDZ_PRE_SLOTS 8
 struct mdz_solver {
     mg_hier<double> mg64;
     mg_hier<float> mg32;
@@ -98,14 +99,16 @@ struct mdz_solver {
                                  // each: cheaper at 1025x513 than the iterations a sparser check overshoots)
     int restart = 30;            // GCR basis size
     int mg_jacobian = 0;         // 1: multigrid on the Newton Jacobian's velocity block (else Picard)
+    int schur = 0;               // pressure block of Newton solves: 0 eta_n / cell volume, 1 the Jacobian's
+                                 // D11 / 2 (tangent viscosity) where positive
     int bottom_cs[2] = {1, 1};   // cluster size of the V-cycle bottom kernel ([0] FP64, [1] FP32)
     // preconditioner application captured as a CUDA graph, per precision
     // ([0] FP64, [1] FP32): one graph launch per Krylov iteration
-    // [precision (0 FP64, 1 FP32) * 2 + newton]
-    cudaGraphExec_t pre[4] = {nullptr, nullptr, nullptr, nullptr};
-    long long pre_launches[4] = {0, 0, 0, 0};
-    const double *pre_eta[4] = {nullptr, nullptr, nullptr, nullptr};
-    double pre_bytes[4] = {0, 0, 0, 0};   // algorithmic bytes of one application
+    // [precision (0 FP64, 1 FP32) * 2 + newton hierarchy + 4 * tangent Schur]
+    cudaGraphExec_t pre[MDZ_PRE_SLOTS] = {};
+    long long pre_launches[MDZ_PRE_SLOTS] = {};
+    const double *pre_eta[MDZ_PRE_SLOTS] = {};
+    double pre_bytes[MDZ_PRE_SLOTS] = {};   // algorithmic bytes of one application
 };
 
 // ---------------------------------------------------------------------------
@@ -1441,7 +1444,7 @@ extern "C" mdz_status mdz_set_solver_options(mdz_ctx *ctx, int nu1, int nu2, dou
     if (!ctx->solver) ctx->solver = new mdz_solver();
     mdz_solver *S = ctx->solver;
     MDZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    for (int q = 0; q < 4; q++)
+    for (int q = 0; q < MDZ_PRE_SLOTS; q++)
         if (S->pre[q]) { cudaGraphExecDestroy(S->pre[q]); S->pre[q] = nullptr; }
     S->nu1 = nu1; S->nu2 = nu2; S->omega = omega; S->check = check; S->mg_jacobian = mg_jacobian;
     if (S->ready && restart != S->restart) {
@@ -1458,6 +1461,14 @@ extern "C" mdz_status mdz_set_solver_options(mdz_ctx *ctx, int nu1, int nu2, dou
     return MDZ_OK;
 }
 
+extern "C" mdz_status mdz_set_schur_scaling(mdz_ctx *ctx, int mode) {
+    if (!ctx) return MDZ_ERR_ARG;
+    if (mode != 0 && mode != 1) return mdz_fail(ctx, MDZ_ERR_ARG, "Schur scaling: mode 0 or 1");
+    if (!ctx->solver) ctx->solver = new mdz_solver();
+    ctx->solver->schur = mode;   // graphs of both kinds have their own slots
+    return MDZ_OK;
+}
+
 // The grid spacing changed (PureShearALE): every level's spacing follows the
 // fine one (doubling per level, as the hierarchy was built) and the captured
 // preconditioner graphs, which hold the old spacings as kernel arguments, are
@@ -1466,7 +1477,7 @@ mdz_status mdz_solver_regrid(mdz_ctx *ctx) {
     mdz_solver *S = ctx->solver;
     if (!S) return MDZ_OK;
     MDZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    for (int q = 0; q < 4; q++)
+    for (int q = 0; q < MDZ_PRE_SLOTS; q++)
         if (S->pre[q]) { cudaGraphExecDestroy(S->pre[q]); S->pre[q] = nullptr; S->pre_eta[q] = nullptr; }
     S->mg64.built = false;   // no solve may keep operators of the old spacing
     S->mg32.built = false;
@@ -1480,7 +1491,7 @@ mdz_status mdz_solver_regrid(mdz_ctx *ctx) {
 void mdz_solver_free(mdz_ctx *ctx) {
     if (!ctx->solver) return;
     mdz_solver *S = ctx->solver;
-    for (int q = 0; q < 4; q++)
+    for (int q = 0; q < MDZ_PRE_SLOTS; q++)
         if (S->pre[q]) cudaGraphExecDestroy(S->pre[q]);
     free_hierarchy(S->mg64);
     free_hierarchy(S->mg32);
@@ -1565,11 +1576,29 @@ static mdz_status mg_setup(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n, con
 
 static inline dim3 box_grid(int Nx, int Nz) { return dim3((Nx + 1 + 31) / 32, (Nz + 1 + 7) / 8); }
 
+// Whether vcycle() smooths level l with its own sweeps (not the dense
+// coarsest solve, the coarse CG, nor the one-launch bottom kernel).
+template <typename T>
+static bool vcycle_smoothed(const mdz_ctx *ctx, const mg_hier<T> &H, int l) {
+    const mg_level<T> &L = H.L[l];
+    if (l == H.nlev - 1) return false;
+    const bool viscous = l == 0 && !H.newton;
+    const mg_level<T> &Cd = H.L[H.nlev - 1];
+    const int cs = ctx->solver->bottom_cs[sizeof(T) == 8 ? 0 : 1];
+    return !(!viscous && Cd.ndense && H.nlev - l <= MG_BOTTOM_MAX &&
+             (long long)(L.Nx + 1) * (L.Nz + 1) <= mg_bottom_points(cs));
+}
+
 // One V-cycle: H.L[l].x <- approx A^-1 H.L[l].f.  Level 0 smooths with the
 // re-discretised stencil (viscosities read directly), coarser levels with the
-// Galerkin stencils.
+// Galerkin stencils.  x0_done: the first sweep from x = 0 (x = omega D^-1 f)
+// was already written into L.xu / L.xv with the right-hand side
+// (k_precond_rhs); out_u / out_v: where the last post-smoothing sweep writes
+// (the caller's vector), else the level's own buffers.  Both only for a level
+// that vcycle_smoothed() accepts.
 template <typename T>
-static mdz_status vcycle(mdz_ctx *ctx, mg_hier<T> &H, int l, int nu1, int nu2, T omega, cudaStream_t st) {
+static mdz_status vcycle(mdz_ctx *ctx, mg_hier<T> &H, int l, int nu1, int nu2, T omega, cudaStream_t st,
+                         bool x0_done = false, T *out_u = nullptr, T *out_v = nullptr) {
     mg_level<T> &L = H.L[l];
     stokes_geom G = L.geom();
     stokes_coefs<T> D = L.coefs();
@@ -1628,8 +1657,10 @@ static mdz_status vcycle(mdz_ctx *ctx, mg_hier<T> &H, int l, int nu1, int nu2, T
         else k_st_smooth<T><<<rows_grid, 128, 0, st>>>(G, L.su, L.sv, xu, xv, L.fu, L.fv, L.idu, L.idv, omega, ou, ov);
     };
     // pre-smoothing from x = 0
-    smooth(nullptr, nullptr, L.xu, L.xv);
-    MDZ_LAUNCHED(ctx);
+    if (!x0_done) {
+        smooth(nullptr, nullptr, L.xu, L.xv);
+        MDZ_LAUNCHED(ctx);
+    }
     for (int s = 1; s < nu1; s++) {
         smooth(L.xu, L.xv, L.yu, L.yv);
         MDZ_LAUNCHED(ctx);
@@ -1646,6 +1677,11 @@ static mdz_status vcycle(mdz_ctx *ctx, mg_hier<T> &H, int l, int nu1, int nu2, T
     k_mg_prolong_add<T><<<gr, bl, 0, st>>>(G, C.geom(), C.xu, C.xv, L.xu, L.xv);
     MDZ_LAUNCHED(ctx);
     for (int q = 0; q < nu2; q++) {
+        if (q == nu2 - 1 && out_u) {   // the last sweep straight into the caller's vector
+            smooth(L.xu, L.xv, out_u, out_v);
+            MDZ_LAUNCHED(ctx);
+            break;
+        }
         smooth(L.xu, L.xv, L.yu, L.yv);
         MDZ_LAUNCHED(ctx);
         std::swap(L.xu, L.yu); std::swap(L.xv, L.yv);
@@ -1683,46 +1719,72 @@ __global__ void k_psub(int np, const signed char *__restrict__ tp, const double 
 // the sum and count of zp over the pressure equations (as k_psum) for the
 // zero-mean projection applied by k_copy_out
 template <typename T>
-__global__ void __launch_bounds__(256) k_precond_p(stokes_geom G, const T *__restrict__ D11, const T *__restrict__ rp,
-                                                   T *__restrict__ zp, double *part, unsigned int *counter,
-                                                   double *psum) {
+__global__ void __launch_bounds__(256) k_precond_p(stokes_geom G, const T *__restrict__ D11, const T *__restrict__ Dt,
+                                                   const T *__restrict__ rp, T *__restrict__ zp, double *part,
+                                                   unsigned int *counter, double *psum) {
     const int np = G.ncx * G.ncz;
     const T c = T(0.5) * gc<T>(G, GC_IXZ);
     T acc = 0;
     int cnt = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
         T v = 0;
-        if (G.BCp[i] == -1) { v = c * D11[i] * rp[i]; acc += v; cnt++; }
+        if (G.BCp[i] == -1) {
+            T d = D11[i];
+            if (Dt) {   // the Jacobian's tangent D11 where it is positive
+                const T t = Dt[i];
+                if (t > T(0)) d = t;
+            }
+            v = c * d * rp[i];
+            acc += v;
+            cnt++;
+        }
         zp[i] = v;
     }
     const T v[2] = {acc, (T)cnt};
     mdz_grid_sum<2, T>(v, part, counter, psum);
 }
 
-// f = r_vel - B zp  on the fine MG level (B: celvol-scaled pressure gradient)
+// f = r_vel - B zp  on the fine MG level (B: celvol-scaled pressure gradient);
+// with xu non-null also the V-cycle's first sweep from x = 0, x = omega D^-1 f
+// (the smoother's own arithmetic for a zero x), in the same pass
 template <typename T>
 __global__ void k_precond_rhs(stokes_geom G, const T *__restrict__ ru, const T *__restrict__ rv,
-                              const T *__restrict__ zp, T *__restrict__ fu, T *__restrict__ fv) {
+                              const T *__restrict__ zp, T *__restrict__ fu, T *__restrict__ fv,
+                              const T *__restrict__ idu, const T *__restrict__ idv, T omega, T *__restrict__ xu,
+                              T *__restrict__ xv) {
     int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
     const int Nx = G.Nx, Nz = G.Nz, ncx = G.ncx;
     if (i < Nx && j <= Nz) {
         int c = i + j * Nx;
-        T r = 0;
+        T r = 0, x0 = 0;
         if (G.BCu[c] == -1) {
             int c2 = i - 1 + (j - 1) * ncx;
             r = ru[c] - gc<T>(G, GC_DZ) * (zp[c2 + 1] - zp[c2]);
+            if (xu) x0 = T(0) + omega * idu[c] * (r - T(0));
         }
         fu[c] = r;
+        if (xu) xu[c] = x0;
     }
     if (i <= Nx && j < Nz) {
         int c = i + j * (Nx + 1);
-        T r = 0;
+        T r = 0, x0 = 0;
         if (G.BCv[c] == -1) {
             int c2 = i - 1 + (j - 1) * ncx;
             r = rv[c] - gc<T>(G, GC_DX) * (zp[c2 + ncx] - zp[c2]);
+            if (xv) x0 = T(0) + omega * idv[c] * (r - T(0));
         }
         fv[c] = r;
+        if (xv) xv[c] = x0;
     }
+}
+
+// z pressure <- zero mean over the pressure equations (the mean cancels in
+// the gradient of the right-hand side, so it is removed only here)
+template <typename T>
+__global__ void k_pmean_out(int np, const signed char *__restrict__ tp, const double *__restrict__ psum,
+                            T *__restrict__ zp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < np && tp[i] == -1 && psum[1] > 0) zp[i] -= (T)psum[0] / (T)psum[1];
 }
 
 // z velocity <- the V-cycle's result; z pressure <- zero mean over the
@@ -1739,8 +1801,8 @@ __global__ void k_copy_out(size_t nu, size_t nv, int np, const T *__restrict__ x
 }
 
 template <typename T>
-static mdz_status precondition(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n, const T *r, T *z, size_t nu,
-                               size_t nv, cudaStream_t st) {
+static mdz_status precondition(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n, const T *Dt, const T *r, T *z,
+                               size_t nu, size_t nv, cudaStream_t st) {
     mg_level<T> &F = H.L[0];
     stokes_geom G = F.geom();
     const int np = F.ncx * F.ncz;
@@ -1749,19 +1811,29 @@ static mdz_status precondition(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n,
     {
         int blocks = mdz_blocks(np, 256);
         if (blocks > 152 * 4) blocks = 152 * 4;
-        k_precond_p<T><<<blocks, 256, 0, st>>>(G, F.D11, r + nu + nv, z + nu + nv, ctx->red_part + MDZ_RP_PRECP,
+        k_precond_p<T><<<blocks, 256, 0, st>>>(G, F.D11, Dt, r + nu + nv, z + nu + nv, ctx->red_part + MDZ_RP_PRECP,
                                                ctx->red_cnt + MDZ_RC_PRECP, H.pmean);
         MDZ_LAUNCHED(ctx);
     }
-    k_precond_rhs<T><<<box_grid(F.Nx, F.Nz), dim3(32, 8), 0, st>>>(G, r, r + nu, z + nu + nv, F.fu, F.fv);
-    MDZ_LAUNCHED(ctx);
     mdz_solver *S = ctx->solver;
-    mdz_status s = vcycle<T>(ctx, H, 0, S->nu1, S->nu2, (T)S->omega, st);
+    // a level-0 V-cycle of its own sweeps takes its first sweep from the
+    // right-hand side kernel and writes its last sweep into z
+    const bool fused = vcycle_smoothed<T>(ctx, H, 0) && S->nu2 > 0;
+    k_precond_rhs<T><<<box_grid(F.Nx, F.Nz), dim3(32, 8), 0, st>>>(G, r, r + nu, z + nu + nv, F.fu, F.fv, F.idu,
+                                                                  F.idv, (T)S->omega, fused ? F.xu : nullptr,
+                                                                  fused ? F.xv : nullptr);
+    MDZ_LAUNCHED(ctx);
+    mdz_status s = vcycle<T>(ctx, H, 0, S->nu1, S->nu2, (T)S->omega, st, fused, fused ? z : nullptr,
+                             fused ? z + nu : nullptr);
     if (s != MDZ_OK) return s;
-    size_t n = nu > nv ? nu : nv;
-    if ((size_t)np > n) n = np;
-    k_copy_out<T><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(nu, nv, np, F.xu, F.xv, G.BCp, H.pmean, z, z + nu,
-                                                         z + nu + nv);
+    if (fused) {
+        k_pmean_out<T><<<mdz_blocks(np), MDZ_THREADS, 0, st>>>(np, G.BCp, H.pmean, z + nu + nv);
+    } else {
+        size_t n = nu > nv ? nu : nv;
+        if ((size_t)np > n) n = np;
+        k_copy_out<T><<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(nu, nv, np, F.xu, F.xv, G.BCp, H.pmean, z, z + nu,
+                                                             z + nu + nv);
+    }
     MDZ_LAUNCHED(ctx);
     return MDZ_OK;
 }
@@ -2030,10 +2102,11 @@ static mdz_status dots_launch(mdz_ctx *ctx, gcr_space<T> &S, int q0, int nq, con
 // (its buffers, coefficients and the Krylov vectors r, z never move; the
 // coefficients' values are refreshed by mg_setup outside the graph).
 template <typename T>
-static mdz_status precond_graph(mdz_ctx *ctx, gcr_space<T> &S, mg_hier<T> &H, const double *eta_n, cudaStream_t st,
-                                cudaGraphExec_t *out, long long *launches) {
+static mdz_status precond_graph(mdz_ctx *ctx, gcr_space<T> &S, mg_hier<T> &H, const double *eta_n, const T *Dt,
+                                cudaStream_t st, cudaGraphExec_t *out, long long *launches, int *slot_out) {
     mdz_solver *SV = ctx->solver;
-    const int slot = (sizeof(T) == 8 ? 0 : 2) + (H.newton ? 1 : 0);
+    const int slot = (sizeof(T) == 8 ? 0 : 2) + (H.newton ? 1 : 0) + (Dt ? 4 : 0);
+    *slot_out = slot;
     if (SV->pre[slot] && SV->pre_eta[slot] == eta_n) {
         *out = SV->pre[slot];
         *launches = SV->pre_launches[slot];
@@ -2042,7 +2115,7 @@ static mdz_status precond_graph(mdz_ctx *ctx, gcr_space<T> &S, mg_hier<T> &H, co
     if (SV->pre[slot]) { cudaGraphExecDestroy(SV->pre[slot]); SV->pre[slot] = nullptr; }
     const long long l0 = ctx->launches;
     MDZ_CUDA(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    mdz_status s = precondition<T>(ctx, H, eta_n, S.r, S.z, S.nu, S.nv, st);
+    mdz_status s = precondition<T>(ctx, H, eta_n, Dt, S.r, S.z, S.nu, S.nv, st);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &g);
     if (s != MDZ_OK) { if (g) cudaGraphDestroy(g); return s; }
@@ -2064,6 +2137,7 @@ static mdz_status precond_graph(mdz_ctx *ctx, gcr_space<T> &S, mg_hier<T> &H, co
             b += 4.0 * sizeof(T) * nuv;
         }
         b += 3.0 * sizeof(T) * (double)S.n;
+        if (Dt) b += sizeof(T) * (double)S.np;
         SV->pre_bytes[slot] = b;
     }
     ctx->launches = l0;
@@ -2104,7 +2178,9 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
     mdz_status s;
     cudaGraphExec_t pre = nullptr;
     long long pre_launches = 0;
-    if ((s = precond_graph<P>(ctx, SP, H, eta_n, st, &pre, &pre_launches)) != MDZ_OK) return s;
+    int pslot = 0;
+    const P *Dt = newton && SV->schur == 1 ? K.D11 : nullptr;   // tangent Schur scaling (Newton solves)
+    if ((s = precond_graph<P>(ctx, SP, H, eta_n, Dt, st, &pre, &pre_launches, &pslot)) != MDZ_OK) return s;
     // (r, r) via the pointer-table slot m+1 against r itself
     if ((s = dots_launch<T>(ctx, S, S.m + 1, 1, S.r, dots, st)) != MDZ_OK) return s;
     k_set_scalar<<<1, 32, 0, st>>>(sc + 3, dots);
@@ -2135,7 +2211,7 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
         mdz_prof_begin(ctx, MDZ_PROF_MG_SMOOTH, st, &ev);
         MDZ_CUDA(ctx, cudaGraphLaunch(pre, st));
         ctx->launches += pre_launches;
-        mdz_prof_end(ctx, MDZ_PROF_MG_SMOOTH, SV->pre_bytes[(sizeof(P) == 8 ? 0 : 2) + (H.newton ? 1 : 0)], st, ev);
+        mdz_prof_end(ctx, MDZ_PROF_MG_SMOOTH, SV->pre_bytes[pslot], st, ev);
         mdz_prof_begin(ctx, MDZ_PROF_STOKES_APPLY, st, &ev);
         stokes_apply_launch<P>(G, K, stokes_cvec<P>{SP.z, SP.z + nu, SP.z + nu + nv},
                                stokes_vec<P>{SP.w, SP.w + nu, SP.w + nu + nv}, nullptr, newton, st);

@@ -10,17 +10,39 @@
 // ---------------------------------------------------------------------------
 // y = K x (linear) or F = (K x - b) (residual), each row times the cell volume.
 // Non-equation entries of y are written 0 so Krylov vectors stay masked.
+// A 32 x 8 block covers a 32 x 8 tile of the index box; it first computes the
+// strain rates of the input once per centroid and vertex the tile's rows read
+// (34 x 10 of each, with a two-cell halo) into shared memory, then each
+// thread evaluates its rows from them.  A Newton row reads six centroid and
+// six vertex rates, each shared by about ten rows: computed per row they made
+// the FP64 apply FP64-pipe bound (FP64 runs at a small fraction of the FP32
+// rate on this part) and the FP32 apply load-bound.
 template <typename T, bool NEWTON, bool RES>
 __global__ void __launch_bounds__(256) k_stokes_apply(stokes_geom G, stokes_coefs<T> D, stokes_cvec<T> x,
                                                       stokes_vec<T> y, stokes_cvec<T> b, T celvol) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int Nx = G.Nx, Nz = G.Nz;
+    __shared__ T s_ex[RT_H][RT_W], s_ez[RT_H][RT_W], s_g[RT_H][RT_W];
+    const int Nx = G.Nx, Nz = G.Nz, ncx = G.ncx, ncz = G.ncz;
+    const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 8;
+    const rates_tile<T> rt{s_ex, s_ez, s_g, i0 - 2, j0 - 2, i0 - 1, j0 - 1};
+    {
+        const rates_direct<T> rd = direct_rates<T>(G, x);
+        for (int t = threadIdx.x + threadIdx.y * 32; t < RT_W * RT_H; t += 256) {
+            const int a = t % RT_W, h = t / RT_W;
+            const int kc = rt.c0x + a, lc = rt.c0z + h, kv = rt.v0x + a, lv = rt.v0z + h;
+            pair2<T> e{T(0), T(0)};
+            if (kc >= 0 && kc < ncx && lc >= 0 && lc < ncz) e = rd.exx(kc, lc);
+            s_ex[h][a] = e.x;
+            s_ez[h][a] = e.y;
+            s_g[h][a] = (kv >= 0 && kv < Nx && lv >= 0 && lv < Nz) ? rd.gxz(kv, lv) : T(0);
+        }
+    }
+    __syncthreads();
+    const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
     if (i < Nx && j <= Nz) {            // Vx node (i, j)
         int c = i + j * Nx;
         T r = 0;
         if (G.BCu[c] == -1) {
-            r = xrow<T, NEWTON>(G, D, x, i, j);
+            r = xrow<T, NEWTON>(G, D, x, i, j, rt);
             if (RES) r -= b.u[c];
             r *= celvol;
         }
@@ -30,7 +52,7 @@ __global__ void __launch_bounds__(256) k_stokes_apply(stokes_geom G, stokes_coef
         int c = i + j * (Nx + 1);
         T r = 0;
         if (G.BCv[c] == -1) {
-            r = zrow<T, NEWTON>(G, D, x, i, j);
+            r = zrow<T, NEWTON>(G, D, x, i, j, rt);
             if (RES) r -= b.v[c];
             r *= celvol;
         }

@@ -76,10 +76,51 @@ __device__ __forceinline__ T wrecip(T w) {
     return w > T(3.5) ? T(0.25) : (w > T(2.5) ? T(1.0 / 3.0) : (w > T(1.5) ? T(0.5) : w));
 }
 
+// Strain rates of the input the rows are built from: deviatoric normal
+// rates at centroid (kc, lc) and the engineering shear rate at vertex
+// (kv, lv).  rates_direct computes them from the velocities where a row asks;
+// rates_tile (k_stokes_apply) reads them from a shared-memory tile where the
+// block computed each one once (a Newton row reads six of each, and every
+// centroid / vertex is shared by about ten rows).
+template <typename T>
+struct rates_direct {
+    const T *u, *v;
+    int nx, nxvz;
+    T idx, idz;
+    __device__ __forceinline__ pair2<T> exx(int kc, int lc) const {
+        const int cu = kc + (lc + 1) * nx, cv = kc + 1 + lc * nxvz;
+        const T dudx = (u[cu + 1] - u[cu]) * idx, dvdz = (v[cv + nxvz] - v[cv]) * idz;
+        const T div = dudx + dvdz;
+        return pair2<T>{dudx - div * T(1.0 / 3.0), dvdz - div * T(1.0 / 3.0)};
+    }
+    __device__ __forceinline__ T gxz(int kv, int lv) const {
+        const int cu = kv + lv * nx, cv = kv + lv * nxvz;
+        return (u[cu + nx] - u[cu]) * idz + (v[cv + 1] - v[cv]) * idx;
+    }
+};
+
+// centroids kc in [c0x, c0x + RT_W), lc in [c0z, c0z + RT_H); vertices
+// kv in [v0x, v0x + RT_W), lv in [v0z, v0z + RT_H)
+constexpr int RT_W = 34, RT_H = 10;
+template <typename T>
+struct rates_tile {
+    const T (*ex)[RT_W], (*ez)[RT_W], (*g)[RT_W];
+    int c0x, c0z, v0x, v0z;
+    __device__ __forceinline__ pair2<T> exx(int kc, int lc) const {
+        return pair2<T>{ex[lc - c0z][kc - c0x], ez[lc - c0z][kc - c0x]};
+    }
+    __device__ __forceinline__ T gxz(int kv, int lv) const { return g[lv - v0z][kv - v0x]; }
+};
+
+template <typename T>
+__device__ __forceinline__ rates_direct<T> direct_rates(const stokes_geom &G, const stokes_cvec<T> &x) {
+    return rates_direct<T>{x.u, x.v, G.Nx, G.Nx + 1, gc<T>(G, GC_IDX), gc<T>(G, GC_IDZ)};
+}
+
 // x-momentum row at Vx node (k, l), k in 1..Nx-2, l in 1..Nz-1.
-template <typename T, bool NEWTON>
+template <typename T, bool NEWTON, typename RS>
 __device__ __forceinline__ T xrow(const stokes_geom &G, const stokes_coefs<T> &D, const stokes_cvec<T> &x, int k,
-                                  int l) {
+                                  int l, const RS &rs) {
     const int nx = G.Nx, ncx = G.ncx, nxvz = nx + 1;
     const int c1 = k + l * nx, c2 = k - 1 + (l - 1) * ncx, c3 = k + l * nxvz;
     const T idx = gc<T>(G, GC_IDX), idz = gc<T>(G, GC_IDZ);
@@ -88,17 +129,10 @@ __device__ __forceinline__ T xrow(const stokes_geom &G, const stokes_coefs<T> &D
     const T inS = (G.BCg[ixyS] != 30 && G.BCu[c1 - nx] != 13) ? T(1) : T(0);
     const T inN = (G.BCg[ixyN] != 30 && G.BCu[c1 + nx] != 13) ? T(1) : T(0);
     // velocity gradients on the row's control volume
-    const T *u = x.u, *v = x.v, *p = x.p;
-    auto exx_c = [&](int kc, int lc) {   // deviatoric normal rates at centroid (kc, lc)
-        int cu = kc + (lc + 1) * nx, cv = kc + 1 + lc * nxvz;
-        T dudx = (u[cu + 1] - u[cu]) * idx, dvdz = (v[cv + nxvz] - v[cv]) * idz;
-        T div = dudx + dvdz;
-        return pair2<T>{dudx - div * T(1.0 / 3.0), dvdz - div * T(1.0 / 3.0)};
-    };
-    auto gxz_v = [&](int kv, int lv) {   // engineering shear rate at vertex (kv, lv)
-        int cu = kv + lv * nx, cv = kv + lv * nxvz;
-        return (u[cu + nx] - u[cu]) * idz + (v[cv + 1] - v[cv]) * idx;
-    };
+    const T *p = x.p;
+    (void)nxvz;
+    auto exx_c = [&](int kc, int lc) { return rs.exx(kc, lc); };
+    auto gxz_v = [&](int kv, int lv) { return rs.gxz(kv, lv); };
     pair2<T> eW = exx_c(k - 1, l - 1), eE = exx_c(k, l - 1);
     T gN = gxz_v(k, l), gS = gxz_v(k, l - 1);
     T TxxE, TxxW, TxzN, TxzS;
@@ -163,9 +197,9 @@ __device__ __forceinline__ T xrow(const stokes_geom &G, const stokes_coefs<T> &D
 }
 
 // z-momentum row at Vz node (k, l), k in 1..Nx-1, l in 1..Nz-2.
-template <typename T, bool NEWTON>
+template <typename T, bool NEWTON, typename RS>
 __device__ __forceinline__ T zrow(const stokes_geom &G, const stokes_coefs<T> &D, const stokes_cvec<T> &x, int k,
-                                  int l) {
+                                  int l, const RS &rs) {
     const int nx = G.Nx, ncx = G.ncx, nxvz = nx + 1;
     const int c3 = k + l * nxvz, c1 = k + l * nx, c2 = k - 1 + (l - 1) * ncx;
     const T idx = gc<T>(G, GC_IDX), idz = gc<T>(G, GC_IDZ);
@@ -178,17 +212,9 @@ __device__ __forceinline__ T zrow(const stokes_geom &G, const stokes_coefs<T> &D
     if (G.BCp[iPrN] == -1) inN = 1;
     const T inW = (G.BCg[ixyW] != 30 && G.BCv[c3 - 1] != 13) ? T(1) : T(0);
     const T inE = (G.BCg[ixyE] != 30 && G.BCv[c3 + 1] != 13) ? T(1) : T(0);
-    const T *u = x.u, *v = x.v, *p = x.p;
-    auto exx_c = [&](int kc, int lc) {
-        int cu = kc + (lc + 1) * nx, cv = kc + 1 + lc * nxvz;
-        T dudx = (u[cu + 1] - u[cu]) * idx, dvdz = (v[cv + nxvz] - v[cv]) * idz;
-        T div = dudx + dvdz;
-        return pair2<T>{dudx - div * T(1.0 / 3.0), dvdz - div * T(1.0 / 3.0)};
-    };
-    auto gxz_v = [&](int kv, int lv) {
-        int cu = kv + lv * nx, cv = kv + lv * nxvz;
-        return (u[cu + nx] - u[cu]) * idz + (v[cv + 1] - v[cv]) * idx;
-    };
+    const T *v = x.v, *p = x.p;
+    auto exx_c = [&](int kc, int lc) { return rs.exx(kc, lc); };
+    auto gxz_v = [&](int kv, int lv) { return rs.gxz(kv, lv); };
     pair2<T> eS = exx_c(k - 1, l - 1), eN = exx_c(k - 1, l);
     T gW = gxz_v(k - 1, l), gE = gxz_v(k, l);
     T TzzN, TzzS, TxzE, TxzW, ndrop = 0;
@@ -271,6 +297,17 @@ __device__ __forceinline__ T zrow(const stokes_geom &G, const stokes_coefs<T> &D
     }
     T grad = (p && G.BCp[iPrS] != 30 && G.BCp[iPrN] != 30) ? (p[iPrN] - p[iPrS]) * idz : T(0);
     return -(inN * TzzN - inS * TzzS) * idz - (inE * TxzE - inW * TxzW) * idx + grad - ndrop;
+}
+
+template <typename T, bool NEWTON>
+__device__ __forceinline__ T xrow(const stokes_geom &G, const stokes_coefs<T> &D, const stokes_cvec<T> &x, int k,
+                                  int l) {
+    return xrow<T, NEWTON>(G, D, x, k, l, direct_rates<T>(G, x));
+}
+template <typename T, bool NEWTON>
+__device__ __forceinline__ T zrow(const stokes_geom &G, const stokes_coefs<T> &D, const stokes_cvec<T> &x, int k,
+                                  int l) {
+    return zrow<T, NEWTON>(G, D, x, k, l, direct_rates<T>(G, x));
 }
 
 // continuity row at centroid (k, l)

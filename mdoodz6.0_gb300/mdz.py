@@ -531,6 +531,10 @@ class Context:
         self._check(self.L.mdz_set_solver_options(self.h, C.c_int(nu1), C.c_int(nu2), C.c_double(omega),
                                                   C.c_int(restart), C.c_int(check), C.c_int(mg_jacobian)))
 
+    def set_schur_scaling(self, mode):
+        """Pressure block of Newton solves: 0 eta_n / cell volume, 1 the
+        Jacobian's tangent D11 / 2 where positive."""
+        self._check(self.L.mdz_set_schur_scaling(self.h, C.c_int(mode)))
 
     def mg_stencils(self, precision, level):
         """(levels, Nx, Nz, su[31, Nx*(Nz+1)], sv[31, (Nx+1)*Nz]) of one multigrid level."""
