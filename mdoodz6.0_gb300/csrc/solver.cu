@@ -70,6 +70,8 @@ struct gcr_space {
     int m = 0;
     T *Z = nullptr, *W = nullptr;       // m basis vectors each (u, v, p contiguous)
     T *x = nullptr, *r = nullptr, *z = nullptr, *w = nullptr, *t = nullptr;
+    T *pin = nullptr;                   // the preconditioner's input (graph-captured pointer)
+    double *tri = nullptr;              // Gram-Schmidt triangle U (column q at q * GCR_MAX_M), then gamma
     const T **dA0 = nullptr, **dA1 = nullptr, **dA2 = nullptr;   // dot-product pointer tables (k_dots uses dA0)
     double *dots = nullptr;             // device scalars
     // FP32 copies of the operator (only used for T = float)
@@ -1341,12 +1343,13 @@ static mdz_status alloc_gcr(mdz_ctx *ctx, gcr_space<T> &S, int m) {
     S.m = m;
     cudaError_t e = alloc0(&S.Z, S.n * m);
     if (e == cudaSuccess) e = alloc0(&S.W, S.n * m);
-    T **v[] = {&S.x, &S.r, &S.z, &S.w, &S.t};
+    T **v[] = {&S.x, &S.r, &S.z, &S.w, &S.t, &S.pin};
     for (T **b : v) if (e == cudaSuccess) e = alloc0(b, S.n);
     if (e == cudaSuccess) e = cudaMalloc((void **)&S.dA0, sizeof(T *) * (GCR_MAX_M + 4));
     if (e == cudaSuccess) e = cudaMalloc((void **)&S.dA1, sizeof(T *) * (GCR_MAX_M + 4));
     if (e == cudaSuccess) e = cudaMalloc((void **)&S.dA2, sizeof(T *) * (GCR_MAX_M + 4));
     if (e == cudaSuccess) e = alloc0(&S.dots, 8 * (GCR_MAX_M + 8));   // see the layout in gcr_solve
+    if (e == cudaSuccess) e = alloc0(&S.tri, (size_t)GCR_MAX_M * GCR_MAX_M + GCR_MAX_M);
     if (e != cudaSuccess) return mdz_cuda_check(ctx, e, "GCR allocation");
     // pointer tables: rows 0..m-1 = W_i, row m = w, row m+1 = r
     std::vector<const T *> a0(m + 2), a1(m + 2), a2(m + 2);
@@ -1368,7 +1371,7 @@ static mdz_status alloc_gcr(mdz_ctx *ctx, gcr_space<T> &S, int m) {
 
 template <typename T>
 static void free_gcr(gcr_space<T> &S) {
-    void *p[] = {S.Z, S.W, S.x, S.r, S.z, S.w, S.t, S.dA0, S.dA1, S.dA2, S.dots};
+    void *p[] = {S.Z, S.W, S.x, S.r, S.z, S.w, S.t, S.pin, S.tri, S.dA0, S.dA1, S.dA2, S.dots};
     for (void *q : p) if (q) cudaFree(q);
     for (int q = 0; q < 12; q++) if (S.Dc[q]) cudaFree(S.Dc[q]);
 }
@@ -1850,37 +1853,52 @@ static mdz_status precondition(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n,
 // whose coefficients the finish applies; sc[0] = 1/||w||, sc[1] = alpha,
 // sc[2] = ||w||^2, sc[3] = running ||r||^2 (so the host reads it only every
 // few iterations).
-__device__ void gcr_scalars(int k, const double *dots, double *sc) {
-    double nrm2 = dots[k], wr = dots[k + 1];
-    for (int q = 0; q < k; q++) nrm2 -= dots[q] * dots[q];
+__device__ void gcr_scalars(int k, const double *d, double *sc, double *tri, bool second) {
+    // column k of U: the pass's Gram-Schmidt coefficients (added to the first
+    // pass's after a second pass) and the new direction's norm
+    double *U = tri + (size_t)k * GCR_MAX_M;
+    double nrm2 = d[k], wr = d[k + 1];
+    for (int q = 0; q < k; q++) {
+        nrm2 -= d[q] * d[q];
+        wr -= d[q] * sc[8 + q];   // (w - sum beta_q W_q, r0) = (w, r0) - sum beta_q alpha_q
+        U[q] = second ? U[q] + d[q] : d[q];
+    }
     double nrm = sqrt(nrm2 > 0 ? nrm2 : 0.0);
-    double alpha = nrm > 0 ? wr / nrm : 0.0;   // alpha = (r, w_hat); r is orthogonal to W_q, q < k
+    double alpha = nrm > 0 ? wr / nrm : 0.0;   // alpha_k = (W_k, r0) = (W_k, r_k): W orthonormal
+    U[k] = nrm;
     sc[0] = nrm > 0 ? 1.0 / nrm : 0.0;
     sc[1] = alpha;
     sc[2] = nrm2;
-    sc[3] -= alpha * alpha;
-    sc[8 + k] = alpha;   // x = sum alpha_q Z_q is formed once per basis (k_gcr_xupdate)
+    sc[3] -= alpha * alpha;   // ||r_k||^2 = ||r_k-1||^2 - alpha_k^2
+    sc[8 + k] = alpha;
 }
 
+// gamma = U^-1 alpha (back substitution, one thread): x = x0 + Z gamma with
+// the raw preconditioned vectors Z, whose orthogonalised combinations
+// Z U^-1 are the directions whose images are the orthonormal W
+__global__ void k_gcr_gamma(int k, const double *__restrict__ sc, double *__restrict__ tri) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double *g = tri + (size_t)GCR_MAX_M * GCR_MAX_M;
+    for (int i = k - 1; i >= 0; i--) {
+        double v = sc[8 + i];
+        for (int j = i + 1; j < k; j++) v -= tri[(size_t)j * GCR_MAX_M + i] * g[j];
+        const double dgl = tri[(size_t)i * GCR_MAX_M + i];
+        g[i] = dgl != 0.0 ? v / dgl : 0.0;
+    }
+}
 
-
-// first-pass correction z -= sum beta_q Z_q, w -= sum beta_q W_q, only when
-// sc[5] asks for a second pass (grid-stride, so a skipped launch is short)
+// first-pass correction w -= sum beta_q W_q, only when sc[5] asks for a
+// second pass (grid-stride, so a skipped launch is short)
 template <typename P>
-__global__ void k_gcr_orth_if(size_t n, int k, const P *__restrict__ Z, const P *__restrict__ W,
-                              const double *__restrict__ beta, const double *__restrict__ sc, P *__restrict__ z,
-                              P *__restrict__ w) {
+__global__ void k_gcr_orth_if(size_t n, int k, const P *__restrict__ W, const double *__restrict__ beta,
+                              const double *__restrict__ sc, P *__restrict__ w) {
     if (sc[5] == 0.0) return;
     __shared__ P bsh[GCR_MAX_M];
     for (int q = threadIdx.x; q < k; q += blockDim.x) bsh[q] = (P)beta[q];
     __syncthreads();
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        P zs = z[i], ws = w[i];
-        for (int q = 0; q < k; q++) {
-            zs -= bsh[q] * Z[q * n + i];
-            ws -= bsh[q] * W[q * n + i];
-        }
-        z[i] = zs;
+        P ws = w[i];
+        for (int q = 0; q < k; q++) ws -= bsh[q] * W[q * n + i];
         w[i] = ws;
     }
 }
@@ -1889,17 +1907,19 @@ __global__ void k_set_scalar(double *dst, const double *src) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *dst = *src;
 }
 
-// Basis Z, W and the new pair z, w in precision P; r in precision T.  With
-// P = float the basis arithmetic is FP32 (FP64 throughput is a small fraction
-// of FP32 on this part); r is updated in FP64 and, in the FP32 form, its FP32
-// copy for the next preconditioner application is written in the same pass
-// (rp; null otherwise).  The iterate is not touched here: x = sum alpha_q Z_q
-// is formed once per basis by k_gcr_xupdate.
-template <typename P, typename T>
-__global__ void k_gcr_finish(size_t n, int k, P *__restrict__ Z, P *__restrict__ W, const double *__restrict__ dots1,
+// W_k = (w - sum beta_q W_q) / ||.||, Z_k = z (the raw preconditioned
+// vector) and the preconditioner's next input W_k, in precision P.  The
+// residual is not touched per iteration: alpha_k = (W_k, r0) and the
+// running norm are scalars (gcr_scalars), and r = r0 - sum alpha_q W_q is
+// formed once per basis (k_gcr_rupdate), as is x (k_gcr_xupdate).  Per
+// iteration this reads the basis W twice (the sums and here) and nothing of
+// Z: about 2k + 7 vectors against 3k + 11 for the form that orthogonalised
+// z and updated r every iteration.
+template <typename P>
+__global__ void k_gcr_finish(size_t n, int k, P *__restrict__ W, P *__restrict__ Z, const double *__restrict__ dots1,
                              const double *__restrict__ dots2, const double *__restrict__ sc,
-                             const P *__restrict__ z, const P *__restrict__ w, T *__restrict__ r,
-                             P *__restrict__ rp, double *__restrict__ next1, double *__restrict__ next2) {
+                             const P *__restrict__ z, const P *__restrict__ w, P *__restrict__ pin,
+                             double *__restrict__ next1, double *__restrict__ next2) {
     // the next iteration accumulates into the other parity's buffers, which
     // no kernel of this iteration reads: clear them here instead of by memsets
     if (blockIdx.x == 0 && next1)
@@ -1910,29 +1930,49 @@ __global__ void k_gcr_finish(size_t n, int k, P *__restrict__ Z, P *__restrict__
     __syncthreads();
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    P zs = z[i], ws = w[i];
-    for (int q = 0; q < k; q++) {
-        const P b = bsh[q];
-        zs -= b * Z[q * n + i];
-        ws -= b * W[q * n + i];
-    }
-    const P inv = (P)sc[0];
-    zs *= inv;
-    ws *= inv;
-    Z[(size_t)k * n + i] = zs;
+    P ws = w[i];
+    for (int q = 0; q < k; q++) ws -= bsh[q] * W[q * n + i];
+    ws *= (P)sc[0];
     W[(size_t)k * n + i] = ws;
-    const T rn = (T)((double)r[i] - sc[1] * (double)ws);
-    r[i] = rn;
-    if (rp) rp[i] = (P)rn;
+    pin[i] = ws;
+    Z[(size_t)k * n + i] = z[i];
 }
 
-// x += sum_{q < k} alpha_q Z_q (alpha_q = sc[8 + q]): the basis part of the
-// iterate, once per basis (at a restart and at the end of the solve)
+// r = r - sum alpha_q W_q over the basis (end of a basis); the P copy of the
+// new r0 for the sums (rp, the FP32 form) and the preconditioner's input
 template <typename P, typename T>
-__global__ void k_gcr_xupdate(size_t n, int k, const P *__restrict__ Z, const double *__restrict__ sc,
-                              T *__restrict__ x) {
+__global__ void k_gcr_rupdate(size_t n, int k, const P *__restrict__ W, const double *__restrict__ sc,
+                              T *__restrict__ r, P *__restrict__ rp, P *__restrict__ pin) {
     __shared__ P ash[GCR_MAX_M];
     for (int q = threadIdx.x; q < k; q += blockDim.x) ash[q] = (P)sc[8 + q];
+    __syncthreads();
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    P a = 0;
+    for (int q = 0; q < k; q++) a += ash[q] * W[q * n + i];
+    const T rn = (T)((double)r[i] - (double)a);
+    r[i] = rn;
+    if (rp) rp[i] = (P)rn;
+    pin[i] = (P)rn;
+}
+
+// start of the solve: the P copy of r0 (FP32 form) and the first input
+template <typename P, typename T>
+__global__ void k_gcr_start(size_t n, const T *__restrict__ r, P *__restrict__ rp, P *__restrict__ pin) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const P v = (P)r[i];
+    if (rp) rp[i] = v;
+    pin[i] = v;
+}
+
+// x += sum_{q < k} gamma_q Z_q (gamma = U^-1 alpha, k_gcr_gamma): the basis
+// part of the iterate, once per basis (at a restart and at the end)
+template <typename P, typename T>
+__global__ void k_gcr_xupdate(size_t n, int k, const P *__restrict__ Z, const double *__restrict__ gamma,
+                              T *__restrict__ x) {
+    __shared__ P ash[GCR_MAX_M];
+    for (int q = threadIdx.x; q < k; q += blockDim.x) ash[q] = (P)gamma[q];
     __syncthreads();
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -2037,7 +2077,7 @@ template <typename T, int MDOT_Q>
 __global__ void __launch_bounds__(256) k_gcr_dots(int k, size_t n, const T *const *__restrict__ a,
                                                   const T *__restrict__ w, const T *__restrict__ r, double *part,
                                                   double *out, const double *flag, int mode, double *sc,
-                                                  unsigned int *cnt) {
+                                                  double *tri, unsigned int *cnt) {
     if (flag && *flag == 0.0) return;
     __shared__ double sh[32 * MDOT_Q];
     const int nq = k + 2, q0 = blockIdx.y * MDOT_Q;
@@ -2059,10 +2099,14 @@ __global__ void __launch_bounds__(256) k_gcr_dots(int k, size_t n, const T *cons
     if (mode == 1) {
         double nrm2 = d[k];
         for (int q = 0; q < k; q++) nrm2 -= d[q] * d[q];
-        if (k > 0 && !(nrm2 > 1e-3 * d[k])) { sc[5] = 1.0; return; }
+        if (k > 0 && !(nrm2 > 1e-3 * d[k])) {   // second pass: keep this pass's coefficients in U
+            for (int q = 0; q < k; q++) tri[(size_t)k * GCR_MAX_M + q] = d[q];
+            sc[5] = 1.0;
+            return;
+        }
         sc[5] = 0.0;
     }
-    gcr_scalars(k, d, sc);
+    gcr_scalars(k, d, sc, tri, mode == 2);
 }
 
 template <typename T>
@@ -2075,7 +2119,7 @@ static mdz_status gcr_dots_launch(mdz_ctx *ctx, gcr_space<T> &S, int k, const T 
     if (bx > cap) bx = cap;
     if (bx < 8) bx = 8;
     k_gcr_dots<T, Q><<<dim3(bx, tiles), 256, 0, st>>>(k, S.n, S.dA0, w, r, ctx->red_part + MDZ_RP_DOTS, out, flag,
-                                                       mode, sc, ctx->red_cnt + MDZ_RC_GCR);
+                                                       mode, sc, S.tri, ctx->red_cnt + MDZ_RC_GCR);
     MDZ_LAUNCHED(ctx);
     return MDZ_OK;
 }
@@ -2115,7 +2159,7 @@ static mdz_status precond_graph(mdz_ctx *ctx, gcr_space<T> &S, mg_hier<T> &H, co
     if (SV->pre[slot]) { cudaGraphExecDestroy(SV->pre[slot]); SV->pre[slot] = nullptr; }
     const long long l0 = ctx->launches;
     MDZ_CUDA(ctx, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    mdz_status s = precondition<T>(ctx, H, eta_n, Dt, S.r, S.z, S.nu, S.nv, st);
+    mdz_status s = precondition<T>(ctx, H, eta_n, Dt, S.pin, S.z, S.nu, S.nv, st);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &g);
     if (s != MDZ_OK) { if (g) cudaGraphDestroy(g); return s; }
@@ -2195,19 +2239,29 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
     double rn2 = SV->sc[0], rn02 = rn2;
     int it = 0;
     if (rn02 == 0.0) { if (its_out) *its_out = 0; if (rel_out) *rel_out = 0.0; return MDZ_OK; }
+    // the preconditioner's first input r0 and (FP32 form) the FP32 copy of r0
+    k_gcr_start<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, S.r, mixed ? SP.r : (P *)nullptr, SP.pin);
+    MDZ_LAUNCHED(ctx);
     int k = 0;
+    const double *gamma = SP.tri + (size_t)GCR_MAX_M * GCR_MAX_M;
+    // end of a basis: x += Z U^-1 alpha, r = r0 - W alpha (and its copies)
+    auto end_basis = [&](bool need_r) -> mdz_status {
+        if (k == 0) return MDZ_OK;
+        k_gcr_gamma<<<1, 32, 0, st>>>(k, sc, SP.tri);
+        MDZ_LAUNCHED(ctx);
+        k_gcr_xupdate<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, k, SP.Z, gamma, S.x);
+        MDZ_LAUNCHED(ctx);
+        if (need_r) {
+            k_gcr_rupdate<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, k, SP.W, sc, S.r, mixed ? SP.r : (P *)nullptr, SP.pin);
+            MDZ_LAUNCHED(ctx);
+        }
+        k = 0;
+        return MDZ_OK;
+    };
     const int check = SV->check > 0 ? SV->check : 1;
     for (it = 0; it < maxit; it++) {
-        if (k == S.m) {   // restart: fold the basis into x, keep r, drop the basis
-            k_gcr_xupdate<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, k, SP.Z, sc, S.x);
-            MDZ_LAUNCHED(ctx);
-            k = 0;
-        }
+        if (k == S.m && (s = end_basis(true)) != MDZ_OK) return s;   // restart: fold the basis into x and r
         cudaEvent_t ev;
-        if (mixed && it == 0) {   // r (T) -> r (P) for the first preconditioner application
-            k_convert<T, P><<<nb, MDZ_THREADS, 0, st>>>(n, S.r, SP.r);
-            MDZ_LAUNCHED(ctx);
-        }
         mdz_prof_begin(ctx, MDZ_PROF_MG_SMOOTH, st, &ev);
         MDZ_CUDA(ctx, cudaGraphLaunch(pre, st));
         ctx->launches += pre_launches;
@@ -2223,34 +2277,27 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
             mdz_prof_end(ctx, MDZ_PROF_STOKES_APPLY, bytes, st, ev);
         }
         mdz_prof_begin(ctx, MDZ_PROF_KRYLOV, st, &ev);
-        // The basis Z, W and the new pair z, K z stay in the apply's precision
-        // P (in the FP32 form: as the FP32 V-cycle and apply produced them; the
-        // FP32 rounding of a stored basis vector is the rounding K z already
-        // carries); x, r and every sum are FP64.
-        // First pass: (w, W_q) q < k, (w, w), (w, r); the check decides on the
-        // device whether a second pass runs.
+        // The basis W and the raw preconditioned vectors Z stay in the apply's
+        // precision P (in the FP32 form: as the FP32 V-cycle and apply
+        // produced them); x, r and every sum are FP64.  First pass:
+        // (w, W_q) q < k, (w, w), (w, r0); the check decides on the device
+        // whether a second pass runs.
         const int ng = nb < 152 * 8 ? nb : 152 * 8;
-        // one launch per pass: (w, W_q), (w, w) and (w, r) against the residual
-        // as the preconditioner saw it (SP.r: the FP32 copy in the FP32 form,
-        // r itself otherwise), then the check / scalars in its last block
         double *d1 = dots1p[it & 1], *d2 = dots2p[it & 1];
         if ((s = gcr_dots_launch<P>(ctx, SP, k, SP.w, SP.r, d1, nullptr, 1, sc, st)) != MDZ_OK) return s;
         if (k > 0) {   // second pass (each launch returns at once unless sc[5] = 1)
-            k_gcr_orth_if<P><<<ng, MDZ_THREADS, 0, st>>>(n, k, SP.Z, SP.W, d1, sc, SP.z, SP.w);
+            k_gcr_orth_if<P><<<ng, MDZ_THREADS, 0, st>>>(n, k, SP.W, d1, sc, SP.w);
             MDZ_LAUNCHED(ctx);
             if ((s = gcr_dots_launch<P>(ctx, SP, k, SP.w, SP.r, d2, sc + 5, 2, sc, st)) != MDZ_OK) return s;
         }
-        k_gcr_finish<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, k, SP.Z, SP.W, d1, d2, sc, SP.z, SP.w, S.r,
-                                                        mixed ? SP.r : (P *)nullptr, dots1p[(it + 1) & 1],
-                                                        dots2p[(it + 1) & 1]);
+        k_gcr_finish<P><<<nb, MDZ_THREADS, 0, st>>>(n, k, SP.W, SP.Z, d1, d2, sc, SP.z, SP.w, SP.pin,
+                                                     dots1p[(it + 1) & 1], dots2p[(it + 1) & 1]);
         MDZ_LAUNCHED(ctx);
-        {   // algorithmic bytes (one Gram-Schmidt pass): the dots read W_q, w
-            // (k + 1 P vectors) and w, r (P); the finish reads Z_q, W_q, z, w
-            // (P), r (T) and writes Z_k, W_k (P), r (T) and its P copy; x is
-            // formed once per basis (k + 2 vectors, not counted per iteration)
-            double pv = (k > 0 ? k + 1.0 : 0.0) + 2.0 + (2.0 * k + 2.0) + 2.0 + (mixed ? 1.0 : 0.0), tv = 2.0;
-            double bytes = (double)n * (sizeof(P) * pv + sizeof(T) * tv);
-            mdz_prof_end(ctx, MDZ_PROF_KRYLOV, bytes, st, ev);
+        {   // algorithmic bytes (one Gram-Schmidt pass): the sums read W_q,
+            // w and r0 (k + 2 P vectors); the finish reads W_q, w, z and
+            // writes W_k, Z_k and the next input (k + 5)
+            double pv = 2.0 * k + 7.0;
+            mdz_prof_end(ctx, MDZ_PROF_KRYLOV, (double)n * sizeof(P) * pv, st, ev);
         }
         k++;
         // the running norm lives on the device; the host looks every `check`
@@ -2261,7 +2308,9 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
         rn2 = SV->sc[3];
         if (!std::isfinite(rn2)) return mdz_fail(ctx, MDZ_ERR_NAN, "GCR: NaN in the Krylov iteration");
         if (rn2 <= rtol * rtol * rn02 || (k == S.m)) {
-            // recompute the true norm of r at convergence and at each restart
+            // fold the basis in and take the true norm of r at convergence
+            // and at each restart
+            if ((s = end_basis(true)) != MDZ_OK) return s;
             if ((s = dots_launch<T>(ctx, S, S.m + 1, 1, S.r, dots, st)) != MDZ_OK) return s;
             k_set_scalar<<<1, 32, 0, st>>>(sc + 3, dots);
             MDZ_LAUNCHED(ctx);
@@ -2271,10 +2320,7 @@ static mdz_status gcr_solve(mdz_ctx *ctx, gcr_space<T> &S, gcr_space<P> &SP, mg_
             if (rn2 <= rtol * rtol * rn02) { it++; break; }
         }
     }
-    if (k > 0) {   // the current basis' part of the iterate
-        k_gcr_xupdate<P, T><<<nb, MDZ_THREADS, 0, st>>>(n, k, SP.Z, sc, S.x);
-        MDZ_LAUNCHED(ctx);
-    }
+    if ((s = end_basis(false)) != MDZ_OK) return s;   // the current basis' part of the iterate
     if (its_out) *its_out = it;
     if (rel_out) *rel_out = sqrt(rn2 > 0 ? rn2 : 0.0) / sqrt(rn02);
     return MDZ_OK;

@@ -122,7 +122,7 @@ template <typename T, bool NEWTON, typename RS>
 __device__ __forceinline__ T xrow(const stokes_geom &G, const stokes_coefs<T> &D, const stokes_cvec<T> &x, int k,
                                   int l, const RS &rs) {
     const int nx = G.Nx, ncx = G.ncx, nxvz = nx + 1;
-    const int c1 = k + l * nx, c2 = k - 1 + (l - 1) * ncx, c3 = k + l * nxvz;
+    const int c1 = k + l * nx, c2 = k - 1 + (l - 1) * ncx;
     const T idx = gc<T>(G, GC_IDX), idz = gc<T>(G, GC_IDZ);
     const int iPrW = c2, iPrE = c2 + 1, ixyN = c1, ixyS = c1 - nx;
     const T inW = G.BCp[iPrW] == -1 ? T(1) : T(0), inE = G.BCp[iPrE] == -1 ? T(1) : T(0);
