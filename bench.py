@@ -308,18 +308,16 @@ def e2e_form(cfg_builder, precision, learned, steps, size, warmup):
     h2d = d2h = 0
     for step in range(warmup + steps):   # the same steps as the device-resident form; the last `steps` timed
         t0 = time.perf_counter()
-        ctx.set_markers(hin["x"][:n], hin["z"][:n], hin["phase"][:n])
-        for attr, key in attrs:
-            ctx.set_marker_attr(attr, hin[key][:n])
+        # one batched upload and one batched download per step (mdz_set/get_marker_state: the copies of a
+        # call spread over several streams and copy engines)
+        ctx.set_marker_state(hin["x"][:n], hin["z"][:n], hin["phase"][:n], {attr: hin[key][:n] for attr, key in attrs})
         t1 = time.perf_counter()
         rep = ctx.time_step(mat, model)
         t2 = time.perf_counter()
         n_in, n = n, ctx.n_markers
         reps.append({k: rep.as_dict()[k] for k in ("nonlinear_its", "linear_its", "ms_solve", "ms_rheology",
                                                     "ms_total", "markers_added")})
-        ctx.get_markers(out=hout)
-        for attr, key in attrs:
-            ctx.get_marker_attr(attr, out=hin[key])
+        ctx.get_marker_state(hout, {attr: hin[key] for attr, key in attrs})
         ctx.L.mdz_get_velocity(ctx.h, mdz._dptr(hu), None, None)
         t3 = time.perf_counter()
         if step < warmup:

@@ -502,6 +502,19 @@ mdz_status mdz_AccumulatedStrainII(mdz_ctx *ctx, mdz_fields *f, double dt);
 mdz_status mdz_set_marker_attr(mdz_ctx *ctx, int attr, int n, const double *values);
 mdz_status mdz_get_marker_attr(mdz_ctx *ctx, int attr, int n, double *values);
 
+/* Batched marker transfers for a host-side time loop (the reference keeps
+ * its markers in host arrays): positions, phases and any of the MDZ_M_NATTR
+ * attributes (attrs[a] null: attribute a not copied; attrs null: none) in one
+ * call, the copies spread over several streams so that they run on several
+ * copy engines at once.  set: makes n the resident marker count, as
+ * mdz_set_markers.  get: any of x, z, phase, vx, vz may be null.  Both return
+ * when the copies are done.  Register the host arrays (mdz_host_register) to
+ * make them DMA transfers. */
+mdz_status mdz_set_marker_state(mdz_ctx *ctx, int n, const double *x, const double *z, const int *phase,
+                                const double *const *attrs);
+mdz_status mdz_get_marker_state(mdz_ctx *ctx, int n, double *x, double *z, int *phase, double *vx, double *vz,
+                                double *const *attrs);
+
 /* Copy grid fields between the caller's host arrays and the context's device
  * mirrors: to_device = 1 uploads every non-NULL member, 0 downloads them. */
 mdz_status mdz_sync_fields(mdz_ctx *ctx, mdz_fields *f, int to_device);

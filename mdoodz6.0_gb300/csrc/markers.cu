@@ -204,8 +204,8 @@ __device__ __forceinline__ void cell_range(int i, int h, int kind, int n_nodes, 
 template <int NF, int NPH>
 __global__ void __launch_bounds__(128) k_p2g_gather(
     int nnx, int nnz, const double *__restrict__ X, const double *__restrict__ Z, const signed char *__restrict__ tag,
-    int kindx, int kindz, int h, double dx, double dz, double dx_itp, double dz_itp, int ncx, int ncz,
-    const int *__restrict__ start, const int *__restrict__ sorted, const int *__restrict__ qvert,
+    int kindx, int kindz, int h, double dx, double dz, double idx, double idz, double idxi, double idzi, int ncx,
+    int ncz, const int *__restrict__ start, const int *__restrict__ sorted, const int *__restrict__ qvert,
     const double *__restrict__ mx, const double *__restrict__ mz, const int *__restrict__ mphase, p2g_fields F,
     int nph_rt, double *__restrict__ phase_perc) {
     int node = blockIdx.x * blockDim.x + threadIdx.x;
@@ -220,7 +220,8 @@ __global__ void __launch_bounds__(128) k_p2g_gather(
 #pragma unroll
     for (int p = 0; p < NPH; p++) Wph[p] = 0.0;
     const double X0 = X[0], Z0 = Z[0];
-    const double idx = 1.0 / dx, idz = 1.0 / dz, idxi = 1.0 / dx_itp, idzi = 1.0 / dz_itp;
+    // (1/dx, 1/dz and the reciprocal interpolation widths come from the host:
+    // an FP64 division per thread is a long instruction sequence on this part)
     // contribution of marker k, whose nearest node (ip, jp) is within h of this one
     auto add = [&](int k, int ip, int jp, int di, int dj) {
         const double xk = mx[k], zk = mz[k];
@@ -301,14 +302,16 @@ static void launch_p2g_nf(int nph, dim3 gr, dim3 bl, cudaStream_t st, int nnx, i
     const mdz_bins &B = ctx->bins;
     const int *qv = kx == 1 && kz == 1 ? B.qvert : nullptr;   // vertex lines in both directions
     if (pp == nullptr || nph <= 0)
-        k_p2g_gather<NF, 0><<<gr, bl, 0, st>>>(nnx, nnz, X, Z, tag, kx, kz, h, dx, dz, dxi, dzi, ncx, ncz, B.start,
+        k_p2g_gather<NF, 0><<<gr, bl, 0, st>>>(nnx, nnz, X, Z, tag, kx, kz, h, dx, dz, 1.0 / dx, 1.0 / dz, 1.0 / dxi,
+                                               1.0 / dzi, ncx, ncz, B.start,
                                                B.sorted, qv, ctx->m.x, ctx->m.z, ctx->m.phase, F, 0, nullptr);
     else if (nph <= 4)
-        k_p2g_gather<NF, 4><<<gr, bl, 0, st>>>(nnx, nnz, X, Z, tag, kx, kz, h, dx, dz, dxi, dzi, ncx, ncz, B.start,
+        k_p2g_gather<NF, 4><<<gr, bl, 0, st>>>(nnx, nnz, X, Z, tag, kx, kz, h, dx, dz, 1.0 / dx, 1.0 / dz, 1.0 / dxi,
+                                               1.0 / dzi, ncx, ncz, B.start,
                                                B.sorted, qv, ctx->m.x, ctx->m.z, ctx->m.phase, F, nph, pp);
     else
-        k_p2g_gather<NF, MDZ_MAX_PHASES><<<gr, bl, 0, st>>>(nnx, nnz, X, Z, tag, kx, kz, h, dx, dz, dxi, dzi, ncx,
-                                                            ncz, B.start, B.sorted, qv, ctx->m.x,
+        k_p2g_gather<NF, MDZ_MAX_PHASES><<<gr, bl, 0, st>>>(nnx, nnz, X, Z, tag, kx, kz, h, dx, dz, 1.0 / dx, 1.0 / dz,
+                                                            1.0 / dxi, 1.0 / dzi, ncx, ncz, B.start, B.sorted, qv, ctx->m.x,
                                                             ctx->m.z, ctx->m.phase, F, nph, pp);
 }
 
@@ -652,13 +655,12 @@ __global__ void k_rk4(int n, double *__restrict__ mx, double *__restrict__ mz, i
                       const double *__restrict__ v, const double *__restrict__ xg, const double *__restrict__ zg,
                       const double *__restrict__ zvx, const double *__restrict__ xvz, int Nx, int Nz,
                       const signed char *__restrict__ tu, const signed char *__restrict__ tv, double dx, double dz,
-                      double dt, double xmin, double xmax, double zmin, double zmax) {
+                      double idx, double idz, double dt, double xmin, double xmax, double zmin, double zmax) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     int ph = mphase[k];
     double xA = mx[k], zA = mz[k], x = xA, z = zA;
     double VxA = 0, VzA = 0, VxB = 0, VzB = 0, VxC = 0, VzC = 0, VxD = 0, VzD = 0;
-    const double idx = 1.0 / dx, idz = 1.0 / dz;
 #define OUT_CHECK() if (x < xmin || x > xmax || z < zmin || z > zmax) ph = -1;
     if (ph != -1) v2p(x, z, u, v, xg, zg, zvx, xvz, Nx, Nz, tu, dx, dz, idx, idz, tv, VxA, VzA);
     if (ph != -1) { x = xA + 0.5 * dt * VxA; z = zA + 0.5 * dt * VzA; }
@@ -687,7 +689,7 @@ mdz_status mdz_dev_rk4(mdz_ctx *ctx, const double *du, const double *dv, double 
     if (n > 0) {
         k_rk4<<<mdz_blocks(n), MDZ_THREADS, 0, st>>>(n, ctx->m.x, ctx->m.z, ctx->m.phase, ctx->m.vx, ctx->m.vz, du, dv,
                                                      g.xg, g.zg, g.zvx, g.xvz, g.Nx, g.Nz, g.BCu, g.BCv, g.dx, g.dz,
-                                                     dt, g.xmin, g.xmax, g.zmin, g.zmax);
+                                                     g.idx, g.idz, dt, g.xmin, g.xmax, g.zmin, g.zmax);
         MDZ_LAUNCHED(ctx);
     }
     ctx->bins.valid = false;

@@ -65,6 +65,7 @@ struct mdz_bins {
     int *scan_partials = nullptr;
 };
 
+#define MDZ_XFER_STREAMS 4
 struct mdz_ctx {
     // the grid description with the context's own copies of its coordinate
     // lines and tags (host_desc points at these; the Dirichlet values live on
@@ -78,6 +79,7 @@ struct mdz_ctx {
     mdz_markers m;
     mdz_bins bins;
     cudaStream_t stream = nullptr;
+    cudaStream_t xfer[MDZ_XFER_STREAMS] = {};   // copy streams of the batched marker transfers (lazy)
     long long launches = 0;
     mdz_fields d{};              // device mirrors of every grid field (allocated on first use)
     bool fields_ready = false;

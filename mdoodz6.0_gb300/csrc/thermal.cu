@@ -28,6 +28,7 @@ constexpr int EN_MAX_BLOCKS = 2048;   // partial slots per reduced value
 struct energy_bc_dev {
     const signed char *type, *typW, *typE, *typS, *typN;
     const double *valW, *valE, *valS, *valN;
+    double ixx, izz;   // 1/dx/dx, 1/dz/dz as the reference forms them (host: no FP64 division per row)
 };
 
 __device__ __forceinline__ bool active(const energy_bc_dev &B, int c) { return B.type[c] != 30; }
@@ -41,7 +42,7 @@ __global__ void k_energy_setup(mdz_dgrid g, mdz_fields f, energy_bc_dev B, doubl
     if (c2 >= ncx * ncz) return;
     const int k = c2 % ncx, l = c2 / ncx;
     if (!active(B, c2)) { diag[c2] = 1.0; rhs[c2] = 0.0; return; }
-    const double ixx = 1.0 / g.dx / g.dx, izz = 1.0 / g.dz / g.dz;
+    const double ixx = B.ixx, izz = B.izz;
     const double rhoCp = f.rho_n[c2] * f.Cv[c2], T = f.T[c2];
     double b = 1.0 * rhoCp * T / dt;
     b += 1.0 * f.Qr[c2];
@@ -73,7 +74,7 @@ __device__ __forceinline__ double energy_row(const mdz_dgrid &g, const mdz_field
                                              const double *diag, const double *x, int c2) {
     const int ncx = g.ncx, ncz = g.ncz, nx = g.Nx, nxvz = g.Nx + 1;
     const int k = c2 % ncx, l = c2 / ncx;
-    const double ixx = 1.0 / g.dx / g.dx, izz = 1.0 / g.dz / g.dz;
+    const double ixx = B.ixx, izz = B.izz;
     const int c1 = k + (l + 1) * nx, c3 = k + l * nxvz + 1;
     double y = diag[c2] * x[c2];
     if (l > 0 && active(B, c2 - ncx)) y += -1.0 * f.kz[c3] * izz * x[c2 - ncx];
@@ -211,7 +212,7 @@ extern "C" mdz_status mdz_EnergyDirectSolve(mdz_ctx *ctx, mdz_fields *f, const m
     MDZ_CUDA(ctx, cudaMemcpyAsync(vals + 2 * ncz + ncx, bc->valN, sizeof(double) * ncx, cudaMemcpyHostToDevice, st));
     MDZ_CUDA(ctx, cudaMemsetAsync(neg, 0, sizeof(int), st));
     energy_bc_dev B{tags, tags + n, tags + n + ncz, tags + n + 2 * ncz, tags + n + 2 * ncz + ncx,
-                    vals, vals + ncz, vals + 2 * ncz, vals + 2 * ncz + ncx};
+                    vals, vals + ncz, vals + 2 * ncz, vals + 2 * ncz + ncx, 1.0 / g.dx / g.dx, 1.0 / g.dz / g.dz};
     const mdz_fields &d = ctx->d;
     k_energy_setup<<<mdz_blocks(n, EN_THREADS), EN_THREADS, 0, st>>>(g, d, B, dt, gz, shear_heating, adiab_heating,
                                                                       diag, rhs);

@@ -471,6 +471,35 @@ class Context:
         v = np.ascontiguousarray(values, np.float64)
         self._check(self.L.mdz_set_marker_attr(self.h, C.c_int(attr), C.c_int(len(v)), _dptr(v)))
 
+    def set_marker_state(self, x, z, phase, attrs):
+        """Upload positions, phases and attributes ({attr index: array}) in
+        one batched call (mdz_set_marker_state); arrays are used in place and
+        must be contiguous float64 (phase int32)."""
+        n = len(x)
+        for a in [x, z] + list(attrs.values()):
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.size < n:
+                raise MdzError(1, "set_marker_state: contiguous float64 arrays of the marker count")
+        if phase.dtype != np.int32 or not phase.flags.c_contiguous:
+            raise MdzError(1, "set_marker_state: phase must be contiguous int32")
+        tab = (_dp * M_NATTR)()
+        for a, v in attrs.items():
+            tab[a] = _dptr(v)
+        self._check(self.L.mdz_set_marker_state(self.h, C.c_int(n), _dptr(x), _dptr(z), _iptr(phase), tab))
+
+    def get_marker_state(self, out, attrs):
+        """Download (x, z, phase, vx, vz) into the five arrays of `out` (None
+        to skip one) and the attributes into {attr index: array}, in one batched
+        call (mdz_get_marker_state)."""
+        n = self.n_markers
+        x, z, ph, vx, vz = out
+        tab = (_dp * M_NATTR)()
+        for a, v in attrs.items():
+            if v.dtype != np.float64 or v.size < n or not v.flags.c_contiguous:
+                raise MdzError(1, "get_marker_state: contiguous float64 arrays of the marker count")
+            tab[a] = _dptr(v)
+        self._check(self.L.mdz_get_marker_state(self.h, C.c_int(n), _dptr(x), _dptr(z), _iptr(ph), _dptr(vx),
+                                                _dptr(vz), tab))
+
     def get_marker_attr(self, attr, out=None):
         n = self.n_markers
         v = np.zeros(n) if out is None else out
