@@ -1136,26 +1136,38 @@ __global__ void __launch_bounds__(MG_BOTTOM_THREADS) k_mg_bottom(const __grid_co
         T *t = xu[l]; xu[l] = yu[l]; yu[l] = t;
         t = xv[l]; xv[l] = yv[l]; yv[l] = t;
     };
+    // one smoothing sweep / residual over a level's rows, one row per thread
+    // (u rows, then v rows: twice the threads of a point per thread, so that
+    // each phase's critical path is one 31-point row)
+    auto smooth_rows = [&](const mg_bottom_level<T> &L, const T *ixu, const T *ixv, T *ou, T *ov, int t0, int nt) {
+        const int Nx = L.G.Nx, nuL = Nx * (L.G.Nz + 1), nvL = (Nx + 1) * L.G.Nz;
+        for (int r = t0; r < nuL + nvL; r += nt) {
+            if (r < nuL) st_smooth_u<T>(L.G, L.su, L.sv, ixu, ixv, L.fu, L.idu, A.omega, ou, r % Nx, r / Nx);
+            else st_smooth_v<T>(L.G, L.su, L.sv, ixu, ixv, L.fv, L.idv, A.omega, ov, (r - nuL) % (Nx + 1),
+                                (r - nuL) / (Nx + 1));
+        }
+    };
+    auto residual_rows = [&](const mg_bottom_level<T> &L, const T *ixu, const T *ixv, int t0, int nt) {
+        const int Nx = L.G.Nx, nuL = Nx * (L.G.Nz + 1), nvL = (Nx + 1) * L.G.Nz;
+        for (int r = t0; r < nuL + nvL; r += nt) {
+            if (r < nuL) st_residual_u<T>(L.G, L.su, ixu, ixv, L.fu, L.ru, r % Nx, r / Nx);
+            else st_residual_v<T>(L.G, L.sv, ixu, ixv, L.fv, L.rv, (r - nuL) % (Nx + 1), (r - nuL) / (Nx + 1));
+        }
+    };
     // One level's descent (pre-smoothing, residual, restriction) or ascent
     // (prolongation, post-smoothing) by a team of threads t0, t0 + nt, ...
     // (act = false: the thread only keeps its pointer swaps in step) with the
     // team's barrier after each phase.
     auto down = [&](int l, bool act, int t0, int nt, auto &&sync) {
         const mg_bottom_level<T> &L = A.L[l];
-        const int W = L.G.Nx + 1, npt = W * (L.G.Nz + 1);
-        for (int p = t0; act && p < npt; p += nt)
-            st_smooth_pt<T>(L.G, L.su, L.sv, nullptr, nullptr, L.fu, L.fv, L.idu, L.idv, A.omega, xu[l], xv[l],
-                            p % W, p / W);
+        if (act) smooth_rows(L, nullptr, nullptr, xu[l], xv[l], t0, nt);
         sync();
         for (int s = 1; s < A.nu1; s++) {
-            for (int p = t0; act && p < npt; p += nt)
-                st_smooth_pt<T>(L.G, L.su, L.sv, xu[l], xv[l], L.fu, L.fv, L.idu, L.idv, A.omega, yu[l], yv[l],
-                                p % W, p / W);
+            if (act) smooth_rows(L, xu[l], xv[l], yu[l], yv[l], t0, nt);
             sync();
             swap_xy(l);
         }
-        for (int p = t0; act && p < npt; p += nt)
-            st_residual_pt<T>(L.G, L.su, L.sv, xu[l], xv[l], L.fu, L.fv, L.ru, L.rv, p % W, p / W);
+        if (act) residual_rows(L, xu[l], xv[l], t0, nt);
         sync();
         const mg_bottom_level<T> &C = A.L[l + 1];
         const int Wc = C.G.Nx + 1, nptc = Wc * (C.G.Nz + 1);
@@ -1171,9 +1183,7 @@ __global__ void __launch_bounds__(MG_BOTTOM_THREADS) k_mg_bottom(const __grid_co
             mg_prolong_pt<T>(L.G, C.G, xu[l + 1], xv[l + 1], xu[l], xv[l], p % W, p / W);
         sync();
         for (int s = 0; s < A.nu2; s++) {
-            for (int p = t0; act && p < npt; p += nt)
-                st_smooth_pt<T>(L.G, L.su, L.sv, xu[l], xv[l], L.fu, L.fv, L.idu, L.idv, A.omega, yu[l], yv[l],
-                                p % W, p / W);
+            if (act) smooth_rows(L, xu[l], xv[l], yu[l], yv[l], t0, nt);
             sync();
             swap_xy(l);
         }
