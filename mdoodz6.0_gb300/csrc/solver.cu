@@ -966,14 +966,17 @@ __global__ void __launch_bounds__(512) k_coarse_dense_setup(stokes_geom G, const
     // [A | I] in shared memory when it fits (the launch passes the dynamic
     // size), else in the global work array: each of the n elimination steps
     // reads and writes all of it between barriers
+    // in the hierarchy's precision: the FP32 hierarchy's inverse is stored in
+    // FP32 and only corrects a V-cycle; FP64 elimination runs at a small
+    // fraction of the FP32 rate on this part (one CTA: ~300 us per set-up)
     extern __shared__ double dsm[];
-    double *A = (size_t)2 * n * n * sizeof(double) <= MG_DENSE_SMEM ? dsm : Ag;
-    __shared__ double col[MG_DENSE_MAX];
+    T *A = (size_t)2 * n * n * sizeof(T) <= MG_DENSE_SMEM ? reinterpret_cast<T *>(dsm) : reinterpret_cast<T *>(Ag);
+    __shared__ T col[MG_DENSE_MAX];
     __shared__ int bad;
     const int Nx = G.Nx, Nz = G.Nz;
     const size_t nu = (size_t)Nx * (Nz + 1), nv = (size_t)(Nx + 1) * Nz;
     if (threadIdx.x == 0) bad = 0;
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) A[e] = 0.0;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) A[e] = T(0);
     __syncthreads();
     for (int r = threadIdx.x; r < n; r += blockDim.x) {
         const int m = map[r];
@@ -981,42 +984,42 @@ __global__ void __launch_bounds__(512) k_coarse_dense_setup(stokes_geom G, const
             const int k = m % Nx, l = m / Nx;
             for (int q = 0; q < 15; q++) {
                 int c = dense_u(Nx, Nz, k + q % 3 - 1, l + q / 3 - 2);
-                if (c >= 0) A[(size_t)r * n + c] += (double)su[(size_t)q * nu + m];
+                if (c >= 0) A[(size_t)r * n + c] += su[(size_t)q * nu + m];
             }
             for (int q = 0; q < 16; q++) {
                 int c = dense_v(Nx, Nz, k + q % 4 - 1, l + q / 4 - 2);
-                if (c >= 0) A[(size_t)r * n + c] += (double)su[(size_t)(15 + q) * nu + m];
+                if (c >= 0) A[(size_t)r * n + c] += su[(size_t)(15 + q) * nu + m];
             }
         } else {
             const int mv = m - (int)nu, i = mv % (Nx + 1), j = mv / (Nx + 1);
             for (int q = 0; q < 15; q++) {
                 int c = dense_v(Nx, Nz, i + q % 5 - 2, j + q / 5 - 1);
-                if (c >= 0) A[(size_t)r * n + c] += (double)sv[(size_t)q * nv + mv];
+                if (c >= 0) A[(size_t)r * n + c] += sv[(size_t)q * nv + mv];
             }
             for (int q = 0; q < 16; q++) {
                 int c = dense_u(Nx, Nz, i + q % 4 - 2, j + q / 4 - 1);
-                if (c >= 0) A[(size_t)r * n + c] += (double)sv[(size_t)(15 + q) * nv + mv];
+                if (c >= 0) A[(size_t)r * n + c] += sv[(size_t)(15 + q) * nv + mv];
             }
         }
     }
     __syncthreads();
     // Gauss-Jordan on [A | I] with partial pivoting (the Newton block is
     // neither symmetric nor definite); B ends as A^-1
-    double *B = A + (size_t)n * n;
-    __shared__ double red_v[32];
+    T *B = A + (size_t)n * n;
+    __shared__ T red_v[32];
     __shared__ int red_i[32];
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) B[e] = (e / n == e % n) ? 1.0 : 0.0;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) B[e] = (e / n == e % n) ? T(1) : T(0);
     __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
     for (int k = 0; k < n; k++) {
-        double bv = -1.0;
+        T bv = T(-1);
         int bi = k;
         for (int i = k + threadIdx.x; i < n; i += blockDim.x) {
-            const double v = fabs(A[(size_t)i * n + k]);
+            const T v = fabs(A[(size_t)i * n + k]);
             if (v > bv) { bv = v; bi = i; }
         }
         for (int o = 16; o > 0; o >>= 1) {
-            const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+            const T ov = __shfl_xor_sync(0xffffffffu, bv, o);
             const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
             if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
         }
@@ -1030,16 +1033,16 @@ __global__ void __launch_bounds__(512) k_coarse_dense_setup(stokes_geom G, const
                 }
         }
         __syncthreads();
-        const double pmax = red_v[0];
+        const T pmax = red_v[0];
         const int pr = red_i[0];
-        if (!(pmax > 0.0) || !isfinite(pmax)) { if (threadIdx.x == 0) bad = 1; break; }   // uniform
+        if (!(pmax > T(0)) || !isfinite(pmax)) { if (threadIdx.x == 0) bad = 1; break; }   // uniform
         if (pr != k)
             for (int j = threadIdx.x; j < n; j += blockDim.x) {
-                double t = A[(size_t)k * n + j]; A[(size_t)k * n + j] = A[(size_t)pr * n + j]; A[(size_t)pr * n + j] = t;
+                T t = A[(size_t)k * n + j]; A[(size_t)k * n + j] = A[(size_t)pr * n + j]; A[(size_t)pr * n + j] = t;
                 t = B[(size_t)k * n + j]; B[(size_t)k * n + j] = B[(size_t)pr * n + j]; B[(size_t)pr * n + j] = t;
             }
         __syncthreads();
-        const double inv = 1.0 / A[(size_t)k * n + k];
+        const T inv = T(1) / A[(size_t)k * n + k];
         __syncthreads();
         for (int j = threadIdx.x; j < n; j += blockDim.x) {
             A[(size_t)k * n + j] *= inv;
@@ -1569,7 +1572,7 @@ static mdz_status mg_setup(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n, con
     }
     mg_level<T> &C = H.L[H.nlev - 1];
     if (C.ndense) {
-        const size_t smem = (size_t)2 * C.ndense * C.ndense * sizeof(double);
+        const size_t smem = (size_t)2 * C.ndense * C.ndense * sizeof(T);
         k_coarse_dense_setup<T><<<1, 512, smem <= MG_DENSE_SMEM ? smem : 0, st>>>(C.geom(), C.su, C.sv, C.ndense,
                                                                               C.dmap, C.Awork, C.AinvT, status);
         MDZ_LAUNCHED(ctx);
