@@ -510,6 +510,28 @@ mdz_status mdz_get_marker_attr(mdz_ctx *ctx, int attr, int n, double *values);
  * mdz_set_markers.  get: any of x, z, phase, vx, vz may be null.  Both return
  * when the copies are done.  Register the host arrays (mdz_host_register) to
  * make them DMA transfers. */
+/* Output preparation (the data-parallel part of WriteOutputHDF5,
+ * SOURCE/HDF5Output.c:237-895; the HDF5 calls stay with the caller).
+ *
+ * mdz_Interp_Phase2VizGrid replaces Interp_Phase2VizGrid
+ * (SOURCE/ParticleRoutines.c:3004-3095) as WriteOutputHDF5 calls it
+ * (HDF5Output.c:266-297): the visualisation grid of res_fact times the grid
+ * resolution, its lines built by accumulation from the first grid line
+ * (xviz: res_fact*(Nx-1)+1 values, zviz: res_fact*(Nz-1)+1; either may be
+ * null), and per visualisation cell the phase of the resident marker with the
+ * largest tent weight (the first in index order among equal ones), markers in
+ * air centroids (BCp 30 / 31) left out, -1 where none: compo holds
+ * (nxviz-1)*(nzviz-1) values, the reference's "VizGrid/compo" (res_fact 1)
+ * and "VizGrid/compo_hr" (res_fact 2).
+ *
+ * mdz_output_field: the resident grid field `name` (an mdz_fields member, e.g.
+ * "u", "p", "sxxd", "eta_n", "rho_s", "T") cast to float and multiplied by
+ * `scale` with the product rounded to float, as DoubleToFloat + ScaleBack
+ * (HDF5Output.c:44-73) prepare each "Centers/..", "Vertices/..", "VxNodes/..",
+ * "VzNodes/.." dataset; out holds the field's node count. */
+mdz_status mdz_Interp_Phase2VizGrid(mdz_ctx *ctx, int res_fact, signed char *compo, double *xviz, double *zviz);
+mdz_status mdz_output_field(mdz_ctx *ctx, const char *name, double scale, float *out);
+
 mdz_status mdz_set_marker_state(mdz_ctx *ctx, int n, const double *x, const double *z, const int *phase,
                                 const double *const *attrs);
 mdz_status mdz_get_marker_state(mdz_ctx *ctx, int n, double *x, double *z, int *phase, double *vx, double *vz,

@@ -500,6 +500,23 @@ class Context:
         self._check(self.L.mdz_get_marker_state(self.h, C.c_int(n), _dptr(x), _dptr(z), _iptr(ph), _dptr(vx),
                                                 _dptr(vz), tab))
 
+    def Interp_Phase2VizGrid(self, res_fact):
+        """(compo as int8, xviz, zviz) of the visualisation grid of res_fact x
+        the grid resolution (mdz_Interp_Phase2VizGrid)."""
+        g = self.grid
+        nxv, nzv = res_fact * (g.Nx - 1) + 1, res_fact * (g.Nz - 1) + 1
+        compo = np.zeros((nxv - 1) * (nzv - 1), np.int8)
+        xv, zv = np.zeros(nxv), np.zeros(nzv)
+        self._check(self.L.mdz_Interp_Phase2VizGrid(self.h, C.c_int(res_fact), _sptr(compo), _dptr(xv), _dptr(zv)))
+        return compo, xv, zv
+
+    def output_field(self, name, scale, size):
+        """float32 copy of a resident field, scaled back (mdz_output_field)."""
+        out = np.zeros(size, np.float32)
+        self._check(self.L.mdz_output_field(self.h, os.fsencode(name), C.c_double(scale),
+                                            out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out
+
     def get_marker_attr(self, attr, out=None):
         n = self.n_markers
         v = np.zeros(n) if out is None else out

@@ -277,6 +277,23 @@ int ref_rk4(void) {
     return 0;
 }
 
+/* Closest-marker phase map on the visualisation grid of res_fact times the
+ * computational resolution, built and filled as WriteOutputHDF5 does
+ * (HDF5Output.c:266-297: lines by accumulation from the first grid line,
+ * Interp_Phase2VizGrid); compo holds (nxviz-1)*(nzviz-1) chars, xviz / zviz
+ * the nxviz / nzviz lines. */
+int ref_phase_viz(int res_fact, char *compo, double *xviz, double *zviz) {
+    const int nxviz = res_fact * (g_mesh.Nx - 1) + 1, nzviz = res_fact * (g_mesh.Nz - 1) + 1;
+    xviz[0] = g_mesh.xg_coord[0];
+    zviz[0] = g_mesh.zg_coord[0];
+    for (int k = 1; k < nxviz; k++) xviz[k] = xviz[k - 1] + g_mesh.dx / res_fact;
+    for (int k = 1; k < nzviz; k++) zviz[k] = zviz[k - 1] + g_mesh.dz / res_fact;
+    surface topo;
+    memset(&topo, 0, sizeof topo);
+    Interp_Phase2VizGrid(g_parts, g_parts.phase, &g_mesh, compo, xviz, zviz, nxviz, nzviz, g_model, topo);
+    return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 int ref_strain_rates(void) { StrainRateComponents(&g_mesh, g_scale, &g_model); return 0; }
 int ref_viscosity_grid(void) { NonNewtonianViscosityGrid(&g_mesh, &g_mat, &g_model, g_nmodel, &g_scale); return 0; }

@@ -162,6 +162,16 @@ class RefMDOODZ:
     def rk4(self):
         self.lib.ref_rk4()
 
+    def phase_viz(self, res_fact):
+        """Interp_Phase2VizGrid on the visualisation grid of res_fact x the
+        grid resolution: (compo as int8, xviz, zviz)."""
+        nxv, nzv = res_fact * (self.Nx - 1) + 1, res_fact * (self.Nz - 1) + 1
+        compo = np.zeros((nxv - 1) * (nzv - 1), np.int8)
+        xv, zv = np.zeros(nxv), np.zeros(nzv)
+        self.lib.ref_phase_viz(C.c_int(res_fact), compo.ctypes.data_as(C.c_char_p), xv.ctypes.data_as(_dp),
+                               zv.ctypes.data_as(_dp))
+        return compo, xv, zv
+
     # grid operators --------------------------------------------------------
     def strain_rates(self):
         self.lib.ref_strain_rates()

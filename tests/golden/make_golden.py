@@ -172,6 +172,25 @@ def set_neumann_walls(tu, vu, tv, vv, seed=21):
     vv[0, 1:Nx] = 0.2 * rng.standard_normal(Nx - 1)
 
 
+def make_phasemap_fixture():
+    """Interp_Phase2VizGrid as WriteOutputHDF5 calls it (visualisation grids of
+    1x and 2x the grid resolution) on the markers of the markers fixture, with
+    a patch of air centroids (BCp 30) whose markers must not mark the map."""
+    g = _grid()
+    r = RefMDOODZ(NX, NZ, XMIN, XMAX, ZMIN, ZMAX, 3)
+    r.set_bc_pureshear(1.0)
+    bcp = r.tags("BCp").reshape(NZ - 1, NX - 1)
+    bcp[-2:, 3:9] = 30
+    x, z, ph = _markers(g, seed=5)
+    r.set_markers(x, z, ph)
+    out = dict(Nx=NX, Nz=NZ, box=np.array([XMIN, XMAX, ZMIN, ZMAX]), x=x, z=z, phase=ph,
+               BCp=r.tags("BCp").copy())
+    for res in (1, 2):
+        compo, xv, zv = r.phase_viz(res)
+        out["compo_r%d" % res], out["xviz_r%d" % res], out["zviz_r%d" % res] = compo, xv, zv
+    np.savez_compressed(os.path.join(HERE, "phasemap_ref.npz"), **out)
+
+
 def make_rheology_fixture(avg=0, tag="", phases=None, model=None, neumann=False):
     g = _grid()
     r = RefMDOODZ(NX, NZ, XMIN, XMAX, ZMIN, ZMAX, 3)
@@ -534,7 +553,8 @@ def make_pressure_fixture():
 
 
 if __name__ == "__main__":
-    what = sys.argv[1:] or ["markers", "rheology", "reseed", "strain", "stress", "gridprops", "pressure", "thermal"]
+    what = sys.argv[1:] or ["markers", "rheology", "reseed", "strain", "stress", "gridprops", "pressure", "thermal",
+                            "phasemap"]
     if "gridprops" in what:
         make_gridprops_fixture()
     if "pressure" in what:
@@ -555,5 +575,7 @@ if __name__ == "__main__":
         make_rheology_fixture(0, "_mech", RHEO_PHASES_MECH, RHEO_MODEL_MECH)
     if "thermal" in what:
         make_thermal_fixture()
+    if "phasemap" in what:
+        make_phasemap_fixture()
     if "rheology" in what or "neumann" in what:
         make_rheology_fixture(0, "_neumann", neumann=True)
