@@ -257,16 +257,16 @@ def mlp_workload():
     loss = ctx.mlp_train(n // 65536, 65536, 2e-3)
     t_epoch = time.perf_counter() - t0
     ctx.mlp_set_engine(0)
-    b = ctx.mlp_benchmark(65536, 5)               # tcgen05 inference (the default)
+    b = ctx.mlp_benchmark(65536, 5)               # tcgen05 inference and training (the default)
     ctx.mlp_set_engine(1)
-    b1 = ctx.mlp_benchmark(65536, 5)              # warp-level mma.sync inference
+    b1 = ctx.mlp_benchmark(65536, 5)              # warp-level mma.sync
     ctx.close()
-    flops = 2.0 * (8 * 64 + 64 * 64 + 64 * 2)     # algorithmic FLOP per row (9472)
+    flops = 2.0 * (8 * 64 + 64 * 64 + 64 * 2)     # algorithmic FLOP per row of the forward pass (9472)
     return {"tuples": n, "batch": 65536, "generate_s": t_gen, "epoch_s": t_epoch, "loss": loss,
             "ms_infer_2^24": b["ms_infer"], "ms_train_step": b["ms_train_step"], "rms_error": b["rms_error"],
-            "infer_tflops": flops * n / (b["ms_infer"] * 1e-3) / 1e12, "infer_engine": "tcgen05",
+            "infer_tflops": flops * n / (b["ms_infer"] * 1e-3) / 1e12, "engine": "tcgen05",
             "mma_sync": {"ms_infer_2^24": b1["ms_infer"], "infer_tflops": flops * n / (b1["ms_infer"] * 1e-3) / 1e12,
-                         "rms_error": b1["rms_error"]}}
+                         "ms_train_step": b1["ms_train_step"], "rms_error": b1["rms_error"]}}
 
 
 def e2e_form(cfg_builder, precision, learned, steps, size, warmup):

@@ -325,10 +325,10 @@ mdz_status mdz_mlp_get_weights(mdz_ctx *ctx, float *params);
  * x = 2 (v - lo) / (hi - lo) - 1, temperature as 1000 / T over
  * [1000 / hi, 1000 / lo]. */
 mdz_status mdz_mlp_set_ranges(mdz_ctx *ctx, const double *lo, const double *hi);
-/* Kernel of mdz_mlp_infer and mdz_mlp_benchmark's inference: 0 (default)
- * tcgen05.mma on 128-row tiles with the accumulators in tensor memory,
- * 1 the warp-level mma.sync kernel.  Both compute the same BF16 network with
- * FP32 accumulation. */
+/* Kernels of inference (mdz_mlp_infer, mdz_mlp_benchmark) and training
+ * (mdz_mlp_train, mdz_mlp_gradients): 0 (default) tcgen05.mma on 128-row
+ * tiles with the accumulators in tensor memory, 1 the warp-level mma.sync
+ * kernels.  Both compute the same BF16 network with FP32 accumulation. */
 mdz_status mdz_mlp_set_engine(mdz_ctx *ctx, int engine);
 /* n training tuples on the device, drawn uniformly in the ranges (phase
  * uniform among the materials' phases) and labelled by the plain local solve

@@ -1,6 +1,7 @@
-// Learned local-rheology guess: state, BF16 tensor-core training (fused
-// forward + backward + weight gradients per 128-row tile, deterministic
-// reduction, Adam) and inference kernels, and the C entry points.  None of this
+// Learned local-rheology guess: state, the warp-level BF16 tensor-core training
+// (fused forward + backward + weight gradients per 128-row tile) and inference
+// kernels (engine 1; the tcgen05 kernels of engine 0 are in mlp_tc.cu), the
+// deterministic reduction with the Adam step, and the C entry points.  None of this
 // has a counterpart in the reference, whose local Newton iteration
 // (SOURCE/RheologyDensity.c:44-707) always starts from the smallest viscosity of
 // the active creep mechanisms; the plain solve here keeps that start and remains
@@ -246,16 +247,29 @@ __global__ void __launch_bounds__(128) k_mlp_train(const unsigned char *__restri
     if (threadIdx.x == 0) P[MLP_NPARAM] = BACC[130];
 }
 
-// Sum of the CTA partials in block order; optionally one Adam step on the FP32
-// master weights, which also rewrites the packed BF16 image.
-__global__ void k_mlp_reduce(int nblk, const float *__restrict__ partials, float *__restrict__ grad,
-                             float *__restrict__ params, float *__restrict__ m, float *__restrict__ v,
-                             unsigned char *packed, float lr, float b1, float b2, float eps, float bc1, float bc2,
-                             int adam) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p > MLP_NPARAM) return;
+// Sum of the CTA partials in a fixed order (8 interleaved slices of the CTAs,
+// then the slices in order); optionally one Adam step on the FP32 master
+// weights, which also rewrites the packed BF16 image.  Block: 32 parameters x
+// 8 slices.
+__global__ void __launch_bounds__(256) k_mlp_reduce(int nblk, const float *__restrict__ partials,
+                                                    float *__restrict__ grad, float *__restrict__ params,
+                                                    float *__restrict__ m, float *__restrict__ v,
+                                                    unsigned char *packed, float lr, float b1, float b2, float eps,
+                                                    float bc1, float bc2, int adam, const int *__restrict__ tc_err) {
+    __shared__ float part[8][33];
+    const int lane = threadIdx.x & 31, slice = threadIdx.x >> 5, p = blockIdx.x * 32 + lane;
+    if (*tc_err) return;   // a timed-out tensor-core pass leaves the weights alone
     float s = 0.f;
-    for (int b = 0; b < nblk; b++) s += partials[(size_t)b * (MLP_NPARAM + 1) + p];
+    if (p <= MLP_NPARAM) {
+#pragma unroll 4
+        for (int b = slice; b < nblk; b += 8) s += partials[(size_t)b * (MLP_NPARAM + 1) + p];
+    }
+    part[slice][lane] = s;
+    __syncthreads();
+    if (slice != 0 || p > MLP_NPARAM) return;
+    s = part[0][lane];
+#pragma unroll
+    for (int q = 1; q < 8; q++) s += part[q][lane];
     grad[p] = s;
     if (!adam || p == MLP_NPARAM) return;
     const float mm = b1 * m[p] + (1.f - b1) * s, vv = b2 * v[p] + (1.f - b2) * s * s;
@@ -314,7 +328,8 @@ static mdz_status mlp_ensure(mdz_ctx *ctx) {
     if (e == cudaSuccess) e = cudaMalloc((void **)&M->adam_v, sizeof(float) * MLP_NPARAM);
     if (e == cudaSuccess) e = cudaMalloc((void **)&M->packed, MLP_PACK_BYTES);
     if (e == cudaSuccess) e = cudaMemset(M->packed, 0, MLP_PACK_BYTES);
-    if (e == cudaSuccess) e = cudaMalloc((void **)&M->partials, sizeof(float) * (MLP_NPARAM + 1) * M->max_blocks);
+    // partial gradient rows: one per CTA, two CTAs per SM for the tcgen05 pass
+    if (e == cudaSuccess) e = cudaMalloc((void **)&M->partials, sizeof(float) * (MLP_NPARAM + 1) * 2 * M->max_blocks);
     if (e == cudaSuccess) e = cudaMalloc((void **)&M->grad, sizeof(float) * (MLP_NPARAM + 1));
     if (e == cudaSuccess) e = cudaMalloc((void **)&M->tc_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(M->tc_err, 0, sizeof(int));
@@ -459,16 +474,25 @@ extern "C" mdz_status mdz_mlp_generate(mdz_ctx *ctx, const mdz_materials *m, con
     return MDZ_OK;
 }
 
+static mdz_status mlp_tc_status(mdz_ctx *ctx);
+
 // one pass over `rows` rows starting at row0: partial gradients + reduction (+ Adam)
 static mdz_status mlp_step(mdz_ctx *ctx, const uint4 *X, const float2 *Y, long long row0, int rows, int adam,
                            float lr) {
     mdz_mlp *M = ctx->mlp;
     cudaStream_t st = ctx->stream;
-    int tiles = (rows + MLP_TILE - 1) / MLP_TILE;
-    int nblk = tiles < M->max_blocks ? tiles : M->max_blocks;
+    const int tiles = (rows + MLP_TILE - 1) / MLP_TILE, cap = (M->engine == 0 ? 2 : 1) * M->max_blocks;
+    int nblk = tiles < cap ? tiles : cap;
     if (nblk < 1) nblk = 1;
-    k_mlp_train<<<nblk, 128, train_smem_bytes(), st>>>(M->packed, X, Y, row0, rows, 1.0f / (float)rows, M->partials);
-    MDZ_LAUNCHED(ctx);
+    if (M->engine == 0) {
+        mdz_status r = mdz_mlp_train_tc(ctx, M->packed, X, Y, row0, rows, 1.0f / (float)rows, M->partials, nblk,
+                                        M->tc_err, st);
+        if (r != MDZ_OK) return r;
+    } else {
+        k_mlp_train<<<nblk, 128, train_smem_bytes(), st>>>(M->packed, X, Y, row0, rows, 1.0f / (float)rows,
+                                                           M->partials);
+        MDZ_LAUNCHED(ctx);
+    }
     float bc1 = 1.f, bc2 = 1.f;
     const float b1 = 0.9f, b2 = 0.999f;
     if (adam) {
@@ -476,9 +500,9 @@ static mdz_status mlp_step(mdz_ctx *ctx, const uint4 *X, const float2 *Y, long l
         bc1 = 1.f - powf(b1, (float)M->adam_t);
         bc2 = 1.f - powf(b2, (float)M->adam_t);
     }
-    k_mlp_reduce<<<mdz_blocks(MLP_NPARAM + 1), MDZ_THREADS, 0, st>>>(nblk, M->partials, M->grad, M->params,
+    k_mlp_reduce<<<(MLP_NPARAM + 1 + 31) / 32, 256, 0, st>>>(nblk, M->partials, M->grad, M->params,
                                                                      M->adam_m, M->adam_v, M->packed, lr, b1, b2,
-                                                                     1e-8f, bc1, bc2, adam);
+                                                                     1e-8f, bc1, bc2, adam, M->tc_err);
     MDZ_LAUNCHED(ctx);
     return MDZ_OK;
 }
@@ -508,6 +532,8 @@ extern "C" mdz_status mdz_mlp_train(mdz_ctx *ctx, int steps, int batch, double l
         }
     }
     MDZ_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    mdz_status ts = mlp_tc_status(ctx);
+    if (ts != MDZ_OK) return ts;
     M->trained = true;
     M->last_loss = loss_n ? loss_acc / loss_n : 0.0;
     if (final_loss) *final_loss = M->last_loss;
@@ -537,6 +563,7 @@ extern "C" mdz_status mdz_mlp_gradients(mdz_ctx *ctx, int n, const float *x, con
     MDZ_CUDA(ctx, cudaMemcpyAsync(h.data(), ctx->mlp->grad, sizeof(float) * (MLP_NPARAM + 1), cudaMemcpyDeviceToHost,
                                   st));
     MDZ_CUDA(ctx, cudaStreamSynchronize(st));
+    if ((s = mlp_tc_status(ctx)) != MDZ_OK) return s;
     memcpy(grad, h.data(), sizeof(float) * MLP_NPARAM);
     if (loss) *loss = h[MLP_NPARAM] / (double)n;
     return MDZ_OK;
@@ -548,7 +575,7 @@ static mdz_status mlp_tc_status(mdz_ctx *ctx) {
     MDZ_CUDA(ctx, cudaMemcpy(&e, ctx->mlp->tc_err, sizeof(int), cudaMemcpyDeviceToHost));
     if (!e) return MDZ_OK;
     MDZ_CUDA(ctx, cudaMemset(ctx->mlp->tc_err, 0, sizeof(int)));
-    return mdz_fail(ctx, MDZ_ERR_STATE, "mlp inference: a tensor-core commit did not arrive (time-out)");
+    return mdz_fail(ctx, MDZ_ERR_STATE, "mlp: a tensor-core commit did not arrive (time-out)");
 }
 
 static mdz_status mlp_infer_dev(mdz_ctx *ctx, const uint4 *X, long long n, float2 *Y, cudaStream_t st) {
@@ -640,6 +667,7 @@ extern "C" mdz_status mdz_mlp_benchmark(mdz_ctx *ctx, int batch, int reps, doubl
     MDZ_CUDA(ctx, cudaEventSynchronize(b));
     cudaEventElapsedTime(&ms, a, b);
     if (ms_train_step) *ms_train_step = ms / reps;
+    if ((s = mlp_tc_status(ctx)) != MDZ_OK) return s;
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     MDZ_CUDA(ctx, cudaMemcpy(M->params, keep.data(), sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice));

@@ -1,5 +1,8 @@
 // Learned initial guess for the local rheology: a 8 -> 64 -> 64 -> 2 ReLU MLP
-// in BF16 with FP32 accumulation on the tensor cores (mma.sync m16n8k16).
+// in BF16 with FP32 accumulation on the tensor cores: training and batch
+// inference on tcgen05 with TMEM accumulators (mlp_tc.cu; engine 0), the
+// warp-level mma.sync m16n8k16 kernels as engine 1 and inside the per-node
+// guess of the rheology kernels.
 //
 // Inputs (normalised to [-1, 1] by the training ranges): log10 of the strain
 // rate invariant [1/s], T [K] (as 1000 / T), P [Pa], log10 dt [s], and a
@@ -62,7 +65,7 @@ struct mdz_mlp {
     float2 *guess = nullptr;             // n_phases x (centroids + vertices)
     size_t guess_cap = 0;
     double last_loss = 0.0;
-    int engine = 0;                      // inference: 0 tcgen05 (mlp_tc.cu), 1 warp-level mma.sync
+    int engine = 0;                      // inference and training: 0 tcgen05 (mlp_tc.cu), 1 warp-level mma.sync
     int *tc_err = nullptr;               // device flag: a tcgen05 commit timed out
 };
 
@@ -71,6 +74,11 @@ bool mdz_mlp_ready(const mdz_ctx *ctx);
 // tensor-core commit never arrived
 mdz_status mdz_mlp_infer_tc(mdz_ctx *ctx, const unsigned char *packed, const uint4 *X, long long n, float2 *Y,
                             int *d_err, cudaStream_t st);
+// tcgen05 training pass over nrows rows from row0: one partial gradient row (and
+// the loss) per CTA in `partials`, nblk CTAs (mlp_tc.cu)
+mdz_status mdz_mlp_train_tc(mdz_ctx *ctx, const unsigned char *packed, const uint4 *X, const float2 *Y,
+                            long long row0, int nrows, float scale, float *partials, int nblk, int *d_err,
+                            cudaStream_t st);
 void mdz_mlp_free(mdz_ctx *ctx);
 // guess buffer for n_phases x (nc + nv) nodes (allocated on first use)
 float2 *mdz_mlp_guess_buffer(mdz_ctx *ctx, size_t n);

@@ -430,7 +430,7 @@ class Context:
         return its.value, rel.value
 
     def mlp_set_engine(self, engine):
-        """Inference kernel: 0 tcgen05 (tensor memory accumulators), 1 mma.sync."""
+        """Inference and training kernels: 0 tcgen05 (tensor memory accumulators), 1 mma.sync."""
         self._check(self.L.mdz_mlp_set_engine(self.h, C.c_int(engine)))
 
     def mlp_benchmark(self, batch, reps):

@@ -32,10 +32,12 @@ def _rel(a, b):
     return np.linalg.norm(a - b) / np.linalg.norm(b)
 
 
+@pytest.mark.parametrize("engine", [0, 1])   # tcgen05 / mma.sync
 @pytest.mark.parametrize("n", [128, 1000, 70000])     # one tile, a ragged tail, many CTAs
-def test_gradients_match_cpu_oracle(n):
+def test_gradients_match_cpu_oracle(n, engine):
     ctx = _ctx()
     ctx.mlp_init(11)
+    ctx.mlp_set_engine(engine)
     p = ctx.mlp_get_weights().astype(np.float64)
     rng = np.random.default_rng(5)
     p[mo.SLICES["b1"][0]:mo.SLICES["b1"][0] + 64] = rng.normal(0, 0.1, 64)   # non-zero biases
@@ -83,6 +85,26 @@ def test_tensor_core_engines_agree():
     y1 = ctx.mlp_infer(x)
     assert np.max(np.abs(y0 - y1)) <= 2e-2 * (1.0 + np.max(np.abs(y1)))
     assert np.mean(np.abs(y0 - y1)) <= 1e-3 * (1.0 + np.max(np.abs(y1)))
+    ctx.close()
+
+
+def test_training_gradients_engines_and_repeatability():
+    """The tcgen05 training pass (TMEM-resident weight-gradient sums over each
+    CTA's tiles) gives the same gradients as the mma.sync pass to accumulation
+    order, and the same bits on a repeated call (fixed-order sums)."""
+    ctx = _ctx()
+    ctx.mlp_init(13)
+    x, y = _rows(200000, 17)
+    ctx.mlp_set_engine(0)
+    g0, l0 = ctx.mlp_gradients(x, y)
+    g0b, l0b = ctx.mlp_gradients(x, y)
+    ctx.mlp_set_engine(1)
+    g1, l1 = ctx.mlp_gradients(x, y)
+    assert np.array_equal(g0, g0b) and l0 == l0b
+    assert abs(l0 - l1) <= 1e-5 * l1
+    for name, (o, shape) in mo.SLICES.items():
+        k = int(np.prod(shape))
+        assert _rel(g0[o:o + k], g1[o:o + k]) < 2e-3, name
     ctx.close()
 
 
