@@ -110,6 +110,29 @@ int mdz_marker_count(const mdz_ctx *ctx);
  * markers exceed the capacity. */
 mdz_status mdz_save_breakpoint(mdz_ctx *ctx, const char *path);
 mdz_status mdz_load_breakpoint(mdz_ctx *ctx, const char *path);
+
+/* Flags and scales of the reference run that wrote a breakpoint: the model
+ * switches that decide which sections its file holds (params free_surf,
+ * iselastic, fstrain, aniso, rec_T_P_x_z) and its scale (scaling.L, .V, .S,
+ * .T, .t). */
+typedef struct {
+    int free_surf, iselastic, fstrain, aniso, rec_T_P_x_z;
+    double L, V, S, T, t;
+} mdz_ref_breakpoint_desc;
+
+/* Restart from the reference's own breakpoint file (Breakpoint%05d.dat of
+ * MakeBreakpointParticles, SOURCE/InputOutput.c:515-903), read as
+ * LoadBreakpointParticles (:160-514) reads it: marker positions, velocities,
+ * phases, P, deviatoric stresses (iselastic), strain, plastic strain and T,
+ * and u_in, v_in, p_in as the next step's starting u, v, p, divided by the
+ * run's scales; the box is restored; MDZ_M_CMUL is set to 1.  dt and time
+ * (scaled) are returned when the pointers are not NULL.  The file's length
+ * must be the one the flags give for this context's grid and phase count:
+ * MDZ_ERR_ARG otherwise (wrong flags, another grid, a truncated file), and
+ * for phases outside -1..n_phases-1, with the context unchanged;
+ * MDZ_ERR_CAPACITY when its markers exceed the capacity. */
+mdz_status mdz_load_reference_breakpoint(mdz_ctx *ctx, const char *path, const mdz_ref_breakpoint_desc *desc,
+                                         double *dt, double *time);
 /* Upload the resident markers' velocities (particles.Vx, Vz; RK4 writes them,
  * reseeding copies them), e.g. when markers are restored from a saved state. */
 mdz_status mdz_set_marker_velocity(mdz_ctx *ctx, int n, const double *vx, const double *vz);

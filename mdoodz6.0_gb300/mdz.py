@@ -190,6 +190,13 @@ class Grid:
         return d
 
 
+class RefBreakpointDesc(C.Structure):
+    """mdz_ref_breakpoint_desc: the flags and scales of the reference run that
+    wrote a Breakpoint%05d.dat."""
+    _fields_ = [(n, C.c_int) for n in ("free_surf", "iselastic", "fstrain", "aniso", "rec_T_P_x_z")] + \
+               [(n, C.c_double) for n in ("L", "V", "S", "T", "t")]
+
+
 class ThermalBC(C.Structure):
     """mdz_thermal_bc (the reference's BCT BCt)."""
     _fields_ = [("type", _sp), ("typW", _sp), ("typE", _sp), ("typS", _sp), ("typN", _sp),
@@ -244,6 +251,19 @@ class Context:
         the box it was saved with."""
         self._check(self.L.mdz_load_breakpoint(self.h, os.fsencode(path)))
         self._follow_box()
+
+    def load_reference_breakpoint(self, path, scales, iselastic=1, free_surf=0, fstrain=0, aniso=0,
+                                  rec_T_P_x_z=0):
+        """Restart from the reference's own breakpoint file (LoadBreakpointParticles'
+        reading): scales = dict of the run's L, V, S, T, t.  Returns (dt, time)
+        in scaled units; the context's grid follows the restored box."""
+        d = RefBreakpointDesc(free_surf, iselastic, fstrain, aniso, rec_T_P_x_z,
+                              *(float(scales[k]) for k in ("L", "V", "S", "T", "t")))
+        dt, tm = C.c_double(0.0), C.c_double(0.0)
+        self._check(self.L.mdz_load_reference_breakpoint(self.h, os.fsencode(path), C.byref(d), C.byref(dt),
+                                                          C.byref(tm)))
+        self._follow_box()
+        return dt.value, tm.value
 
     # the box (PureShearALE) ---------------------------------------------------
     def get_box(self):

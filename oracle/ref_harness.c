@@ -277,6 +277,52 @@ int ref_rk4(void) {
     return 0;
 }
 
+/* Scaling factors by name (the breakpoint writer and loader scale with them). */
+int ref_set_scale(const char *name, double v) {
+#define S_D(f) if (!strcmp(name, #f)) { g_scale.f = v; return 0; }
+    S_D(L) S_D(V) S_D(S) S_D(T) S_D(t) S_D(E) S_D(rho) S_D(eta) S_D(rhoE)
+#undef S_D
+    return -1;
+}
+
+/* MakeBreakpointParticles (SOURCE/InputOutput.c:515-903) of the harness state
+ * into BreakpointXXXXX.dat in the working directory (delete_breakpoints = -1;
+ * no free surface, so the topography arguments are not read). */
+int ref_make_breakpoint(void) {
+    markers chain, chain_ini;
+    surface topo, topo_ini;
+    memset(&chain, 0, sizeof chain); memset(&chain_ini, 0, sizeof chain_ini);
+    memset(&topo, 0, sizeof topo); memset(&topo_ini, 0, sizeof topo_ini);
+    if (!g_have_grid || !g_have_parts) return -1;
+    g_model.delete_breakpoints = -1;
+    MakeBreakpointParticles(&g_parts, &g_mesh, &chain, &chain_ini, g_model, &topo, &topo_ini, g_scale);
+    return 0;
+}
+
+/* LoadBreakpointParticles (SOURCE/InputOutput.c:160-514) of BreakpointXXXXX.dat
+ * into the harness state; returns the loaded Nb_part. */
+int ref_load_breakpoint(void) {
+    markers chain, chain_ini;
+    surface topo, topo_ini;
+    memset(&chain, 0, sizeof chain); memset(&chain_ini, 0, sizeof chain_ini);
+    memset(&topo, 0, sizeof topo); memset(&topo_ini, 0, sizeof topo_ini);
+    if (!g_have_grid || !g_have_parts) return -1;
+    g_model.delete_breakpoints = -1;
+    LoadBreakpointParticles(&g_parts, &g_mesh, &chain, &chain_ini, &g_model, &topo, &topo_ini, g_scale);
+    return g_parts.Nb_part;
+}
+
+/* Model scalars the breakpoint loader sets. */
+double ref_get_model(const char *name) {
+    if (!strcmp(name, "dt")) return g_model.dt;
+    if (!strcmp(name, "time")) return g_model.time;
+    if (!strcmp(name, "xmin")) return g_model.xmin;
+    if (!strcmp(name, "xmax")) return g_model.xmax;
+    if (!strcmp(name, "zmin")) return g_model.zmin;
+    if (!strcmp(name, "zmax")) return g_model.zmax;
+    return 0.0;
+}
+
 /* Closest-marker phase map on the visualisation grid of res_fact times the
  * computational resolution, built and filled as WriteOutputHDF5 does
  * (HDF5Output.c:266-297: lines by accumulation from the first grid line,

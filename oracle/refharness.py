@@ -38,6 +38,7 @@ class RefMDOODZ:
         L.ref_marker_phase.restype = _ip
         L.ref_dx.restype = C.c_double
         L.ref_dz.restype = C.c_double
+        L.ref_get_model.restype = C.c_double
         L.ref_eqn.restype = _ip
         L.ref_residual_vec.restype = _dp
         L.ref_rhs_vec.restype = _dp
@@ -171,6 +172,26 @@ class RefMDOODZ:
         self.lib.ref_phase_viz(C.c_int(res_fact), compo.ctypes.data_as(C.c_char_p), xv.ctypes.data_as(_dp),
                                zv.ctypes.data_as(_dp))
         return compo, xv, zv
+
+    def set_scale(self, name, v):
+        if self.lib.ref_set_scale(name.encode(), C.c_double(v)) != 0:
+            raise KeyError(name)
+
+    def make_breakpoint(self):
+        """MakeBreakpointParticles into BreakpointXXXXX.dat in the working directory."""
+        if self.lib.ref_make_breakpoint() != 0:
+            raise RuntimeError("make_breakpoint: no grid or markers")
+
+    def load_breakpoint(self):
+        """LoadBreakpointParticles from BreakpointXXXXX.dat in the working directory."""
+        n = self.lib.ref_load_breakpoint()
+        if n < 0:
+            raise RuntimeError("load_breakpoint: no grid or markers")
+        self.n_markers = n
+        return n
+
+    def model(self, name):
+        return self.lib.ref_get_model(name.encode())
 
     # grid operators --------------------------------------------------------
     def strain_rates(self):

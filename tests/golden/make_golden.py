@@ -191,6 +191,59 @@ def make_phasemap_fixture():
     np.savez_compressed(os.path.join(HERE, "phasemap_ref.npz"), **out)
 
 
+# scales of the breakpoint fixture (a lithosphere-like set: km, cm/yr, 10 MPa)
+BRK_SCALE = {"L": 1.0e4, "V": 3.0e-10, "S": 2.0e7, "T": 700.0, "t": 1.0e4 / 3.0e-10, "E": 3.0e-14,
+             "rho": 3300.0, "eta": 1.0e21, "rhoE": 6.6e10}
+BRK_MARKER = ("P", "Vx", "Vz", "sxxd", "szzd", "sxz", "strain", "strain_pl", "T")
+
+
+def make_breakpoint_fixture():
+    """The reference's own breakpoint file: MakeBreakpointParticles
+    (iselastic = 1, no free surface) of a seeded state given in scaled units,
+    with non-trivial scales, and what LoadBreakpointParticles reads back from
+    that file into cleared arrays (the expected restart state)."""
+    import tempfile
+    g = _grid()
+    r = RefMDOODZ(NX, NZ, XMIN, XMAX, ZMIN, ZMAX, 3)
+    r.set_bc_pureshear(1.0)
+    r.set_param("iselastic", 1)
+    r.set_param("dt", 0.37)
+    for k, v in BRK_SCALE.items():
+        r.set_scale(k, v)
+    x, z, ph = (a[::8].copy() for a in _markers(g, seed=13))   # 640 markers keep the file small
+    r.set_markers(x, z, ph)
+    rng = np.random.default_rng(17)
+    for nm in BRK_MARKER:
+        r.marker_field(nm)[:] = rng.normal(0.0, 1.0, len(x))
+    for nm in ("u_in", "v_in", "p_in"):
+        r.field(nm)[:] = rng.normal(0.0, 1.0, r.field(nm).size)
+    cwd = os.getcwd()
+    with tempfile.TemporaryDirectory() as d:
+        os.chdir(d)
+        try:
+            r.make_breakpoint()
+            with open("BreakpointXXXXX.dat", "rb") as f:
+                data = f.read()
+            for nm in BRK_MARKER + ("x", "z"):
+                r.marker_field(nm)[:] = 0.0
+            r.marker_phase()[:] = -9
+            for nm in ("u_in", "v_in", "p_in"):
+                r.field(nm)[:] = 0.0
+            n = r.load_breakpoint()
+        finally:
+            os.chdir(cwd)
+    out = dict(Nx=NX, Nz=NZ, n_phases=3, image=np.frombuffer(data, np.uint8).copy(), n=n,
+               scale=np.array([BRK_SCALE[k] for k in ("L", "V", "S", "T", "t")]),
+               dt=r.model("dt"), time=r.model("time"),
+               box=np.array([r.model(k) for k in ("xmin", "xmax", "zmin", "zmax")]),
+               phase=r.marker_phase().copy(), u=r.field("u_in").copy(), v=r.field("v_in").copy(),
+               p=r.field("p_in").copy())
+    for nm in BRK_MARKER + ("x", "z"):
+        out["m_" + nm] = r.marker_field(nm).copy()
+    np.savez_compressed(os.path.join(HERE, "breakpoint_ref.npz"), **out)
+    print("breakpoint_ref.npz: %d markers, %d bytes" % (n, len(data)))
+
+
 def make_rheology_fixture(avg=0, tag="", phases=None, model=None, neumann=False):
     g = _grid()
     r = RefMDOODZ(NX, NZ, XMIN, XMAX, ZMIN, ZMAX, 3)
@@ -554,7 +607,7 @@ def make_pressure_fixture():
 
 if __name__ == "__main__":
     what = sys.argv[1:] or ["markers", "rheology", "reseed", "strain", "stress", "gridprops", "pressure", "thermal",
-                            "phasemap"]
+                            "phasemap", "breakpoint"]
     if "gridprops" in what:
         make_gridprops_fixture()
     if "pressure" in what:
@@ -577,5 +630,7 @@ if __name__ == "__main__":
         make_thermal_fixture()
     if "phasemap" in what:
         make_phasemap_fixture()
+    if "breakpoint" in what:
+        make_breakpoint_fixture()
     if "rheology" in what or "neumann" in what:
         make_rheology_fixture(0, "_neumann", neumann=True)

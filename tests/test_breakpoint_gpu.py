@@ -125,3 +125,49 @@ def test_breakpoint_refused(tmp_path):
     for x, y in zip(before, after):
         assert np.array_equal(x, y)
     a.close()
+
+
+def test_restart_from_reference_breakpoint_file(tmp_path):
+    """A file written by the reference's own MakeBreakpointParticles (scaled
+    lithosphere-like units, iselastic = 1) loads into a context exactly as the
+    reference's LoadBreakpointParticles reads it back: markers, phases,
+    velocities, P, stresses, strains, T, u_in / v_in / p_in, dt, time and the
+    box, bit for bit; wrong flags, a truncated file and another grid are
+    refused with the context unchanged."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "breakpoint_ref.npz"))
+    scales = dict(zip(("L", "V", "S", "T", "t"), d["scale"]))
+    Nx, Nz, nph, n = int(d["Nx"]), int(d["Nz"]), int(d["n_phases"]), int(d["n"])
+    box = d["box"]
+    path = tmp_path / "Breakpoint00001.dat"
+    path.write_bytes(d["image"].tobytes())
+    g = mdz.Grid(Nx, Nz, box[0], box[1], box[2], box[3]).set_bc_pureshear(1.0)
+    ctx = mdz.Context(g, nph, n + 64)
+    # refusals first: the context must stay empty
+    with pytest.raises(mdz.MdzError):
+        ctx.load_reference_breakpoint(str(path), scales, iselastic=0)
+    short = tmp_path / "short.dat"
+    short.write_bytes(d["image"].tobytes()[:-8])
+    with pytest.raises(mdz.MdzError):
+        ctx.load_reference_breakpoint(str(short), scales)
+    assert ctx.n_markers == 0
+    other = mdz.Context(mdz.Grid(Nx + 2, Nz, box[0], box[1], box[2], box[3]).set_bc_pureshear(1.0), nph, n + 64)
+    with pytest.raises(mdz.MdzError):
+        other.load_reference_breakpoint(str(path), scales)
+    other.close()
+    dt, time = ctx.load_reference_breakpoint(str(path), scales)
+    assert dt == float(d["dt"]) and time == float(d["time"])
+    assert ctx.n_markers == n
+    x, z, ph, vx, vz = ctx.get_markers()
+    assert np.array_equal(ph, d["phase"])
+    for k, a in (("x", x), ("z", z), ("Vx", vx), ("Vz", vz)):
+        assert np.array_equal(a, d["m_" + k]), k
+    for k, a in (("P", mdz.M_P), ("sxxd", mdz.M_SXXD), ("szzd", mdz.M_SZZD), ("sxz", mdz.M_SXZ),
+                 ("strain", mdz.M_STRAIN), ("strain_pl", mdz.M_STRAIN_PL), ("T", mdz.M_T)):
+        assert np.array_equal(ctx.get_marker_attr(a), d["m_" + k]), k
+    assert np.all(ctx.get_marker_attr(mdz.M_CMUL) == 1.0)
+    out = mdz.GridFields(g, nph)
+    ctx.download_fields(out)
+    for k in ("u", "v", "p"):
+        assert np.array_equal(out[k], d[k]), k
+    ctx.close()
