@@ -71,7 +71,8 @@ def test_struct_layouts_match_header(tmp_path):
     if cc is None:
         pytest.skip("no C compiler")
     mirrors = {"mdz_grid_desc": mdz.GridDesc, "mdz_fields": mdz.FieldsStruct, "mdz_materials": mdz.Materials,
-               "mdz_rheo_params": mdz.RheoParams, "mdz_model": mdz.Model, "mdz_step_report": mdz.StepReport}
+               "mdz_rheo_params": mdz.RheoParams, "mdz_model": mdz.Model, "mdz_step_report": mdz.StepReport,
+               "mdz_ref_breakpoint_desc": mdz.RefBreakpointDesc}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "mdoodz_gpu.h"', "int main(void) {"]
     for cname, py in mirrors.items():
         lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
