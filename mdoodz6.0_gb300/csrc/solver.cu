@@ -1857,9 +1857,11 @@ static mdz_status precondition(mdz_ctx *ctx, mg_hier<T> &H, const double *eta_n,
 // ---------------------------------------------------------------------------
 // GCR kernels (vectors are u|v|p contiguous of length n).
 // Orthogonalisation: classical Gram-Schmidt, with a second pass only where
-// the first removed all but 1e-3 of w's squared norm (a DGKS-type test; with
-// the usual 1/2 the second pass ran in almost every FP32 iteration and made
-// the plain FP64 solve 7 % slower for the same iteration counts),
+// the first removed all but 1e-3 (FP64 basis) or 1e-1 (FP32 basis) of w's
+// squared norm (a DGKS-type test; with the usual 1/2 the second pass ran in
+// almost every FP32 iteration and made the plain FP64 solve 7 % slower for
+// the same iteration counts; 1e-3 on FP32 bases cost 15-25 % more iterations
+// on a 401^2 visco-elasto-plastic box),
 // decided on the device: the first pass's k_gcr_dots sets sc[5] = 1 for a
 // second pass, and the second-pass kernels return at once when it is 0.
 // dots[0..k-1] = (w, W_q), dots[k] = (w, w), dots[k+1] = (w, r) of the pass
@@ -2112,7 +2114,10 @@ __global__ void __launch_bounds__(256) k_gcr_dots(int k, size_t n, const T *cons
     if (mode == 1) {
         double nrm2 = d[k];
         for (int q = 0; q < k; q++) nrm2 -= d[q] * d[q];
-        if (k > 0 && !(nrm2 > 1e-3 * d[k])) {   // second pass: keep this pass's coefficients in U
+        // second pass when the first removed all but 1e-3 (FP64 basis) or 1e-1
+        // (FP32 basis: its orthogonality decays faster, and alpha is taken
+        // from r0 through the triangle) of w's squared norm
+        if (k > 0 && !(nrm2 > (sizeof(T) == 4 ? 1e-1 : 1e-3) * d[k])) {   // keep this pass's coefficients in U
             for (int q = 0; q < k; q++) tri[(size_t)k * GCR_MAX_M + q] = d[q];
             sc[5] = 1.0;
             return;
